@@ -1,0 +1,412 @@
+"""Generate golden fixtures by running the reference Simple-RF model code on CPU.
+
+Run in a container where the reference project is available (default
+``/root/reference``; override with ``SRF_REFERENCE_ROOT``):
+
+    python tests/golden/make_golden.py
+
+The reference is imported read-only (``sys.dont_write_bytecode``) with a stub
+for ``matplotlib`` (imported but unused by ``utils/CommonUtils04.py``).  Random
+draws inside the reference (``torch.rand`` at SimpleNeRF17.py:355/397 and
+SimpleTensoRF09.py:398) are replaced by explicit uniforms so every fixture is a
+pure function of its stored inputs.  Weights come from numpy PCG64 seeds
+(``oracle.nerf.xavier_params``) so the fixtures need not store them.
+"""
+import os
+import sys
+import types
+import contextlib
+
+import numpy as np
+import torch
+
+sys.dont_write_bytecode = True
+REF = os.environ.get('SRF_REFERENCE_ROOT', '/root/reference')
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REF, 'src'))
+sys.path.insert(0, REPO)
+for name in ('matplotlib', 'matplotlib.pyplot'):
+    sys.modules.setdefault(name, types.ModuleType(name))
+
+from models import SimpleNeRF17 as RN  # noqa: E402
+from models import SimpleTensoRF09 as RT  # noqa: E402
+from utils import CommonUtils04 as CU  # noqa: E402
+from oracle import nerf as onerf  # noqa: E402
+
+torch.set_num_threads(4)
+
+
+@contextlib.contextmanager
+def patched_rand(queue):
+    """Replace torch.rand / torch.rand_like by a queue of prepared tensors."""
+    orig_rand, orig_like = torch.rand, torch.rand_like
+
+    def fake(*args, **kwargs):
+        t = queue.pop(0)
+        return t.clone()
+
+    torch.rand = fake
+    torch.rand_like = fake
+    try:
+        yield
+    finally:
+        torch.rand, torch.rand_like = orig_rand, orig_like
+
+
+def mlp_cfg(width=256, depth=8, wv=128, lp=10, lv=4, views=True, vdr=True, lps=None, ns=64):
+    c = {'num_samples': ns, 'points_net_depth': depth, 'views_net_depth': 1, 'points_net_width': width,
+         'views_net_width': wv, 'points_positional_encoding_degree': lp, 'views_positional_encoding_degree': lv,
+         'use_view_dirs': views, 'view_dependent_rgb': vdr, 'predict_visibility': False}
+    if lps is not None:
+        c['points_sigma_positional_encoding_degree'] = lps
+    return c
+
+
+def nerf_configs(coarse, fine, ndc=False, white=False, augs=None):
+    model = {'name': 'SimpleNeRF17', 'coarse_model': coarse, 'learn_camera_focal_length': False,
+             'learn_camera_rotation': False, 'learn_camera_translation': False, 'chunk': 1 << 20,
+             'lindisp': False, 'netchunk': 1 << 20, 'perturb': True, 'raw_noise_std': 0.0, 'white_bkgd': white}
+    if fine is not None:
+        model['fine_model'] = fine
+    if augs:
+        model['augmentations'] = augs
+    configs = {'data_loader': {'ndc': ndc}, 'model': model, 'database': 'synthetic'}
+    model_configs = {'intrinsics': np.eye(3)[None].repeat(1, 0), 'extrinsics': np.eye(4)[None].repeat(1, 0),
+                     'resolution': (378, 504), 'near': 2.0 if not ndc else 1.0, 'far': 6.0,
+                     'near_ndc': 0.0, 'far_ndc': 1.0}
+    return configs, model_configs
+
+
+def load_mlp(mlp, seed):
+    spec = onerf.MlpSpec.from_config(mlp.mlp_configs)
+    p = onerf.xavier_params(spec, seed)
+    sd = {k: torch.from_numpy(v) for k, v in p.items()}
+    missing = mlp.load_state_dict(sd, strict=True)
+    assert not missing.missing_keys
+    return spec, p
+
+
+def synthetic_rays(n, seed):
+    g = torch.Generator().manual_seed(seed)
+    o = torch.randn(n, 3, generator=g) * 0.1
+    d = torch.randn(n, 3, generator=g)
+    d = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    return o, d
+
+
+def ndc_world_rays(n, seed):
+    """Forward-facing rays: origins on z=-1 with x,y ~ U[-1,1]; directions with z in [-1.2,-0.8]."""
+    g = torch.Generator().manual_seed(seed)
+    o = torch.empty(n, 3)
+    o[:, :2] = torch.rand(n, 2, generator=g) * 2 - 1
+    o[:, 2] = -1.0
+    d = torch.empty(n, 3)
+    d[:, :2] = torch.rand(n, 2, generator=g) * 0.4 - 0.2
+    d[:, 2] = -(torch.rand(n, generator=g) * 0.4 + 0.8)
+    d = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    return o, d
+
+
+def render_case(n, sc, sf, seed, coarse_cfg, fine_cfg, ndc=False, white=False, augs=None, aug_seeds=None,
+                with_grads=False):
+    configs, model_configs = nerf_configs(coarse_cfg, fine_cfg, ndc=ndc, white=white, augs=augs)
+    model = RN.SimpleNeRF(configs, model_configs)
+    model.train()
+    spec_c, pc = load_mlp(model.coarse_model, seed)
+    spec_f, pf = load_mlp(model.fine_model, seed + 1)
+    aug_seeds = aug_seeds or []
+    for am, s in zip(getattr(model, 'augmented_models', []), aug_seeds):
+        load_mlp(am['coarse_model'], s)
+    rays_o, rays_d = ndc_world_rays(n, seed) if ndc else synthetic_rays(n, seed)
+    g = torch.Generator().manual_seed(seed + 100)
+    u_c = torch.rand(n, sc, generator=g)
+    u_f = torch.rand(n, sf, generator=g)
+    focal = 400.0
+    intr = torch.tensor([[focal, 0, 252.0], [0, focal, 189.0], [0, 0, 1.0]])[None].repeat(n, 1, 1)
+    inp = {'pixel_id': torch.zeros(n, 3, dtype=torch.int32), 'intrinsics': intr,
+           'extrinsics': torch.eye(4)[None].repeat(n, 1, 1), 'common_data': {}, 'num_frames': 1}
+    orig = RN.CommonUtils.get_rays_tr
+    RN.CommonUtils.get_rays_tr = lambda *a, **k: (rays_o.clone(), rays_d.clone())
+    try:
+        with patched_rand([u_c, u_f]):
+            ret = model.render_rays(inp, retraw=True, sec_views_vis=False, mode=None)
+    finally:
+        RN.CommonUtils.get_rays_tr = orig
+    out = {'rays_o': rays_o.numpy(), 'rays_d': rays_d.numpy(), 'u_coarse': u_c.numpy(), 'u_fine': u_f.numpy(),
+           'seed': np.array(seed), 'focal': np.array(focal)}
+    for k, v in ret.items():
+        out['out_' + k] = v.detach().numpy()
+    if with_grads:
+        tg = torch.Generator().manual_seed(seed + 200)
+        t_rgb = torch.rand(n, 3, generator=tg)
+        t_depth = torch.rand(n, generator=tg) * 4 + 2
+        dmask = torch.zeros(n)
+        dmask[:max(n // 4, 1)] = 1
+        loss = 0
+        for tag in ('coarse', 'fine'):
+            loss = loss + torch.mean(torch.mean((ret[f'rgb_{tag}'] - t_rgb) ** 2, 1))
+            loss = loss + 0.1 * torch.sum(torch.abs(ret[f'depth_{tag}'] - t_depth) * dmask) / dmask.sum()
+        loss.backward()
+        out['t_rgb'], out['t_depth'], out['dmask'] = t_rgb.numpy(), t_depth.numpy(), dmask.numpy()
+        out['loss'] = np.array(loss.item())
+        for tag, mlp in (('coarse', model.coarse_model), ('fine', model.fine_model)):
+            for k, prm in mlp.named_parameters():
+                out[f'grad_{tag}.{k}'] = prm.grad.numpy().copy()
+    return out
+
+
+def sampling_case():
+    g = torch.Generator().manual_seed(7)
+    n, sc, sf = 32, 64, 128
+    u_c = torch.rand(n, sc, generator=g)
+    fake = types.SimpleNamespace(ndc=False, training=True,
+                                 configs={'model': {'perturb': True, 'lindisp': False,
+                                                    'coarse_model': {'num_samples': sc},
+                                                    'fine_model': {'num_samples': sf}}},
+                                 model_configs={'near': 2.0, 'far': 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0},
+                                 sample_pdf=RN.SimpleNeRF.sample_pdf)
+    inp = {'pixel_id': torch.zeros(n, 3)}
+    with patched_rand([u_c]):
+        zc = RN.SimpleNeRF.get_z_vals_coarse(fake, inp)
+    fake.training = False
+    zc_det = RN.SimpleNeRF.get_z_vals_coarse(fake, inp)
+    w = torch.rand(n, sc, generator=g) ** 4
+    w[0] = 0.0                      # all-zero weights: uniform pdf (+1e-5 floor)
+    w[1, :] = 0.0
+    w[1, 30] = 5.0                  # one spike
+    w[2, ::2] = 0.0                 # alternating zeros -> denom < 1e-5 cases
+    u_f = torch.rand(n, sf, generator=g)
+    u_f[3, :4] = torch.tensor([0.0, 1.0, 0.5, 0.999999])
+    fake.training = True
+    with patched_rand([u_f]):
+        zf = RN.SimpleNeRF.get_z_vals_fine(fake, zc, w)
+    mids = .5 * (zc[..., 1:] + zc[..., :-1])
+    with patched_rand([u_f]):
+        samples = RN.SimpleNeRF.sample_pdf(mids, w[..., 1:-1], sf, det=False)
+    samples_det = RN.SimpleNeRF.sample_pdf(mids, w[..., 1:-1], sf, det=True)
+    fake.training = False
+    zf_det = RN.SimpleNeRF.get_z_vals_fine(fake, zc, w)
+    return {'u_coarse': u_c.numpy(), 'z_coarse': zc.numpy(), 'z_coarse_det': zc_det.numpy(), 'weights': w.numpy(),
+            'u_fine': u_f.numpy(), 'z_fine': zf.numpy(), 'samples': samples.numpy(),
+            'samples_det': samples_det.numpy(), 'z_fine_det': zf_det.numpy()}
+
+
+def pe_case():
+    g = torch.Generator().manual_seed(11)
+    x = torch.randn(257, 3, generator=g) * 3
+    x[0] = torch.tensor([0.0, -1.5, 1e-3])
+    x[1] = torch.tensor([30.0, -41.0, 7.25])
+    out = {'x': x.numpy()}
+    for deg in (10, 4, 3, 2, 0):
+        fn, dim = RN.MLP.get_positional_encoder(deg)
+        out[f'pe{deg}'] = fn(x).numpy()
+    return out
+
+
+def mlp_case():
+    g = torch.Generator().manual_seed(13)
+    m = 96
+    pts = torch.randn(m, 3, generator=g)
+    vd = torch.randn(m, 3, generator=g)
+    vd = vd / torch.linalg.norm(vd, dim=-1, keepdim=True)
+    out = {'pts': pts.numpy(), 'vdirs': vd.numpy()}
+    variants = {
+        'main': mlp_cfg(),
+        'aug_l4_noview': mlp_cfg(lp=4, views=False, vdr=False),
+        'points_aug': mlp_cfg(lps=3),
+    }
+    configs, _ = nerf_configs(mlp_cfg(), None)
+    for i, (name, cfg) in enumerate(variants.items()):
+        mlp = RN.MLP(name, configs, cfg, {})
+        mlp.eval()
+        load_mlp(mlp, 1000 + i)
+        res = mlp({'pts': pts, 'view_dirs': vd})
+        out[f'{name}_sigma'] = res['sigma'].detach().numpy()
+        out[f'{name}_rgb'] = res['rgb'].detach().numpy()
+    return out
+
+
+def composite_case():
+    out = {}
+    g = torch.Generator().manual_seed(17)
+    n, s = 24, 48
+    for ndc in (False, True):
+        tag = 'ndc' if ndc else 'world'
+        configs, _ = nerf_configs(mlp_cfg(), None, ndc=ndc, white=True)
+        fake = types.SimpleNamespace(ndc=ndc, configs=configs, predict_visibility=False,
+                                     convert_depth_from_ndc=RN.SimpleNeRF.convert_depth_from_ndc)
+        sigma = (torch.randn(n, s, 1, generator=g) * 2).relu()
+        sigma[0] = 0.0
+        sigma[1, 5:] = 1e4
+        rgb = torch.rand(n, s, 3, generator=g)
+        if ndc:
+            o, d = ndc_world_rays(n, 3)
+            intr = torch.tensor([[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]])[None].repeat(n, 1, 1)
+            o_ndc, d_ndc = CU.get_ndc_rays_tr(o, d, (378, 504), intr, near=1.0)
+            z = torch.sort(torch.rand(n, s, generator=g), -1)[0]
+            z[2, -1] = 1.0
+        else:
+            o, d = synthetic_rays(n, 4)
+            d = d * (1 + torch.rand(n, 1, generator=g))
+            z = 2 + 4 * torch.sort(torch.rand(n, s, generator=g), -1)[0]
+            o_ndc = d_ndc = None
+        sigma.requires_grad_(True)
+        rgb.requires_grad_(True)
+        if ndc:
+            res = RN.SimpleNeRF.volume_rendering(fake, {'sigma': sigma, 'rgb': rgb}, z_vals_ndc=z, rays_d_ndc=d_ndc,
+                                                 rays_o=o, rays_d=d)
+        else:
+            res = RN.SimpleNeRF.volume_rendering(fake, {'sigma': sigma, 'rgb': rgb}, z_vals=z, rays_d=d)
+        gw = torch.Generator().manual_seed(19)
+        loss = 0
+        for k in sorted(res):
+            c = torch.randn(res[k].shape, generator=gw)
+            out[f'{tag}_cot_{k}'] = c.numpy()
+            loss = loss + torch.sum(res[k] * c) if k not in ('alpha', 'visibility') else loss
+            out[f'{tag}_out_{k}'] = res[k].detach().numpy()
+        loss.backward()
+        out[f'{tag}_sigma'] = sigma.detach().numpy()[..., 0]
+        out[f'{tag}_rgb'] = rgb.detach().numpy()
+        out[f'{tag}_z'] = z.numpy()
+        out[f'{tag}_rays_o'] = o.numpy()
+        out[f'{tag}_rays_d'] = d.numpy()
+        if ndc:
+            out[f'{tag}_rays_d_ndc'] = d_ndc.numpy()
+            out[f'{tag}_rays_o_ndc'] = o_ndc.numpy()
+        out[f'{tag}_dsigma'] = sigma.grad.numpy()[..., 0]
+        out[f'{tag}_drgb'] = rgb.grad.numpy()
+    return out
+
+
+def rays_case():
+    g = torch.Generator().manual_seed(23)
+    n = 40
+    pix = torch.stack([torch.zeros(n, dtype=torch.int64), torch.randint(0, 504, (n,), generator=g),
+                       torch.randint(0, 378, (n,), generator=g)], 1).int()
+    intr = torch.tensor([[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]])[None].repeat(n, 1, 1)
+    ext = torch.eye(4)[None].repeat(n, 1, 1)
+    ext[:, :3, 3] = torch.rand(n, 3, generator=g) * 0.2 - 0.1
+    o, d = CU.get_rays_tr(pix, intr, ext, mip_nerf_used=False)
+    o2, d2 = CU.get_rays_tr(pix, intr, ext, mip_nerf_used=True)
+    on, dn = CU.get_ndc_rays_tr(o, d, (378, 504), intr, near=1.0)
+    vd = CU.get_view_dirs_tr(d)
+    return {'pixel_id': pix.numpy(), 'intrinsics': intr.numpy(), 'extrinsics': ext.numpy(), 'rays_o': o.numpy(),
+            'rays_d': d.numpy(), 'rays_o_half': o2.numpy(), 'rays_d_half': d2.numpy(), 'rays_o_ndc': on.numpy(),
+            'rays_d_ndc': dn.numpy(), 'view_dirs': vd.numpy()}
+
+
+def tensorf_case():
+    """VM density/colour, alpha mask, renderer MLP and LowRankTensor.forward on a small grid."""
+    g = torch.Generator().manual_seed(29)
+    res = torch.tensor([20, 22, 24])
+    bbox = [[-1.5, -1.5, -1.5], [1.5, 1.5, 1.5]]
+    tcfg = {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [4, 3, 2],
+            'num_components_color': [6, 5, 4], 'bounding_box': bbox, 'num_voxels_initial': int(res.prod()),
+            'num_voxels_final': int(res.prod()), 'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5,
+            'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4,
+            'use_view_dirs': True, 'view_dependent_color': True, 'views_positional_encoding_degree': 2,
+            'features_positional_encoding_degree': 2, 'features_dimension_color': 7, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 16, 'predict_visibility': False}
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': False}, 'database': 'synthetic'}
+    tm = RT.VmDecomposedTensor('coarse_model', configs, tcfg, {'bounding_box': bbox})
+    tm.update_tensor_params(res, torch.tensor(bbox))
+    tm.matrices_density, tm.vectors_density = tm.create_decomposed_tensor([4, 3, 2], res, 0.1)
+    tm.matrices_color, tm.vectors_color = tm.create_decomposed_tensor([6, 5, 4], res, 0.1)
+    with torch.no_grad():
+        for plist in (tm.matrices_density, tm.vectors_density):
+            for prm in plist:
+                prm.copy_(torch.randn(prm.shape, generator=g) * 0.3 + 0.15)
+        for plist in (tm.matrices_color, tm.vectors_color):
+            for prm in plist:
+                prm.copy_(torch.randn(prm.shape, generator=g) * 0.3)
+        for prm in list(tm.basis_matrix_color.parameters()) + list(tm.color_predictor.parameters()):
+            prm.copy_(torch.randn(prm.shape, generator=g) * 0.3)
+    vol = (torch.rand(12, 10, 8, generator=g) < 0.3).float()
+    tm.alpha_mask = RT.AlphaGridMask(vol, torch.tensor(bbox))
+    tm.train()
+    n = 12
+    o = torch.zeros(n, 3)
+    o[:, 2] = -3.0
+    o[:, :2] = torch.rand(n, 2, generator=g) * 0.6 - 0.3
+    d = torch.randn(n, 3, generator=g) * 0.15
+    d[:, 2] = 1.0
+    d = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    u = torch.rand(n, 1, generator=g)
+    fake = types.SimpleNamespace(ndc=False, training=True,
+                                 configs={'model': {'perturb': True, 'lindisp': False}},
+                                 model_configs={'near': 0.5, 'far': 6.0})
+    with patched_rand([u]):
+        z = RT.SimpleTensoRF.get_z_vals_coarse(fake, {'pixel_id': torch.zeros(n, 3)},
+                                               {'rays_o': o, 'rays_d': d}, tm)
+    pts = o[:, None, :] + d[:, None, :] * z[:, :, None]
+    vdir = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    inp = {'pts': pts, 'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vdir}
+    with patched_rand([torch.tensor([0.25])]):       # white-background coin: rand < 0.5 -> white
+        ret = tm(inp, retraw=True)
+    tg = torch.Generator().manual_seed(31)
+    loss = 0
+    out = {}
+    for k in ('rgb', 'depth', 'acc'):
+        c = torch.randn(ret[k].shape, generator=tg)
+        out[f'cot_{k}'] = c.numpy()
+        loss = loss + torch.sum(ret[k] * c)
+    loss.backward()
+    out.update({'res': res.numpy(), 'bbox': np.array(bbox, np.float32), 'alpha_vol': vol.numpy(), 'u': u.numpy(),
+                'rays_o': o.numpy(), 'rays_d': d.numpy(), 'z': z.numpy(), 'step_size': tm.step_size.numpy(),
+                'num_samples': tm.num_samples.numpy()})
+    for i in range(3):
+        out[f'planes_density.{i}'] = tm.matrices_density[i].detach().numpy()[0]
+        out[f'lines_density.{i}'] = tm.vectors_density[i].detach().numpy()[0]
+        out[f'planes_color.{i}'] = tm.matrices_color[i].detach().numpy()[0]
+        out[f'lines_color.{i}'] = tm.vectors_color[i].detach().numpy()[0]
+        out[f'grad_planes_density.{i}'] = tm.matrices_density[i].grad.numpy()[0]
+        out[f'grad_lines_density.{i}'] = tm.vectors_density[i].grad.numpy()[0]
+        out[f'grad_planes_color.{i}'] = tm.matrices_color[i].grad.numpy()[0]
+        out[f'grad_lines_color.{i}'] = tm.vectors_color[i].grad.numpy()[0]
+    out['basis_matrix_color.weight'] = tm.basis_matrix_color.weight.detach().numpy()
+    out['grad_basis_matrix_color.weight'] = tm.basis_matrix_color.weight.grad.numpy()
+    for k, prm in tm.color_predictor.named_parameters():
+        out['color_predictor.' + k] = prm.detach().numpy()
+        out['grad_color_predictor.' + k] = prm.grad.numpy()
+    for k, v in ret.items():
+        out['out_' + k] = v.detach().numpy()
+    # alpha-mask query alone, including points on grid nodes / faces and outside the box
+    q = torch.rand(300, 3, generator=g) * 3.4 - 1.7
+    q[:8] = torch.tensor([[-1.5, -1.5, -1.5], [1.5, 1.5, 1.5], [0.0, 0.0, 0.0], [-1.5, 0.3, 1.5],
+                          [1.5000001, 0, 0], [0.1, -1.5, 0.2], [-1.0714285, 0.5, -0.4285714], [0.5, 0.5, 0.5]])
+    out['alpha_q'] = q.numpy()
+    out['alpha_q_pos'] = (tm.alpha_mask.sample_alpha(q) > 0).numpy()
+    return out
+
+
+def main():
+    cases = {
+        'nerf_sampling': sampling_case,
+        'nerf_pe': pe_case,
+        'nerf_mlp': mlp_case,
+        'nerf_composite': composite_case,
+        'rays': rays_case,
+        'nerf_render': lambda: render_case(16, 64, 128, 3, mlp_cfg(ns=64), mlp_cfg(ns=128)),
+        'nerf_train_grads': lambda: render_case(16, 16, 32, 5, mlp_cfg(width=32, wv=16, ns=16),
+                                                mlp_cfg(width=32, wv=16, ns=32), white=True, with_grads=True),
+        'nerf_ndc_pair': lambda: render_case(
+            12, 64, 128, 9, mlp_cfg(ns=64), mlp_cfg(ns=128), ndc=True,
+            augs=[{'name': 'views_augmentation', 'coarse_model': mlp_cfg(lp=4, views=False, vdr=False)}],
+            aug_seeds=[77]),
+        'tensorf': tensorf_case,
+    }
+    only = sys.argv[1:]
+    for name, fn in cases.items():
+        if only and name not in only:
+            continue
+        data = fn()
+        data['torch_version'] = np.array(torch.__version__)
+        path = os.path.join(HERE, f'{name}.npz')
+        np.savez_compressed(path, **data)
+        print(f'{name}: {len(data)} arrays, {os.path.getsize(path) / 1024:.1f} KiB')
+
+
+if __name__ == '__main__':
+    main()
