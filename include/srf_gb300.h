@@ -1,0 +1,274 @@
+/*
+ * srf_gb300.h -- C ABI of the GB300-native Simple-RF rendering hot path.
+ *
+ * Every entry point takes caller-owned device pointers, explicit sizes, an
+ * explicit CUDA stream (as `void*`, a cudaStream_t) and, where it needs
+ * temporaries, a caller-provided workspace.  The library never allocates device
+ * memory and never frees caller memory.  All functions are stateless and
+ * re-entrant; work is enqueued on the given stream only (so calls are legal
+ * inside CUDA stream capture).  Return value: SRF_OK (0) or an srf_status code;
+ * no exceptions cross this boundary and no device code traps.
+ *
+ * Reference citations are `file:line` inside the Simple-RF project
+ * (NagabhushanSN95/Simple-RF, src/...).
+ */
+#ifndef SRF_GB300_H
+#define SRF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SRF_OK = 0,
+    SRF_ERR_NULL = 1,          /* a required pointer is NULL                      */
+    SRF_ERR_SHAPE = 2,         /* a size / dimension is out of the supported range */
+    SRF_ERR_ALIGN = 3,         /* a pointer or stride breaks an alignment rule     */
+    SRF_ERR_WORKSPACE = 4,     /* workspace smaller than srf_*_workspace_size()    */
+    SRF_ERR_CUDA = 5,          /* a CUDA launch or runtime call failed             */
+    SRF_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up               */
+    SRF_ERR_RANGE = 7,         /* a device-side index check failed (see flag)      */
+    SRF_ERR_UNSUPPORTED = 8    /* configuration valid in the reference, not here   */
+} srf_status;
+
+/* Human-readable name of a status code (static string). */
+const char* srf_status_string(int status);
+/* Library version, e.g. "srf_gb300 1.0 sm_103a". */
+const char* srf_version(void);
+/* Text of the last CUDA error seen by this thread (static thread-local buffer). */
+const char* srf_last_cuda_error(void);
+/* Reads and clears the device-side error flag (bounded-wait timeouts, index
+ * range violations) that kernels set instead of trapping.  Synchronises `stream`.
+ * Writes the flag value (0 = clean) to *flag_out. */
+int srf_read_device_flag(int* flag_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Ray generation and sampling                                               */
+/* ------------------------------------------------------------------------ */
+
+/* NDC warp + view directions of world rays.
+ * Replaces CommonUtils04.get_ndc_rays_tr (src/utils/CommonUtils04.py:120-138)
+ * and get_view_dirs_tr (:147-149).  fx, fy per ray (N,); any output may be NULL. */
+int srf_ndc_rays(const float* rays_o, const float* rays_d, const float* fx, const float* fy, int n_rays,
+                 int height, int width, float near_plane, float* rays_o_ndc, float* rays_d_ndc,
+                 float* view_dirs, void* stream);
+
+/* Stratified coarse depths z (N,S).  u (N,S) uniforms or NULL (no jitter).
+ * Replaces SimpleNeRF.get_z_vals_coarse (src/models/SimpleNeRF17.py:330-358). */
+int srf_stratified_z(float* z, const float* u, int n_rays, int n_samples, float near_plane, float far_plane,
+                     int lindisp, void* stream);
+
+/* Inverse-CDF samples (N,n_samples) from bins (N,n_bins) and weights (N,n_bins-1);
+ * u (N,n_samples) uniforms or NULL for the deterministic linspace(0,1).
+ * Replaces SimpleNeRF.sample_pdf (src/models/SimpleNeRF17.py:384-417; identical
+ * copy SimpleTensoRF09.py:427-460); searchsorted(right=True) bin semantics. */
+int srf_sample_pdf(float* samples, const float* bins, const float* weights, const float* u, int n_rays,
+                   int n_bins, int n_samples, void* stream);
+
+/* Fine depths: mids of z_coarse, sample_pdf on weights_coarse[:,1:-1], merged and
+ * sorted with z_coarse -> z_fine (N, n_coarse+n_fine).  n_coarse+n_fine <= 1024.
+ * Replaces SimpleNeRF.get_z_vals_fine (src/models/SimpleNeRF17.py:360-371). */
+int srf_fine_z(float* z_fine, const float* z_coarse, const float* weights_coarse, const float* u, int n_rays,
+               int n_coarse, int n_fine, void* stream);
+
+/* TensoRF AABB ray marching depths z (N,S) = t_min + step*(arange(S) + u_ray).
+ * u (N,) or NULL.  Replaces SimpleTensoRF.get_z_vals_coarse non-NDC branch
+ * (src/models/SimpleTensoRF09.py:388-400). */
+int srf_aabb_z(float* z, const float* rays_o, const float* rays_d, const float* u, int n_rays, int n_samples,
+               const float* bbox /* host (2,3) */, float near_plane, float far_plane, float step_size,
+               void* stream);
+
+/* Positional encoding [x, sin(2^0 x), cos(2^0 x), ...] of x (M,dims) into
+ * out (M, ld_out) columns [0, dims*(2L+1)).
+ * Replaces PositionalEncoder (src/models/SimpleNeRF17.py:581-613). */
+int srf_positional_encoding(float* out, int ld_out, const float* x, int64_t m, int dims, int degree, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* NeRF MLP (fused PE + trunk + heads), forward and backward                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int points_net_depth;        /* Dp (reference: points_net_depth)             */
+    int points_net_width;        /* Wp                                           */
+    int views_net_depth;         /* Dv                                           */
+    int views_net_width;         /* Wv                                           */
+    int points_pe_degree;        /* L for xyz                                    */
+    int views_pe_degree;         /* L for view directions                        */
+    int points_sigma_pe_degree;  /* -1 when absent (points-augmentation variant) */
+    int use_view_dirs;
+    int view_dependent_rgb;
+    int skip_layer;              /* 4: concat [input, h] after this layer        */
+} srf_nerf_mlp_desc;
+
+enum { SRF_PRECISION_FP32 = 0, SRF_PRECISION_BF16 = 1 };
+
+/* Number of parameter tensors and, for index i, the reference state_dict name
+ * and element count (order = the order the params/grads arrays use). */
+int srf_nerf_mlp_num_params(const srf_nerf_mlp_desc* desc);
+int srf_nerf_mlp_param_info(const srf_nerf_mlp_desc* desc, int index, char* name, int name_len, int64_t* numel);
+
+/* Workspace bytes for srf_nerf_mlp_forward (+ backward when for_backward). */
+size_t srf_nerf_mlp_workspace_size(const srf_nerf_mlp_desc* desc, int64_t m, int precision, int for_backward);
+
+/* Forward of one MLP over m samples.  pts (m,3); dirs (ceil(m/dir_div),3) per-ray
+ * directions shared by dir_div consecutive samples (NULL when !use_view_dirs);
+ * sigma_noise (m) pre-scaled raw_noise_std*randn or NULL.  Outputs sigma (m)
+ * after ReLU and rgb (m,3) after sigmoid.  With for_backward, the workspace keeps
+ * what srf_nerf_mlp_backward needs (same workspace, same inputs).
+ * Replaces MLP.forward (src/models/SimpleNeRF17.py:696-785) including the
+ * chunking of run_network/batchify (:419-484). */
+int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* const* params, const float* pts,
+                         const float* dirs, int dir_div, int64_t m, const float* sigma_noise, float* sigma,
+                         float* rgb, int precision, int for_backward, void* workspace, size_t workspace_bytes,
+                         void* stream);
+
+/* Backward: dsigma (m) w.r.t. the ReLU'd sigma, drgb (m,3) w.r.t. the sigmoid
+ * rgb; dir_div as in the forward.  grads[i] receives (accumulate ? += : =) the
+ * gradient of params[i].  Uses the activations the forward left in the workspace. */
+int srf_nerf_mlp_backward(const srf_nerf_mlp_desc* desc, const float* const* params, const float* dsigma,
+                          const float* drgb, int dir_div, int64_t m, float* const* grads, int accumulate,
+                          int precision, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Alpha compositing                                                         */
+/* ------------------------------------------------------------------------ */
+
+enum {
+    SRF_COMPOSITE_NDC = 1,        /* z is NDC depth; also emit depth_ndc / depth_var_ndc  */
+    SRF_COMPOSITE_WHITE_BKGD = 2  /* rgb += 1 - acc                                        */
+};
+
+typedef struct {
+    int n_rays, n_samples, flags;
+    float distance_scale;          /* 1 for NeRF, tensor_configs['distance_scale'] for TensoRF */
+    const float* sigma;            /* (N,S)                                       */
+    const float* rgb;              /* (N,S,3)                                     */
+    const float* z;                /* (N,S) depth used for delta (NDC depth if NDC) */
+    const float* rays_d;           /* (N,3) world directions                       */
+    const float* rays_o;           /* (N,3) world origins (NDC only)               */
+    const float* rays_d_ndc;       /* (N,3) NDC directions (NDC only)              */
+    const uint8_t* white_per_ray;  /* (N) optional per-ray white-background flags  */
+    /* forward outputs (any may be NULL) */
+    float *rgb_map, *acc, *depth, *depth_var, *depth_ndc, *depth_var_ndc, *alpha, *visibility, *weights;
+    /* backward inputs: gradients of the outputs (any may be NULL = zero) */
+    const float *g_rgb, *g_acc, *g_depth, *g_depth_var, *g_depth_ndc, *g_depth_var_ndc, *g_weights;
+    /* backward outputs */
+    float *d_sigma, *d_rgb;
+} srf_composite_args;
+
+/* Replaces SimpleNeRF.volume_rendering (src/models/SimpleNeRF17.py:486-539),
+ * convert_depth_from_ndc (:541-558), LowRankTensor.get_volume_rendering_weights
+ * and volume_render (src/models/SimpleTensoRF09.py:767-819). */
+int srf_composite_forward(const srf_composite_args* args, void* stream);
+/* Adjoint: reverse-scan transmittance gradient, recomputing the forward per ray. */
+int srf_composite_backward(const srf_composite_args* args, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* TensoRF VM decomposition                                                  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int res[3];            /* grid resolution per world axis (x, y, z)                    */
+    int n_comp[3];         /* components per plane/line pair i (matrix_axes[i], vector_axes[i]) */
+    float* planes[3];      /* plane i: logical (1,R_i,res[m1],res[m0]), channels-last (H,W,R_i) */
+    float* lines[3];       /* line i:  logical (1,R_i,res[v],1), channels-last (L,R_i)         */
+} srf_vm_grid;
+
+/* Density features: out[p] = sum_i sum_r plane_i[r](x_m0,x_m1) * line_i[r](x_v) at
+ * normalised points pts (P,3) (bilinear, align_corners=True, zero padding).
+ * Replaces VmDecomposedTensor.get_volume_density (src/models/SimpleTensoRF09.py:1214-1239). */
+int srf_vm_density_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features,
+                           void* stream);
+/* Adds d(features) into the grid gradients (grad_grid: same layout as grid). */
+int srf_vm_density_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                            int64_t n_pts, const float* d_features, void* stream);
+/* Colour features (P, sum R_i): concat_i plane_i * line_i.
+ * Replaces VmDecomposedTensor.get_color lookups (src/models/SimpleTensoRF09.py:1252-1262). */
+int srf_vm_color_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features,
+                         void* stream);
+int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                          int64_t n_pts, const float* d_features, void* stream);
+
+/* Sample validity for TensoRF: inside the bbox and (when alpha_volume != NULL)
+ * alpha-mask trilinear value > 0; writes normalised points and a 0/1 mask.
+ * Replaces LowRankTensor.forward:705-710 + AlphaGridMask.sample_alpha
+ * (src/models/SimpleTensoRF09.py:1342-1349) + normalize_points (:763-765). */
+int srf_tensorf_sample_mask(const float* rays_o, const float* rays_d, const float* z, int n_rays, int n_samples,
+                            const float* bbox /* host (2,3) */, const float* alpha_volume, int vol_d, int vol_h,
+                            int vol_w, const float* alpha_bbox /* host (2,3) */, float* pts_norm,
+                            uint8_t* mask, void* stream);
+/* Alpha-mask query alone: out[p] = (trilinear(volume, pts_norm[p]) > 0). */
+int srf_alpha_mask_query(const float* alpha_volume, int vol_d, int vol_h, int vol_w, const float* pts_norm,
+                         int64_t n_pts, uint8_t* out, void* stream);
+
+/* Stream compaction: idx[0..count) = positions where mask != 0 (ascending).
+ * count is written to *count_dev (device int).  Workspace: srf_compact_workspace_size. */
+size_t srf_compact_workspace_size(int64_t n);
+int srf_compact(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* count_dev, void* workspace,
+                size_t workspace_bytes, void* stream);
+/* Mask of weights > threshold (surface samples, src/models/SimpleTensoRF09.py:726). */
+int srf_threshold_mask(const float* x, int64_t n, float threshold, uint8_t* mask, void* stream);
+
+/* Gather rows src[idx[i]] -> dst[i] (cols floats each), for i < *count_dev (max n). */
+int srf_gather_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
+                    int cols, int src_row_div, void* stream);
+/* Scatter rows src[i] -> dst[idx[i]] (dst not cleared; rows not in idx untouched). */
+int srf_scatter_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
+                     int cols, void* stream);
+
+/* Density activation on compacted features: ReLU (mode 0) or softplus(x+offset)
+ * (mode 1), written to sigma[idx[i]]; backward multiplies by the derivative.
+ * Replaces LowRankTensor.get_density_predictor (src/models/SimpleTensoRF09.py:671-679). */
+int srf_density_activation(float* sigma_dense, const float* features, const int32_t* idx,
+                           const int32_t* count_dev, int64_t n, int mode, float offset, void* stream);
+int srf_density_activation_backward(float* d_features, const float* d_sigma_dense, const float* features,
+                                    const int32_t* idx, const int32_t* count_dev, int64_t n, int mode,
+                                    float offset, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Generic dense layer (TensoRF renderer MLP and basis matrix)               */
+/* ------------------------------------------------------------------------ */
+
+enum { SRF_ACT_NONE = 0, SRF_ACT_RELU = 1, SRF_ACT_SIGMOID = 2 };
+
+/* y[r, :n] = act(x[r, :k] . W^T + bias) for r < rows (rows = *rows_dev if rows_dev
+ * else max_rows).  W (n,k) row-major as torch.nn.Linear.weight; bias may be NULL.
+ * Replaces the nn.Linear layers of MlpFeaturesColorPredictor and
+ * basis_matrix_color (src/models/SimpleTensoRF09.py:1151,1389-1392). */
+int srf_linear_forward(float* y, int ldy, const float* x, int ldx, const float* weight, const float* bias,
+                       int64_t max_rows, const int32_t* rows_dev, int n, int k, int act, void* stream);
+/* dx = (dy * act'(y)) . W ; dW (+)= dz^T x ; db (+)= sum dz, where dz = dy*act'(y).
+ * Any of dx, dw, db may be NULL.  dz scratch (rows, n) is caller-provided (may alias dy). */
+int srf_linear_backward(float* dx, int lddx, float* dw, float* db, const float* dy, int lddy, const float* y,
+                        int ldy, const float* x, int ldx, const float* weight, float* dz_scratch,
+                        int64_t max_rows, const int32_t* rows_dev, int n, int k, int act, int accumulate,
+                        void* stream);
+/* Positional-encoding backward d x (m,dims) from d out (m, ld) (TensoRF feature PE). */
+int srf_positional_encoding_backward(float* dx, const float* x, const float* dout, int ld_dout, int64_t m,
+                                     const int32_t* rows_dev, int dims, int degree, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Training-step helpers                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* Config-2 style loss on one net's outputs: mean over rays of mean over channels
+ * of (rgb - target)^2 (MSE14.compute_mse, src/loss_functions/MSE14.py:81-94) plus
+ * depth_weight * mean |depth - target_depth| over rays with depth_mask != 0.
+ * Adds the loss to *loss_dev (device float) and writes g_rgb (N,3), g_depth (N). */
+int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* depth, const float* target_depth,
+                       const uint8_t* depth_mask, int n_rays, int n_depth_rays, float depth_weight,
+                       float* loss_dev, float* g_rgb, float* g_depth, void* stream);
+
+/* Fused Adam (torch.optim.Adam semantics, bias-corrected, no amsgrad) over n
+ * elements; step is the 1-based step count after this update. */
+int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
+                  float beta1, float beta2, float eps, float weight_decay, int step, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SRF_GB300_H */

@@ -1,0 +1,134 @@
+"""ctypes binding of the srf_gb300 C ABI (``include/srf_gb300.h``).
+
+This is the same binding a Simple-RF maintainer would add on the reference
+side: plain pointers, sizes and a CUDA stream cross the boundary; a non-zero
+status becomes a ``RuntimeError``.  There is no fallback: if the shared library
+is missing, importing the package's kernels raises.
+"""
+import ctypes
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, 'libsrf_gb300.so')
+
+c_int, c_float, c_void_p, c_size_t = ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_size_t
+c_int64, c_char_p = ctypes.c_int64, ctypes.c_char_p
+P = ctypes.c_void_p            # device pointer
+FP = ctypes.POINTER(ctypes.c_float)
+
+
+class NerfMlpDesc(ctypes.Structure):
+    _fields_ = [('points_net_depth', c_int), ('points_net_width', c_int), ('views_net_depth', c_int),
+                ('views_net_width', c_int), ('points_pe_degree', c_int), ('views_pe_degree', c_int),
+                ('points_sigma_pe_degree', c_int), ('use_view_dirs', c_int), ('view_dependent_rgb', c_int),
+                ('skip_layer', c_int)]
+
+
+class CompositeArgs(ctypes.Structure):
+    _fields_ = [('n_rays', c_int), ('n_samples', c_int), ('flags', c_int), ('distance_scale', c_float),
+                ('sigma', P), ('rgb', P), ('z', P), ('rays_d', P), ('rays_o', P), ('rays_d_ndc', P),
+                ('white_per_ray', P),
+                ('rgb_map', P), ('acc', P), ('depth', P), ('depth_var', P), ('depth_ndc', P), ('depth_var_ndc', P),
+                ('alpha', P), ('visibility', P), ('weights', P),
+                ('g_rgb', P), ('g_acc', P), ('g_depth', P), ('g_depth_var', P), ('g_depth_ndc', P),
+                ('g_depth_var_ndc', P), ('g_weights', P),
+                ('d_sigma', P), ('d_rgb', P)]
+
+
+class VmGrid(ctypes.Structure):
+    _fields_ = [('res', c_int * 3), ('n_comp', c_int * 3), ('planes', P * 3), ('lines', P * 3)]
+
+
+SRF_COMPOSITE_NDC = 1
+SRF_COMPOSITE_WHITE_BKGD = 2
+SRF_PRECISION_FP32 = 0
+SRF_PRECISION_BF16 = 1
+SRF_ACT_NONE, SRF_ACT_RELU, SRF_ACT_SIGMOID = 0, 1, 2
+
+# name -> (restype, argtypes)
+_SIGS = {
+    'srf_status_string': (c_char_p, [c_int]),
+    'srf_version': (c_char_p, []),
+    'srf_last_cuda_error': (c_char_p, []),
+    'srf_read_device_flag': (c_int, [ctypes.POINTER(c_int), P]),
+    'srf_ndc_rays': (c_int, [P, P, P, P, c_int, c_int, c_int, c_float, P, P, P, P]),
+    'srf_stratified_z': (c_int, [P, P, c_int, c_int, c_float, c_float, c_int, P]),
+    'srf_sample_pdf': (c_int, [P, P, P, P, c_int, c_int, c_int, P]),
+    'srf_fine_z': (c_int, [P, P, P, P, c_int, c_int, c_int, P]),
+    'srf_aabb_z': (c_int, [P, P, P, P, c_int, c_int, FP, c_float, c_float, c_float, P]),
+    'srf_positional_encoding': (c_int, [P, c_int, P, c_int64, c_int, c_int, P]),
+    'srf_nerf_mlp_num_params': (c_int, [ctypes.POINTER(NerfMlpDesc)]),
+    'srf_nerf_mlp_param_info': (c_int, [ctypes.POINTER(NerfMlpDesc), c_int, c_char_p, c_int,
+                                        ctypes.POINTER(c_int64)]),
+    'srf_nerf_mlp_workspace_size': (c_size_t, [ctypes.POINTER(NerfMlpDesc), c_int64, c_int, c_int]),
+    'srf_nerf_mlp_forward': (c_int, [ctypes.POINTER(NerfMlpDesc), ctypes.POINTER(P), P, P, c_int, c_int64, P, P, P,
+                                     c_int, c_int, P, c_size_t, P]),
+    'srf_nerf_mlp_backward': (c_int, [ctypes.POINTER(NerfMlpDesc), ctypes.POINTER(P), P, P, c_int, c_int64,
+                                      ctypes.POINTER(P), c_int, c_int, P, c_size_t, P]),
+    'srf_composite_forward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
+    'srf_composite_backward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
+    'srf_vm_density_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_vm_density_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_vm_color_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_vm_color_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_tensorf_sample_mask': (c_int, [P, P, P, c_int, c_int, FP, P, c_int, c_int, c_int, FP, P, P, P]),
+    'srf_alpha_mask_query': (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
+    'srf_compact_workspace_size': (c_size_t, [c_int64]),
+    'srf_compact': (c_int, [P, c_int64, P, P, P, c_size_t, P]),
+    'srf_threshold_mask': (c_int, [P, c_int64, c_float, P, P]),
+    'srf_gather_rows': (c_int, [P, P, P, P, c_int64, c_int, c_int, P]),
+    'srf_scatter_rows': (c_int, [P, P, P, P, c_int64, c_int, P]),
+    'srf_density_activation': (c_int, [P, P, P, P, c_int64, c_int, c_float, P]),
+    'srf_density_activation_backward': (c_int, [P, P, P, P, P, c_int64, c_int, c_float, P]),
+    'srf_linear_forward': (c_int, [P, c_int, P, c_int, P, P, c_int64, P, c_int, c_int, c_int, P]),
+    'srf_linear_backward': (c_int, [P, c_int, P, P, P, c_int, P, c_int, P, c_int, P, P, c_int64, P, c_int, c_int,
+                                    c_int, c_int, P]),
+    'srf_positional_encoding_backward': (c_int, [P, P, P, c_int, c_int64, P, c_int, c_int, P]),
+    'srf_rgb_depth_loss': (c_int, [P, P, P, P, P, c_int, c_int, c_float, P, P, P, P]),
+    'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P]),
+}
+
+
+def exported_symbols():
+    """Names of every function the C header declares (used by the ABI test)."""
+    return sorted(_SIGS)
+
+
+_lib = None
+
+
+def load():
+    """Load the shared library (once); raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f'srf_gb300 CUDA library not built: {LIB_PATH} is missing '
+                           '(run `python -m simple_rf_gb300.build`); there is no CPU fallback')
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status, what=''):
+    if status != 0:
+        lib = load()
+        msg = lib.srf_status_string(status).decode()
+        if status == 5:
+            msg += ' (' + lib.srf_last_cuda_error().decode() + ')'
+        raise RuntimeError(f'{what}: {msg}')
+
+
+def call(name, *args):
+    """Call ``name`` and raise RuntimeError on a non-zero status."""
+    lib = load()
+    check(getattr(lib, name)(*args), name)
+
+
+def host_floats(vals):
+    arr = (ctypes.c_float * len(vals))(*[float(v) for v in vals])
+    return arr

@@ -1,0 +1,70 @@
+// Status strings, CUDA error text and the device-side error flag.
+#include <cstdio>
+#include <cstring>
+
+#include "srf_common.cuh"
+
+namespace {
+__device__ int g_srf_flag = 0;
+thread_local char g_last_error[256] = "no error";
+}  // namespace
+
+namespace srf {
+
+void set_cuda_error(cudaError_t e) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+int* device_flag() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    static int* cache[64] = {nullptr};
+    if (dev < 0 || dev >= 64) return nullptr;
+    if (!cache[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_srf_flag) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        cache[dev] = static_cast<int*>(p);
+    }
+    return cache[dev];
+}
+
+}  // namespace srf
+
+extern "C" const char* srf_status_string(int status) {
+    switch (status) {
+        case SRF_OK: return "SRF_OK";
+        case SRF_ERR_NULL: return "SRF_ERR_NULL: a required pointer is NULL";
+        case SRF_ERR_SHAPE: return "SRF_ERR_SHAPE: a size is out of the supported range";
+        case SRF_ERR_ALIGN: return "SRF_ERR_ALIGN: a pointer or stride breaks an alignment rule";
+        case SRF_ERR_WORKSPACE: return "SRF_ERR_WORKSPACE: workspace too small";
+        case SRF_ERR_CUDA: return "SRF_ERR_CUDA: a CUDA call failed";
+        case SRF_ERR_TIMEOUT: return "SRF_ERR_TIMEOUT: a bounded device wait gave up";
+        case SRF_ERR_RANGE: return "SRF_ERR_RANGE: a device-side index check failed";
+        case SRF_ERR_UNSUPPORTED: return "SRF_ERR_UNSUPPORTED: configuration not supported";
+        default: return "unknown srf status";
+    }
+}
+
+extern "C" const char* srf_version(void) { return "srf_gb300 1.0 sm_103a"; }
+
+extern "C" const char* srf_last_cuda_error(void) { return g_last_error; }
+
+extern "C" int srf_read_device_flag(int* flag_out, void* stream) {
+    if (!flag_out) return SRF_ERR_NULL;
+    int* f = srf::device_flag();
+    if (!f) return SRF_ERR_CUDA;
+    int host = 0;
+    cudaStream_t s = srf::as_stream(stream);
+    cudaError_t e = cudaMemcpyAsync(&host, f, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(f, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        srf::set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    *flag_out = host;
+    return SRF_OK;
+}

@@ -1,0 +1,334 @@
+// Alpha compositing, forward and adjoint.  One warp per ray; samples are
+// processed in rounds of 32 (lane j <-> sample base+j, coalesced), the
+// transmittance is a multiplicative warp scan with a carry between rounds, and
+// the backward transmittance adjoint is a reverse affine scan.
+//
+// Formulas follow SimpleNeRF17.py:486-558 (NeRF) and SimpleTensoRF09.py:767-819
+// (TensoRF: the extra distance_scale factor).
+#include "srf_common.cuh"
+
+namespace srf {
+namespace {
+
+constexpr float kEps = 1e-6f;
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct RayCtx {
+    const float* sigma;
+    const float* z;
+    int s;
+    float dnorm;
+    float ds;
+    float inf_depth;
+    bool ndc;
+    float oz, dz;   // world origin/direction z (NDC depth conversion)
+};
+
+// SimpleNeRF17.py:541-558 convert_depth_from_ndc (near = 1).
+__device__ __forceinline__ float depth_from_ndc(float zn, float oz, float dz) {
+    float tn = -(1.f + oz) / dz;
+    float c = zn == 1.f ? 1e-3f : 0.f;
+    return (oz + tn * dz) / dz * (1.f / (1.f - zn + c) - 1.f) + tn;
+}
+
+// Per-sample quantities of sample i.
+__device__ __forceinline__ void sample_terms(const RayCtx& c, int i, float& delta, float& ex, float& alpha,
+                                             float& p) {
+    float zi = c.z[i];
+    float zn = i + 1 < c.s ? c.z[i + 1] : c.inf_depth;
+    delta = (zn - zi) * c.dnorm;
+    float x = -c.sigma[i] * delta;
+    x = x * c.ds;
+    ex = expf(x);
+    alpha = 1.f - ex;
+    p = 1.f - alpha + 1e-10f;
+}
+
+// Pass over the ray storing T (exclusive cumprod of p) and alpha in shared memory.
+__device__ void forward_scan(const RayCtx& c, float* sT, float* sA) {
+    int lane = threadIdx.x & 31;
+    float carry = 1.f;
+    for (int base = 0; base < c.s; base += 32) {
+        int i = base + lane;
+        float delta, ex, alpha, p;
+        if (i < c.s) {
+            sample_terms(c, i, delta, ex, alpha, p);
+        } else {
+            alpha = 0.f;
+            p = 1.f;
+        }
+        float inc = p;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            float t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc *= t;
+        }
+        float exc = __shfl_up_sync(0xffffffffu, inc, 1);
+        if (lane == 0) exc = 1.f;
+        float T = carry * exc;
+        if (i < c.s) {
+            sT[i] = T;
+            sA[i] = alpha;
+        }
+        carry = carry * __shfl_sync(0xffffffffu, inc, 31);
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ RayCtx make_ctx(const srf_composite_args& a, int r) {
+    RayCtx c;
+    c.s = a.n_samples;
+    c.sigma = a.sigma + int64_t(r) * c.s;
+    c.z = a.z + int64_t(r) * c.s;
+    c.ndc = (a.flags & SRF_COMPOSITE_NDC) != 0;
+    const float* dv = c.ndc ? a.rays_d_ndc + 3 * r : a.rays_d + 3 * r;
+    c.dnorm = sqrtf(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    c.ds = a.distance_scale;
+    c.inf_depth = c.ndc ? 1.f : 1e10f;
+    c.oz = c.ndc ? a.rays_o[3 * r + 2] : 0.f;
+    c.dz = c.ndc ? a.rays_d[3 * r + 2] : 0.f;
+    return c;
+}
+
+__device__ __forceinline__ bool white_for(const srf_composite_args& a, int r) {
+    return (a.flags & SRF_COMPOSITE_WHITE_BKGD) || (a.white_per_ray && a.white_per_ray[r]);
+}
+
+__global__ void composite_fwd_kernel(srf_composite_args a) {
+    extern __shared__ float smem[];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (r >= a.n_rays) return;
+    float* sT = smem + size_t(warp) * 2 * a.n_samples;
+    float* sA = sT + a.n_samples;
+    RayCtx c = make_ctx(a, r);
+    forward_scan(c, sT, sA);
+    const float* rgb = a.rgb + int64_t(r) * c.s * 3;
+    float cr = 0.f, cg = 0.f, cb = 0.f, acc = 0.f, wz = 0.f, wzn = 0.f;
+    for (int i = lane; i < c.s; i += 32) {
+        float w = sA[i] * sT[i];
+        cr += w * rgb[3 * i];
+        cg += w * rgb[3 * i + 1];
+        cb += w * rgb[3 * i + 2];
+        acc += w;
+        float zi = c.z[i];
+        if (c.ndc) {
+            wzn += w * zi;
+            wz += w * depth_from_ndc(zi, c.oz, c.dz);
+        } else {
+            wz += w * zi;
+        }
+    }
+    cr = warp_sum(cr); cg = warp_sum(cg); cb = warp_sum(cb);
+    acc = warp_sum(acc); wz = warp_sum(wz); wzn = warp_sum(wzn);
+    float depth = wz / (acc + kEps);
+    float depth_ndc = wzn / (acc + kEps);
+    float var = 0.f, var_ndc = 0.f;
+    int64_t ro = int64_t(r) * c.s;
+    for (int i = lane; i < c.s; i += 32) {
+        float w = sA[i] * sT[i];
+        float zi = c.z[i];
+        float zm = c.ndc ? depth_from_ndc(zi, c.oz, c.dz) : zi;
+        float d = zm - depth;
+        var += w * (d * d);
+        if (c.ndc) {
+            float dn = zi - depth_ndc;
+            var_ndc += w * (dn * dn);
+        }
+        if (a.alpha) a.alpha[ro + i] = sA[i];
+        if (a.visibility) a.visibility[ro + i] = sT[i];
+        if (a.weights) a.weights[ro + i] = w;
+    }
+    var = warp_sum(var);
+    var_ndc = warp_sum(var_ndc);
+    if (lane == 0) {
+        if (white_for(a, r)) {
+            cr = cr + (1.f - acc);
+            cg = cg + (1.f - acc);
+            cb = cb + (1.f - acc);
+        }
+        if (a.rgb_map) {
+            a.rgb_map[3 * r] = cr;
+            a.rgb_map[3 * r + 1] = cg;
+            a.rgb_map[3 * r + 2] = cb;
+        }
+        if (a.acc) a.acc[r] = acc;
+        if (a.depth) a.depth[r] = depth;
+        if (a.depth_var) a.depth_var[r] = var;
+        if (c.ndc) {
+            if (a.depth_ndc) a.depth_ndc[r] = depth_ndc;
+            if (a.depth_var_ndc) a.depth_var_ndc[r] = var_ndc;
+        }
+    }
+}
+
+__global__ void composite_bwd_kernel(srf_composite_args a) {
+    extern __shared__ float smem[];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (r >= a.n_rays) return;
+    float* sT = smem + size_t(warp) * 2 * a.n_samples;
+    float* sA = sT + a.n_samples;
+    RayCtx c = make_ctx(a, r);
+    forward_scan(c, sT, sA);
+    const float* rgb = a.rgb + int64_t(r) * c.s * 3;
+    // forward sums: acc, depth (and NDC depth)
+    float acc = 0.f, wz = 0.f, wzn = 0.f;
+    for (int i = lane; i < c.s; i += 32) {
+        float w = sA[i] * sT[i];
+        acc += w;
+        float zi = c.z[i];
+        if (c.ndc) {
+            wzn += w * zi;
+            wz += w * depth_from_ndc(zi, c.oz, c.dz);
+        } else {
+            wz += w * zi;
+        }
+    }
+    acc = warp_sum(acc); wz = warp_sum(wz); wzn = warp_sum(wzn);
+    float inv = 1.f / (acc + kEps);
+    float depth = wz / (acc + kEps), depth_ndc = wzn / (acc + kEps);
+    float gd = a.g_depth ? a.g_depth[r] : 0.f;
+    float gv = a.g_depth_var ? a.g_depth_var[r] : 0.f;
+    float gdn = (c.ndc && a.g_depth_ndc) ? a.g_depth_ndc[r] : 0.f;
+    float gvn = (c.ndc && a.g_depth_var_ndc) ? a.g_depth_var_ndc[r] : 0.f;
+    // B = sum w (z - depth): the depth_var gradient's coupling term
+    float bsum = 0.f, bsum_n = 0.f;
+    if (gv != 0.f || gvn != 0.f) {
+        for (int i = lane; i < c.s; i += 32) {
+            float w = sA[i] * sT[i];
+            float zi = c.z[i];
+            float zm = c.ndc ? depth_from_ndc(zi, c.oz, c.dz) : zi;
+            bsum += w * (zm - depth);
+            if (c.ndc) bsum_n += w * (zi - depth_ndc);
+        }
+        bsum = warp_sum(bsum);
+        bsum_n = warp_sum(bsum_n);
+    }
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    if (a.g_rgb) {
+        g0 = a.g_rgb[3 * r];
+        g1 = a.g_rgb[3 * r + 1];
+        g2 = a.g_rgb[3 * r + 2];
+    }
+    float gacc = a.g_acc ? a.g_acc[r] : 0.f;
+    if (white_for(a, r)) gacc -= g0 + g1 + g2;
+    int64_t ro = int64_t(r) * c.s;
+    // dL/dw_i
+    auto G_of = [&](int i) -> float {
+        float zi = c.z[i];
+        float zm = c.ndc ? depth_from_ndc(zi, c.oz, c.dz) : zi;
+        float g = rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 + gacc;
+        if (a.g_weights) g += a.g_weights[ro + i];
+        float d = zm - depth;
+        g += gd * d * inv + gv * (d * d - 2.f * bsum * d * inv);
+        if (c.ndc) {
+            float dn = zi - depth_ndc;
+            g += gdn * dn * inv + gvn * (dn * dn - 2.f * bsum_n * dn * inv);
+        }
+        return g;
+    };
+    // reverse affine scan: R_i = G_{i+1} a_{i+1} + p_{i+1} R_{i+1}, R_{S-1} = 0
+    float carry = 0.f;                  // R at the first sample of the round to the right
+    float next_ga = 0.f, next_p = 0.f;  // G*alpha and p of that first sample
+    int last_base = ((c.s - 1) / 32) * 32;
+    for (int base = last_base; base >= 0; base -= 32) {
+        int i = base + lane;
+        bool in = i < c.s;
+        float Gi = 0.f, alpha = 0.f, T = 0.f, p = 1.f, ga = 0.f;
+        if (in) {
+            Gi = G_of(i);
+            alpha = sA[i];
+            T = sT[i];
+            p = 1.f - alpha + 1e-10f;
+            ga = Gi * alpha;
+        }
+        // coefficients of sample i: a_i = G_{i+1} alpha_{i+1}, b_i = p_{i+1}
+        float ga_next = __shfl_down_sync(0xffffffffu, ga, 1);
+        float p_next = __shfl_down_sync(0xffffffffu, p, 1);
+        if (lane == 31) {
+            ga_next = next_ga;
+            p_next = next_p;
+        }
+        float A = in && i + 1 < c.s ? ga_next : 0.f;
+        float B = in && i + 1 < c.s ? p_next : 0.f;
+        // inclusive suffix composition of the affine maps lane..31
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            float A2 = __shfl_down_sync(0xffffffffu, A, o);
+            float B2 = __shfl_down_sync(0xffffffffu, B, o);
+            if (lane + o < 32) {
+                A = A + B * A2;
+                B = B * B2;
+            }
+        }
+        float R = A + B * carry;
+        if (in) {
+            float dalpha = T * (Gi - R);
+            float delta, ex, al, pp;
+            sample_terms(c, i, delta, ex, al, pp);
+            float dx = -dalpha * ex;
+            dx = dx * c.ds;
+            a.d_sigma[ro + i] = -dx * delta;
+            if (a.d_rgb) {
+                float w = alpha * T;
+                float* dr = a.d_rgb + (ro + i) * 3;
+                dr[0] = w * g0;
+                dr[1] = w * g1;
+                dr[2] = w * g2;
+            }
+        }
+        carry = __shfl_sync(0xffffffffu, R, 0);
+        next_ga = __shfl_sync(0xffffffffu, ga, 0);
+        next_p = __shfl_sync(0xffffffffu, p, 0);
+    }
+}
+
+int check_args(const srf_composite_args* a, bool bwd) {
+    if (!a || !a->sigma || !a->z || !a->rays_d) return SRF_ERR_NULL;
+    if ((a->flags & SRF_COMPOSITE_NDC) && (!a->rays_o || !a->rays_d_ndc)) return SRF_ERR_NULL;
+    if (a->n_rays < 0 || a->n_samples < 1 || a->n_samples > 16384) return SRF_ERR_SHAPE;
+    if (!a->rgb && (a->rgb_map || bwd)) return SRF_ERR_NULL;
+    if (bwd && !a->d_sigma) return SRF_ERR_NULL;
+    return SRF_OK;
+}
+
+template <class K>
+int launch(K kernel, const srf_composite_args* a, void* stream) {
+    size_t per_warp = size_t(2) * a->n_samples * sizeof(float);
+    int warps = int(49152 / per_warp);
+    if (warps > 8) warps = 8;
+    if (warps < 1) warps = 1;
+    size_t smem = per_warp * warps;
+    if (smem > 49152) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+    }
+    kernel<<<grid_1d(a->n_rays, warps), warps * 32, smem, as_stream(stream)>>>(*a);
+    return launch_status();
+}
+
+}  // namespace
+}  // namespace srf
+
+using namespace srf;
+
+extern "C" int srf_composite_forward(const srf_composite_args* args, void* stream) {
+    int st = check_args(args, false);
+    if (st != SRF_OK || args->n_rays == 0) return st;
+    return launch(composite_fwd_kernel, args, stream);
+}
+
+extern "C" int srf_composite_backward(const srf_composite_args* args, void* stream) {
+    int st = check_args(args, true);
+    if (st != SRF_OK || args->n_rays == 0) return st;
+    return launch(composite_bwd_kernel, args, stream);
+}

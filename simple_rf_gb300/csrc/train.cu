@@ -1,0 +1,90 @@
+// Training-step helpers: the config-2 loss gradient and a fused Adam update.
+#include "srf_common.cuh"
+
+namespace srf {
+namespace {
+
+__global__ void loss_kernel(const float* __restrict__ rgb, const float* __restrict__ trgb,
+                            const float* __restrict__ depth, const float* __restrict__ tdepth,
+                            const uint8_t* __restrict__ dmask, int n, int nd, float dw, float* loss, float* g_rgb,
+                            float* g_depth) {
+    __shared__ float red[32];
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (r < n) {
+        float inv = 2.f / float(3 * n);
+        for (int c = 0; c < 3; ++c) {
+            float e = rgb[3 * r + c] - trgb[3 * r + c];
+            l += e * e / float(3 * n);
+            g_rgb[3 * r + c] = inv * e;
+        }
+        float gd = 0.f;
+        if (depth && dmask && dmask[r] && nd > 0) {
+            float e = depth[r] - tdepth[r];
+            l += dw * fabsf(e) / float(nd);
+            gd = dw / float(nd) * (e > 0.f ? 1.f : (e < 0.f ? -1.f : 0.f));
+        }
+        if (g_depth) g_depth[r] = gd;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        l = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        if (threadIdx.x == 0 && loss) atomicAdd(loss, l);
+    }
+}
+
+// torch.optim.Adam (foreach=False math): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
+// p -= lr / (1 - b1^t) * m / (sqrt(v) / sqrt(1 - b2^t) + eps).
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float wd,
+                            float bc1, float bc2_sqrt) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (; i < n; i += stride) {
+        float gi = g[i];
+        if (wd != 0.f) gi += wd * p[i];
+        float mi = b1 * m[i] + (1.f - b1) * gi;
+        float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        float denom = sqrtf(vi) / bc2_sqrt + eps;
+        p[i] -= (lr / bc1) * mi / denom;
+    }
+}
+
+}  // namespace
+}  // namespace srf
+
+using namespace srf;
+
+extern "C" int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* depth,
+                                  const float* target_depth, const uint8_t* depth_mask, int n_rays, int n_depth_rays,
+                                  float depth_weight, float* loss_dev, float* g_rgb, float* g_depth, void* stream) {
+    if (!rgb || !target_rgb || !g_rgb) return SRF_ERR_NULL;
+    if (depth_mask && (!depth || !target_depth)) return SRF_ERR_NULL;
+    if (n_rays < 0 || n_depth_rays < 0) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    loss_kernel<<<grid_1d(n_rays, 256), 256, 0, as_stream(stream)>>>(rgb, target_rgb, depth, target_depth, depth_mask,
+                                                                     n_rays, n_depth_rays, depth_weight, loss_dev,
+                                                                     g_rgb, g_depth);
+    return launch_status();
+}
+
+extern "C" int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
+                             float beta1, float beta2, float eps, float weight_decay, int step, void* stream) {
+    if (!param || !grad || !exp_avg || !exp_avg_sq) return SRF_ERR_NULL;
+    if (n < 0 || step < 1) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    float bc1 = 1.f - powf(beta1, float(step));
+    float bc2 = sqrtf(1.f - powf(beta2, float(step)));
+    unsigned blocks = grid_1d(n, 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    adam_kernel<<<blocks, 256, 0, as_stream(stream)>>>(param, grad, exp_avg, exp_avg_sq, n, lr, beta1, beta2, eps,
+                                                       weight_decay, bc1, bc2);
+    return launch_status();
+}

@@ -1,0 +1,522 @@
+// TensoRF VM (vector-matrix) plane/line lookups, alpha-mask query, sample
+// masks and stream compaction (SimpleTensoRF09.py:701-765, 1214-1272, 1342-1349).
+//
+// Planes and lines are stored channels-last (plane (H,W,R), line (L,R)) so one
+// bilinear corner is R contiguous floats: a corner of a 16-component plane is a
+// single 64-byte line, read with 128-bit loads.  One thread handles one
+// (point, plane) pair for the density path, and one point for colour.
+#include "srf_common.cuh"
+
+namespace srf {
+namespace {
+
+__constant__ int kMatrixAxes[3][2] = {{0, 1}, {0, 2}, {1, 2}};   // SimpleTensoRF09.py:1131
+__constant__ int kVectorAxes[3] = {2, 1, 0};                      // SimpleTensoRF09.py:1132
+
+// Bilinear taps of torch's CPU grid sampler (align_corners=True, zeros padding):
+// ix = (x + 1) * ((W - 1) / 2); weights from the fractional parts.
+struct Taps {
+    int idx[4];    // flat corner index (y * W + x), -1 when out of bounds
+    float w[4];
+};
+
+__device__ __forceinline__ Taps bilinear(float gx, float gy, int h, int w) {
+    Taps t;
+    float ix = (gx + 1.f) * (float(w - 1) * 0.5f);
+    float iy = (gy + 1.f) * (float(h - 1) * 0.5f);
+    float x0f = floorf(ix), y0f = floorf(iy);
+    float fw = ix - x0f, fe = 1.f - fw;
+    float fn = iy - y0f, fs = 1.f - fn;
+    int x0 = int(x0f), y0 = int(y0f);
+    const int dx[4] = {0, 1, 0, 1}, dy[4] = {0, 0, 1, 1};
+    const float ww[4] = {fs * fe, fs * fw, fn * fe, fn * fw};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        int xi = x0 + dx[c], yi = y0 + dy[c];
+        bool ok = xi >= 0 && xi < w && yi >= 0 && yi < h && isfinite(ix) && isfinite(iy);
+        t.idx[c] = ok ? yi * w + xi : -1;
+        t.w[c] = ok ? ww[c] : 0.f;
+    }
+    return t;
+}
+
+// Line lookup: grid (0, v) on a (L, 1) image; x taps collapse to ix = 0.
+__device__ __forceinline__ Taps line_taps(float gv, int len) {
+    return bilinear(0.f, gv, len, 1);
+}
+
+// sum_r plane[r] * line[r] for R components (R multiple of 4 uses float4 loads).
+__device__ __forceinline__ float vm_dot(const float* __restrict__ plane, const float* __restrict__ line, int R,
+                                        const Taps& pt, const Taps& lt) {
+    float acc = 0.f;
+    if ((R & 3) == 0) {
+        for (int r = 0; r < R; r += 4) {
+            float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), lv = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) {
+                    float4 v = *reinterpret_cast<const float4*>(plane + int64_t(pt.idx[c]) * R + r);
+                    pv.x += v.x * pt.w[c]; pv.y += v.y * pt.w[c]; pv.z += v.z * pt.w[c]; pv.w += v.w * pt.w[c];
+                }
+                if (lt.idx[c] >= 0) {
+                    float4 v = *reinterpret_cast<const float4*>(line + int64_t(lt.idx[c]) * R + r);
+                    lv.x += v.x * lt.w[c]; lv.y += v.y * lt.w[c]; lv.z += v.z * lt.w[c]; lv.w += v.w * lt.w[c];
+                }
+            }
+            acc += pv.x * lv.x;
+            acc += pv.y * lv.y;
+            acc += pv.z * lv.z;
+            acc += pv.w * lv.w;
+        }
+    } else {
+        for (int r = 0; r < R; ++r) {
+            float pv = 0.f, lv = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) pv += plane[int64_t(pt.idx[c]) * R + r] * pt.w[c];
+                if (lt.idx[c] >= 0) lv += line[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+            }
+            acc += pv * lv;
+        }
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void plane_taps(const srf_vm_grid& g, int i, const float* p, Taps& pt, Taps& lt) {
+    int m0 = kMatrixAxes[i][0], m1 = kMatrixAxes[i][1], v = kVectorAxes[i];
+    pt = bilinear(p[m0], p[m1], g.res[m1], g.res[m0]);
+    lt = line_taps(p[v], g.res[v]);
+}
+
+__global__ void density_fwd_kernel(srf_vm_grid g, const float* __restrict__ pts, int64_t n, float* out) {
+    int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* q = pts + 3 * p;
+    float acc = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        Taps pt, lt;
+        plane_taps(g, i, q, pt, lt);
+        acc = acc + vm_dot(g.planes[i], g.lines[i], g.n_comp[i], pt, lt);
+    }
+    out[p] = acc;
+}
+
+__global__ void color_fwd_kernel(srf_vm_grid g, const float* __restrict__ pts, int64_t n, int ld, float* out) {
+    int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* q = pts + 3 * p;
+    float* o = out + p * ld;
+    int off = 0;
+    for (int i = 0; i < 3; ++i) {
+        Taps pt, lt;
+        plane_taps(g, i, q, pt, lt);
+        int R = g.n_comp[i];
+        const float* pl = g.planes[i];
+        const float* ln = g.lines[i];
+        for (int r = 0; r < R; ++r) {
+            float pv = 0.f, lv = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
+                if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+            }
+            o[off + r] = pv * lv;
+        }
+        off += R;
+    }
+}
+
+// Adjoint: d plane[r] at corner c += w_c * d * line_value[r] (and symmetrically).
+// Colour: d_features (P, ld) per component; density: one scalar per point.
+__global__ void vm_bwd_kernel(srf_vm_grid gg, srf_vm_grid g, const float* __restrict__ pts, int64_t n,
+                              const float* __restrict__ dfeat, int ld, int per_component) {
+    int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* q = pts + 3 * p;
+    int off = 0;
+    for (int i = 0; i < 3; ++i) {
+        Taps pt, lt;
+        plane_taps(g, i, q, pt, lt);
+        int R = g.n_comp[i];
+        const float* pl = g.planes[i];
+        const float* ln = g.lines[i];
+        float* gpl = gg.planes[i];
+        float* gln = gg.lines[i];
+        for (int r = 0; r < R; ++r) {
+            float pv = 0.f, lv = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
+                if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+            }
+            float d = per_component ? dfeat[p * ld + off + r] : dfeat[p];
+            float dp = d * lv, dl = d * pv;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0 && dp != 0.f) atomicAdd(gpl + int64_t(pt.idx[c]) * R + r, dp * pt.w[c]);
+                if (lt.idx[c] >= 0 && dl != 0.f) atomicAdd(gln + int64_t(lt.idx[c]) * R + r, dl * lt.w[c]);
+            }
+        }
+        off += R;
+    }
+}
+
+// AlphaGridMask.sample_alpha + "> 0": true iff an occupied in-bound corner has a
+// positive trilinear weight (all terms are >= 0, so the float sum is positive
+// exactly then).  Weights use torch's CPU 3-D formula ((x1 - ix) * (y1 - iy) * ...).
+__device__ __forceinline__ bool alpha_positive(const float* __restrict__ vol, int d, int h, int w, float x, float y,
+                                               float z) {
+    float ix = ((x + 1.f) / 2.f) * float(w - 1);
+    float iy = ((y + 1.f) / 2.f) * float(h - 1);
+    float iz = ((z + 1.f) / 2.f) * float(d - 1);
+    if (!(isfinite(ix) && isfinite(iy) && isfinite(iz))) return false;
+    float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    float x1 = x0 + 1.f, y1 = y0 + 1.f, z1 = z0 + 1.f;
+    float wx[2] = {x1 - ix, ix - x0}, wy[2] = {y1 - iy, iy - y0}, wz[2] = {z1 - iz, iz - z0};
+    int xi0 = int(x0), yi0 = int(y0), zi0 = int(z0);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+        int xi = xi0 + cx, yi = yi0 + cy, zi = zi0 + cz;
+        if (xi < 0 || xi >= w || yi < 0 || yi >= h || zi < 0 || zi >= d) continue;
+        float wt = wx[cx] * wy[cy] * wz[cz];
+        if (wt > 0.f && vol[(int64_t(zi) * h + yi) * w + xi] * wt > 0.f) return true;
+    }
+    return false;
+}
+
+__global__ void alpha_query_kernel(const float* __restrict__ vol, int d, int h, int w, const float* __restrict__ p,
+                                   int64_t n, uint8_t* out) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = alpha_positive(vol, d, h, w, p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+}
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+__global__ void sample_mask_kernel(const float* __restrict__ o, const float* __restrict__ dir,
+                                   const float* __restrict__ z, int n, int s, Box box, const float* __restrict__ vol,
+                                   int vd, int vh, int vw, Box abox, float* pn, uint8_t* mask) {
+    int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= int64_t(n) * s) return;
+    int r = int(idx / s);
+    float zz = z[idx];
+    float q[3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        q[a] = o[3 * r + a] + dir[3 * r + a] * zz;   // SimpleTensoRF09.py:261
+        inside = inside && box.lo[a] <= q[a] && q[a] <= box.hi[a];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pn[3 * idx + a] = ((q[a] - box.lo[a]) / (box.hi[a] - box.lo[a])) * 2.f - 1.f;
+    if (inside && vol) {
+        float an[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) an[a] = ((q[a] - abox.lo[a]) / (abox.hi[a] - abox.lo[a])) * 2.f - 1.f;
+        inside = alpha_positive(vol, vd, vh, vw, an[0], an[1], an[2]);
+    }
+    mask[idx] = inside;
+}
+
+__global__ void threshold_kernel(const float* __restrict__ x, int64_t n, float thr, uint8_t* m) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) m[i] = x[i] > thr;
+}
+
+// ---- compaction: per-block counts -> exclusive scan of block counts -> write
+constexpr int kCompactBlock = 1024;
+
+__global__ void count_kernel(const uint8_t* __restrict__ mask, int64_t n, int* block_counts) {
+    __shared__ int warp_counts[32];
+    int64_t i = int64_t(blockIdx.x) * kCompactBlock + threadIdx.x;
+    int v = i < n ? (mask[i] != 0) : 0;
+    unsigned b = __ballot_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) warp_counts[threadIdx.x >> 5] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int c = warp_counts[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (threadIdx.x == 0) block_counts[blockIdx.x] = c;
+    }
+}
+
+// Single-block exclusive scan over the block counts (in place), total -> *count.
+__global__ void scan_counts_kernel(int* counts, int nb, int* total) {
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? counts[i] : 0;
+        int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        int inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        __shared__ int wsum[32];
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            int ws = lane < int(blockDim.x >> 5) ? wsum[lane] : 0;
+            int wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+            wsum[lane] = wi - ws;
+        }
+        __syncthreads();
+        int excl = carry + wsum[warp] + inc - v;
+        if (i < nb) counts[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void write_idx_kernel(const uint8_t* __restrict__ mask, int64_t n, const int* __restrict__ offsets,
+                                 int32_t* idx) {
+    __shared__ int warp_base[32];
+    int64_t i = int64_t(blockIdx.x) * kCompactBlock + threadIdx.x;
+    int v = i < n ? (mask[i] != 0) : 0;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned b = __ballot_sync(0xffffffffu, v);
+    if (lane == 0) warp_base[warp] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int w = 0; w < kCompactBlock / 32; ++w) {
+            int c = warp_base[w];
+            warp_base[w] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (v) {
+        int pos = offsets[blockIdx.x] + warp_base[warp] + __popc(b & ((1u << lane) - 1u));
+        idx[pos] = int32_t(i);
+    }
+}
+
+__global__ void gather_rows_kernel(float* dst, const float* __restrict__ src, const int32_t* __restrict__ idx,
+                                   const int32_t* count, int64_t n, int cols, int div) {
+    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t cnt = *count < n ? *count : n;
+    if (t >= cnt * cols) return;
+    int64_t i = t / cols;
+    int c = int(t % cols);
+    int64_t row = idx[i];
+    if (div > 1) row /= div;
+    dst[t] = src[row * cols + c];
+}
+
+__global__ void scatter_rows_kernel(float* dst, const float* __restrict__ src, const int32_t* __restrict__ idx,
+                                    const int32_t* count, int64_t n, int cols) {
+    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t cnt = *count < n ? *count : n;
+    if (t >= cnt * cols) return;
+    int64_t i = t / cols;
+    int c = int(t % cols);
+    dst[int64_t(idx[i]) * cols + c] = src[t];
+}
+
+__device__ __forceinline__ float softplus_f(float x) {
+    // torch softplus (beta 1, threshold 20)
+    return x > 20.f ? x : log1pf(expf(x));
+}
+
+__global__ void density_act_kernel(float* sigma, const float* __restrict__ f, const int32_t* __restrict__ idx,
+                                   const int32_t* count, int64_t n, int mode, float offset) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t cnt = *count < n ? *count : n;
+    if (i >= cnt) return;
+    float x = f[i];
+    sigma[idx[i]] = mode == 0 ? relu_f(x) : softplus_f(x + offset);
+}
+
+__global__ void density_act_bwd_kernel(float* df, const float* __restrict__ ds, const float* __restrict__ f,
+                                       const int32_t* __restrict__ idx, const int32_t* count, int64_t n, int mode,
+                                       float offset) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t cnt = *count < n ? *count : n;
+    if (i >= cnt) return;
+    float x = f[i];
+    float g = ds[idx[i]];
+    if (mode == 0) df[i] = x > 0.f ? g : 0.f;
+    else {
+        float y = x + offset;
+        df[i] = y > 20.f ? g : g * sigmoid_f(y);
+    }
+}
+
+int check_grid(const srf_vm_grid* g, bool need) {
+    if (!g) return SRF_ERR_NULL;
+    for (int i = 0; i < 3; ++i) {
+        if (need && (!g->planes[i] || !g->lines[i])) return SRF_ERR_NULL;
+        if (g->res[i] < 1 || g->n_comp[i] < 0 || g->n_comp[i] > 1024) return SRF_ERR_SHAPE;
+        if ((g->n_comp[i] & 3) == 0 && (!aligned16(g->planes[i]) || !aligned16(g->lines[i]))) return SRF_ERR_ALIGN;
+    }
+    return SRF_OK;
+}
+
+}  // namespace
+}  // namespace srf
+
+using namespace srf;
+
+extern "C" int srf_vm_density_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features,
+                                      void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if (!pts || !features) return SRF_ERR_NULL;
+    if (n_pts < 0) return SRF_ERR_SHAPE;
+    if (n_pts == 0) return SRF_OK;
+    density_fwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, features);
+    return launch_status();
+}
+
+extern "C" int srf_vm_density_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                       int64_t n_pts, const float* d_features, void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if ((st = check_grid(grad_grid, true))) return st;
+    if (!pts || !d_features) return SRF_ERR_NULL;
+    if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, 1, 0);
+    return launch_status();
+}
+
+extern "C" int srf_vm_color_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features,
+                                    void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if (!pts || !features) return SRF_ERR_NULL;
+    if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
+    color_fwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, ld, features);
+    return launch_status();
+}
+
+extern "C" int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                     int64_t n_pts, const float* d_features, void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if ((st = check_grid(grad_grid, true))) return st;
+    if (!pts || !d_features) return SRF_ERR_NULL;
+    if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
+    vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, ld, 1);
+    return launch_status();
+}
+
+extern "C" int srf_tensorf_sample_mask(const float* rays_o, const float* rays_d, const float* z, int n_rays,
+                                       int n_samples, const float* bbox, const float* alpha_volume, int vol_d,
+                                       int vol_h, int vol_w, const float* alpha_bbox, float* pts_norm, uint8_t* mask,
+                                       void* stream) {
+    if (!rays_o || !rays_d || !z || !bbox || !pts_norm || !mask) return SRF_ERR_NULL;
+    if (alpha_volume && !alpha_bbox) return SRF_ERR_NULL;
+    if (n_rays < 0 || n_samples < 1) return SRF_ERR_SHAPE;
+    if (alpha_volume && (vol_d < 1 || vol_h < 1 || vol_w < 1)) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    Box b{{bbox[0], bbox[1], bbox[2]}, {bbox[3], bbox[4], bbox[5]}};
+    Box ab = b;
+    if (alpha_bbox) ab = Box{{alpha_bbox[0], alpha_bbox[1], alpha_bbox[2]}, {alpha_bbox[3], alpha_bbox[4], alpha_bbox[5]}};
+    int64_t tot = int64_t(n_rays) * n_samples;
+    sample_mask_kernel<<<grid_1d(tot, 256), 256, 0, as_stream(stream)>>>(rays_o, rays_d, z, n_rays, n_samples, b,
+                                                                        alpha_volume, vol_d, vol_h, vol_w, ab,
+                                                                        pts_norm, mask);
+    return launch_status();
+}
+
+extern "C" int srf_alpha_mask_query(const float* alpha_volume, int vol_d, int vol_h, int vol_w, const float* pts_norm,
+                                    int64_t n_pts, uint8_t* out, void* stream) {
+    if (!alpha_volume || !pts_norm || !out) return SRF_ERR_NULL;
+    if (vol_d < 1 || vol_h < 1 || vol_w < 1 || n_pts < 0) return SRF_ERR_SHAPE;
+    if (n_pts == 0) return SRF_OK;
+    alpha_query_kernel<<<grid_1d(n_pts, 256), 256, 0, as_stream(stream)>>>(alpha_volume, vol_d, vol_h, vol_w,
+                                                                          pts_norm, n_pts, out);
+    return launch_status();
+}
+
+extern "C" size_t srf_compact_workspace_size(int64_t n) {
+    if (n < 0) return 0;
+    return size_t((n + kCompactBlock - 1) / kCompactBlock + 1) * sizeof(int);
+}
+
+extern "C" int srf_compact(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* count_dev, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+    if (!mask || !idx || !count_dev) return SRF_ERR_NULL;
+    if (n < 0 || n > 0x7fffffff) return SRF_ERR_SHAPE;
+    cudaStream_t s = as_stream(stream);
+    if (n == 0) {
+        cudaError_t e = cudaMemsetAsync(count_dev, 0, sizeof(int32_t), s);
+        return e == cudaSuccess ? SRF_OK : SRF_ERR_CUDA;
+    }
+    if (!workspace || workspace_bytes < srf_compact_workspace_size(n)) return SRF_ERR_WORKSPACE;
+    int nb = int((n + kCompactBlock - 1) / kCompactBlock);
+    int* counts = static_cast<int*>(workspace);
+    count_kernel<<<nb, kCompactBlock, 0, s>>>(mask, n, counts);
+    int st = launch_status();
+    if (st) return st;
+    scan_counts_kernel<<<1, 1024, 0, s>>>(counts, nb, count_dev);
+    if ((st = launch_status())) return st;
+    write_idx_kernel<<<nb, kCompactBlock, 0, s>>>(mask, n, counts, idx);
+    return launch_status();
+}
+
+extern "C" int srf_threshold_mask(const float* x, int64_t n, float threshold, uint8_t* mask, void* stream) {
+    if (!x || !mask) return SRF_ERR_NULL;
+    if (n < 0) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    threshold_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(x, n, threshold, mask);
+    return launch_status();
+}
+
+extern "C" int srf_gather_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
+                               int cols, int src_row_div, void* stream) {
+    if (!dst || !src || !idx || !count_dev) return SRF_ERR_NULL;
+    if (n < 0 || cols < 1 || src_row_div < 1) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    gather_rows_kernel<<<grid_1d(n * cols, 256), 256, 0, as_stream(stream)>>>(dst, src, idx, count_dev, n, cols,
+                                                                              src_row_div);
+    return launch_status();
+}
+
+extern "C" int srf_scatter_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
+                                int cols, void* stream) {
+    if (!dst || !src || !idx || !count_dev) return SRF_ERR_NULL;
+    if (n < 0 || cols < 1) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    scatter_rows_kernel<<<grid_1d(n * cols, 256), 256, 0, as_stream(stream)>>>(dst, src, idx, count_dev, n, cols);
+    return launch_status();
+}
+
+extern "C" int srf_density_activation(float* sigma_dense, const float* features, const int32_t* idx,
+                                      const int32_t* count_dev, int64_t n, int mode, float offset, void* stream) {
+    if (!sigma_dense || !features || !idx || !count_dev) return SRF_ERR_NULL;
+    if (n < 0 || mode < 0 || mode > 1) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    density_act_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(sigma_dense, features, idx, count_dev, n, mode,
+                                                                      offset);
+    return launch_status();
+}
+
+extern "C" int srf_density_activation_backward(float* d_features, const float* d_sigma_dense, const float* features,
+                                               const int32_t* idx, const int32_t* count_dev, int64_t n, int mode,
+                                               float offset, void* stream) {
+    if (!d_features || !d_sigma_dense || !features || !idx || !count_dev) return SRF_ERR_NULL;
+    if (n < 0 || mode < 0 || mode > 1) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    density_act_bwd_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(d_features, d_sigma_dense, features, idx,
+                                                                          count_dev, n, mode, offset);
+    return launch_status();
+}

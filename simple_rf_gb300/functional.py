@@ -1,0 +1,311 @@
+"""Torch-facing operators over the srf_gb300 C ABI.
+
+Each operator allocates its outputs (and any workspace) with torch's caching
+allocator, passes raw device pointers and the current CUDA stream to the C ABI,
+and raises ``RuntimeError`` on a non-zero status.  Differentiable operators are
+``torch.autograd.Function``s whose backward calls the hand-written adjoint
+kernels.  Inputs must be contiguous float32 CUDA tensors; nothing here runs on
+the CPU.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import call
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(t=None):
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _require(t, name, shape=None, dtype=torch.float32):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f'{name} must be a tensor')
+    if not t.is_cuda:
+        raise RuntimeError(f'{name} must be a CUDA tensor (the srf_gb300 kernels have no CPU path)')
+    if t.dtype != dtype:
+        raise TypeError(f'{name} must be {dtype}, got {t.dtype}')
+    if not t.is_contiguous():
+        raise RuntimeError(f'{name} must be contiguous')
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise RuntimeError(f'{name} has shape {tuple(t.shape)}, expected {tuple(shape)}')
+    return t
+
+
+# ---------------------------------------------------------------- sampling --
+
+def stratified_z(n_rays, n_samples, near, far, u=None, lindisp=False, device='cuda'):
+    """SimpleNeRF17.py:330-358 (u: (N,S) uniforms, None = no jitter)."""
+    z = torch.empty(n_rays, n_samples, device=device)
+    if u is not None:
+        _require(u, 'u', (n_rays, n_samples))
+    call('srf_stratified_z', _ptr(z), _ptr(u), n_rays, n_samples, float(near), float(far), int(lindisp), _stream())
+    return z
+
+
+def sample_pdf(bins, weights, n_samples, u=None):
+    """SimpleNeRF17.py:384-417."""
+    n, nb = bins.shape
+    _require(bins, 'bins')
+    _require(weights, 'weights', (n, nb - 1))
+    if u is not None:
+        _require(u, 'u', (n, n_samples))
+    out = torch.empty(n, n_samples, device=bins.device)
+    call('srf_sample_pdf', _ptr(out), _ptr(bins), _ptr(weights), _ptr(u), n, nb, n_samples, _stream())
+    return out
+
+
+def fine_z(z_coarse, weights_coarse, n_fine, u=None):
+    """SimpleNeRF17.py:360-371: sorted [z_coarse, pdf samples] (no gradient)."""
+    n, nc = z_coarse.shape
+    _require(z_coarse, 'z_coarse')
+    weights_coarse = weights_coarse.detach().contiguous()
+    _require(weights_coarse, 'weights_coarse', (n, nc))
+    if u is not None:
+        _require(u, 'u', (n, n_fine))
+    out = torch.empty(n, nc + n_fine, device=z_coarse.device)
+    call('srf_fine_z', _ptr(out), _ptr(z_coarse), _ptr(weights_coarse), _ptr(u), n, nc, n_fine, _stream())
+    return out
+
+
+def aabb_z(rays_o, rays_d, n_samples, bbox, near, far, step_size, u=None):
+    """SimpleTensoRF09.py:388-400."""
+    n = rays_o.shape[0]
+    _require(rays_o, 'rays_o', (n, 3))
+    _require(rays_d, 'rays_d', (n, 3))
+    if u is not None:
+        u = u.reshape(n).contiguous()
+        _require(u, 'u', (n,))
+    z = torch.empty(n, n_samples, device=rays_o.device)
+    bb = _lib.host_floats([float(v) for v in torch.as_tensor(bbox).reshape(-1).tolist()])
+    call('srf_aabb_z', _ptr(z), _ptr(rays_o), _ptr(rays_d), _ptr(u), n, n_samples, bb, float(near), float(far),
+         float(step_size), _stream())
+    return z
+
+
+def ndc_rays(rays_o, rays_d, fx, fy, height, width, near):
+    """CommonUtils04.py:120-149: NDC rays and view directions."""
+    n = rays_o.shape[0]
+    _require(rays_o, 'rays_o', (n, 3))
+    _require(rays_d, 'rays_d', (n, 3))
+    _require(fx, 'fx', (n,))
+    _require(fy, 'fy', (n,))
+    o = torch.empty_like(rays_o)
+    d = torch.empty_like(rays_d)
+    call('srf_ndc_rays', _ptr(rays_o), _ptr(rays_d), _ptr(fx), _ptr(fy), n, int(height), int(width), float(near),
+         _ptr(o), _ptr(d), None, _stream())
+    return o, d
+
+
+def view_dirs(rays_d):
+    """CommonUtils04.py:147-149."""
+    n = rays_d.shape[0]
+    _require(rays_d, 'rays_d', (n, 3))
+    out = torch.empty_like(rays_d)
+    call('srf_ndc_rays', None, _ptr(rays_d), None, None, n, 1, 1, 0.0, None, None, _ptr(out), _stream())
+    return out
+
+
+def positional_encoding(x, degree):
+    """SimpleNeRF17.py:581-613 on (M, dims) rows."""
+    m, dims = x.shape
+    _require(x, 'x')
+    out = torch.empty(m, dims * (2 * degree + 1), device=x.device)
+    call('srf_positional_encoding', _ptr(out), out.shape[1], _ptr(x), m, dims, degree, _stream())
+    return out
+
+
+# ---------------------------------------------------------------- NeRF MLP --
+
+class MlpSpec:
+    """C descriptor of one reference MLP plus its parameter order."""
+
+    def __init__(self, points_net_depth=8, points_net_width=256, views_net_depth=1, views_net_width=128,
+                 points_pe_degree=10, views_pe_degree=4, use_view_dirs=True, view_dependent_rgb=True,
+                 points_sigma_pe_degree=None, skip_layer=4):
+        self.desc = _lib.NerfMlpDesc(points_net_depth, points_net_width, views_net_depth, views_net_width,
+                                     points_pe_degree, views_pe_degree,
+                                     -1 if points_sigma_pe_degree is None else points_sigma_pe_degree,
+                                     int(use_view_dirs), int(view_dependent_rgb), skip_layer)
+        self.use_view_dirs = bool(use_view_dirs)
+        lib = _lib.load()
+        n = lib.srf_nerf_mlp_num_params(ctypes.byref(self.desc))
+        if n <= 0:
+            raise RuntimeError('invalid MLP descriptor')
+        self.param_names = []
+        self.param_numel = []
+        buf = ctypes.create_string_buffer(128)
+        numel = ctypes.c_int64()
+        for i in range(n):
+            _lib.check(lib.srf_nerf_mlp_param_info(ctypes.byref(self.desc), i, buf, 128, ctypes.byref(numel)),
+                       'srf_nerf_mlp_param_info')
+            self.param_names.append(buf.value.decode())
+            self.param_numel.append(numel.value)
+
+    @classmethod
+    def from_config(cls, c):
+        """From a reference MLP config dict (NerfLlffTrainerTester10.py:296-370 form)."""
+        if c.get('predict_visibility', False):
+            raise NotImplementedError('predict_visibility is not supported by the srf_gb300 MLP')
+        return cls(c['points_net_depth'], c['points_net_width'], c['views_net_depth'], c['views_net_width'],
+                   c['points_positional_encoding_degree'], c.get('views_positional_encoding_degree', 0),
+                   c['use_view_dirs'], c['view_dependent_rgb'], c.get('points_sigma_positional_encoding_degree'))
+
+    def workspace_bytes(self, m, precision, for_backward):
+        lib = _lib.load()
+        return lib.srf_nerf_mlp_workspace_size(ctypes.byref(self.desc), m, precision, int(for_backward))
+
+
+def _ptr_array(tensors):
+    arr = (ctypes.c_void_p * len(tensors))()
+    for i, t in enumerate(tensors):
+        arr[i] = t.data_ptr()
+    return arr
+
+
+class NerfMlpFunction(torch.autograd.Function):
+    """MLP.forward (SimpleNeRF17.py:696-785) with the hand-written backward."""
+
+    @staticmethod
+    def forward(ctx, spec, precision, pts, dirs, dir_div, noise, *params):
+        m = pts.shape[0]
+        _require(pts, 'pts', (m, 3))
+        if spec.use_view_dirs:
+            _require(dirs, 'dirs')
+        if noise is not None:
+            _require(noise, 'noise', (m,))
+        params = [p.detach().contiguous() for p in params]
+        need_grad = any(ctx.needs_input_grad[6:])
+        ws = torch.empty(max(spec.workspace_bytes(m, precision, need_grad), 1), dtype=torch.uint8,
+                         device=pts.device)
+        sigma = torch.empty(m, device=pts.device)
+        rgb = torch.empty(m, 3, device=pts.device)
+        call('srf_nerf_mlp_forward', ctypes.byref(spec.desc), _ptr_array(params), _ptr(pts), _ptr(dirs),
+             int(dir_div), m, _ptr(noise), _ptr(sigma), _ptr(rgb), precision, int(need_grad), _ptr(ws),
+             ws.numel(), _stream())
+        ctx.spec, ctx.precision, ctx.dir_div, ctx.m = spec, precision, dir_div, m
+        ctx.ws = ws if need_grad else None
+        ctx.params = params
+        ctx.set_materialize_grads(True)
+        return sigma, rgb
+
+    @staticmethod
+    def backward(ctx, dsigma, drgb):
+        grads = [torch.empty_like(p) for p in ctx.params]
+        dsigma = dsigma.contiguous()
+        drgb = drgb.contiguous()
+        call('srf_nerf_mlp_backward', ctypes.byref(ctx.spec.desc), _ptr_array(ctx.params), _ptr(dsigma), _ptr(drgb),
+             int(ctx.dir_div), ctx.m, _ptr_array(grads), 0, ctx.precision, _ptr(ctx.ws), ctx.ws.numel(), _stream())
+        ctx.ws = None
+        return (None, None, None, None, None, None) + tuple(grads)
+
+
+# -------------------------------------------------------------- compositing --
+
+_COMPOSITE_OUT = ('rgb', 'acc', 'depth', 'depth_var', 'alpha', 'visibility', 'weights', 'depth_ndc', 'depth_var_ndc')
+
+
+class CompositeFunction(torch.autograd.Function):
+    """volume_rendering (SimpleNeRF17.py:486-539) / get_volume_rendering_weights +
+    volume_render (SimpleTensoRF09.py:767-819); the adjoint is a reverse scan."""
+
+    @staticmethod
+    def forward(ctx, sigma, rgb, z, rays_d, rays_o, rays_d_ndc, flags, distance_scale, white_per_ray):
+        n, s = sigma.shape
+        _require(sigma, 'sigma', (n, s))
+        _require(rgb, 'rgb', (n, s, 3))
+        _require(z, 'z', (n, s))
+        _require(rays_d, 'rays_d', (n, 3))
+        ndc = bool(flags & _lib.SRF_COMPOSITE_NDC)
+        dev = sigma.device
+        out = dict.fromkeys(_COMPOSITE_OUT)
+        out['rgb'] = torch.empty(n, 3, device=dev)
+        for k in ('acc', 'depth', 'depth_var'):
+            out[k] = torch.empty(n, device=dev)
+        for k in ('alpha', 'visibility', 'weights'):
+            out[k] = torch.empty(n, s, device=dev)
+        if ndc:
+            out['depth_ndc'] = torch.empty(n, device=dev)
+            out['depth_var_ndc'] = torch.empty(n, device=dev)
+        a = _lib.CompositeArgs()
+        a.n_rays, a.n_samples, a.flags, a.distance_scale = n, s, int(flags), float(distance_scale)
+        a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), rays_d.data_ptr()
+        if ndc:
+            a.rays_o, a.rays_d_ndc = rays_o.data_ptr(), rays_d_ndc.data_ptr()
+        if white_per_ray is not None:
+            a.white_per_ray = white_per_ray.data_ptr()
+        for k in _COMPOSITE_OUT:
+            if out[k] is not None:
+                setattr(a, 'rgb_map' if k == 'rgb' else k, out[k].data_ptr())
+        call('srf_composite_forward', ctypes.byref(a), _stream())
+        ctx.save_for_backward(sigma, rgb, z, rays_d, rays_o, rays_d_ndc, white_per_ray)
+        ctx.flags, ctx.ds = int(flags), float(distance_scale)
+        ctx.set_materialize_grads(False)
+        return tuple(out[k] if out[k] is not None else torch.empty(0, device=dev) for k in _COMPOSITE_OUT)
+
+    @staticmethod
+    def backward(ctx, g_rgb, g_acc, g_depth, g_depth_var, g_alpha, g_vis, g_weights, g_depth_ndc, g_depth_var_ndc):
+        sigma, rgb, z, rays_d, rays_o, rays_d_ndc, white = ctx.saved_tensors
+        if (g_alpha is not None and bool(g_alpha.any())) or (g_vis is not None and bool(g_vis.any())):
+            raise NotImplementedError('gradients through alpha/visibility outputs are not supported')
+        n, s = sigma.shape
+        a = _lib.CompositeArgs()
+        a.n_rays, a.n_samples, a.flags, a.distance_scale = n, s, ctx.flags, ctx.ds
+        a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), rays_d.data_ptr()
+        if ctx.flags & _lib.SRF_COMPOSITE_NDC:
+            a.rays_o, a.rays_d_ndc = rays_o.data_ptr(), rays_d_ndc.data_ptr()
+        if white is not None:
+            a.white_per_ray = white.data_ptr()
+        keep = []
+        for name, g in (('g_rgb', g_rgb), ('g_acc', g_acc), ('g_depth', g_depth), ('g_depth_var', g_depth_var),
+                        ('g_weights', g_weights), ('g_depth_ndc', g_depth_ndc),
+                        ('g_depth_var_ndc', g_depth_var_ndc)):
+            if g is not None and g.numel() > 0:
+                g = g.contiguous()
+                keep.append(g)
+                setattr(a, name, g.data_ptr())
+        d_sigma = torch.empty_like(sigma)
+        d_rgb = torch.empty_like(rgb)
+        a.d_sigma, a.d_rgb = d_sigma.data_ptr(), d_rgb.data_ptr()
+        call('srf_composite_backward', ctypes.byref(a), _stream())
+        return d_sigma, d_rgb, None, None, None, None, None, None, None
+
+
+def adam_step(param, grad, exp_avg, exp_avg_sq, *, lr, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0, step):
+    """In-place fused Adam update (torch.optim.Adam semantics)."""
+    for name, x in (('param', param), ('grad', grad), ('exp_avg', exp_avg), ('exp_avg_sq', exp_avg_sq)):
+        _require(x, name, param.shape)
+    call('srf_adam_step', _ptr(param), _ptr(grad), _ptr(exp_avg), _ptr(exp_avg_sq), param.numel(), float(lr),
+         float(beta1), float(beta2), float(eps), float(weight_decay), int(step), _stream())
+
+
+def rgb_depth_loss(rgb, target_rgb, depth, target_depth, depth_mask, n_depth_rays, depth_weight, loss=None):
+    """Loss of one net's outputs and its gradients w.r.t. rgb (N,3) and depth (N,)."""
+    n = rgb.shape[0]
+    if loss is None:
+        loss = torch.zeros(1, device=rgb.device)
+    g_rgb = torch.empty_like(rgb)
+    g_depth = torch.empty_like(depth)
+    call('srf_rgb_depth_loss', _ptr(rgb), _ptr(target_rgb), _ptr(depth), _ptr(target_depth), _ptr(depth_mask), n,
+         int(n_depth_rays), float(depth_weight), _ptr(loss), _ptr(g_rgb), _ptr(g_depth), _stream())
+    return loss, g_rgb, g_depth
+
+
+def composite(sigma, rgb, z, rays_d, *, ndc=False, rays_o=None, rays_d_ndc=None, white_bkgd=False,
+              distance_scale=1.0, white_per_ray=None):
+    """Returns the reference's volume-rendering dict (keys as SimpleNeRF17.py:521-533)."""
+    flags = (_lib.SRF_COMPOSITE_NDC if ndc else 0) | (_lib.SRF_COMPOSITE_WHITE_BKGD if white_bkgd else 0)
+    if white_per_ray is not None:
+        white_per_ray = white_per_ray.to(torch.uint8).contiguous()
+    outs = CompositeFunction.apply(sigma.contiguous(), rgb.contiguous(), z.contiguous(), rays_d.contiguous(),
+                                   None if rays_o is None else rays_o.contiguous(),
+                                   None if rays_d_ndc is None else rays_d_ndc.contiguous(), flags, distance_scale,
+                                   white_per_ray)
+    d = dict(zip(_COMPOSITE_OUT, outs))
+    if not ndc:
+        del d['depth_ndc'], d['depth_var_ndc']
+    return d

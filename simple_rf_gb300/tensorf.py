@@ -1,0 +1,173 @@
+"""TensoRF VM operators over the srf_gb300 C ABI (SimpleTensoRF09.py:1126-1421).
+
+VM planes/lines keep the reference's logical shapes ``(1, R, H, W)`` /
+``(1, R, L, 1)`` but live in ``torch.channels_last`` memory, i.e. physically
+``(H, W, R)`` / ``(L, R)``: one bilinear corner is R contiguous floats.  The
+TV loss, upsampling, shrinking and Adam of the reference keep working on the
+logical view.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call
+from .functional import _ptr, _require, _stream
+
+
+def to_channels_last(t):
+    """(1,R,H,W) tensor in the physical (H,W,R) layout the VM kernels read."""
+    return t.contiguous(memory_format=torch.channels_last)
+
+
+def _is_cl(t):
+    return t.dim() == 4 and t.is_contiguous(memory_format=torch.channels_last)
+
+
+class VmGridTensors:
+    """Three plane/line pairs (one VM tensor), as torch tensors."""
+
+    def __init__(self, planes, lines, res):
+        self.planes = list(planes)
+        self.lines = list(lines)
+        self.res = [int(r) for r in res]
+
+    @classmethod
+    def from_numpy(cls, planes, lines, res, device):
+        pl = [to_channels_last(torch.from_numpy(np.ascontiguousarray(p)).to(device)[None]) for p in planes]
+        ln = [to_channels_last(torch.from_numpy(np.ascontiguousarray(l)).to(device)[None]) for l in lines]
+        return cls(pl, ln, res)
+
+    def requires_grad_(self, flag=True):
+        for x in self.planes + self.lines:
+            x.requires_grad_(flag)
+        return self
+
+    def tensors(self):
+        return self.planes + self.lines
+
+    def plane_grad_numpy(self, i):
+        return self.planes[i].grad[0].detach().cpu().numpy()
+
+    def line_grad_numpy(self, i):
+        return self.lines[i].grad[0].detach().cpu().numpy()
+
+
+def _grid_struct(res, planes, lines):
+    g = _lib.VmGrid()
+    for i in range(3):
+        g.res[i] = res[i]
+        g.n_comp[i] = planes[i].shape[1]
+        if not (_is_cl(planes[i]) and _is_cl(lines[i])):
+            raise RuntimeError('VM planes/lines must be channels_last (see to_channels_last)')
+        if planes[i].dtype != torch.float32 or not planes[i].is_cuda:
+            raise RuntimeError('VM planes/lines must be float32 CUDA tensors')
+        g.planes[i] = planes[i].data_ptr()
+        g.lines[i] = lines[i].data_ptr()
+    return g
+
+
+class _VmFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, kind, res, pts, *tensors):
+        planes, lines = list(tensors[:3]), list(tensors[3:])
+        g = _grid_struct(res, planes, lines)
+        p = pts.shape[0]
+        _require(pts, 'pts', (p, 3))
+        if kind == 'density':
+            out = torch.empty(p, device=pts.device)
+            call('srf_vm_density_forward', ctypes.byref(g), _ptr(pts), p, _ptr(out), _stream())
+        else:
+            out = torch.empty(p, sum(x.shape[1] for x in planes), device=pts.device)
+            call('srf_vm_color_forward', ctypes.byref(g), _ptr(pts), p, _ptr(out), _stream())
+        ctx.kind, ctx.res = kind, res
+        ctx.save_for_backward(pts, *tensors)
+        return out
+
+    @staticmethod
+    def backward(ctx, dout):
+        pts, *tensors = ctx.saved_tensors
+        planes, lines = tensors[:3], tensors[3:]
+        grads = [torch.zeros_like(x) for x in tensors]
+        g = _grid_struct(ctx.res, planes, lines)
+        gg = _grid_struct(ctx.res, grads[:3], grads[3:])
+        dout = dout.contiguous()
+        name = 'srf_vm_density_backward' if ctx.kind == 'density' else 'srf_vm_color_backward'
+        call(name, ctypes.byref(gg), ctypes.byref(g), _ptr(pts), pts.shape[0], _ptr(dout), _stream())
+        return (None, None, None) + tuple(grads)
+
+
+def vm_density(grid, pts):
+    """Density features sum_i sum_r plane_i[r] * line_i[r] (SimpleTensoRF09.py:1224-1236)."""
+    return _VmFunction.apply('density', grid.res, pts.contiguous(), *grid.tensors())
+
+
+def vm_color(grid, pts):
+    """Colour features (P, sum R_i) = concat_i plane_i * line_i (SimpleTensoRF09.py:1252-1262)."""
+    return _VmFunction.apply('color', grid.res, pts.contiguous(), *grid.tensors())
+
+
+def alpha_mask_query(volume, pts_norm):
+    """AlphaGridMask.sample_alpha(...) > 0 on normalised points (SimpleTensoRF09.py:1342-1349)."""
+    vol = volume.reshape(volume.shape[-3:]).contiguous()
+    _require(vol, 'alpha_volume')
+    p = pts_norm.shape[0]
+    _require(pts_norm, 'pts_norm', (p, 3))
+    out = torch.empty(p, dtype=torch.uint8, device=pts_norm.device)
+    d, h, w = vol.shape
+    call('srf_alpha_mask_query', _ptr(vol), d, h, w, _ptr(pts_norm), p, _ptr(out), _stream())
+    return out
+
+
+def compact(mask):
+    """Ascending indices of nonzero mask entries; returns (idx (n,), count (1,) device int32)."""
+    mask = mask.reshape(-1).contiguous()
+    _require(mask, 'mask', dtype=torch.uint8)
+    n = mask.numel()
+    idx = torch.empty(max(n, 1), dtype=torch.int32, device=mask.device)
+    cnt = torch.empty(1, dtype=torch.int32, device=mask.device)
+    lib = _lib.load()
+    ws = torch.empty(max(lib.srf_compact_workspace_size(n), 4), dtype=torch.uint8, device=mask.device)
+    call('srf_compact', _ptr(mask), n, _ptr(idx), _ptr(cnt), _ptr(ws), ws.numel(), _stream())
+    return idx, cnt
+
+
+class _LinearFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, w, b, act, rows_dev):
+        rows, k = x.shape
+        nn_ = w.shape[0]
+        _require(x, 'x')
+        _require(w, 'weight', (nn_, k))
+        if b is not None:
+            _require(b, 'bias', (nn_,))
+        y = torch.empty(rows, nn_, device=x.device)
+        call('srf_linear_forward', _ptr(y), nn_, _ptr(x), k, _ptr(w), _ptr(b), rows, _ptr(rows_dev), nn_, k, act,
+             _stream())
+        ctx.act = act
+        ctx.has_b = b is not None
+        ctx.save_for_backward(x, w, y, rows_dev)
+        return y
+
+    @staticmethod
+    def backward(ctx, gy):
+        x, w, y, rows_dev = ctx.saved_tensors
+        rows, k = x.shape
+        nn_ = w.shape[0]
+        gy = gy.contiguous()
+        dx = torch.empty_like(x) if ctx.needs_input_grad[0] else None
+        dw = torch.empty_like(w) if ctx.needs_input_grad[1] else None
+        db = torch.empty(nn_, device=x.device) if (ctx.has_b and ctx.needs_input_grad[2]) else None
+        dz = torch.empty_like(y)
+        if dx is not None and rows_dev is not None:
+            dx.zero_()
+        call('srf_linear_backward', _ptr(dx), k, _ptr(dw), _ptr(db), _ptr(gy), nn_, _ptr(y), nn_, _ptr(x), k, _ptr(w),
+             _ptr(dz), rows, _ptr(rows_dev), nn_, k, ctx.act, 0, _stream())
+        return dx, dw, db, None, None
+
+
+def linear(x, weight, bias=None, act=_lib.SRF_ACT_NONE, rows_dev=None):
+    """act(x @ weight.T + bias) on the first ``*rows_dev`` rows (all rows when None)."""
+    return _LinearFunction.apply(x.contiguous(), weight.contiguous(), None if bias is None else bias.contiguous(), act,
+                                 rows_dev)

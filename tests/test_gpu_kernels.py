@@ -1,0 +1,301 @@
+"""CUDA kernels (through the C ABI) against the numpy oracle, kernel by kernel.
+
+Tolerances (FP32 plain path): 1e-5 relative with a small absolute floor where a
+value can be near zero; integer/mask/index outputs bit-exact; inverse-CDF
+samples in CDF space (see tests/test_oracle_golden.py::close_pdf).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import nerf as on
+from oracle import tensorf as ot
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+def t(x):
+    return torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(DEV)
+
+
+def n(x):
+    return x.detach().cpu().numpy()
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def cdf_of(bins, weights, x):
+    w = weights.astype(np.float64) + 1e-5
+    cdf = np.concatenate([np.zeros((w.shape[0], 1)), np.cumsum(w / w.sum(-1, keepdims=True), -1)], -1)
+    return np.stack([np.interp(x[r], bins[r].astype(np.float64), cdf[r]) for r in range(x.shape[0])])
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from simple_rf_gb300 import build as b
+    b.build()
+    import simple_rf_gb300.functional  # noqa: F401
+    assert torch.cuda.is_available(), 'GPU tests need CUDA'
+
+
+def test_stratified_z_bit_exact():
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(0)
+    for n_rays, s, near, far in ((37, 64, 2.0, 6.0), (5, 1039, 0.0, 1.0), (3, 2, 2.0, 6.0)):
+        u = rng.random((n_rays, s), dtype=np.float32)
+        z = F.stratified_z(n_rays, s, near, far, t(u))
+        assert np.array_equal(n(z), on.stratified_z(near, far, n_rays, s, u))
+        z0 = F.stratified_z(n_rays, s, near, far, None)
+        assert np.array_equal(n(z0), on.stratified_z(near, far, n_rays, s, None))
+
+
+def test_sample_pdf_and_fine_z():
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(1)
+    nr, sc, sf = 300, 64, 128
+    zc = on.stratified_z(2.0, 6.0, nr, sc, rng.random((nr, sc), dtype=np.float32))
+    w = (rng.random((nr, sc), dtype=np.float32) ** 4).astype(np.float32)
+    w[0] = 0
+    w[1, :] = 0
+    w[1, 30] = 5
+    w[2, ::2] = 0
+    u = rng.random((nr, sf), dtype=np.float32)
+    u[3, :3] = [0.0, 1.0, 0.5]
+    mids = np.float32(.5) * (zc[:, 1:] + zc[:, :-1])
+    for uu in (u, None):
+        got = n(F.sample_pdf(t(mids), t(w[:, 1:-1]), sf, None if uu is None else t(uu)))
+        ref = on.sample_pdf(mids, w[:, 1:-1], sf, uu)
+        assert np.abs(cdf_of(mids, w[:, 1:-1], got) - cdf_of(mids, w[:, 1:-1], ref)).max() < 1e-5
+        assert np.mean(~np.isclose(got, ref, rtol=1e-5, atol=1e-5)) < 0.01
+        zf = n(F.fine_z(t(zc), t(w), sf, None if uu is None else t(uu)))
+        zr = on.fine_z(zc, w, sf, uu)
+        assert np.all(np.diff(zf, axis=1) >= 0)
+        assert np.abs(cdf_of(mids, w[:, 1:-1], zf) - cdf_of(mids, w[:, 1:-1], zr)).max() < 1e-5
+        # every coarse depth survives the merge unchanged
+        for r in range(0, nr, 37):
+            assert np.isin(zc[r], zf[r]).all()
+
+
+def test_positional_encoding():
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(2)
+    x = (rng.standard_normal((4099, 3)) * 3).astype(np.float32)
+    for deg in (10, 4, 0):
+        got = n(F.positional_encoding(t(x), deg))
+        np.testing.assert_allclose(got, on.positional_encoding(x, deg), rtol=1e-5, atol=3e-6)
+
+
+def test_ndc_rays_and_view_dirs():
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(3)
+    nr = 513
+    o = np.zeros((nr, 3), np.float32)
+    o[:, :2] = rng.uniform(-1, 1, (nr, 2))
+    o[:, 2] = -1
+    d = np.stack([rng.uniform(-.2, .2, nr), rng.uniform(-.2, .2, nr), -rng.uniform(.8, 1.2, nr)], 1).astype(np.float32)
+    f = np.full(nr, 400.0, np.float32)
+    go, gd = F.ndc_rays(t(o), t(d), t(f), t(f), 378, 504, 1.0)
+    ro, rd = on.ndc_rays(o, d, 378, 504, f, f, 1.0)
+    np.testing.assert_allclose(n(go), ro, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(n(gd), rd, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(n(F.view_dirs(t(d))), on.view_dirs(d), rtol=1e-6, atol=1e-7)
+
+
+SPECS = {
+    'main': dict(),
+    'aug_l4_noview': dict(points_pe_degree=4, use_view_dirs=False, view_dependent_rgb=False),
+    'points_aug': dict(points_sigma_pe_degree=3),
+    'narrow': dict(points_net_width=40, views_net_width=24, views_net_depth=2),
+}
+
+
+def _oracle_spec(kw):
+    return on.MlpSpec(points_net_depth=kw.get('points_net_depth', 8), points_net_width=kw.get('points_net_width', 256),
+                      views_net_depth=kw.get('views_net_depth', 1), views_net_width=kw.get('views_net_width', 128),
+                      points_pe_degree=kw.get('points_pe_degree', 10), views_pe_degree=kw.get('views_pe_degree', 4),
+                      use_view_dirs=kw.get('use_view_dirs', True), view_dependent_rgb=kw.get('view_dependent_rgb', True),
+                      points_sigma_pe_degree=kw.get('points_sigma_pe_degree'))
+
+
+@pytest.mark.parametrize('name', list(SPECS))
+def test_nerf_mlp_fp32_forward_backward(name):
+    from simple_rf_gb300 import functional as F
+    kw = SPECS[name]
+    ospec = _oracle_spec(kw)
+    spec = F.MlpSpec(**kw)
+    assert spec.param_names == list(ospec.param_shapes())
+    p = on.xavier_params(ospec, 10)
+    rng = np.random.default_rng(4)
+    div = 16
+    m = 97 * div
+    pts = rng.standard_normal((m, 3)).astype(np.float32)
+    vd = rng.standard_normal((m // div, 3)).astype(np.float32)
+    vd /= np.linalg.norm(vd, axis=1, keepdims=True)
+    params = [t(p[k]).requires_grad_(True) for k in spec.param_names]
+    sigma, rgb = F.NerfMlpFunction.apply(spec, 0, t(pts), t(vd) if spec.use_view_dirs else None, div, None, *params)
+    rs, rr, cache = on.mlp_forward(p, ospec, pts, np.repeat(vd, div, 0))
+    np.testing.assert_allclose(n(rgb), rr, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(n(sigma), rs[:, 0], rtol=1e-5, atol=1e-5 * max(1.0, float(np.abs(rs).max())))
+    cs = rng.standard_normal(m).astype(np.float32)
+    cr = rng.standard_normal((m, 3)).astype(np.float32)
+    (sigma * t(cs)).sum().add((rgb * t(cr)).sum()).backward()
+    g = on.mlp_backward(p, ospec, cache, cs[:, None], cr)
+    for k, prm in zip(spec.param_names, params):
+        assert rel_l2(n(prm.grad), g[k]) < 1e-5, (k, rel_l2(n(prm.grad), g[k]))
+
+
+@pytest.mark.parametrize('ndc', [False, True])
+def test_composite_forward_backward(ndc):
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(5)
+    nr, s = 301, 192 if not ndc else 70
+    sigma = np.maximum(rng.standard_normal((nr, s)) * 3, 0).astype(np.float32)
+    sigma[0] = 0
+    sigma[1, 10:] = 1e4
+    rgb = rng.random((nr, s, 3), dtype=np.float32)
+    kw = {}
+    if ndc:
+        o = np.zeros((nr, 3), np.float32)
+        o[:, :2] = rng.uniform(-1, 1, (nr, 2))
+        o[:, 2] = -1
+        d = np.stack([rng.uniform(-.2, .2, nr), rng.uniform(-.2, .2, nr), -rng.uniform(.8, 1.2, nr)], 1).astype(np.float32)
+        f = np.full(nr, 400.0, np.float32)
+        _, dn = on.ndc_rays(o, d, 378, 504, f, f, 1.0)
+        z = np.sort(rng.random((nr, s), dtype=np.float32), 1)
+        z[2, -1] = 1.0
+        kw = dict(ndc=True, rays_o=o, rays_d_ndc=dn.astype(np.float32))
+    else:
+        d = rng.standard_normal((nr, 3)).astype(np.float32)
+        z = (2 + 4 * np.sort(rng.random((nr, s), dtype=np.float32), 1)).astype(np.float32)
+    ref, cache = on.composite_forward(sigma, rgb, z, d, white_bkgd=True, **kw)
+    sg, rg = t(sigma).requires_grad_(True), t(rgb).requires_grad_(True)
+    got = F.composite(sg, rg, t(z), t(d), white_bkgd=True, ndc=ndc,
+                      rays_o=t(kw['rays_o']) if ndc else None, rays_d_ndc=t(kw['rays_d_ndc']) if ndc else None)
+    for k, v in ref.items():
+        scale = max(1.0, float(np.abs(v).max()))
+        np.testing.assert_allclose(n(got[k]), v, rtol=1e-5, atol=1e-6 * scale, err_msg=k)
+    cot = {k: rng.standard_normal(ref[k].shape).astype(np.float32) for k in ref if k not in ('alpha', 'visibility')}
+    loss = sum((got[k] * t(c)).sum() for k, c in cot.items())
+    loss.backward()
+    ds, dr = on.composite_backward(cache, cot)
+    assert rel_l2(n(sg.grad), ds) < 1e-5
+    assert rel_l2(n(rg.grad), dr) < 1e-6
+
+
+def _vm_grid(rng, res, comps, scale=0.3, shift=0.0):
+    planes, lines = [], []
+    for i in range(3):
+        m0, m1 = ot.MATRIX_AXES[i]
+        v = ot.VECTOR_AXES[i]
+        planes.append((rng.standard_normal((comps[i], res[m1], res[m0])) * scale + shift).astype(np.float32))
+        lines.append((rng.standard_normal((comps[i], res[v], 1)) * scale + shift).astype(np.float32))
+    return planes, lines
+
+
+@pytest.mark.parametrize('comps', [(4, 3, 2), (16, 16, 16), (48, 12, 12)])
+def test_vm_density_and_color(comps):
+    from simple_rf_gb300 import tensorf as T
+    rng = np.random.default_rng(6)
+    res = (20, 22, 24)
+    planes, lines = _vm_grid(rng, res, comps)
+    p = rng.uniform(-1.1, 1.1, (3001, 3)).astype(np.float32)
+    p[:6] = [[-1, -1, -1], [1, 1, 1], [0, 0, 0], [1, -1, 0.5], [1.0000001, 0, 0], [-1, 1, 1]]
+    grid = T.VmGridTensors.from_numpy(planes, lines, res, DEV)
+    grid.requires_grad_(True)
+    dens = T.vm_density(grid, t(p))
+    np.testing.assert_allclose(n(dens), ot.vm_density(planes, lines, p), rtol=1e-5, atol=2e-6)
+    col = T.vm_color(grid, t(p))
+    feats = ot.vm_features(planes, lines, p)
+    ref_col = np.concatenate([pc * lc for pc, lc in feats], 0).T
+    np.testing.assert_allclose(n(col), ref_col, rtol=1e-5, atol=2e-6)
+    gd = rng.standard_normal(p.shape[0]).astype(np.float32)
+    gc = rng.standard_normal(ref_col.shape).astype(np.float32)
+    ((dens * t(gd)).sum() + (col * t(gc)).sum()).backward()
+    off = 0
+    for i in range(3):
+        m0, m1 = ot.MATRIX_AXES[i]
+        v = ot.VECTOR_AXES[i]
+        pc, lc = feats[i]
+        r = comps[i]
+        dcol = gc[:, off:off + r].T
+        off += r
+        ref_gp = ot.grid_sample_2d_backward(planes[i].shape, p[:, m0], p[:, m1], gd[None] * lc + dcol * lc, np.float32)
+        ref_gl = ot.grid_sample_2d_backward(lines[i].shape, np.zeros_like(p[:, v]), p[:, v], gd[None] * pc + dcol * pc,
+                                            np.float32)
+        assert rel_l2(grid.plane_grad_numpy(i), ref_gp) < 1e-5
+        assert rel_l2(grid.line_grad_numpy(i), ref_gl) < 1e-5
+
+
+def test_alpha_mask_and_compaction():
+    from simple_rf_gb300 import tensorf as T
+    rng = np.random.default_rng(7)
+    vol = (rng.random((12, 10, 8)) < 0.3).astype(np.float32)
+    q = rng.uniform(-1.2, 1.2, (20000, 3)).astype(np.float32)
+    # grid nodes and faces: zero-weight corners must not count
+    q[:200] = np.round(q[:200] * 3.5) / 3.5
+    got = n(T.alpha_mask_query(t(vol), t(q)))
+    assert np.array_equal(got.astype(bool), ot.grid_sample_3d_positive(vol, q))
+    mask = rng.random(100003) < 0.3
+    idx, cnt = T.compact(torch.from_numpy(mask.astype(np.uint8)).to(DEV))
+    ref = np.nonzero(mask)[0]
+    assert int(cnt.item()) == ref.size
+    assert np.array_equal(n(idx)[:ref.size], ref)
+
+
+def test_linear_layer_forward_backward():
+    from simple_rf_gb300 import tensorf as T
+    rng = np.random.default_rng(8)
+    rows, k, nn_ = 1000, 150, 128
+    x = rng.standard_normal((rows, k)).astype(np.float32)
+    w = (rng.standard_normal((nn_, k)) * 0.1).astype(np.float32)
+    b = (rng.standard_normal(nn_) * 0.1).astype(np.float32)
+    for act in (0, 1, 2):
+        xt, wt, bt = t(x).requires_grad_(True), t(w).requires_grad_(True), t(b).requires_grad_(True)
+        y = T.linear(xt, wt, bt, act)
+        z = x @ w.T + b
+        ref = z if act == 0 else (np.maximum(z, 0) if act == 1 else 1 / (1 + np.exp(-z)))
+        np.testing.assert_allclose(n(y), ref, rtol=1e-5, atol=1e-5)
+        gy = rng.standard_normal(ref.shape).astype(np.float32)
+        (y * t(gy)).sum().backward()
+        dz = gy if act == 0 else (gy * (z > 0) if act == 1 else gy * ref * (1 - ref))
+        assert rel_l2(n(wt.grad), dz.T @ x) < 1e-5
+        assert rel_l2(n(bt.grad), dz.sum(0)) < 1e-5
+        assert rel_l2(n(xt.grad), dz @ w) < 1e-5
+
+
+def test_adam_matches_torch():
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(9)
+    p0 = rng.standard_normal(10007).astype(np.float32)
+    ours = t(p0)
+    ref = torch.nn.Parameter(t(p0))
+    opt = torch.optim.Adam([ref], lr=5e-4, betas=(0.9, 0.999), eps=1e-8)
+    m = torch.zeros_like(ours)
+    v = torch.zeros_like(ours)
+    for step in range(1, 6):
+        g = t(rng.standard_normal(p0.shape).astype(np.float32))
+        F.adam_step(ours, g, m, v, lr=5e-4, beta1=0.9, beta2=0.999, eps=1e-8, step=step)
+        ref.grad = g.clone()
+        opt.step()
+    np.testing.assert_allclose(n(ours), n(ref.detach()), rtol=1e-6, atol=1e-7)
+
+
+def test_loss_kernel():
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(10)
+    nr = 4096
+    rgb = rng.random((nr, 3), dtype=np.float32)
+    tr = rng.random((nr, 3), dtype=np.float32)
+    dep = rng.uniform(2, 6, nr).astype(np.float32)
+    td = rng.uniform(2, 6, nr).astype(np.float32)
+    mask = np.zeros(nr, np.float32)
+    mask[:nr // 4] = 1
+    loss, g_rgb, g_depth = F.rgb_depth_loss(t(rgb), t(tr), t(dep), t(td), t(mask).to(torch.uint8), nr // 4, 0.1)
+    ret = {'rgb_c': rgb, 'depth_c': dep}
+    ref_loss, grads = on.train_loss(ret, tr, td, mask, nets=('c',))
+    assert abs(float(loss.item()) - ref_loss) < 1e-5 * max(1, ref_loss)
+    np.testing.assert_allclose(n(g_rgb), grads['rgb_c'], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(n(g_depth), grads['depth_c'], rtol=1e-5, atol=1e-9)
