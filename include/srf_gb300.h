@@ -49,6 +49,13 @@ int srf_read_device_flag(int* flag_out, void* stream);
 /* Ray generation and sampling                                               */
 /* ------------------------------------------------------------------------ */
 
+/* World rays of pixels: pixel_id (N,3) int32 (image, x, y), intrinsics (N,3,3),
+ * extrinsics (N,4,4) camera-to-world; half_pixel adds 0.5 to x and y (the
+ * reference's mip_nerf_used flag).  Replaces CommonUtils04.get_rays_tr
+ * (src/utils/CommonUtils04.py:73-95, non-synthetic branch). */
+int srf_pixel_rays(const int32_t* pixel_id, const float* intrinsics, const float* extrinsics, int n_rays,
+                   int half_pixel, float* rays_o, float* rays_d, void* stream);
+
 /* NDC warp + view directions of world rays.
  * Replaces CommonUtils04.get_ndc_rays_tr (src/utils/CommonUtils04.py:120-138)
  * and get_view_dirs_tr (:147-149).  fx, fy per ray (N,); any output may be NULL. */

@@ -51,6 +51,7 @@ _SIGS = {
     'srf_version': (c_char_p, []),
     'srf_last_cuda_error': (c_char_p, []),
     'srf_read_device_flag': (c_int, [ctypes.POINTER(c_int), P]),
+    'srf_pixel_rays': (c_int, [P, P, P, c_int, c_int, P, P, P]),
     'srf_ndc_rays': (c_int, [P, P, P, P, c_int, c_int, c_int, c_float, P, P, P, P]),
     'srf_stratified_z': (c_int, [P, P, c_int, c_int, c_float, c_float, c_int, P]),
     'srf_sample_pdf': (c_int, [P, P, P, P, c_int, c_int, c_int, P]),

@@ -293,7 +293,7 @@ int check_args(const srf_composite_args* a, bool bwd) {
     if (!a || !a->sigma || !a->z || !a->rays_d) return SRF_ERR_NULL;
     if ((a->flags & SRF_COMPOSITE_NDC) && (!a->rays_o || !a->rays_d_ndc)) return SRF_ERR_NULL;
     if (a->n_rays < 0 || a->n_samples < 1 || a->n_samples > 16384) return SRF_ERR_SHAPE;
-    if (!a->rgb && (a->rgb_map || bwd)) return SRF_ERR_NULL;
+    if (!a->rgb) return SRF_ERR_NULL;
     if (bwd && !a->d_sigma) return SRF_ERR_NULL;
     return SRF_OK;
 }

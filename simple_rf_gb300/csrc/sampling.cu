@@ -19,7 +19,6 @@ __global__ void ndc_rays_kernel(const float* __restrict__ o, const float* __rest
                                 float* d_ndc, float* vdirs) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
-    float ox = o[3 * r], oy = o[3 * r + 1], oz = o[3 * r + 2];
     float dx = d[3 * r], dy = d[3 * r + 1], dz = d[3 * r + 2];
     if (vdirs) {
         float nrm = sqrtf(dx * dx + dy * dy + dz * dz);
@@ -28,6 +27,8 @@ __global__ void ndc_rays_kernel(const float* __restrict__ o, const float* __rest
         vdirs[3 * r + 2] = dz / nrm;
     }
     if (!o_ndc && !d_ndc) return;
+    // only reached when the host checked that o, fx and fy are non-NULL
+    float ox = o[3 * r], oy = o[3 * r + 1], oz = o[3 * r + 2];
     // CommonUtils04.py:124-137
     float t = -(near_plane + oz) / dz;
     float sx = ox + t * dx, sy = oy + t * dy, sz = oz + t * dz;
@@ -42,6 +43,36 @@ __global__ void ndc_rays_kernel(const float* __restrict__ o, const float* __rest
         d_ndc[3 * r] = ax * (dx / dz - sx / sz);
         d_ndc[3 * r + 1] = ay * (dy / dz - sy / sz);
         d_ndc[3 * r + 2] = -2.f * near_plane / sz;
+    }
+}
+
+// CommonUtils04.py:73-95 get_rays_tr (non-synthetic branch): dirs = K^-1 [x, y, 1]
+// (y and z negated), rotated by the camera-to-world matrix; origin = its translation.
+// K^-1 by the adjugate (K is a 3x3 intrinsics matrix).
+__global__ void pixel_rays_kernel(const int* __restrict__ pix, const float* __restrict__ K,
+                                  const float* __restrict__ E, int n, int half_pixel, float* o, float* d) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    float x = float(pix[3 * r + 1]), y = float(pix[3 * r + 2]);
+    if (half_pixel) {
+        x = x + 0.5f;
+        y = y + 0.5f;
+    }
+    const float* k = K + 9 * r;
+    float a = k[0], b = k[1], c = k[2], dd = k[3], e = k[4], f = k[5], g = k[6], h = k[7], i = k[8];
+    float A = e * i - f * h, B = -(dd * i - f * g), C = dd * h - e * g;
+    float det = a * A + b * B + c * C;
+    float inv[9] = {A / det, -(b * i - c * h) / det, (b * f - c * e) / det,
+                    B / det, (a * i - c * g) / det, -(a * f - c * dd) / det,
+                    C / det, -(a * h - b * g) / det, (a * e - b * dd) / det};
+    float cam[3];
+    for (int q = 0; q < 3; ++q) cam[q] = inv[3 * q] * x + inv[3 * q + 1] * y + inv[3 * q + 2];
+    cam[1] = -cam[1];
+    cam[2] = -cam[2];
+    const float* m = E + 16 * r;
+    for (int q = 0; q < 3; ++q) {
+        d[3 * r + q] = cam[0] * m[4 * q] + cam[1] * m[4 * q + 1] + cam[2] * m[4 * q + 2];
+        o[3 * r + q] = m[4 * q + 3];
     }
 }
 
@@ -231,6 +262,16 @@ extern "C" int srf_ndc_rays(const float* rays_o, const float* rays_d, const floa
     return launch_status();
 }
 
+extern "C" int srf_pixel_rays(const int32_t* pixel_id, const float* intrinsics, const float* extrinsics, int n_rays,
+                              int half_pixel, float* rays_o, float* rays_d, void* stream) {
+    if (!pixel_id || !intrinsics || !extrinsics || !rays_o || !rays_d) return SRF_ERR_NULL;
+    if (n_rays < 0) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    pixel_rays_kernel<<<grid_1d(n_rays, 256), 256, 0, as_stream(stream)>>>(pixel_id, intrinsics, extrinsics, n_rays,
+                                                                          half_pixel, rays_o, rays_d);
+    return launch_status();
+}
+
 extern "C" int srf_stratified_z(float* z, const float* u, int n_rays, int n_samples, float near_plane,
                                 float far_plane, int lindisp, void* stream) {
     if (!z) return SRF_ERR_NULL;
@@ -245,7 +286,8 @@ extern "C" int srf_stratified_z(float* z, const float* u, int n_rays, int n_samp
 extern "C" int srf_sample_pdf(float* samples, const float* bins, const float* weights, const float* u, int n_rays,
                               int n_bins, int n_samples, void* stream) {
     if (!samples || !bins || !weights) return SRF_ERR_NULL;
-    if (n_rays < 0 || n_bins < 2 || n_bins > 4096 || n_samples < 1) return SRF_ERR_SHAPE;
+    // 4 warps x (cdf + bins) x n_bins floats must fit the default 48 KB of shared memory
+    if (n_rays < 0 || n_bins < 2 || n_bins > 1536 || n_samples < 1) return SRF_ERR_SHAPE;
     if (n_rays == 0) return SRF_OK;
     const int warps = 4;
     size_t smem = size_t(warps) * 2 * n_bins * sizeof(float);

@@ -24,6 +24,10 @@ __device__ __forceinline__ Taps bilinear(float gx, float gy, int h, int w) {
     Taps t;
     float ix = (gx + 1.f) * (float(w - 1) * 0.5f);
     float iy = (gy + 1.f) * (float(h - 1) * 0.5f);
+    // far-outside coordinates only ever touch padding; clamp before the int
+    // conversion so the corner indices stay small
+    if (isfinite(ix)) ix = fminf(fmaxf(ix, -4.f), float(w) + 4.f);
+    if (isfinite(iy)) iy = fminf(fmaxf(iy, -4.f), float(h) + 4.f);
     float x0f = floorf(ix), y0f = floorf(iy);
     float fw = ix - x0f, fe = 1.f - fw;
     float fn = iy - y0f, fs = 1.f - fn;
@@ -171,6 +175,8 @@ __device__ __forceinline__ bool alpha_positive(const float* __restrict__ vol, in
     float iy = ((y + 1.f) / 2.f) * float(h - 1);
     float iz = ((z + 1.f) / 2.f) * float(d - 1);
     if (!(isfinite(ix) && isfinite(iy) && isfinite(iz))) return false;
+    // outside [-1, size] every corner is padding
+    if (ix < -1.f || iy < -1.f || iz < -1.f || ix > float(w) || iy > float(h) || iz > float(d)) return false;
     float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
     float x1 = x0 + 1.f, y1 = y0 + 1.f, z1 = z0 + 1.f;
     float wx[2] = {x1 - ix, ix - x0}, wy[2] = {y1 - iy, iy - y0}, wz[2] = {z1 - iz, iz - z0};

@@ -309,3 +309,17 @@ def composite(sigma, rgb, z, rays_d, *, ndc=False, rays_o=None, rays_d_ndc=None,
     if not ndc:
         del d['depth_ndc'], d['depth_var_ndc']
     return d
+
+
+def pixel_rays(pixel_id, intrinsics, extrinsics, half_pixel=False):
+    """CommonUtils04.py:73-95 get_rays_tr: world rays of (image, x, y) pixel ids."""
+    n = pixel_id.shape[0]
+    pid = pixel_id.to(torch.int32).contiguous()
+    k = intrinsics.float().contiguous()
+    e = extrinsics.float().contiguous()
+    _require(k, 'intrinsics', (n, 3, 3))
+    _require(e, 'extrinsics', (n, 4, 4))
+    o = torch.empty(n, 3, device=k.device)
+    d = torch.empty(n, 3, device=k.device)
+    call('srf_pixel_rays', _ptr(pid), _ptr(k), _ptr(e), n, int(half_pixel), _ptr(o), _ptr(d), _stream())
+    return o, d
