@@ -139,6 +139,25 @@ int srf_nerf_mlp_backward(const srf_nerf_mlp_desc* desc, const float* const* par
                           const float* drgb, int dir_div, int64_t m, float* const* grads, int accumulate,
                           int precision, void* workspace, size_t workspace_bytes, void* stream);
 
+/* BF16 tcgen05 dense layer (the building block of the BF16 MLP path):
+ * out[m, :n] = relu?(x0[m, :k0] . Wb^T + x1[m, :k1] . Wb'^T + bias) * (mask > 0)?
+ * where W (w_rows x ldw, BF16, row-major like nn.Linear.weight) supplies rows
+ * [w_row0, w_row0 + n) over columns [0, k0 + k1).  k0, k1 multiples of 64;
+ * n in {64, 128, 256}; BF16 pointers 16-byte aligned, leading dims multiples
+ * of 8.  colsum (n floats, optional) accumulates the column sums of the output.
+ * Replaces one torch.nn.Linear (+ReLU) of MLP.forward (src/models/SimpleNeRF17.py:729-733). */
+int srf_bf16_linear(void* out, int64_t ld_out, const void* x0, int64_t ld0, int k0, const void* x1, int64_t ld1,
+                    int k1, const void* w, int64_t ldw, int w_rows, int w_row0, const float* bias, int64_t m, int n,
+                    int relu, const void* mask, int64_t ld_mask, float* colsum, void* stream);
+/* BF16 weight gradient partials: partial[s, j, k] = sum over split s of
+ * dz[i, j] * [x0 | x1][i, k]; *splits receives the split count (sum over s
+ * gives dW).  n_dz multiple of 128, k0 + k1 <= 512 (multiples of 64).
+ * Replaces the autograd weight gradient of those nn.Linear layers. */
+size_t srf_bf16_wgrad_workspace_size(int n_dz, int k_total);
+int srf_bf16_wgrad(float* partial, size_t partial_bytes, int* splits, const void* dz, int64_t ld_dz, int n_dz,
+                   const void* x0, int64_t ld0, int k0, const void* x1, int64_t ld1, int k1, int64_t m,
+                   void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Alpha compositing                                                         */
 /* ------------------------------------------------------------------------ */

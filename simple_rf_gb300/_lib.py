@@ -66,6 +66,11 @@ _SIGS = {
                                      c_int, c_int, P, c_size_t, P]),
     'srf_nerf_mlp_backward': (c_int, [ctypes.POINTER(NerfMlpDesc), ctypes.POINTER(P), P, P, c_int, c_int64,
                                       ctypes.POINTER(P), c_int, c_int, P, c_size_t, P]),
+    'srf_bf16_linear': (c_int, [P, c_int64, P, c_int64, c_int, P, c_int64, c_int, P, c_int64, c_int, c_int, P,
+                                c_int64, c_int, c_int, P, c_int64, P, P]),
+    'srf_bf16_wgrad_workspace_size': (c_size_t, [c_int, c_int]),
+    'srf_bf16_wgrad': (c_int, [P, c_size_t, ctypes.POINTER(c_int), P, c_int64, c_int, P, c_int64, c_int, P, c_int64,
+                               c_int, c_int64, P]),
     'srf_composite_forward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
     'srf_composite_backward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
     'srf_vm_density_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),

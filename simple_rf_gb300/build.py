@@ -21,8 +21,9 @@ LIB = os.path.join(PKG, 'libsrf_gb300.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
           '-I' + os.path.join(REPO, 'include')]
-# Per-file flags: the sampling formulas must round like separate torch ops.
-EXTRA = {'sampling.cu': ['-fmad=false']}
+# Per-file flags: the sampling and compositing formulas (the NDC depth
+# conversion amplifies rounding near z = 1) must round like separate torch ops.
+EXTRA = {'sampling.cu': ['-fmad=false'], 'composite.cu': ['-fmad=false']}
 
 
 def _nvcc():

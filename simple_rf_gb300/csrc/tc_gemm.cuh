@@ -1,0 +1,431 @@
+// Persistent tcgen05 BF16 GEMM with a fused epilogue: the tensor-core form of
+// one MLP layer over a tile of 128 samples.
+//
+//   out[m, n] = epilogue( sum_k A[m, k] * B[n, k] ),  A = [A0 | A1] (two sources
+//   along K, e.g. the skip concat [PE(x), h]), B resident in shared memory.
+//
+// Warp roles (192 threads): warp 0 issues TMA loads, warp 1 allocates tensor
+// memory and issues tcgen05.mma (one thread), warps 2..5 drain the FP32
+// accumulator from tensor memory (tcgen05.ld), apply bias / ReLU / ReLU-mask /
+// rank-1 update and store BF16 rows.  Two accumulators in tensor memory let the
+// epilogue of tile t overlap the MMAs of tile t+1.  Operands are K-major with the
+// 128-byte swizzle that TMA writes (8-row x 128-byte atoms, SBO = 1024 B).
+//
+// Every mbarrier wait is bounded: on a timeout the CTA sets the device error
+// flag, stops issuing work, waits (bounded) for its own copies and MMAs, frees
+// its tensor memory and returns.
+#pragma once
+
+#include "tc_primitives.cuh"
+
+namespace srf {
+namespace tc {
+
+constexpr int kBlockM = 128;
+constexpr int kBlockK = 64;   // one 128-byte swizzle atom of BF16
+constexpr int kThreads = 192;
+constexpr uint32_t kATileBytes = kBlockM * kBlockK * 2;
+constexpr size_t kMaxSmem = 232448;
+
+struct GemmEpilogue {
+    const float* bias;              // [N] or NULL
+    int relu;                       // apply ReLU to the result
+    const __nv_bfloat16* mask;      // multiply by (mask[m, n] > 0) when non-NULL
+    int64_t ld_mask;
+    const float* r1_row;            // result += r1_row[m] * r1_col[n] (before ReLU/mask) when non-NULL
+    const float* r1_col;
+    __nv_bfloat16* out;             // [M, ld_out] BF16
+    int64_t ld_out;
+    float* colsum;                  // += column sums of the stored values (a bias gradient) when non-NULL
+    int* flag;
+};
+
+// Lane i of the warp ends with sum over the 32 lanes of v[i] (recursive halving).
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int j = 0; j < off; ++j) {
+            float send = upper ? v[j] : v[j + off];
+            float keep = upper ? v[j + off] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    return v[0];
+}
+
+struct GemmShape {
+    int64_t M;
+    int kb0, kb1;   // 64-wide K blocks from A0 and A1
+    int b_row0;     // first B row (output column 0)
+};
+
+template <int BN>
+struct SmemPlan {
+    static constexpr uint32_t kBBlockBytes = BN * kBlockK * 2;
+    // 1024 B alignment slack + 256 B of barriers + BN floats of bias + BN of column sums
+    static constexpr size_t kReserve = 1024 + 256 + BN * 8;
+    static __host__ __device__ int stages(int kb_total) {
+        size_t b = size_t(kb_total) * kBBlockBytes;
+        if (b + kReserve + 2 * kATileBytes > kMaxSmem) return 0;
+        int s = int((kMaxSmem - kReserve - b) / kATileBytes);
+        return s > 8 ? 8 : s;
+    }
+    static __host__ __device__ size_t bytes(int kb_total) {
+        return kReserve + size_t(kb_total) * kBBlockBytes + size_t(stages(kb_total)) * kATileBytes;
+    }
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
+                   const __grid_constant__ CUtensorMap tmB, GemmShape shape, GemmEpilogue ep) {
+    extern __shared__ uint8_t smem_raw[];
+    // 1024-byte alignment for the swizzle atoms
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int kb_total = shape.kb0 + shape.kb1;
+    const int stages = SmemPlan<BN>::stages(kb_total);
+    uint8_t* sB = base;
+    uint8_t* sA = sB + size_t(kb_total) * SmemPlan<BN>::kBBlockBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + size_t(stages) * kATileBytes);
+    uint64_t* full = bars;              // [stages]
+    uint64_t* empty = bars + 8;         // [stages]
+    uint64_t* acc_full = bars + 16;     // [2]
+    uint64_t* acc_empty = bars + 18;    // [2]
+    uint64_t* b_full = bars + 20;
+    uint64_t* done = bars + 21;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 22);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 23);
+    float* sbias = reinterpret_cast<float*>(bars + 24);   // BN floats
+    float* scol = sbias + BN;                              // BN floats
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t num_tiles = (shape.M + kBlockM - 1) / kBlockM;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&acc_full[a], 1);
+            mbar_init(&acc_empty[a], 128);
+        }
+        mbar_init(b_full, 1);
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    for (int i = threadIdx.x; i < BN; i += blockDim.x) {
+        sbias[i] = ep.bias ? ep.bias[i] : 0.f;
+        scol[i] = 0.f;
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, 2 * BN);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------------------------------------------------- producer
+        prefetch_tmap(&tmA0);
+        if (shape.kb1) prefetch_tmap(&tmA1);
+        prefetch_tmap(&tmB);
+        mbar_arrive_expect_tx(b_full, uint32_t(kb_total) * SmemPlan<BN>::kBBlockBytes);
+        for (int kb = 0; kb < kb_total; ++kb)
+            tma_load_2d(sB + size_t(kb) * SmemPlan<BN>::kBBlockBytes, &tmB, b_full, kb * kBlockK, shape.b_row0);
+        uint32_t it = 0;
+        uint32_t last_parity[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        bool used[8] = {false, false, false, false, false, false, false, false};
+        for (int64_t tile = blockIdx.x; tile < num_tiles && !*abort_flag; tile += gridDim.x) {
+            for (int kb = 0; kb < kb_total; ++kb, ++it) {
+                int s = int(it % stages);
+                uint32_t ph = (it / stages) & 1;
+                if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[s], kATileBytes);
+                int32_t row = int32_t(tile * kBlockM);
+                if (kb < shape.kb0) tma_load_2d(sA + size_t(s) * kATileBytes, &tmA0, &full[s], kb * kBlockK, row);
+                else tma_load_2d(sA + size_t(s) * kATileBytes, &tmA1, &full[s], (kb - shape.kb0) * kBlockK, row);
+                used[s] = true;
+                last_parity[s] = ph;
+            }
+        }
+        // every copy this thread started has landed before the CTA may exit
+        for (int s = 0; s < stages; ++s)
+            if (used[s] && !mbar_wait(&full[s], last_parity[s], nullptr)) *abort_flag = 1;
+        if (!mbar_wait(b_full, 0, nullptr)) *abort_flag = 1;
+    } else if (warp == 1 && lane == 0) {
+        // -------------------------------------------------------------- MMA
+        constexpr uint32_t idesc = idesc_bf16(kBlockM, BN, 0, 0);
+        bool ok = mbar_wait(b_full, 0, abort_flag);
+        uint32_t it = 0, t = 0;
+        for (int64_t tile = blockIdx.x; ok && tile < num_tiles; tile += gridDim.x, ++t) {
+            uint32_t acc = t & 1;
+            if (!mbar_wait(&acc_empty[acc], ((t >> 1) & 1) ^ 1, abort_flag)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            uint32_t d_tmem = tmem + acc * BN;
+            for (int kb = 0; kb < kb_total; ++kb, ++it) {
+                int s = int(it % stages);
+                if (!mbar_wait(&full[s], (it / stages) & 1, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t a_addr = smem_u32(sA + size_t(s) * kATileBytes);
+                uint32_t b_addr = smem_u32(sB + size_t(kb) * SmemPlan<BN>::kBBlockBytes);
+#pragma unroll
+                for (int k = 0; k < kBlockK / 16; ++k) {
+                    uint64_t ad = smem_desc(a_addr + k * 32, 0, 1024, kSwizzle128B);
+                    uint64_t bd = smem_desc(b_addr + k * 32, 0, 1024, kSwizzle128B);
+                    mma_bf16(d_tmem, ad, bd, idesc, (kb | k) != 0);
+                }
+                mma_commit(&empty[s]);
+            }
+            if (!ok) break;
+            mma_commit(&acc_full[acc]);
+        }
+        if (!ok) *abort_flag = 1;
+        // all MMAs issued by this thread complete before tensor memory is freed
+        mma_commit(done);
+        if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
+    } else if (warp >= 2) {
+        // --------------------------------------------------------- epilogue
+        const int q = warp & 3;   // tensor-memory lane quadrant this warp may read
+        uint32_t t = 0;
+        for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
+            uint32_t acc = t & 1;
+            if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const int64_t m = tile * kBlockM + q * 32 + lane;
+            const bool live = m < shape.M;
+            const float r1 = (ep.r1_row && live) ? ep.r1_row[m] : 0.f;
+#pragma unroll 1
+            for (int c = 0; c < BN / 32; ++c) {
+                uint32_t r[32];
+                tmem_ld_32x32b_x32(tmem + acc * BN + (uint32_t(q * 32) << 16) + uint32_t(c * 32), r);
+                tmem_ld_wait();
+                float v[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    v[j] = __uint_as_float(r[j]) + sbias[c * 32 + j];
+                    if (ep.r1_row) v[j] += r1 * ep.r1_col[c * 32 + j];
+                    if (ep.relu) v[j] = v[j] > 0.f ? v[j] : 0.f;
+                    if (!live) v[j] = 0.f;
+                }
+                if (ep.mask && live) {
+                    const uint4* mp = reinterpret_cast<const uint4*>(ep.mask + m * ep.ld_mask + c * 32);
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        uint4 mv = mp[g];
+                        uint32_t w4[4] = {mv.x, mv.y, mv.z, mv.w};
+#pragma unroll
+                        for (int h = 0; h < 4; ++h) {
+                            float2 f = unpack_bf16(w4[h]);
+                            if (!(f.x > 0.f)) v[g * 8 + h * 2] = 0.f;
+                            if (!(f.y > 0.f)) v[g * 8 + h * 2 + 1] = 0.f;
+                        }
+                    }
+                }
+                if (live) {
+                    uint4* op = reinterpret_cast<uint4*>(ep.out + m * ep.ld_out + c * 32);
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+                        op[g] = make_uint4(pack_bf16(v[g * 8], v[g * 8 + 1]), pack_bf16(v[g * 8 + 2], v[g * 8 + 3]),
+                                           pack_bf16(v[g * 8 + 4], v[g * 8 + 5]),
+                                           pack_bf16(v[g * 8 + 6], v[g * 8 + 7]));
+                }
+                if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
+            }
+            tc_fence_before();
+            mbar_arrive(&acc_empty[acc]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort_flag) raise_flag(ep.flag, kFlagTimeout);
+    if (ep.colsum)
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.colsum + i, scol[i]);
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 2 * BN);
+    }
+}
+
+// --------------------------------------------------------------------------
+// Weight gradient: partial[split, n, k] = sum_{m in split} dZ[m, n] * X[m, k]
+// for one 128-row block of n and all k (X = [X0 | X1], at most 512 columns).
+// The reduction runs over samples, so both operands are MN-major in shared
+// memory: TMA boxes of 64 samples x 64 features (128-byte swizzle), LBO = the
+// 8 KB step between 64-wide feature chunks, SBO = 1024 B between 8-sample groups.
+// --------------------------------------------------------------------------
+
+struct WgradShape {
+    int64_t M;        // samples
+    int64_t m_chunk;  // samples per split (multiple of 64)
+    int n_dz;         // columns of dZ (rows of dW)
+    int kc0, kc1;     // 64-wide column chunks of X0 / X1
+};
+
+constexpr uint32_t kBox64Bytes = 64 * 64 * 2;
+
+__host__ __device__ inline int wgrad_stages(int nchunks) {
+    size_t stage = size_t(2 + nchunks) * kBox64Bytes;
+    int s = int((kMaxSmem - 1024 - 256) / stage);
+    return s > 6 ? 6 : s;
+}
+__host__ __device__ inline size_t wgrad_smem(int nchunks) {
+    return 1024 + 256 + size_t(wgrad_stages(nchunks)) * (2 + nchunks) * kBox64Bytes;
+}
+__host__ __device__ inline uint32_t tmem_cols_for(int n) {
+    uint32_t c = 32;
+    while (c < uint32_t(n)) c <<= 1;
+    return c;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_wgrad_kernel(const __grid_constant__ CUtensorMap tmDZ, const __grid_constant__ CUtensorMap tmX0,
+                    const __grid_constant__ CUtensorMap tmX1, WgradShape s, float* partial, int* flag) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int nchunks = s.kc0 + s.kc1;
+    const int np = nchunks * 64;
+    const int stages = wgrad_stages(nchunks);
+    const uint32_t stage_bytes = uint32_t(2 + nchunks) * kBox64Bytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + size_t(stages) * stage_bytes);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + 8;
+    uint64_t* acc_full = bars + 16;
+    uint64_t* done = bars + 17;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 18);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 19);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * 128;
+    const int64_t m_begin = int64_t(blockIdx.y) * s.m_chunk;
+    int64_t m_end = m_begin + s.m_chunk;
+    if (m_end > s.M) m_end = s.M;
+    const int nblk = m_end > m_begin ? int((m_end - m_begin + 63) / 64) : 0;
+    const uint32_t ncols = tmem_cols_for(np);
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < stages; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(acc_full, 1);
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, ncols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        prefetch_tmap(&tmDZ);
+        prefetch_tmap(&tmX0);
+        if (s.kc1) prefetch_tmap(&tmX1);
+        uint32_t last_parity[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        bool used[8] = {false, false, false, false, false, false, false, false};
+        for (int b = 0; b < nblk; ++b) {
+            int st = b % stages;
+            uint32_t ph = (b / stages) & 1;
+            if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            uint8_t* sa = base + size_t(st) * stage_bytes;
+            int32_t row = int32_t(m_begin + int64_t(b) * 64);
+            mbar_arrive_expect_tx(&full[st], stage_bytes);
+            tma_load_2d(sa, &tmDZ, &full[st], n0, row);
+            tma_load_2d(sa + kBox64Bytes, &tmDZ, &full[st], n0 + 64, row);
+            for (int c = 0; c < nchunks; ++c) {
+                uint8_t* dst = sa + size_t(2 + c) * kBox64Bytes;
+                if (c < s.kc0) tma_load_2d(dst, &tmX0, &full[st], c * 64, row);
+                else tma_load_2d(dst, &tmX1, &full[st], (c - s.kc0) * 64, row);
+            }
+            used[st] = true;
+            last_parity[st] = ph;
+        }
+        for (int i = 0; i < stages; ++i)
+            if (used[i] && !mbar_wait(&full[i], last_parity[i], nullptr)) *abort_flag = 1;
+    } else if (warp == 1 && lane == 0) {
+        bool ok = true;
+        for (int b = 0; b < nblk; ++b) {
+            int st = b % stages;
+            if (!mbar_wait(&full[st], (b / stages) & 1, abort_flag)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            uint32_t sa = smem_u32(base + size_t(st) * stage_bytes);
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                uint64_t ad = smem_desc(sa + ks * 2048, kBox64Bytes, 1024, kSwizzle128B);
+                for (int p = 0; p * 4 < nchunks; ++p) {
+                    int cnt = nchunks - p * 4 < 4 ? nchunks - p * 4 : 4;
+                    uint64_t bd = smem_desc(sa + (2 + p * 4) * kBox64Bytes + ks * 2048, kBox64Bytes, 1024,
+                                            kSwizzle128B);
+                    mma_bf16(tmem + uint32_t(p * 256), ad, bd, idesc_bf16(128, cnt * 64, 1, 1), (b | ks) != 0);
+                }
+            }
+            mma_commit(&empty[st]);
+        }
+        if (!ok) *abort_flag = 1;
+        mma_commit(acc_full);
+        mma_commit(done);
+        if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
+    } else if (warp >= 2) {
+        const int q = warp & 3;
+        bool ok = mbar_wait(acc_full, 0, abort_flag);
+        if (!ok) *abort_flag = 1;
+        tc_fence_after();
+        const int n = n0 + q * 32 + lane;
+        float* dst = partial + (int64_t(blockIdx.y) * s.n_dz + n) * np;
+        for (int c = 0; c < np / 32; ++c) {
+            uint32_t r[32];
+            tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(c * 32), r);
+            tmem_ld_wait();
+            if (n >= s.n_dz) continue;
+            float4* o = reinterpret_cast<float4*>(dst + c * 32);
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                float4 v;
+                if (nblk > 0 && ok) {
+                    v = make_float4(__uint_as_float(r[4 * g]), __uint_as_float(r[4 * g + 1]),
+                                    __uint_as_float(r[4 * g + 2]), __uint_as_float(r[4 * g + 3]));
+                } else {
+                    v = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                o[g] = v;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort_flag) raise_flag(flag, kFlagTimeout);
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+}  // namespace tc
+}  // namespace srf

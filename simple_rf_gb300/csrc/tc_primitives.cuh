@@ -46,16 +46,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: gives up after `limit` polls (each poll may itself suspend
-// briefly), so a lost arrival ends in an error flag instead of a hang.
-constexpr uint32_t kWaitLimit = 1u << 26;
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up after kWaitNs of wall time (or as soon as another role
+// of the CTA aborted, when abort_flag is given), so a lost arrival ends in an
+// error flag, not a hang.  Drains of in-flight copies/MMAs pass no abort flag:
+// they must wait for completion even after an abort (still bounded in time).
+constexpr uint64_t kWaitNs = 4000000000ull;
 
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    uint64_t start = 0;
+    for (uint32_t i = 0;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 1023) == 1023 && *abort_flag) return false;
+        if ((i & 255) == 255) {
+            if (abort_flag && *abort_flag) return false;
+            uint64_t now = globaltimer_ns();
+            if (start == 0) start = now;
+            else if (now - start > kWaitNs) return false;
+        }
     }
-    return false;
 }
 
 // ----------------------------------------------------------------------- TMA --

@@ -1,0 +1,139 @@
+"""tcgen05 BF16 GEMMs against a plain torch FP32 reference of the same op, and
+the BF16 NeRF MLP against the float64 oracle.
+
+Tolerances: the GEMM output is stored in BF16, so 1.5e-2 relative of the
+row scale; weight-gradient partials are FP32 sums of exact BF16 products, so
+1e-4 relative L2.  MLP: rgb within 2e-3 max-abs and parameter gradients within
+1e-2 relative L2 of the float64 oracle (the BF16 bars of the benchmark spec).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import nerf as on
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from simple_rf_gb300 import build as b
+    b.build()
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _bf(x):
+    return x.to(torch.bfloat16).contiguous()
+
+
+def _linear(x0, x1, w, w_row0, n, bias, relu, mask=None, colsum=None):
+    from simple_rf_gb300 import _lib
+    m = x0.shape[0]
+    out = torch.empty(m, n, dtype=torch.bfloat16, device=DEV)
+    k0, k1 = x0.shape[1], (0 if x1 is None else x1.shape[1])
+    _lib.call('srf_bf16_linear', _p(out), n, _p(x0), x0.shape[1], k0, _p(x1), k1, k1, _p(w), w.shape[1], w.shape[0],
+              w_row0, _p(bias), m, n, int(relu), _p(mask), 0 if mask is None else mask.shape[1], _p(colsum),
+              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return out
+
+
+@pytest.mark.parametrize('m,k0,k1,n,relu', [(1000, 64, 256, 256, True), (4096, 256, 0, 256, True),
+                                           (777, 256, 64, 128, True), (130, 128, 0, 64, False)])
+def test_bf16_linear(m, k0, k1, n, relu):
+    g = torch.Generator(device=DEV).manual_seed(0)
+    x0 = _bf(torch.randn(m, k0, device=DEV, generator=g))
+    x1 = _bf(torch.randn(m, k1, device=DEV, generator=g)) if k1 else None
+    w = _bf(torch.randn(n, k0 + k1, device=DEV, generator=g) * 0.1)
+    b = torch.randn(n, device=DEV, generator=g)
+    out = _linear(x0, x1, w, 0, n, b, relu)
+    x = x0.float() if x1 is None else torch.cat([x0.float(), x1.float()], 1)
+    ref = x @ w.float().T + b
+    if relu:
+        ref = ref.relu()
+    err = (out.float() - ref).abs().max().item()
+    assert err < 1.5e-2 * ref.abs().max().item(), err
+
+
+def test_bf16_linear_dgrad_mask_colsum():
+    """The backward-data form: rows [row0, row0 + n) of a transposed weight,
+    ReLU mask from a forward activation, column sums for the bias gradient."""
+    g = torch.Generator(device=DEV).manual_seed(1)
+    m, kin, n, row0 = 2000, 256, 256, 64
+    dz = _bf(torch.randn(m, kin, device=DEV, generator=g))
+    wt = _bf(torch.randn(row0 + n, kin, device=DEV, generator=g) * 0.1)
+    mask = _bf(torch.randn(m, n, device=DEV, generator=g))
+    colsum = torch.zeros(n, device=DEV)
+    out = _linear(dz, None, wt, row0, n, None, False, mask=mask, colsum=colsum)
+    ref = (dz.float() @ wt[row0:row0 + n].float().T) * (mask.float() > 0)
+    err = (out.float() - ref).abs().max().item()
+    assert err < 1.5e-2 * ref.abs().max().item(), err
+    cs_err = (colsum - ref.sum(0)).abs().max().item()
+    assert cs_err < 1e-3 * ref.abs().sum(0).max().item(), cs_err
+
+
+@pytest.mark.parametrize('m,n_dz,k0,k1', [(1000, 256, 64, 256), (8192, 256, 256, 0), (3000, 128, 256, 64)])
+def test_bf16_wgrad(m, n_dz, k0, k1):
+    from simple_rf_gb300 import _lib
+    lib = _lib.load()
+    g = torch.Generator(device=DEV).manual_seed(2)
+    dz = _bf(torch.randn(m, n_dz, device=DEV, generator=g))
+    x0 = _bf(torch.randn(m, k0, device=DEV, generator=g))
+    x1 = _bf(torch.randn(m, k1, device=DEV, generator=g)) if k1 else None
+    nbytes = lib.srf_bf16_wgrad_workspace_size(n_dz, k0 + k1)
+    part = torch.empty(nbytes // 4, device=DEV)
+    splits = ctypes.c_int(0)
+    _lib.call('srf_bf16_wgrad', _p(part), nbytes, ctypes.byref(splits), _p(dz), n_dz, n_dz, _p(x0), k0, k0, _p(x1),
+              k1, k1, m, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    s = splits.value
+    got = part[:s * n_dz * (k0 + k1)].reshape(s, n_dz, k0 + k1).sum(0)
+    x = x0.float() if x1 is None else torch.cat([x0.float(), x1.float()], 1)
+    ref = dz.float().T @ x
+    rel = ((got - ref).norm() / ref.norm()).item()
+    assert rel < 1e-4, rel
+
+
+SPECS = {
+    'main': dict(),
+    'aug_l4_noview': dict(points_pe_degree=4, use_view_dirs=False, view_dependent_rgb=False),
+    'points_aug': dict(points_sigma_pe_degree=3),
+}
+
+
+@pytest.mark.parametrize('name', list(SPECS))
+def test_bf16_mlp_against_fp64_oracle(name):
+    from simple_rf_gb300 import functional as F
+    kw = SPECS[name]
+    ospec = on.MlpSpec(points_pe_degree=kw.get('points_pe_degree', 10), use_view_dirs=kw.get('use_view_dirs', True),
+                       view_dependent_rgb=kw.get('view_dependent_rgb', True),
+                       points_sigma_pe_degree=kw.get('points_sigma_pe_degree'))
+    spec = F.MlpSpec(**kw)
+    p64 = on.xavier_params(ospec, 20, np.float64)
+    rng = np.random.default_rng(21)
+    div = 64
+    m = 64 * div
+    pts = rng.standard_normal((m, 3)) * 0.7
+    vd = rng.standard_normal((m // div, 3))
+    vd /= np.linalg.norm(vd, axis=1, keepdims=True)
+    params = [torch.from_numpy(p64[k].astype(np.float32)).to(DEV).requires_grad_(True) for k in spec.param_names]
+    tp = torch.from_numpy(pts.astype(np.float32)).to(DEV)
+    tv = torch.from_numpy(vd.astype(np.float32)).to(DEV) if spec.use_view_dirs else None
+    sigma, rgb = F.NerfMlpFunction.apply(spec, 1, tp, tv, div, None, *params)
+    rs, rr, cache = on.mlp_forward(p64, ospec, pts.astype(np.float32).astype(np.float64),
+                                   np.repeat(vd.astype(np.float32).astype(np.float64), div, 0))
+    assert np.abs(rgb.detach().cpu().numpy() - rr).max() < 2e-3
+    assert np.abs(sigma.detach().cpu().numpy() - rs[:, 0]).max() < 2e-2 * max(1.0, np.abs(rs).max())
+    cs = rng.standard_normal(m)
+    cr = rng.standard_normal((m, 3))
+    ((sigma * torch.from_numpy(cs.astype(np.float32)).to(DEV)).sum() +
+     (rgb * torch.from_numpy(cr.astype(np.float32)).to(DEV)).sum()).backward()
+    gref = on.mlp_backward(p64, ospec, cache, cs[:, None], cr)
+    for k, prm in zip(spec.param_names, params):
+        got = prm.grad.double().cpu().numpy()
+        rel = np.linalg.norm(got - gref[k]) / max(np.linalg.norm(gref[k]), 1e-30)
+        assert rel < 1e-2, (k, rel)
