@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the Simple-NeRF training step (fwd + bwd + Adam) on GB300.
+
+Workload (the spec training configuration): 4096 rays per step,
+64 stratified coarse + 128 inverse-CDF fine samples, two 8x256 NeRF MLPs with
+the skip at layer 5 and a 128-wide view branch, white background, loss = rgb MSE
+(coarse + fine) + 0.1 * L1 depth on 25% of the rays, Adam.  Synthetic inputs:
+o ~ N(0, 0.1^2), d = normalize(N(0, I)), targets ~ U[0,1]^3, depth ~ U[2,6].
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value`  : train rays/s of the BF16 tcgen05 step, inputs resident in HBM,
+           whole step replayed as one CUDA graph, timed with CUDA events.
+`e2e`    : the same through the public train-step API with host (pinned)
+           inputs copied H2D and the loss read back D2H every step.
+`fp32_plain`: the FP32 SIMT path on the same workload (the headline ratio's
+           denominator), fewer steps.
+`--impl reference`: the reference algorithm's CPU restatement (the numpy
+           oracle port of SimpleNeRF17) timed on the host cores.
+With N > 1 (torchrun) every rank trains its own replica (no collective on the
+data path; rays are independent) and `value` sums the ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = 'train rays/s fwd+bwd, BF16 fused vs FP32 plain on 1 GB300 at <=2e-3 RGB error'
+N_RAYS, N_COARSE, N_FINE = 4096, 64, 128
+MACS_PER_SAMPLE = 593408
+
+
+def peaks():
+    path = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), float(p['bf16_tflops']), 'measured'
+    except Exception:
+        return 6800.0, 1900.0, 'fallback'
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), f'--query-gpu={self.FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == 'active':
+                    reasons.add(name)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def dist_setup(args):
+    import torch
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault('MASTER_ADDR', '127.0.0.1')
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl' if args.impl == 'ours' else 'gloo')
+    return ws, rank, local
+
+
+def time_steps(step, k, stream):
+    import torch
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for i in range(k):
+        step(i)
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end) / 1000.0
+
+
+def roofline_gemm(dev, peak_tflops, peak_kind, reps=20):
+    """The dominant kernel (tcgen05 layer GEMM, fine-net trunk shape) timed alone."""
+    import ctypes
+    import torch
+    from simple_rf_gb300 import _lib
+    m, k, n = N_RAYS * (N_COARSE + N_FINE), 256, 256
+    x = torch.randn(m, k, device=dev).to(torch.bfloat16)
+    w = (torch.randn(n, k, device=dev) * 0.05).to(torch.bfloat16)
+    b = torch.zeros(n, device=dev)
+    y = torch.empty(m, n, device=dev, dtype=torch.bfloat16)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def launch():
+        _lib.call('srf_bf16_linear', p(y), n, p(x), k, k, None, 0, 0, p(w), k, n, 0, p(b), m, n, 1, None, 0, None, st)
+
+    for _ in range(3):
+        launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        launch()
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0 / reps
+    flops = 2.0 * m * n * k
+    achieved = flops / t / 1e12
+    traffic = None
+    tpath = os.path.join(REPO, 'profiles', 'traffic.json')
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get('tc_gemm_kernel_256_bytes_per_launch')
+        except Exception:
+            traffic = None
+    return {'kernel': 'tc_gemm_kernel<256> (M=786432, K=256, N=256, bias+ReLU epilogue)', 'bound': 'tensor',
+            'achieved': round(achieved, 1), 'peak': peak_tflops, 'unit': 'TFLOP/s',
+            'frac': round(achieved / peak_tflops, 4), 'peak_source': peak_kind + ' (bf16 burst)',
+            'traffic': traffic, 'launch_ms': round(t * 1e3, 4),
+            'algorithmic_bytes_per_launch': int((m * k + m * n + n * k) * 2)}
+
+
+def cpu_baseline(sample_rays=128, min_seconds=10.0):
+    """The oracle port of the reference step on the host cores (bounded sample)."""
+    import numpy as np
+    from oracle import nerf as on
+    spec = on.MlpSpec()
+    pc, pf = on.xavier_params(spec, 0), on.xavier_params(spec, 1)
+    rng = np.random.default_rng(0)
+    n = sample_rays
+    o = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
+    d = rng.standard_normal((n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    t_rgb = rng.random((n, 3), dtype=np.float32)
+    t_d = (rng.random(n, dtype=np.float32) * 4 + 2).astype(np.float32)
+    mask = np.zeros(n, np.float32)
+    mask[:n // 4] = 1
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        u_c = rng.random((n, N_COARSE), dtype=np.float32)
+        u_f = rng.random((n, N_FINE), dtype=np.float32)
+        ret, caches = on.render_rays(pc, pf, spec, spec, o, d, 2.0, 6.0, N_COARSE, N_FINE, u_c, u_f, white_bkgd=True)
+        _, grads = on.train_loss(ret, t_rgb, t_d, mask)
+        g = on.backward_render({'coarse': pc, 'fine': pf}, {'coarse': spec, 'fine': spec}, caches, grads, n)
+        for net, p in (('coarse', pc), ('fine', pf)):
+            for k in p:
+                p[k] -= np.float32(5e-4) * np.sign(g[net][k])
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or steps >= 50:
+            break
+    return {'value': round(n * steps / el, 2), 'unit': 'rays/s', 'cores': os.cpu_count(), 'kind': 'port',
+            'sample': f'{steps} oracle train steps of {n} rays (64+128 samples, 8x256 coarse+fine MLPs, '
+                      f'numpy float32, BLAS threads = host cores) in {el:.1f} s'}
+
+
+def run_reference(args):
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    total_t, total_rays = 0.0, 0
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(sample_rays=64, min_seconds=0.0)
+        if i >= args.warmup:
+            total_rays += 64
+            total_t += 64 / cb['value']
+    v = total_rays / total_t
+    line = {'impl': 'reference', 'metric': METRIC, 'value': round(v, 2), 'unit': 'rays/s', 'n_gpus': ws,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(1e3 * total_t / args.steps, 2),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'nerf_train_step_4096rays_64+128samples_8x256', 'sample_rays_per_step': 64},
+            'cpu_baseline': {'value': round(v, 2), 'unit': 'rays/s', 'cores': os.cpu_count(), 'kind': 'port',
+                             'sample': f'{args.steps} steps of 64 rays of the config-2 step (numpy oracle port of '
+                                       'SimpleNeRF17 forward + hand-derived backward)'},
+            'e2e': {'value': round(v, 2), 'unit': 'rays/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_setup(args)
+    dev = torch.device('cuda', local)
+    torch.cuda.set_device(dev)
+    import __graft_entry__
+    __graft_entry__.build()
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.train_step import NerfTrainStep, synthetic_batch
+
+    stream = torch.cuda.current_stream(dev)
+    pool = [synthetic_batch(N_RAYS, N_COARSE, N_FINE, seed=100 + i + 1000 * rank, device=dev) for i in range(4)]
+    host = [synthetic_batch(N_RAYS, N_COARSE, N_FINE, seed=200 + i + 1000 * rank, pin=True) for i in range(4)]
+    h2d = sum(t.numel() * t.element_size() for t in host[0])
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- BF16 tcgen05 step (headline) ----
+    bf = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision='bf16', device=dev)
+    bf.set_batch(*pool[0])
+    bf.capture(warmup=2)
+
+    def bf_step(i):
+        bf.set_batch(*pool[i % 4])
+        bf.step()
+
+    for i in range(args.warmup):
+        bf_step(i)
+    barrier()
+    with ClockSampler(local) as clocks:
+        t_bf = time_steps(bf_step, args.steps, stream)
+    barrier()
+    t_bf = max_over_ranks(t_bf)
+    # rgb agreement of the BF16 step with the FP32 plain step (same weights, same batch)
+    loss_host = torch.zeros(1, pin_memory=True)
+
+    def e2e_step(i):
+        bf.set_batch(*host[i % 4], non_blocking=True)
+        bf.step()
+        loss_host.copy_(bf.loss, non_blocking=True)
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    barrier()
+    t_e2e = max_over_ranks(time_steps(e2e_step, args.steps, stream))
+    barrier()
+    launches = bf.launches_per_step
+
+    # ---- FP32 plain step (ratio denominator) ----
+    fp = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision='fp32', device=dev)
+    fp.set_batch(*pool[0])
+    fp.capture(warmup=1)
+    k32 = max(2, min(args.steps, 5))
+
+    def fp_step(i):
+        fp.set_batch(*pool[i % 4])
+        fp.step()
+
+    fp_step(0)
+    barrier()
+    t_fp = max_over_ranks(time_steps(fp_step, k32, stream))
+    barrier()
+
+    # accuracy: one forward of both paths from identical weights and inputs
+    acc = {}
+    cmp_bf = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision='bf16', device=dev, seed=7)
+    cmp_fp = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision='fp32', device=dev, seed=7)
+    for s in (cmp_bf, cmp_fp):
+        s.set_batch(*pool[1])
+        s.step()
+    torch.cuda.synchronize(dev)
+    for tag in ('coarse', 'fine'):
+        d = (cmp_bf.buf[tag]['rgb_map'] - cmp_fp.buf[tag]['rgb_map']).abs().max().item()
+        acc[f'rgb_{tag}_max_abs_bf16_vs_fp32'] = round(d, 6)
+    del cmp_bf, cmp_fp
+    flag = torch.zeros(1, dtype=torch.int32)
+    import ctypes
+    fl = ctypes.c_int(0)
+    _lib.check(_lib.load().srf_read_device_flag(ctypes.byref(fl), ctypes.c_void_p(stream.cuda_stream)), 'flag')
+    del flag
+
+    hbm_peak, tf_peak, peak_kind = peaks()
+    roof = roofline_gemm(dev, tf_peak, peak_kind) if rank == 0 else None
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
+    value = ws * N_RAYS * args.steps / t_bf
+    line = {
+        'metric': METRIC, 'value': round(value, 1), 'unit': 'rays/s', 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': round(1e3 * t_bf / args.steps, 4), 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'bf16', 'data': 'synthetic',
+        'config': {'workload': 'nerf_train_step_4096rays_64+128samples_8x256', 'rays_per_step_per_gpu': N_RAYS,
+                   'samples': '64 stratified + 128 inverse-CDF (fine net evaluates 192)',
+                   'mlp': '8x256 ReLU, skip at layer 5, sigma head, 256->128 view layer, sigmoid rgb; coarse+fine',
+                   'loss': 'rgb MSE (coarse+fine) + 0.1 L1 depth on 25% of rays; Adam',
+                   'parallelism': f'replicas x{ws}' if ws > 1 else 'single GPU',
+                   'l2': 'per-step working set ~5 GB of activations >> 129 MB L2 (no flush needed)',
+                   'cuda_graph': True},
+        'samples_per_s': round(value * (N_COARSE + N_COARSE + N_FINE), 1),
+        'tflops_model': round(value * 6 * MACS_PER_SAMPLE * (N_COARSE + N_COARSE + N_FINE) / 1e12, 1),
+        'fp32_plain': {'value': round(ws * N_RAYS * k32 / t_fp, 1), 'unit': 'rays/s',
+                       'ms_per_step': round(1e3 * t_fp / k32, 3), 'steps': k32},
+        'speedup_bf16_vs_fp32_plain': round((N_RAYS * args.steps / t_bf) / (N_RAYS * k32 / t_fp), 2),
+        'accuracy': acc,
+        'device_flag': fl.value,
+        'e2e': {'value': round(ws * N_RAYS * args.steps / t_e2e, 1), 'unit': 'rays/s', 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': 4},
+        'gpu_launches': launches * args.steps if launches else None,
+        'gpu_launches_per_step': launches,
+        'clocks': clocks.summary(),
+        'roofline': roof,
+    }
+    if ws == 1:
+        line['cpu_baseline'] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

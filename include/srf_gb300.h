@@ -40,6 +40,9 @@ const char* srf_status_string(int status);
 const char* srf_version(void);
 /* Text of the last CUDA error seen by this thread (static thread-local buffer). */
 const char* srf_last_cuda_error(void);
+/* Number of kernels this library has launched (or captured into a graph) in
+ * this process; used to count launches per training step. */
+int64_t srf_launch_count(void);
 /* Reads and clears the device-side error flag (bounded-wait timeouts, index
  * range violations) that kernels set instead of trapping.  Synchronises `stream`.
  * Writes the flag value (0 = clean) to *flag_out. */
@@ -289,9 +292,17 @@ int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* d
                        float* loss_dev, float* g_rgb, float* g_depth, void* stream);
 
 /* Fused Adam (torch.optim.Adam semantics, bias-corrected, no amsgrad) over n
- * elements; step is the 1-based step count after this update. */
+ * elements; step is the 1-based step count after this update, or, when
+ * step_dev != NULL, read from device memory (for CUDA-graph replays).
+ * Replaces the optimizer step of Trainer10.train_one_iter (src/Trainer10.py:110). */
 int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
-                  float beta1, float beta2, float eps, float weight_decay, int step, void* stream);
+                  float beta1, float beta2, float eps, float weight_decay, int step, const int32_t* step_dev,
+                  void* stream);
+/* *counter_dev += value on the stream (advances a graph-replayed step count). */
+int srf_counter_add(int32_t* counter_dev, int value, void* stream);
+/* Sample points pts (N*S,3) = o + d * z (src/models/SimpleNeRF17.py:213-215). */
+int srf_ray_points(const float* rays_o, const float* rays_d, const float* z, int n_rays, int n_samples, float* pts,
+                   void* stream);
 
 #ifdef __cplusplus
 }

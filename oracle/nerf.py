@@ -460,12 +460,14 @@ def composite_backward(cache, g):
 
 
 def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n_coarse, n_fine,
-                u_coarse=None, u_fine=None, white_bkgd=False, ndc=None, aug=None):
+                u_coarse=None, u_fine=None, white_bkgd=False, ndc=None, aug=None, z_fine=None):
     """SimpleNeRF17.py:159-328 render_rays for synthetic rays (ray generation patched out).
 
     ``ndc`` = dict(h, w, fx, fy, near) switches to NDC rays (config 3).  ``aug`` =
     list of (name, params, spec) augmented coarse nets run on the coarse samples
     (:244-261) and, when they also carry fine params, on the fine samples (:296-313).
+    ``z_fine`` (N, Sc+Sf) replaces the inverse-CDF depths (tests use it to check
+    the fine pass on exactly the depths another implementation sampled).
     Returns (outputs dict keyed like the reference, caches for backward).
     """
     ret, caches = {}, {}
@@ -501,7 +503,7 @@ def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n
         for k, v in o.items():
             ret[f'{name}_{k}_coarse'] = v
     if params_f is not None:
-        zf = fine_z(zc, out_c['weights'], n_fine, u_fine)
+        zf = fine_z(zc, out_c['weights'], n_fine, u_fine) if z_fine is None else z_fine.astype(zc.dtype)
         out_f, sf, rf = run(params_f, spec_f, zf, 'fine')
         ret['z_vals_fine'] = zf
         for k, v in out_f.items():

@@ -91,7 +91,10 @@ _SIGS = {
                                     c_int, c_int, P]),
     'srf_positional_encoding_backward': (c_int, [P, P, P, c_int, c_int64, P, c_int, c_int, P]),
     'srf_rgb_depth_loss': (c_int, [P, P, P, P, P, c_int, c_int, c_float, P, P, P, P]),
-    'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P]),
+    'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P, P]),
+    'srf_counter_add': (c_int, [P, c_int, P]),
+    'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
+    'srf_launch_count': (c_int64, []),
 }
 
 

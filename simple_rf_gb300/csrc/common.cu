@@ -1,4 +1,5 @@
-// Status strings, CUDA error text and the device-side error flag.
+// Status strings, CUDA error text, the launch counter and the device-side error flag.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -10,6 +11,10 @@ thread_local char g_last_error[256] = "no error";
 }  // namespace
 
 namespace srf {
+
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_cuda_error(cudaError_t e) {
     std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
@@ -51,6 +56,8 @@ extern "C" const char* srf_status_string(int status) {
 extern "C" const char* srf_version(void) { return "srf_gb300 1.0 sm_103a"; }
 
 extern "C" const char* srf_last_cuda_error(void) { return g_last_error; }
+
+extern "C" int64_t srf_launch_count(void) { return srf::g_launches.load(); }
 
 extern "C" int srf_read_device_flag(int* flag_out, void* stream) {
     if (!flag_out) return SRF_ERR_NULL;

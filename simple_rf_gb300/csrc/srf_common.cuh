@@ -22,7 +22,12 @@ __device__ __forceinline__ void raise_flag(int* flag, int bits) {
     if (flag) atomicOr(flag, bits);
 }
 
+// Counts kernel launches issued by this library (every launch site calls
+// launch_status() once); read through srf_launch_count().
+void count_launch();
+
 inline int launch_status() {
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_cuda_error(e);

@@ -39,12 +39,18 @@ __global__ void loss_kernel(const float* __restrict__ rgb, const float* __restri
 }
 
 // torch.optim.Adam (foreach=False math): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
-// p -= lr / (1 - b1^t) * m / (sqrt(v) / sqrt(1 - b2^t) + eps).
+// p -= lr / (1 - b1^t) * m / (sqrt(v) / sqrt(1 - b2^t) + eps).  With step_dev the
+// step count t is read on the device (graph replays advance it with srf_counter_add).
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                             float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float wd,
-                            float bc1, float bc2_sqrt) {
+                            float bc1, float bc2_sqrt, const int* step_dev) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    if (step_dev) {
+        float t = float(*step_dev);
+        bc1 = 1.f - powf(b1, t);
+        bc2_sqrt = sqrtf(1.f - powf(b2, t));
+    }
     for (; i < n; i += stride) {
         float gi = g[i];
         if (wd != 0.f) gi += wd * p[i];
@@ -57,10 +63,39 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     }
 }
 
+__global__ void counter_add_kernel(int* c, int v) { *c += v; }
+
+// pts[r * S + i] = o[r] + d[r] * z[r, i]  (SimpleNeRF17.py:213-215)
+__global__ void ray_points_kernel(const float* __restrict__ o, const float* __restrict__ d,
+                                  const float* __restrict__ z, int64_t n, int s, float* pts) {
+    int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= n * s) return;
+    int64_t r = idx / s;
+    float zz = z[idx];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pts[3 * idx + a] = o[3 * r + a] + d[3 * r + a] * zz;
+}
+
 }  // namespace
 }  // namespace srf
 
 using namespace srf;
+
+extern "C" int srf_counter_add(int32_t* counter_dev, int value, void* stream) {
+    if (!counter_dev) return SRF_ERR_NULL;
+    counter_add_kernel<<<1, 1, 0, as_stream(stream)>>>(counter_dev, value);
+    return launch_status();
+}
+
+extern "C" int srf_ray_points(const float* rays_o, const float* rays_d, const float* z, int n_rays, int n_samples,
+                              float* pts, void* stream) {
+    if (!rays_o || !rays_d || !z || !pts) return SRF_ERR_NULL;
+    if (n_rays < 0 || n_samples < 1) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    int64_t tot = int64_t(n_rays) * n_samples;
+    ray_points_kernel<<<grid_1d(tot, 256), 256, 0, as_stream(stream)>>>(rays_o, rays_d, z, n_rays, n_samples, pts);
+    return launch_status();
+}
 
 extern "C" int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* depth,
                                   const float* target_depth, const uint8_t* depth_mask, int n_rays, int n_depth_rays,
@@ -76,15 +111,17 @@ extern "C" int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, con
 }
 
 extern "C" int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
-                             float beta1, float beta2, float eps, float weight_decay, int step, void* stream) {
+                             float beta1, float beta2, float eps, float weight_decay, int step,
+                             const int32_t* step_dev, void* stream) {
     if (!param || !grad || !exp_avg || !exp_avg_sq) return SRF_ERR_NULL;
-    if (n < 0 || step < 1) return SRF_ERR_SHAPE;
+    if (n < 0 || (step < 1 && !step_dev)) return SRF_ERR_SHAPE;
+    if (step < 1) step = 1;
     if (n == 0) return SRF_OK;
     float bc1 = 1.f - powf(beta1, float(step));
     float bc2 = sqrtf(1.f - powf(beta2, float(step)));
     unsigned blocks = grid_1d(n, 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
     adam_kernel<<<blocks, 256, 0, as_stream(stream)>>>(param, grad, exp_avg, exp_avg_sq, n, lr, beta1, beta2, eps,
-                                                       weight_decay, bc1, bc2);
+                                                       weight_decay, bc1, bc2, step_dev);
     return launch_status();
 }

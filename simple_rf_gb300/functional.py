@@ -280,7 +280,7 @@ def adam_step(param, grad, exp_avg, exp_avg_sq, *, lr, beta1=0.9, beta2=0.999, e
     for name, x in (('param', param), ('grad', grad), ('exp_avg', exp_avg), ('exp_avg_sq', exp_avg_sq)):
         _require(x, name, param.shape)
     call('srf_adam_step', _ptr(param), _ptr(grad), _ptr(exp_avg), _ptr(exp_avg_sq), param.numel(), float(lr),
-         float(beta1), float(beta2), float(eps), float(weight_decay), int(step), _stream())
+         float(beta1), float(beta2), float(eps), float(weight_decay), int(step), None, _stream())
 
 
 def rgb_depth_loss(rgb, target_rgb, depth, target_depth, depth_mask, n_depth_rays, depth_weight, loss=None):
