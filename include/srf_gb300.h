@@ -195,6 +195,13 @@ int srf_composite_forward(const srf_composite_args* args, void* stream);
 /* Adjoint: reverse-scan transmittance gradient, recomputing the forward per ray. */
 int srf_composite_backward(const srf_composite_args* args, void* stream);
 
+/* out (N,C) = sum_s weights (N,S) * values (N,S,C), C <= 4, and its adjoint.
+ * Replaces LowRankTensor.volume_render (src/models/SimpleTensoRF09.py:816-819). */
+int srf_weighted_sum(const float* weights, const float* values, int n_rays, int n_samples, int channels, float* out,
+                     void* stream);
+int srf_weighted_sum_backward(const float* weights, const float* values, const float* g_out, int n_rays,
+                              int n_samples, int channels, float* d_weights, float* d_values, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* TensoRF VM decomposition                                                  */
 /* ------------------------------------------------------------------------ */

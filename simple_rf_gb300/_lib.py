@@ -73,6 +73,8 @@ _SIGS = {
                                c_int, c_int64, P]),
     'srf_composite_forward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
     'srf_composite_backward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
+    'srf_weighted_sum': (c_int, [P, P, c_int, c_int, c_int, P, P]),
+    'srf_weighted_sum_backward': (c_int, [P, P, P, c_int, c_int, c_int, P, P, P]),
     'srf_vm_density_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_vm_density_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_vm_color_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),

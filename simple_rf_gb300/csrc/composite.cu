@@ -289,6 +289,38 @@ __global__ void composite_bwd_kernel(srf_composite_args a) {
     }
 }
 
+// out[r, c] = sum_s w[r, s] x[r, s, c] (one warp per ray); the adjoint gives
+// dw[r, s] = sum_c g[r, c] x[r, s, c] and dx[r, s, c] = w[r, s] g[r, c].
+__global__ void weighted_sum_kernel(const float* __restrict__ w, const float* __restrict__ x, int n, int s, int c,
+                                    float* out) {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (r >= n) return;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int i = lane; i < s; i += 32) {
+        float wi = w[int64_t(r) * s + i];
+        for (int k = 0; k < c; ++k) acc[k] += wi * x[(int64_t(r) * s + i) * c + k];
+    }
+    for (int k = 0; k < c; ++k) {
+        float v = warp_sum(acc[k]);
+        if (lane == 0) out[int64_t(r) * c + k] = v;
+    }
+}
+
+__global__ void weighted_sum_bwd_kernel(const float* __restrict__ w, const float* __restrict__ x,
+                                        const float* __restrict__ g, int n, int s, int c, float* dw, float* dx) {
+    int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= int64_t(n) * s) return;
+    int64_t r = idx / s;
+    float acc = 0.f;
+    for (int k = 0; k < c; ++k) {
+        float gk = g[r * c + k];
+        acc += gk * x[idx * c + k];
+        if (dx) dx[idx * c + k] = w[idx] * gk;
+    }
+    if (dw) dw[idx] = acc;
+}
+
 int check_args(const srf_composite_args* a, bool bwd) {
     if (!a || !a->sigma || !a->z || !a->rays_d) return SRF_ERR_NULL;
     if ((a->flags & SRF_COMPOSITE_NDC) && (!a->rays_o || !a->rays_d_ndc)) return SRF_ERR_NULL;
@@ -331,4 +363,27 @@ extern "C" int srf_composite_backward(const srf_composite_args* args, void* stre
     int st = check_args(args, true);
     if (st != SRF_OK || args->n_rays == 0) return st;
     return launch(composite_bwd_kernel, args, stream);
+}
+
+extern "C" int srf_weighted_sum(const float* weights, const float* values, int n_rays, int n_samples, int channels,
+                                float* out, void* stream) {
+    if (!weights || !values || !out) return SRF_ERR_NULL;
+    if (n_rays < 0 || n_samples < 1 || channels < 1 || channels > 4) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    weighted_sum_kernel<<<grid_1d(n_rays, 8), 256, 0, as_stream(stream)>>>(weights, values, n_rays, n_samples,
+                                                                          channels, out);
+    return launch_status();
+}
+
+extern "C" int srf_weighted_sum_backward(const float* weights, const float* values, const float* g_out, int n_rays,
+                                         int n_samples, int channels, float* d_weights, float* d_values,
+                                         void* stream) {
+    if (!weights || !values || !g_out) return SRF_ERR_NULL;
+    if (n_rays < 0 || n_samples < 1 || channels < 1 || channels > 4) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    int64_t tot = int64_t(n_rays) * n_samples;
+    weighted_sum_bwd_kernel<<<grid_1d(tot, 256), 256, 0, as_stream(stream)>>>(weights, values, g_out, n_rays,
+                                                                             n_samples, channels, d_weights,
+                                                                             d_values);
+    return launch_status();
 }

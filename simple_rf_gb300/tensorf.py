@@ -167,6 +167,125 @@ class _LinearFunction(torch.autograd.Function):
         return dx, dw, db, None, None
 
 
+class _WeightedSum(torch.autograd.Function):
+    """volume_render (SimpleTensoRF09.py:816-819): sum_s w * x."""
+
+    @staticmethod
+    def forward(ctx, w, x):
+        n, s = w.shape
+        c = x.shape[-1]
+        out = torch.empty(n, c, device=w.device)
+        call('srf_weighted_sum', _ptr(w), _ptr(x), n, s, c, _ptr(out), _stream())
+        ctx.save_for_backward(w, x)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        w, x = ctx.saved_tensors
+        n, s = w.shape
+        dw = torch.empty_like(w) if ctx.needs_input_grad[0] else None
+        dx = torch.empty_like(x) if ctx.needs_input_grad[1] else None
+        call('srf_weighted_sum_backward', _ptr(w), _ptr(x), _ptr(g.contiguous()), n, s, x.shape[-1], _ptr(dw),
+             _ptr(dx), _stream())
+        return dw, dx
+
+
+def weighted_sum(w, x):
+    return _WeightedSum.apply(w.contiguous(), x.contiguous())
+
+
+def gather_rows(src, idx, count, n, row_div=1):
+    """dst[i] = src[idx[i] // row_div] for i < count (no gradient)."""
+    cols = src.shape[-1]
+    dst = torch.empty(n, cols, device=src.device)
+    if n:
+        call('srf_gather_rows', _ptr(dst), _ptr(src.contiguous()), _ptr(idx), _ptr(count), n, cols, int(row_div),
+             _stream())
+    return dst
+
+
+class _ScatterRows(torch.autograd.Function):
+    """Dense (rows, C) zeros with src rows placed at idx (the reference's
+    ``rgb[mask] = surface_rgb``, SimpleTensoRF09.py:1247,1271)."""
+
+    @staticmethod
+    def forward(ctx, src, idx, count, rows):
+        n, c = src.shape
+        out = torch.zeros(rows, c, device=src.device)
+        if n:
+            call('srf_scatter_rows', _ptr(out), _ptr(src.contiguous()), _ptr(idx), _ptr(count), n, c, _stream())
+        ctx.save_for_backward(idx, count)
+        ctx.n = n
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        idx, count = ctx.saved_tensors
+        return gather_rows(g.contiguous(), idx, count, ctx.n), None, None, None
+
+
+def scatter_rows(src, idx, count, rows):
+    return _ScatterRows.apply(src, idx, count, rows)
+
+
+class _DensityActivation(torch.autograd.Function):
+    """sigma (rows,) zeros with density_predictor(features) at idx
+    (SimpleTensoRF09.py:671-679, 1237-1238)."""
+
+    @staticmethod
+    def forward(ctx, feat, idx, count, rows, mode, offset):
+        sigma = torch.zeros(rows, device=feat.device)
+        n = feat.shape[0]
+        if n:
+            call('srf_density_activation', _ptr(sigma), _ptr(feat), _ptr(idx), _ptr(count), n, mode, float(offset),
+                 _stream())
+        ctx.save_for_backward(feat, idx, count)
+        ctx.mode, ctx.offset = mode, offset
+        return sigma
+
+    @staticmethod
+    def backward(ctx, g):
+        feat, idx, count = ctx.saved_tensors
+        df = torch.zeros_like(feat)
+        if feat.shape[0]:
+            call('srf_density_activation_backward', _ptr(df), _ptr(g.contiguous()), _ptr(feat), _ptr(idx), _ptr(count),
+                 feat.shape[0], ctx.mode, float(ctx.offset), _stream())
+        return df, None, None, None, None, None
+
+
+def density_activation(feat, idx, count, rows, mode, offset):
+    return _DensityActivation.apply(feat.contiguous(), idx, count, rows, mode, offset)
+
+
+class _PosEnc(torch.autograd.Function):
+    """PositionalEncoder.encode (SimpleTensoRF09.py:547-579) with its adjoint."""
+
+    @staticmethod
+    def forward(ctx, x, degree):
+        m, dims = x.shape
+        out = torch.empty(m, dims * (2 * degree + 1), device=x.device)
+        if m:
+            call('srf_positional_encoding', _ptr(out), out.shape[1], _ptr(x), m, dims, degree, _stream())
+        ctx.save_for_backward(x)
+        ctx.degree = degree
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        (x,) = ctx.saved_tensors
+        m, dims = x.shape
+        dx = torch.empty_like(x)
+        if m:
+            g = g.contiguous()
+            call('srf_positional_encoding_backward', _ptr(dx), _ptr(x), _ptr(g), g.shape[1], m, None, dims, ctx.degree,
+                 _stream())
+        return dx, None
+
+
+def positional_encoding(x, degree):
+    return _PosEnc.apply(x.contiguous(), int(degree))
+
+
 def linear(x, weight, bias=None, act=_lib.SRF_ACT_NONE, rows_dev=None):
     """act(x @ weight.T + bias) on the first ``*rows_dev`` rows (all rows when None)."""
     return _LinearFunction.apply(x.contiguous(), weight.contiguous(), None if bias is None else bias.contiguous(), act,

@@ -1,0 +1,556 @@
+"""Drop-in Simple-TensoRF model running on the srf_gb300 CUDA kernels.
+
+``GbSimpleTensoRF(configs, model_configs)`` mirrors ``SimpleTensoRF``
+(src/models/SimpleTensoRF09.py:16-544) with the VM decomposition
+(``VmDecomposedTensor`` :1126-1320): same constructor, forward contract, output
+keys, buffer/parameter names and logical shapes.  The render path runs on the
+hand-written kernels: ray generation, AABB ray marching or stratified NDC
+samples, bbox + alpha-mask validity with stream compaction of the uneven
+per-ray sample lists, VM density/colour gathers from channels-last planes, the
+basis + renderer MLP, and compositing; the backward passes are the adjoint
+kernels (VM gradients are scatter-adds).
+
+Training-time maintenance (alpha-mask rebuild, bbox shrink, grid upsampling,
+optimizer surgery; SimpleTensoRF09.py:821-944) runs every few thousand
+iterations and is written with torch tensor ops on the channels-last views,
+with the dense density evaluation on the VM density kernel.  The CP
+decomposition (``CpDecomposedTensor``) raises NotImplementedError.
+"""
+import numpy
+import torch
+import torch.nn.functional as tF
+from torch.nn import ModuleDict, ModuleList
+
+from . import _lib
+from . import functional as F
+from . import tensorf as T
+from .nerf import ExtrinsicsLearner, IntrinsicsLearner
+
+MATRIX_AXES = [[0, 1], [0, 2], [1, 2]]   # SimpleTensoRF09.py:1131
+VECTOR_AXES = [2, 1, 0]                  # SimpleTensoRF09.py:1132
+
+
+def compute_resolution_in_voxels(num_voxels, bounding_box):
+    """SimpleTensoRF09.py:625-638: cubic voxels filling the box."""
+    lo, hi = bounding_box
+    size = ((hi - lo).prod() / num_voxels).pow(1 / len(lo))
+    return ((hi - lo) / size).long()
+
+
+class AlphaGridMask(torch.nn.Module):
+    """Occupancy volume (SimpleTensoRF09.py:1323-1367); state saved as bool, used as float."""
+
+    def __init__(self, alpha_volume, bounding_box):
+        super().__init__()
+        self.register_buffer('alpha_volume', torch.tensor(0, dtype=torch.bool))
+        self.register_buffer('bounding_box', torch.zeros(2, 3))
+        self.register_buffer('bounding_box_size', torch.zeros(3))
+        self.register_buffer('resolution', torch.zeros(3, dtype=torch.long))
+        self.alpha_volume = alpha_volume.float().view(1, 1, *alpha_volume.shape[-3:])
+        self.bounding_box = bounding_box
+        self.bounding_box_size = self.bounding_box[1] - self.bounding_box[0]
+        d, h, w = alpha_volume.shape[-3:]
+        self.resolution = torch.tensor([w, h, d], dtype=torch.long, device=alpha_volume.device)
+        self._register_state_dict_hook(lambda mod, sd, prefix, *a: sd.__setitem__(
+            f'{prefix}alpha_volume', sd[f'{prefix}alpha_volume'].bool()))
+        self._register_load_state_dict_pre_hook(self._load_hook)
+
+    @staticmethod
+    def _load_hook(sd, prefix, *args, **kwargs):
+        sd[f'{prefix}alpha_volume'] = sd[f'{prefix}alpha_volume'].float()
+
+    def volume(self):
+        return self.alpha_volume.reshape(self.alpha_volume.shape[-3:]).contiguous().float()
+
+    def sample_alpha(self, pts):
+        """Positive/zero occupancy (as float) of world points (:1342-1345 followed by > 0)."""
+        pn = ((pts - self.bounding_box[0]) / self.bounding_box_size) * 2 - 1
+        return T.alpha_mask_query(self.volume(), pn.reshape(-1, 3).contiguous().float()).float()
+
+
+class MlpFeaturesColorPredictor(torch.nn.Module):
+    """SimpleTensoRF09.py:1370-1421: PE(features) + PE(view dirs) -> 128 -> 128 -> 3."""
+
+    def __init__(self, tensor_configs, features_dim, num_units):
+        super().__init__()
+        self.tensor_configs = tensor_configs
+        self.lf = tensor_configs['features_positional_encoding_degree']
+        self.lv = tensor_configs['views_positional_encoding_degree']
+        self.features_dimension = features_dim
+        self.use_view_dirs = tensor_configs['use_view_dirs']
+        self.input_dim = features_dim * (2 * self.lf + 1) + (3 * (2 * self.lv + 1) if self.use_view_dirs else 0)
+        layer1 = torch.nn.Linear(self.input_dim, num_units)
+        layer2 = torch.nn.Linear(num_units, num_units)
+        layer3 = torch.nn.Linear(num_units, 3)
+        self.mlp = torch.nn.Sequential(layer1, torch.nn.ReLU(inplace=True), layer2, torch.nn.ReLU(inplace=True), layer3,
+                                       torch.nn.Sigmoid())
+        torch.nn.init.constant_(self.mlp[-2].bias, 0)
+
+    def forward(self, input_batch):
+        x = T.positional_encoding(input_batch['features'], self.lf)
+        if self.tensor_configs['view_dependent_color']:
+            x = torch.cat([x, T.positional_encoding(input_batch['view_dirs'], self.lv)], -1)
+        h = T.linear(x, self.mlp[0].weight, self.mlp[0].bias, _lib.SRF_ACT_RELU)
+        h = T.linear(h, self.mlp[2].weight, self.mlp[2].bias, _lib.SRF_ACT_RELU)
+        return {'color': T.linear(h, self.mlp[4].weight, self.mlp[4].bias, _lib.SRF_ACT_SIGMOID)}
+
+
+class GbVmTensor(torch.nn.Module):
+    """LowRankTensor + VmDecomposedTensor (SimpleTensoRF09.py:582-961, 1126-1320)."""
+
+    def __init__(self, name, configs, tensor_configs, model_configs):
+        super().__init__()
+        if tensor_configs['decomposition_type'] != 'VectorMatrix':
+            raise NotImplementedError('only the VectorMatrix decomposition runs on the srf_gb300 kernels')
+        if tensor_configs.get('predict_visibility', False):
+            raise NotImplementedError('predict_visibility is not supported')
+        self.name = name
+        self.configs = configs
+        self.tensor_configs = tensor_configs
+        self.model_configs = model_configs
+        self.ndc = configs['data_loader']['ndc']
+        self.predict_visibility = False
+        self.matrix_axes, self.vector_axes = MATRIX_AXES, VECTOR_AXES
+        for b, shape, dt in (('bounding_box', (2, 3), None), ('resolution', (3,), None), ('num_samples', (), 'i'),
+                             ('bounding_box_size', (3,), None), ('voxel_length', (3,), None), ('step_size', (), None)):
+            self.register_buffer(b, torch.zeros(shape) if dt is None else torch.tensor(0))
+        bbox = torch.tensor(tensor_configs.get('bounding_box', model_configs['bounding_box']), dtype=torch.float32)
+        self.update_tensor_params(compute_resolution_in_voxels(tensor_configs['num_voxels_initial'], bbox), bbox)
+        self.alpha_mask = None
+        self.optimizers = None
+        self.matrices_density, self.vectors_density = self.create_decomposed_tensor(
+            tensor_configs['num_components_density'], self.resolution)
+        self.matrices_color, self.vectors_color = self.create_decomposed_tensor(
+            tensor_configs['num_components_color'], self.resolution)
+        self.basis_matrix_color = torch.nn.Linear(sum(tensor_configs['num_components_color']),
+                                                  tensor_configs['features_dimension_color'], bias=False)
+        self.density_mode = {'ReLU': 0, 'SoftPlus': 1}[tensor_configs['density_predictor']]
+        self.density_offset = float(tensor_configs.get('density_offset', 0.0))
+        if tensor_configs['color_predictor'] != 'MLP_Features':
+            raise NotImplementedError(tensor_configs['color_predictor'])
+        self.color_predictor = MlpFeaturesColorPredictor(tensor_configs, tensor_configs['features_dimension_color'],
+                                                         tensor_configs['num_units_color_predictor'])
+        self._register_load_state_dict_pre_hook(self._load_hook)
+
+    # ------------------------------------------------------------ geometry --
+    def update_tensor_params(self, new_resolution, new_bounding_box):
+        """SimpleTensoRF09.py:652-665."""
+        self.bounding_box = new_bounding_box.float()
+        self.bounding_box_size = self.bounding_box[1] - self.bounding_box[0]
+        self.resolution = new_resolution.long()
+        self.voxel_length = self.bounding_box_size / (self.resolution - 1)
+        nvps = self.tensor_configs['num_voxels_per_sample']
+        self.step_size = torch.mean(self.voxel_length) * nvps
+        n = (torch.linalg.norm(self.resolution.float()) / nvps).round().long()
+        self.num_samples = torch.clamp(n, max=int(self.tensor_configs['num_samples_max']))
+
+    def create_decomposed_tensor(self, num_components, resolution, scale=0.1):
+        """Planes (1,R,res[m1],res[m0]) and lines (1,R,res[v],1), stored channels-last."""
+        mats, vecs = [], []
+        for i in range(3):
+            m0, m1 = MATRIX_AXES[i]
+            v = VECTOR_AXES[i]
+            mats.append(torch.nn.Parameter(T.to_channels_last(
+                scale * torch.randn(1, num_components[i], int(resolution[m1]), int(resolution[m0])))))
+            vecs.append(torch.nn.Parameter(T.to_channels_last(
+                scale * torch.randn(1, num_components[i], int(resolution[v]), 1))))
+        return torch.nn.ParameterList(mats), torch.nn.ParameterList(vecs)
+
+    def _grid(self, kind):
+        mats = self.matrices_density if kind == 'density' else self.matrices_color
+        vecs = self.vectors_density if kind == 'density' else self.vectors_color
+        for p in list(mats) + list(vecs):
+            if not p.is_contiguous(memory_format=torch.channels_last):
+                p.data = T.to_channels_last(p.data)
+        return T.VmGridTensors(list(mats), list(vecs), [int(r) for r in self.resolution])
+
+    def get_trainable_parameters(self, optimizer_configs):
+        """SimpleTensoRF09.py:1167-1194."""
+        tensor_params = torch.nn.ParameterList()
+        network_params = torch.nn.ParameterList()
+        tensor_params.extend(self.vectors_density)
+        tensor_params.extend(self.matrices_density)
+        tensor_params.extend(self.vectors_color)
+        tensor_params.extend(self.matrices_color)
+        network_params.extend(self.basis_matrix_color.parameters())
+        network_params.extend(self.color_predictor.parameters())
+        return [{'name': f'{self.name}_tensor_params', 'params': tensor_params,
+                 'lr': optimizer_configs['lr_initial_tensor']},
+                {'name': f'{self.name}_network_params', 'params': network_params,
+                 'lr': optimizer_configs['lr_initial_network']}]
+
+    # ------------------------------------------------------------- forward --
+    def forward(self, input_dict, retraw):
+        """LowRankTensor.forward (SimpleTensoRF09.py:701-761) on the CUDA path."""
+        z = input_dict['z_vals_ndc'] if self.ndc else input_dict['z_vals']
+        o, d = (input_dict['rays_o_ndc'], input_dict['rays_d_ndc']) if self.ndc else \
+            (input_dict['rays_o'], input_dict['rays_d'])
+        n, s = z.shape
+        rows = n * s
+        dev = z.device
+        bbox = self.bounding_box.detach().float().cpu().reshape(-1).tolist()
+        pn = torch.empty(rows, 3, device=dev)
+        mask = torch.empty(rows, dtype=torch.uint8, device=dev)
+        vol = None
+        vd = vh = vw = 0
+        abox = None
+        if self.alpha_mask is not None:
+            vol = self.alpha_mask.volume()
+            vd, vh, vw = vol.shape
+            abox = _lib.host_floats(self.alpha_mask.bounding_box.detach().float().cpu().reshape(-1).tolist())
+        _lib.call('srf_tensorf_sample_mask', F._ptr(o.contiguous()), F._ptr(d.contiguous()), F._ptr(z.contiguous()),
+                  n, s, _lib.host_floats(bbox), F._ptr(vol), vd, vh, vw, abox, F._ptr(pn), F._ptr(mask), F._stream())
+        # density on the valid samples (uneven per ray): compact, gather, VM lookup
+        idx_v, cnt_v = T.compact(mask)
+        nv = int(cnt_v.item())
+        pv = T.gather_rows(pn, idx_v, cnt_v, nv)
+        feat = T.vm_density(self._grid('density'), pv) if nv else torch.zeros(0, device=dev)
+        sigma = T.density_activation(feat, idx_v, cnt_v, rows, self.density_mode, self.density_offset).view(n, s)
+        flags = _lib.SRF_COMPOSITE_NDC if self.ndc else 0
+        zero_rgb = torch.zeros(n, s, 3, device=dev)
+        vr = F.composite(sigma, zero_rgb, z, input_dict['rays_d'], ndc=self.ndc, rays_o=input_dict['rays_o'],
+                         rays_d_ndc=input_dict.get('rays_d_ndc'),
+                         distance_scale=self.tensor_configs['distance_scale'])
+        del flags
+        out = {k: vr[k] for k in ('acc', 'alpha', 'visibility', 'weights', 'depth', 'depth_var')}
+        if self.ndc:
+            out['depth_ndc'], out['depth_var_ndc'] = vr['depth_ndc'], vr['depth_var_ndc']
+        # colour on the surface samples (weights > threshold)
+        w = vr['weights']
+        smask = torch.empty(rows, dtype=torch.uint8, device=dev)
+        _lib.call('srf_threshold_mask', F._ptr(w.detach().contiguous()), rows,
+                  float(self.tensor_configs['ray_marching_weight_threshold']), F._ptr(smask), F._stream())
+        idx_s, cnt_s = T.compact(smask)
+        ns = int(cnt_s.item())
+        if ns:
+            ps = T.gather_rows(pn, idx_s, cnt_s, ns)
+            feats = T.vm_color(self._grid('color'), ps)
+            basis = T.linear(feats, self.basis_matrix_color.weight)
+            cin = {'features': basis}
+            if self.tensor_configs['view_dependent_color']:
+                cin['view_dirs'] = T.gather_rows(input_dict['view_dirs'].contiguous().float(), idx_s, cnt_s, ns, s)
+            rgb_s = self.color_predictor(cin)['color']
+            rgb = T.scatter_rows(rgb_s, idx_s, cnt_s, rows).view(n, s, 3)
+        else:
+            rgb = torch.zeros(n, s, 3, device=dev)
+        rgb_map = T.weighted_sum(w, rgb)
+        if self.configs['model']['white_bkgd'] or (self.training and torch.rand((1,)) < 0.5):
+            rgb_map = rgb_map + (1 - out['acc'][..., None])
+        out['rgb'] = rgb_map
+        if retraw:
+            out['raw_sigma'] = sigma[..., None]
+            out['raw_rgb'] = rgb
+        return out
+
+    def normalize_points(self, pts):
+        """SimpleTensoRF09.py:763-765."""
+        return ((pts - self.bounding_box[0]) / self.bounding_box_size) * 2 - 1
+
+    # ------------------------------------------------ training maintenance --
+    def run_model_modifications(self, iter_num):
+        """SimpleTensoRF09.py:821-830."""
+        if self.training and iter_num in self.tensor_configs['alpha_mask_update_iters']:
+            bbox_new = self.update_alpha_mask(iter_num)
+            if iter_num == self.tensor_configs['alpha_mask_update_iters'][0]:
+                self.shrink_tensor(bbox_new)
+        if self.training and iter_num in self.tensor_configs['tensor_upsampling_iters']:
+            self.upsample_model_resolution(iter_num)
+            self.reconfigure_optimizer()
+
+    def get_new_num_voxels(self, iter_num):
+        """SimpleTensoRF09.py:838-847: log-linear schedule between initial and final voxel counts."""
+        iters = self.tensor_configs['tensor_upsampling_iters']
+        k = iters.index(iter_num) + 1
+        lo = numpy.log(self.tensor_configs['num_voxels_initial'])
+        hi = numpy.log(self.tensor_configs['num_voxels_final'])
+        return int(numpy.round(numpy.exp(lo + (hi - lo) * k / len(iters))))
+
+    def upsample_model_resolution(self, iter_num):
+        res = compute_resolution_in_voxels(self.get_new_num_voxels(iter_num), self.bounding_box)
+        self.update_tensor_params(res, self.bounding_box)
+        self.matrices_density, self.vectors_density = self.resize(self.matrices_density, self.vectors_density,
+                                                                  self.resolution)
+        self.matrices_color, self.vectors_color = self.resize(self.matrices_color, self.vectors_color, self.resolution)
+
+    def resize(self, mats, vecs, res):
+        """Bilinear (align_corners) resampling of planes and lines to a new resolution (:1284-1301)."""
+        new_m, new_v = [], []
+        for i in range(3):
+            m0, m1 = MATRIX_AXES[i]
+            v = VECTOR_AXES[i]
+            new_m.append(torch.nn.Parameter(T.to_channels_last(tF.interpolate(
+                mats[i].data, size=(int(res[m1]), int(res[m0])), mode='bilinear', align_corners=True))))
+            new_v.append(torch.nn.Parameter(T.to_channels_last(tF.interpolate(
+                vecs[i].data, size=(int(res[v]), 1), mode='bilinear', align_corners=True))))
+        return torch.nn.ParameterList(new_m), torch.nn.ParameterList(new_v)
+
+    @torch.no_grad()
+    def compute_alpha(self, xyz, length):
+        """SimpleTensoRF09.py:878-897: 1 - exp(-sigma * length) on world points."""
+        pn = self.normalize_points(xyz).contiguous().float()
+        keep = torch.ones(xyz.shape[0], dtype=torch.uint8, device=xyz.device)
+        if self.alpha_mask is not None:
+            keep = (self.alpha_mask.sample_alpha(xyz) > 0).to(torch.uint8)
+        idx, cnt = T.compact(keep)
+        nv = int(cnt.item())
+        feat = T.vm_density(self._grid('density'), T.gather_rows(pn, idx, cnt, nv)) if nv else \
+            torch.zeros(0, device=xyz.device)
+        sigma = T.density_activation(feat, idx, cnt, xyz.shape[0], self.density_mode, self.density_offset)
+        return 1 - torch.exp(-sigma * length)
+
+    @torch.no_grad()
+    def update_alpha_mask(self, iter_num):
+        """SimpleTensoRF09.py:849-876: dense alpha, 3^3 max-pool, threshold; returns the occupied bbox."""
+        gs = [int(r) for r in self.resolution]
+        dev = self.bounding_box.device
+        t = [torch.linspace(0, 1, g, device=dev) for g in gs]
+        samples = torch.stack(torch.meshgrid(*t, indexing='ij'), -1)
+        xyz = self.bounding_box[0] * (1 - samples) + self.bounding_box[1] * samples
+        alpha = torch.empty(gs, device=dev).view(-1)
+        flat = xyz.view(-1, 3)
+        chunk = 1 << 22
+        for a in range(0, flat.shape[0], chunk):
+            alpha[a:a + chunk] = self.compute_alpha(flat[a:a + chunk], self.step_size)
+        alpha = alpha.view(gs).clamp(0, 1).transpose(0, 2).contiguous()[None, None]
+        xyz = xyz.transpose(0, 2).contiguous()
+        alpha = tF.max_pool3d(alpha, kernel_size=3, padding=1, stride=1).view(gs[::-1])
+        thr = self.tensor_configs['alpha_mask_threshold']
+        alpha = (alpha >= thr).float()
+        self.alpha_mask = AlphaGridMask(alpha, self.bounding_box)
+        valid = xyz[alpha > 0.5]
+        return torch.stack((valid.amin(0), valid.amax(0)))
+
+    @torch.no_grad()
+    def shrink_tensor(self, bbox_new):
+        """SimpleTensoRF09.py:899-914, 1303-1320: crop the grid to the occupied box."""
+        lo, hi = bbox_new
+        t_l = torch.round((lo - self.bounding_box[0]) / self.voxel_length).long()
+        b_r = torch.round((hi - self.bounding_box[0]) / self.voxel_length).long() + 1
+        b_r = torch.stack([b_r, self.resolution]).amin(0)
+        if not torch.equal(self.alpha_mask.resolution, self.resolution):
+            tl_r, br_r = t_l / (self.resolution - 1), (b_r - 1) / (self.resolution - 1)
+            fixed = torch.zeros_like(bbox_new)
+            fixed[0] = (1 - tl_r) * self.bounding_box[0] + tl_r * self.bounding_box[1]
+            fixed[1] = (1 - br_r) * self.bounding_box[0] + br_r * self.bounding_box[1]
+            bbox_new = fixed
+        self.update_tensor_params(b_r - t_l, bbox_new)
+        for plist, vlist in ((self.matrices_density, self.vectors_density), (self.matrices_color, self.vectors_color)):
+            for i in range(3):
+                m0, m1 = MATRIX_AXES[i]
+                v = VECTOR_AXES[i]
+                vlist[i] = torch.nn.Parameter(T.to_channels_last(vlist[i].data[..., t_l[v]:b_r[v], :]))
+                plist[i] = torch.nn.Parameter(T.to_channels_last(
+                    plist[i].data[..., t_l[m1]:b_r[m1], t_l[m0]:b_r[m0]]))
+
+    def reconfigure_optimizer(self):
+        """SimpleTensoRF09.py:916-944: replace this model's param groups in the optimizer."""
+        opt = self.optimizers['optimizer_nerf']
+        cfg = next(c for c in self.configs['optimizers'] if c['name'] == 'optimizer_main')
+        groups = self.get_trainable_parameters(cfg)
+        names = {g['name'] for g in groups}
+        keep = [g for g in opt.param_groups if g.get('name') not in names]
+        dropped = [p for g in opt.param_groups if g.get('name') in names for p in g['params']]
+        for p in dropped:
+            opt.state.pop(p, None)
+        opt.param_groups = keep
+        for g in groups:
+            opt.add_param_group(g)
+
+    def _load_hook(self, sd, prefix, *args, **kwargs):
+        """SimpleTensoRF09.py:946-961, 1196-1212: rebuild the alpha mask and resize the grid
+        to the checkpoint's resolution before the tensors are copied in."""
+        key = f'{prefix}alpha_mask.alpha_volume'
+        if key in sd:
+            self.alpha_mask = AlphaGridMask(sd[key].float(), sd[f'{prefix}alpha_mask.bounding_box'])
+        res = sd.get(f'{prefix}resolution')
+        if res is not None:
+            self.matrices_density, self.vectors_density = self.resize(self.matrices_density, self.vectors_density, res)
+            self.matrices_color, self.vectors_color = self.resize(self.matrices_color, self.vectors_color, res)
+
+
+class GbSimpleTensoRF(torch.nn.Module):
+    """Drop-in for ``SimpleTensoRF`` (src/models/SimpleTensoRF09.py:16)."""
+
+    def __init__(self, configs, model_configs):
+        super().__init__()
+        self.configs = configs
+        self.model_configs = model_configs
+        self.ndc = configs['data_loader']['ndc']
+        self.coarse_model_needed = 'coarse_model' in configs['model']
+        self.fine_model_needed = 'fine_model' in configs['model']
+        self.predict_visibility = False
+        self.nerf_synthetic = configs.get('database') == 'NeRF_Synthetic'
+        if self.nerf_synthetic:
+            raise NotImplementedError('the NeRF-Synthetic camera convention is not supported')
+        self.coarse_model = self.fine_model = None
+        self.augmentations_needed = 'augmentations' in configs['model']
+        if self.augmentations_needed:
+            self.augmented_models = []
+            self.augmented_models_nn = []
+        self.build_nerf()
+        self.optimizers = None
+        self.train_data_preprocessor = None
+
+    def build_nerf(self):
+        m = self.configs['model']
+        if self.coarse_model_needed:
+            self.coarse_model = GbVmTensor('coarse_model', self.configs, m['coarse_model'], self.model_configs)
+        if self.fine_model_needed:
+            self.fine_model = GbVmTensor('fine_model', self.configs, m['fine_model'], self.model_configs)
+        self.intrinsics_learner = IntrinsicsLearner(numpy.array(self.model_configs['intrinsics']),
+                                                    learn_focal=m['learn_camera_focal_length'])
+        self.extrinsics_learner = ExtrinsicsLearner(numpy.array(self.model_configs['extrinsics']),
+                                                    learn_rotation=m['learn_camera_rotation'],
+                                                    learn_translation=m['learn_camera_translation'])
+        if self.augmentations_needed:
+            for aug in m['augmentations']:
+                nn_dict = ModuleDict()
+                entry = {'name': aug['name'], 'coarse_model': None, 'fine_model': None}
+                for key in ('coarse_model', 'fine_model'):
+                    if key in aug:
+                        entry[key] = GbVmTensor(f"{aug['name']}_{key}", self.configs, aug[key], self.model_configs)
+                        nn_dict[key] = entry[key]
+                self.augmented_models.append(entry)
+                self.augmented_models_nn.append(nn_dict)
+            self.augmented_models_nn = ModuleList(self.augmented_models_nn)
+
+    def _models(self):
+        ms = [self.coarse_model, self.fine_model]
+        if self.augmentations_needed:
+            for a in self.augmented_models:
+                ms += [a['coarse_model'], a['fine_model']]
+        return [x for x in ms if x is not None]
+
+    def __setattr__(self, name, value):
+        super().__setattr__(name, value)
+        if name == 'optimizers' and value is not None:
+            for mdl in self._models():
+                mdl.optimizers = value
+
+    def get_trainable_parameters(self, optimizer_configs):
+        params = []
+        for mdl in self._models():
+            params.extend(mdl.get_trainable_parameters(optimizer_configs))
+        return params
+
+    def rebuild_camera_params_learners(self, *, intrinsics=None, extrinsics=None, device):
+        m = self.configs['model']
+        if intrinsics is not None:
+            self.intrinsics_learner = IntrinsicsLearner(intrinsics, m['learn_camera_focal_length']).to(device)
+        if extrinsics is not None:
+            self.extrinsics_learner = ExtrinsicsLearner(extrinsics, m['learn_camera_rotation'],
+                                                        m['learn_camera_translation']).to(device)
+
+    def forward(self, input_batch, *, retraw=False, sec_views_vis=False, mode=None):
+        """SimpleTensoRF09.py:133-162."""
+        input_batch = {k: (dict(v) if isinstance(v, dict) else v) for k, v in input_batch.items()}
+        if 'common_data' in input_batch:
+            for key, val in input_batch['common_data'].items():
+                if isinstance(val, torch.Tensor):
+                    input_batch['common_data'][key] = val[0]
+        if self.training and mode != 'test_camera_params_optimization' and input_batch.get('sub_batch_index') == 0:
+            for mdl in self._models():
+                mdl.run_model_modifications(input_batch['iter_num'])
+        image_id = input_batch['pixel_id'][:, 0]
+        intrinsics = self.intrinsics_learner(image_id)
+        extrinsics = self.extrinsics_learner(image_id)
+        all_ext = self.extrinsics_learner(torch.arange(input_batch['num_frames']).to(image_id))
+        input_batch['intrinsics'], input_batch['extrinsics'] = intrinsics, extrinsics
+        out = {} if mode == 'camera_params_only' else self.render(input_batch, retraw=retraw or self.training,
+                                                                  mode=mode)
+        out['intrinsics'], out['extrinsics'], out['extrinsics_all'] = intrinsics, extrinsics, all_ext
+        return out
+
+    def render(self, input_dict, *, retraw, mode):
+        all_ret = {}
+        n = input_dict['pixel_id'].shape[0]
+        chunk = self.configs['model']['chunk']
+        for i in range(0, n, chunk):
+            sub = {k: (v[i:i + chunk] if isinstance(v, (torch.Tensor, numpy.ndarray)) and v.shape[0] == n else v)
+                   for k, v in input_dict.items()}
+            for k, v in self.render_rays(sub, retraw=retraw, mode=mode).items():
+                all_ret.setdefault(k, []).append(v)
+        return {k: torch.cat(v, 0) for k, v in all_ret.items()}
+
+    def render_rays(self, input_dict, *, retraw, mode):
+        """SimpleTensoRF09.py:194-351."""
+        ret = {}
+        # mip_nerf_used=True (+0.5 px) and the x-flip of origins/directions (:205-207)
+        o, d = F.pixel_rays(input_dict['pixel_id'], input_dict['intrinsics'], input_dict['extrinsics'],
+                            half_pixel=True)
+        flip = torch.tensor([-1.0, 1.0, 1.0], device=o.device)
+        o, d = (o * flip).contiguous(), (d * flip).contiguous()
+        ret['rays_o'], ret['rays_d'] = o, d
+        if self.ndc:
+            k = input_dict['intrinsics'].float()
+            h, w = self.model_configs['resolution']
+            ret['rays_o_ndc'], ret['rays_d_ndc'] = F.ndc_rays(o, d, k[:, 0, 0].contiguous(), k[:, 1, 1].contiguous(),
+                                                              h, w, self.model_configs['near'])
+        m = self.configs['model']
+        if any(m[key]['use_view_dirs'] for key in ('coarse_model', 'fine_model') if key in m):
+            if mode == 'static_camera':
+                raise NotImplementedError('static_camera view directions are not supported for TensoRF')
+            ret['view_dirs'] = F.view_dirs(ret['rays_d_ndc'] if self.ndc else d)
+        train_augs = self.augmentations_needed and self.training and mode != 'test_camera_params_optimization'
+
+        def model_input(z):
+            mi = {'iter_num': input_dict.get('iter_num'), 'z_vals': z, 'rays_o': o, 'rays_d': d}
+            if self.ndc:
+                mi.update({'z_vals_ndc': z, 'rays_o_ndc': ret['rays_o_ndc'], 'rays_d_ndc': ret['rays_d_ndc']})
+            if 'view_dirs' in ret:
+                mi['view_dirs'] = ret['view_dirs']
+            return mi
+
+        weights_c = z_c = None
+        if self.coarse_model_needed:
+            z_c = self.get_z_vals_coarse(input_dict, ret, self.coarse_model)
+            mi = model_input(z_c)
+            outs = self.coarse_model(mi, retraw)
+            weights_c = outs['weights']
+            ret['z_vals_coarse'] = z_c
+            for k, v in outs.items():
+                ret[f'{k}_coarse'] = v
+            if train_augs:
+                for aug in self.augmented_models:
+                    if aug['coarse_model'] is not None:
+                        for k, v in aug['coarse_model'](mi, retraw).items():
+                            ret[f"{aug['name']}_{k}_coarse"] = v
+        if self.fine_model_needed:
+            nf = m['fine_model']['num_samples']
+            u = torch.rand(z_c.shape[0], nf, device=z_c.device) if (m['perturb'] and self.training) else None
+            z_f = F.fine_z(z_c.contiguous(), weights_c.detach(), nf, u)
+            mi = model_input(z_f)
+            outs = self.fine_model(mi, retraw)
+            ret['z_vals_fine'] = z_f
+            for k, v in outs.items():
+                ret[f'{k}_fine'] = v
+            if train_augs:
+                for aug in self.augmented_models:
+                    if aug['fine_model'] is not None:
+                        for k, v in aug['fine_model'](mi, retraw).items():
+                            ret[f"{aug['name']}_{k}_fine"] = v
+        if not retraw:
+            for tag, needed in (('coarse', self.coarse_model_needed), ('fine', self.fine_model_needed)):
+                if needed:
+                    for k in ('z_vals', 'alpha', 'visibility', 'weights'):
+                        ret.pop(f'{k}_{tag}', None)
+        return ret
+
+    def get_z_vals_coarse(self, input_dict, output_dict, tensor_model):
+        """SimpleTensoRF09.py:353-401."""
+        n = input_dict['pixel_id'].shape[0]
+        s = int(tensor_model.num_samples.item())
+        perturb = self.training and self.configs['model']['perturb']
+        dev = input_dict['pixel_id'].device
+        if self.ndc:
+            near, far = self.model_configs['near_ndc'], self.model_configs['far_ndc']
+            u = torch.rand(n, s, device=dev) if perturb else None
+            return F.stratified_z(n, s, near, far, u, lindisp=self.configs['model']['lindisp'], device=dev)
+        near, far = self.model_configs['near'], self.model_configs['far']
+        u = torch.rand(n, device=dev) if perturb else None
+        return F.aabb_z(output_dict['rays_o'], output_dict['rays_d'], s, tensor_model.bounding_box.detach().cpu(),
+                        near, far, float(tensor_model.step_size), u)
+
+
+# ModelFactory02 convention (class name = module name minus the two-digit suffix).
+SimpleTensoRF = GbSimpleTensoRF

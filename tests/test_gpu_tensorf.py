@@ -1,0 +1,104 @@
+"""The drop-in TensoRF VM model (CUDA path) against the reference's own outputs and
+autograd gradients (golden fixture produced by tests/golden/make_golden.py from
+SimpleTensoRF09.LowRankTensor.forward), and against the numpy oracle.
+
+Tolerances: outputs 1e-4 relative (absolute floor 2e-4: a sample whose weight
+sits on the 1e-4 surface threshold may switch sides between implementations and
+moves rgb by at most ~1e-4); parameter gradients 1e-3 relative L2.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+def _tcfg():
+    return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [4, 3, 2],
+            'num_components_color': [6, 5, 4], 'bounding_box': [[-1.5] * 3, [1.5] * 3],
+            'num_voxels_initial': 20 * 22 * 24, 'num_voxels_final': 20 * 22 * 24, 'tensor_upsampling_iters': [],
+            'num_voxels_per_sample': 0.5, 'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4,
+            'ray_marching_weight_threshold': 1e-4, 'use_view_dirs': True, 'view_dependent_color': True,
+            'views_positional_encoding_degree': 2, 'features_positional_encoding_degree': 2,
+            'features_dimension_color': 7, 'density_offset': -10, 'distance_scale': 25, 'density_predictor': 'ReLU',
+            'color_predictor': 'MLP_Features', 'num_units_color_predictor': 16, 'predict_visibility': False}
+
+
+def _model(g):
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300 import tensorf as T
+    from simple_rf_gb300.tensorf_model import AlphaGridMask, GbVmTensor
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
+    tm = GbVmTensor('coarse_model', configs, _tcfg(), {'bounding_box': _tcfg()['bounding_box']})
+    tm.update_tensor_params(torch.tensor(g['res']), torch.tensor(g['bbox']))
+    with torch.no_grad():
+        for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                            ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+            for i in range(3):
+                plist[i] = torch.nn.Parameter(T.to_channels_last(torch.from_numpy(g[f'{kind}.{i}'])[None]))
+        tm.basis_matrix_color.weight.copy_(torch.from_numpy(g['basis_matrix_color.weight']))
+        for k, prm in tm.color_predictor.named_parameters():
+            prm.copy_(torch.from_numpy(g['color_predictor.' + k]))
+    tm = tm.to(DEV)
+    tm.alpha_mask = AlphaGridMask(torch.from_numpy(g['alpha_vol']).to(DEV), torch.tensor(g['bbox']).to(DEV))
+    tm.eval()
+    return tm
+
+
+def test_tensorf_forward_backward_matches_reference_golden(golden):
+    g = golden('tensorf')
+    tm = _model(g)
+    o = torch.from_numpy(g['rays_o']).to(DEV)
+    d = torch.from_numpy(g['rays_d']).to(DEV)
+    z = torch.from_numpy(g['z']).to(DEV)
+    vd = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=True)
+    for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'depth_var'):
+        ref = g['out_' + k]
+        got = out[k].detach().cpu().numpy()
+        np.testing.assert_allclose(got, ref, rtol=1e-4, atol=2e-4 * max(1.0, float(np.abs(ref).max())), err_msg=k)
+    loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'acc'))
+    loss.backward()
+    pairs = []
+    for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                        ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+        for i in range(3):
+            pairs.append((f'{kind}.{i}', plist[i].grad[0]))
+    pairs.append(('basis_matrix_color.weight', tm.basis_matrix_color.weight.grad))
+    for k, prm in tm.color_predictor.named_parameters():
+        pairs.append(('color_predictor.' + k, prm.grad))
+    for name, grad in pairs:
+        ref = g['grad_' + name]
+        got = grad.detach().cpu().numpy()
+        rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert rel < 1e-3, (name, rel)
+
+
+def test_tensorf_aabb_marching_matches_reference(golden):
+    from simple_rf_gb300 import functional as F
+    g = golden('tensorf')
+    z = F.aabb_z(torch.from_numpy(g['rays_o']).to(DEV), torch.from_numpy(g['rays_d']).to(DEV),
+                 int(g['num_samples']), g['bbox'], 0.5, 6.0, float(g['step_size']),
+                 torch.from_numpy(g['u']).to(DEV))
+    np.testing.assert_allclose(z.cpu().numpy(), g['z'], rtol=1e-6, atol=1e-6)
+
+
+def test_tensorf_full_size_grid_gather_roundtrip():
+    """300^3-class grid with R = 16/48 components (the benchmark shape): the VM
+    density gather is linear in the planes, so scaling every plane by 2 doubles
+    the features exactly (size-independent property at full size)."""
+    from simple_rf_gb300 import tensorf as T
+    torch.manual_seed(0)
+    res = [300, 300, 300]
+    planes = [T.to_channels_last(torch.randn(1, 16, 300, 300, device=DEV) * 0.1) for _ in range(3)]
+    lines = [T.to_channels_last(torch.randn(1, 16, 300, 1, device=DEV) * 0.1) for _ in range(3)]
+    pts = torch.rand(1 << 20, 3, device=DEV) * 2 - 1
+    f1 = T.vm_density(T.VmGridTensors(planes, lines, res), pts)
+    f2 = T.vm_density(T.VmGridTensors([p * 2 for p in planes], lines, res), pts)
+    assert torch.equal(f2, 2 * f1)
+    cp = [T.to_channels_last(torch.randn(1, 48, 300, 300, device=DEV) * 0.1) for _ in range(3)]
+    cl = [T.to_channels_last(torch.randn(1, 48, 300, 1, device=DEV) * 0.1) for _ in range(3)]
+    c1 = T.vm_color(T.VmGridTensors(cp, cl, res), pts[:4096])
+    assert c1.shape == (4096, 144) and torch.isfinite(c1).all()
