@@ -245,6 +245,24 @@ int srf_alpha_mask_query(const float* alpha_volume, int vol_d, int vol_h, int vo
 size_t srf_compact_workspace_size(int64_t n);
 int srf_compact(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* count_dev, void* workspace,
                 size_t workspace_bytes, void* stream);
+/* Stream compaction for callers that cannot allocate device memory (no
+ * counterpart in the reference; the reference compacts with torch boolean
+ * indexing).  Same result as srf_compact, but it takes no workspace: its scratch
+ * is a fixed 64 KB array inside the library, present on every GPU that loads it
+ * until the process exits.  Meant for code that runs inside another framework's
+ * fixed memory pool, under a no-allocation guarantee, or behind a binding that
+ * only holds the mask and output pointers.
+ *   - n may not exceed SRF_COMPACT_NOALLOC_MAX_ELEMENTS; larger masks return
+ *     SRF_ERR_SHAPE without launching anything (use srf_compact for those).
+ *   - The first call on a device looks up the array's device address; make that
+ *     first call before any CUDA stream capture on that device.
+ *   - All calls share the one array: calls whose kernels may overlap on the GPU
+ *     (different streams, or different host threads) race and must be ordered by
+ *     the caller.  Each call fully rewrites the scratch it reads. */
+#define SRF_COMPACT_NOALLOC_MAX_BLOCKS 16384
+#define SRF_COMPACT_NOALLOC_MAX_ELEMENTS (SRF_COMPACT_NOALLOC_MAX_BLOCKS * 1024)
+int srf_compact_noalloc(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* count_dev, void* stream);
+
 /* Mask of weights > threshold (surface samples, src/models/SimpleTensoRF09.py:726). */
 int srf_threshold_mask(const float* x, int64_t n, float threshold, uint8_t* mask, void* stream);
 

@@ -83,6 +83,7 @@ _SIGS = {
     'srf_alpha_mask_query': (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
     'srf_compact_workspace_size': (c_size_t, [c_int64]),
     'srf_compact': (c_int, [P, c_int64, P, P, P, c_size_t, P]),
+    'srf_compact_noalloc': (c_int, [P, c_int64, P, P, P]),
     'srf_threshold_mask': (c_int, [P, c_int64, c_float, P, P]),
     'srf_gather_rows': (c_int, [P, P, P, P, c_int64, c_int, c_int, P]),
     'srf_scatter_rows': (c_int, [P, P, P, P, c_int64, c_int, P]),

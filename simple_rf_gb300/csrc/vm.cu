@@ -5,6 +5,8 @@
 // bilinear corner is R contiguous floats: a corner of a 16-component plane is a
 // single 64-byte line, read with 128-bit loads.  One thread handles one
 // (point, plane) pair for the density path, and one point for colour.
+#include <mutex>
+
 #include "srf_common.cuh"
 
 namespace srf {
@@ -476,6 +478,75 @@ extern "C" int srf_compact(const uint8_t* mask, int64_t n, int32_t* idx, int32_t
     scan_counts_kernel<<<1, 1024, 0, s>>>(counts, nb, count_dev);
     if ((st = launch_status())) return st;
     write_idx_kernel<<<nb, kCompactBlock, 0, s>>>(mask, n, counts, idx);
+    return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// Compaction without any caller-provided or library-allocated memory.
+//
+// srf_compact needs a small scratch buffer (one int per 1024 mask elements) that
+// the caller allocates.  Some callers cannot allocate device memory at all: a
+// plugin that runs inside another framework's fixed memory pool, code holding a
+// no-allocation guarantee (a real-time loop where cudaMalloc's implicit device
+// synchronisation is not acceptable), or a thin foreign-language binding that
+// only has the mask and output pointers.  For them the scratch below is a fixed
+// array compiled into this library: every GPU that loads the library keeps
+// these 64 KB until the process exits.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) int g_compact_noalloc_scratch[SRF_COMPACT_NOALLOC_MAX_BLOCKS];
+
+namespace {
+
+// The array's name is only a host-side handle in host code; the device address
+// comes from cudaGetSymbolAddress, looked up once per device with that device
+// current and cached.
+int* compact_noalloc_scratch(int* status) {
+    static std::mutex mu;
+    static int* cache[64] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) {
+        if (e != cudaSuccess) set_cuda_error(e);
+        *status = SRF_ERR_CUDA;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cache[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_compact_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_cuda_error(e);
+            *status = SRF_ERR_CUDA;
+            return nullptr;
+        }
+        cache[dev] = static_cast<int*>(p);
+    }
+    *status = SRF_OK;
+    return cache[dev];
+}
+
+}  // namespace
+
+extern "C" int srf_compact_noalloc(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* count_dev, void* stream) {
+    if (!mask || !idx || !count_dev) return SRF_ERR_NULL;
+    if (n < 0 || n > int64_t(SRF_COMPACT_NOALLOC_MAX_ELEMENTS)) return SRF_ERR_SHAPE;
+    cudaStream_t s = as_stream(stream);
+    if (n == 0) {
+        cudaError_t e = cudaMemsetAsync(count_dev, 0, sizeof(int32_t), s);
+        if (e != cudaSuccess) set_cuda_error(e);
+        return e == cudaSuccess ? SRF_OK : SRF_ERR_CUDA;
+    }
+    int st = SRF_OK;
+    int* scratch = compact_noalloc_scratch(&st);
+    if (!scratch) return st;
+    // Each call writes every scratch entry it later reads (one count per block,
+    // then the in-place scan), so leftovers of an earlier call never leak in.
+    int nb = int((n + kCompactBlock - 1) / kCompactBlock);
+    count_kernel<<<nb, kCompactBlock, 0, s>>>(mask, n, scratch);
+    if ((st = launch_status())) return st;
+    scan_counts_kernel<<<1, 1024, 0, s>>>(scratch, nb, count_dev);
+    if ((st = launch_status())) return st;
+    write_idx_kernel<<<nb, kCompactBlock, 0, s>>>(mask, n, scratch, idx);
     return launch_status();
 }
 
