@@ -65,7 +65,9 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
 
 __global__ void counter_add_kernel(int* c, int v) { *c += v; }
 
-// pts[r * S + i] = o[r] + d[r] * z[r, i]  (SimpleNeRF17.py:213-215)
+// pts[r * S + i] = o[r] + d[r] * z[r, i]  (SimpleNeRF17.py:213-215).  The product
+// and the sum round separately, as the reference's two torch ops do: PE scales
+// pts by up to 2^9, so a one-ulp difference here moves the network's output.
 __global__ void ray_points_kernel(const float* __restrict__ o, const float* __restrict__ d,
                                   const float* __restrict__ z, int64_t n, int s, float* pts) {
     int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -73,7 +75,7 @@ __global__ void ray_points_kernel(const float* __restrict__ o, const float* __re
     int64_t r = idx / s;
     float zz = z[idx];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) pts[3 * idx + a] = o[3 * r + a] + d[3 * r + a] * zz;
+    for (int a = 0; a < 3; ++a) pts[3 * idx + a] = __fadd_rn(o[3 * r + a], __fmul_rn(d[3 * r + a], zz));
 }
 
 }  // namespace

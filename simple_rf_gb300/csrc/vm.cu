@@ -214,17 +214,20 @@ __global__ void sample_mask_kernel(const float* __restrict__ o, const float* __r
     float zz = z[idx];
     float q[3];
     bool inside = true;
+    // products and sums round separately, like the reference's torch ops
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        q[a] = o[3 * r + a] + dir[3 * r + a] * zz;   // SimpleTensoRF09.py:261
+        q[a] = __fadd_rn(o[3 * r + a], __fmul_rn(dir[3 * r + a], zz));   // SimpleTensoRF09.py:261
         inside = inside && box.lo[a] <= q[a] && q[a] <= box.hi[a];
     }
 #pragma unroll
-    for (int a = 0; a < 3; ++a) pn[3 * idx + a] = ((q[a] - box.lo[a]) / (box.hi[a] - box.lo[a])) * 2.f - 1.f;
+    for (int a = 0; a < 3; ++a)
+        pn[3 * idx + a] = __fsub_rn(__fmul_rn((q[a] - box.lo[a]) / (box.hi[a] - box.lo[a]), 2.f), 1.f);
     if (inside && vol) {
         float an[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) an[a] = ((q[a] - abox.lo[a]) / (abox.hi[a] - abox.lo[a])) * 2.f - 1.f;
+        for (int a = 0; a < 3; ++a)
+            an[a] = __fsub_rn(__fmul_rn((q[a] - abox.lo[a]) / (abox.hi[a] - abox.lo[a]), 2.f), 1.f);
         inside = alpha_positive(vol, vd, vh, vw, an[0], an[1], an[2]);
     }
     mask[idx] = inside;

@@ -231,6 +231,42 @@ class NerfTrainStep:
                 for k in ('rgb_map', 'acc', 'depth', 'depth_var', 'weights', 'z')}
 
 
+def main(argv=None):
+    """Run the fused training step on synthetic config-2 data and print ms/step:
+
+        python -m simple_rf_gb300.train_step --rays 4096 --steps 10 --warmup 3 [--precision fp32] [--eager]
+    """
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--rays', type=int, default=4096)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--precision', default='bf16', choices=['bf16', 'fp32'])
+    ap.add_argument('--eager', action='store_true', help='launch kernels directly instead of replaying a CUDA graph')
+    args = ap.parse_args(argv)
+    from . import build as _build
+    _build.build()
+    dev = torch.device('cuda')
+    step = NerfTrainStep(args.rays, 64, 128, precision=args.precision, device=dev)
+    step.set_batch(*synthetic_batch(args.rays, 64, 128, seed=1, device=dev))
+    if not args.eager:
+        step.capture(warmup=1)
+    for _ in range(args.warmup):
+        step.step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step.step()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    print(json.dumps({'rays': args.rays, 'precision': args.precision, 'graph': not args.eager,
+                      'ms_per_step': round(ms, 4), 'rays_per_s': round(args.rays / ms * 1e3, 1),
+                      'loss': float(step.loss.item())}))
+
+
 def synthetic_batch(n_rays, n_coarse, n_fine, seed, device='cpu', pin=False):
     """Config-2 synthetic inputs: o ~ N(0, 0.1^2), d = normalize(N(0, I)), rgb
     targets ~ U[0,1]^3, depth targets ~ U[2,6], stratified/pdf uniforms ~ U[0,1)."""
@@ -248,3 +284,7 @@ def synthetic_batch(n_rays, n_coarse, n_fine, seed, device='cpu', pin=False):
     if str(device) != 'cpu':
         out = [x.to(device) for x in out]
     return out
+
+
+if __name__ == '__main__':
+    main()
