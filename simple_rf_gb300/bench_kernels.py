@@ -1,0 +1,122 @@
+"""Kernel-level benchmarks of the hot-path kernels, one launch shape at a time.
+
+    python -m simple_rf_gb300.bench_kernels gemm --m 786432 --k 256 --n 256
+    python -m simple_rf_gb300.bench_kernels wgrad --m 786432 --n 256 --k 256
+    python -m simple_rf_gb300.bench_kernels composite --rays 4096 --samples 192
+
+Each prints one JSON line: the average launch time over --reps launches
+(CUDA events on the launching stream, after --warmup launches) and the achieved
+FLOP/s and algorithmic bytes/s.  With --reps 1 --warmup 0 it launches the kernel
+exactly once (for profilers).
+"""
+import argparse
+import ctypes
+import json
+
+import torch
+
+from . import _lib
+
+_P = ctypes.c_void_p
+
+
+def _p(t):
+    return None if t is None else _P(t.data_ptr())
+
+
+def _st():
+    return _P(torch.cuda.current_stream().cuda_stream)
+
+
+def _time(fn, reps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / max(reps, 1)
+
+
+def gemm(args):
+    m, k, n = args.m, args.k, args.n
+    g = torch.Generator(device='cuda').manual_seed(0)
+    x = torch.randn(m, k, device='cuda', generator=g).to(torch.bfloat16)
+    w = (torch.randn(n, k, device='cuda', generator=g) * 0.05).to(torch.bfloat16)
+    b = torch.zeros(n, device='cuda')
+    y = torch.empty(m, n, device='cuda', dtype=torch.bfloat16)
+
+    def run():
+        _lib.call('srf_bf16_linear', _p(y), n, _p(x), k, k, None, 0, 0, _p(w), k, n, 0, _p(b), m, n, 1, None, 0, None,
+                  _st())
+    t = _time(run, args.reps, args.warmup)
+    flops = 2.0 * m * n * k
+    nbytes = (m * k + m * n + n * k) * 2
+    return {'kernel': 'tc_gemm_kernel', 'm': m, 'k': k, 'n': n, 'ms': t * 1e3, 'tflops': flops / t / 1e12,
+            'gbs': nbytes / t / 1e9, 'bytes': nbytes}
+
+
+def wgrad(args):
+    m, k, n = args.m, args.k, args.n
+    lib = _lib.load()
+    g = torch.Generator(device='cuda').manual_seed(0)
+    dz = torch.randn(m, n, device='cuda', generator=g).to(torch.bfloat16)
+    x = torch.randn(m, k, device='cuda', generator=g).to(torch.bfloat16)
+    nb = lib.srf_bf16_wgrad_workspace_size(n, k)
+    part = torch.empty(nb // 4, device='cuda')
+    sp = ctypes.c_int()
+
+    def run():
+        _lib.call('srf_bf16_wgrad', _p(part), nb, ctypes.byref(sp), _p(dz), n, n, _p(x), k, k, None, 0, 0, m, _st())
+    t = _time(run, args.reps, args.warmup)
+    flops = 2.0 * m * n * k
+    nbytes = (m * n + m * k) * 2 + sp.value * n * k * 4
+    return {'kernel': 'tc_wgrad_kernel', 'm': m, 'k': k, 'n': n, 'splits': sp.value, 'ms': t * 1e3,
+            'tflops': flops / t / 1e12, 'gbs': nbytes / t / 1e9, 'bytes': nbytes}
+
+
+def composite(args):
+    nr, s = args.rays, args.samples
+    g = torch.Generator(device='cuda').manual_seed(0)
+    sigma = torch.rand(nr, s, device='cuda', generator=g)
+    rgb = torch.rand(nr, s, 3, device='cuda', generator=g)
+    z = torch.sort(torch.rand(nr, s, device='cuda', generator=g) * 4 + 2, 1)[0]
+    d = torch.randn(nr, 3, device='cuda', generator=g)
+    outs = {k: torch.empty(nr, 3 if k == 'rgb_map' else 1, device='cuda') for k in ('rgb_map', 'acc', 'depth', 'dv')}
+    w = torch.empty(nr, s, device='cuda')
+    a = _lib.CompositeArgs()
+    a.n_rays, a.n_samples, a.flags, a.distance_scale = nr, s, _lib.SRF_COMPOSITE_WHITE_BKGD, 1.0
+    a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), d.data_ptr()
+    a.rgb_map, a.acc, a.depth, a.depth_var, a.weights = (outs['rgb_map'].data_ptr(), outs['acc'].data_ptr(),
+                                                         outs['depth'].data_ptr(), outs['dv'].data_ptr(), w.data_ptr())
+
+    def run():
+        _lib.call('srf_composite_forward', ctypes.byref(a), _st())
+    t = _time(run, args.reps, args.warmup)
+    nbytes = nr * s * (4 + 12 + 4 + 4) + nr * (12 + 12)
+    return {'kernel': 'composite_fwd_kernel', 'rays': nr, 'samples': s, 'ms': t * 1e3, 'gbs': nbytes / t / 1e9,
+            'bytes': nbytes}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument('which', choices=['gemm', 'wgrad', 'composite'])
+    ap.add_argument('--m', type=int, default=786432)
+    ap.add_argument('--k', type=int, default=256)
+    ap.add_argument('--n', type=int, default=256)
+    ap.add_argument('--rays', type=int, default=4096)
+    ap.add_argument('--samples', type=int, default=192)
+    ap.add_argument('--reps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    args = ap.parse_args(argv)
+    from . import build as _build
+    _build.build()
+    res = {'gemm': gemm, 'wgrad': wgrad, 'composite': composite}[args.which](args)
+    print(json.dumps({k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.items()}))
+
+
+if __name__ == '__main__':
+    main()
