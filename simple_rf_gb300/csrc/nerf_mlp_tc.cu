@@ -1,6 +1,7 @@
 // BF16 tensor-core (tcgen05) path of the NeRF MLP: FP32 master weights, BF16
-// activations in HBM, FP32 accumulation in tensor memory.  PE sin/cos and the
-// small heads (sigma: 1 output, rgb: 3 outputs) stay in FP32 SIMT kernels.
+// activations in HBM, FP32 accumulation in tensor memory.  PE sin/cos is
+// computed in FP32; the small heads (sigma: 1 output, rgb: 3 outputs) are FP32
+// dot products fused into the epilogue of the layer that feeds them.
 //
 // Forward per layer: one persistent tcgen05 GEMM with the bias/ReLU epilogue.
 // Backward per layer: a dgrad GEMM (dZ . W^T with the ReLU mask of the forward
@@ -88,19 +89,32 @@ int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
 
 }  // namespace
 
-// out[m, :n] = epilogue(x0[m, :k0] . B0^T + x1[m, :k1] . B1^T) with B the rows
+tc::GemmEpilogue make_epilogue(bf16* out, int64_t ld_out, const float* bias, int relu) {
+    tc::GemmEpilogue ep{};
+    ep.out = out;
+    ep.ld_out = ld_out;
+    ep.bias = bias;
+    ep.relu = relu;
+    ep.head_mode = tc::kHeadNone;
+    ep.flag = device_flag();
+    return ep;
+}
+
+// ep.out[m, :n] = epilogue(x0[m, :k0] . B0^T + x1[m, :k1] . B1^T) with B the rows
 // [w_row0, w_row0 + n) of the BF16 matrix w (w_rows x ldw, K-major).
-int tc_linear(bf16* out, int64_t ld_out, const bf16* x0, int64_t ld0, int k0, const bf16* x1, int64_t ld1, int k1,
-              const bf16* w, int64_t ldw, int w_rows, int w_row0, int64_t M, int n, const float* bias, int relu,
-              const bf16* mask, int64_t ld_mask, const float* r1_row, const float* r1_col, float* colsum,
-              cudaStream_t s) {
+int tc_linear(const tc::GemmEpilogue& ep, const bf16* x0, int64_t ld0, int k0, const bf16* x1, int64_t ld1, int k1,
+              const bf16* w, int64_t ldw, int w_rows, int w_row0, int64_t M, int n, cudaStream_t s) {
+    const bf16* mask = ep.mask;
+    const int64_t ld_out = ep.ld_out, ld_mask = ep.ld_mask;
     if (M <= 0) return SRF_OK;
-    if (!out || !x0 || !w) return SRF_ERR_NULL;
+    if (!ep.out || !x0 || !w) return SRF_ERR_NULL;
+    if (ep.head_mode && (!ep.head_w || !ep.head_b)) return SRF_ERR_NULL;
+    if (ep.r1_mask_colsum && !mask) return SRF_ERR_NULL;
     if ((k0 % 64) || (k1 % 64) || k0 <= 0 || (k1 && !x1)) return SRF_ERR_SHAPE;
     if (n != 64 && n != 128 && n != 256) return SRF_ERR_UNSUPPORTED;
     if (w_row0 < 0 || w_row0 + n > w_rows || ldw < k0 + k1) return SRF_ERR_SHAPE;
     if (ld_out < n || ld0 < k0 || (x1 && ld1 < k1) || (mask && ld_mask < n)) return SRF_ERR_SHAPE;
-    if (!ok16(out) || !ok16(x0) || !ok16(w) || (x1 && !ok16(x1)) || (mask && !ok16(mask))) return SRF_ERR_ALIGN;
+    if (!ok16(ep.out) || !ok16(x0) || !ok16(w) || (x1 && !ok16(x1)) || (mask && !ok16(mask))) return SRF_ERR_ALIGN;
     if ((ld_out % 8) || (ld0 % 8) || (ldw % 8) || (x1 && (ld1 % 8)) || (mask && (ld_mask % 8))) return SRF_ERR_ALIGN;
     CUtensorMap ma0, ma1, mb;
     if (!make_map(&ma0, x0, uint64_t(k0), uint64_t(M), uint64_t(ld0) * 2, 64, tc::kBlockM)) return SRF_ERR_CUDA;
@@ -112,7 +126,6 @@ int tc_linear(bf16* out, int64_t ld_out, const bf16* x0, int64_t ld0, int k0, co
     if (!make_map(&mb, w, uint64_t(k0 + k1), uint64_t(w_rows), uint64_t(ldw) * 2, 64, uint32_t(n)))
         return SRF_ERR_CUDA;
     tc::GemmShape sh{M, k0 / 64, k1 / 64, w_row0};
-    tc::GemmEpilogue ep{bias, relu, mask, ld_mask, r1_row, r1_col, out, ld_out, colsum, device_flag()};
     switch (n) {
         case 64: return launch_gemm_bn<64>(ma0, ma1, mb, sh, ep, s);
         case 128: return launch_gemm_bn<128>(ma0, ma1, mb, sh, ep, s);
@@ -220,157 +233,162 @@ __global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partia
     grad[int64_t(n) * L.kref() + rc] += acc;
 }
 
-// enc[m] = PE(pts[m], Lp) zero-padded to enc_w; vext[m] = [PE cols pin..ppe, PE(dirs[m/div], Lv)] padded.
+// Column `col` of PE(x) = [x, sin(2^0 x), cos(2^0 x), ...] for a 3-vector x.
+__device__ __forceinline__ float pe_column(const float (&x)[3], int col) {
+    int j = col % 3, b = col / 3;
+    if (b == 0) return x[j];
+    int k = (b - 1) >> 1;
+    float a = x[j] * float(1 << k);
+    return ((b - 1) & 1) ? cosf(a) : sinf(a);
+}
+
+// enc[m] = PE(pts[m], Lp)[:pin] zero-padded to enc_w; vext[m] = [PE(pts[m])[pin:ppe],
+// PE(dirs[m/div], Lv)] zero-padded to vx_w.  One thread writes one 16-byte chunk
+// (8 BF16 columns) of a row, so a warp stores whole contiguous rows.
 __global__ void encode_bf16_kernel(const float* __restrict__ pts, const float* __restrict__ dirs, int div, int64_t M,
                                    int lp, int lv, int pin, int enc_w, int vx_w, bf16* enc, bf16* vext) {
-    int64_t m = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (m >= M) return;
-    float p[3] = {pts[3 * m], pts[3 * m + 1], pts[3 * m + 2]};
-    int ppe = 3 * (2 * lp + 1);
-    bf16* e = enc + m * enc_w;
-    bf16* v = vext ? vext + m * vx_w : nullptr;
-    auto put = [&](int col, float val) {
-        if (col < pin) e[col] = __float2bfloat16_rn(val);
-        else {
-            e[col] = __float2bfloat16_rn(0.f);
-            if (v) v[col - pin] = __float2bfloat16_rn(val);
+    const int ce = enc_w / 8, cv = vext ? vx_w / 8 : 0, per = ce + cv;
+    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= M * per) return;
+    int64_t m = t / per;
+    int chunk = int(t % per);
+    const int ppe = 3 * (2 * lp + 1);
+    const float p[3] = {pts[3 * m], pts[3 * m + 1], pts[3 * m + 2]};
+    float v[8];
+    if (chunk < ce) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            int col = chunk * 8 + i;
+            v[i] = col < pin ? pe_column(p, col) : 0.f;
         }
-    };
-    for (int j = 0; j < 3; ++j) put(j, p[j]);
-    float f = 1.f;
-    for (int k = 0; k < lp; ++k) {
-        for (int j = 0; j < 3; ++j) {
-            float a = p[j] * f;
-            put(3 * (1 + 2 * k) + j, sinf(a));
-            put(3 * (2 + 2 * k) + j, cosf(a));
+    } else {
+        const int c0 = ppe - pin;   // extra PE columns of the points-augmentation variant
+        const int vpe = dirs ? 3 * (2 * lv + 1) : 0;
+        float q[3] = {0.f, 0.f, 0.f};
+        if (dirs) {
+            const float* d = dirs + 3 * (m / div);
+            q[0] = d[0];
+            q[1] = d[1];
+            q[2] = d[2];
         }
-        f *= 2.f;
-    }
-    for (int c = ppe; c < enc_w; ++c) e[c] = __float2bfloat16_rn(0.f);
-    if (!v) return;
-    int c0 = ppe - pin;
-    int vpe = 0;
-    if (dirs) {
-        const float* d = dirs + 3 * (m / div);
-        float q[3] = {d[0], d[1], d[2]};
-        vpe = 3 * (2 * lv + 1);
-        for (int j = 0; j < 3; ++j) v[c0 + j] = __float2bfloat16_rn(q[j]);
-        float g = 1.f;
-        for (int k = 0; k < lv; ++k) {
-            for (int j = 0; j < 3; ++j) {
-                float a = q[j] * g;
-                v[c0 + 3 * (1 + 2 * k) + j] = __float2bfloat16_rn(sinf(a));
-                v[c0 + 3 * (2 + 2 * k) + j] = __float2bfloat16_rn(cosf(a));
-            }
-            g *= 2.f;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            int col = (chunk - ce) * 8 + i;
+            v[i] = col < c0 ? pe_column(p, pin + col) : (col < c0 + vpe ? pe_column(q, col - c0) : 0.f);
         }
     }
-    for (int c = c0 + vpe; c < vx_w; ++c) v[c] = __float2bfloat16_rn(0.f);
+    uint4 packed = make_uint4(tc::pack_bf16(v[0], v[1]), tc::pack_bf16(v[2], v[3]), tc::pack_bf16(v[4], v[5]),
+                              tc::pack_bf16(v[6], v[7]));
+    bf16* dst = chunk < ce ? enc + m * enc_w + chunk * 8 : vext + m * vx_w + (chunk - ce) * 8;
+    *reinterpret_cast<uint4*>(dst) = packed;
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
+// Backward of a small head (1-4 outputs) fused with what consumes it, in one
+// pass over the head's input activation h (BF16, M x K):
+//   g[m]       = head output gradients (mode 3: rgb; mode 4: sigma + rgb), through
+//                the ReLU of the raw sigma and the sigmoid of rgb;
+//   dz[m, k]   = (sum_u g[m, u] W[u, k]) * (h[m, k] > 0)   (BF16, the previous layer's dZ)
+//   colsum[k] += sum_m dz[m, k]                           (that layer's bias gradient)
+//   dW[u, k]  += sum_m g[m, u] h[m, k];  db[u] += sum_m g[m, u]  (the head's own gradients)
+// One thread owns 8 consecutive columns (a 16-byte chunk) of a row; a block
+// covers rows_per_block rows and strides over the rest, keeping its partial
+// sums in registers until one shared-memory reduction at the end.
+template <int NO>
+__global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict__ dsigma,
+                                      const float* __restrict__ sraw, const float* __restrict__ drgb,
+                                      const float* __restrict__ rgb, const float* __restrict__ W,
+                                      const bf16* __restrict__ h, bf16* dz, float* colsum, float* dW, float* db) {
+    extern __shared__ float red[];
+    const int cpr = K / 8;
+    const int rpb = blockDim.x / cpr;
+    const int chunk = threadIdx.x % cpr, rloc = threadIdx.x / cpr;
+    float w[NO][8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Heads on BF16 activations; one warp per row.  mode 0: sigma (1 output),
-// 1: rgb (3), 2: sigma + rgb (4).
-__global__ void head_fwd_bf16_kernel(int64_t M, int K, const bf16* __restrict__ h, const float* __restrict__ W,
-                                     const float* __restrict__ b, int mode, const float* __restrict__ noise,
-                                     float* sraw, float* sigma, float* rgb_ws, float* rgb_out) {
-    int lane = threadIdx.x & 31;
-    int64_t row = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (row >= M) return;
-    int no = mode == 0 ? 1 : (mode == 1 ? 3 : 4);
-    float d[4] = {0.f, 0.f, 0.f, 0.f};
-    const bf16* hr = h + row * K;
-    for (int k0 = lane * 8; k0 < K; k0 += 256) {
-        uint4 raw = *reinterpret_cast<const uint4*>(hr + k0);
-        uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+    for (int u = 0; u < NO; ++u)
 #pragma unroll
-        for (int g = 0; g < 4; ++g) {
-            float2 x = tc::unpack_bf16(w4[g]);
+        for (int i = 0; i < 8; ++i) w[u][i] = W[u * K + chunk * 8 + i];
+    float cs[8], dwl[NO][8], dbl[NO];
 #pragma unroll
-            for (int n = 0; n < 4; ++n)
-                if (n < no) d[n] += x.x * W[int64_t(n) * K + k0 + 2 * g] + x.y * W[int64_t(n) * K + k0 + 2 * g + 1];
+    for (int i = 0; i < 8; ++i) {
+        cs[i] = 0.f;
+#pragma unroll
+        for (int u = 0; u < NO; ++u) dwl[u][i] = 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < NO; ++u) dbl[u] = 0.f;
+    for (int64_t r = int64_t(blockIdx.x) * rpb + rloc; r < M; r += int64_t(gridDim.x) * rpb) {
+        float g[NO];
+        int u0 = 0;
+        if (NO == 4) {
+            g[0] = sraw[r] > 0.f ? dsigma[r] : 0.f;
+            u0 = 1;
         }
-    }
 #pragma unroll
-    for (int n = 0; n < 4; ++n) d[n] = warp_sum(d[n]);
-    if (lane != 0) return;
-    int c0 = 0;
-    if (mode != 1) {
-        float s = d[0] + b[0];
-        if (noise) s += noise[row];
-        sraw[row] = s;
-        sigma[row] = s > 0.f ? s : 0.f;
-        c0 = 1;
-    }
-    if (mode != 0) {
         for (int c = 0; c < 3; ++c) {
-            float v = 1.f / (1.f + expf(-(d[c0 + c] + b[c0 + c])));
-            rgb_ws[3 * row + c] = v;
-            rgb_out[3 * row + c] = v;
+            float v = rgb[3 * r + c];
+            g[u0 + c] = drgb[3 * r + c] * v * (1.f - v);
         }
-    }
-}
-
-// Head adjoint: g = [dsigma*(sraw>0)] and/or [drgb * rgb * (1 - rgb)] -> dout (M x 4);
-// when dz != NULL also dz[m, :] = (g . W) * (h > 0) (BF16) with its column sums.
-// Threads over columns, rows looped in chunks of `rows`.
-__global__ void head_bwd_bf16_kernel(int64_t M, int K, int mode, const float* __restrict__ dsigma,
-                                     const float* __restrict__ drgb, const float* __restrict__ sraw,
-                                     const float* __restrict__ rgb, const float* __restrict__ W,
-                                     const bf16* __restrict__ h, bf16* dz, float* colsum, float* dout, float* dsig,
-                                     int64_t rows) {
-    int64_t r0 = int64_t(blockIdx.x) * rows;
-    int64_t r1 = r0 + rows < M ? r0 + rows : M;
-    float cs[2] = {0.f, 0.f};
-    for (int64_t r = r0; r < r1; ++r) {
-        float g[4] = {0.f, 0.f, 0.f, 0.f};
-        int no = 0;
-        if (mode != 1) g[no++] = sraw[r] > 0.f ? dsigma[r] : 0.f;
-        if (mode != 0)
-            for (int c = 0; c < 3; ++c) {
-                float v = rgb[3 * r + c];
-                g[no++] = drgb[3 * r + c] * v * (1.f - v);
-            }
-        if (threadIdx.x < 4) dout[r * 4 + threadIdx.x] = int(threadIdx.x) < no ? g[threadIdx.x] : 0.f;
-        if (dsig && threadIdx.x == 0) dsig[r] = g[0];
-        if (!dz) continue;
-        for (int k = threadIdx.x, i = 0; k < K; k += blockDim.x, ++i) {
-            float v = 0.f;
-            for (int n = 0; n < no; ++n) v += g[n] * W[int64_t(n) * K + k];
-            if (!(__bfloat162float(h[r * K + k]) > 0.f)) v = 0.f;
-            dz[r * K + k] = __float2bfloat16_rn(v);
-            cs[i & 1] += v;
-        }
-    }
-    if (dz && colsum)
-        for (int k = threadIdx.x, i = 0; k < K; k += blockDim.x, ++i) atomicAdd(colsum + k, cs[i & 1]);
-}
-
-// dW (no x K) += dout^T h ; db += colsum(dout) for heads with no <= 4 outputs.
-__global__ void head_dw_bf16_kernel(int64_t M, int K, int no, const float* __restrict__ dout,
-                                    const bf16* __restrict__ h, float* dw, float* db, int64_t rows) {
-    int64_t r0 = int64_t(blockIdx.x) * rows;
-    int64_t r1 = r0 + rows < M ? r0 + rows : M;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int64_t r = r0; r < r1; ++r) {
-            float x = __bfloat162float(h[r * K + k]);
+        uint4 raw = *reinterpret_cast<const uint4*>(h + r * K + chunk * 8);
+        uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+        float hx[8];
 #pragma unroll
-            for (int n = 0; n < 4; ++n)
-                if (n < no) acc[n] += dout[r * 4 + n] * x;
+        for (int q = 0; q < 4; ++q) {
+            float2 f = tc::unpack_bf16(w4[q]);
+            hx[2 * q] = f.x;
+            hx[2 * q + 1] = f.y;
         }
-        for (int n = 0; n < no; ++n) atomicAdd(dw + int64_t(n) * K + k, acc[n]);
+        float o[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            float v = 0.f;
+#pragma unroll
+            for (int u = 0; u < NO; ++u) {
+                v += g[u] * w[u][i];
+                dwl[u][i] += g[u] * hx[i];
+            }
+            o[i] = hx[i] > 0.f ? v : 0.f;
+            cs[i] += o[i];
+        }
+        *reinterpret_cast<uint4*>(dz + r * K + chunk * 8) =
+            make_uint4(tc::pack_bf16(o[0], o[1]), tc::pack_bf16(o[2], o[3]), tc::pack_bf16(o[4], o[5]),
+                       tc::pack_bf16(o[6], o[7]));
+        if (chunk == 0) {
+#pragma unroll
+            for (int u = 0; u < NO; ++u) dbl[u] += g[u];
+        }
     }
-    if (threadIdx.x < unsigned(no)) {
-        float s = 0.f;
-        for (int64_t r = r0; r < r1; ++r) s += dout[r * 4 + threadIdx.x];
-        atomicAdd(db + threadIdx.x, s);
+    // block reduction over the rloc rows, one quantity (K floats) at a time
+    auto reduce = [&](const float (&vals)[8], float* dst) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) red[rloc * K + chunk * 8 + i] = vals[i];
+        __syncthreads();
+        for (int k = threadIdx.x; k < K; k += blockDim.x) {
+            float s = 0.f;
+            for (int rr = 0; rr < rpb; ++rr) s += red[rr * K + k];
+            atomicAdd(dst + k, s);
+        }
+        __syncthreads();
+    };
+    if (colsum) reduce(cs, colsum);
+#pragma unroll
+    for (int u = 0; u < NO; ++u) reduce(dwl[u], dW + u * K);
+    if (chunk == 0) {
+#pragma unroll
+        for (int u = 0; u < NO; ++u) atomicAdd(db + u, dbl[u]);
     }
+}
+
+template <int NO>
+int head_bwd_fused(int64_t M, int K, const float* dsigma, const float* sraw, const float* drgb, const float* rgb,
+                   const float* W, const bf16* h, bf16* dz, float* colsum, float* dW, float* db, cudaStream_t s) {
+    const int threads = 256;
+    const int rpb = threads / (K / 8);
+    int64_t blocks = (M + rpb - 1) / rpb;
+    if (blocks > int64_t(num_sms()) * 8) blocks = int64_t(num_sms()) * 8;
+    if (blocks < 1) blocks = 1;
+    head_bwd_fused_kernel<NO><<<unsigned(blocks), threads, size_t(rpb) * K * sizeof(float), s>>>(
+        M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum, dW, db);
+    return launch_status();
 }
 
 int pad64(int x) { return (x + 63) / 64 * 64; }
@@ -513,45 +531,55 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
         for (int j = 0; j < L.Dv; ++j)
             if ((st = pack(T.view[j], P[L.idx_view_w(j)], w.Wv[j], w.WTv[j], s))) return st;
     }
-    encode_bf16_kernel<<<grid_1d(m, 128), 128, 0, s>>>(pts, L.vpe ? dirs : nullptr, dir_div, m,
-                                                       L.desc.points_pe_degree, L.desc.views_pe_degree, L.pin,
-                                                       T.enc_w, T.vx_w, w.enc, w.vext);
+    const int enc_threads = (T.enc_w + (L.vdep ? T.vx_w : 0)) / 8;
+    encode_bf16_kernel<<<grid_1d(m * enc_threads, 256), 256, 0, s>>>(pts, L.vpe ? dirs : nullptr, dir_div, m,
+                                                                     L.desc.points_pe_degree, L.desc.views_pe_degree,
+                                                                     L.pin, T.enc_w, T.vx_w, w.enc,
+                                                                     L.vdep ? w.vext : nullptr);
     if ((st = launch_status())) return st;
     for (int j = 0; j < L.Dp; ++j) {
         const LayerMap& lm = T.trunk[j];
         const bf16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
         const bf16* x1 = lm.nsrc > 1 ? w.h[j - 1] : nullptr;
-        st = tc_linear(w.h[j], L.Wp, x0, ld0, lm.padw[0], x1, L.Wp, lm.nsrc > 1 ? lm.padw[1] : 0, w.W[j], lm.kpad(),
-                       lm.n, 0, m, lm.n, P[L.idx_trunk_w(j) + 1], 1, nullptr, 0, nullptr, nullptr, nullptr, s);
+        tc::GemmEpilogue ep = make_epilogue(w.h[j], L.Wp, P[L.idx_trunk_w(j) + 1], 1);
+        if (j == L.Dp - 1) {
+            // sigma head (and, without view dependence, the rgb head) on the last trunk layer's rows
+            ep.head_mode = L.vdep ? tc::kHeadSigma : tc::kHeadSigmaRgb;
+            ep.head_w = P[L.idx_out_w()];
+            ep.head_b = P[L.idx_out_w() + 1];
+            ep.head_noise = noise;
+            ep.head_sraw = w.sraw;
+            ep.head_sigma = sigma;
+            ep.head_rgb_ws = w.rgb;
+            ep.head_rgb_out = rgb;
+        }
+        st = tc_linear(ep, x0, ld0, lm.padw[0], x1, L.Wp, lm.nsrc > 1 ? lm.padw[1] : 0, w.W[j], lm.kpad(), lm.n, 0, m,
+                       lm.n, s);
         if (st) return st;
     }
+    if (!L.vdep) return SRF_OK;
     const bf16* hl = w.h[L.Dp - 1];
-    const int wpr = 8;
-    if (!L.vdep) {
-        head_fwd_bf16_kernel<<<grid_1d(m, wpr), wpr * 32, 0, s>>>(m, L.Wp, hl, P[L.idx_out_w()], P[L.idx_out_w() + 1],
-                                                                  2, noise, w.sraw, sigma, w.rgb, rgb);
-        return launch_status();
-    }
-    head_fwd_bf16_kernel<<<grid_1d(m, wpr), wpr * 32, 0, s>>>(m, L.Wp, hl, P[L.idx_out_w()], P[L.idx_out_w() + 1], 0,
-                                                              noise, w.sraw, sigma, nullptr, nullptr);
-    if ((st = launch_status())) return st;
-    st = tc_linear(w.feat, L.Wp, hl, L.Wp, L.Wp, nullptr, 0, 0, w.Wf, L.Wp, L.Wp, 0, m, L.Wp, P[L.idx_feat_w() + 1], 0,
-                   nullptr, 0, nullptr, nullptr, nullptr, s);
+    st = tc_linear(make_epilogue(w.feat, L.Wp, P[L.idx_feat_w() + 1], 0), hl, L.Wp, L.Wp, nullptr, 0, 0, w.Wf, L.Wp,
+                   L.Wp, 0, m, L.Wp, s);
     if (st) return st;
     for (int j = 0; j < L.Dv; ++j) {
         const LayerMap& lm = T.view[j];
         const bf16* x0 = j == 0 ? w.feat : w.hv[j - 1];
         int64_t ld0 = j == 0 ? L.Wp : L.Wv;
-        st = tc_linear(w.hv[j], L.Wv, x0, ld0, lm.padw[0], lm.nsrc > 1 ? w.vext : nullptr, T.vx_w,
-                       lm.nsrc > 1 ? lm.padw[1] : 0, w.Wv[j], lm.kpad(), lm.n, 0, m, lm.n, P[L.idx_view_w(j) + 1], 1,
-                       nullptr, 0, nullptr, nullptr, nullptr, s);
+        tc::GemmEpilogue ep = make_epilogue(w.hv[j], L.Wv, P[L.idx_view_w(j) + 1], 1);
+        if (j == L.Dv - 1) {
+            ep.head_mode = tc::kHeadRgb;
+            ep.head_w = P[L.idx_rgb_w()];
+            ep.head_b = P[L.idx_rgb_w() + 1];
+            ep.head_rgb_ws = w.rgb;
+            ep.head_rgb_out = rgb;
+        }
+        st = tc_linear(ep, x0, ld0, lm.padw[0], lm.nsrc > 1 ? w.vext : nullptr, T.vx_w, lm.nsrc > 1 ? lm.padw[1] : 0,
+                       w.Wv[j], lm.kpad(), lm.n, 0, m, lm.n, s);
         if (st) return st;
     }
-    head_fwd_bf16_kernel<<<grid_1d(m, wpr), wpr * 32, 0, s>>>(m, L.Wv, w.hv[L.Dv - 1], P[L.idx_rgb_w()],
-                                                              P[L.idx_rgb_w() + 1], 1, nullptr, nullptr, nullptr,
-                                                              w.rgb, rgb);
-    return launch_status();
+    return SRF_OK;
 }
 
 int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsigma, const float* drgb, int64_t m,
@@ -562,19 +590,14 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
     TcWs w;
     if (carve_tc(L, T, m, true, ws, ws_bytes, &w) > ws_bytes) return SRF_ERR_WORKSPACE;
     int st;
-    const int64_t rows = 512;
-    const unsigned hblocks = grid_1d(m, int(rows));
     bf16* dz = w.dz0;
     bf16* dz2 = w.dz1;
     const bf16* hl = w.h[L.Dp - 1];
     if (L.vdep) {
-        const bf16* hvl = w.hv[L.Dv - 1];
-        head_bwd_bf16_kernel<<<hblocks, 128, 0, s>>>(m, L.Wv, 1, nullptr, drgb, nullptr, w.rgb, P[L.idx_rgb_w()], hvl,
-                                                     dz, G[L.idx_view_w(L.Dv - 1) + 1], w.dout, nullptr, rows);
-        if ((st = launch_status())) return st;
-        head_dw_bf16_kernel<<<hblocks, 128, 0, s>>>(m, L.Wv, 3, w.dout, hvl, G[L.idx_rgb_w()], G[L.idx_rgb_w() + 1],
-                                                    rows);
-        if ((st = launch_status())) return st;
+        // rgb head: dZ of the last view layer, its bias gradient, the head's dW/db
+        st = head_bwd_fused<3>(m, L.Wv, nullptr, nullptr, drgb, w.rgb, P[L.idx_rgb_w()], w.hv[L.Dv - 1], dz,
+                               G[L.idx_view_w(L.Dv - 1) + 1], G[L.idx_rgb_w()], G[L.idx_rgb_w() + 1], s);
+        if (st) return st;
         for (int j = L.Dv - 1; j >= 0; --j) {
             const LayerMap& lm = T.view[j];
             const bf16* x0 = j == 0 ? w.feat : w.hv[j - 1];
@@ -582,36 +605,40 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
             st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.vext : nullptr, T.vx_w, m, G[L.idx_view_w(j)], s);
             if (st) return st;
             if (j > 0) {
-                st = tc_linear(dz2, L.Wv, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[j], L.Wv, lm.kpad(), 0, m, L.Wv,
-                               nullptr, 0, w.hv[j - 1], L.Wv, nullptr, nullptr, G[L.idx_view_w(j - 1) + 1], s);
+                tc::GemmEpilogue ep = make_epilogue(dz2, L.Wv, nullptr, 0);
+                ep.mask = w.hv[j - 1];
+                ep.ld_mask = L.Wv;
+                ep.colsum = G[L.idx_view_w(j - 1) + 1];
+                st = tc_linear(ep, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[j], L.Wv, lm.kpad(), 0, m, L.Wv, s);
                 if (st) return st;
                 std::swap(dz, dz2);
             } else {
-                st = tc_linear(w.dfeat, L.Wp, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[0], L.Wv, lm.kpad(), 0, m, L.Wp,
-                               nullptr, 0, nullptr, 0, nullptr, nullptr, G[L.idx_feat_w() + 1], s);
+                tc::GemmEpilogue ep = make_epilogue(w.dfeat, L.Wp, nullptr, 0);
+                ep.colsum = G[L.idx_feat_w() + 1];
+                st = tc_linear(ep, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[0], L.Wv, lm.kpad(), 0, m, L.Wp, s);
                 if (st) return st;
             }
         }
         st = wgrad_layer(T.feat, w, w.dfeat, hl, L.Wp, nullptr, 0, m, G[L.idx_feat_w()], s);
         if (st) return st;
-        // sigma head: dsig = dsigma * (sraw > 0), its weight gradient, and the
-        // rank-1 term added in the feature-layer dgrad epilogue
-        head_bwd_bf16_kernel<<<hblocks, 128, 0, s>>>(m, L.Wp, 0, dsigma, nullptr, w.sraw, nullptr, P[L.idx_out_w()],
-                                                     hl, nullptr, nullptr, w.dout, w.dsig, rows);
-        if ((st = launch_status())) return st;
-        head_dw_bf16_kernel<<<hblocks, 128, 0, s>>>(m, L.Wp, 1, w.dout, hl, G[L.idx_out_w()], G[L.idx_out_w() + 1],
-                                                    rows);
-        if ((st = launch_status())) return st;
-        st = tc_linear(dz, L.Wp, w.dfeat, L.Wp, L.Wp, nullptr, 0, 0, w.WTf, L.Wp, L.Wp, 0, m, L.Wp, nullptr, 0, hl,
-                       L.Wp, w.dsig, P[L.idx_out_w()], G[L.idx_trunk_w(L.Dp - 1) + 1], s);
+        // feature-layer dgrad with the sigma head's adjoint fused in: dZ_last =
+        // (dfeat . Wf + dsig w_sigma) * (h_last > 0), dsig = dsigma * (sraw > 0);
+        // the same pass adds the sigma head's weight (sum dsig h_last) and bias gradients
+        tc::GemmEpilogue ep = make_epilogue(dz, L.Wp, nullptr, 0);
+        ep.mask = hl;
+        ep.ld_mask = L.Wp;
+        ep.r1_row = dsigma;
+        ep.r1_gate = w.sraw;
+        ep.r1_col = P[L.idx_out_w()];
+        ep.r1_mask_colsum = G[L.idx_out_w()];
+        ep.r1_sum = G[L.idx_out_w() + 1];
+        ep.colsum = G[L.idx_trunk_w(L.Dp - 1) + 1];
+        st = tc_linear(ep, w.dfeat, L.Wp, L.Wp, nullptr, 0, 0, w.WTf, L.Wp, L.Wp, 0, m, L.Wp, s);
         if (st) return st;
     } else {
-        head_bwd_bf16_kernel<<<hblocks, 128, 0, s>>>(m, L.Wp, 2, dsigma, drgb, w.sraw, w.rgb, P[L.idx_out_w()], hl, dz,
-                                                     G[L.idx_trunk_w(L.Dp - 1) + 1], w.dout, nullptr, rows);
-        if ((st = launch_status())) return st;
-        head_dw_bf16_kernel<<<hblocks, 128, 0, s>>>(m, L.Wp, 4, w.dout, hl, G[L.idx_out_w()], G[L.idx_out_w() + 1],
-                                                    rows);
-        if ((st = launch_status())) return st;
+        st = head_bwd_fused<4>(m, L.Wp, dsigma, w.sraw, drgb, w.rgb, P[L.idx_out_w()], hl, dz,
+                               G[L.idx_trunk_w(L.Dp - 1) + 1], G[L.idx_out_w()], G[L.idx_out_w() + 1], s);
+        if (st) return st;
     }
     for (int j = L.Dp - 1; j >= 0; --j) {
         const LayerMap& lm = T.trunk[j];
@@ -621,8 +648,11 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         if (st) return st;
         if (j == 0) break;
         int row0 = lm.nsrc > 1 ? lm.padw[0] : 0;
-        st = tc_linear(dz2, L.Wp, dz, L.Wp, L.Wp, nullptr, 0, 0, w.WT[j], L.Wp, lm.kpad(), row0, m, L.Wp, nullptr, 0,
-                       w.h[j - 1], L.Wp, nullptr, nullptr, G[L.idx_trunk_w(j - 1) + 1], s);
+        tc::GemmEpilogue ep = make_epilogue(dz2, L.Wp, nullptr, 0);
+        ep.mask = w.h[j - 1];
+        ep.ld_mask = L.Wp;
+        ep.colsum = G[L.idx_trunk_w(j - 1) + 1];
+        st = tc_linear(ep, dz, L.Wp, L.Wp, nullptr, 0, 0, w.WT[j], L.Wp, lm.kpad(), row0, m, L.Wp, s);
         if (st) return st;
         std::swap(dz, dz2);
     }
@@ -639,10 +669,12 @@ extern "C" int srf_bf16_linear(void* out, int64_t ld_out, const void* x0, int64_
                                int64_t ld1, int k1, const void* w, int64_t ldw, int w_rows, int w_row0,
                                const float* bias, int64_t m, int n, int relu, const void* mask, int64_t ld_mask,
                                float* colsum, void* stream) {
-    return tc_linear(static_cast<bf16*>(out), ld_out, static_cast<const bf16*>(x0), ld0, k0,
-                     static_cast<const bf16*>(x1), ld1, k1, static_cast<const bf16*>(w), ldw, w_rows, w_row0, m, n,
-                     bias, relu, static_cast<const bf16*>(mask), ld_mask, nullptr, nullptr, colsum,
-                     as_stream(stream));
+    tc::GemmEpilogue ep = make_epilogue(static_cast<bf16*>(out), ld_out, bias, relu);
+    ep.mask = static_cast<const bf16*>(mask);
+    ep.ld_mask = ld_mask;
+    ep.colsum = colsum;
+    return tc_linear(ep, static_cast<const bf16*>(x0), ld0, k0, static_cast<const bf16*>(x1), ld1, k1,
+                     static_cast<const bf16*>(w), ldw, w_rows, w_row0, m, n, as_stream(stream));
 }
 
 extern "C" size_t srf_bf16_wgrad_workspace_size(int n_dz, int k_total) {

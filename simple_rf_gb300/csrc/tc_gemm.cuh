@@ -27,18 +27,36 @@ constexpr int kThreads = 192;
 constexpr uint32_t kATileBytes = kBlockM * kBlockK * 2;
 constexpr size_t kMaxSmem = 232448;
 
+enum { kHeadNone = 0, kHeadSigma = 1, kHeadRgb = 2, kHeadSigmaRgb = 3 };
+
 struct GemmEpilogue {
     const float* bias;              // [N] or NULL
     int relu;                       // apply ReLU to the result
     const __nv_bfloat16* mask;      // multiply by (mask[m, n] > 0) when non-NULL
     int64_t ld_mask;
-    const float* r1_row;            // result += r1_row[m] * r1_col[n] (before ReLU/mask) when non-NULL
-    const float* r1_col;
+    const float* r1_row;            // result += r1[m] * r1_col[n] (before ReLU/mask) when non-NULL, where
+    const float* r1_col;            // r1[m] = r1_row[m], or 0 when r1_gate is given and r1_gate[m] <= 0
+    const float* r1_gate;
+    float* r1_mask_colsum;          // += sum_m r1[m] * mask[m, n]   (the head's weight gradient)
+    float* r1_sum;                  // += sum_m r1[m]                (the head's bias gradient)
     __nv_bfloat16* out;             // [M, ld_out] BF16
     int64_t ld_out;
     float* colsum;                  // += column sums of the stored values (a bias gradient) when non-NULL
+    // Head fused on the FP32 result rows: 1 (sigma), 3 (rgb) or 4 (sigma + rgb) dot products.
+    int head_mode;
+    const float* head_w;            // [units][N]
+    const float* head_b;            // [units]
+    const float* head_noise;        // [M] added to the raw sigma, or NULL
+    float* head_sraw;               // [M] raw sigma
+    float* head_sigma;              // [M] ReLU(raw sigma)
+    float* head_rgb_ws;             // [M, 3] sigmoid rgb (kept for the backward)
+    float* head_rgb_out;            // [M, 3] sigmoid rgb
     int* flag;
 };
+
+__host__ __device__ inline int head_units(int mode) {
+    return mode == kHeadSigma ? 1 : (mode == kHeadRgb ? 3 : (mode == kHeadSigmaRgb ? 4 : 0));
+}
 
 // Lane i of the warp ends with sum over the 32 lanes of v[i] (recursive halving).
 __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
@@ -65,8 +83,9 @@ struct GemmShape {
 template <int BN>
 struct SmemPlan {
     static constexpr uint32_t kBBlockBytes = BN * kBlockK * 2;
-    // 1024 B alignment slack + 256 B of barriers + BN floats of bias + BN of column sums
-    static constexpr size_t kReserve = 1024 + 256 + BN * 8;
+    // 1024 B alignment slack + 256 B of barriers + BN floats each of bias, column
+    // sums and r1 mask column sums + 4 x BN head weights + 4 head biases
+    static constexpr size_t kReserve = 1024 + 256 + BN * 12 + 4 * BN * 4 + 16;
     static __host__ __device__ int stages(int kb_total) {
         size_t b = size_t(kb_total) * kBBlockBytes;
         if (b + kReserve + 2 * kATileBytes > kMaxSmem) return 0;
@@ -100,6 +119,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 23);
     float* sbias = reinterpret_cast<float*>(bars + 24);   // BN floats
     float* scol = sbias + BN;                              // BN floats
+    float* scol2 = scol + BN;                              // BN floats
+    float* shw = scol2 + BN;                               // 4 x BN floats
+    float* shb = shw + 4 * BN;                             // 4 floats
+    const int hunits = head_units(ep.head_mode);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t num_tiles = (shape.M + kBlockM - 1) / kBlockM;
@@ -121,7 +144,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int i = threadIdx.x; i < BN; i += blockDim.x) {
         sbias[i] = ep.bias ? ep.bias[i] : 0.f;
         scol[i] = 0.f;
+        scol2[i] = 0.f;
+        for (int u = 0; u < hunits; ++u) shw[u * BN + i] = ep.head_w[u * BN + i];
     }
+    if (threadIdx.x < 4) shb[threadIdx.x] = int(threadIdx.x) < hunits ? ep.head_b[threadIdx.x] : 0.f;
     if (warp == 1) {
         tmem_alloc(tmem_slot, 2 * BN);
         tmem_relinquish();
@@ -203,6 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // --------------------------------------------------------- epilogue
         const int q = warp & 3;   // tensor-memory lane quadrant this warp may read
         uint32_t t = 0;
+        float r1_total = 0.f;
         for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
             uint32_t acc = t & 1;
             if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
@@ -212,7 +239,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc_fence_after();
             const int64_t m = tile * kBlockM + q * 32 + lane;
             const bool live = m < shape.M;
-            const float r1 = (ep.r1_row && live) ? ep.r1_row[m] : 0.f;
+            float r1 = (ep.r1_row && live) ? ep.r1_row[m] : 0.f;
+            if (ep.r1_gate && live && !(ep.r1_gate[m] > 0.f)) r1 = 0.f;
+            r1_total += r1;
+            float hacc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
                 uint32_t r[32];
@@ -226,17 +256,40 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (ep.relu) v[j] = v[j] > 0.f ? v[j] : 0.f;
                     if (!live) v[j] = 0.f;
                 }
-                if (ep.mask && live) {
-                    const uint4* mp = reinterpret_cast<const uint4*>(ep.mask + m * ep.ld_mask + c * 32);
+                if (ep.mask) {   // kernel-uniform branch; rows past M contribute zeros
+                    float mw[32];
 #pragma unroll
-                    for (int g = 0; g < 4; ++g) {
-                        uint4 mv = mp[g];
-                        uint32_t w4[4] = {mv.x, mv.y, mv.z, mv.w};
+                    for (int j = 0; j < 32; ++j) mw[j] = 0.f;
+                    if (live) {
+                        const uint4* mp = reinterpret_cast<const uint4*>(ep.mask + m * ep.ld_mask + c * 32);
 #pragma unroll
-                        for (int h = 0; h < 4; ++h) {
-                            float2 f = unpack_bf16(w4[h]);
-                            if (!(f.x > 0.f)) v[g * 8 + h * 2] = 0.f;
-                            if (!(f.y > 0.f)) v[g * 8 + h * 2 + 1] = 0.f;
+                        for (int g = 0; g < 4; ++g) {
+                            uint4 mv = mp[g];
+                            uint32_t w4[4] = {mv.x, mv.y, mv.z, mv.w};
+#pragma unroll
+                            for (int h = 0; h < 4; ++h) {
+                                float2 f = unpack_bf16(w4[h]);
+                                mw[g * 8 + h * 2] = f.x;
+                                mw[g * 8 + h * 2 + 1] = f.y;
+                                if (!(f.x > 0.f)) v[g * 8 + h * 2] = 0.f;
+                                if (!(f.y > 0.f)) v[g * 8 + h * 2 + 1] = 0.f;
+                            }
+                        }
+                    }
+                    if (ep.r1_mask_colsum) {   // needs the mask; r1 is 0 on rows past M
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) mw[j] *= r1;
+                        atomicAdd(&scol2[c * 32 + lane], warp_reduce_scatter32(mw));
+                    }
+                }
+                if (hunits) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (u < hunits) {
+                            float sacc = 0.f;
+#pragma unroll
+                            for (int j = 0; j < 32; ++j) sacc += v[j] * shw[u * BN + c * 32 + j];
+                            hacc[u] += sacc;
                         }
                     }
                 }
@@ -250,14 +303,40 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
             }
+            if (hunits && live) {
+                // SimpleNeRF17.py:735-750 (sigma head + noise + ReLU) and :771-777 (sigmoid rgb)
+                int u0 = 0;
+                if (ep.head_mode != kHeadRgb) {
+                    float s = hacc[0] + shb[0];
+                    if (ep.head_noise) s += ep.head_noise[m];
+                    ep.head_sraw[m] = s;
+                    ep.head_sigma[m] = s > 0.f ? s : 0.f;
+                    u0 = 1;
+                }
+                if (ep.head_mode != kHeadSigma) {
+#pragma unroll
+                    for (int cc = 0; cc < 3; ++cc) {
+                        float rv = 1.f / (1.f + expf(-(hacc[u0 + cc] + shb[u0 + cc])));
+                        ep.head_rgb_ws[3 * m + cc] = rv;
+                        ep.head_rgb_out[3 * m + cc] = rv;
+                    }
+                }
+            }
             tc_fence_before();
             mbar_arrive(&acc_empty[acc]);
+        }
+        if (ep.r1_sum) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r1_total += __shfl_xor_sync(0xffffffffu, r1_total, o);
+            if (lane == 0) atomicAdd(ep.r1_sum, r1_total);
         }
     }
     __syncthreads();
     if (threadIdx.x == 0 && *abort_flag) raise_flag(ep.flag, kFlagTimeout);
     if (ep.colsum)
         for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.colsum + i, scol[i]);
+    if (ep.r1_mask_colsum)
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.r1_mask_colsum + i, scol2[i]);
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, 2 * BN);
