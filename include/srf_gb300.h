@@ -323,6 +323,15 @@ int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* d
 int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
                   float beta1, float beta2, float eps, float weight_decay, int step, const int32_t* step_dev,
                   void* stream);
+/* Depth-consistency term of AugmentationsDepthLoss11.compute_depth_mse
+ * (src/loss_functions/AugmentationsDepthLoss11.py:208-226): with m_r = mask[r]
+ * (all ones when mask == NULL), loss += weight * mean_r m_r (pred_r - target_r)^2
+ * over all n rays and grad[r] += weight * 2 m_r (pred_r - target_r) / n
+ * (accumulated).  The target is detached, as the reference's .detach() makes it.
+ * The mask is the caller's choice of rays where the target model is trusted
+ * (the reference picks it by patch reprojection, :105-190). */
+int srf_depth_consistency_loss(const float* pred, const float* target, const uint8_t* mask, int n, float weight,
+                               float* loss_dev, float* grad, void* stream);
 /* *counter_dev += value on the stream (advances a graph-replayed step count). */
 int srf_counter_add(int32_t* counter_dev, int value, void* stream);
 /* Sample points pts (N*S,3) = o + d * z (src/models/SimpleNeRF17.py:213-215). */

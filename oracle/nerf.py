@@ -460,7 +460,7 @@ def composite_backward(cache, g):
 
 
 def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n_coarse, n_fine,
-                u_coarse=None, u_fine=None, white_bkgd=False, ndc=None, aug=None, z_fine=None):
+                u_coarse=None, u_fine=None, white_bkgd=False, ndc=None, aug=None, z_fine=None, pts_fp32=False):
     """SimpleNeRF17.py:159-328 render_rays for synthetic rays (ray generation patched out).
 
     ``ndc`` = dict(h, w, fx, fy, near) switches to NDC rays (config 3).  ``aug`` =
@@ -468,6 +468,10 @@ def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n
     (:244-261) and, when they also carry fine params, on the fine samples (:296-313).
     ``z_fine`` (N, Sc+Sf) replaces the inverse-CDF depths (tests use it to check
     the fine pass on exactly the depths another implementation sampled).
+    ``pts_fp32`` forms the sample positions in float32 (product, then sum, as the
+    reference's two torch ops do at :213-215) before the network sees them, so a
+    float64 evaluation shares the float32 input quantisation of any float32
+    implementation: PE scales that rounding by up to 2^9.
     Returns (outputs dict keyed like the reference, caches for backward).
     """
     ret, caches = {}, {}
@@ -483,7 +487,12 @@ def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n
 
     def run(params, spec, z, tag):
         s = z.shape[1]
-        pts = (po[:, None, :] + pd[:, None, :] * z[:, :, None]).reshape(-1, 3)
+        if pts_fp32:
+            f = np.float32
+            pts = (po.astype(f)[:, None, :] + pd.astype(f)[:, None, :] * z.astype(f)[:, :, None])
+            pts = pts.reshape(-1, 3).astype(z.dtype)
+        else:
+            pts = (po[:, None, :] + pd[:, None, :] * z[:, :, None]).reshape(-1, 3)
         vds = np.repeat(vd, s, axis=0) if spec.use_view_dirs else None
         sigma, rgb, mc = mlp_forward(params, spec, pts, vds)
         sigma = sigma.reshape(n, s)

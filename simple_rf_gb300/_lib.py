@@ -96,6 +96,7 @@ _SIGS = {
     'srf_rgb_depth_loss': (c_int, [P, P, P, P, P, c_int, c_int, c_float, P, P, P, P]),
     'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P, P]),
     'srf_counter_add': (c_int, [P, c_int, P]),
+    'srf_depth_consistency_loss': (c_int, [P, P, P, c_int, c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
     'srf_launch_count': (c_int64, []),
 }

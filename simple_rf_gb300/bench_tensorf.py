@@ -1,0 +1,143 @@
+"""TensoRF VM training-step workload: a 300^3 main model and a 75^3 augmented
+model forward + backward + Adam on the srf_gb300 kernels, through the drop-in
+``GbVmTensor`` modules (the path ``SimpleTensoRF.render_rays`` drives,
+src/models/SimpleTensoRF09.py:194-351 and LowRankTensor.forward :701-761).
+
+Workload (per step): 8192 rays; bbox [-1.5, 1.5]^3; density 16 components per
+plane/line, appearance 48 per plane/line projected to 27 features; renderer
+PE L=2 on features and view direction -> 128 -> 128 -> 3; planes/lines ~
+N(0, 0.1^2); ReLU density, distance scale 25; sample step half a voxel (1039
+samples per ray at 300^3, 260 at 75^3); a 128^3 alpha-mask volume with
+Bernoulli(0.15) occupancy (trilinear lookup > 0, so a sample is kept when any of
+its 8 neighbouring cells is occupied).  Rays: origins uniform on the sphere of
+radius 4 about the box centre, directions towards the centre perturbed by
+N(0, 0.3^2) per axis, near 2, far 6.  Loss: MSE of each model's rgb against
+targets ~ U[0,1]^3.
+
+    python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3
+"""
+import argparse
+import json
+
+import torch
+
+from . import _lib
+from . import functional as F
+
+BBOX = [[-1.5] * 3, [1.5] * 3]
+
+
+def tensor_configs(n_voxels):
+    return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [16, 16, 16],
+            'num_components_color': [48, 48, 48], 'bounding_box': BBOX, 'num_voxels_initial': n_voxels,
+            'num_voxels_final': n_voxels, 'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5,
+            'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4,
+            'use_view_dirs': True, 'view_dependent_color': True, 'views_positional_encoding_degree': 2,
+            'features_positional_encoding_degree': 2, 'features_dimension_color': 27, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 128, 'predict_visibility': False}
+
+
+def make_models(device, seed=0, mask_res=128, mask_occupancy=0.15):
+    from .tensorf_model import AlphaGridMask, GbVmTensor
+    torch.manual_seed(seed)
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
+    models = []
+    for name, nv in (('coarse_model', 300 ** 3), ('views_augmentation_coarse_model', 75 ** 3)):
+        tm = GbVmTensor(name, configs, tensor_configs(nv), {'bounding_box': BBOX}).to(device)
+        g = torch.Generator().manual_seed(seed + 1)
+        vol = (torch.rand(mask_res, mask_res, mask_res, generator=g) < mask_occupancy).to(device)
+        tm.alpha_mask = AlphaGridMask(vol, tm.bounding_box.detach().clone())
+        models.append(tm)
+    return models
+
+
+def synthetic_rays(n, seed, device):
+    g = torch.Generator().manual_seed(seed)
+    o = torch.randn(n, 3, generator=g)
+    o = 4.0 * o / torch.linalg.norm(o, dim=-1, keepdim=True)
+    d = -o / 4.0 + 0.3 * torch.randn(n, 3, generator=g)
+    d = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    t_rgb = torch.rand(n, 3, generator=g)
+    u = torch.rand(n, 2, generator=g)
+    return [x.to(device) for x in (o, d, t_rgb, u)]
+
+
+class TensorfTrainStep:
+    """forward (both models) -> rgb MSE -> backward -> Adam (srf_adam_step per tensor)."""
+
+    def __init__(self, models, lr_tensor=0.02, lr_network=1e-3):
+        self.models = models
+        self.params = []
+        for tm in models:
+            tensor_ps = list(tm.matrices_density) + list(tm.vectors_density) + list(tm.matrices_color) + \
+                list(tm.vectors_color)
+            net_ps = [tm.basis_matrix_color.weight] + list(tm.color_predictor.parameters())
+            self.params += [(p, lr_tensor) for p in tensor_ps] + [(p, lr_network) for p in net_ps]
+        self.state = [(torch.zeros_like(p), torch.zeros_like(p)) for p, _ in self.params]
+        self.t = 0
+        self.last = {}
+
+    def step(self, o, d, t_rgb, u):
+        n = o.shape[0]
+        vd = F.view_dirs(d)
+        loss = 0.0
+        counts = []
+        for i, tm in enumerate(self.models):
+            s = int(tm.num_samples.item())
+            z = F.aabb_z(o, d, s, tm.bounding_box.detach().cpu(), 2.0, 6.0, float(tm.step_size), u[:, i].contiguous())
+            out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=False)
+            loss = loss + torch.mean(torch.mean((out['rgb'] - t_rgb) ** 2, -1))
+            counts.append(dict(tm.last_sample_counts))
+        for p, _ in self.params:
+            p.grad = None
+        loss.backward()
+        self.t += 1
+        st = F._stream()
+        for (p, lr), (m, v) in zip(self.params, self.state):
+            if p.grad is None:
+                continue
+            _lib.call('srf_adam_step', F._ptr(p.data), F._ptr(p.grad.contiguous(memory_format=_fmt(p))), F._ptr(m),
+                      F._ptr(v), p.numel(), lr, 0.9, 0.99, 1e-8, 0.0, self.t, None, st)
+        self.last = {'loss': loss.detach(), 'samples': counts}
+        return loss
+
+
+def _fmt(p):
+    return torch.channels_last if p.dim() == 4 and p.is_contiguous(memory_format=torch.channels_last) else \
+        torch.contiguous_format
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--rays', type=int, default=8192)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    args = ap.parse_args(argv)
+    from . import build as _build
+    _build.build()
+    dev = torch.device('cuda')
+    models = make_models(dev)
+    step = TensorfTrainStep(models)
+    batches = [synthetic_rays(args.rays, 10 + i, dev) for i in range(4)]
+    for i in range(args.warmup):
+        step.step(*batches[i % 4])
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    l0 = lib.srf_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.steps):
+        step.step(*batches[i % 4])
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    launches = (lib.srf_launch_count() - l0) / max(args.steps, 1)
+    print(json.dumps({'workload': f'tensorf_vm_train_step_{args.rays}rays_300^3+75^3', 'rays': args.rays,
+                      'ms_per_step': round(ms, 4), 'rays_per_s': round(args.rays / ms * 1e3, 1),
+                      'samples_per_step': {m.name: c for m, c in zip(models, step.last['samples'])},
+                      'gpu_launches_per_step': launches, 'loss': float(step.last['loss'].item())}))
+
+
+if __name__ == '__main__':
+    main()

@@ -458,9 +458,24 @@ size_t carve_tc(const MlpLayout& L, const TcLayout& T, int64_t m, bool bwd, void
     TcWs w;
     w.enc = c.take<bf16>(size_t(m) * T.enc_w);
     w.vext = L.vdep ? c.take<bf16>(size_t(m) * T.vx_w) : nullptr;
-    for (int j = 0; j < L.Dp; ++j) w.h.push_back(c.take<bf16>(size_t(m) * L.Wp));
-    w.feat = L.vdep ? c.take<bf16>(size_t(m) * L.Wp) : nullptr;
-    for (int j = 0; L.vdep && j < L.Dv; ++j) w.hv.push_back(c.take<bf16>(size_t(m) * L.Wv));
+    if (bwd) {
+        // the backward reads every layer's activation
+        for (int j = 0; j < L.Dp; ++j) w.h.push_back(c.take<bf16>(size_t(m) * L.Wp));
+        w.feat = L.vdep ? c.take<bf16>(size_t(m) * L.Wp) : nullptr;
+        for (int j = 0; L.vdep && j < L.Dv; ++j) w.hv.push_back(c.take<bf16>(size_t(m) * L.Wv));
+    } else {
+        // forward only: layer j reads only layer j-1 (the skip input is the
+        // encoding, kept separately), so two activation buffers alternate
+        bf16* ping = c.take<bf16>(size_t(m) * L.Wp);
+        bf16* pong = L.Dp > 1 || L.vdep ? c.take<bf16>(size_t(m) * L.Wp) : ping;
+        for (int j = 0; j < L.Dp; ++j) w.h.push_back(j & 1 ? pong : ping);
+        // feature layer reads h[Dp-1]; the view layers read the feature, then each other
+        bf16* other = (L.Dp - 1) & 1 ? ping : pong;
+        w.feat = L.vdep ? other : nullptr;
+        bf16* hv0 = (L.vdep && L.Dv > 0) ? c.take<bf16>(size_t(m) * L.Wv) : nullptr;
+        bf16* hv1 = (L.vdep && L.Dv > 1) ? c.take<bf16>(size_t(m) * L.Wv) : hv0;
+        for (int j = 0; L.vdep && j < L.Dv; ++j) w.hv.push_back(j & 1 ? hv1 : hv0);
+    }
     w.sraw = c.take<float>(size_t(m));
     w.rgb = c.take<float>(size_t(m) * 3);
     for (auto& lm : T.trunk) {

@@ -65,6 +65,30 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
 
 __global__ void counter_add_kernel(int* c, int v) { *c += v; }
 
+// loss += weight * mean_r m_r (pred - target)^2;  grad[r] += 2 weight m_r (pred - target) / n
+__global__ void depth_consistency_kernel(const float* __restrict__ pred, const float* __restrict__ target,
+                                         const uint8_t* __restrict__ mask, int n, float weight, float* loss,
+                                         float* grad) {
+    __shared__ float red[32];
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (r < n && (!mask || mask[r])) {
+        float e = pred[r] - target[r];
+        l = weight * e * e / float(n);
+        grad[r] += 2.f * weight * e / float(n);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        l = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        if (threadIdx.x == 0 && loss) atomicAdd(loss, l);
+    }
+}
+
 // pts[r * S + i] = o[r] + d[r] * z[r, i]  (SimpleNeRF17.py:213-215).  The product
 // and the sum round separately, as the reference's two torch ops do: PE scales
 // pts by up to 2^9, so a one-ulp difference here moves the network's output.
@@ -82,6 +106,16 @@ __global__ void ray_points_kernel(const float* __restrict__ o, const float* __re
 }  // namespace srf
 
 using namespace srf;
+
+extern "C" int srf_depth_consistency_loss(const float* pred, const float* target, const uint8_t* mask, int n,
+                                          float weight, float* loss_dev, float* grad, void* stream) {
+    if (!pred || !target || !grad) return SRF_ERR_NULL;
+    if (n < 0) return SRF_ERR_SHAPE;
+    if (n == 0) return SRF_OK;
+    depth_consistency_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(pred, target, mask, n, weight, loss_dev,
+                                                                             grad);
+    return launch_status();
+}
 
 extern "C" int srf_counter_add(int32_t* counter_dev, int value, void* stream) {
     if (!counter_dev) return SRF_ERR_NULL;

@@ -222,6 +222,7 @@ class GbVmTensor(torch.nn.Module):
                   float(self.tensor_configs['ray_marching_weight_threshold']), F._ptr(smask), F._stream())
         idx_s, cnt_s = T.compact(smask)
         ns = int(cnt_s.item())
+        self.last_sample_counts = {'marched': rows, 'valid': nv, 'surface': ns}
         if ns:
             ps = T.gather_rows(pn, idx_s, cnt_s, ns)
             feats = T.vm_color(self._grid('color'), ps)

@@ -87,26 +87,72 @@ class NetState:
         return {n: v.detach().clone() for n, v in zip(self.spec.param_names, self.views)}
 
 
+class _Net:
+    """One MLP evaluated in the step: its parameters and its per-sample buffers."""
+
+    def __init__(self, name, level, spec, state, n, ss, precision, dev, train=True):
+        f32 = dict(device=dev, dtype=torch.float32)
+        self.name, self.level, self.spec, self.state = name, level, spec, state
+        self.b = {'sigma': torch.zeros(n * ss, **f32), 'rgb': torch.zeros(n * ss, 3, **f32),
+                  'rgb_map': torch.zeros(n, 3, **f32), 'acc': torch.zeros(n, **f32), 'depth': torch.zeros(n, **f32),
+                  'depth_var': torch.zeros(n, **f32), 'weights': torch.zeros(n, ss, **f32),
+                  'depth_ndc': torch.zeros(n, **f32), 'depth_var_ndc': torch.zeros(n, **f32),
+                  'g_rgb': torch.zeros(n, 3, **f32), 'g_depth': torch.zeros(n, **f32),
+                  'd_sigma': torch.zeros(n * ss, **f32), 'd_rgb': torch.zeros(n * ss, 3, **f32)}
+        if not train:
+            for k in ('g_rgb', 'g_depth', 'd_sigma', 'd_rgb'):
+                del self.b[k]
+        ws_bytes = spec.workspace_bytes(n * ss, precision, train)
+        if ws_bytes == 0:
+            raise RuntimeError(f'MLP configuration of {name} not supported at this precision')
+        self.b['ws'] = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+
+
 class NerfTrainStep:
-    """Preallocated, graph-capturable config-2 training step (coarse + fine NeRF)."""
+    """Preallocated, graph-capturable Simple-NeRF training step.
+
+    Config-2 form (default): world rays, coarse + fine nets, white background.
+    Config-3 form: ``ndc=dict(h=378, w=504, focal=400.0, near=1.0)`` switches to
+    forward-facing NDC rays (CommonUtils04.py:120-138; z in [near_ndc, far_ndc] =
+    [0, 1]) and ``aug=[(name, spec_kwargs), ...]`` adds augmented nets evaluated
+    on the same coarse samples (SimpleNeRF17.py:244-261) and, with
+    ``aug_fine=True``, on the fine samples too (:296-313).  Each augmented net is
+    trained on the rgb loss, and its (detached) coarse depth is a squared-error
+    target of the main coarse depth with ``consistency_weight``
+    (AugmentationsDepthLoss11.py:208-226 with every ray trusting the augmented net).
+    """
 
     def __init__(self, n_rays=4096, n_coarse=64, n_fine=128, near=2.0, far=6.0, white_bkgd=True,
                  depth_fraction=0.25, depth_weight=0.1, precision='bf16', spec_kwargs=None, lr=5e-4,
-                 betas=(0.9, 0.999), eps=1e-8, seed=0, device='cuda'):
+                 betas=(0.9, 0.999), eps=1e-8, seed=0, device='cuda', ndc=None, aug=None, aug_fine=False,
+                 consistency_weight=0.1, train=True, perturb=True):
         self.dev = torch.device(device)
         self.n, self.sc, self.sf = n_rays, n_coarse, n_fine
         self.s = n_coarse + n_fine
-        self.near, self.far = float(near), float(far)
+        self.ndc = dict(ndc) if ndc else None
+        self.near, self.far = (0.0, 1.0) if self.ndc else (float(near), float(far))
         self.white = bool(white_bkgd)
         self.n_depth = max(int(round(n_rays * depth_fraction)), 0)
         self.depth_weight = float(depth_weight)
+        self.consistency_weight = float(consistency_weight)
+        self.train, self.perturb = bool(train), bool(perturb)
         self.precision = _lib.SRF_PRECISION_BF16 if precision == 'bf16' else _lib.SRF_PRECISION_FP32
         self.lr, self.betas, self.eps = float(lr), betas, float(eps)
         self.spec = MlpSpec(**(spec_kwargs or {}))
         rng = np.random.default_rng(seed)
-        self.nets = {'coarse': NetState(self.spec, self.dev, rng), 'fine': NetState(self.spec, self.dev, rng)}
         n, sc, s = n_rays, n_coarse, self.s
         f32 = dict(device=self.dev, dtype=torch.float32)
+        self.nets = {'coarse': NetState(self.spec, self.dev, rng), 'fine': NetState(self.spec, self.dev, rng)}
+        self.run = [_Net('coarse', 'coarse', self.spec, self.nets['coarse'], n, sc, self.precision, self.dev, train),
+                    _Net('fine', 'fine', self.spec, self.nets['fine'], n, s, self.precision, self.dev, train)]
+        for name, kw in (aug or []):
+            aspec = MlpSpec(**kw)
+            for level, ss in (('coarse', sc), ('fine', s)):
+                if level == 'fine' and not aug_fine:
+                    continue
+                tag = f'{name}_{level}'
+                self.nets[tag] = NetState(aspec, self.dev, rng)
+                self.run.append(_Net(tag, level, aspec, self.nets[tag], n, ss, self.precision, self.dev, train))
         # inputs (static buffers the host copies into)
         self.rays_o = torch.zeros(n, 3, **f32)
         self.rays_d = torch.zeros(n, 3, **f32)
@@ -116,38 +162,45 @@ class NerfTrainStep:
         self.u_f = torch.zeros(n, n_fine, **f32)
         self.depth_mask = torch.zeros(n, dtype=torch.uint8, device=self.dev)
         self.depth_mask[:self.n_depth] = 1
-        # intermediates
+        # intermediates shared by the nets of one level
         self.vdirs = torch.zeros(n, 3, **f32)
-        self.buf = {}
-        for tag, ss in (('coarse', sc), ('fine', s)):
-            b = {'z': torch.zeros(n, ss, **f32), 'pts': torch.zeros(n * ss, 3, **f32), 'sigma': torch.zeros(n * ss, **f32),
-                 'rgb': torch.zeros(n * ss, 3, **f32), 'rgb_map': torch.zeros(n, 3, **f32), 'acc': torch.zeros(n, **f32),
-                 'depth': torch.zeros(n, **f32), 'depth_var': torch.zeros(n, **f32), 'weights': torch.zeros(n, ss, **f32),
-                 'g_rgb': torch.zeros(n, 3, **f32), 'g_depth': torch.zeros(n, **f32),
-                 'd_sigma': torch.zeros(n * ss, **f32), 'd_rgb': torch.zeros(n * ss, 3, **f32)}
-            ws_bytes = self.spec.workspace_bytes(n * ss, self.precision, True)
-            if ws_bytes == 0:
-                raise RuntimeError('MLP configuration not supported at this precision')
-            b['ws'] = torch.empty(ws_bytes, dtype=torch.uint8, device=self.dev)
-            self.buf[tag] = b
+        self.rays_o_ndc = torch.zeros(n, 3, **f32)
+        self.rays_d_ndc = torch.zeros(n, 3, **f32)
+        self.focal = torch.full((n,), float(self.ndc['focal']) if self.ndc else 1.0, **f32)
+        self.level = {lv: {'z': torch.zeros(n, ss, **f32), 'pts': torch.zeros(n * ss, 3, **f32)}
+                      for lv, ss in (('coarse', sc), ('fine', s))}
         self.loss = torch.zeros(1, **f32)
         self.step_count = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.graph = None
         self.launches_per_step = None
 
+    @property
+    def buf(self):
+        """Per-net buffers keyed by net tag, with the level's depths under 'z'."""
+        out = {}
+        for net in self.run:
+            d = dict(net.b)
+            d['z'] = self.level[net.level]['z']
+            out[net.name] = d
+        return out
+
     # ------------------------------------------------------------ enqueue --
-    def _composite_args(self, tag, backward):
-        b = self.buf[tag]
-        ss = b['z'].shape[1]
+    def _composite_args(self, net, backward):
+        b = net.b
+        z = self.level[net.level]['z']
         a = _lib.CompositeArgs()
-        a.n_rays, a.n_samples = self.n, ss
-        a.flags = _lib.SRF_COMPOSITE_WHITE_BKGD if self.white else 0
+        a.n_rays, a.n_samples = self.n, z.shape[1]
+        a.flags = (_lib.SRF_COMPOSITE_WHITE_BKGD if self.white else 0) | (_lib.SRF_COMPOSITE_NDC if self.ndc else 0)
         a.distance_scale = 1.0
-        a.sigma, a.rgb, a.z, a.rays_d = b['sigma'].data_ptr(), b['rgb'].data_ptr(), b['z'].data_ptr(), \
+        a.sigma, a.rgb, a.z, a.rays_d = b['sigma'].data_ptr(), b['rgb'].data_ptr(), z.data_ptr(), \
             self.rays_d.data_ptr()
+        if self.ndc:
+            a.rays_o, a.rays_d_ndc = self.rays_o.data_ptr(), self.rays_d_ndc.data_ptr()
         if not backward:
             a.rgb_map, a.acc, a.depth = b['rgb_map'].data_ptr(), b['acc'].data_ptr(), b['depth'].data_ptr()
             a.depth_var, a.weights = b['depth_var'].data_ptr(), b['weights'].data_ptr()
+            if self.ndc:
+                a.depth_ndc, a.depth_var_ndc = b['depth_ndc'].data_ptr(), b['depth_var_ndc'].data_ptr()
         else:
             a.g_rgb, a.g_depth = b['g_rgb'].data_ptr(), b['g_depth'].data_ptr()
             a.d_sigma, a.d_rgb = b['d_sigma'].data_ptr(), b['d_rgb'].data_ptr()
@@ -158,37 +211,58 @@ class NerfTrainStep:
         st = _P(torch.cuda.current_stream(self.dev).cuda_stream)
         chk = _lib.check
         n = self.n
-        chk(lib.srf_ndc_rays(None, _vp(self.rays_d), None, None, n, 1, 1, 0.0, None, None, _vp(self.vdirs), st),
-            'view_dirs')
-        self.loss.zero_()
-        chk(lib.srf_stratified_z(_vp(self.buf['coarse']['z']), _vp(self.u_c), n, self.sc, self.near, self.far, 0, st),
-            'stratified_z')
-        for tag in ('coarse', 'fine'):
-            b = self.buf[tag]
-            net = self.nets[tag]
-            ss = b['z'].shape[1]
-            if tag == 'fine':
-                cb = self.buf['coarse']
-                chk(lib.srf_fine_z(_vp(b['z']), _vp(cb['z']), _vp(cb['weights']), _vp(self.u_f), n, self.sc, self.sf,
-                                   st), 'fine_z')
-            chk(lib.srf_ray_points(_vp(self.rays_o), _vp(self.rays_d), _vp(b['z']), n, ss, _vp(b['pts']), st),
-                'ray_points')
-            chk(lib.srf_nerf_mlp_forward(ctypes.byref(self.spec.desc), net.pptr, _vp(b['pts']), _vp(self.vdirs), ss,
-                                         n * ss, None, _vp(b['sigma']), _vp(b['rgb']), self.precision, 1, _vp(b['ws']),
-                                         b['ws'].numel(), st), 'mlp_forward')
-            chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(tag, False)), st), 'composite_forward')
-            chk(lib.srf_rgb_depth_loss(_vp(b['rgb_map']), _vp(self.target_rgb), _vp(b['depth']),
-                                       _vp(self.target_depth), _vp(self.depth_mask), n, self.n_depth,
-                                       self.depth_weight, _vp(self.loss), _vp(b['g_rgb']), _vp(b['g_depth']), st),
-                'loss')
-        for tag in ('fine', 'coarse'):
-            b = self.buf[tag]
-            net = self.nets[tag]
-            ss = b['z'].shape[1]
-            chk(lib.srf_composite_backward(ctypes.byref(self._composite_args(tag, True)), st), 'composite_backward')
-            chk(lib.srf_nerf_mlp_backward(ctypes.byref(self.spec.desc), net.pptr, _vp(b['d_sigma']), _vp(b['d_rgb']),
-                                          ss, n * ss, net.gptr, 0, self.precision, _vp(b['ws']), b['ws'].numel(), st),
-                'mlp_backward')
+        if self.ndc:
+            h, w = self.ndc['h'], self.ndc['w']
+            chk(lib.srf_ndc_rays(_vp(self.rays_o), _vp(self.rays_d), _vp(self.focal), _vp(self.focal), n, h, w,
+                                 float(self.ndc['near']), _vp(self.rays_o_ndc), _vp(self.rays_d_ndc),
+                                 _vp(self.vdirs), st), 'ndc_rays')
+            po, pd = self.rays_o_ndc, self.rays_d_ndc
+        else:
+            chk(lib.srf_ndc_rays(None, _vp(self.rays_d), None, None, n, 1, 1, 0.0, None, None, _vp(self.vdirs),
+                                 st), 'view_dirs')
+            po, pd = self.rays_o, self.rays_d
+        if self.train:
+            self.loss.zero_()
+        zc = self.level['coarse']['z']
+        u_c, u_f = (self.u_c, self.u_f) if self.perturb else (None, None)
+        chk(lib.srf_stratified_z(_vp(zc), _vp(u_c), n, self.sc, self.near, self.far, 0, st), 'stratified_z')
+        main_coarse = self.run[0]
+        for level in ('coarse', 'fine'):
+            lv = self.level[level]
+            ss = lv['z'].shape[1]
+            if level == 'fine':
+                chk(lib.srf_fine_z(_vp(lv['z']), _vp(zc), _vp(main_coarse.b['weights']), _vp(u_f), n, self.sc,
+                                   self.sf, st), 'fine_z')
+            chk(lib.srf_ray_points(_vp(po), _vp(pd), _vp(lv['z']), n, ss, _vp(lv['pts']), st), 'ray_points')
+            for net in (x for x in self.run if x.level == level):
+                b = net.b
+                chk(lib.srf_nerf_mlp_forward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(lv['pts']),
+                                             _vp(self.vdirs), ss, n * ss, None, _vp(b['sigma']), _vp(b['rgb']),
+                                             self.precision, int(self.train), _vp(b['ws']), b['ws'].numel(), st),
+                    'mlp_forward')
+                chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(net, False)), st),
+                    'composite_forward')
+                if not self.train:
+                    continue
+                chk(lib.srf_rgb_depth_loss(_vp(b['rgb_map']), _vp(self.target_rgb), _vp(b['depth']),
+                                           _vp(self.target_depth), _vp(self.depth_mask), n, self.n_depth,
+                                           self.depth_weight, _vp(self.loss), _vp(b['g_rgb']), _vp(b['g_depth']),
+                                           st), 'loss')
+        if not self.train:
+            return
+        # augmented depth as a (detached) target of the main coarse depth
+        for net in self.run[2:]:
+            if net.level == 'coarse' and self.consistency_weight > 0:
+                chk(lib.srf_depth_consistency_loss(_vp(main_coarse.b['depth']), _vp(net.b['depth']), None, n,
+                                                   self.consistency_weight, _vp(self.loss),
+                                                   _vp(main_coarse.b['g_depth']), st), 'consistency')
+        for net in reversed(self.run):
+            b = net.b
+            ss = self.level[net.level]['z'].shape[1]
+            chk(lib.srf_composite_backward(ctypes.byref(self._composite_args(net, True)), st), 'composite_backward')
+            chk(lib.srf_nerf_mlp_backward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(b['d_sigma']),
+                                          _vp(b['d_rgb']), ss, n * ss, net.state.gptr, 0, self.precision, _vp(b['ws']),
+                                          b['ws'].numel(), st), 'mlp_backward')
         chk(lib.srf_counter_add(_vp(self.step_count), 1, st), 'counter')
         for net in self.nets.values():
             chk(lib.srf_adam_step(_vp(net.flat), _vp(net.grad), _vp(net.m), _vp(net.v), net.flat.numel(), self.lr,
@@ -227,14 +301,19 @@ class NerfTrainStep:
             self._enqueue()
 
     def outputs(self):
-        return {f'{k}_{tag}': self.buf[tag][k] for tag in ('coarse', 'fine')
-                for k in ('rgb_map', 'acc', 'depth', 'depth_var', 'weights', 'z')}
+        out = {}
+        for net in self.run:
+            for k in ('rgb_map', 'acc', 'depth', 'depth_var', 'weights') + (('depth_ndc',) if self.ndc else ()):
+                out[f'{k}_{net.name}'] = net.b[k]
+            out[f'z_{net.name}'] = self.level[net.level]['z']
+        return out
 
 
 def main(argv=None):
-    """Run the fused training step on synthetic config-2 data and print ms/step:
+    """Run a fused training step on synthetic data and print ms/step:
 
         python -m simple_rf_gb300.train_step --rays 4096 --steps 10 --warmup 3 [--precision fp32] [--eager]
+            [--config nerf|nerf_pair]
     """
     import argparse
     import json
@@ -244,12 +323,13 @@ def main(argv=None):
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--precision', default='bf16', choices=['bf16', 'fp32'])
     ap.add_argument('--eager', action='store_true', help='launch kernels directly instead of replaying a CUDA graph')
+    ap.add_argument('--config', default='nerf', choices=['nerf', 'nerf_pair'])
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
     dev = torch.device('cuda')
-    step = NerfTrainStep(args.rays, 64, 128, precision=args.precision, device=dev)
-    step.set_batch(*synthetic_batch(args.rays, 64, 128, seed=1, device=dev))
+    step, batch_fn = make_step(args.config, args.rays, args.precision, dev)
+    step.set_batch(*batch_fn(1, dev))
     if not args.eager:
         step.capture(warmup=1)
     for _ in range(args.warmup):
@@ -262,7 +342,7 @@ def main(argv=None):
     e1.record()
     e1.synchronize()
     ms = e0.elapsed_time(e1) / max(args.steps, 1)
-    print(json.dumps({'rays': args.rays, 'precision': args.precision, 'graph': not args.eager,
+    print(json.dumps({'config': args.config, 'rays': args.rays, 'precision': args.precision, 'graph': not args.eager,
                       'ms_per_step': round(ms, 4), 'rays_per_s': round(args.rays / ms * 1e3, 1),
                       'loss': float(step.loss.item())}))
 
@@ -284,6 +364,54 @@ def synthetic_batch(n_rays, n_coarse, n_fine, seed, device='cpu', pin=False):
     if str(device) != 'cpu':
         out = [x.to(device) for x in out]
     return out
+
+
+def synthetic_batch_ndc(n_rays, n_coarse, n_fine, seed, device='cpu', pin=False):
+    """Forward-facing synthetic inputs: origins on the z = -1 plane with x, y ~ U[-1, 1];
+    directions normalise (U[-0.2, 0.2], U[-0.2, 0.2], U[-1.2, -0.8]); rgb targets
+    ~ U[0,1]^3; depth targets unused (zeros); stratified/pdf uniforms ~ U[0,1)."""
+    g = torch.Generator().manual_seed(seed)
+    o = torch.rand(n_rays, 3, generator=g) * 2 - 1
+    o[:, 2] = -1.0
+    d = torch.rand(n_rays, 3, generator=g)
+    d[:, :2] = d[:, :2] * 0.4 - 0.2
+    d[:, 2] = -(d[:, 2] * 0.4 + 0.8)
+    d = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    t_rgb = torch.rand(n_rays, 3, generator=g)
+    t_depth = torch.zeros(n_rays)
+    u_c = torch.rand(n_rays, n_coarse, generator=g)
+    u_f = torch.rand(n_rays, n_fine, generator=g)
+    out = [o, d, t_rgb, t_depth, u_c, u_f]
+    if pin:
+        out = [x.pin_memory() for x in out]
+    if str(device) != 'cpu':
+        out = [x.to(device) for x in out]
+    return out
+
+
+AUG_VIEWS = ('views_augmentation', dict(points_pe_degree=4, use_view_dirs=False, view_dependent_rgb=False))
+NDC_LLFF = dict(h=378, w=504, focal=400.0, near=1.0)
+
+
+def make_step(config, n_rays=4096, precision='bf16', device='cuda', seed=0, **kw):
+    """The two training-step workloads by name:
+
+    'nerf'      -- world rays, coarse + fine nets, white background, 25% depth-supervised rays;
+    'nerf_pair' -- NDC forward-facing rays (H 378, W 504, focal 400, near 1), main coarse + fine
+                   nets plus a coarse augmented net (PE L=4 on xyz, no view directions) on the
+                   same coarse samples, its depth a 0.1-weighted squared-error target of the
+                   main coarse depth, no sparse-depth rays, black background.
+    Returns (step, batch_fn) where batch_fn(seed, device, pin) makes matching inputs.
+    """
+    if config == 'nerf':
+        step = NerfTrainStep(n_rays, 64, 128, precision=precision, device=device, seed=seed, **kw)
+        return step, lambda sd, dev, pin=False: synthetic_batch(n_rays, 64, 128, sd, dev, pin)
+    if config == 'nerf_pair':
+        args = dict(white_bkgd=False, depth_fraction=0.0, ndc=NDC_LLFF, aug=[AUG_VIEWS], consistency_weight=0.1)
+        args.update(kw)
+        step = NerfTrainStep(n_rays, 64, 128, precision=precision, device=device, seed=seed, **args)
+        return step, lambda sd, dev, pin=False: synthetic_batch_ndc(n_rays, 64, 128, sd, dev, pin)
+    raise ValueError(f'unknown training-step workload {config!r}')
 
 
 if __name__ == '__main__':

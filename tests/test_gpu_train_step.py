@@ -2,9 +2,10 @@
 and the drop-in GbSimpleNeRF against the oracle's render.
 
 FP32 plain path: rgb/depth/weights within 1e-5 relative (absolute floor 1e-6 of
-the value range) of the float32 oracle; parameter gradients within 1e-4 relative
-L2 per tensor of the float64 oracle (3e-4: PE scales the float32 rounding of the
-sample positions by up to 2^9, which the float32 oracle shares).
+the value range) of the float32 oracle; parameter gradients (of a network whose
+sigma-head bias keeps every ray off the last-sample step) within 3e-4 relative
+L2 per tensor of the float64 oracle, which is given the same float32 sample
+positions (PE scales their rounding by up to 2^9).
 BF16 path: rendered rgb within 2e-3 max-abs of the float64 oracle; whole-gradient
 relative L2 of each net within 1e-2 of the float64 oracle.
 The fine pass is compared on the depths the GPU sampled (the inverse-CDF
@@ -49,7 +50,7 @@ def _oracle(params, host, z_fine, dtype):
     spec = on.MlpSpec()
     p = {tag: {k: v.astype(dtype) for k, v in params[tag].items()} for tag in params}
     ret, caches = on.render_rays(p['coarse'], p['fine'], spec, spec, o, d, 2.0, 6.0, 64, 128, u_c, u_f,
-                                 white_bkgd=True, z_fine=z_fine.astype(dtype))
+                                 white_bkgd=True, z_fine=z_fine.astype(dtype), pts_fp32=True)
     n = o.shape[0]
     mask = np.zeros(n, dtype)
     mask[:n // 4] = 1
@@ -71,11 +72,25 @@ def test_fp32_train_step_matches_oracle():
             rtol = 3e-5 if k == 'depth' else 1e-5
             np.testing.assert_allclose(out[f'{k}_{tag}'], ref, rtol=rtol,
                                        atol=1e-6 * max(1.0, float(np.abs(ref).max())), err_msg=f'{k}_{tag}')
+
+
+def test_fp32_train_step_gradients_against_fp64_oracle():
+    """Parameter gradients of the FP32 plain step vs the float64 oracle.
+
+    The non-NDC last sample has delta = 1e10 |d| (SimpleNeRF17.py:489-492), so
+    alpha_last is a step function of sigma at 0 and a ray whose last raw sigma
+    lies within float32 rounding of 0 has an ill-conditioned gradient (any two
+    implementations disagree there).  The sigma-head bias is set to 0.5 so no
+    ray sits on that step; the comparison then measures the kernels."""
+    step, params, out, grads, host = _run_step('fp32', sigma_bias=0.5)
     _, _, g64 = _oracle(params, host, out['z_fine'], np.float64)
+    worst = 0.0
     for tag in ('coarse', 'fine'):
         for k, ref in g64[tag].items():
             rel = np.linalg.norm(grads[tag][k] - ref) / max(np.linalg.norm(ref), 1e-30)
+            worst = max(worst, rel)
             assert rel < 3e-4, (tag, k, rel)
+    print('fp32 step worst per-tensor gradient rel-L2', worst)
 
 
 def test_bf16_train_step_against_fp64_oracle():
