@@ -113,7 +113,41 @@ typedef struct {
     int skip_layer;              /* 4: concat [input, h] after this layer        */
 } srf_nerf_mlp_desc;
 
-enum { SRF_PRECISION_FP32 = 0, SRF_PRECISION_BF16 = 1 };
+/* FP32: the plain path (SIMT, FP32 throughout).  BF16 / FP16: tcgen05 tensor
+ * cores with FP32 master weights and FP32 accumulation, 16-bit operands of that
+ * format.  FP16 keeps 3 more mantissa bits (forward activations are the dominant
+ * source of gradient error) and its backward runs on loss-scaled gradients:
+ * it needs an srf_loss_scaler. */
+enum { SRF_PRECISION_FP32 = 0, SRF_PRECISION_BF16 = 1, SRF_PRECISION_FP16 = 2 };
+
+/* Dynamic loss scale in device memory, with torch.cuda.amp.GradScaler's
+ * semantics (torch/amp/grad_scaler.py: init scale 2^16, growth 2 every 2000
+ * clean steps, backoff 0.5): the FP16 backward multiplies the incoming
+ * gradients by `scale` and its weight/bias gradients by inv_scale, and sets
+ * found_inf when a stored 16-bit value is not finite or out of range (the
+ * forward sets it too).  A step that found inf is skipped (srf_adam_step's
+ * skip_dev) and backs the scale off. */
+typedef struct {
+    float scale;
+    float inv_scale;
+    int32_t found_inf;
+    int32_t growth_tracker;
+} srf_loss_scaler;
+
+/* scaler_dev = {init_scale, 1 / init_scale, 0, 0}. */
+int srf_loss_scaler_init(srf_loss_scaler* scaler_dev, float init_scale, void* stream);
+/* Per-call scale for a backward whose gradients have no running scale: the
+ * largest |value| over a (na) and b (nb) maps to within a factor 2 below
+ * target, scale = 2^floor(log2(target / max)) in [2^-24, 2^40] (1 when max is 0);
+ * found_inf and growth_tracker are cleared. */
+int srf_loss_scaler_fit(srf_loss_scaler* scaler_dev, const float* a, int64_t na, const float* b, int64_t nb,
+                        float target, void* stream);
+/* End of a step: if found_inf, scale *= backoff and growth_tracker = 0, else
+ * growth_tracker += 1 and, on reaching growth_interval, scale *= growth and
+ * growth_tracker = 0; then inv_scale = 1 / scale and found_inf = 0
+ * (torch's _amp_update_scale_). */
+int srf_loss_scaler_update(srf_loss_scaler* scaler_dev, float growth, float backoff, int growth_interval,
+                           void* stream);
 
 /* Number of parameter tensors and, for index i, the reference state_dict name
  * and element count (order = the order the params/grads arrays use). */
@@ -127,20 +161,24 @@ size_t srf_nerf_mlp_workspace_size(const srf_nerf_mlp_desc* desc, int64_t m, int
  * directions shared by dir_div consecutive samples (NULL when !use_view_dirs);
  * sigma_noise (m) pre-scaled raw_noise_std*randn or NULL.  Outputs sigma (m)
  * after ReLU and rgb (m,3) after sigmoid.  With for_backward, the workspace keeps
- * what srf_nerf_mlp_backward needs (same workspace, same inputs).
+ * what srf_nerf_mlp_backward needs (same workspace, same inputs).  scaler
+ * (optional; 16-bit precisions) receives found_inf when an activation overflows.
  * Replaces MLP.forward (src/models/SimpleNeRF17.py:696-785) including the
  * chunking of run_network/batchify (:419-484). */
 int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* const* params, const float* pts,
                          const float* dirs, int dir_div, int64_t m, const float* sigma_noise, float* sigma,
                          float* rgb, int precision, int for_backward, void* workspace, size_t workspace_bytes,
-                         void* stream);
+                         srf_loss_scaler* scaler, void* stream);
 
 /* Backward: dsigma (m) w.r.t. the ReLU'd sigma, drgb (m,3) w.r.t. the sigmoid
  * rgb; dir_div as in the forward.  grads[i] receives (accumulate ? += : =) the
- * gradient of params[i].  Uses the activations the forward left in the workspace. */
+ * gradient of params[i].  Uses the activations the forward left in the workspace.
+ * SRF_PRECISION_FP16 requires scaler (the gradients are unscaled before they are
+ * written; a non-finite or out-of-range scaled value sets found_inf). */
 int srf_nerf_mlp_backward(const srf_nerf_mlp_desc* desc, const float* const* params, const float* dsigma,
                           const float* drgb, int dir_div, int64_t m, float* const* grads, int accumulate,
-                          int precision, void* workspace, size_t workspace_bytes, void* stream);
+                          int precision, void* workspace, size_t workspace_bytes, srf_loss_scaler* scaler,
+                          void* stream);
 
 /* BF16 tcgen05 dense layer (the building block of the BF16 MLP path):
  * out[m, :n] = relu?(x0[m, :k0] . Wb^T + x1[m, :k1] . Wb'^T + bias) * (mask > 0)?
@@ -318,11 +356,13 @@ int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* d
 
 /* Fused Adam (torch.optim.Adam semantics, bias-corrected, no amsgrad) over n
  * elements; step is the 1-based step count after this update, or, when
- * step_dev != NULL, read from device memory (for CUDA-graph replays).
+ * step_dev != NULL, read from device memory (for CUDA-graph replays).  When
+ * skip_dev != NULL and *skip_dev != 0 nothing is updated (a loss-scaled step
+ * that found inf, as GradScaler.step skips optimizer.step).
  * Replaces the optimizer step of Trainer10.train_one_iter (src/Trainer10.py:110). */
 int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
                   float beta1, float beta2, float eps, float weight_decay, int step, const int32_t* step_dev,
-                  void* stream);
+                  const int32_t* skip_dev, void* stream);
 /* Depth-consistency term of AugmentationsDepthLoss11.compute_depth_mse
  * (src/loss_functions/AugmentationsDepthLoss11.py:208-226): with m_r = mask[r]
  * (all ones when mask == NULL), loss += weight * mean_r m_r (pred_r - target_r)^2
@@ -332,8 +372,9 @@ int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_av
  * (the reference picks it by patch reprojection, :105-190). */
 int srf_depth_consistency_loss(const float* pred, const float* target, const uint8_t* mask, int n, float weight,
                                float* loss_dev, float* grad, void* stream);
-/* *counter_dev += value on the stream (advances a graph-replayed step count). */
-int srf_counter_add(int32_t* counter_dev, int value, void* stream);
+/* *counter_dev += value on the stream (advances a graph-replayed step count),
+ * unless skip_dev != NULL and *skip_dev != 0. */
+int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, void* stream);
 /* Sample points pts (N*S,3) = o + d * z (src/models/SimpleNeRF17.py:213-215). */
 int srf_ray_points(const float* rays_o, const float* rays_d, const float* z, int n_rays, int n_samples, float* pts,
                    void* stream);

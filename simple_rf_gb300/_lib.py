@@ -43,6 +43,8 @@ SRF_COMPOSITE_NDC = 1
 SRF_COMPOSITE_WHITE_BKGD = 2
 SRF_PRECISION_FP32 = 0
 SRF_PRECISION_BF16 = 1
+SRF_PRECISION_FP16 = 2
+PRECISIONS = {'fp32': SRF_PRECISION_FP32, 'bf16': SRF_PRECISION_BF16, 'fp16': SRF_PRECISION_FP16}
 SRF_ACT_NONE, SRF_ACT_RELU, SRF_ACT_SIGMOID = 0, 1, 2
 
 # name -> (restype, argtypes)
@@ -63,9 +65,12 @@ _SIGS = {
                                         ctypes.POINTER(c_int64)]),
     'srf_nerf_mlp_workspace_size': (c_size_t, [ctypes.POINTER(NerfMlpDesc), c_int64, c_int, c_int]),
     'srf_nerf_mlp_forward': (c_int, [ctypes.POINTER(NerfMlpDesc), ctypes.POINTER(P), P, P, c_int, c_int64, P, P, P,
-                                     c_int, c_int, P, c_size_t, P]),
+                                     c_int, c_int, P, c_size_t, P, P]),
     'srf_nerf_mlp_backward': (c_int, [ctypes.POINTER(NerfMlpDesc), ctypes.POINTER(P), P, P, c_int, c_int64,
-                                      ctypes.POINTER(P), c_int, c_int, P, c_size_t, P]),
+                                      ctypes.POINTER(P), c_int, c_int, P, c_size_t, P, P]),
+    'srf_loss_scaler_init': (c_int, [P, c_float, P]),
+    'srf_loss_scaler_update': (c_int, [P, c_float, c_float, c_int, P]),
+    'srf_loss_scaler_fit': (c_int, [P, P, c_int64, P, c_int64, c_float, P]),
     'srf_bf16_linear': (c_int, [P, c_int64, P, c_int64, c_int, P, c_int64, c_int, P, c_int64, c_int, c_int, P,
                                 c_int64, c_int, c_int, P, c_int64, P, P]),
     'srf_bf16_wgrad_workspace_size': (c_size_t, [c_int, c_int]),
@@ -94,8 +99,8 @@ _SIGS = {
                                     c_int, c_int, P]),
     'srf_positional_encoding_backward': (c_int, [P, P, P, c_int, c_int64, P, c_int, c_int, P]),
     'srf_rgb_depth_loss': (c_int, [P, P, P, P, P, c_int, c_int, c_float, P, P, P, P]),
-    'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P, P]),
-    'srf_counter_add': (c_int, [P, c_int, P]),
+    'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P, P, P]),
+    'srf_counter_add': (c_int, [P, c_int, P, P]),
     'srf_depth_consistency_loss': (c_int, [P, P, P, c_int, c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
     'srf_launch_count': (c_int64, []),

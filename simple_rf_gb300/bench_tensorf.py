@@ -98,7 +98,7 @@ class TensorfTrainStep:
             if p.grad is None:
                 continue
             _lib.call('srf_adam_step', F._ptr(p.data), F._ptr(p.grad.contiguous(memory_format=_fmt(p))), F._ptr(m),
-                      F._ptr(v), p.numel(), lr, 0.9, 0.99, 1e-8, 0.0, self.t, None, st)
+                      F._ptr(v), p.numel(), lr, 0.9, 0.99, 1e-8, 0.0, self.t, None, None, st)
         self.last = {'loss': loss.detach(), 'samples': counts}
         return loss
 

@@ -455,7 +455,9 @@ extern "C" size_t srf_nerf_mlp_workspace_size(const srf_nerf_mlp_desc* desc, int
     if (!desc || m < 0) return 0;
     MlpLayout L(*desc);
     if (!L.valid) return 0;
-    if (precision == SRF_PRECISION_BF16) return mlp_tc_workspace(L, m, for_backward != 0);
+    if (precision == SRF_PRECISION_BF16 || precision == SRF_PRECISION_FP16)
+        return mlp_tc_workspace(L, m, for_backward != 0);
+    if (precision != SRF_PRECISION_FP32) return 0;
     return mlp_f32_workspace(L, m, for_backward != 0);
 }
 
@@ -469,7 +471,7 @@ static int check_params(const MlpLayout& L, const float* const* p) {
 extern "C" int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* const* params, const float* pts,
                                     const float* dirs, int dir_div, int64_t m, const float* sigma_noise,
                                     float* sigma, float* rgb, int precision, int for_backward, void* workspace,
-                                    size_t workspace_bytes, void* stream) {
+                                    size_t workspace_bytes, srf_loss_scaler* scaler, void* stream) {
     if (!desc || !pts || !sigma || !rgb) return SRF_ERR_NULL;
     MlpLayout L(*desc);
     if (!L.valid) return SRF_ERR_UNSUPPORTED;
@@ -479,9 +481,9 @@ extern "C" int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* 
     if (st) return st;
     if (m == 0) return SRF_OK;
     if (!workspace) return SRF_ERR_WORKSPACE;
-    if (precision == SRF_PRECISION_BF16)
+    if (precision == SRF_PRECISION_BF16 || precision == SRF_PRECISION_FP16)
         return mlp_tc_forward(L, params, pts, dirs, dir_div, m, sigma_noise, sigma, rgb, for_backward != 0, workspace,
-                              workspace_bytes, as_stream(stream));
+                              workspace_bytes, precision == SRF_PRECISION_FP16 ? 1 : 0, scaler, as_stream(stream));
     if (precision != SRF_PRECISION_FP32) return SRF_ERR_UNSUPPORTED;
     return mlp_f32_forward(L, params, pts, dirs, dir_div, m, sigma_noise, sigma, rgb, for_backward != 0, workspace,
                            workspace_bytes, as_stream(stream));
@@ -489,8 +491,10 @@ extern "C" int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* 
 
 extern "C" int srf_nerf_mlp_backward(const srf_nerf_mlp_desc* desc, const float* const* params, const float* dsigma,
                                      const float* drgb, int dir_div, int64_t m, float* const* grads, int accumulate,
-                                     int precision, void* workspace, size_t workspace_bytes, void* stream) {
+                                     int precision, void* workspace, size_t workspace_bytes, srf_loss_scaler* scaler,
+                                     void* stream) {
     if (!desc || !dsigma || !drgb || !grads) return SRF_ERR_NULL;
+    if (precision == SRF_PRECISION_FP16 && !scaler) return SRF_ERR_NULL;
     MlpLayout L(*desc);
     if (!L.valid) return SRF_ERR_UNSUPPORTED;
     int st = check_params(L, params);
@@ -512,8 +516,9 @@ extern "C" int srf_nerf_mlp_backward(const srf_nerf_mlp_desc* desc, const float*
     }
     if (m == 0) return SRF_OK;
     if (!workspace) return SRF_ERR_WORKSPACE;
-    if (precision == SRF_PRECISION_BF16)
-        return mlp_tc_backward(L, params, dsigma, drgb, m, dir_div, grads, workspace, workspace_bytes, s);
+    if (precision == SRF_PRECISION_BF16 || precision == SRF_PRECISION_FP16)
+        return mlp_tc_backward(L, params, dsigma, drgb, m, dir_div, grads, workspace, workspace_bytes,
+                               precision == SRF_PRECISION_FP16 ? 1 : 0, scaler, s);
     if (precision != SRF_PRECISION_FP32) return SRF_ERR_UNSUPPORTED;
     return mlp_f32_backward(L, params, dsigma, drgb, m, dir_div, grads, workspace, workspace_bytes, s);
 }

@@ -36,10 +36,12 @@ struct MlpLayout {
 };
 
 size_t mlp_tc_workspace(const MlpLayout& L, int64_t m, bool bwd);
+// fmt: tc::kFmtBF16 (0) or tc::kFmtF16 (1); scaler: optional in the forward, required by the FP16 backward
 int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, const float* dirs, int dir_div,
                    int64_t m, const float* noise, float* sigma, float* rgb, bool bwd, void* ws, size_t ws_bytes,
-                   cudaStream_t s);
+                   int fmt, srf_loss_scaler* scaler, cudaStream_t s);
 int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsigma, const float* drgb, int64_t m,
-                    int dir_div, float* const* G, void* ws, size_t ws_bytes, cudaStream_t s);
+                    int dir_div, float* const* G, void* ws, size_t ws_bytes, int fmt, srf_loss_scaler* scaler,
+                    cudaStream_t s);
 
 }  // namespace srf

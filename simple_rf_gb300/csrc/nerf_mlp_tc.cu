@@ -1,5 +1,7 @@
-// BF16 tensor-core (tcgen05) path of the NeRF MLP: FP32 master weights, BF16
-// activations in HBM, FP32 accumulation in tensor memory.  PE sin/cos is
+// 16-bit tensor-core (tcgen05) path of the NeRF MLP: FP32 master weights, BF16
+// or FP16 operands (weights and activations in HBM), FP32 accumulation in tensor
+// memory.  The FP16 format keeps 3 more mantissa bits; its backward runs on
+// loss-scaled gradients (srf_loss_scaler) so they stay in range.  PE sin/cos is
 // computed in FP32; the small heads (sigma: 1 output, rgb: 3 outputs) are FP32
 // dot products fused into the epilogue of the layer that feeds them.
 //
@@ -18,7 +20,7 @@
 
 namespace srf {
 
-using bf16 = __nv_bfloat16;
+using op16 = uint16_t;   // one 16-bit operand word: BF16 or FP16 bits, by the path's format
 
 namespace {
 
@@ -89,8 +91,11 @@ int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
 
 }  // namespace
 
-tc::GemmEpilogue make_epilogue(bf16* out, int64_t ld_out, const float* bias, int relu) {
+tc::GemmEpilogue make_epilogue(op16* out, int64_t ld_out, const float* bias, int relu, int fmt = tc::kFmtBF16,
+                               int* found_inf = nullptr) {
     tc::GemmEpilogue ep{};
+    ep.fmt = fmt;
+    ep.found_inf = found_inf;
     ep.out = out;
     ep.ld_out = ld_out;
     ep.bias = bias;
@@ -102,9 +107,9 @@ tc::GemmEpilogue make_epilogue(bf16* out, int64_t ld_out, const float* bias, int
 
 // ep.out[m, :n] = epilogue(x0[m, :k0] . B0^T + x1[m, :k1] . B1^T) with B the rows
 // [w_row0, w_row0 + n) of the BF16 matrix w (w_rows x ldw, K-major).
-int tc_linear(const tc::GemmEpilogue& ep, const bf16* x0, int64_t ld0, int k0, const bf16* x1, int64_t ld1, int k1,
-              const bf16* w, int64_t ldw, int w_rows, int w_row0, int64_t M, int n, cudaStream_t s) {
-    const bf16* mask = ep.mask;
+int tc_linear(const tc::GemmEpilogue& ep, const op16* x0, int64_t ld0, int k0, const op16* x1, int64_t ld1, int k1,
+              const op16* w, int64_t ldw, int w_rows, int w_row0, int64_t M, int n, cudaStream_t s) {
+    const op16* mask = ep.mask;
     const int64_t ld_out = ep.ld_out, ld_mask = ep.ld_mask;
     if (M <= 0) return SRF_OK;
     if (!ep.out || !x0 || !w) return SRF_ERR_NULL;
@@ -140,8 +145,9 @@ size_t tc_wgrad_partial_floats(int n_dz, int np) {
 }
 
 // partial[split, n, k] = sum_m dz[m, n] x[m, k] (x = [x0 | x1]); returns the split count.
-int tc_wgrad(float* partial, size_t partial_floats, const bf16* dz, int64_t ld_dz, int n_dz, const bf16* x0,
-             int64_t ld0, int k0, const bf16* x1, int64_t ld1, int k1, int64_t M, int* splits_out, cudaStream_t s) {
+int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_dz, int n_dz, const op16* x0,
+             int64_t ld0, int k0, const op16* x1, int64_t ld1, int k1, int64_t M, int* splits_out, cudaStream_t s,
+             int fmt = tc::kFmtBF16) {
     if (n_dz % 128 || k0 % 64 || k1 % 64 || k0 <= 0 || k0 + k1 > 512) return SRF_ERR_UNSUPPORTED;
     if (ld_dz < n_dz || ld0 < k0 || (k1 && (!x1 || ld1 < k1))) return SRF_ERR_SHAPE;
     if (!ok16(dz) || !ok16(x0) || (x1 && !ok16(x1)) || (ld_dz % 8) || (ld0 % 8) || (x1 && (ld1 % 8)))
@@ -176,7 +182,7 @@ int tc_wgrad(float* partial, size_t partial_floats, const bf16* dz, int64_t ld_d
         }
         attr_done = true;
     }
-    tc::WgradShape sh{M, chunk, n_dz, k0 / 64, k1 / 64};
+    tc::WgradShape sh{M, chunk, n_dz, k0 / 64, k1 / 64, fmt};
     dim3 grid(ntile, splits);
     tc::tc_wgrad_kernel<<<grid, tc::kThreads, tc::wgrad_smem(nchunks), s>>>(mdz, m0, m1, sh, partial,
                                                                           device_flag());
@@ -207,21 +213,22 @@ __device__ __forceinline__ int ref_col(const LayerMap& L, int kp) {
     return -1;
 }
 
-// W (n x kref, fp32) -> Wp (n x kpad, bf16) and WT (kpad x n, bf16).
-__global__ void pack_weight_kernel(LayerMap L, const float* __restrict__ w, bf16* wp, bf16* wt) {
+// W (n x kref, fp32) -> Wp (n x kpad) and WT (kpad x n), 16-bit words of format fmt.
+__global__ void pack_weight_kernel(LayerMap L, const float* __restrict__ w, op16* wp, op16* wt, int fmt) {
     int kp = blockIdx.x * blockDim.x + threadIdx.x;
     int n = blockIdx.y;
     int kpad = L.kpad();
     if (kp >= kpad) return;
     int rc = ref_col(L, kp);
     float v = rc >= 0 ? w[int64_t(n) * L.kref() + rc] : 0.f;
-    bf16 b = __float2bfloat16_rn(v);
+    op16 b = tc::to16(v, fmt);
     wp[int64_t(n) * kpad + kp] = b;
     wt[int64_t(kp) * L.n + n] = b;
 }
 
-// grad[n, ref] += sum_s partial[s, n, kp] for the mapped columns.
-__global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits, int n_dz, float* grad) {
+// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns.
+__global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits, int n_dz, float* grad,
+                                    const float* gscale) {
     int kp = blockIdx.x * blockDim.x + threadIdx.x;
     int n = blockIdx.y;
     int kpad = L.kpad();
@@ -230,6 +237,7 @@ __global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partia
     if (rc < 0) return;
     float acc = 0.f;
     for (int sp = 0; sp < splits; ++sp) acc += partial[(int64_t(sp) * n_dz + n) * kpad + kp];
+    if (gscale) acc *= gscale[1];
     grad[int64_t(n) * L.kref() + rc] += acc;
 }
 
@@ -243,10 +251,10 @@ __device__ __forceinline__ float pe_column(const float (&x)[3], int col) {
 }
 
 // enc[m] = PE(pts[m], Lp)[:pin] zero-padded to enc_w; vext[m] = [PE(pts[m])[pin:ppe],
-// PE(dirs[m/div], Lv)] zero-padded to vx_w.  One thread writes one 16-byte chunk
-// (8 BF16 columns) of a row, so a warp stores whole contiguous rows.
-__global__ void encode_bf16_kernel(const float* __restrict__ pts, const float* __restrict__ dirs, int div, int64_t M,
-                                   int lp, int lv, int pin, int enc_w, int vx_w, bf16* enc, bf16* vext) {
+// PE(dirs[m/div], Lv)] zero-padded to vx_w, in format fmt.  One thread writes one
+// 16-byte chunk (8 columns) of a row, so a warp stores whole contiguous rows.
+__global__ void encode16_kernel(const float* __restrict__ pts, const float* __restrict__ dirs, int div, int64_t M,
+                                int lp, int lv, int pin, int enc_w, int vx_w, op16* enc, op16* vext, int fmt) {
     const int ce = enc_w / 8, cv = vext ? vx_w / 8 : 0, per = ce + cv;
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= M * per) return;
@@ -277,18 +285,19 @@ __global__ void encode_bf16_kernel(const float* __restrict__ pts, const float* _
             v[i] = col < c0 ? pe_column(p, pin + col) : (col < c0 + vpe ? pe_column(q, col - c0) : 0.f);
         }
     }
-    uint4 packed = make_uint4(tc::pack_bf16(v[0], v[1]), tc::pack_bf16(v[2], v[3]), tc::pack_bf16(v[4], v[5]),
-                              tc::pack_bf16(v[6], v[7]));
-    bf16* dst = chunk < ce ? enc + m * enc_w + chunk * 8 : vext + m * vx_w + (chunk - ce) * 8;
+    uint4 packed = make_uint4(tc::pack16(v[0], v[1], fmt), tc::pack16(v[2], v[3], fmt), tc::pack16(v[4], v[5], fmt),
+                              tc::pack16(v[6], v[7], fmt));
+    op16* dst = chunk < ce ? enc + m * enc_w + chunk * 8 : vext + m * vx_w + (chunk - ce) * 8;
     *reinterpret_cast<uint4*>(dst) = packed;
 }
 
 // Backward of a small head (1-4 outputs) fused with what consumes it, in one
-// pass over the head's input activation h (BF16, M x K):
+// pass over the head's input activation h (16-bit format fmt, M x K):
 //   g[m]       = head output gradients (mode 3: rgb; mode 4: sigma + rgb), through
 //                the ReLU of the raw sigma and the sigmoid of rgb;
-//   dz[m, k]   = (sum_u g[m, u] W[u, k]) * (h[m, k] > 0)   (BF16, the previous layer's dZ)
-//   colsum[k] += sum_m dz[m, k]                           (that layer's bias gradient)
+//   dz[m, k]   = S (sum_u g[m, u] W[u, k]) * (h[m, k] > 0)   (fmt, the previous layer's dZ,
+//                times the loss scale S = gscale[0], 1 when gscale is NULL)
+//   colsum[k] += sum_m dz[m, k] / S                          (that layer's bias gradient)
 //   dW[u, k]  += sum_m g[m, u] h[m, k];  db[u] += sum_m g[m, u]  (the head's own gradients)
 // One thread owns 8 consecutive columns (a 16-byte chunk) of a row; a block
 // covers rows_per_block rows and strides over the rest, keeping its partial
@@ -297,8 +306,12 @@ template <int NO>
 __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict__ dsigma,
                                       const float* __restrict__ sraw, const float* __restrict__ drgb,
                                       const float* __restrict__ rgb, const float* __restrict__ W,
-                                      const bf16* __restrict__ h, bf16* dz, float* colsum, float* dW, float* db) {
+                                      const op16* __restrict__ h, op16* dz, float* colsum, float* dW, float* db,
+                                      int fmt, const float* gscale, int* found_inf) {
     extern __shared__ float red[];
+    const float gs0 = gscale ? gscale[0] : 1.f, gs1 = gscale ? gscale[1] : 1.f;
+    const float vmax = tc::fmt_max(fmt);
+    bool bad = false;
     const int cpr = K / 8;
     const int rpb = blockDim.x / cpr;
     const int chunk = threadIdx.x % cpr, rloc = threadIdx.x / cpr;
@@ -333,7 +346,7 @@ __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict_
         float hx[8];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            float2 f = tc::unpack_bf16(w4[q]);
+            float2 f = tc::unpack16(w4[q], fmt);
             hx[2 * q] = f.x;
             hx[2 * q + 1] = f.y;
         }
@@ -346,12 +359,13 @@ __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict_
                 v += g[u] * w[u][i];
                 dwl[u][i] += g[u] * hx[i];
             }
-            o[i] = hx[i] > 0.f ? v : 0.f;
+            o[i] = hx[i] > 0.f ? v * gs0 : 0.f;
             cs[i] += o[i];
+            bad |= !(fabsf(o[i]) <= vmax);
         }
         *reinterpret_cast<uint4*>(dz + r * K + chunk * 8) =
-            make_uint4(tc::pack_bf16(o[0], o[1]), tc::pack_bf16(o[2], o[3]), tc::pack_bf16(o[4], o[5]),
-                       tc::pack_bf16(o[6], o[7]));
+            make_uint4(tc::pack16(o[0], o[1], fmt), tc::pack16(o[2], o[3], fmt), tc::pack16(o[4], o[5], fmt),
+                       tc::pack16(o[6], o[7], fmt));
         if (chunk == 0) {
 #pragma unroll
             for (int u = 0; u < NO; ++u) dbl[u] += g[u];
@@ -369,7 +383,12 @@ __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict_
         }
         __syncthreads();
     };
-    if (colsum) reduce(cs, colsum);
+    if (found_inf && bad) atomicExch(found_inf, 1);
+    if (colsum) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) cs[i] *= gs1;
+        reduce(cs, colsum);
+    }
 #pragma unroll
     for (int u = 0; u < NO; ++u) reduce(dwl[u], dW + u * K);
     if (chunk == 0) {
@@ -380,14 +399,15 @@ __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict_
 
 template <int NO>
 int head_bwd_fused(int64_t M, int K, const float* dsigma, const float* sraw, const float* drgb, const float* rgb,
-                   const float* W, const bf16* h, bf16* dz, float* colsum, float* dW, float* db, cudaStream_t s) {
+                   const float* W, const op16* h, op16* dz, float* colsum, float* dW, float* db, int fmt,
+                   const float* gscale, int* found_inf, cudaStream_t s) {
     const int threads = 256;
     const int rpb = threads / (K / 8);
     int64_t blocks = (M + rpb - 1) / rpb;
     if (blocks > int64_t(num_sms()) * 8) blocks = int64_t(num_sms()) * 8;
     if (blocks < 1) blocks = 1;
     head_bwd_fused_kernel<NO><<<unsigned(blocks), threads, size_t(rpb) * K * sizeof(float), s>>>(
-        M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum, dW, db);
+        M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum, dW, db, fmt, gscale, found_inf);
     return launch_status();
 }
 
@@ -443,56 +463,56 @@ struct TcLayout {
 };
 
 struct TcWs {
-    bf16* enc; bf16* vext;
-    std::vector<bf16*> h, hv;
-    bf16* feat;
+    op16* enc; op16* vext;
+    std::vector<op16*> h, hv;
+    op16* feat;
     float* sraw; float* rgb;
-    std::vector<bf16*> W, WT, Wv, WTv;
-    bf16* Wf; bf16* WTf;
-    bf16* dz0; bf16* dz1; bf16* dfeat;
+    std::vector<op16*> W, WT, Wv, WTv;
+    op16* Wf; op16* WTf;
+    op16* dz0; op16* dz1; op16* dfeat;
     float* dsig; float* dout; float* partial; size_t partial_floats;
 };
 
 size_t carve_tc(const MlpLayout& L, const TcLayout& T, int64_t m, bool bwd, void* base, size_t cap, TcWs* out) {
     Carver c(base, cap);
     TcWs w;
-    w.enc = c.take<bf16>(size_t(m) * T.enc_w);
-    w.vext = L.vdep ? c.take<bf16>(size_t(m) * T.vx_w) : nullptr;
+    w.enc = c.take<op16>(size_t(m) * T.enc_w);
+    w.vext = L.vdep ? c.take<op16>(size_t(m) * T.vx_w) : nullptr;
     if (bwd) {
         // the backward reads every layer's activation
-        for (int j = 0; j < L.Dp; ++j) w.h.push_back(c.take<bf16>(size_t(m) * L.Wp));
-        w.feat = L.vdep ? c.take<bf16>(size_t(m) * L.Wp) : nullptr;
-        for (int j = 0; L.vdep && j < L.Dv; ++j) w.hv.push_back(c.take<bf16>(size_t(m) * L.Wv));
+        for (int j = 0; j < L.Dp; ++j) w.h.push_back(c.take<op16>(size_t(m) * L.Wp));
+        w.feat = L.vdep ? c.take<op16>(size_t(m) * L.Wp) : nullptr;
+        for (int j = 0; L.vdep && j < L.Dv; ++j) w.hv.push_back(c.take<op16>(size_t(m) * L.Wv));
     } else {
         // forward only: layer j reads only layer j-1 (the skip input is the
         // encoding, kept separately), so two activation buffers alternate
-        bf16* ping = c.take<bf16>(size_t(m) * L.Wp);
-        bf16* pong = L.Dp > 1 || L.vdep ? c.take<bf16>(size_t(m) * L.Wp) : ping;
+        op16* ping = c.take<op16>(size_t(m) * L.Wp);
+        op16* pong = L.Dp > 1 || L.vdep ? c.take<op16>(size_t(m) * L.Wp) : ping;
         for (int j = 0; j < L.Dp; ++j) w.h.push_back(j & 1 ? pong : ping);
         // feature layer reads h[Dp-1]; the view layers read the feature, then each other
-        bf16* other = (L.Dp - 1) & 1 ? ping : pong;
+        op16* other = (L.Dp - 1) & 1 ? ping : pong;
         w.feat = L.vdep ? other : nullptr;
-        bf16* hv0 = (L.vdep && L.Dv > 0) ? c.take<bf16>(size_t(m) * L.Wv) : nullptr;
-        bf16* hv1 = (L.vdep && L.Dv > 1) ? c.take<bf16>(size_t(m) * L.Wv) : hv0;
+        op16* hv0 = (L.vdep && L.Dv > 0) ? c.take<op16>(size_t(m) * L.Wv) : nullptr;
+        op16* hv1 = (L.vdep && L.Dv > 1) ? c.take<op16>(size_t(m) * L.Wv) : hv0;
         for (int j = 0; L.vdep && j < L.Dv; ++j) w.hv.push_back(j & 1 ? hv1 : hv0);
     }
     w.sraw = c.take<float>(size_t(m));
     w.rgb = c.take<float>(size_t(m) * 3);
     for (auto& lm : T.trunk) {
-        w.W.push_back(c.take<bf16>(size_t(lm.n) * lm.kpad()));
-        w.WT.push_back(c.take<bf16>(size_t(lm.n) * lm.kpad()));
+        w.W.push_back(c.take<op16>(size_t(lm.n) * lm.kpad()));
+        w.WT.push_back(c.take<op16>(size_t(lm.n) * lm.kpad()));
     }
-    w.Wf = c.take<bf16>(size_t(L.Wp) * L.Wp);
-    w.WTf = c.take<bf16>(size_t(L.Wp) * L.Wp);
+    w.Wf = c.take<op16>(size_t(L.Wp) * L.Wp);
+    w.WTf = c.take<op16>(size_t(L.Wp) * L.Wp);
     for (auto& lm : T.view) {
-        w.Wv.push_back(c.take<bf16>(size_t(lm.n) * lm.kpad()));
-        w.WTv.push_back(c.take<bf16>(size_t(lm.n) * lm.kpad()));
+        w.Wv.push_back(c.take<op16>(size_t(lm.n) * lm.kpad()));
+        w.WTv.push_back(c.take<op16>(size_t(lm.n) * lm.kpad()));
     }
     int wmax = L.Wp > L.Wv ? L.Wp : L.Wv;
     if (bwd) {
-        w.dz0 = c.take<bf16>(size_t(m) * wmax);
-        w.dz1 = c.take<bf16>(size_t(m) * wmax);
-        w.dfeat = L.vdep ? c.take<bf16>(size_t(m) * L.Wp) : nullptr;
+        w.dz0 = c.take<op16>(size_t(m) * wmax);
+        w.dz1 = c.take<op16>(size_t(m) * wmax);
+        w.dfeat = L.vdep ? c.take<op16>(size_t(m) * L.Wp) : nullptr;
         w.dsig = c.take<float>(size_t(m));
         w.dout = c.take<float>(size_t(m) * 4);
         w.partial_floats = tc_wgrad_partial_floats(wmax, 512);
@@ -506,20 +526,28 @@ size_t carve_tc(const MlpLayout& L, const TcLayout& T, int64_t m, bool bwd, void
     return c.used;
 }
 
-int pack(const LayerMap& lm, const float* w, bf16* wp, bf16* wt, cudaStream_t s) {
+int pack(const LayerMap& lm, const float* w, op16* wp, op16* wt, int fmt, cudaStream_t s) {
     dim3 grid((lm.kpad() + 127) / 128, lm.n);
-    pack_weight_kernel<<<grid, 128, 0, s>>>(lm, w, wp, wt);
+    pack_weight_kernel<<<grid, 128, 0, s>>>(lm, w, wp, wt, fmt);
     return launch_status();
 }
 
-int wgrad_layer(const LayerMap& lm, const TcWs& w, const bf16* dz, const bf16* x0, int64_t ld0, const bf16* x1,
-                int64_t ld1, int64_t M, float* grad, cudaStream_t s) {
+// Operand format and loss scaler of one forward/backward call.
+struct TcCtx {
+    int fmt;
+    srf_loss_scaler* scaler;   // {scale, 1/scale, found_inf, growth}; required by the FP16 backward
+    const float* gscale() const { return scaler ? &scaler->scale : nullptr; }
+    int* found_inf() const { return scaler ? &scaler->found_inf : nullptr; }
+};
+
+int wgrad_layer(const LayerMap& lm, const TcWs& w, const op16* dz, const op16* x0, int64_t ld0, const op16* x1,
+                int64_t ld1, int64_t M, float* grad, const TcCtx& cx, cudaStream_t s) {
     int splits = 0;
     int st = tc_wgrad(w.partial, w.partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
-                      lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s);
+                      lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt);
     if (st) return st;
     dim3 grid((lm.kpad() + 127) / 128, lm.n);
-    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, w.partial, splits, lm.n, grad);
+    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, w.partial, splits, lm.n, grad, cx.gscale());
     return launch_status();
 }
 
@@ -533,31 +561,32 @@ size_t mlp_tc_workspace(const MlpLayout& L, int64_t m, bool bwd) {
 
 int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, const float* dirs, int dir_div,
                    int64_t m, const float* noise, float* sigma, float* rgb, bool bwd, void* ws, size_t ws_bytes,
-                   cudaStream_t s) {
+                   int fmt, srf_loss_scaler* scaler, cudaStream_t s) {
+    const TcCtx cx{fmt, scaler};
     TcLayout T(L);
     if (!T.ok) return SRF_ERR_UNSUPPORTED;
     TcWs w;
     if (carve_tc(L, T, m, bwd, ws, ws_bytes, &w) > ws_bytes) return SRF_ERR_WORKSPACE;
     int st;
     for (int j = 0; j < L.Dp; ++j)
-        if ((st = pack(T.trunk[j], P[L.idx_trunk_w(j)], w.W[j], w.WT[j], s))) return st;
+        if ((st = pack(T.trunk[j], P[L.idx_trunk_w(j)], w.W[j], w.WT[j], fmt, s))) return st;
     if (L.vdep) {
-        if ((st = pack(T.feat, P[L.idx_feat_w()], w.Wf, w.WTf, s))) return st;
+        if ((st = pack(T.feat, P[L.idx_feat_w()], w.Wf, w.WTf, fmt, s))) return st;
         for (int j = 0; j < L.Dv; ++j)
-            if ((st = pack(T.view[j], P[L.idx_view_w(j)], w.Wv[j], w.WTv[j], s))) return st;
+            if ((st = pack(T.view[j], P[L.idx_view_w(j)], w.Wv[j], w.WTv[j], fmt, s))) return st;
     }
     const int enc_threads = (T.enc_w + (L.vdep ? T.vx_w : 0)) / 8;
-    encode_bf16_kernel<<<grid_1d(m * enc_threads, 256), 256, 0, s>>>(pts, L.vpe ? dirs : nullptr, dir_div, m,
+    encode16_kernel<<<grid_1d(m * enc_threads, 256), 256, 0, s>>>(pts, L.vpe ? dirs : nullptr, dir_div, m,
                                                                      L.desc.points_pe_degree, L.desc.views_pe_degree,
                                                                      L.pin, T.enc_w, T.vx_w, w.enc,
-                                                                     L.vdep ? w.vext : nullptr);
+                                                                     L.vdep ? w.vext : nullptr, fmt);
     if ((st = launch_status())) return st;
     for (int j = 0; j < L.Dp; ++j) {
         const LayerMap& lm = T.trunk[j];
-        const bf16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
+        const op16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
-        const bf16* x1 = lm.nsrc > 1 ? w.h[j - 1] : nullptr;
-        tc::GemmEpilogue ep = make_epilogue(w.h[j], L.Wp, P[L.idx_trunk_w(j) + 1], 1);
+        const op16* x1 = lm.nsrc > 1 ? w.h[j - 1] : nullptr;
+        tc::GemmEpilogue ep = make_epilogue(w.h[j], L.Wp, P[L.idx_trunk_w(j) + 1], 1, fmt, cx.found_inf());
         if (j == L.Dp - 1) {
             // sigma head (and, without view dependence, the rgb head) on the last trunk layer's rows
             ep.head_mode = L.vdep ? tc::kHeadSigma : tc::kHeadSigmaRgb;
@@ -574,15 +603,15 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
         if (st) return st;
     }
     if (!L.vdep) return SRF_OK;
-    const bf16* hl = w.h[L.Dp - 1];
-    st = tc_linear(make_epilogue(w.feat, L.Wp, P[L.idx_feat_w() + 1], 0), hl, L.Wp, L.Wp, nullptr, 0, 0, w.Wf, L.Wp,
-                   L.Wp, 0, m, L.Wp, s);
+    const op16* hl = w.h[L.Dp - 1];
+    st = tc_linear(make_epilogue(w.feat, L.Wp, P[L.idx_feat_w() + 1], 0, fmt, cx.found_inf()), hl, L.Wp, L.Wp,
+                   nullptr, 0, 0, w.Wf, L.Wp, L.Wp, 0, m, L.Wp, s);
     if (st) return st;
     for (int j = 0; j < L.Dv; ++j) {
         const LayerMap& lm = T.view[j];
-        const bf16* x0 = j == 0 ? w.feat : w.hv[j - 1];
+        const op16* x0 = j == 0 ? w.feat : w.hv[j - 1];
         int64_t ld0 = j == 0 ? L.Wp : L.Wv;
-        tc::GemmEpilogue ep = make_epilogue(w.hv[j], L.Wv, P[L.idx_view_w(j) + 1], 1);
+        tc::GemmEpilogue ep = make_epilogue(w.hv[j], L.Wv, P[L.idx_view_w(j) + 1], 1, fmt, cx.found_inf());
         if (j == L.Dv - 1) {
             ep.head_mode = tc::kHeadRgb;
             ep.head_w = P[L.idx_rgb_w()];
@@ -598,29 +627,39 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
 }
 
 int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsigma, const float* drgb, int64_t m,
-                    int dir_div, float* const* G, void* ws, size_t ws_bytes, cudaStream_t s) {
+                    int dir_div, float* const* G, void* ws, size_t ws_bytes, int fmt, srf_loss_scaler* scaler,
+                    cudaStream_t s) {
     (void)dir_div;
+    const TcCtx cx{fmt, scaler};
+    // a dgrad epilogue in this call's format, with the loss scale applied
+    auto bwd_epilogue = [&](op16* out, int64_t ld) {
+        tc::GemmEpilogue ep = make_epilogue(out, ld, nullptr, 0, fmt, cx.found_inf());
+        ep.gscale = cx.gscale();
+        return ep;
+    };
     TcLayout T(L);
     if (!T.ok) return SRF_ERR_UNSUPPORTED;
     TcWs w;
     if (carve_tc(L, T, m, true, ws, ws_bytes, &w) > ws_bytes) return SRF_ERR_WORKSPACE;
     int st;
-    bf16* dz = w.dz0;
-    bf16* dz2 = w.dz1;
-    const bf16* hl = w.h[L.Dp - 1];
+    op16* dz = w.dz0;
+    op16* dz2 = w.dz1;
+    const op16* hl = w.h[L.Dp - 1];
     if (L.vdep) {
         // rgb head: dZ of the last view layer, its bias gradient, the head's dW/db
         st = head_bwd_fused<3>(m, L.Wv, nullptr, nullptr, drgb, w.rgb, P[L.idx_rgb_w()], w.hv[L.Dv - 1], dz,
-                               G[L.idx_view_w(L.Dv - 1) + 1], G[L.idx_rgb_w()], G[L.idx_rgb_w() + 1], s);
+                               G[L.idx_view_w(L.Dv - 1) + 1], G[L.idx_rgb_w()], G[L.idx_rgb_w() + 1], fmt,
+                               cx.gscale(), cx.found_inf(), s);
         if (st) return st;
         for (int j = L.Dv - 1; j >= 0; --j) {
             const LayerMap& lm = T.view[j];
-            const bf16* x0 = j == 0 ? w.feat : w.hv[j - 1];
+            const op16* x0 = j == 0 ? w.feat : w.hv[j - 1];
             int64_t ld0 = j == 0 ? L.Wp : L.Wv;
-            st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.vext : nullptr, T.vx_w, m, G[L.idx_view_w(j)], s);
+            st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.vext : nullptr, T.vx_w, m, G[L.idx_view_w(j)], cx,
+                             s);
             if (st) return st;
             if (j > 0) {
-                tc::GemmEpilogue ep = make_epilogue(dz2, L.Wv, nullptr, 0);
+                tc::GemmEpilogue ep = bwd_epilogue(dz2, L.Wv);
                 ep.mask = w.hv[j - 1];
                 ep.ld_mask = L.Wv;
                 ep.colsum = G[L.idx_view_w(j - 1) + 1];
@@ -628,18 +667,18 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
                 if (st) return st;
                 std::swap(dz, dz2);
             } else {
-                tc::GemmEpilogue ep = make_epilogue(w.dfeat, L.Wp, nullptr, 0);
+                tc::GemmEpilogue ep = bwd_epilogue(w.dfeat, L.Wp);
                 ep.colsum = G[L.idx_feat_w() + 1];
                 st = tc_linear(ep, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[0], L.Wv, lm.kpad(), 0, m, L.Wp, s);
                 if (st) return st;
             }
         }
-        st = wgrad_layer(T.feat, w, w.dfeat, hl, L.Wp, nullptr, 0, m, G[L.idx_feat_w()], s);
+        st = wgrad_layer(T.feat, w, w.dfeat, hl, L.Wp, nullptr, 0, m, G[L.idx_feat_w()], cx, s);
         if (st) return st;
         // feature-layer dgrad with the sigma head's adjoint fused in: dZ_last =
         // (dfeat . Wf + dsig w_sigma) * (h_last > 0), dsig = dsigma * (sraw > 0);
         // the same pass adds the sigma head's weight (sum dsig h_last) and bias gradients
-        tc::GemmEpilogue ep = make_epilogue(dz, L.Wp, nullptr, 0);
+        tc::GemmEpilogue ep = bwd_epilogue(dz, L.Wp);
         ep.mask = hl;
         ep.ld_mask = L.Wp;
         ep.r1_row = dsigma;
@@ -652,18 +691,20 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         if (st) return st;
     } else {
         st = head_bwd_fused<4>(m, L.Wp, dsigma, w.sraw, drgb, w.rgb, P[L.idx_out_w()], hl, dz,
-                               G[L.idx_trunk_w(L.Dp - 1) + 1], G[L.idx_out_w()], G[L.idx_out_w() + 1], s);
+                               G[L.idx_trunk_w(L.Dp - 1) + 1], G[L.idx_out_w()], G[L.idx_out_w() + 1], fmt,
+                               cx.gscale(), cx.found_inf(), s);
         if (st) return st;
     }
     for (int j = L.Dp - 1; j >= 0; --j) {
         const LayerMap& lm = T.trunk[j];
-        const bf16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
+        const op16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
-        st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.h[j - 1] : nullptr, L.Wp, m, G[L.idx_trunk_w(j)], s);
+        st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.h[j - 1] : nullptr, L.Wp, m, G[L.idx_trunk_w(j)], cx,
+                         s);
         if (st) return st;
         if (j == 0) break;
         int row0 = lm.nsrc > 1 ? lm.padw[0] : 0;
-        tc::GemmEpilogue ep = make_epilogue(dz2, L.Wp, nullptr, 0);
+        tc::GemmEpilogue ep = bwd_epilogue(dz2, L.Wp);
         ep.mask = w.h[j - 1];
         ep.ld_mask = L.Wp;
         ep.colsum = G[L.idx_trunk_w(j - 1) + 1];
@@ -684,12 +725,12 @@ extern "C" int srf_bf16_linear(void* out, int64_t ld_out, const void* x0, int64_
                                int64_t ld1, int k1, const void* w, int64_t ldw, int w_rows, int w_row0,
                                const float* bias, int64_t m, int n, int relu, const void* mask, int64_t ld_mask,
                                float* colsum, void* stream) {
-    tc::GemmEpilogue ep = make_epilogue(static_cast<bf16*>(out), ld_out, bias, relu);
-    ep.mask = static_cast<const bf16*>(mask);
+    tc::GemmEpilogue ep = make_epilogue(static_cast<op16*>(out), ld_out, bias, relu);
+    ep.mask = static_cast<const op16*>(mask);
     ep.ld_mask = ld_mask;
     ep.colsum = colsum;
-    return tc_linear(ep, static_cast<const bf16*>(x0), ld0, k0, static_cast<const bf16*>(x1), ld1, k1,
-                     static_cast<const bf16*>(w), ldw, w_rows, w_row0, m, n, as_stream(stream));
+    return tc_linear(ep, static_cast<const op16*>(x0), ld0, k0, static_cast<const op16*>(x1), ld1, k1,
+                     static_cast<const op16*>(w), ldw, w_rows, w_row0, m, n, as_stream(stream));
 }
 
 extern "C" size_t srf_bf16_wgrad_workspace_size(int n_dz, int k_total) {
@@ -701,7 +742,7 @@ extern "C" int srf_bf16_wgrad(float* partial, size_t partial_bytes, int* splits,
                               int64_t m, void* stream) {
     if (!partial || !splits || !dz || !x0) return SRF_ERR_NULL;
     if (m <= 0) return SRF_ERR_SHAPE;
-    return tc_wgrad(partial, partial_bytes / sizeof(float), static_cast<const bf16*>(dz), ld_dz, n_dz,
-                    static_cast<const bf16*>(x0), ld0, k0, static_cast<const bf16*>(x1), ld1, k1, m, splits,
+    return tc_wgrad(partial, partial_bytes / sizeof(float), static_cast<const op16*>(dz), ld_dz, n_dz,
+                    static_cast<const op16*>(x0), ld0, k0, static_cast<const op16*>(x1), ld1, k1, m, splits,
                     as_stream(stream));
 }

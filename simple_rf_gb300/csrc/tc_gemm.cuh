@@ -32,16 +32,22 @@ enum { kHeadNone = 0, kHeadSigma = 1, kHeadRgb = 2, kHeadSigmaRgb = 3 };
 struct GemmEpilogue {
     const float* bias;              // [N] or NULL
     int relu;                       // apply ReLU to the result
-    const __nv_bfloat16* mask;      // multiply by (mask[m, n] > 0) when non-NULL
+    int fmt;                        // operand / output format (kFmtBF16, kFmtF16)
+    const uint16_t* mask;           // multiply by (mask[m, n] > 0) when non-NULL
     int64_t ld_mask;
     const float* r1_row;            // result += r1[m] * r1_col[n] (before ReLU/mask) when non-NULL, where
     const float* r1_col;            // r1[m] = r1_row[m], or 0 when r1_gate is given and r1_gate[m] <= 0
     const float* r1_gate;
     float* r1_mask_colsum;          // += sum_m r1[m] * mask[m, n]   (the head's weight gradient)
     float* r1_sum;                  // += sum_m r1[m]                (the head's bias gradient)
-    __nv_bfloat16* out;             // [M, ld_out] BF16
+    uint16_t* out;                  // [M, ld_out] in fmt
     int64_t ld_out;
     float* colsum;                  // += column sums of the stored values (a bias gradient) when non-NULL
+    // Loss scale of a scaled backward: {scale, 1 / scale}.  The r1 term enters the
+    // stored values multiplied by scale; colsum receives the sums times 1 / scale.
+    // NULL = 1.  The head gradients (r1_mask_colsum, r1_sum) are never scaled.
+    const float* gscale;
+    int* found_inf;                 // set to 1 when a stored value is not finite or exceeds the fmt range
     // Head fused on the FP32 result rows: 1 (sigma), 3 (rgb) or 4 (sigma + rgb) dot products.
     int head_mode;
     const float* head_w;            // [units][N]
@@ -190,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(b_full, 0, nullptr)) *abort_flag = 1;
     } else if (warp == 1 && lane == 0) {
         // -------------------------------------------------------------- MMA
-        constexpr uint32_t idesc = idesc_bf16(kBlockM, BN, 0, 0);
+        const uint32_t idesc = idesc_f16(kBlockM, BN, 0, 0, ep.fmt);
         bool ok = mbar_wait(b_full, 0, abort_flag);
         uint32_t it = 0, t = 0;
         for (int64_t tile = blockIdx.x; ok && tile < num_tiles; tile += gridDim.x, ++t) {
@@ -214,7 +220,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int k = 0; k < kBlockK / 16; ++k) {
                     uint64_t ad = smem_desc(a_addr + k * 32, 0, 1024, kSwizzle128B);
                     uint64_t bd = smem_desc(b_addr + k * 32, 0, 1024, kSwizzle128B);
-                    mma_bf16(d_tmem, ad, bd, idesc, (kb | k) != 0);
+                    mma_f16(d_tmem, ad, bd, idesc, (kb | k) != 0);
                 }
                 mma_commit(&empty[s]);
             }
@@ -230,6 +236,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int q = warp & 3;   // tensor-memory lane quadrant this warp may read
         uint32_t t = 0;
         float r1_total = 0.f;
+        const float gs0 = ep.gscale ? ep.gscale[0] : 1.f;
+        const float vmax = fmt_max(ep.fmt);
+        bool bad = false;
         for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
             uint32_t acc = t & 1;
             if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
@@ -252,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     v[j] = __uint_as_float(r[j]) + sbias[c * 32 + j];
-                    if (ep.r1_row) v[j] += r1 * ep.r1_col[c * 32 + j];
+                    if (ep.r1_row) v[j] += (r1 * gs0) * ep.r1_col[c * 32 + j];
                     if (ep.relu) v[j] = v[j] > 0.f ? v[j] : 0.f;
                     if (!live) v[j] = 0.f;
                 }
@@ -268,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                             uint32_t w4[4] = {mv.x, mv.y, mv.z, mv.w};
 #pragma unroll
                             for (int h = 0; h < 4; ++h) {
-                                float2 f = unpack_bf16(w4[h]);
+                                float2 f = unpack16(w4[h], ep.fmt);
                                 mw[g * 8 + h * 2] = f.x;
                                 mw[g * 8 + h * 2 + 1] = f.y;
                                 if (!(f.x > 0.f)) v[g * 8 + h * 2] = 0.f;
@@ -295,11 +304,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 if (live) {
                     uint4* op = reinterpret_cast<uint4*>(ep.out + m * ep.ld_out + c * 32);
+                    const int f = ep.fmt;
 #pragma unroll
                     for (int g = 0; g < 4; ++g)
-                        op[g] = make_uint4(pack_bf16(v[g * 8], v[g * 8 + 1]), pack_bf16(v[g * 8 + 2], v[g * 8 + 3]),
-                                           pack_bf16(v[g * 8 + 4], v[g * 8 + 5]),
-                                           pack_bf16(v[g * 8 + 6], v[g * 8 + 7]));
+                        op[g] = make_uint4(pack16(v[g * 8], v[g * 8 + 1], f), pack16(v[g * 8 + 2], v[g * 8 + 3], f),
+                                           pack16(v[g * 8 + 4], v[g * 8 + 5], f),
+                                           pack16(v[g * 8 + 6], v[g * 8 + 7], f));
+                    if (ep.found_inf) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) bad |= !(fabsf(v[j]) <= vmax);
+                    }
                 }
                 if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
             }
@@ -330,11 +344,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int o = 16; o > 0; o >>= 1) r1_total += __shfl_xor_sync(0xffffffffu, r1_total, o);
             if (lane == 0) atomicAdd(ep.r1_sum, r1_total);
         }
+        if (ep.found_inf && __any_sync(0xffffffffu, bad) && lane == 0) atomicExch(ep.found_inf, 1);
     }
     __syncthreads();
     if (threadIdx.x == 0 && *abort_flag) raise_flag(ep.flag, kFlagTimeout);
-    if (ep.colsum)
-        for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.colsum + i, scol[i]);
+    if (ep.colsum) {
+        const float gs1 = ep.gscale ? ep.gscale[1] : 1.f;
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.colsum + i, scol[i] * gs1);
+    }
     if (ep.r1_mask_colsum)
         for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.r1_mask_colsum + i, scol2[i]);
     if (warp == 1) {
@@ -356,6 +373,7 @@ struct WgradShape {
     int64_t m_chunk;  // samples per split (multiple of 64)
     int n_dz;         // columns of dZ (rows of dW)
     int kc0, kc1;     // 64-wide column chunks of X0 / X1
+    int fmt;          // operand format (kFmtBF16, kFmtF16)
 };
 
 constexpr uint32_t kBox64Bytes = 64 * 64 * 2;
@@ -463,7 +481,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     int cnt = nchunks - p * 4 < 4 ? nchunks - p * 4 : 4;
                     uint64_t bd = smem_desc(sa + (2 + p * 4) * kBox64Bytes + ks * 2048, kBox64Bytes, 1024,
                                             kSwizzle128B);
-                    mma_bf16(tmem + uint32_t(p * 256), ad, bd, idesc_bf16(128, cnt * 64, 1, 1), (b | ks) != 0);
+                    mma_f16(tmem + uint32_t(p * 256), ad, bd, idesc_f16(128, cnt * 64, 1, 1, s.fmt),
+                             (b | ks) != 0);
                 }
             }
             mma_commit(&empty[st]);

@@ -4,6 +4,7 @@
 
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 
 #include "srf_common.cuh"
@@ -111,7 +112,7 @@ __device__ __forceinline__ void tc_fence_after() {
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, both described by shared-memory descriptors.
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -156,10 +157,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return d;
 }
 
-// Instruction descriptor of kind::f16 with BF16 A/B and FP32 accumulation.
-// a_mn / b_mn select MN-major (1) instead of K-major (0) operands.
-__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n, int a_mn, int b_mn) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(a_mn) << 15) | (uint32_t(b_mn) << 16) |
+// 16-bit operand formats of a kind::f16 MMA (A and B always share one).
+enum { kFmtBF16 = 0, kFmtF16 = 1 };
+
+// Instruction descriptor of kind::f16 with FP32 accumulation: c_format (bits 4-5)
+// = F32; a_format (7-9) and b_format (10-12) = 0 for F16, 1 for BF16; a_mn / b_mn
+// (bits 15 / 16) select MN-major (1) instead of K-major (0) operands; N >> 3 at
+// bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n, int a_mn, int b_mn, int fmt) {
+    const uint32_t ab = fmt == kFmtF16 ? 0u : 1u;
+    return (1u << 4) | (ab << 7) | (ab << 10) | (uint32_t(a_mn) << 15) | (uint32_t(b_mn) << 16) |
            (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
 }
 
@@ -172,6 +179,31 @@ __device__ __forceinline__ float2 unpack_bf16(uint32_t v) {
     __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&v);
     return __bfloat1622float2(h);
 }
+
+// Two floats -> two 16-bit words (round to nearest) of the given format; a in the low half.
+__device__ __forceinline__ uint32_t pack16(float a, float b, int fmt) {
+    if (fmt == kFmtF16) {
+        __half2 v = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t*>(&v);
+    }
+    return pack_bf16(a, b);
+}
+
+__device__ __forceinline__ float2 unpack16(uint32_t v, int fmt) {
+    if (fmt == kFmtF16) {
+        __half2 h = *reinterpret_cast<__half2*>(&v);
+        return __half22float2(h);
+    }
+    return unpack_bf16(v);
+}
+
+__device__ __forceinline__ uint16_t to16(float a, int fmt) {
+    if (fmt == kFmtF16) return __half_as_ushort(__float2half_rn(a));
+    return __bfloat16_as_ushort(__float2bfloat16_rn(a));
+}
+
+// Largest finite magnitude a stored value may have in the format (FP16: 65504).
+__host__ __device__ constexpr float fmt_max(int fmt) { return fmt == kFmtF16 ? 65504.f : 3.38e38f; }
 
 }  // namespace tc
 }  // namespace srf

@@ -43,7 +43,8 @@ __global__ void loss_kernel(const float* __restrict__ rgb, const float* __restri
 // step count t is read on the device (graph replays advance it with srf_counter_add).
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                             float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float wd,
-                            float bc1, float bc2_sqrt, const int* step_dev) {
+                            float bc1, float bc2_sqrt, const int* step_dev, const int* skip_dev) {
+    if (skip_dev && *skip_dev) return;
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t stride = int64_t(gridDim.x) * blockDim.x;
     if (step_dev) {
@@ -63,7 +64,57 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     }
 }
 
-__global__ void counter_add_kernel(int* c, int v) { *c += v; }
+__global__ void counter_add_kernel(int* c, int v, const int* skip) {
+    if (!skip || !*skip) *c += v;
+}
+
+__global__ void loss_scaler_init_kernel(srf_loss_scaler* s, float init) {
+    s->scale = init;
+    s->inv_scale = 1.f / init;
+    s->found_inf = 0;
+    s->growth_tracker = 0;
+}
+
+// growth_tracker (as float bits) <- max |x| over a and b (non-negative floats order like their bits).
+__global__ void absmax_kernel(const float* __restrict__ a, int64_t na, const float* __restrict__ b, int64_t nb,
+                              srf_loss_scaler* s) {
+    float mx = 0.f;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < na + nb; i += stride) {
+        float v = fabsf(i < na ? a[i] : b[i - na]);
+        mx = v > mx ? v : mx;   // a NaN never wins, so a non-finite input leaves the scale finite
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&s->growth_tracker, __float_as_int(mx));
+}
+
+// scale = 2^floor(log2(target / max)), within [2^-24, 2^40]; 1 when max is 0 or not finite.
+__global__ void fit_scale_kernel(srf_loss_scaler* s, float target) {
+    float mx = __int_as_float(s->growth_tracker);
+    float sc = 1.f;
+    if (mx > 0.f && mx < 3.0e38f) {
+        int e = int(floorf(log2f(target / mx)));
+        e = e < -24 ? -24 : (e > 40 ? 40 : e);
+        sc = ldexpf(1.f, e);
+    }
+    s->scale = sc;
+    s->inv_scale = 1.f / sc;
+    s->found_inf = 0;
+    s->growth_tracker = 0;
+}
+
+__global__ void loss_scaler_update_kernel(srf_loss_scaler* s, float growth, float backoff, int interval) {
+    if (s->found_inf) {
+        s->scale *= backoff;
+        s->growth_tracker = 0;
+    } else if (++s->growth_tracker >= interval) {
+        s->scale *= growth;
+        s->growth_tracker = 0;
+    }
+    s->inv_scale = 1.f / s->scale;
+    s->found_inf = 0;
+}
 
 // loss += weight * mean_r m_r (pred - target)^2;  grad[r] += 2 weight m_r (pred - target) / n
 __global__ void depth_consistency_kernel(const float* __restrict__ pred, const float* __restrict__ target,
@@ -117,9 +168,45 @@ extern "C" int srf_depth_consistency_loss(const float* pred, const float* target
     return launch_status();
 }
 
-extern "C" int srf_counter_add(int32_t* counter_dev, int value, void* stream) {
+extern "C" int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, void* stream) {
     if (!counter_dev) return SRF_ERR_NULL;
-    counter_add_kernel<<<1, 1, 0, as_stream(stream)>>>(counter_dev, value);
+    counter_add_kernel<<<1, 1, 0, as_stream(stream)>>>(counter_dev, value, skip_dev);
+    return launch_status();
+}
+
+extern "C" int srf_loss_scaler_init(srf_loss_scaler* scaler_dev, float init_scale, void* stream) {
+    if (!scaler_dev) return SRF_ERR_NULL;
+    if (!(init_scale > 0.f)) return SRF_ERR_SHAPE;
+    loss_scaler_init_kernel<<<1, 1, 0, as_stream(stream)>>>(scaler_dev, init_scale);
+    return launch_status();
+}
+
+extern "C" int srf_loss_scaler_fit(srf_loss_scaler* scaler_dev, const float* a, int64_t na, const float* b,
+                                   int64_t nb, float target, void* stream) {
+    if (!scaler_dev || (na > 0 && !a) || (nb > 0 && !b)) return SRF_ERR_NULL;
+    if (na < 0 || nb < 0 || !(target > 0.f)) return SRF_ERR_SHAPE;
+    cudaStream_t st = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(&scaler_dev->growth_tracker, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    if (na + nb > 0) {
+        unsigned blocks = grid_1d(na + nb, 256);
+        if (blocks > 152 * 4) blocks = 152 * 4;
+        absmax_kernel<<<blocks, 256, 0, st>>>(a, na, b, nb, scaler_dev);
+        int ls = launch_status();
+        if (ls) return ls;
+    }
+    fit_scale_kernel<<<1, 1, 0, st>>>(scaler_dev, target);
+    return launch_status();
+}
+
+extern "C" int srf_loss_scaler_update(srf_loss_scaler* scaler_dev, float growth, float backoff, int growth_interval,
+                                      void* stream) {
+    if (!scaler_dev) return SRF_ERR_NULL;
+    if (!(growth >= 1.f) || !(backoff > 0.f) || !(backoff <= 1.f) || growth_interval < 1) return SRF_ERR_SHAPE;
+    loss_scaler_update_kernel<<<1, 1, 0, as_stream(stream)>>>(scaler_dev, growth, backoff, growth_interval);
     return launch_status();
 }
 
@@ -148,7 +235,7 @@ extern "C" int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, con
 
 extern "C" int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
                              float beta1, float beta2, float eps, float weight_decay, int step,
-                             const int32_t* step_dev, void* stream) {
+                             const int32_t* step_dev, const int32_t* skip_dev, void* stream) {
     if (!param || !grad || !exp_avg || !exp_avg_sq) return SRF_ERR_NULL;
     if (n < 0 || (step < 1 && !step_dev)) return SRF_ERR_SHAPE;
     if (step < 1) step = 1;
@@ -158,6 +245,6 @@ extern "C" int srf_adam_step(float* param, const float* grad, float* exp_avg, fl
     unsigned blocks = grid_1d(n, 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
     adam_kernel<<<blocks, 256, 0, as_stream(stream)>>>(param, grad, exp_avg, exp_avg_sq, n, lr, beta1, beta2, eps,
-                                                       weight_decay, bc1, bc2, step_dev);
+                                                       weight_decay, bc1, bc2, step_dev, skip_dev);
     return launch_status();
 }

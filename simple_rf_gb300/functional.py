@@ -167,8 +167,27 @@ def _ptr_array(tensors):
     return arr
 
 
+def loss_scaler(device, init_scale=65536.0):
+    """A device srf_loss_scaler {scale, 1/scale, found_inf, growth_tracker} as a 16-byte tensor."""
+    t = torch.empty(4, dtype=torch.float32, device=device)
+    call('srf_loss_scaler_init', _ptr(t), float(init_scale), _stream())
+    return t
+
+
+def found_inf_ptr(scaler):
+    """Device address of the scaler's found_inf word."""
+    return None if scaler is None else ctypes.c_void_p(scaler.data_ptr() + 8)
+
+
 class NerfMlpFunction(torch.autograd.Function):
-    """MLP.forward (SimpleNeRF17.py:696-785) with the hand-written backward."""
+    """MLP.forward (SimpleNeRF17.py:696-785) with the hand-written backward.
+
+    With SRF_PRECISION_FP16 each backward fits its own loss scale to the incoming
+    gradients (the largest maps to about 2^10, leaving 2^5 of headroom for growth
+    through the layers; srf_loss_scaler_fit); a gradient that still leaves the
+    FP16 range gives non-finite parameter gradients and sets the scaler's
+    found_inf.  The fused training step (train_step.py) instead carries one
+    dynamic scale across steps and skips steps that overflow."""
 
     @staticmethod
     def forward(ctx, spec, precision, pts, dirs, dir_div, noise, *params):
@@ -184,10 +203,13 @@ class NerfMlpFunction(torch.autograd.Function):
                          device=pts.device)
         sigma = torch.empty(m, device=pts.device)
         rgb = torch.empty(m, 3, device=pts.device)
+        scaler = None
+        if precision == _lib.SRF_PRECISION_FP16:
+            scaler = loss_scaler(pts.device)
         call('srf_nerf_mlp_forward', ctypes.byref(spec.desc), _ptr_array(params), _ptr(pts), _ptr(dirs),
              int(dir_div), m, _ptr(noise), _ptr(sigma), _ptr(rgb), precision, int(need_grad), _ptr(ws),
-             ws.numel(), _stream())
-        ctx.spec, ctx.precision, ctx.dir_div, ctx.m = spec, precision, dir_div, m
+             ws.numel(), _ptr(scaler), _stream())
+        ctx.spec, ctx.precision, ctx.dir_div, ctx.m, ctx.scaler = spec, precision, dir_div, m, scaler
         ctx.ws = ws if need_grad else None
         ctx.params = params
         ctx.set_materialize_grads(True)
@@ -198,8 +220,12 @@ class NerfMlpFunction(torch.autograd.Function):
         grads = [torch.empty_like(p) for p in ctx.params]
         dsigma = dsigma.contiguous()
         drgb = drgb.contiguous()
+        if ctx.scaler is not None:
+            call('srf_loss_scaler_fit', _ptr(ctx.scaler), _ptr(dsigma), dsigma.numel(), _ptr(drgb), drgb.numel(),
+                 1024.0, _stream())
         call('srf_nerf_mlp_backward', ctypes.byref(ctx.spec.desc), _ptr_array(ctx.params), _ptr(dsigma), _ptr(drgb),
-             int(ctx.dir_div), ctx.m, _ptr_array(grads), 0, ctx.precision, _ptr(ctx.ws), ctx.ws.numel(), _stream())
+             int(ctx.dir_div), ctx.m, _ptr_array(grads), 0, ctx.precision, _ptr(ctx.ws), ctx.ws.numel(),
+             _ptr(ctx.scaler), _stream())
         ctx.ws = None
         return (None, None, None, None, None, None) + tuple(grads)
 
@@ -280,7 +306,7 @@ def adam_step(param, grad, exp_avg, exp_avg_sq, *, lr, beta1=0.9, beta2=0.999, e
     for name, x in (('param', param), ('grad', grad), ('exp_avg', exp_avg), ('exp_avg_sq', exp_avg_sq)):
         _require(x, name, param.shape)
     call('srf_adam_step', _ptr(param), _ptr(grad), _ptr(exp_avg), _ptr(exp_avg_sq), param.numel(), float(lr),
-         float(beta1), float(beta2), float(eps), float(weight_decay), int(step), None, _stream())
+         float(beta1), float(beta2), float(eps), float(weight_decay), int(step), None, None, _stream())
 
 
 def rgb_depth_loss(rgb, target_rgb, depth, target_depth, depth_mask, n_depth_rays, depth_weight, loss=None):

@@ -24,9 +24,9 @@ from . import functional as F
 
 def _precision(configs):
     p = str(configs['model'].get('precision', 'fp32')).lower()
-    if p not in ('fp32', 'bf16'):
-        raise ValueError(f"configs['model']['precision'] must be 'fp32' or 'bf16', got {p!r}")
-    return _lib.SRF_PRECISION_BF16 if p == 'bf16' else _lib.SRF_PRECISION_FP32
+    if p not in _lib.PRECISIONS:
+        raise ValueError(f"configs['model']['precision'] must be one of {sorted(_lib.PRECISIONS)}, got {p!r}")
+    return _lib.PRECISIONS[p]
 
 
 class GbMLP(torch.nn.Module):

@@ -11,7 +11,10 @@ coarse and a fine net, restated as a fixed sequence of hand-written kernels:
 
 Every buffer is allocated once, so the whole step can be captured as one CUDA
 graph and replayed.  ``precision='bf16'`` runs the MLP GEMMs on tcgen05 tensor
-cores (BF16 operands, FP32 accumulation); ``'fp32'`` is the plain path.
+cores (BF16 operands, FP32 accumulation); ``'fp16'`` does the same with FP16
+operands and a dynamic loss scale (GradScaler semantics, kept on the device: a
+step whose scaled gradients overflow is skipped and halves the scale); ``'fp32'``
+is the plain path.
 """
 import ctypes
 
@@ -19,6 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import functional as F
 from .functional import MlpSpec, _ptr_array
 
 _P = ctypes.c_void_p
@@ -125,7 +129,7 @@ class NerfTrainStep:
     def __init__(self, n_rays=4096, n_coarse=64, n_fine=128, near=2.0, far=6.0, white_bkgd=True,
                  depth_fraction=0.25, depth_weight=0.1, precision='bf16', spec_kwargs=None, lr=5e-4,
                  betas=(0.9, 0.999), eps=1e-8, seed=0, device='cuda', ndc=None, aug=None, aug_fine=False,
-                 consistency_weight=0.1, train=True, perturb=True):
+                 consistency_weight=0.1, train=True, perturb=True, loss_scale_init=65536.0):
         self.dev = torch.device(device)
         self.n, self.sc, self.sf = n_rays, n_coarse, n_fine
         self.s = n_coarse + n_fine
@@ -136,7 +140,9 @@ class NerfTrainStep:
         self.depth_weight = float(depth_weight)
         self.consistency_weight = float(consistency_weight)
         self.train, self.perturb = bool(train), bool(perturb)
-        self.precision = _lib.SRF_PRECISION_BF16 if precision == 'bf16' else _lib.SRF_PRECISION_FP32
+        self.precision = _lib.PRECISIONS[precision]
+        self.scaler = F.loss_scaler(self.dev, loss_scale_init) if self.precision == _lib.SRF_PRECISION_FP16 else None
+        self.found_inf = F.found_inf_ptr(self.scaler)
         self.lr, self.betas, self.eps = float(lr), betas, float(eps)
         self.spec = MlpSpec(**(spec_kwargs or {}))
         rng = np.random.default_rng(seed)
@@ -238,7 +244,8 @@ class NerfTrainStep:
                 b = net.b
                 chk(lib.srf_nerf_mlp_forward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(lv['pts']),
                                              _vp(self.vdirs), ss, n * ss, None, _vp(b['sigma']), _vp(b['rgb']),
-                                             self.precision, int(self.train), _vp(b['ws']), b['ws'].numel(), st),
+                                             self.precision, int(self.train), _vp(b['ws']), b['ws'].numel(),
+                                             _vp(self.scaler), st),
                     'mlp_forward')
                 chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(net, False)), st),
                     'composite_forward')
@@ -262,11 +269,14 @@ class NerfTrainStep:
             chk(lib.srf_composite_backward(ctypes.byref(self._composite_args(net, True)), st), 'composite_backward')
             chk(lib.srf_nerf_mlp_backward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(b['d_sigma']),
                                           _vp(b['d_rgb']), ss, n * ss, net.state.gptr, 0, self.precision, _vp(b['ws']),
-                                          b['ws'].numel(), st), 'mlp_backward')
-        chk(lib.srf_counter_add(_vp(self.step_count), 1, st), 'counter')
+                                          b['ws'].numel(), _vp(self.scaler), st), 'mlp_backward')
+        chk(lib.srf_counter_add(_vp(self.step_count), 1, self.found_inf, st), 'counter')
         for net in self.nets.values():
             chk(lib.srf_adam_step(_vp(net.flat), _vp(net.grad), _vp(net.m), _vp(net.v), net.flat.numel(), self.lr,
-                                  self.betas[0], self.betas[1], self.eps, 0.0, 1, _vp(self.step_count), st), 'adam')
+                                  self.betas[0], self.betas[1], self.eps, 0.0, 1, _vp(self.step_count),
+                                  self.found_inf, st), 'adam')
+        if self.scaler is not None:
+            chk(lib.srf_loss_scaler_update(_vp(self.scaler), 2.0, 0.5, 2000, st), 'loss_scaler_update')
 
     # ------------------------------------------------------------- public --
     def set_batch(self, rays_o, rays_d, target_rgb, target_depth, u_coarse, u_fine, non_blocking=True):
@@ -321,7 +331,7 @@ def main(argv=None):
     ap.add_argument('--rays', type=int, default=4096)
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
-    ap.add_argument('--precision', default='bf16', choices=['bf16', 'fp32'])
+    ap.add_argument('--precision', default='bf16', choices=['bf16', 'fp16', 'fp32'])
     ap.add_argument('--eager', action='store_true', help='launch kernels directly instead of replaying a CUDA graph')
     ap.add_argument('--config', default='nerf', choices=['nerf', 'nerf_pair'])
     args = ap.parse_args(argv)

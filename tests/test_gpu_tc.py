@@ -105,8 +105,11 @@ SPECS = {
 }
 
 
+@pytest.mark.parametrize('precision', ['bf16', 'fp16'])
 @pytest.mark.parametrize('name', list(SPECS))
-def test_bf16_mlp_against_fp64_oracle(name):
+def test_tc_mlp_against_fp64_oracle(name, precision):
+    """16-bit tensor-core MLP (forward + backward) vs the float64 oracle."""
+    from simple_rf_gb300 import _lib
     from simple_rf_gb300 import functional as F
     kw = SPECS[name]
     ospec = on.MlpSpec(points_pe_degree=kw.get('points_pe_degree', 10), use_view_dirs=kw.get('use_view_dirs', True),
@@ -123,7 +126,7 @@ def test_bf16_mlp_against_fp64_oracle(name):
     params = [torch.from_numpy(p64[k].astype(np.float32)).to(DEV).requires_grad_(True) for k in spec.param_names]
     tp = torch.from_numpy(pts.astype(np.float32)).to(DEV)
     tv = torch.from_numpy(vd.astype(np.float32)).to(DEV) if spec.use_view_dirs else None
-    sigma, rgb = F.NerfMlpFunction.apply(spec, 1, tp, tv, div, None, *params)
+    sigma, rgb = F.NerfMlpFunction.apply(spec, _lib.PRECISIONS[precision], tp, tv, div, None, *params)
     rs, rr, cache = on.mlp_forward(p64, ospec, pts.astype(np.float32).astype(np.float64),
                                    np.repeat(vd.astype(np.float32).astype(np.float64), div, 0))
     assert np.abs(rgb.detach().cpu().numpy() - rr).max() < 2e-3
@@ -136,9 +139,10 @@ def test_bf16_mlp_against_fp64_oracle(name):
     got = np.concatenate([prm.grad.double().cpu().numpy().ravel() for prm in params])
     ref = np.concatenate([gref[k].ravel() for k in spec.param_names])
     rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
-    # Independent random cotangents per sample are the worst case for BF16
+    # Independent random cotangents per sample are the worst case for 16-bit
     # operands (no cancellation between correlated samples): rounding weights and
     # stored activations to BF16 alone gives ~5% whole-gradient rel-L2 against
-    # float64 in an exact emulation (7% measured on the GPU).  The training-step
-    # loss is checked in test_gpu_train_step.py.
-    assert rel < 8e-2, rel
+    # float64 in an exact emulation (7% measured on the GPU); FP16 keeps 3 more
+    # mantissa bits.  The training-step loss is checked in test_gpu_train_step.py.
+    print(name, precision, 'whole-gradient rel-L2', rel)
+    assert rel < (8e-2 if precision == 'bf16' else 2e-2), rel

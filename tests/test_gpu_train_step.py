@@ -118,6 +118,66 @@ def test_bf16_train_step_against_fp64_oracle():
         assert rel < 3e-2, (tag, rel)
 
 
+def test_fp16_train_step_meets_gradient_bar():
+    """FP16-operand tensor-core step (dynamic loss scale) vs the float64 oracle on
+    the same non-degenerate network as the BF16 test: rgb within 2e-3 max-abs and
+    whole-gradient relative L2 of each net within 1e-2."""
+    step, params, out, grads, host = _run_step('fp16', sigma_bias=0.5)
+    ret64, _, g64 = _oracle(params, host, out['z_fine'], np.float64)
+    sc = step.scaler.cpu()
+    assert sc[0].item() == 65536.0 and sc[2:3].view(torch.int32).item() == 0, sc
+    for tag in ('coarse', 'fine'):
+        err = np.abs(out[f'rgb_map_{tag}'] - ret64[f'rgb_{tag}']).max()
+        assert err < 2e-3, (tag, err)
+        got = np.concatenate([grads[tag][k].ravel() for k in g64[tag]])
+        ref = np.concatenate([g64[tag][k].ravel() for k in g64[tag]])
+        rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        print(tag, 'fp16 whole-gradient rel-L2', rel, 'rgb max-abs', err)
+        assert rel < 1e-2, (tag, rel)
+
+
+def test_fp16_overflow_skips_the_step():
+    """A loss scale of 2^100 overflows the FP16 gradients: found_inf is raised,
+    Adam leaves every parameter and the step count untouched, and the end of the
+    step halves the scale and clears found_inf (GradScaler semantics)."""
+    from simple_rf_gb300.train_step import NerfTrainStep, synthetic_batch
+    step = NerfTrainStep(64, 64, 128, precision='fp16', device=DEV, seed=2, loss_scale_init=2.0 ** 100)
+    step.set_batch(*synthetic_batch(64, 64, 128, seed=3, device=DEV))
+    before = {tag: net.flat.clone() for tag, net in step.nets.items()}
+    step.step()
+    torch.cuda.synchronize()
+    sc = step.scaler.cpu()
+    assert sc[0].item() == 2.0 ** 99 and sc[2:3].view(torch.int32).item() == 0, sc
+    assert step.step_count.item() == 0
+    for tag, net in step.nets.items():
+        assert torch.equal(net.flat, before[tag]), tag
+    # a sane scale then trains: the parameters move
+    step.scaler.copy_(torch.tensor([65536.0, 1 / 65536.0, 0.0, 0.0]))
+    step.step()
+    torch.cuda.synchronize()
+    assert step.step_count.item() == 1
+    assert not torch.equal(step.nets['coarse'].flat, before['coarse'])
+
+
+def test_loss_scaler_update_and_fit():
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300 import functional as F
+    s = F.loss_scaler(DEV, 1024.0)
+    p, st = F._ptr(s), F._stream()
+    _lib.call('srf_loss_scaler_update', p, 2.0, 0.5, 3, st)      # clean: tracker 1
+    _lib.call('srf_loss_scaler_update', p, 2.0, 0.5, 3, st)      # clean: tracker 2
+    assert s[0].item() == 1024.0 and s[3:4].view(torch.int32).item() == 2
+    _lib.call('srf_loss_scaler_update', p, 2.0, 0.5, 3, st)      # third clean step grows the scale
+    assert s[0].item() == 2048.0 and s[1].item() == 1 / 2048.0 and s[3:4].view(torch.int32).item() == 0
+    s[2:3].view(torch.int32).fill_(1)                            # found_inf
+    _lib.call('srf_loss_scaler_update', p, 2.0, 0.5, 3, st)
+    assert s[0].item() == 1024.0 and s[2:3].view(torch.int32).item() == 0
+    a = torch.tensor([0.001, -0.5, 0.0], device=DEV)
+    b = torch.tensor([0.25, float('nan')], device=DEV)
+    _lib.call('srf_loss_scaler_fit', p, F._ptr(a), 3, F._ptr(b), 2, 1024.0, st)
+    assert s[0].item() == 2048.0 and s[1].item() == 1 / 2048.0
+
+
 def test_graph_replay_equals_eager():
     """A captured step replays the same kernels on the same buffers: two fresh
     steps (eager vs graph) from the same weights and batch give identical outputs."""
