@@ -85,7 +85,7 @@ int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
     }
     int64_t tiles = (sh.M + tc::kBlockM - 1) / tc::kBlockM;
     int grid = int(tiles < num_sms() ? tiles : num_sms());
-    tc::tc_gemm_kernel<BN><<<grid, tc::kThreads, smem, s>>>(a0, a1, b, sh, ep);
+    tc::tc_gemm_kernel<BN><<<grid, tc::kGemmThreads, smem, s>>>(a0, a1, b, sh, ep);
     return launch_status();
 }
 
@@ -241,54 +241,75 @@ __global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partia
     grad[int64_t(n) * L.kref() + rc] += acc;
 }
 
-// Column `col` of PE(x) = [x, sin(2^0 x), cos(2^0 x), ...] for a 3-vector x.
-__device__ __forceinline__ float pe_column(const float (&x)[3], int col) {
-    int j = col % 3, b = col / 3;
-    if (b == 0) return x[j];
-    int k = (b - 1) >> 1;
-    float a = x[j] * float(1 << k);
-    return ((b - 1) & 1) ? cosf(a) : sinf(a);
-}
-
 // enc[m] = PE(pts[m], Lp)[:pin] zero-padded to enc_w; vext[m] = [PE(pts[m])[pin:ppe],
-// PE(dirs[m/div], Lv)] zero-padded to vx_w, in format fmt.  One thread writes one
-// 16-byte chunk (8 columns) of a row, so a warp stores whole contiguous rows.
-__global__ void encode16_kernel(const float* __restrict__ pts, const float* __restrict__ dirs, int div, int64_t M,
-                                int lp, int lv, int pin, int enc_w, int vx_w, op16* enc, op16* vext, int fmt) {
-    const int ce = enc_w / 8, cv = vext ? vx_w / 8 : 0, per = ce + cv;
-    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= M * per) return;
-    int64_t m = t / per;
-    int chunk = int(t % per);
-    const int ppe = 3 * (2 * lp + 1);
-    const float p[3] = {pts[3 * m], pts[3 * m + 1], pts[3 * m + 2]};
-    float v[8];
-    if (chunk < ce) {
+// PE(dirs[m/div], Lv)] zero-padded to vx_w, in format fmt, with PE(x, L) = [x,
+// sin(2^0 x), cos(2^0 x), ..., sin(2^(L-1) x), cos(2^(L-1) x)] in 3-wide blocks
+// (SimpleNeRF17.py:581-613).  One thread builds one row in shared memory (one
+// sincosf per frequency and axis); the block then stores its kEncRows rows with
+// consecutive threads on consecutive 4-byte words.  The row stride of
+// enc_w + vx_w + 2 words16 (an odd number of 4-byte words) keeps the per-row
+// writes free of bank conflicts.
+constexpr int kEncRows = 64;
+
+__global__ void __launch_bounds__(kEncRows)
+    encode16_kernel(const float* __restrict__ pts, const float* __restrict__ dirs, int div, int64_t M, int lp,
+                    int lv, int pin, int enc_w, int vx_w, op16* enc, op16* vext, int fmt) {
+    extern __shared__ uint32_t enc_smem[];
+    const int stride = enc_w + vx_w + 2;   // 16-bit words per staged row
+    op16* srow = reinterpret_cast<op16*>(enc_smem);
+    const int64_t row0 = int64_t(blockIdx.x) * kEncRows;
+    const int r = threadIdx.x;
+    const int64_t m = row0 + r;
+    op16* my = srow + r * stride;
+    for (int c = 0; c < (enc_w + vx_w) / 2; ++c) reinterpret_cast<uint32_t*>(my)[c] = 0u;
+    if (m < M) {
+        const int ppe = 3 * (2 * lp + 1);
+        const float p[3] = {pts[3 * m], pts[3 * m + 1], pts[3 * m + 2]};
+        // column col of PE(pts): enc below pin, the rest continues vext (dropped when there is none)
+        auto put = [&](int col, float v) {
+            if (col < pin) my[col] = tc::to16(v, fmt);
+            else if (col - pin < vx_w) my[enc_w + (col - pin)] = tc::to16(v, fmt);
+        };
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            int col = chunk * 8 + i;
-            v[i] = col < pin ? pe_column(p, col) : 0.f;
+        for (int a = 0; a < 3; ++a) put(a, p[a]);
+        for (int k = 0; k < lp; ++k) {
+            const float f = float(1 << k);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                float sn, cs;
+                sincosf(p[a] * f, &sn, &cs);
+                put(3 + 6 * k + a, sn);
+                put(6 + 6 * k + a, cs);
+            }
         }
-    } else {
-        const int c0 = ppe - pin;   // extra PE columns of the points-augmentation variant
-        const int vpe = dirs ? 3 * (2 * lv + 1) : 0;
-        float q[3] = {0.f, 0.f, 0.f};
-        if (dirs) {
+        if (dirs && vext && (ppe - pin) + 3 * (2 * lv + 1) <= vx_w) {
             const float* d = dirs + 3 * (m / div);
-            q[0] = d[0];
-            q[1] = d[1];
-            q[2] = d[2];
-        }
+            const float q[3] = {d[0], d[1], d[2]};
+            op16* vd = my + enc_w + (ppe - pin);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            int col = (chunk - ce) * 8 + i;
-            v[i] = col < c0 ? pe_column(p, pin + col) : (col < c0 + vpe ? pe_column(q, col - c0) : 0.f);
+            for (int a = 0; a < 3; ++a) vd[a] = tc::to16(q[a], fmt);
+            for (int k = 0; k < lv; ++k) {
+                const float f = float(1 << k);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    float sn, cs;
+                    sincosf(q[a] * f, &sn, &cs);
+                    vd[3 + 6 * k + a] = tc::to16(sn, fmt);
+                    vd[6 + 6 * k + a] = tc::to16(cs, fmt);
+                }
+            }
         }
     }
-    uint4 packed = make_uint4(tc::pack16(v[0], v[1], fmt), tc::pack16(v[2], v[3], fmt), tc::pack16(v[4], v[5], fmt),
-                              tc::pack16(v[6], v[7], fmt));
-    op16* dst = chunk < ce ? enc + m * enc_w + chunk * 8 : vext + m * vx_w + (chunk - ce) * 8;
-    *reinterpret_cast<uint4*>(dst) = packed;
+    __syncthreads();
+    const int64_t rows = M - row0 < kEncRows ? M - row0 : kEncRows;
+    const uint32_t* src = enc_smem;
+    const int we = enc_w / 2, wv = vx_w / 2, ws = stride / 2;
+    uint32_t* ge = reinterpret_cast<uint32_t*>(enc + row0 * enc_w);
+    for (int w = threadIdx.x; w < rows * we; w += kEncRows) ge[w] = src[(w / we) * ws + w % we];
+    if (vext) {
+        uint32_t* gv = reinterpret_cast<uint32_t*>(vext + row0 * vx_w);
+        for (int w = threadIdx.x; w < rows * wv; w += kEncRows) gv[w] = src[(w / wv) * ws + we + w % wv];
+    }
 }
 
 // Backward of a small head (1-4 outputs) fused with what consumes it, in one
@@ -575,11 +596,13 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
         for (int j = 0; j < L.Dv; ++j)
             if ((st = pack(T.view[j], P[L.idx_view_w(j)], w.Wv[j], w.WTv[j], fmt, s))) return st;
     }
-    const int enc_threads = (T.enc_w + (L.vdep ? T.vx_w : 0)) / 8;
-    encode16_kernel<<<grid_1d(m * enc_threads, 256), 256, 0, s>>>(pts, L.vpe ? dirs : nullptr, dir_div, m,
-                                                                     L.desc.points_pe_degree, L.desc.views_pe_degree,
-                                                                     L.pin, T.enc_w, T.vx_w, w.enc,
-                                                                     L.vdep ? w.vext : nullptr, fmt);
+    {
+        const int vx = L.vdep ? T.vx_w : 0;
+        const size_t smem = size_t(kEncRows) * (T.enc_w + vx + 2) * sizeof(op16);
+        encode16_kernel<<<unsigned((m + kEncRows - 1) / kEncRows), kEncRows, smem, s>>>(
+            pts, L.vpe ? dirs : nullptr, dir_div, m, L.desc.points_pe_degree, L.desc.views_pe_degree, L.pin, T.enc_w,
+            vx, w.enc, L.vdep ? w.vext : nullptr, fmt);
+    }
     if ((st = launch_status())) return st;
     for (int j = 0; j < L.Dp; ++j) {
         const LayerMap& lm = T.trunk[j];

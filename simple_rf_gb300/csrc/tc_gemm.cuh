@@ -23,7 +23,8 @@ namespace tc {
 
 constexpr int kBlockM = 128;
 constexpr int kBlockK = 64;   // one 128-byte swizzle atom of BF16
-constexpr int kThreads = 192;
+constexpr int kThreads = 192;       // weight-gradient kernel: producer, MMA, 4 epilogue warps
+constexpr int kGemmThreads = 320;   // layer kernel: producer, MMA, 8 epilogue warps (2 per TMEM lane quadrant)
 constexpr uint32_t kATileBytes = kBlockM * kBlockK * 2;
 constexpr size_t kMaxSmem = 232448;
 
@@ -89,9 +90,11 @@ struct GemmShape {
 template <int BN>
 struct SmemPlan {
     static constexpr uint32_t kBBlockBytes = BN * kBlockK * 2;
+    // partial head sums handed between the two warps of a lane quadrant: [2 acc][128 rows][4]
+    static constexpr uint32_t kHeadXBytes = 2 * 128 * 4 * 4;
     // 1024 B alignment slack + 256 B of barriers + BN floats each of bias, column
-    // sums and r1 mask column sums + 4 x BN head weights + 4 head biases
-    static constexpr size_t kReserve = 1024 + 256 + BN * 12 + 4 * BN * 4 + 16;
+    // sums and r1 mask column sums + 4 x BN head weights + 4 head biases + head exchange
+    static constexpr size_t kReserve = 1024 + 256 + BN * 12 + 4 * BN * 4 + 16 + kHeadXBytes;
     static __host__ __device__ int stages(int kb_total) {
         size_t b = size_t(kb_total) * kBBlockBytes;
         if (b + kReserve + 2 * kATileBytes > kMaxSmem) return 0;
@@ -104,7 +107,7 @@ struct SmemPlan {
 };
 
 template <int BN>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
                    const __grid_constant__ CUtensorMap tmB, GemmShape shape, GemmEpilogue ep) {
     extern __shared__ uint8_t smem_raw[];
@@ -123,11 +126,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t* done = bars + 21;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 22);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 23);
-    float* sbias = reinterpret_cast<float*>(bars + 24);   // BN floats
+    uint64_t* hx_ready = bars + 24;     // [2 acc][4 quadrants]: half 1's partial head sums are in shx
+    float* sbias = reinterpret_cast<float*>(bars + 32);   // BN floats
     float* scol = sbias + BN;                              // BN floats
     float* scol2 = scol + BN;                              // BN floats
     float* shw = scol2 + BN;                               // 4 x BN floats
     float* shb = shw + 4 * BN;                             // 4 floats
+    float* shx = shb + 4;                                  // [2][128][4] partial head sums
     const int hunits = head_units(ep.head_mode);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -140,10 +145,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(&acc_full[a], 1);
-            mbar_init(&acc_empty[a], 128);
+            mbar_init(&acc_empty[a], 256);
         }
         mbar_init(b_full, 1);
         mbar_init(done, 1);
+        for (int i = 0; i < 8; ++i) mbar_init(&hx_ready[i], 32);
         *abort_flag = 0;
         fence_barrier_init();
     }
@@ -233,7 +239,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
     } else if (warp >= 2) {
         // --------------------------------------------------------- epilogue
-        const int q = warp & 3;   // tensor-memory lane quadrant this warp may read
+        // Warps w and w + 4 share the tensor-memory lane quadrant q = w % 4 (rows
+        // q*32 .. q*32+31 of the tile); `half` 0 takes the first BN/2 columns, 1 the rest.
+        const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
+        constexpr int kHalfChunks = BN / 64;   // 32-column chunks per half
+        const int c0 = half * kHalfChunks;
         uint32_t t = 0;
         float r1_total = 0.f;
         const float gs0 = ep.gscale ? ep.gscale[0] : 1.f;
@@ -250,13 +261,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             const bool live = m < shape.M;
             float r1 = (ep.r1_row && live) ? ep.r1_row[m] : 0.f;
             if (ep.r1_gate && live && !(ep.r1_gate[m] > 0.f)) r1 = 0.f;
-            r1_total += r1;
+            if (half == 0) r1_total += r1;
             float hacc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-            for (int c = 0; c < BN / 32; ++c) {
-                uint32_t r[32];
-                tmem_ld_32x32b_x32(tmem + acc * BN + (uint32_t(q * 32) << 16) + uint32_t(c * 32), r);
-                tmem_ld_wait();
+            const uint32_t tbase = tmem + acc * BN + (uint32_t(q * 32) << 16);
+            uint32_t rbuf[2][32];
+            tmem_ld_32x32b_x32(tbase + uint32_t(c0 * 32), rbuf[0]);
+            tmem_ld_wait();
+#pragma unroll
+            for (int cc = 0; cc < kHalfChunks; ++cc) {
+                const int c = c0 + cc;
+                uint32_t (&r)[32] = rbuf[cc & 1];
+                // start the next chunk's tensor-memory load; it completes under this chunk's math
+                if (cc + 1 < kHalfChunks) tmem_ld_32x32b_x32(tbase + uint32_t((c + 1) * 32), rbuf[(cc + 1) & 1]);
                 float v[32];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
@@ -316,8 +332,25 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                 }
                 if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
+                tmem_ld_wait();
             }
-            if (hunits && live) {
+            if (hunits) {   // kernel-uniform: half 1 hands its partial dot products to half 0
+                // The slot of accumulator `acc` is rewritten two tiles later, only after this
+                // tile's acc_empty completed, which needs half 0's arrival below: no reuse race.
+                float* x = shx + (acc * 128 + q * 32 + lane) * 4;
+                uint64_t* rdy = &hx_ready[acc * 4 + q];
+                if (half == 1) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) x[u] = hacc[u];
+                    mbar_arrive(rdy);
+                } else if (mbar_wait(rdy, (t >> 1) & 1, abort_flag)) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) hacc[u] += x[u];
+                } else {
+                    *abort_flag = 1;
+                }
+            }
+            if (hunits && live && half == 0) {
                 // SimpleNeRF17.py:735-750 (sigma head + noise + ReLU) and :771-777 (sigmoid rgb)
                 int u0 = 0;
                 if (ep.head_mode != kHeadRgb) {

@@ -2,7 +2,8 @@
 
 Two 24x20 forward-facing views (960 rays) in chunks of 256, so the last chunk is
 partial (192 rays on a padded batch).  FP32 plain path: coarse, fine and augmented
-rgb/acc within 1e-5 relative of the float32 oracle (deterministic samples, no
+rgb/acc within 1e-5 relative of the float32 oracle (acc with an absolute allowance
+of one ulp(1) per sample) (deterministic samples, no
 jitter; the fine pass is compared on the depths the GPU sampled).  The BF16 graph
 render equals the BF16 eager render bit for bit.
 """
@@ -49,9 +50,13 @@ def test_fp32_render_matches_oracle():
     np.testing.assert_allclose(out['coarse']['z'].cpu().numpy(), ret['z_vals_coarse'], rtol=0, atol=1.2e-7)
     for tag, pre in (('coarse', ''), ('fine', ''), (f'{AUG}_coarse', f'{AUG}_')):
         lvl = 'fine' if tag == 'fine' else 'coarse'
+        n_s = out[tag]['z'].shape[1]
         for k in ('rgb', 'acc'):
             ref = ret[f'{pre}{k}_{lvl}']
-            np.testing.assert_allclose(out[tag][k].cpu().numpy(), ref, rtol=1e-5, atol=1e-6, err_msg=f'{k}_{tag}')
+            # acc sums one alpha = 1 - exp(-sigma delta) per sample, each with an
+            # absolute rounding of up to ulp(1) = 2^-23 from the subtraction
+            atol = n_s * 2.0 ** -23 if k == 'acc' else 1e-6
+            np.testing.assert_allclose(out[tag][k].cpu().numpy(), ref, rtol=1e-5, atol=atol, err_msg=f'{k}_{tag}')
 
 
 def test_bf16_graph_render_equals_eager():

@@ -6,9 +6,10 @@ the same coarse samples, loss = MSE of every net's rgb + 0.1 * mean squared
 difference of the main coarse depth and the (detached) augmented coarse depth.
 
 FP32 plain path: rgb/acc/depth_ndc/weights within 1e-5 relative of the float32
-oracle, metric depth within 1e-5 of the reduction of the GPU's weights; parameter
-gradients of all three nets within 3e-4 relative L2 per tensor of the float64
-oracle.  BF16 path: rgb within 2e-3 max-abs and whole-gradient relative
+oracle (acc with an absolute allowance of one ulp(1) per sample), metric depth
+within 1e-5 of the reduction of the GPU's weights; parameter gradients of all
+three nets within max(1e-4, 3x the float32 oracle's own error) relative L2 per
+tensor of the float64 oracle.  BF16 path: rgb within 2e-3 max-abs and whole-gradient relative
 L2 per net within 3e-2 of the float64 oracle.  The fine pass is compared on the
 depths the GPU sampled.
 """
@@ -91,8 +92,11 @@ def test_fp32_pair_step_matches_oracle():
     for tag in ('coarse', 'fine', f'{AUG}_coarse'):
         for k in ('rgb_map', 'depth_ndc', 'weights', 'acc'):
             ref = ret32[_ret_key(k, tag)]
-            np.testing.assert_allclose(out[f'{k}_{tag}'], ref, rtol=1e-5,
-                                       atol=1e-6 * max(1.0, float(np.abs(ref).max())), err_msg=f'{k}_{tag}')
+            # acc sums one alpha = 1 - exp(-sigma delta) per sample, each carrying an
+            # absolute rounding of up to ulp(1) = 2^-23 from the subtraction
+            atol = out[f'weights_{tag}'].shape[1] * 2.0 ** -23 if k == 'acc' else \
+                1e-6 * max(1.0, float(np.abs(ref).max()))
+            np.testing.assert_allclose(out[f'{k}_{tag}'], ref, rtol=1e-5, atol=atol, err_msg=f'{k}_{tag}')
         w = out[f'weights_{tag}'].astype(np.float64)
         zm = on.depth_from_ndc(out[f'z_{tag}'].astype(np.float64), o64, d64)
         ref = np.sum(w * zm, -1) / (np.sum(w, -1) + 1e-6)
@@ -104,16 +108,12 @@ def test_fp32_pair_step_gradients_against_fp64_oracle():
     """Parameter gradients of all three nets vs the float64 oracle.  The last
     coarse uniform is drawn from [0, 0.5) so 1 - z_last >= (1 - z_mid) / 2 and the
     metric depth feeding the consistency term stays well conditioned."""
+    from test_gpu_train_step import check_fp32_gradients
     step, params, out, grads, host = _run('fp32', last_u_max=0.5)
     _, g64 = _oracle(params, host, out['z_fine'], np.float64)
+    _, g32 = _oracle(params, host, out['z_fine'], np.float32)
     assert set(g64) == set(step.nets)
-    worst = 0.0
-    for tag in g64:
-        for k, ref in g64[tag].items():
-            rel = np.linalg.norm(grads[tag][k] - ref) / max(np.linalg.norm(ref), 1e-30)
-            worst = max(worst, rel)
-            assert rel < 3e-4, (tag, k, rel)
-    print('fp32 pair step worst per-tensor gradient rel-L2', worst)
+    check_fp32_gradients(grads, g32, g64)
 
 
 def test_consistency_term_reaches_main_coarse_only():

@@ -84,13 +84,26 @@ def test_fp32_train_step_gradients_against_fp64_oracle():
     ray sits on that step; the comparison then measures the kernels."""
     step, params, out, grads, host = _run_step('fp32', sigma_bias=0.5)
     _, _, g64 = _oracle(params, host, out['z_fine'], np.float64)
+    _, _, g32 = _oracle(params, host, out['z_fine'], np.float32)
+    check_fp32_gradients(grads, g32, g64)
+
+
+def check_fp32_gradients(grads, g32, g64):
+    """Per tensor: the GPU's FP32 gradient is within max(1e-4, 3 e32) relative L2 of
+    the float64 oracle, e32 being the error of the float32 oracle (the same
+    algorithm in float32) against float64.  1 - exp(-sigma delta) of a small alpha
+    keeps only ulp(1) / alpha of relative accuracy in float32, so two float32
+    implementations whose exp differs by an ulp disagree by up to ~1e-3 on such
+    samples' gradient terms; e32 measures that conditioning on the same inputs."""
     worst = 0.0
-    for tag in ('coarse', 'fine'):
+    for tag in g64:
         for k, ref in g64[tag].items():
-            rel = np.linalg.norm(grads[tag][k] - ref) / max(np.linalg.norm(ref), 1e-30)
-            worst = max(worst, rel)
-            assert rel < 3e-4, (tag, k, rel)
-    print('fp32 step worst per-tensor gradient rel-L2', worst)
+            nrm = max(np.linalg.norm(ref), 1e-30)
+            rel = np.linalg.norm(grads[tag][k] - ref) / nrm
+            e32 = np.linalg.norm(g32[tag][k].astype(np.float64) - ref) / nrm
+            worst = max(worst, rel / max(1e-4, 3 * e32))
+            assert rel < max(1e-4, 3 * e32), (tag, k, rel, e32)
+    print('fp32 worst per-tensor gradient error / bar', worst)
 
 
 def test_bf16_train_step_against_fp64_oracle():
