@@ -333,11 +333,40 @@ enum { SRF_ACT_NONE = 0, SRF_ACT_RELU = 1, SRF_ACT_SIGMOID = 2 };
 int srf_linear_forward(float* y, int ldy, const float* x, int ldx, const float* weight, const float* bias,
                        int64_t max_rows, const int32_t* rows_dev, int n, int k, int act, void* stream);
 /* dx = (dy * act'(y)) . W ; dW (+)= dz^T x ; db (+)= sum dz, where dz = dy*act'(y).
- * Any of dx, dw, db may be NULL.  dz scratch (rows, n) is caller-provided (may alias dy). */
+ * Any of dx, dw, db may be NULL; y may be NULL when act is SRF_ACT_NONE.  dz scratch
+ * (rows, n) is caller-provided (may alias dy). */
 int srf_linear_backward(float* dx, int lddx, float* dw, float* db, const float* dy, int lddy, const float* y,
                         int ldy, const float* x, int ldx, const float* weight, float* dz_scratch,
                         int64_t max_rows, const int32_t* rows_dev, int n, int k, int act, int accumulate,
                         void* stream);
+/* TensoRF renderer on tcgen05 tensor cores (16-bit operands, FP32 accumulation):
+ * basis_matrix_color (n_comp -> features, no bias) followed by
+ * MlpFeaturesColorPredictor: x = [PE(features, Lf), PE(view, Lv)] -> units ReLU
+ * -> units ReLU -> 3 sigmoid.  Replaces SimpleTensoRF09.py:1151 and :1370-1421
+ * for precision SRF_PRECISION_BF16 / SRF_PRECISION_FP16 (the FP32 path is
+ * srf_linear_* + srf_positional_encoding).  units must be 128 or 256.
+ * params / grads: {basis (features x n_comp), W1 (units x k1), b1, W2 (units x units),
+ * b2, W3 (3 x units), b3}, k1 = features (2 Lf + 1) + 3 (2 Lv + 1); grads accumulate.
+ * view_dirs (m,3) per sample.  The backward writes d_feats (m, n_comp) and needs
+ * the forward's workspace (for_backward) and, for FP16, a loss scaler. */
+typedef struct {
+    int n_comp;               /* colour components: sum of the three planes' R */
+    int features;             /* features_dimension_color                      */
+    int units;                /* num_units_color_predictor                     */
+    int features_pe_degree;
+    int views_pe_degree;
+    int view_dependent;       /* view_dependent_color (view PE appended)       */
+} srf_tensorf_renderer_desc;
+
+size_t srf_tensorf_renderer_workspace_size(const srf_tensorf_renderer_desc* desc, int64_t m, int precision,
+                                           int for_backward);
+int srf_tensorf_renderer_forward(const srf_tensorf_renderer_desc* desc, const float* const* params, const float* feats,
+                                 const float* view_dirs, int64_t m, float* rgb, int precision, int for_backward,
+                                 void* workspace, size_t workspace_bytes, srf_loss_scaler* scaler, void* stream);
+int srf_tensorf_renderer_backward(const srf_tensorf_renderer_desc* desc, const float* const* params,
+                                  const float* feats, const float* d_rgb, int64_t m, float* const* grads,
+                                  float* d_feats, int precision, void* workspace, size_t workspace_bytes,
+                                  srf_loss_scaler* scaler, void* stream);
 /* Positional-encoding backward d x (m,dims) from d out (m, ld) (TensoRF feature PE). */
 int srf_positional_encoding_backward(float* dx, const float* x, const float* dout, int ld_dout, int64_t m,
                                      const int32_t* rows_dev, int dims, int degree, void* stream);
@@ -363,15 +392,46 @@ int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* d
 int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
                   float beta1, float beta2, float eps, float weight_decay, int step, const int32_t* step_dev,
                   const int32_t* skip_dev, void* stream);
-/* Depth-consistency term of AugmentationsDepthLoss11.compute_depth_mse
- * (src/loss_functions/AugmentationsDepthLoss11.py:208-226): with m_r = mask[r]
- * (all ones when mask == NULL), loss += weight * mean_r m_r (pred_r - target_r)^2
- * over all n rays and grad[r] += weight * 2 m_r (pred_r - target_r) / n
- * (accumulated).  The target is detached, as the reference's .detach() makes it.
- * The mask is the caller's choice of rays where the target model is trusted
- * (the reference picks it by patch reprojection, :105-190). */
-int srf_depth_consistency_loss(const float* pred, const float* target, const uint8_t* mask, int n, float weight,
-                               float* loss_dev, float* grad, void* stream);
+/* Squared depth error with the matching gradients (accumulated into grad_pred and
+ * grad_target, either may be NULL): with m_r = mask[r] (all ones when mask == NULL)
+ * and count = n, or the number of masked rays when mean_over_mask,
+ *   loss += weight * sum_r m_r (pred_r - target_r)^2 / count,
+ *   grad_pred[r] += 2 weight m_r (pred_r - target_r) / count, grad_target[r] -= the same.
+ * Replaces AugmentationsDepthLoss11.compute_depth_mse
+ * (src/loss_functions/AugmentationsDepthLoss11.py:208-226: count = n, target detached:
+ * grad_target NULL; the reprojection mask of :105-190 is the caller's),
+ * SparseDepthMSE14.compute_depth_loss (src/loss_functions/SparseDepthMSE14.py:84-97:
+ * mean_over_mask) and CoarseFineConsistencyLoss33 (src/loss_functions/
+ * CoarseFineConsistencyLoss33.py:35-44: no mask, gradients into both). */
+int srf_depth_mse_loss(const float* pred, const float* target, const uint8_t* mask, int n, float weight,
+                       int mean_over_mask, float* loss_dev, float* grad_pred, float* grad_target, void* stream);
+/* MassConcentrationLoss06.compute_entropy_loss
+ * (src/loss_functions/MassConcentrationLoss06.py:63-83): weights (n_rays, n_samples)
+ * summed over num_bins contiguous bins (n_samples / num_bins samples each, one more
+ * in the bins torch.linspace(0, num_bins - 1, n_samples % num_bins).long() picks),
+ * loss += weight * mean over masked rays of sum_bins -(b + 1e-3) ln(b + 1e-3), and
+ * grad_weights (may be NULL) += its gradient (feed it to srf_composite_backward's
+ * g_weights).  num_bins in [1, 64]. */
+int srf_mass_concentration_loss(const float* weights, int n_rays, int n_samples, int num_bins, const uint8_t* mask,
+                                float weight, float* loss_dev, float* grad_weights, void* stream);
+/* The masks of AugmentationsDepthLoss11.compute_loss_nerf
+ * (src/loss_functions/AugmentationsDepthLoss11.py:105-190) for n_rays NeRF rays:
+ * per ray, the camera b with the nearest origin to the ray's own camera (ties: the
+ * lowest index), the points o + d depth1 and o + d depth2 reprojected into b with
+ * the first view's intrinsics (CommonUtils04.reproject, src/utils/CommonUtils04.py:227-253)
+ * and rounded, and the patch_h x patch_w RMSE of the ray's own patch against the
+ * patch at each reprojection (zero outside the image).  mask1 = depth1 is the more
+ * consistent one (a target for depth2), mask2 the reverse, with the reference's
+ * validity and tie rules.  pixel_ids (n,3) int32 (image, x, y); poses (n_views,4,4)
+ * camera-to-world; intrinsics0 (3,3); images (n_views, height, width, channels).
+ * The reference then adds compute_depth_mse(depth1, depth2, mask2) (srf_depth_mse_loss
+ * with grad_target NULL); its second term, on mask1, sees tensors the first zeroed
+ * in place outside mask2 and so contributes only on mask1 & mask2, which is empty. */
+int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth1, const float* depth2,
+                                 const int32_t* pixel_ids, int n_rays, const float* poses, int n_views,
+                                 const float* intrinsics0, const float* images, int height, int width, int channels,
+                                 int patch_w, int patch_h, float rmse_threshold, uint8_t* mask1, uint8_t* mask2,
+                                 void* stream);
 /* *counter_dev += value on the stream (advances a graph-replayed step count),
  * unless skip_dev != NULL and *skip_dev != 0. */
 int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, void* stream);

@@ -35,6 +35,11 @@ class CompositeArgs(ctypes.Structure):
                 ('d_sigma', P), ('d_rgb', P)]
 
 
+class RendererDesc(ctypes.Structure):
+    _fields_ = [('n_comp', c_int), ('features', c_int), ('units', c_int), ('features_pe_degree', c_int),
+                ('views_pe_degree', c_int), ('view_dependent', c_int)]
+
+
 class VmGrid(ctypes.Structure):
     _fields_ = [('res', c_int * 3), ('n_comp', c_int * 3), ('planes', P * 3), ('lines', P * 3)]
 
@@ -94,6 +99,11 @@ _SIGS = {
     'srf_scatter_rows': (c_int, [P, P, P, P, c_int64, c_int, P]),
     'srf_density_activation': (c_int, [P, P, P, P, c_int64, c_int, c_float, P]),
     'srf_density_activation_backward': (c_int, [P, P, P, P, P, c_int64, c_int, c_float, P]),
+    'srf_tensorf_renderer_workspace_size': (c_size_t, [ctypes.POINTER(RendererDesc), c_int64, c_int, c_int]),
+    'srf_tensorf_renderer_forward': (c_int, [ctypes.POINTER(RendererDesc), ctypes.POINTER(P), P, P, c_int64, P, c_int,
+                                             c_int, P, c_size_t, P, P]),
+    'srf_tensorf_renderer_backward': (c_int, [ctypes.POINTER(RendererDesc), ctypes.POINTER(P), P, P, c_int64,
+                                              ctypes.POINTER(P), P, c_int, P, c_size_t, P, P]),
     'srf_linear_forward': (c_int, [P, c_int, P, c_int, P, P, c_int64, P, c_int, c_int, c_int, P]),
     'srf_linear_backward': (c_int, [P, c_int, P, P, P, c_int, P, c_int, P, c_int, P, P, c_int64, P, c_int, c_int,
                                     c_int, c_int, P]),
@@ -101,7 +111,10 @@ _SIGS = {
     'srf_rgb_depth_loss': (c_int, [P, P, P, P, P, c_int, c_int, c_float, P, P, P, P]),
     'srf_adam_step': (c_int, [P, P, P, P, c_int64, c_float, c_float, c_float, c_float, c_float, c_int, P, P, P]),
     'srf_counter_add': (c_int, [P, c_int, P, P]),
-    'srf_depth_consistency_loss': (c_int, [P, P, P, c_int, c_float, P, P, P]),
+    'srf_depth_mse_loss': (c_int, [P, P, P, c_int, c_float, c_int, P, P, P, P]),
+    'srf_mass_concentration_loss': (c_int, [P, c_int, c_int, c_int, P, c_float, P, P, P]),
+    'srf_depth_reprojection_masks': (c_int, [P, P, P, P, P, c_int, P, c_int, P, P, c_int, c_int, c_int, c_int, c_int,
+                                             c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
     'srf_launch_count': (c_int64, []),
 }

@@ -14,7 +14,7 @@ radius 4 about the box centre, directions towards the centre perturbed by
 N(0, 0.3^2) per axis, near 2, far 6.  Loss: MSE of each model's rgb against
 targets ~ U[0,1]^3.
 
-    python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3
+    python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3 [--precision fp16]
 """
 import argparse
 import json
@@ -38,12 +38,12 @@ def tensor_configs(n_voxels):
             'num_units_color_predictor': 128, 'predict_visibility': False}
 
 
-def make_models(device, seed=0, mask_res=128, mask_occupancy=0.15):
+def make_models(device, seed=0, mask_res=128, mask_occupancy=0.15, precision='fp32', grids=(300, 75)):
     from .tensorf_model import AlphaGridMask, GbVmTensor
     torch.manual_seed(seed)
-    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True, 'precision': precision}}
     models = []
-    for name, nv in (('coarse_model', 300 ** 3), ('views_augmentation_coarse_model', 75 ** 3)):
+    for name, nv in (('coarse_model', grids[0] ** 3), ('views_augmentation_coarse_model', grids[1] ** 3)):
         tm = GbVmTensor(name, configs, tensor_configs(nv), {'bounding_box': BBOX}).to(device)
         g = torch.Generator().manual_seed(seed + 1)
         vol = (torch.rand(mask_res, mask_res, mask_res, generator=g) < mask_occupancy).to(device)
@@ -113,11 +113,13 @@ def main(argv=None):
     ap.add_argument('--rays', type=int, default=8192)
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'bf16', 'fp16'],
+                    help='renderer MLP: FP32 SIMT or 16-bit tensor cores')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
     dev = torch.device('cuda')
-    models = make_models(dev)
+    models = make_models(dev, precision=args.precision)
     step = TensorfTrainStep(models)
     batches = [synthetic_rays(args.rays, 10 + i, dev) for i in range(4)]
     for i in range(args.warmup):
@@ -134,6 +136,7 @@ def main(argv=None):
     ms = e0.elapsed_time(e1) / max(args.steps, 1)
     launches = (lib.srf_launch_count() - l0) / max(args.steps, 1)
     print(json.dumps({'workload': f'tensorf_vm_train_step_{args.rays}rays_300^3+75^3', 'rays': args.rays,
+                      'precision': args.precision,
                       'ms_per_step': round(ms, 4), 'rays_per_s': round(args.rays / ms * 1e3, 1),
                       'samples_per_step': {m.name: c for m, c in zip(models, step.last['samples'])},
                       'gpu_launches_per_step': launches, 'loss': float(step.last['loss'].item())}))

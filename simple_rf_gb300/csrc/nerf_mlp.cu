@@ -157,7 +157,7 @@ __global__ void act_grad_kernel(float* dz, int64_t ldz, const float* dy, int64_t
     int64_t r = idx / n;
     int c = int(idx % n);
     float g = dy[r * lddy + c];
-    float v = y[r * ldy + c];
+    float v = act != SRF_ACT_NONE ? y[r * ldy + c] : 0.f;
     if (act == SRF_ACT_RELU) g = v > 0.f ? g : 0.f;
     else if (act == SRF_ACT_SIGMOID) g = g * v * (1.f - v);
     dz[r * ldz + c] = g;
@@ -538,7 +538,7 @@ extern "C" int srf_linear_backward(float* dx, int lddx, float* dw, float* db, co
                                    const float* y, int ldy, const float* x, int ldx, const float* weight,
                                    float* dz_scratch, int64_t max_rows, const int32_t* rows_dev, int n, int k, int act,
                                    int accumulate, void* stream) {
-    if (!dy || !y || !dz_scratch || !weight) return SRF_ERR_NULL;
+    if (!dy || !dz_scratch || !weight || (act != SRF_ACT_NONE && !y)) return SRF_ERR_NULL;
     if ((dw && !x)) return SRF_ERR_NULL;
     if (max_rows < 0 || n < 1 || k < 1) return SRF_ERR_SHAPE;
     cudaStream_t s = as_stream(stream);
@@ -547,10 +547,14 @@ extern "C" int srf_linear_backward(float* dx, int lddx, float* dw, float* db, co
         if (db && cudaMemsetAsync(db, 0, size_t(n) * sizeof(float), s) != cudaSuccess) return SRF_ERR_CUDA;
     }
     if (max_rows == 0) return SRF_OK;
-    act_grad_kernel<<<grid_1d(max_rows * n, 256), 256, 0, s>>>(dz_scratch, n, dy, lddy, y, ldy, max_rows, rows_dev, n,
-                                                               act);
-    int st = launch_status();
-    if (st) return st;
+    int st = SRF_OK;
+    // without an activation dz = dy: no pass when the scratch already is dy
+    if (!(act == SRF_ACT_NONE && dz_scratch == dy && lddy == n)) {
+        act_grad_kernel<<<grid_1d(max_rows * n, 256), 256, 0, s>>>(dz_scratch, n, dy, lddy, y, ldy, max_rows,
+                                                                   rows_dev, n, act);
+        st = launch_status();
+        if (st) return st;
+    }
     if (dw) {
         SegRows a = seg1(x, ldx, k);
         a.ones_col = db != nullptr;

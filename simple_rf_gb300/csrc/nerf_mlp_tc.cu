@@ -236,7 +236,10 @@ __global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partia
     int rc = ref_col(L, kp);
     if (rc < 0) return;
     float acc = 0.f;
-    for (int sp = 0; sp < splits; ++sp) acc += partial[(int64_t(sp) * n_dz + n) * kpad + kp];
+    const float* src = partial + int64_t(n) * kpad + kp;
+    const int64_t step = int64_t(n_dz) * kpad;
+#pragma unroll 8
+    for (int sp = 0; sp < splits; ++sp) acc += src[sp * step];
     if (gscale) acc *= gscale[1];
     grad[int64_t(n) * L.kref() + rc] += acc;
 }
@@ -561,14 +564,14 @@ struct TcCtx {
     int* found_inf() const { return scaler ? &scaler->found_inf : nullptr; }
 };
 
-int wgrad_layer(const LayerMap& lm, const TcWs& w, const op16* dz, const op16* x0, int64_t ld0, const op16* x1,
-                int64_t ld1, int64_t M, float* grad, const TcCtx& cx, cudaStream_t s) {
+int wgrad_layer(const LayerMap& lm, float* partial, size_t partial_floats, const op16* dz, const op16* x0,
+                int64_t ld0, const op16* x1, int64_t ld1, int64_t M, float* grad, const TcCtx& cx, cudaStream_t s) {
     int splits = 0;
-    int st = tc_wgrad(w.partial, w.partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
+    int st = tc_wgrad(partial, partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
                       lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt);
     if (st) return st;
     dim3 grid((lm.kpad() + 127) / 128, lm.n);
-    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, w.partial, splits, lm.n, grad, cx.gscale());
+    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale());
     return launch_status();
 }
 
@@ -678,8 +681,8 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
             const LayerMap& lm = T.view[j];
             const op16* x0 = j == 0 ? w.feat : w.hv[j - 1];
             int64_t ld0 = j == 0 ? L.Wp : L.Wv;
-            st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.vext : nullptr, T.vx_w, m, G[L.idx_view_w(j)], cx,
-                             s);
+            st = wgrad_layer(lm, w.partial, w.partial_floats, dz, x0, ld0, lm.nsrc > 1 ? w.vext : nullptr, T.vx_w,
+                             m, G[L.idx_view_w(j)], cx, s);
             if (st) return st;
             if (j > 0) {
                 tc::GemmEpilogue ep = bwd_epilogue(dz2, L.Wv);
@@ -696,7 +699,8 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
                 if (st) return st;
             }
         }
-        st = wgrad_layer(T.feat, w, w.dfeat, hl, L.Wp, nullptr, 0, m, G[L.idx_feat_w()], cx, s);
+        st = wgrad_layer(T.feat, w.partial, w.partial_floats, w.dfeat, hl, L.Wp, nullptr, 0, m, G[L.idx_feat_w()],
+                         cx, s);
         if (st) return st;
         // feature-layer dgrad with the sigma head's adjoint fused in: dZ_last =
         // (dfeat . Wf + dsig w_sigma) * (h_last > 0), dsig = dsigma * (sraw > 0);
@@ -722,8 +726,8 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         const LayerMap& lm = T.trunk[j];
         const op16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
-        st = wgrad_layer(lm, w, dz, x0, ld0, lm.nsrc > 1 ? w.h[j - 1] : nullptr, L.Wp, m, G[L.idx_trunk_w(j)], cx,
-                         s);
+        st = wgrad_layer(lm, w.partial, w.partial_floats, dz, x0, ld0, lm.nsrc > 1 ? w.h[j - 1] : nullptr, L.Wp, m,
+                         G[L.idx_trunk_w(j)], cx, s);
         if (st) return st;
         if (j == 0) break;
         int row0 = lm.nsrc > 1 ? lm.padw[0] : 0;
@@ -736,6 +740,275 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         std::swap(dz, dz2);
     }
     return SRF_OK;
+}
+
+// ======================================================================
+// TensoRF renderer on tcgen05: basis_matrix_color (C -> F, no bias) and
+// MlpFeaturesColorPredictor (SimpleTensoRF09.py:1151, 1370-1421):
+//   B = feats . Wb^T;  x = [PE(B, Lf), PE(view, Lv)];  h1 = relu(x W1^T + b1);
+//   h2 = relu(h1 W2^T + b2);  rgb = sigmoid(h2 W3^T + b3)
+// The basis and the encodings run in one SIMT pass (3,888 MAC per sample for
+// C = 144, F = 27) that writes x as a 16-bit row padded to a multiple of 64;
+// the two U-wide layers are tcgen05 GEMMs with the rgb head fused into the
+// second one's epilogue.  The backward mirrors the NeRF path, then the PE
+// adjoint and the basis layer's FP32 backward give d feats for the VM adjoint.
+// ======================================================================
+
+namespace {
+
+constexpr int kBasisRows = 128;  // samples (and threads) per block of the basis + encoding pass
+constexpr int kMaxBasis = 32;    // largest basis width (features_dimension_color) it holds in registers
+
+struct RenderLayout {
+    int C, F, U, lf, lv, view, k1, k1p;
+    LayerMap l1, l2;
+    bool ok;
+    RenderLayout(int c, int f, int u, int lf_, int lv_, int view_) : C(c), F(f), U(u), lf(lf_), lv(lv_), view(view_) {
+        k1 = F * (2 * lf + 1) + (view ? 3 * (2 * lv + 1) : 0);
+        k1p = pad64(k1);
+        l1 = LayerMap{};
+        l1.n = U; l1.nsrc = 1; l1.padw[0] = k1p; l1.refw[0] = k1;
+        l2 = LayerMap{};
+        l2.n = U; l2.nsrc = 1; l2.padw[0] = U; l2.refw[0] = U;
+        ok = (U == 128 || U == 256) && C >= 1 && C <= 1024 && F >= 1 && F <= kMaxBasis && k1p <= 256 && lf >= 0 &&
+             lv >= 0 && lf <= 10 && lv <= 10;
+    }
+};
+
+struct RenderWs {
+    float* B;        // (m, F) basis outputs (kept for the PE adjoint)
+    op16* x;         // (m, k1p)
+    op16* h1;        // (m, U)
+    op16* h2;        // (m, U)
+    float* rgb;      // (m, 3)
+    op16 *W1, *W1T, *W2, *W2T;
+    op16 *dz0, *dz1, *dx;   // (m, U), (m, U), (m, k1p)
+    float* dB;       // (m, F)
+    float* partial;
+    size_t partial_floats;
+};
+
+size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size_t cap, RenderWs* out) {
+    Carver c(base, cap);
+    RenderWs w{};
+    w.B = c.take<float>(size_t(m) * R.F);
+    w.x = c.take<op16>(size_t(m) * R.k1p);
+    w.h1 = c.take<op16>(size_t(m) * R.U);
+    w.h2 = c.take<op16>(size_t(m) * R.U);
+    w.rgb = c.take<float>(size_t(m) * 3);
+    w.W1 = c.take<op16>(size_t(R.U) * R.k1p);
+    w.W1T = c.take<op16>(size_t(R.U) * R.k1p);
+    w.W2 = c.take<op16>(size_t(R.U) * R.U);
+    w.W2T = c.take<op16>(size_t(R.U) * R.U);
+    if (bwd) {
+        w.dz0 = c.take<op16>(size_t(m) * R.U);
+        w.dz1 = c.take<op16>(size_t(m) * R.U);
+        w.dx = c.take<op16>(size_t(m) * R.k1p);
+        w.dB = c.take<float>(size_t(m) * R.F);
+        w.partial_floats = tc_wgrad_partial_floats(R.U, 256);
+        w.partial = c.take<float>(w.partial_floats);
+    }
+    if (out) *out = w;
+    return c.used;
+}
+
+// B = feats . Wb^T (FP32) and x = [PE(B, lf), PE(view, lv), 0...] in format fmt for
+// kBasisRows samples per block.  The block copies its feature rows into shared
+// memory with coalesced loads (row stride C + 1 words) next to Wb transposed and
+// padded to kMaxBasis columns; thread t computes rows 8 (t / 8) .. +7 times
+// columns 4 (t % 8) .. +3 (per input: 8 row reads, spread over 4 banks x 8-way
+// broadcast, and one 128-bit weight read), then writes its PE entries into the
+// same row area re-used as the 16-bit staging, which the block stores with
+// consecutive threads on consecutive 4-byte words.
+__host__ __device__ inline size_t basis_stage_bytes(int C, int k1p) {
+    size_t fb = size_t(kBasisRows) * (C + 1) * sizeof(float);
+    size_t xb = size_t(kBasisRows) * (k1p + 2) * sizeof(op16);
+    return fb > xb ? fb : xb;
+}
+
+__global__ void __launch_bounds__(kBasisRows)
+    basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ Wb, int F,
+                        const float* __restrict__ view, int64_t M, int lf, int lv, int k1p, float* B, op16* x,
+                        int fmt) {
+    extern __shared__ float bsm[];
+    float* sWt = bsm;                                          // C x kMaxBasis (Wb^T, zero-padded)
+    float* sF = bsm + C * kMaxBasis;                           // kBasisRows x (C + 1), then the 16-bit rows
+    op16* srow = reinterpret_cast<op16*>(sF);                  // kBasisRows x (k1p + 2)
+    const int stride = k1p + 2;
+    const int64_t row0 = int64_t(blockIdx.x) * kBasisRows;
+    const int64_t rows = M - row0 < kBasisRows ? M - row0 : kBasisRows;
+    for (int i = threadIdx.x; i < C * kMaxBasis; i += blockDim.x) {
+        const int c = i / kMaxBasis, o = i % kMaxBasis;
+        sWt[i] = o < F ? Wb[o * C + c] : 0.f;
+    }
+    const float* gf = feats + row0 * C;
+    for (int64_t i = threadIdx.x; i < rows * C; i += blockDim.x) sF[(i / C) * (C + 1) + i % C] = gf[i];
+    __syncthreads();
+    const int rg = threadIdx.x >> 3, cg = threadIdx.x & 7;   // rows rg*8.., columns cg*4..
+    float acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    const float* f0 = sF + (rg * 8) * (C + 1);
+    for (int c = 0; c < C; ++c) {
+        const float4 wv = *reinterpret_cast<const float4*>(sWt + c * kMaxBasis + cg * 4);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const float fv = f0[i * (C + 1) + c];
+            acc[i][0] += fv * wv.x;
+            acc[i][1] += fv * wv.y;
+            acc[i][2] += fv * wv.z;
+            acc[i][3] += fv * wv.w;
+        }
+    }
+    __syncthreads();   // the row area becomes the staging of the encoded rows
+    for (int i = threadIdx.x; i < kBasisRows * stride / 2; i += blockDim.x) reinterpret_cast<uint32_t*>(srow)[i] = 0u;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = rg * 8 + i;
+        if (r >= rows) break;
+        const int64_t m = row0 + r;
+        op16* my = srow + r * stride;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int o = cg * 4 + j;
+            if (o >= F) break;
+            const float v = acc[i][j];
+            B[m * F + o] = v;
+            my[o] = tc::to16(v, fmt);
+            for (int k = 0; k < lf; ++k) {
+                float sn, cs;
+                sincosf(v * float(1 << k), &sn, &cs);
+                my[F + 2 * k * F + o] = tc::to16(sn, fmt);
+                my[F + (2 * k + 1) * F + o] = tc::to16(cs, fmt);
+            }
+        }
+        if (view && cg == 0) {
+            const int v0 = F * (2 * lf + 1);
+            for (int a = 0; a < 3; ++a) {
+                const float q = view[m * 3 + a];
+                my[v0 + a] = tc::to16(q, fmt);
+                for (int k = 0; k < lv; ++k) {
+                    float sn, cs;
+                    sincosf(q * float(1 << k), &sn, &cs);
+                    my[v0 + 3 + 6 * k + a] = tc::to16(sn, fmt);
+                    my[v0 + 6 + 6 * k + a] = tc::to16(cs, fmt);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(srow);
+    const int wx = k1p / 2, ws = stride / 2;
+    uint32_t* gx = reinterpret_cast<uint32_t*>(x + row0 * k1p);
+    for (int w = threadIdx.x; w < rows * wx; w += kBasisRows) gx[w] = src[(w / wx) * ws + w % wx];
+}
+
+// dB[m, o] = sum over the PE columns of B[m, o] of dx * d(column)/dB, with dx the
+// 16-bit (loss-scaled by gscale[0]) gradient of the encoded row; unscaled here.
+__global__ void basis_pe_bwd_kernel(const op16* __restrict__ dx, const float* __restrict__ B, int64_t M, int F,
+                                    int lf, int k1p, int fmt, const float* gscale, float* dB) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= M * F) return;
+    const int64_t m = i / F;
+    const int o = int(i % F);
+    const op16* row = dx + m * k1p;
+    auto rd = [&](int col) {
+        const uint32_t w = reinterpret_cast<const uint32_t*>(row)[col >> 1];
+        float2 f = tc::unpack16(w, fmt);
+        return (col & 1) ? f.y : f.x;
+    };
+    const float b = B[m * F + o];
+    float g = rd(o);
+    for (int k = 0; k < lf; ++k) {
+        const float fk = float(1 << k);
+        float sn, cs;
+        sincosf(b * fk, &sn, &cs);
+        g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
+    }
+    dB[i] = gscale ? g * gscale[1] : g;
+}
+
+}  // namespace
+
+size_t render_tc_workspace(int C, int F, int U, int lf, int lv, int view, int64_t m, bool bwd) {
+    RenderLayout R(C, F, U, lf, lv, view);
+    if (!R.ok) return 0;
+    return carve_render(R, m, bwd, nullptr, ~size_t(0), nullptr);
+}
+
+// P = {Wb (F x C), W1 (U x k1), b1, W2 (U x U), b2, W3 (3 x U), b3}
+int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float* const* P, const float* feats,
+                      const float* vdirs, int64_t m, float* rgb, bool bwd, void* ws, size_t ws_bytes, int fmt,
+                      srf_loss_scaler* scaler, cudaStream_t s) {
+    RenderLayout R(C, F, U, lf, lv, view);
+    if (!R.ok) return SRF_ERR_UNSUPPORTED;
+    RenderWs w;
+    if (carve_render(R, m, bwd, ws, ws_bytes, &w) > ws_bytes) return SRF_ERR_WORKSPACE;
+    const TcCtx cx{fmt, scaler};
+    int st;
+    if ((st = pack(R.l1, P[1], w.W1, w.W1T, fmt, s))) return st;
+    if ((st = pack(R.l2, P[3], w.W2, w.W2T, fmt, s))) return st;
+    const size_t smem = size_t(C) * kMaxBasis * sizeof(float) + basis_stage_bytes(C, R.k1p);
+    if (smem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(basis_encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(smem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+    }
+    basis_encode_kernel<<<unsigned((m + kBasisRows - 1) / kBasisRows), kBasisRows, smem, s>>>(
+        feats, C, P[0], F, view ? vdirs : nullptr, m, lf, lv, R.k1p, w.B, w.x, fmt);
+    if ((st = launch_status())) return st;
+    if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
+                        w.W1, R.k1p, U, 0, m, U, s)))
+        return st;
+    tc::GemmEpilogue ep = make_epilogue(w.h2, U, P[4], 1, fmt, cx.found_inf());
+    ep.head_mode = tc::kHeadRgb;
+    ep.head_w = P[5];
+    ep.head_b = P[6];
+    ep.head_rgb_ws = w.rgb;
+    ep.head_rgb_out = rgb;
+    return tc_linear(ep, w.h1, U, U, nullptr, 0, 0, w.W2, U, U, 0, m, U, s);
+}
+
+// G = gradients in P's order (accumulated); d_feats (m x C) is written.
+int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const float* const* P, const float* feats,
+                       const float* drgb, int64_t m, float* const* G, float* d_feats, void* ws, size_t ws_bytes,
+                       int fmt, srf_loss_scaler* scaler, cudaStream_t s) {
+    RenderLayout R(C, F, U, lf, lv, view);
+    if (!R.ok) return SRF_ERR_UNSUPPORTED;
+    RenderWs w;
+    if (carve_render(R, m, true, ws, ws_bytes, &w) > ws_bytes) return SRF_ERR_WORKSPACE;
+    const TcCtx cx{fmt, scaler};
+    int st;
+    // rgb head: dZ2 (scaled), db2, dW3, db3
+    if ((st = head_bwd_fused<3>(m, U, nullptr, nullptr, drgb, w.rgb, P[5], w.h2, w.dz0, G[4], G[5], G[6], fmt,
+                                cx.gscale(), cx.found_inf(), s)))
+        return st;
+    if ((st = wgrad_layer(R.l2, w.partial, w.partial_floats, w.dz0, w.h1, U, nullptr, 0, m, G[3], cx, s))) return st;
+    tc::GemmEpilogue e2 = make_epilogue(w.dz1, U, nullptr, 0, fmt, cx.found_inf());
+    e2.gscale = cx.gscale();
+    e2.mask = w.h1;
+    e2.ld_mask = U;
+    e2.colsum = G[2];
+    if ((st = tc_linear(e2, w.dz0, U, U, nullptr, 0, 0, w.W2T, U, U, 0, m, U, s))) return st;
+    if ((st = wgrad_layer(R.l1, w.partial, w.partial_floats, w.dz1, w.x, R.k1p, nullptr, 0, m, G[1], cx, s))) return st;
+    // dX = dZ1 . W1 (k1p columns, in blocks of at most 128 output columns)
+    for (int c0 = 0; c0 < R.k1p; c0 += 128) {
+        const int n = R.k1p - c0 >= 128 ? 128 : 64;
+        tc::GemmEpilogue e1 = make_epilogue(w.dx + c0, R.k1p, nullptr, 0, fmt, cx.found_inf());
+        if ((st = tc_linear(e1, w.dz1, U, U, nullptr, 0, 0, w.W1T, U, R.k1p, c0, m, n, s))) return st;
+    }
+    basis_pe_bwd_kernel<<<grid_1d(m * F, 256), 256, 0, s>>>(w.dx, w.B, m, F, lf, R.k1p, fmt, cx.gscale(), w.dB);
+    if ((st = launch_status())) return st;
+    // basis layer (FP32): d_feats = dB . Wb, dWb += dB^T feats
+    return srf_linear_backward(d_feats, C, G[0], nullptr, w.dB, F, nullptr, 0, feats, C, P[0], w.dB, m, nullptr, F,
+                               C, SRF_ACT_NONE, 1, s);
 }
 
 }  // namespace srf
@@ -768,4 +1041,53 @@ extern "C" int srf_bf16_wgrad(float* partial, size_t partial_bytes, int* splits,
     return tc_wgrad(partial, partial_bytes / sizeof(float), static_cast<const op16*>(dz), ld_dz, n_dz,
                     static_cast<const op16*>(x0), ld0, k0, static_cast<const op16*>(x1), ld1, k1, m, splits,
                     as_stream(stream));
+}
+
+// ------------------------------------------------- TensoRF renderer entry --
+
+static int render_fmt(int precision) {
+    return precision == SRF_PRECISION_FP16 ? tc::kFmtF16 : (precision == SRF_PRECISION_BF16 ? tc::kFmtBF16 : -1);
+}
+
+extern "C" size_t srf_tensorf_renderer_workspace_size(const srf_tensorf_renderer_desc* d, int64_t m, int precision,
+                                                      int for_backward) {
+    if (!d || m < 0 || render_fmt(precision) < 0) return 0;
+    return render_tc_workspace(d->n_comp, d->features, d->units, d->features_pe_degree, d->views_pe_degree,
+                               d->view_dependent, m, for_backward != 0);
+}
+
+extern "C" int srf_tensorf_renderer_forward(const srf_tensorf_renderer_desc* d, const float* const* params,
+                                            const float* feats, const float* view_dirs, int64_t m, float* rgb,
+                                            int precision, int for_backward, void* workspace, size_t workspace_bytes,
+                                            srf_loss_scaler* scaler, void* stream) {
+    if (!d || !params || !feats || !rgb) return SRF_ERR_NULL;
+    for (int i = 0; i < 7; ++i)
+        if (!params[i]) return SRF_ERR_NULL;
+    if (d->view_dependent && !view_dirs) return SRF_ERR_NULL;
+    const int fmt = render_fmt(precision);
+    if (fmt < 0) return SRF_ERR_UNSUPPORTED;
+    if (m < 0) return SRF_ERR_SHAPE;
+    if (m == 0) return SRF_OK;
+    if (!workspace) return SRF_ERR_WORKSPACE;
+    return render_tc_forward(d->n_comp, d->features, d->units, d->features_pe_degree, d->views_pe_degree,
+                             d->view_dependent, params, feats, view_dirs, m, rgb, for_backward != 0, workspace,
+                             workspace_bytes, fmt, scaler, as_stream(stream));
+}
+
+extern "C" int srf_tensorf_renderer_backward(const srf_tensorf_renderer_desc* d, const float* const* params,
+                                             const float* feats, const float* d_rgb, int64_t m, float* const* grads,
+                                             float* d_feats, int precision, void* workspace, size_t workspace_bytes,
+                                             srf_loss_scaler* scaler, void* stream) {
+    if (!d || !params || !feats || !d_rgb || !grads || !d_feats) return SRF_ERR_NULL;
+    for (int i = 0; i < 7; ++i)
+        if (!params[i] || !grads[i]) return SRF_ERR_NULL;
+    const int fmt = render_fmt(precision);
+    if (fmt < 0) return SRF_ERR_UNSUPPORTED;
+    if (fmt == tc::kFmtF16 && !scaler) return SRF_ERR_NULL;
+    if (m < 0) return SRF_ERR_SHAPE;
+    if (m == 0) return SRF_OK;
+    if (!workspace) return SRF_ERR_WORKSPACE;
+    return render_tc_backward(d->n_comp, d->features, d->units, d->features_pe_degree, d->views_pe_degree,
+                              d->view_dependent, params, feats, d_rgb, m, grads, d_feats, workspace, workspace_bytes,
+                              fmt, scaler, as_stream(stream));
 }

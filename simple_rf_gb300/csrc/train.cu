@@ -116,28 +116,198 @@ __global__ void loss_scaler_update_kernel(srf_loss_scaler* s, float growth, floa
     s->found_inf = 0;
 }
 
-// loss += weight * mean_r m_r (pred - target)^2;  grad[r] += 2 weight m_r (pred - target) / n
-__global__ void depth_consistency_kernel(const float* __restrict__ pred, const float* __restrict__ target,
-                                         const uint8_t* __restrict__ mask, int n, float weight, float* loss,
-                                         float* grad) {
-    __shared__ float red[32];
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    float l = 0.f;
-    if (r < n && (!mask || mask[r])) {
-        float e = pred[r] - target[r];
-        l = weight * e * e / float(n);
-        grad[r] += 2.f * weight * e / float(n);
-    }
+// Block-wide sum over the 1024 threads of one block (callable by every thread).
+template <class T>
+__device__ T block_sum(T v, T* red) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : T(0);
     if (threadIdx.x < 32) {
-        l = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-        if (threadIdx.x == 0 && loss) atomicAdd(loss, l);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     }
+    if (threadIdx.x == 0) red[0] = v;
+    __syncthreads();
+    v = red[0];
+    __syncthreads();
+    return v;
+}
+
+// Number of rays the mean runs over: the masked ones, or all n.
+__device__ int mean_count(const uint8_t* mask, int n, int over_mask, int* ired) {
+    if (!over_mask || !mask) return n;
+    int c = 0;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) c += mask[r] != 0;
+    return block_sum(c, ired);
+}
+
+// loss += weight * sum_r m_r (pred - target)^2 / count and the matching gradients
+// (one block of 1024 threads: the count precedes every term).
+__global__ void depth_mse_kernel(const float* __restrict__ pred, const float* __restrict__ target,
+                                 const uint8_t* __restrict__ mask, int n, float weight, int over_mask, float* loss,
+                                 float* gp, float* gt) {
+    __shared__ float fred[32];
+    __shared__ int ired[32];
+    const int cnt = mean_count(mask, n, over_mask, ired);
+    if (cnt == 0) return;
+    const float inv = 1.f / float(cnt);
+    float l = 0.f;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        if (mask && !mask[r]) continue;
+        const float e = pred[r] - target[r];
+        l += e * e;
+        const float g = weight * 2.f * e * inv;
+        if (gp) gp[r] += g;
+        if (gt) gt[r] -= g;
+    }
+    l = block_sum(l, fred);
+    if (threadIdx.x == 0 && loss) atomicAdd(loss, weight * l * inv);
+}
+
+// Bin b of a ray covers samples [start[b], start[b + 1]).
+struct BinLayout {
+    int nb;
+    int start[65];
+};
+
+// Per ray: bin sums b_k of the weights, loss term -sum_k (b_k + 1e-3) ln(b_k + 1e-3);
+// mean over the (masked) rays; d/dw_i = -(ln(b_k + 1e-3) + 1) for i in bin k.  One
+// block of 1024 threads, a warp per ray and a lane per bin.
+__global__ void mass_concentration_kernel(const float* __restrict__ w, int n, int s, BinLayout bl,
+                                          const uint8_t* __restrict__ mask, float weight, float* loss, float* gw) {
+    __shared__ float fred[32];
+    __shared__ int ired[32];
+    const int cnt = mean_count(mask, n, 1, ired);
+    if (cnt == 0) return;
+    const float scale = weight / float(cnt);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float l = 0.f;
+    for (int r = warp; r < n; r += nw) {
+        if (mask && !mask[r]) continue;
+        const float* wr = w + int64_t(r) * s;
+        for (int b = lane; b < bl.nb; b += 32) {
+            float sum = 0.f;
+            for (int i = bl.start[b]; i < bl.start[b + 1]; ++i) sum += wr[i];
+            const float x = sum + 1e-3f;
+            const float lx = logf(x);
+            l -= x * lx;
+            if (gw) {
+                const float g = -(lx + 1.f) * scale;
+                float* gr = gw + int64_t(r) * s;
+                for (int i = bl.start[b]; i < bl.start[b + 1]; ++i) gr[i] += g;
+            }
+        }
+    }
+    l = block_sum(l, fred);
+    if (threadIdx.x == 0 && loss) atomicAdd(loss, l * scale);
+}
+
+// AugmentationsDepthLoss11.compute_loss_nerf masks (AugmentationsDepthLoss11.py:105-190),
+// one thread per ray: the nearest other camera b, both depths' points reprojected
+// into b (CommonUtils04.reproject: ((K0 diag(1,-1,-1)) R_b^T) (p - t_b), then x/z,
+// y/z, rounded half to even), the RMSE of the ray's patch in its own image against
+// the patch at each reprojection in image b (zero outside the image), and the
+// reference's mask rules.
+// a0 b0 + a1 b1 + a2 b2 with each product and sum rounded separately (no FMA),
+// as the reference's small float32 matrix products round
+__device__ __forceinline__ float dot3_rn(float a0, float a1, float a2, float b0, float b1, float b2) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
+
+__device__ __forceinline__ float patch_rmse(const float* __restrict__ imgs, int H, int W, int C, int ia, int ya,
+                                            int xa, int ib, int yb, int xb, int hpy, int hpx) {
+    float acc = 0.f;
+    for (int dy = -hpy; dy <= hpy; ++dy) {
+        for (int dx = -hpx; dx <= hpx; ++dx) {
+            const int y1 = ya + dy, x1 = xa + dx, y2 = yb + dy, x2 = xb + dx;
+            const bool in1 = y1 >= 0 && y1 < H && x1 >= 0 && x1 < W;
+            const bool in2 = y2 >= 0 && y2 < H && x2 >= 0 && x2 < W;
+            const float* p1 = in1 ? imgs + ((int64_t(ia) * H + y1) * W + x1) * C : nullptr;
+            const float* p2 = in2 ? imgs + ((int64_t(ib) * H + y2) * W + x2) * C : nullptr;
+            for (int c = 0; c < C; ++c) {
+                const float e = (p1 ? p1[c] : 0.f) - (p2 ? p2[c] : 0.f);
+                acc += e * e;
+            }
+        }
+    }
+    return sqrtf(acc / float((2 * hpy + 1) * (2 * hpx + 1) * C));
+}
+
+__global__ void reprojection_masks_kernel(const float* __restrict__ ro, const float* __restrict__ rd,
+                                          const float* __restrict__ d1, const float* __restrict__ d2,
+                                          const int32_t* __restrict__ pid, int n, const float* __restrict__ poses,
+                                          int V, const float* __restrict__ k0, const float* __restrict__ imgs, int H,
+                                          int W, int C, int hpx, int hpy, float thr, uint8_t* m1, uint8_t* m2,
+                                          int* flag) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int ia = pid[3 * r], xa = pid[3 * r + 1], ya = pid[3 * r + 2];
+    if (ia < 0 || ia >= V) {
+        m1[r] = m2[r] = 0;
+        raise_flag(flag, kFlagRange);
+        return;
+    }
+    // nearest other camera origin (ties: lowest index)
+    const float* pa = poses + 16 * ia;
+    int ib = -1;
+    float best = 0.f;
+    for (int j = 0; j < V; ++j) {
+        if (j == ia) continue;
+        const float* pj = poses + 16 * j;
+        const float ex = pa[3] - pj[3], ey = pa[7] - pj[7], ez = pa[11] - pj[11];
+        const float dist = sqrtf(ex * ex + ey * ey + ez * ez);
+        if (ib < 0 || dist < best) {
+            ib = j;
+            best = dist;
+        }
+    }
+    if (ib < 0) {   // a single view: nothing to compare against
+        m1[r] = m2[r] = 0;
+        return;
+    }
+    const float* pb = poses + 16 * ib;
+    // M = (K0 diag(1, -1, -1)) R_b^T, row by row
+    float kp[9];
+    for (int i = 0; i < 3; ++i) {
+        kp[3 * i] = k0[3 * i];
+        kp[3 * i + 1] = -k0[3 * i + 1];
+        kp[3 * i + 2] = -k0[3 * i + 2];
+    }
+    float M[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)   // (R^T)[k][j] = R[j][k]
+            M[3 * i + j] = dot3_rn(kp[3 * i], kp[3 * i + 1], kp[3 * i + 2], pb[4 * j], pb[4 * j + 1], pb[4 * j + 2]);
+    int qx[2], qy[2];
+    for (int s = 0; s < 2; ++s) {
+        const float dep = s == 0 ? d1[r] : d2[r];
+        float v[3];
+        for (int a = 0; a < 3; ++a)
+            v[a] = __fsub_rn(__fadd_rn(ro[3 * r + a], __fmul_rn(rd[3 * r + a], dep)), pb[4 * a + 3]);
+        float p[3];
+        for (int i = 0; i < 3; ++i) p[i] = dot3_rn(M[3 * i], M[3 * i + 1], M[3 * i + 2], v[0], v[1], v[2]);
+        const float fx = rintf(p[0] / p[2]), fy = rintf(p[1] / p[2]);
+        // far-off or non-finite positions: any out-of-image value keeps the masks' logic
+        qx[s] = isfinite(fx) ? int(fminf(fmaxf(fx, -1e6f), 1e6f)) : -1000000;
+        qy[s] = isfinite(fy) ? int(fminf(fmaxf(fy, -1e6f), 1e6f)) : -1000000;
+    }
+    auto valid = [&](int x, int y) { return x >= hpx && x < W - hpx && y >= hpy && y < H - hpy; };
+    const bool va = valid(xa, ya), v1 = valid(qx[0], qy[0]), v2 = valid(qx[1], qy[1]);
+    const int cx1 = min(max(qx[0], 0), W - 1), cy1 = min(max(qy[0], 0), H - 1);
+    const int cx2 = min(max(qx[1], 0), W - 1), cy2 = min(max(qy[1], 0), H - 1);
+    const int xs = min(max(xa, 0), W - 1), ys = min(max(ya, 0), H - 1);
+    const float r1 = patch_rmse(imgs, H, W, C, ia, ys, xs, ib, cy1, cx1, hpy, hpx);
+    const float r2 = patch_rmse(imgs, H, W, C, ia, ys, xs, ib, cy2, cx2, hpy, hpx);
+    bool a = ((r1 < r2) || !v2) && (r1 < thr) && v1 && va;
+    bool b = ((r2 < r1) || !v1) && (r2 < thr) && v2 && va;
+    if (!(v1 || v2)) {
+        a = a || (d1[r] > d2[r]);
+        b = b || (d2[r] > d1[r]);
+    }
+    m1[r] = a;
+    m2[r] = b;
 }
 
 // pts[r * S + i] = o[r] + d[r] * z[r, i]  (SimpleNeRF17.py:213-215).  The product
@@ -158,13 +328,52 @@ __global__ void ray_points_kernel(const float* __restrict__ o, const float* __re
 
 using namespace srf;
 
-extern "C" int srf_depth_consistency_loss(const float* pred, const float* target, const uint8_t* mask, int n,
-                                          float weight, float* loss_dev, float* grad, void* stream) {
-    if (!pred || !target || !grad) return SRF_ERR_NULL;
+extern "C" int srf_depth_mse_loss(const float* pred, const float* target, const uint8_t* mask, int n, float weight,
+                                  int mean_over_mask, float* loss_dev, float* grad_pred, float* grad_target,
+                                  void* stream) {
     if (n < 0) return SRF_ERR_SHAPE;
     if (n == 0) return SRF_OK;
-    depth_consistency_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(pred, target, mask, n, weight, loss_dev,
-                                                                             grad);
+    if (!pred || !target) return SRF_ERR_NULL;
+    depth_mse_kernel<<<1, 1024, 0, as_stream(stream)>>>(pred, target, mask, n, weight, mean_over_mask, loss_dev,
+                                                        grad_pred, grad_target);
+    return launch_status();
+}
+
+// torch.linspace(0, B - 1, S % B) (CPU/CUDA formula: start + step i below the
+// halfway point, end - step (steps - 1 - i) above it, in float), truncated: the
+// bins that take one extra sample (MassConcentrationLoss06.py:69-72).
+static bool bin_layout(int s, int nb, BinLayout* bl) {
+    if (nb < 1 || nb > 64 || s < nb) return false;
+    bool bigger[64] = {};
+    const int per = s / nb, rem = s % nb;
+    if (rem == 1) {
+        bigger[0] = true;
+    } else if (rem > 1) {
+        const float start = 0.f, end = float(nb - 1);
+        const float step = (end - start) / float(rem - 1);
+        for (int i = 0; i < rem; ++i) {
+            float v = i < rem / 2 ? start + step * float(i) : end - step * float(rem - 1 - i);
+            int k = int(v);
+            if (k < 0 || k >= nb) return false;
+            bigger[k] = true;
+        }
+    }
+    bl->nb = nb;
+    bl->start[0] = 0;
+    for (int b = 0; b < nb; ++b) bl->start[b + 1] = bl->start[b] + per + (bigger[b] ? 1 : 0);
+    return bl->start[nb] == s;
+}
+
+extern "C" int srf_mass_concentration_loss(const float* weights, int n_rays, int n_samples, int num_bins,
+                                           const uint8_t* mask, float weight, float* loss_dev, float* grad_weights,
+                                           void* stream) {
+    if (n_rays < 0) return SRF_ERR_SHAPE;
+    BinLayout bl;
+    if (!bin_layout(n_samples, num_bins, &bl)) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    if (!weights) return SRF_ERR_NULL;
+    mass_concentration_kernel<<<1, 1024, 0, as_stream(stream)>>>(weights, n_rays, n_samples, bl, mask, weight,
+                                                                 loss_dev, grad_weights);
     return launch_status();
 }
 
@@ -246,5 +455,23 @@ extern "C" int srf_adam_step(float* param, const float* grad, float* exp_avg, fl
     if (blocks > 152 * 8) blocks = 152 * 8;
     adam_kernel<<<blocks, 256, 0, as_stream(stream)>>>(param, grad, exp_avg, exp_avg_sq, n, lr, beta1, beta2, eps,
                                                        weight_decay, bc1, bc2, step_dev, skip_dev);
+    return launch_status();
+}
+
+extern "C" int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth1,
+                                            const float* depth2, const int32_t* pixel_ids, int n_rays,
+                                            const float* poses, int n_views, const float* intrinsics0,
+                                            const float* images, int height, int width, int channels, int patch_w,
+                                            int patch_h, float rmse_threshold, uint8_t* mask1, uint8_t* mask2,
+                                            void* stream) {
+    if (n_rays < 0 || n_views < 1 || height < 1 || width < 1 || channels < 1 || channels > 64) return SRF_ERR_SHAPE;
+    if (patch_w < 1 || patch_h < 1 || patch_w > 31 || patch_h > 31) return SRF_ERR_SHAPE;
+    if (n_rays == 0) return SRF_OK;
+    if (!rays_o || !rays_d || !depth1 || !depth2 || !pixel_ids || !poses || !intrinsics0 || !images || !mask1 ||
+        !mask2)
+        return SRF_ERR_NULL;
+    reprojection_masks_kernel<<<grid_1d(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, depth1, depth2, pixel_ids, n_rays, poses, n_views, intrinsics0, images, height, width,
+        channels, patch_w / 2, patch_h / 2, rmse_threshold, mask1, mask2, device_flag());
     return launch_status();
 }

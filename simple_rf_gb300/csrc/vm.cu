@@ -108,6 +108,39 @@ __global__ void density_fwd_kernel(srf_vm_grid g, const float* __restrict__ pts,
     out[p] = acc;
 }
 
+// 4 consecutive floats (16-byte aligned) of one corner: a plane's or a line's R components
+// are contiguous in the channels-last layout.
+__device__ __forceinline__ float4 corner4(const float* __restrict__ base, int idx, int R, int r) {
+    return *reinterpret_cast<const float4*>(base + int64_t(idx) * R + r);
+}
+
+__device__ __forceinline__ void red_add4(float* dst, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
+// Bilinearly interpolated components r..r+3 of a plane and of a line.
+__device__ __forceinline__ void interp4(const float* __restrict__ pl, const float* __restrict__ ln, int R, int r,
+                                        const Taps& pt, const Taps& lt, float4& pv, float4& lv) {
+    pv = make_float4(0.f, 0.f, 0.f, 0.f);
+    lv = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        if (pt.idx[c] >= 0) {
+            float4 v = corner4(pl, pt.idx[c], R, r);
+            float w = pt.w[c];
+            pv.x += v.x * w; pv.y += v.y * w; pv.z += v.z * w; pv.w += v.w * w;
+        }
+        if (lt.idx[c] >= 0) {
+            float4 v = corner4(ln, lt.idx[c], R, r);
+            float w = lt.w[c];
+            lv.x += v.x * w; lv.y += v.y * w; lv.z += v.z * w; lv.w += v.w * w;
+        }
+    }
+}
+
+// Components are grouped by 4 (R multiple of 4, checked on the host) so each
+// corner access is one 128-bit load.
 __global__ void color_fwd_kernel(srf_vm_grid g, const float* __restrict__ pts, int64_t n, int ld, float* out) {
     int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (p >= n) return;
@@ -117,51 +150,90 @@ __global__ void color_fwd_kernel(srf_vm_grid g, const float* __restrict__ pts, i
     for (int i = 0; i < 3; ++i) {
         Taps pt, lt;
         plane_taps(g, i, q, pt, lt);
-        int R = g.n_comp[i];
+        const int R = g.n_comp[i];
         const float* pl = g.planes[i];
         const float* ln = g.lines[i];
-        for (int r = 0; r < R; ++r) {
-            float pv = 0.f, lv = 0.f;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
-                if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+        if ((R & 3) == 0) {
+            for (int r = 0; r < R; r += 4) {
+                float4 pv, lv;
+                interp4(pl, ln, R, r, pt, lt, pv, lv);
+                o[off + r] = pv.x * lv.x;
+                o[off + r + 1] = pv.y * lv.y;
+                o[off + r + 2] = pv.z * lv.z;
+                o[off + r + 3] = pv.w * lv.w;
             }
-            o[off + r] = pv * lv;
+        } else {
+            for (int r = 0; r < R; ++r) {
+                float pv = 0.f, lv = 0.f;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
+                    if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+                }
+                o[off + r] = pv * lv;
+            }
         }
         off += R;
     }
 }
 
-// Adjoint: d plane[r] at corner c += w_c * d * line_value[r] (and symmetrically).
-// Colour: d_features (P, ld) per component; density: one scalar per point.
+// Adjoint: d plane[r] at corner c += w_c * d_r * line_value[r] (and symmetrically),
+// four components per 128-bit reduction.  Colour: d_features (P, ld) per component;
+// density: one scalar per point.
 __global__ void vm_bwd_kernel(srf_vm_grid gg, srf_vm_grid g, const float* __restrict__ pts, int64_t n,
                               const float* __restrict__ dfeat, int ld, int per_component) {
     int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const float* q = pts + 3 * p;
+    const float ds = per_component ? 0.f : dfeat[p];
+    if (!per_component && ds == 0.f) return;
     int off = 0;
     for (int i = 0; i < 3; ++i) {
         Taps pt, lt;
         plane_taps(g, i, q, pt, lt);
-        int R = g.n_comp[i];
-        const float* pl = g.planes[i];
-        const float* ln = g.lines[i];
+        const int R = g.n_comp[i];
         float* gpl = gg.planes[i];
         float* gln = gg.lines[i];
-        for (int r = 0; r < R; ++r) {
-            float pv = 0.f, lv = 0.f;
+        if ((R & 3) != 0 || (per_component && ((ld | off) & 3) != 0)) {
+            // component counts that are not multiples of 4: scalar loads and atomics
+            const float* pl = g.planes[i];
+            const float* ln = g.lines[i];
+            for (int r = 0; r < R; ++r) {
+                float pv = 0.f, lv = 0.f;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
-                if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+                for (int c = 0; c < 4; ++c) {
+                    if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
+                    if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+                }
+                float d = per_component ? dfeat[p * ld + off + r] : ds;
+                float dp = d * lv, dl = d * pv;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (pt.idx[c] >= 0 && dp != 0.f) atomicAdd(gpl + int64_t(pt.idx[c]) * R + r, dp * pt.w[c]);
+                    if (lt.idx[c] >= 0 && dl != 0.f) atomicAdd(gln + int64_t(lt.idx[c]) * R + r, dl * lt.w[c]);
+                }
             }
-            float d = per_component ? dfeat[p * ld + off + r] : dfeat[p];
-            float dp = d * lv, dl = d * pv;
+            off += R;
+            continue;
+        }
+        for (int r = 0; r < R; r += 4) {
+            float4 d = per_component ? *reinterpret_cast<const float4*>(dfeat + p * ld + off + r)
+                                     : make_float4(ds, ds, ds, ds);
+            if (d.x == 0.f && d.y == 0.f && d.z == 0.f && d.w == 0.f) continue;
+            float4 pv, lv;
+            interp4(g.planes[i], g.lines[i], R, r, pt, lt, pv, lv);
+            const float4 dp = make_float4(d.x * lv.x, d.y * lv.y, d.z * lv.z, d.w * lv.w);
+            const float4 dl = make_float4(d.x * pv.x, d.y * pv.y, d.z * pv.z, d.w * pv.w);
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                if (pt.idx[c] >= 0 && dp != 0.f) atomicAdd(gpl + int64_t(pt.idx[c]) * R + r, dp * pt.w[c]);
-                if (lt.idx[c] >= 0 && dl != 0.f) atomicAdd(gln + int64_t(lt.idx[c]) * R + r, dl * lt.w[c]);
+                if (pt.idx[c] >= 0) {
+                    const float w = pt.w[c];
+                    red_add4(gpl + int64_t(pt.idx[c]) * R + r, dp.x * w, dp.y * w, dp.z * w, dp.w * w);
+                }
+                if (lt.idx[c] >= 0) {
+                    const float w = lt.w[c];
+                    red_add4(gln + int64_t(lt.idx[c]) * R + r, dl.x * w, dl.y * w, dl.z * w, dl.w * w);
+                }
             }
         }
         off += R;
@@ -402,6 +474,8 @@ extern "C" int srf_vm_density_backward(const srf_vm_grid* grad_grid, const srf_v
     if ((st = check_grid(grad_grid, true))) return st;
     if (!pts || !d_features) return SRF_ERR_NULL;
     if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    for (int i = 0; i < 3; ++i)
+        if (grad_grid->n_comp[i] != grid->n_comp[i] || grad_grid->res[i] != grid->res[i]) return SRF_ERR_SHAPE;
     vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, 1, 0);
     return launch_status();
 }
@@ -424,7 +498,11 @@ extern "C" int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_
     if ((st = check_grid(grad_grid, true))) return st;
     if (!pts || !d_features) return SRF_ERR_NULL;
     if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    for (int i = 0; i < 3; ++i)
+        if (grad_grid->n_comp[i] != grid->n_comp[i] || grad_grid->res[i] != grid->res[i]) return SRF_ERR_SHAPE;
     int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
+    // rows of d_features are read 16 bytes at a time when ld is a multiple of 4
+    if ((ld & 3) == 0 && !aligned16(d_features)) return SRF_ERR_ALIGN;
     vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, ld, 1);
     return launch_status();
 }

@@ -12,6 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import functional as F
 from ._lib import call
 from .functional import _ptr, _require, _stream
 
@@ -290,3 +291,52 @@ def linear(x, weight, bias=None, act=_lib.SRF_ACT_NONE, rows_dev=None):
     """act(x @ weight.T + bias) on the first ``*rows_dev`` rows (all rows when None)."""
     return _LinearFunction.apply(x.contiguous(), weight.contiguous(), None if bias is None else bias.contiguous(), act,
                                  rows_dev)
+
+
+class _RendererTcFunction(torch.autograd.Function):
+    """basis_matrix_color + MlpFeaturesColorPredictor on the tensor cores
+    (srf_tensorf_renderer_*): feats (m, C) and per-sample view dirs (m, 3) -> rgb (m, 3).
+    FP16 backwards fit a per-call loss scale to the incoming gradient."""
+
+    @staticmethod
+    def forward(ctx, desc, precision, feats, view, *params):
+        m = feats.shape[0]
+        feats = feats.contiguous()
+        params = [p.detach().contiguous() for p in params]
+        need_grad = any(ctx.needs_input_grad[2:3]) or any(ctx.needs_input_grad[4:])
+        lib = _lib.load()
+        ws = torch.empty(max(int(lib.srf_tensorf_renderer_workspace_size(ctypes.byref(desc), m, precision,
+                                                                          int(need_grad))), 1),
+                         dtype=torch.uint8, device=feats.device)
+        if ws.numel() <= 1 and m > 0:
+            raise RuntimeError('TensoRF renderer configuration not supported on the tensor-core path '
+                               '(units must be 128 or 256)')
+        rgb = torch.empty(m, 3, device=feats.device)
+        scaler = F.loss_scaler(feats.device) if precision == _lib.SRF_PRECISION_FP16 else None
+        _lib.call('srf_tensorf_renderer_forward', ctypes.byref(desc), F._ptr_array(params), F._ptr(feats),
+                  F._ptr(view), m, F._ptr(rgb), precision, int(need_grad), F._ptr(ws), ws.numel(), F._ptr(scaler),
+                  F._stream())
+        ctx.desc, ctx.precision, ctx.m, ctx.scaler = desc, precision, m, scaler
+        ctx.ws = ws if need_grad else None
+        ctx.params = params
+        ctx.save_for_backward(feats)
+        return rgb
+
+    @staticmethod
+    def backward(ctx, drgb):
+        (feats,) = ctx.saved_tensors
+        drgb = drgb.contiguous()
+        grads = [torch.zeros_like(p) for p in ctx.params]
+        d_feats = torch.empty_like(feats)
+        if ctx.scaler is not None:
+            _lib.call('srf_loss_scaler_fit', F._ptr(ctx.scaler), F._ptr(drgb), drgb.numel(), None, 0, 1024.0,
+                      F._stream())
+        _lib.call('srf_tensorf_renderer_backward', ctypes.byref(ctx.desc), F._ptr_array(ctx.params), F._ptr(feats),
+                  F._ptr(drgb), ctx.m, F._ptr_array(grads), F._ptr(d_feats), ctx.precision, F._ptr(ctx.ws),
+                  ctx.ws.numel(), F._ptr(ctx.scaler), F._stream())
+        ctx.ws = None
+        return (None, None, d_feats, None) + tuple(grads)
+
+
+def renderer_tc(desc, precision, feats, view, params):
+    return _RendererTcFunction.apply(desc, precision, feats, view, *params)

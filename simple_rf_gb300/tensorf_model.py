@@ -24,7 +24,7 @@ from torch.nn import ModuleDict, ModuleList
 from . import _lib
 from . import functional as F
 from . import tensorf as T
-from .nerf import ExtrinsicsLearner, IntrinsicsLearner
+from .nerf import ExtrinsicsLearner, IntrinsicsLearner, _precision
 
 MATRIX_AXES = [[0, 1], [0, 2], [1, 2]]   # SimpleTensoRF09.py:1131
 VECTOR_AXES = [2, 1, 0]                  # SimpleTensoRF09.py:1132
@@ -130,6 +130,8 @@ class GbVmTensor(torch.nn.Module):
             raise NotImplementedError(tensor_configs['color_predictor'])
         self.color_predictor = MlpFeaturesColorPredictor(tensor_configs, tensor_configs['features_dimension_color'],
                                                          tensor_configs['num_units_color_predictor'])
+        # configs['model']['precision']: 'fp32' (plain) or 'bf16' / 'fp16' (renderer MLP on the tensor cores)
+        self.precision = _precision(configs)
         self._register_load_state_dict_pre_hook(self._load_hook)
 
     # ------------------------------------------------------------ geometry --
@@ -226,11 +228,21 @@ class GbVmTensor(torch.nn.Module):
         if ns:
             ps = T.gather_rows(pn, idx_s, cnt_s, ns)
             feats = T.vm_color(self._grid('color'), ps)
-            basis = T.linear(feats, self.basis_matrix_color.weight)
-            cin = {'features': basis}
+            view_s = None
             if self.tensor_configs['view_dependent_color']:
-                cin['view_dirs'] = T.gather_rows(input_dict['view_dirs'].contiguous().float(), idx_s, cnt_s, ns, s)
-            rgb_s = self.color_predictor(cin)['color']
+                view_s = T.gather_rows(input_dict['view_dirs'].contiguous().float(), idx_s, cnt_s, ns, s)
+            if self.precision == _lib.SRF_PRECISION_FP32:
+                cin = {'features': T.linear(feats, self.basis_matrix_color.weight)}
+                if view_s is not None:
+                    cin['view_dirs'] = view_s
+                rgb_s = self.color_predictor(cin)['color']
+            else:
+                cp = self.color_predictor
+                desc = _lib.RendererDesc(feats.shape[1], cp.features_dimension, cp.mlp[0].out_features, cp.lf, cp.lv,
+                                         int(view_s is not None))
+                rgb_s = T.renderer_tc(desc, self.precision, feats, view_s,
+                                      [self.basis_matrix_color.weight, cp.mlp[0].weight, cp.mlp[0].bias,
+                                       cp.mlp[2].weight, cp.mlp[2].bias, cp.mlp[4].weight, cp.mlp[4].bias])
             rgb = T.scatter_rows(rgb_s, idx_s, cnt_s, rows).view(n, s, 3)
         else:
             rgb = torch.zeros(n, s, 3, device=dev)

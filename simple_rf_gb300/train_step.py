@@ -260,9 +260,9 @@ class NerfTrainStep:
         # augmented depth as a (detached) target of the main coarse depth
         for net in self.run[2:]:
             if net.level == 'coarse' and self.consistency_weight > 0:
-                chk(lib.srf_depth_consistency_loss(_vp(main_coarse.b['depth']), _vp(net.b['depth']), None, n,
-                                                   self.consistency_weight, _vp(self.loss),
-                                                   _vp(main_coarse.b['g_depth']), st), 'consistency')
+                chk(lib.srf_depth_mse_loss(_vp(main_coarse.b['depth']), _vp(net.b['depth']), None, n,
+                                           self.consistency_weight, 0, _vp(self.loss), _vp(main_coarse.b['g_depth']),
+                                           None, st), 'consistency')
         for net in reversed(self.run):
             b = net.b
             ss = self.level[net.level]['z'].shape[1]

@@ -381,6 +381,99 @@ def tensorf_case():
     return out
 
 
+def losses_case():
+    """The reference's per-ray losses on random inputs with autograd gradients:
+    MassConcentrationLoss06.compute_entropy_loss (64 and 67 samples, 5 bins),
+    SparseDepthMSE14.compute_depth_loss, CoarseFineConsistencyLoss33.compute_loss and
+    AugmentationsDepthLoss11.compute_depth_mse."""
+    from loss_functions import AugmentationsDepthLoss11 as LAD
+    from loss_functions import CoarseFineConsistencyLoss33 as LCF
+    from loss_functions import MassConcentrationLoss06 as LMC
+    from loss_functions import SparseDepthMSE14 as LSD
+    g = torch.Generator().manual_seed(31)
+    out = {}
+    n = 40
+    mask = torch.rand(n, generator=g) < 0.7
+    out['mask'] = mask.numpy()
+    for s in (64, 67):
+        w = (torch.rand(n, s, generator=g) * 0.05).requires_grad_(True)
+        mc = LMC.MassConcentrationLoss({'model': {}}, {'num_bins': 5})
+        loss = mc.compute_entropy_loss(w, mask, False)['loss_value']
+        loss.backward()
+        out[f'mc{s}_weights'] = w.detach().numpy()
+        out[f'mc{s}_loss'] = loss.detach().numpy()
+        out[f'mc{s}_grad'] = w.grad.numpy()
+    pred = (torch.rand(n, generator=g) * 4 + 2).requires_grad_(True)
+    true = torch.rand(n, generator=g) * 4 + 2
+    loss = LSD.SparseDepthMSE.compute_depth_loss(pred, true, mask, False)['loss_value']
+    loss.backward()
+    out.update(sd_pred=pred.detach().numpy(), sd_true=true.numpy(), sd_loss=loss.detach().numpy(),
+               sd_grad=pred.grad.numpy())
+    dc = (torch.rand(n, generator=g) * 4 + 2).requires_grad_(True)
+    df = (torch.rand(n, generator=g) * 4 + 2).requires_grad_(True)
+    cf = LCF.CoarseFineConsistencyLoss({'model': {'coarse_model': {}, 'fine_model': {}}, 'data_loader': {'ndc': False}},
+                                       {})
+    loss = cf.compute_loss({'target_rgb': torch.zeros(n, 3)}, {'depth_coarse': dc, 'depth_fine': df}, None,
+                           False)['loss_value']
+    loss.backward()
+    out.update(cf_coarse=dc.detach().numpy(), cf_fine=df.detach().numpy(), cf_loss=loss.detach().numpy(),
+               cf_grad_coarse=dc.grad.numpy(), cf_grad_fine=df.grad.numpy())
+    d1 = (torch.rand(n, generator=g) * 4 + 2).requires_grad_(True)
+    d2 = torch.rand(n, generator=g) * 4 + 2
+    loss, _ = LAD.AugmentationsDepthLoss.compute_depth_mse(d1.clone(), d2.clone(), mask)
+    loss.backward()
+    out.update(ad_pred=d1.detach().numpy(), ad_target=d2.numpy(), ad_loss=loss.detach().numpy(),
+               ad_grad=d1.grad.numpy())
+    return out
+
+
+def reprojection_case():
+    """AugmentationsDepthLoss11.compute_loss_nerf on 4 forward-facing 40x30 views
+    (random images, distinct camera origins) and 300 rays through random pixels,
+    with depths near the scene plane: masks (from the loss maps), loss, gradients."""
+    from loss_functions import AugmentationsDepthLoss11 as LAD
+    g = torch.Generator().manual_seed(41)
+    v, h, w = 4, 30, 40
+    images = torch.rand(v, h, w, 3, generator=g)
+    # a smooth scene so nearby views see similar patches for the right depth
+    yy, xx = torch.meshgrid(torch.arange(h).float(), torch.arange(w).float(), indexing='ij')
+    base = torch.stack([torch.sin(xx / 5), torch.cos(yy / 4), torch.sin((xx + yy) / 7)], -1) * 0.5 + 0.5
+    images = 0.9 * base[None].expand(v, h, w, 3) + 0.1 * images
+    poses = torch.eye(4).repeat(v, 1, 1)
+    poses[:, :3, 3] = torch.tensor([[0.0, 0.0, 0.0], [0.06, 0.0, 0.0], [0.0, 0.05, 0.01], [-0.07, 0.02, 0.0]])
+    k = torch.tensor([[30.0, 0.0, w / 2.0], [0.0, 30.0, h / 2.0], [0.0, 0.0, 1.0]])
+    intr = k[None].repeat(v, 1, 1)
+    n = 300
+    img = torch.randint(0, v, (n,), generator=g)
+    px = torch.randint(0, w, (n,), generator=g)
+    py = torch.randint(0, h, (n,), generator=g)
+    pid = torch.stack([img, px, py], -1)
+    rays_o, rays_d = CU.get_rays_tr(pid, intr[img], poses[img], False)
+    d1 = (1.5 + torch.rand(n, generator=g) * 2).requires_grad_(True)
+    d2 = (1.5 + torch.rand(n, generator=g) * 2).requires_grad_(True)
+    loss_fn = LAD.AugmentationsDepthLoss({'model': {}}, {'patch_size': [5, 5], 'rmse_threshold': 0.2})
+    mask = torch.ones(n, dtype=torch.bool)
+    # record the masks compute_loss_nerf hands to compute_depth_mse (mask2 first, then mask1)
+    seen = []
+    orig = LAD.AugmentationsDepthLoss.compute_depth_mse
+
+    def spy(pred_depth, gt_depth, mask=None):
+        seen.append(mask.clone())
+        return orig(pred_depth, gt_depth, mask)
+
+    LAD.AugmentationsDepthLoss.compute_depth_mse = staticmethod(spy)
+    try:
+        loss, map1, map2 = loss_fn.compute_loss_nerf(d1.clone(), d2.clone(), mask, rays_o, rays_d, poses, images,
+                                                     pid, intr, (h, w))
+    finally:
+        LAD.AugmentationsDepthLoss.compute_depth_mse = orig
+    loss.backward()
+    return dict(images=images.numpy(), poses=poses.numpy(), k=k.numpy(), pixel_ids=pid.numpy().astype(np.int32),
+                rays_o=rays_o.numpy(), rays_d=rays_d.numpy(), depth1=d1.detach().numpy(), depth2=d2.detach().numpy(),
+                loss=loss.detach().numpy(), mask1=seen[1].numpy(), mask2=seen[0].numpy(),
+                grad1=d1.grad.numpy(), grad2=d2.grad.numpy())
+
+
 def main():
     cases = {
         'nerf_sampling': sampling_case,
@@ -396,6 +489,8 @@ def main():
             augs=[{'name': 'views_augmentation', 'coarse_model': mlp_cfg(lp=4, views=False, vdr=False)}],
             aug_seeds=[77]),
         'tensorf': tensorf_case,
+        'losses': losses_case,
+        'reprojection': reprojection_case,
     }
     only = sys.argv[1:]
     for name, fn in cases.items():

@@ -1,0 +1,147 @@
+"""Loss kernels (srf_depth_mse_loss, srf_mass_concentration_loss) against the
+reference's own loss modules (golden fixture) and the loss oracle: loss values
+and gradients within 1e-5 relative."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import losses as ol
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from simple_rf_gb300 import build as b
+    b.build()
+
+
+def _t(a, dtype=torch.float32):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(DEV, dtype)
+
+
+def _mass(weights, bins, mask):
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _ptr, _stream
+    w = _t(weights)
+    m = _t(mask, torch.uint8) if mask is not None else None
+    loss = torch.zeros(1, device=DEV)
+    g = torch.zeros_like(w)
+    _lib.call('srf_mass_concentration_loss', _ptr(w), w.shape[0], w.shape[1], bins, _ptr(m), 1.0, _ptr(loss),
+              _ptr(g), _stream())
+    torch.cuda.synchronize()
+    return float(loss.item()), g.cpu().numpy()
+
+
+def _depth(pred, target, mask, over_mask, both):
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _ptr, _stream
+    p, t = _t(pred), _t(target)
+    m = _t(mask, torch.uint8) if mask is not None else None
+    loss = torch.zeros(1, device=DEV)
+    gp, gt = torch.zeros_like(p), torch.zeros_like(t)
+    _lib.call('srf_depth_mse_loss', _ptr(p), _ptr(t), _ptr(m), p.shape[0], 1.0, int(over_mask), _ptr(loss), _ptr(gp),
+              _ptr(gt) if both else None, _stream())
+    torch.cuda.synchronize()
+    return float(loss.item()), gp.cpu().numpy(), gt.cpu().numpy()
+
+
+def test_mass_concentration_matches_reference_golden(golden):
+    g = golden('losses')
+    for s in (64, 67):
+        loss, grad = _mass(g[f'mc{s}_weights'], 5, g['mask'])
+        assert abs(loss - float(g[f'mc{s}_loss'])) < 1e-5 * abs(float(g[f'mc{s}_loss'])), s
+        np.testing.assert_allclose(grad, g[f'mc{s}_grad'], rtol=1e-5, atol=1e-8)
+
+
+def test_depth_losses_match_reference_golden(golden):
+    g = golden('losses')
+    loss, gp, _ = _depth(g['sd_pred'], g['sd_true'], g['mask'], True, False)
+    assert abs(loss - float(g['sd_loss'])) < 1e-5 * float(g['sd_loss'])
+    np.testing.assert_allclose(gp, g['sd_grad'], rtol=1e-5, atol=1e-9)
+    loss, gc, gf = _depth(g['cf_coarse'], g['cf_fine'], None, False, True)
+    assert abs(loss - float(g['cf_loss'])) < 1e-5 * float(g['cf_loss'])
+    np.testing.assert_allclose(gc, g['cf_grad_coarse'], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(gf, g['cf_grad_fine'], rtol=1e-5, atol=1e-9)
+    loss, gp, _ = _depth(g['ad_pred'], g['ad_target'], g['mask'], False, False)
+    assert abs(loss - float(g['ad_loss'])) < 1e-5 * float(g['ad_loss'])
+    np.testing.assert_allclose(gp, g['ad_grad'], rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.parametrize('n,s,bins', [(4096, 64, 5), (1000, 192, 7), (3, 10, 10), (0, 64, 5)])
+def test_mass_concentration_against_oracle(n, s, bins):
+    rng = np.random.default_rng(n + s)
+    w = (rng.random((n, s)) * 0.03).astype(np.float32)
+    mask = rng.random(n) < 0.8
+    if n == 0:
+        loss, grad = _mass(np.zeros((0, s), np.float32), bins, None)
+        assert loss == 0.0 and grad.size == 0
+        return
+    ref_loss, ref_grad = ol.mass_concentration(w.astype(np.float64), bins, mask)
+    loss, grad = _mass(w, bins, mask)
+    assert abs(loss - ref_loss) < 1e-5 * abs(ref_loss), (loss, ref_loss)
+    np.testing.assert_allclose(grad, ref_grad, rtol=1e-5, atol=1e-9)
+
+
+def test_loss_kernels_reject_bad_shapes():
+    from simple_rf_gb300 import _lib
+    lib = _lib.load()
+    w = torch.zeros(4, 8, device=DEV)
+    assert lib.srf_mass_concentration_loss(w.data_ptr(), 4, 8, 9, None, 1.0, None, None, None) != 0   # bins > S
+    assert lib.srf_mass_concentration_loss(w.data_ptr(), 4, 8, 65, None, 1.0, None, None, None) != 0
+    assert lib.srf_depth_mse_loss(None, None, None, 4, 1.0, 0, None, None, None, None) != 0
+    assert lib.srf_depth_mse_loss(None, None, None, 0, 1.0, 0, None, None, None, None) == 0
+
+
+def _masks(g, thr=0.2):
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _ptr, _stream
+    n = g['depth1'].shape[0]
+    t = {k: _t(g[k]) for k in ('rays_o', 'rays_d', 'depth1', 'depth2', 'poses', 'k', 'images')}
+    pid = _t(g['pixel_ids'], torch.int32)
+    m1 = torch.zeros(n, dtype=torch.uint8, device=DEV)
+    m2 = torch.zeros_like(m1)
+    v, h, w, c = g['images'].shape
+    _lib.call('srf_depth_reprojection_masks', _ptr(t['rays_o']), _ptr(t['rays_d']), _ptr(t['depth1']),
+              _ptr(t['depth2']), _ptr(pid), n, _ptr(t['poses']), v, _ptr(t['k']), _ptr(t['images']), h, w, c, 5, 5,
+              thr, _ptr(m1), _ptr(m2), _stream())
+    torch.cuda.synchronize()
+    return m1.cpu().numpy().astype(bool), m2.cpu().numpy().astype(bool)
+
+
+def test_reprojection_masks_match_reference_golden(golden):
+    g = golden('reprojection')
+    m1, m2 = _masks(g)
+    np.testing.assert_array_equal(m1, g['mask1'])
+    np.testing.assert_array_equal(m2, g['mask2'])
+
+
+def test_reprojection_masks_against_oracle_random_scene():
+    """4000 rays over 6 views with random rotations: masks equal the oracle's except
+    on rays whose reprojection lies within 1e-3 px of a rounding boundary."""
+    rng = np.random.default_rng(8)
+    v, h, w = 6, 48, 64
+    yy, xx = np.meshgrid(np.arange(h), np.arange(w), indexing='ij')
+    base = np.stack([np.sin(xx / 6), np.cos(yy / 5), np.sin((xx + yy) / 9)], -1) * 0.5 + 0.5
+    images = (0.9 * base[None] + 0.1 * rng.random((v, h, w, 3))).astype(np.float32)
+    poses = np.tile(np.eye(4, dtype=np.float32), (v, 1, 1))
+    for i in range(v):
+        a = rng.normal(0, 0.03, 3)
+        kx = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+        poses[i, :3, :3] = (np.eye(3) + kx + kx @ kx / 2).astype(np.float32)
+        poses[i, :3, 3] = rng.uniform(-0.1, 0.1, 3)
+    k = np.array([[40.0, 0, w / 2], [0, 40.0, h / 2], [0, 0, 1]], np.float32)
+    n = 4000
+    pid = np.stack([rng.integers(0, v, n), rng.integers(0, w, n), rng.integers(0, h, n)], 1).astype(np.int32)
+    dirs = np.stack([(pid[:, 1] - w / 2) / 40.0, -(pid[:, 2] - h / 2) / 40.0, -np.ones(n)], 1)
+    rays_d = np.einsum('nij,nj->ni', poses[pid[:, 0], :3, :3], dirs).astype(np.float32)
+    rays_o = poses[pid[:, 0], :3, 3].astype(np.float32)
+    g = dict(images=images, poses=poses, k=k, pixel_ids=pid, rays_o=rays_o, rays_d=rays_d,
+             depth1=rng.uniform(1.0, 4.0, n).astype(np.float32), depth2=rng.uniform(1.0, 4.0, n).astype(np.float32))
+    m1, m2 = _masks(g)
+    r1, r2, p1, p2 = ol.reprojection_masks(g['depth1'], g['depth2'], rays_o, rays_d, pid, poses, k, images, (5, 5), 0.2)
+    near = lambda p: (np.abs(np.abs(p - np.floor(p)) - 0.5) < 1e-3).any(1)  # noqa: E731
+    bad = (m1 != r1) | (m2 != r2)
+    assert r1.sum() > 100 and r2.sum() > 100
+    assert not (bad & ~(near(p1) | near(p2))).any(), np.flatnonzero(bad)[:10]

@@ -102,3 +102,34 @@ def test_tensorf_full_size_grid_gather_roundtrip():
     cl = [T.to_channels_last(torch.randn(1, 48, 300, 1, device=DEV) * 0.1) for _ in range(3)]
     c1 = T.vm_color(T.VmGridTensors(cp, cl, res), pts[:4096])
     assert c1.shape == (4096, 144) and torch.isfinite(c1).all()
+
+
+@pytest.mark.parametrize('precision,bar', [('fp16', 3e-2), ('bf16', 8e-2)])
+def test_tensorf_tensor_core_renderer_against_fp32(precision, bar):
+    """The 16-bit tensor-core renderer (basis + MlpFeaturesColorPredictor) against
+    the FP32 path on the same model and rays (64^3 grid, R = 16/48, 128 units):
+    rgb within 2e-3 max-abs; whole gradient of the renderer and the colour grid
+    within `bar` relative L2."""
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300.bench_tensorf import make_models, synthetic_rays
+    res = {}
+    for prec in ('fp32', precision):
+        tm = make_models(DEV, seed=3, precision=prec, grids=(64, 32))[0]
+        o, d, t_rgb, u = synthetic_rays(256, 5, DEV)
+        from simple_rf_gb300 import functional as F
+        s = int(tm.num_samples.item())
+        z = F.aabb_z(o, d, s, tm.bounding_box.detach().cpu(), 2.0, 6.0, float(tm.step_size), u[:, 0].contiguous())
+        out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': F.view_dirs(d)}, retraw=False)
+        loss = ((out['rgb'] - t_rgb) ** 2).mean()
+        loss.backward()
+        params = [tm.basis_matrix_color.weight] + list(tm.color_predictor.parameters()) + list(tm.matrices_color) + \
+            list(tm.vectors_color)
+        res[prec] = (out['rgb'].detach(), torch.cat([p.grad.reshape(-1) for p in params]), tm.last_sample_counts)
+    (r32, g32, c32), (r16, g16, c16) = res['fp32'], res[precision]
+    assert c32['surface'] > 1000 and c32 == c16, (c32, c16)
+    err = (r16 - r32).abs().max().item()
+    rel = ((g16 - g32).norm() / g32.norm()).item()
+    print(precision, 'rgb max-abs', err, 'renderer+colour-grid gradient rel-L2', rel)
+    assert err < 2e-3, err
+    assert rel < bar, rel

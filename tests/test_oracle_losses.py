@@ -1,0 +1,48 @@
+"""The loss oracle (oracle/losses.py) against the reference's own loss modules
+(golden fixture tests/golden/losses.npz, made by tests/golden/make_golden.py)."""
+import numpy as np
+
+from oracle import losses as ol
+
+
+def test_mass_concentration_matches_reference(golden):
+    g = golden('losses')
+    for s in (64, 67):
+        loss, grad = ol.mass_concentration(g[f'mc{s}_weights'].astype(np.float64), 5, g['mask'])
+        assert abs(loss - float(g[f'mc{s}_loss'])) < 1e-5 * abs(float(g[f'mc{s}_loss'])), s
+        np.testing.assert_allclose(grad, g[f'mc{s}_grad'], rtol=1e-5, atol=1e-8)
+
+
+def test_bin_sizes_follow_linspace_rule():
+    # torch.linspace(0, 4, 4) = [0, 1.33, 2.67, 4] -> bins 0, 1, 2, 4 take the extra sample
+    assert ol.bin_sizes(64, 5) == [13, 13, 13, 12, 13]
+    for s, b in ((64, 5), (67, 5), (192, 7), (100, 10)):
+        assert sum(ol.bin_sizes(s, b)) == s
+
+
+def test_depth_losses_match_reference(golden):
+    g = golden('losses')
+    f64 = lambda k: g[k].astype(np.float64)  # noqa: E731
+    loss, gp, _ = ol.depth_mse(f64('sd_pred'), f64('sd_true'), g['mask'], mean_over_mask=True)
+    assert abs(loss - float(g['sd_loss'])) < 1e-5 * float(g['sd_loss'])
+    np.testing.assert_allclose(gp, g['sd_grad'], rtol=1e-5, atol=1e-9)
+    loss, gc, gf = ol.depth_mse(f64('cf_coarse'), f64('cf_fine'), target_grad=True)
+    assert abs(loss - float(g['cf_loss'])) < 1e-5 * float(g['cf_loss'])
+    np.testing.assert_allclose(gc, g['cf_grad_coarse'], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(gf, g['cf_grad_fine'], rtol=1e-5, atol=1e-9)
+    loss, gp, _ = ol.depth_mse(f64('ad_pred'), f64('ad_target'), g['mask'])
+    assert abs(loss - float(g['ad_loss'])) < 1e-5 * float(g['ad_loss'])
+    np.testing.assert_allclose(gp, g['ad_grad'], rtol=1e-5, atol=1e-9)
+
+
+def test_reprojection_masks_and_loss_match_reference(golden):
+    g = golden('reprojection')
+    m1, m2, _, _ = ol.reprojection_masks(g['depth1'], g['depth2'], g['rays_o'], g['rays_d'], g['pixel_ids'],
+                                         g['poses'], g['k'], g['images'], (5, 5), 0.2)
+    np.testing.assert_array_equal(m1, g['mask1'])
+    np.testing.assert_array_equal(m2, g['mask2'])
+    assert m1.sum() > 10 and m2.sum() > 10
+    loss, g1, g2 = ol.reprojection_depth_loss(g['depth1'].astype(np.float64), g['depth2'].astype(np.float64), m1, m2)
+    assert abs(loss - float(g['loss'])) < 1e-5 * float(g['loss'])
+    np.testing.assert_allclose(g1, g['grad1'], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(g2, g['grad2'], rtol=1e-5, atol=1e-9)
