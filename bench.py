@@ -231,6 +231,47 @@ def time_variant(config, precision, steps, dev, stream):
     return out
 
 
+def time_tensorf(precision, steps, dev, stream):
+    """TensoRF VM training step (300^3 main + 75^3 augmented model, 8192 rays; see
+    simple_rf_gb300/bench_tensorf.py) through the drop-in modules."""
+    import torch
+    from simple_rf_gb300.bench_tensorf import TensorfTrainStep, make_models, synthetic_rays
+    models = make_models(dev, precision=precision)
+    st = TensorfTrainStep(models)
+    batches = [synthetic_rays(8192, 10 + i, dev) for i in range(4)]
+    for i in range(2):
+        st.step(*batches[i % 4])
+    torch.cuda.synchronize(dev)
+    t = time_steps(lambda i: st.step(*batches[i % 4]), steps, stream)
+    counts = {m.name: dict(c) for m, c in zip(models, st.last['samples'])}
+    del st, models, batches
+    torch.cuda.empty_cache()
+    return {'ms_per_step': round(1e3 * t / steps, 3), 'rays_per_s': round(8192 * steps / t, 1), 'steps': steps,
+            'samples_per_step': counts}
+
+
+def time_render(dev, stream):
+    """Full-image render of 8 views of 504x378 NDC rays through the NeRF pair (BF16,
+    chunks of 65536) and a 262,144-ray prefix on the FP32 plain path."""
+    import torch
+    from simple_rf_gb300.render import NerfPairRenderer, pixel_rays, synthetic_views
+    pid, intr, ext = synthetic_views(8, 378, 504, device=dev)
+    o, d = pixel_rays(pid, intr, ext)
+    n = o.shape[0]
+    out = {'rays': n, 'chunk': 65536}
+    for prec, nr in (('bf16', n), ('fp32', 4 * 65536)):
+        r = NerfPairRenderer(65536, prec, dev, graph=(prec != 'fp32'))
+        r.render(o[:65536], d[:65536])
+        torch.cuda.synchronize(dev)
+        t = time_steps(lambda i: r.render(o[:nr], d[:nr]), 1, stream)
+        out[prec] = {'rays': nr, 'ms': round(1e3 * t, 2), 'rays_per_s': round(nr / t, 1),
+                     'samples_per_s': round(nr * r.samples_per_ray() / t, 1)}
+        del r
+        torch.cuda.empty_cache()
+    out['speedup_bf16_vs_fp32_plain'] = round(out['bf16']['rays_per_s'] / out['fp32']['rays_per_s'], 2)
+    return out
+
+
 def cpu_baseline(sample_rays=128, min_seconds=10.0):
     """The oracle port of the reference step on the host cores (bounded sample)."""
     import numpy as np
@@ -371,6 +412,9 @@ def run_ours(args):
         variants['nerf_fp16'] = time_variant('nerf', 'fp16', args.steps, dev, stream)
         for prec, k in (('bf16', args.steps), ('fp16', args.steps), ('fp32', k32)):
             variants[f'nerf_pair_{prec}'] = time_variant('nerf_pair', prec, k, dev, stream)
+        variants['tensorf_fp16'] = time_tensorf('fp16', 5, dev, stream)
+        variants['tensorf_fp32'] = time_tensorf('fp32', 3, dev, stream)
+        variants['render'] = time_render(dev, stream)
     import ctypes
     fl = ctypes.c_int(0)
     _lib.check(_lib.load().srf_read_device_flag(ctypes.byref(fl), ctypes.c_void_p(stream.cuda_stream)), 'flag')
@@ -411,6 +455,13 @@ def run_ours(args):
                       'fp32_plain': variants['nerf_pair_fp32'],
                       'speedup_bf16_vs_fp32_plain': round(variants['nerf_pair_bf16']['rays_per_s'] /
                                                           variants['nerf_pair_fp32']['rays_per_s'], 2)},
+        'tensorf': {'workload': 'TensoRF VM fwd+bwd+Adam, 300^3 (R 16/48) + 75^3 augmented model, 8192 rays, '
+                                'alpha mask 128^3 at 15%, renderer PE L=2 -> 128 -> 128 -> 3',
+                    'fp16': variants['tensorf_fp16'], 'fp32_plain': variants['tensorf_fp32'],
+                    'speedup_fp16_vs_fp32_plain': round(variants['tensorf_fp16']['rays_per_s'] /
+                                                        variants['tensorf_fp32']['rays_per_s'], 2)},
+        'render': dict(variants['render'], workload='8 views x 504x378 NDC rays, NeRF pair (main coarse+fine + '
+                                                    'augmented coarse), 64+128 samples, chunks of 65536'),
         'device_flag': fl.value,
         'e2e': {'value': round(ws * N_RAYS * args.steps / t_e2e, 1), 'unit': 'rays/s', 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': 4},

@@ -67,15 +67,15 @@ int num_sms() {
 
 bool ok16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-template <int BN>
-int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, tc::GemmShape sh,
+template <int BN, int EW>
+int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, tc::GemmShape sh,
                    tc::GemmEpilogue ep, cudaStream_t s) {
     int kb = sh.kb0 + sh.kb1;
     if (tc::SmemPlan<BN>::stages(kb) < 2) return SRF_ERR_UNSUPPORTED;
     size_t smem = tc::SmemPlan<BN>::bytes(kb);
     static bool attr_done = false;
     if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(tc::tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(tc::tc_gemm_kernel<BN, EW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              int(tc::kMaxSmem));
         if (e != cudaSuccess) {
             set_cuda_error(e);
@@ -85,8 +85,17 @@ int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
     }
     int64_t tiles = (sh.M + tc::kBlockM - 1) / tc::kBlockM;
     int grid = int(tiles < num_sms() ? tiles : num_sms());
-    tc::tc_gemm_kernel<BN><<<grid, tc::kGemmThreads, smem, s>>>(a0, a1, b, sh, ep);
+    tc::tc_gemm_kernel<BN, EW><<<grid, tc::gemm_threads(EW), smem, s>>>(a0, a1, b, sh, ep);
     return launch_status();
+}
+
+// Backward epilogues (ReLU mask, column sums, the sigma-head adjoint) carry enough
+// per-element work to keep 8 epilogue warps busy; forward epilogues run on 4.
+template <int BN>
+int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, tc::GemmShape sh,
+                   tc::GemmEpilogue ep, cudaStream_t s) {
+    if (ep.mask || ep.colsum || ep.r1_row) return launch_gemm_ew<BN, 8>(a0, a1, b, sh, ep, s);
+    return launch_gemm_ew<BN, 4>(a0, a1, b, sh, ep, s);
 }
 
 }  // namespace
@@ -782,8 +791,8 @@ struct RenderWs {
     op16* h2;        // (m, U)
     float* rgb;      // (m, 3)
     op16 *W1, *W1T, *W2, *W2T;
+    float* WbT;      // (C, kMaxBasis)
     op16 *dz0, *dz1, *dx;   // (m, U), (m, U), (m, k1p)
-    float* dB;       // (m, F)
     float* partial;
     size_t partial_floats;
 };
@@ -800,11 +809,11 @@ size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size
     w.W1T = c.take<op16>(size_t(R.U) * R.k1p);
     w.W2 = c.take<op16>(size_t(R.U) * R.U);
     w.W2T = c.take<op16>(size_t(R.U) * R.U);
+    w.WbT = c.take<float>(size_t(R.C) * kMaxBasis);
     if (bwd) {
         w.dz0 = c.take<op16>(size_t(m) * R.U);
         w.dz1 = c.take<op16>(size_t(m) * R.U);
         w.dx = c.take<op16>(size_t(m) * R.k1p);
-        w.dB = c.take<float>(size_t(m) * R.F);
         w.partial_floats = tc_wgrad_partial_floats(R.U, 256);
         w.partial = c.take<float>(w.partial_floats);
     }
@@ -826,8 +835,17 @@ __host__ __device__ inline size_t basis_stage_bytes(int C, int k1p) {
     return fb > xb ? fb : xb;
 }
 
+// WbT[c, o] = Wb[o, c] for o < F, 0 up to kMaxBasis: the layout the basis pass
+// loads with 128-bit reads (one per-step pass over F x C weights).
+__global__ void transpose_basis_kernel(const float* __restrict__ Wb, int F, int C, float* WbT) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C * kMaxBasis) return;
+    const int c = i / kMaxBasis, o = i - c * kMaxBasis;
+    WbT[i] = o < F ? Wb[o * C + c] : 0.f;
+}
+
 __global__ void __launch_bounds__(kBasisRows)
-    basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ Wb, int F,
+    basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ WbT, int F,
                         const float* __restrict__ view, int64_t M, int lf, int lv, int k1p, float* B, op16* x,
                         int fmt) {
     extern __shared__ float bsm[];
@@ -837,12 +855,21 @@ __global__ void __launch_bounds__(kBasisRows)
     const int stride = k1p + 2;
     const int64_t row0 = int64_t(blockIdx.x) * kBasisRows;
     const int64_t rows = M - row0 < kBasisRows ? M - row0 : kBasisRows;
-    for (int i = threadIdx.x; i < C * kMaxBasis; i += blockDim.x) {
-        const int c = i / kMaxBasis, o = i % kMaxBasis;
-        sWt[i] = o < F ? Wb[o * C + c] : 0.f;
+    {
+        const float4* src = reinterpret_cast<const float4*>(WbT);
+        float4* dst = reinterpret_cast<float4*>(sWt);
+        for (int i = threadIdx.x; i < C * kMaxBasis / 4; i += blockDim.x) dst[i] = src[i];
     }
-    const float* gf = feats + row0 * C;
-    for (int64_t i = threadIdx.x; i < rows * C; i += blockDim.x) sF[(i / C) * (C + 1) + i % C] = gf[i];
+    {   // warp w copies rows w, w + nwarps, ... (lanes along the row: coalesced, no division)
+        const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        const float* gf = feats + row0 * C;
+        for (int rr = threadIdx.x >> 5; rr < rows; rr += nw) {
+            const float* g = gf + int64_t(rr) * C;
+            float* d = sF + rr * (C + 1);
+#pragma unroll 4
+            for (int c = lane; c < C; c += 32) d[c] = g[c];
+        }
+    }
     __syncthreads();
     const int rg = threadIdx.x >> 3, cg = threadIdx.x & 7;   // rows rg*8.., columns cg*4..
     float acc[8][4];
@@ -906,29 +933,101 @@ __global__ void __launch_bounds__(kBasisRows)
     for (int w = threadIdx.x; w < rows * wx; w += kBasisRows) gx[w] = src[(w / wx) * ws + w % wx];
 }
 
-// dB[m, o] = sum over the PE columns of B[m, o] of dx * d(column)/dB, with dx the
-// 16-bit (loss-scaled by gscale[0]) gradient of the encoded row; unscaled here.
-__global__ void basis_pe_bwd_kernel(const op16* __restrict__ dx, const float* __restrict__ B, int64_t M, int F,
-                                    int lf, int k1p, int fmt, const float* gscale, float* dB) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= M * F) return;
-    const int64_t m = i / F;
-    const int o = int(i % F);
-    const op16* row = dx + m * k1p;
-    auto rd = [&](int col) {
-        const uint32_t w = reinterpret_cast<const uint32_t*>(row)[col >> 1];
-        float2 f = tc::unpack16(w, fmt);
-        return (col & 1) ? f.y : f.x;
-    };
-    const float b = B[m * F + o];
-    float g = rd(o);
-    for (int k = 0; k < lf; ++k) {
-        const float fk = float(1 << k);
-        float sn, cs;
-        sincosf(b * fk, &sn, &cs);
-        g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
+// Basis-layer backward fused with the PE adjoint, over a contiguous range of rows
+// per block, kBwdTile rows at a time:
+//   dB[m, o]    = sum over the PE columns of B[m, o] of dx * d(column)/dB (dx: the
+//                 16-bit encoded-row gradient, loss-scaled by gscale[0]; unscaled here)
+//   d_feats[m]  = dB[m] . Wb                       (written)
+//   dWb        += dB^T . feats                     (one atomic per weight per block)
+// Each tile's feature rows, dx rows and B rows are first copied into shared memory
+// with coalesced, independent loads; thread c then owns feature column c, with its
+// Wb column and its dWb accumulators in registers and the dB rows read as
+// shared-memory broadcasts.
+constexpr int kBwdTile = 32;
+
+__host__ __device__ inline size_t basis_bwd_smem(int C, int F, int k1p) {
+    return size_t(kBwdTile) * kMaxBasis * 4 + size_t(kBwdTile) * C * 4 + size_t(kBwdTile) * F * 4 +
+           size_t(kBwdTile) * k1p * 2;
+}
+
+__global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __restrict__ B,
+                                 const float* __restrict__ feats, const float* __restrict__ Wb, int64_t M, int F,
+                                 int C, int lf, int k1p, int fmt, const float* gscale, int64_t rows_per_block,
+                                 float* d_feats, float* dWb) {
+    extern __shared__ __align__(16) float bb[];
+    float* sdB = bb;                                   // kBwdTile x kMaxBasis
+    float* sF = sdB + kBwdTile * kMaxBasis;            // kBwdTile x C
+    float* sB = sF + kBwdTile * C;                     // kBwdTile x F
+    op16* sdx = reinterpret_cast<op16*>(sB + kBwdTile * F);   // kBwdTile x k1p
+    const float unscale = gscale ? gscale[1] : 1.f;
+    const int c = threadIdx.x;
+    float wcol[kMaxBasis], acc[kMaxBasis];
+#pragma unroll
+    for (int o = 0; o < kMaxBasis; ++o) {
+        wcol[o] = (c < C && o < F) ? Wb[o * C + c] : 0.f;
+        acc[o] = 0.f;
     }
-    dB[i] = gscale ? g * gscale[1] : g;
+    const int64_t r_begin = int64_t(blockIdx.x) * rows_per_block;
+    const int64_t r_end = r_begin + rows_per_block < M ? r_begin + rows_per_block : M;
+    for (int64_t t0 = r_begin; t0 < r_end; t0 += kBwdTile) {
+        const int nt = int(r_end - t0 < kBwdTile ? r_end - t0 : kBwdTile);
+        {   // stage the tile: contiguous rows in global memory
+            const float* gf = feats + t0 * C;
+#pragma unroll 4
+            for (int i = threadIdx.x; i < nt * C; i += blockDim.x) sF[i] = gf[i];
+            const float* gb = B + t0 * F;
+            for (int i = threadIdx.x; i < nt * F; i += blockDim.x) sB[i] = gb[i];
+            const uint4* gx = reinterpret_cast<const uint4*>(dx + t0 * k1p);
+            uint4* sx = reinterpret_cast<uint4*>(sdx);
+            for (int i = threadIdx.x; i < nt * k1p / 8; i += blockDim.x) sx[i] = gx[i];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < kBwdTile * kMaxBasis; i += blockDim.x) {
+            const int rr = i / kMaxBasis, o = i - rr * kMaxBasis;
+            float g = 0.f;
+            if (rr < nt && o < F) {
+                const op16* row = sdx + rr * k1p;
+                auto rd = [&](int col) {
+                    const uint32_t w = reinterpret_cast<const uint32_t*>(row)[col >> 1];
+                    const float2 f = tc::unpack16(w, fmt);
+                    return (col & 1) ? f.y : f.x;
+                };
+                const float b = sB[rr * F + o];
+                g = rd(o);
+                for (int k = 0; k < lf; ++k) {
+                    const float fk = float(1 << k);
+                    float sn, cs;
+                    sincosf(b * fk, &sn, &cs);
+                    g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
+                }
+                g *= unscale;
+            }
+            sdB[i] = g;
+        }
+        __syncthreads();
+        if (c < C) {
+            for (int rr = 0; rr < nt; ++rr) {
+                const float f = sF[rr * C + c];
+                float dfe = 0.f;
+#pragma unroll
+                for (int o4 = 0; o4 < kMaxBasis; o4 += 4) {
+                    const float4 d = *reinterpret_cast<const float4*>(sdB + rr * kMaxBasis + o4);
+                    dfe += d.x * wcol[o4] + d.y * wcol[o4 + 1] + d.z * wcol[o4 + 2] + d.w * wcol[o4 + 3];
+                    acc[o4] += d.x * f;
+                    acc[o4 + 1] += d.y * f;
+                    acc[o4 + 2] += d.z * f;
+                    acc[o4 + 3] += d.w * f;
+                }
+                d_feats[(t0 + rr) * C + c] = dfe;
+            }
+        }
+        __syncthreads();
+    }
+    if (c < C) {
+#pragma unroll
+        for (int o = 0; o < kMaxBasis; ++o)
+            if (o < F) atomicAdd(dWb + o * C + c, acc[o]);
+    }
 }
 
 }  // namespace
@@ -961,8 +1060,10 @@ int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float
             return SRF_ERR_CUDA;
         }
     }
+    transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
+    if ((st = launch_status())) return st;
     basis_encode_kernel<<<unsigned((m + kBasisRows - 1) / kBasisRows), kBasisRows, smem, s>>>(
-        feats, C, P[0], F, view ? vdirs : nullptr, m, lf, lv, R.k1p, w.B, w.x, fmt);
+        feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1p, w.B, w.x, fmt);
     if ((st = launch_status())) return st;
     if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
                         w.W1, R.k1p, U, 0, m, U, s)))
@@ -1004,11 +1105,25 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
         tc::GemmEpilogue e1 = make_epilogue(w.dx + c0, R.k1p, nullptr, 0, fmt, cx.found_inf());
         if ((st = tc_linear(e1, w.dz1, U, U, nullptr, 0, 0, w.W1T, U, R.k1p, c0, m, n, s))) return st;
     }
-    basis_pe_bwd_kernel<<<grid_1d(m * F, 256), 256, 0, s>>>(w.dx, w.B, m, F, lf, R.k1p, fmt, cx.gscale(), w.dB);
-    if ((st = launch_status())) return st;
-    // basis layer (FP32): d_feats = dB . Wb, dWb += dB^T feats
-    return srf_linear_backward(d_feats, C, G[0], nullptr, w.dB, F, nullptr, 0, feats, C, P[0], w.dB, m, nullptr, F,
-                               C, SRF_ACT_NONE, 1, s);
+    // PE adjoint + basis layer: d_feats = dB . Wb, dWb += dB^T feats
+    const int threads = (C + 31) / 32 * 32;
+    int64_t blocks = int64_t(num_sms()) * 2;
+    int64_t per = (m + blocks - 1) / blocks;
+    per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
+    blocks = (m + per - 1) / per;
+    const size_t bsmem = basis_bwd_smem(C, F, R.k1p);
+    if (bsmem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
+    if (bsmem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(basis_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(bsmem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+    }
+    basis_bwd_kernel<<<unsigned(blocks), threads, bsmem, s>>>(w.dx, w.B, feats, P[0], m, F, C, lf, R.k1p, fmt,
+                                                             cx.gscale(), per, d_feats, G[0]);
+    return launch_status();
 }
 
 }  // namespace srf

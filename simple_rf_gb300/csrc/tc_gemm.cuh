@@ -24,7 +24,9 @@ namespace tc {
 constexpr int kBlockM = 128;
 constexpr int kBlockK = 64;   // one 128-byte swizzle atom of BF16
 constexpr int kThreads = 192;       // weight-gradient kernel: producer, MMA, 4 epilogue warps
-constexpr int kGemmThreads = 320;   // layer kernel: producer, MMA, 8 epilogue warps (2 per TMEM lane quadrant)
+// layer kernel: producer warp, MMA warp, EW epilogue warps (4: one per TMEM lane
+// quadrant; 8: two per quadrant, each taking half of the columns)
+constexpr int gemm_threads(int ew) { return 64 + 32 * ew; }
 constexpr uint32_t kATileBytes = kBlockM * kBlockK * 2;
 constexpr size_t kMaxSmem = 232448;
 
@@ -106,8 +108,8 @@ struct SmemPlan {
     }
 };
 
-template <int BN>
-__global__ void __launch_bounds__(kGemmThreads, 1)
+template <int BN, int EW>
+__global__ void __launch_bounds__(gemm_threads(EW), 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
                    const __grid_constant__ CUtensorMap tmB, GemmShape shape, GemmEpilogue ep) {
     extern __shared__ uint8_t smem_raw[];
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(&acc_full[a], 1);
-            mbar_init(&acc_empty[a], 256);
+            mbar_init(&acc_empty[a], 32 * EW);
         }
         mbar_init(b_full, 1);
         mbar_init(done, 1);
@@ -239,11 +241,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
     } else if (warp >= 2) {
         // --------------------------------------------------------- epilogue
-        // Warps w and w + 4 share the tensor-memory lane quadrant q = w % 4 (rows
-        // q*32 .. q*32+31 of the tile); `half` 0 takes the first BN/2 columns, 1 the rest.
+        // Warp w reads the tensor-memory lane quadrant q = w % 4 (rows q*32 .. q*32+31
+        // of the tile).  With 8 epilogue warps, w and w + 4 share a quadrant and `half`
+        // 0 takes the first BN/2 columns, 1 the rest.
+        static_assert(EW == 4 || EW == 8, "4 or 8 epilogue warps");
         const int q = warp & 3;
-        const int half = (warp - 2) >> 2;
-        constexpr int kHalfChunks = BN / 64;   // 32-column chunks per half
+        const int half = EW == 8 ? (warp - 2) >> 2 : 0;
+        constexpr int kHalfChunks = EW == 8 ? BN / 64 : BN / 32;   // 32-column chunks per warp
         const int c0 = half * kHalfChunks;
         uint32_t t = 0;
         float r1_total = 0.f;
@@ -334,7 +338,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
                 tmem_ld_wait();
             }
-            if (hunits) {   // kernel-uniform: half 1 hands its partial dot products to half 0
+            if (EW == 8 && hunits) {   // kernel-uniform: half 1 hands its partial dot products to half 0
                 // The slot of accumulator `acc` is rewritten two tiles later, only after this
                 // tile's acc_empty completed, which needs half 0's arrival below: no reuse race.
                 float* x = shx + (acc * 128 + q * 32 + lane) * 4;

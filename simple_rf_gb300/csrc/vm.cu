@@ -6,6 +6,7 @@
 // single 64-byte line, read with 128-bit loads.  One thread handles one
 // (point, plane) pair for the density path, and one point for colour.
 #include <mutex>
+#include <type_traits>
 
 #include "srf_common.cuh"
 
@@ -237,6 +238,98 @@ __global__ void vm_bwd_kernel(srf_vm_grid gg, srf_vm_grid g, const float* __rest
             }
         }
         off += R;
+    }
+}
+
+// Group forms of the colour gather and of the scatter-add adjoint: G lanes share a
+// point and lane j of the group takes components 4j, 4j + 4G, ... of every plane,
+// so each corner access of a warp covers whole contiguous rows of components
+// (192 bytes for R = 48) instead of 32 unrelated 16-byte pieces.  Needs every
+// R_i and the feature row length to be multiples of 4 (checked on the host).
+template <int G>
+__global__ void color_fwd_group_kernel(srf_vm_grid g, const float* __restrict__ pts, int64_t n, int ld,
+                                       float* __restrict__ out) {
+    const int j = threadIdx.x % G;
+    const int64_t p = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / G;
+    if (p >= n) return;
+    const float* q = pts + 3 * p;
+    float* o = out + p * ld;
+    int off = 0;
+    for (int i = 0; i < 3; ++i) {
+        Taps pt, lt;
+        plane_taps(g, i, q, pt, lt);
+        const int R = g.n_comp[i];
+        for (int r = 4 * j; r < R; r += 4 * G) {
+            float4 pv, lv;
+            interp4(g.planes[i], g.lines[i], R, r, pt, lt, pv, lv);
+            *reinterpret_cast<float4*>(o + off + r) = make_float4(pv.x * lv.x, pv.y * lv.y, pv.z * lv.z, pv.w * lv.w);
+        }
+        off += R;
+    }
+}
+
+template <int G>
+__global__ void vm_bwd_group_kernel(srf_vm_grid gg, srf_vm_grid g, const float* __restrict__ pts, int64_t n,
+                                    const float* __restrict__ dfeat, int ld, int per_component) {
+    const int j = threadIdx.x % G;
+    const int64_t p = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / G;
+    if (p >= n) return;
+    const float* q = pts + 3 * p;
+    const float ds = per_component ? 0.f : dfeat[p];
+    if (!per_component && ds == 0.f) return;
+    int off = 0;
+    for (int i = 0; i < 3; ++i) {
+        Taps pt, lt;
+        plane_taps(g, i, q, pt, lt);
+        const int R = g.n_comp[i];
+        float* gpl = gg.planes[i];
+        float* gln = gg.lines[i];
+        for (int r = 4 * j; r < R; r += 4 * G) {
+            const float4 d = per_component ? *reinterpret_cast<const float4*>(dfeat + p * ld + off + r)
+                                           : make_float4(ds, ds, ds, ds);
+            if (d.x == 0.f && d.y == 0.f && d.z == 0.f && d.w == 0.f) continue;
+            float4 pv, lv;
+            interp4(g.planes[i], g.lines[i], R, r, pt, lt, pv, lv);
+            const float4 dp = make_float4(d.x * lv.x, d.y * lv.y, d.z * lv.z, d.w * lv.w);
+            const float4 dl = make_float4(d.x * pv.x, d.y * pv.y, d.z * pv.z, d.w * pv.w);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) {
+                    const float w = pt.w[c];
+                    red_add4(gpl + int64_t(pt.idx[c]) * R + r, dp.x * w, dp.y * w, dp.z * w, dp.w * w);
+                }
+                if (lt.idx[c] >= 0) {
+                    const float w = lt.w[c];
+                    red_add4(gln + int64_t(lt.idx[c]) * R + r, dl.x * w, dl.y * w, dl.z * w, dl.w * w);
+                }
+            }
+        }
+        off += R;
+    }
+}
+
+// Lanes per point for the group kernels: the smallest power of two >= max_i R_i / 4
+// (0 when some R_i is not a multiple of 4: use the per-thread kernels).
+int group_lanes(const srf_vm_grid& g) {
+    int mx = 0;
+    for (int i = 0; i < 3; ++i) {
+        if (g.n_comp[i] & 3) return 0;
+        mx = g.n_comp[i] / 4 > mx ? g.n_comp[i] / 4 : mx;
+    }
+    int G = 1;
+    while (G < mx && G < 32) G <<= 1;
+    return G;
+}
+
+template <class F>
+int launch_grouped(int G, int64_t n, F&& launch) {
+    switch (G) {
+        case 1: return launch(std::integral_constant<int, 1>{});
+        case 2: return launch(std::integral_constant<int, 2>{});
+        case 4: return launch(std::integral_constant<int, 4>{});
+        case 8: return launch(std::integral_constant<int, 8>{});
+        case 16: return launch(std::integral_constant<int, 16>{});
+        default: return launch(std::integral_constant<int, 32>{});
     }
 }
 
@@ -476,6 +569,15 @@ extern "C" int srf_vm_density_backward(const srf_vm_grid* grad_grid, const srf_v
     if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
     for (int i = 0; i < 3; ++i)
         if (grad_grid->n_comp[i] != grid->n_comp[i] || grad_grid->res[i] != grid->res[i]) return SRF_ERR_SHAPE;
+    const int G = group_lanes(*grid);
+    if (G) {
+        return launch_grouped(G, n_pts, [&](auto gc) {
+            constexpr int g = decltype(gc)::value;
+            vm_bwd_group_kernel<g><<<grid_1d(n_pts * g, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts,
+                                                                                           n_pts, d_features, 1, 0);
+            return launch_status();
+        });
+    }
     vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, 1, 0);
     return launch_status();
 }
@@ -487,6 +589,15 @@ extern "C" int srf_vm_color_forward(const srf_vm_grid* grid, const float* pts, i
     if (!pts || !features) return SRF_ERR_NULL;
     if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
     int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
+    const int G = group_lanes(*grid);
+    if (G && (ld & 3) == 0 && aligned16(features)) {
+        return launch_grouped(G, n_pts, [&](auto gc) {
+            constexpr int g = decltype(gc)::value;
+            color_fwd_group_kernel<g><<<grid_1d(n_pts * g, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, ld,
+                                                                                              features);
+            return launch_status();
+        });
+    }
     color_fwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, ld, features);
     return launch_status();
 }
@@ -503,6 +614,15 @@ extern "C" int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_
     int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
     // rows of d_features are read 16 bytes at a time when ld is a multiple of 4
     if ((ld & 3) == 0 && !aligned16(d_features)) return SRF_ERR_ALIGN;
+    const int G = group_lanes(*grid);
+    if (G) {   // G != 0 implies ld % 4 == 0; d_features alignment is checked above
+        return launch_grouped(G, n_pts, [&](auto gc) {
+            constexpr int g = decltype(gc)::value;
+            vm_bwd_group_kernel<g><<<grid_1d(n_pts * g, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts,
+                                                                                           n_pts, d_features, ld, 1);
+            return launch_status();
+        });
+    }
     vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, ld, 1);
     return launch_status();
 }
