@@ -68,11 +68,11 @@ int num_sms() {
 bool ok16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 template <int BN, int EW>
-int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, tc::GemmShape sh,
-                   tc::GemmEpilogue ep, cudaStream_t s) {
+int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
+                   tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
     int kb = sh.kb0 + sh.kb1;
-    if (tc::SmemPlan<BN>::stages(kb) < 2) return SRF_ERR_UNSUPPORTED;
-    size_t smem = tc::SmemPlan<BN>::bytes(kb);
+    if (tc::SmemPlan<BN, EW>::stages(kb) < 2) return SRF_ERR_UNSUPPORTED;
+    size_t smem = tc::SmemPlan<BN, EW>::bytes(kb);
     static bool attr_done = false;
     if (!attr_done) {
         cudaError_t e = cudaFuncSetAttribute(tc::tc_gemm_kernel<BN, EW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -85,17 +85,17 @@ int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
     }
     int64_t tiles = (sh.M + tc::kBlockM - 1) / tc::kBlockM;
     int grid = int(tiles < num_sms() ? tiles : num_sms());
-    tc::tc_gemm_kernel<BN, EW><<<grid, tc::gemm_threads(EW), smem, s>>>(a0, a1, b, sh, ep);
+    tc::tc_gemm_kernel<BN, EW><<<grid, tc::gemm_threads(EW), smem, s>>>(a0, a1, b, out, sh, ep);
     return launch_status();
 }
 
 // Backward epilogues (ReLU mask, column sums, the sigma-head adjoint) carry enough
 // per-element work to keep 8 epilogue warps busy; forward epilogues run on 4.
 template <int BN>
-int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, tc::GemmShape sh,
-                   tc::GemmEpilogue ep, cudaStream_t s) {
-    if (ep.mask || ep.colsum || ep.r1_row) return launch_gemm_ew<BN, 8>(a0, a1, b, sh, ep, s);
-    return launch_gemm_ew<BN, 4>(a0, a1, b, sh, ep, s);
+int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
+                   tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
+    if (ep.mask || ep.colsum || ep.r1_row) return launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s);
+    return launch_gemm_ew<BN, 4>(a0, a1, b, out, sh, ep, s);
 }
 
 }  // namespace
@@ -139,11 +139,14 @@ int tc_linear(const tc::GemmEpilogue& ep, const op16* x0, int64_t ld0, int k0, c
     }
     if (!make_map(&mb, w, uint64_t(k0 + k1), uint64_t(w_rows), uint64_t(ldw) * 2, 64, uint32_t(n)))
         return SRF_ERR_CUDA;
+    // output map for the TMA-store epilogue: n columns of rows ld_out apart, 64 x 32 boxes
+    CUtensorMap mo;
+    if (!make_map(&mo, ep.out, uint64_t(n), uint64_t(M), uint64_t(ld_out) * 2, 64, 32)) return SRF_ERR_CUDA;
     tc::GemmShape sh{M, k0 / 64, k1 / 64, w_row0};
     switch (n) {
-        case 64: return launch_gemm_bn<64>(ma0, ma1, mb, sh, ep, s);
-        case 128: return launch_gemm_bn<128>(ma0, ma1, mb, sh, ep, s);
-        default: return launch_gemm_bn<256>(ma0, ma1, mb, sh, ep, s);
+        case 64: return launch_gemm_bn<64>(ma0, ma1, mb, mo, sh, ep, s);
+        case 128: return launch_gemm_bn<128>(ma0, ma1, mb, mo, sh, ep, s);
+        default: return launch_gemm_bn<256>(ma0, ma1, mb, mo, sh, ep, s);
     }
 }
 

@@ -89,14 +89,20 @@ struct GemmShape {
     int b_row0;     // first B row (output column 0)
 };
 
-template <int BN>
+// Output through TMA stores when every epilogue warp owns a multiple of 64 columns:
+// each warp stages 32 rows x 64 columns (128-byte rows, 128-byte swizzle) and
+// stores them with one bulk tensor copy.
+constexpr bool tma_store_ok(int bn, int ew) { return (bn / (ew / 4)) % 64 == 0; }
+
+template <int BN, int EW = 4>
 struct SmemPlan {
     static constexpr uint32_t kBBlockBytes = BN * kBlockK * 2;
+    static constexpr uint32_t kStoreBytes = tma_store_ok(BN, EW) ? uint32_t(EW) * 32 * 128 : 0u;
     // partial head sums handed between the two warps of a lane quadrant: [2 acc][128 rows][4]
     static constexpr uint32_t kHeadXBytes = 2 * 128 * 4 * 4;
     // 1024 B alignment slack + 256 B of barriers + BN floats each of bias, column
     // sums and r1 mask column sums + 4 x BN head weights + 4 head biases + head exchange
-    static constexpr size_t kReserve = 1024 + 256 + BN * 12 + 4 * BN * 4 + 16 + kHeadXBytes;
+    static constexpr size_t kReserve = 1024 + 256 + BN * 12 + 4 * BN * 4 + 16 + kHeadXBytes + kStoreBytes;
     static __host__ __device__ int stages(int kb_total) {
         size_t b = size_t(kb_total) * kBBlockBytes;
         if (b + kReserve + 2 * kATileBytes > kMaxSmem) return 0;
@@ -111,15 +117,19 @@ struct SmemPlan {
 template <int BN, int EW>
 __global__ void __launch_bounds__(gemm_threads(EW), 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
-                   const __grid_constant__ CUtensorMap tmB, GemmShape shape, GemmEpilogue ep) {
+                   const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmOut,
+                   GemmShape shape, GemmEpilogue ep) {
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int kb_total = shape.kb0 + shape.kb1;
-    const int stages = SmemPlan<BN>::stages(kb_total);
+    using Plan = SmemPlan<BN, EW>;
+    constexpr bool kTmaStore = tma_store_ok(BN, EW);
+    const int stages = Plan::stages(kb_total);
     uint8_t* sB = base;
-    uint8_t* sA = sB + size_t(kb_total) * SmemPlan<BN>::kBBlockBytes;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + size_t(stages) * kATileBytes);
+    uint8_t* sA = sB + size_t(kb_total) * Plan::kBBlockBytes;
+    uint8_t* sOut = sA + size_t(stages) * kATileBytes;    // [EW warps][32 rows][128 B], 1024-aligned
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sOut + Plan::kStoreBytes);
     uint64_t* full = bars;              // [stages]
     uint64_t* empty = bars + 8;         // [stages]
     uint64_t* acc_full = bars + 16;     // [2]
@@ -176,9 +186,10 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
         prefetch_tmap(&tmA0);
         if (shape.kb1) prefetch_tmap(&tmA1);
         prefetch_tmap(&tmB);
-        mbar_arrive_expect_tx(b_full, uint32_t(kb_total) * SmemPlan<BN>::kBBlockBytes);
+        if (kTmaStore) prefetch_tmap(&tmOut);
+        mbar_arrive_expect_tx(b_full, uint32_t(kb_total) * Plan::kBBlockBytes);
         for (int kb = 0; kb < kb_total; ++kb)
-            tma_load_2d(sB + size_t(kb) * SmemPlan<BN>::kBBlockBytes, &tmB, b_full, kb * kBlockK, shape.b_row0);
+            tma_load_2d(sB + size_t(kb) * Plan::kBBlockBytes, &tmB, b_full, kb * kBlockK, shape.b_row0);
         uint32_t it = 0;
         uint32_t last_parity[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         bool used[8] = {false, false, false, false, false, false, false, false};
@@ -223,7 +234,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                 }
                 tc_fence_after();
                 uint32_t a_addr = smem_u32(sA + size_t(s) * kATileBytes);
-                uint32_t b_addr = smem_u32(sB + size_t(kb) * SmemPlan<BN>::kBBlockBytes);
+                uint32_t b_addr = smem_u32(sB + size_t(kb) * Plan::kBBlockBytes);
 #pragma unroll
                 for (int k = 0; k < kBlockK / 16; ++k) {
                     uint64_t ad = smem_desc(a_addr + k * 32, 0, 1024, kSwizzle128B);
@@ -271,12 +282,18 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             uint32_t rbuf[2][32];
             tmem_ld_32x32b_x32(tbase + uint32_t(c0 * 32), rbuf[0]);
             tmem_ld_wait();
+            // chunks in pairs: the register buffer index stays static while only two copies
+            // of the chunk body are inlined
+#pragma unroll 1
+            for (int cp = 0; cp < kHalfChunks; cp += 2)
 #pragma unroll
-            for (int cc = 0; cc < kHalfChunks; ++cc) {
+            for (int hf = 0; hf < 2; ++hf) {
+                const int cc = cp + hf;
+                if (cc >= kHalfChunks) break;
                 const int c = c0 + cc;
-                uint32_t (&r)[32] = rbuf[cc & 1];
+                uint32_t (&r)[32] = rbuf[hf];
                 // start the next chunk's tensor-memory load; it completes under this chunk's math
-                if (cc + 1 < kHalfChunks) tmem_ld_32x32b_x32(tbase + uint32_t((c + 1) * 32), rbuf[(cc + 1) & 1]);
+                if (cc + 1 < kHalfChunks) tmem_ld_32x32b_x32(tbase + uint32_t((c + 1) * 32), rbuf[hf ^ 1]);
                 float v[32];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
@@ -322,7 +339,34 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                         }
                     }
                 }
-                if (live) {
+                if (kTmaStore) {
+                    // 16-byte piece jj of this lane's 128-byte row sits at jj ^ (row % 8) (the TMA
+                    // 128-byte swizzle); rows past M are written but not stored (TMA clips them)
+                    uint4* stg = reinterpret_cast<uint4*>(sOut) + (warp - 2) * 32 * 8 + lane * 8;
+                    const int f = ep.fmt;
+                    if ((cc & 1) == 0) {
+                        // the previous 64-column store must have read the staging area
+                        if (lane == 0) bulk_wait_read_all();
+                        __syncwarp();
+                    }
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+                        stg[(((cc & 1) * 4 + g) ^ (lane & 7))] =
+                            make_uint4(pack16(v[g * 8], v[g * 8 + 1], f), pack16(v[g * 8 + 2], v[g * 8 + 3], f),
+                                       pack16(v[g * 8 + 4], v[g * 8 + 5], f), pack16(v[g * 8 + 6], v[g * 8 + 7], f));
+                    if (cc & 1) {
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            tma_store_2d(&tmOut, stg, (c - 1) * 32, int32_t(tile * kBlockM + q * 32));
+                            bulk_commit_group();
+                        }
+                    }
+                    if (ep.found_inf && live) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) bad |= !(fabsf(v[j]) <= vmax);
+                    }
+                } else if (live) {
                     uint4* op = reinterpret_cast<uint4*>(ep.out + m * ep.ld_out + c * 32);
                     const int f = ep.fmt;
 #pragma unroll
@@ -382,6 +426,8 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             if (lane == 0) atomicAdd(ep.r1_sum, r1_total);
         }
         if (ep.found_inf && __any_sync(0xffffffffu, bad) && lane == 0) atomicExch(ep.found_inf, 1);
+        // every bulk store of this warp has completed before the CTA may exit
+        if (kTmaStore && lane == 0) bulk_wait_all();
     }
     __syncthreads();
     if (threadIdx.x == 0 && *abort_flag) raise_flag(ep.flag, kFlagTimeout);

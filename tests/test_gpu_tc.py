@@ -60,6 +60,24 @@ def test_bf16_linear(m, k0, k1, n, relu):
     assert err < 1.5e-2 * ref.abs().max().item(), err
 
 
+def test_bf16_linear_strided_output_leaves_the_rest():
+    """Output into columns [64, 320) of a 384-wide buffer (leading dimension 384):
+    the GEMM writes exactly that block, every row of it, and nothing else."""
+    from simple_rf_gb300 import _lib
+    g = torch.Generator(device=DEV).manual_seed(2)
+    m, k, n, ld = 1234, 128, 256, 384
+    x = _bf(torch.randn(m, k, device=DEV, generator=g))
+    w = _bf(torch.randn(n, k, device=DEV, generator=g) * 0.1)
+    buf = torch.full((m, ld), 7.0, dtype=torch.bfloat16, device=DEV)
+    view = buf[:, 64:]
+    _lib.call('srf_bf16_linear', _p(view), ld, _p(x), k, k, None, 0, 0, _p(w), k, n, 0, None, m, n, 0, None, 0, None,
+              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    ref = x.float() @ w.float().T
+    err = (buf[:, 64:64 + n].float() - ref).abs().max().item()
+    assert err < 1.5e-2 * ref.abs().max().item(), err
+    assert torch.all(buf[:, :64] == 7.0) and torch.all(buf[:, 64 + n:] == 7.0)
+
+
 def test_bf16_linear_dgrad_mask_colsum():
     """The backward-data form: rows [row0, row0 + n) of a transposed weight,
     ReLU mask from a forward activation, column sums for the bias gradient."""
