@@ -48,15 +48,19 @@ def gemm(args):
     w = (torch.randn(n, k, device='cuda', generator=g) * 0.05).to(torch.bfloat16)
     b = torch.zeros(n, device='cuda')
     y = torch.empty(m, n, device='cuda', dtype=torch.bfloat16)
+    # --dgrad: the backward-data form (ReLU mask of a forward activation, column sums, no bias)
+    mask = torch.randn(m, n, device='cuda', generator=g).to(torch.bfloat16) if args.dgrad else None
+    colsum = torch.zeros(n, device='cuda') if args.dgrad else None
 
     def run():
-        _lib.call('srf_bf16_linear', _p(y), n, _p(x), k, k, None, 0, 0, _p(w), k, n, 0, _p(b), m, n, 1, None, 0, None,
-                  _st())
+        _lib.call('srf_bf16_linear', _p(y), n, _p(x), k, k, None, 0, 0, _p(w), k, n, 0, None if args.dgrad else _p(b),
+                  m, n, 0 if args.dgrad else 1, _p(mask), n if args.dgrad else 0, _p(colsum), _st())
     t = _time(run, args.reps, args.warmup)
     flops = 2.0 * m * n * k
-    nbytes = (m * k + m * n + n * k) * 2
-    return {'kernel': 'tc_gemm_kernel', 'm': m, 'k': k, 'n': n, 'ms': t * 1e3, 'tflops': flops / t / 1e12,
-            'gbs': nbytes / t / 1e9, 'bytes': nbytes}
+    nbytes = (m * k + m * n * (2 if args.dgrad else 1) + n * k) * 2
+    return {'kernel': 'tc_gemm_kernel', 'form': 'dgrad (mask + colsum)' if args.dgrad else 'forward (bias + ReLU)',
+            'm': m, 'k': k, 'n': n, 'ms': t * 1e3, 'tflops': flops / t / 1e12, 'gbs': nbytes / t / 1e9,
+            'bytes': nbytes}
 
 
 def wgrad(args):
@@ -111,6 +115,7 @@ def main(argv=None):
     ap.add_argument('--samples', type=int, default=192)
     ap.add_argument('--reps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--dgrad', action='store_true', help='gemm: backward-data epilogue (mask + column sums)')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()

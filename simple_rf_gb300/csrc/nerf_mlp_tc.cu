@@ -768,7 +768,8 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
 
 namespace {
 
-constexpr int kBasisRows = 128;  // samples (and threads) per block of the basis + encoding pass
+constexpr int kBasisRows = 128;     // samples per block of the basis + encoding pass
+constexpr int kBasisThreads = 256;  // threads per block: 32 row groups of 4 x 8 column groups of 4
 constexpr int kMaxBasis = 32;    // largest basis width (features_dimension_color) it holds in registers
 
 struct RenderLayout {
@@ -827,8 +828,8 @@ size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size
 // B = feats . Wb^T (FP32) and x = [PE(B, lf), PE(view, lv), 0...] in format fmt for
 // kBasisRows samples per block.  The block copies its feature rows into shared
 // memory with coalesced loads (row stride C + 1 words) next to Wb transposed and
-// padded to kMaxBasis columns; thread t computes rows 8 (t / 8) .. +7 times
-// columns 4 (t % 8) .. +3 (per input: 8 row reads, spread over 4 banks x 8-way
+// padded to kMaxBasis columns; thread t computes rows 4 (t / 8) .. +3 times
+// columns 4 (t % 8) .. +3 (per input: 4 row reads, spread over 4 banks x 8-way
 // broadcast, and one 128-bit weight read), then writes its PE entries into the
 // same row area re-used as the 16-bit staging, which the block stores with
 // consecutive threads on consecutive 4-byte words.
@@ -847,7 +848,7 @@ __global__ void transpose_basis_kernel(const float* __restrict__ Wb, int F, int 
     WbT[i] = o < F ? Wb[o * C + c] : 0.f;
 }
 
-__global__ void __launch_bounds__(kBasisRows)
+__global__ void __launch_bounds__(kBasisThreads)
     basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ WbT, int F,
                         const float* __restrict__ view, int64_t M, int lf, int lv, int k1p, float* B, op16* x,
                         int fmt) {
@@ -874,17 +875,17 @@ __global__ void __launch_bounds__(kBasisRows)
         }
     }
     __syncthreads();
-    const int rg = threadIdx.x >> 3, cg = threadIdx.x & 7;   // rows rg*8.., columns cg*4..
-    float acc[8][4];
+    const int rg = threadIdx.x >> 3, cg = threadIdx.x & 7;   // rows rg*4.., columns cg*4..
+    float acc[4][4];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-    const float* f0 = sF + (rg * 8) * (C + 1);
+    const float* f0 = sF + (rg * 4) * (C + 1);
     for (int c = 0; c < C; ++c) {
         const float4 wv = *reinterpret_cast<const float4*>(sWt + c * kMaxBasis + cg * 4);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < 4; ++i) {
             const float fv = f0[i * (C + 1) + c];
             acc[i][0] += fv * wv.x;
             acc[i][1] += fv * wv.y;
@@ -896,8 +897,8 @@ __global__ void __launch_bounds__(kBasisRows)
     for (int i = threadIdx.x; i < kBasisRows * stride / 2; i += blockDim.x) reinterpret_cast<uint32_t*>(srow)[i] = 0u;
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const int r = rg * 8 + i;
+    for (int i = 0; i < 4; ++i) {
+        const int r = rg * 4 + i;
         if (r >= rows) break;
         const int64_t m = row0 + r;
         op16* my = srow + r * stride;
@@ -933,7 +934,7 @@ __global__ void __launch_bounds__(kBasisRows)
     const uint32_t* src = reinterpret_cast<const uint32_t*>(srow);
     const int wx = k1p / 2, ws = stride / 2;
     uint32_t* gx = reinterpret_cast<uint32_t*>(x + row0 * k1p);
-    for (int w = threadIdx.x; w < rows * wx; w += kBasisRows) gx[w] = src[(w / wx) * ws + w % wx];
+    for (int w = threadIdx.x; w < rows * wx; w += blockDim.x) gx[w] = src[(w / wx) * ws + w % wx];
 }
 
 // Basis-layer backward fused with the PE adjoint, over a contiguous range of rows
@@ -1065,7 +1066,7 @@ int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float
     }
     transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
     if ((st = launch_status())) return st;
-    basis_encode_kernel<<<unsigned((m + kBasisRows - 1) / kBasisRows), kBasisRows, smem, s>>>(
+    basis_encode_kernel<<<unsigned((m + kBasisRows - 1) / kBasisRows), kBasisThreads, smem, s>>>(
         feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1p, w.B, w.x, fmt);
     if ((st = launch_status())) return st;
     if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
@@ -1110,7 +1111,7 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
     }
     // PE adjoint + basis layer: d_feats = dB . Wb, dWb += dB^T feats
     const int threads = (C + 31) / 32 * 32;
-    int64_t blocks = int64_t(num_sms()) * 2;
+    int64_t blocks = int64_t(num_sms()) * 4;
     int64_t per = (m + blocks - 1) / blocks;
     per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
     blocks = (m + per - 1) / per;
