@@ -783,7 +783,8 @@ struct RenderLayout {
         l1.n = U; l1.nsrc = 1; l1.padw[0] = k1p; l1.refw[0] = k1;
         l2 = LayerMap{};
         l2.n = U; l2.nsrc = 1; l2.padw[0] = U; l2.refw[0] = U;
-        ok = (U == 128 || U == 256) && C >= 1 && C <= 1024 && F >= 1 && F <= kMaxBasis && k1p <= 256 && lf >= 0 &&
+        ok = (U == 128 || U == 256) && C >= 4 && C <= 1024 && C % 4 == 0 && F >= 1 && F <= kMaxBasis && k1p <= 256 &&
+             lf >= 0 &&
              lv >= 0 && lf <= 10 && lv <= 10;
     }
 };
@@ -943,15 +944,29 @@ __global__ void __launch_bounds__(kBasisThreads)
 //                 16-bit encoded-row gradient, loss-scaled by gscale[0]; unscaled here)
 //   d_feats[m]  = dB[m] . Wb                       (written)
 //   dWb        += dB^T . feats                     (one atomic per weight per block)
-// Each tile's feature rows, dx rows and B rows are first copied into shared memory
-// with coalesced, independent loads; thread c then owns feature column c, with its
-// Wb column and its dWb accumulators in registers and the dB rows read as
-// shared-memory broadcasts.
+// The feature, dx and B rows of each tile arrive in shared memory by asynchronous
+// copies issued one tile ahead (two buffers), so the loads of tile t + 1 overlap
+// the arithmetic of tile t.  Thread c owns feature column c, with its Wb column
+// and its dWb accumulators in registers; dB rows are shared-memory broadcasts.
 constexpr int kBwdTile = 32;
 
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// shared bytes of one tile buffer: feature rows, dx rows, B rows (16-byte multiples)
+__host__ __device__ inline size_t basis_tile_bytes(int C, int F, int k1p) {
+    size_t fb = size_t(kBwdTile) * C * 4, xb = size_t(kBwdTile) * k1p * 2, bb = size_t(kBwdTile) * F * 4;
+    return fb + xb + (bb + 15) / 16 * 16;
+}
 __host__ __device__ inline size_t basis_bwd_smem(int C, int F, int k1p) {
-    return size_t(kBwdTile) * kMaxBasis * 4 + size_t(kBwdTile) * C * 4 + size_t(kBwdTile) * F * 4 +
-           size_t(kBwdTile) * k1p * 2;
+    return size_t(kBwdTile) * kMaxBasis * 4 + 2 * basis_tile_bytes(C, F, k1p);
 }
 
 __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __restrict__ B,
@@ -960,9 +975,8 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
                                  float* d_feats, float* dWb) {
     extern __shared__ __align__(16) float bb[];
     float* sdB = bb;                                   // kBwdTile x kMaxBasis
-    float* sF = sdB + kBwdTile * kMaxBasis;            // kBwdTile x C
-    float* sB = sF + kBwdTile * C;                     // kBwdTile x F
-    op16* sdx = reinterpret_cast<op16*>(sB + kBwdTile * F);   // kBwdTile x k1p
+    uint8_t* bufs = reinterpret_cast<uint8_t*>(sdB + kBwdTile * kMaxBasis);
+    const size_t tile_bytes = basis_tile_bytes(C, F, k1p);
     const float unscale = gscale ? gscale[1] : 1.f;
     const int c = threadIdx.x;
     float wcol[kMaxBasis], acc[kMaxBasis];
@@ -973,19 +987,34 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
     }
     const int64_t r_begin = int64_t(blockIdx.x) * rows_per_block;
     const int64_t r_end = r_begin + rows_per_block < M ? r_begin + rows_per_block : M;
-    for (int64_t t0 = r_begin; t0 < r_end; t0 += kBwdTile) {
-        const int nt = int(r_end - t0 < kBwdTile ? r_end - t0 : kBwdTile);
-        {   // stage the tile: contiguous rows in global memory
-            const float* gf = feats + t0 * C;
-#pragma unroll 4
-            for (int i = threadIdx.x; i < nt * C; i += blockDim.x) sF[i] = gf[i];
+    // issue the asynchronous copies of the tile at row t0 into buffer `which`
+    auto load_tile = [&](int64_t t0, int which) {
+        if (t0 < r_end) {
+            const int nt = int(r_end - t0 < kBwdTile ? r_end - t0 : kBwdTile);
+            uint8_t* base = bufs + which * tile_bytes;
+            float* sF = reinterpret_cast<float*>(base);
+            op16* sdx = reinterpret_cast<op16*>(base + size_t(kBwdTile) * C * 4);
+            float* sB = reinterpret_cast<float*>(base + size_t(kBwdTile) * C * 4 + size_t(kBwdTile) * k1p * 2);
+            const float* gf = feats + t0 * C;          // rows are contiguous: nt * C floats
+            for (int i = threadIdx.x; i < nt * C / 4; i += blockDim.x) cp_async16(sF + 4 * i, gf + 4 * i);
+            const op16* gx = dx + t0 * k1p;
+            for (int i = threadIdx.x; i < nt * k1p / 8; i += blockDim.x) cp_async16(sdx + 8 * i, gx + 8 * i);
             const float* gb = B + t0 * F;
-            for (int i = threadIdx.x; i < nt * F; i += blockDim.x) sB[i] = gb[i];
-            const uint4* gx = reinterpret_cast<const uint4*>(dx + t0 * k1p);
-            uint4* sx = reinterpret_cast<uint4*>(sdx);
-            for (int i = threadIdx.x; i < nt * k1p / 8; i += blockDim.x) sx[i] = gx[i];
+            for (int i = threadIdx.x; i < nt * F; i += blockDim.x) cp_async4(sB + i, gb + i);
         }
+        cp_async_commit();
+    };
+    load_tile(r_begin, 0);
+    int buf = 0;
+    for (int64_t t0 = r_begin; t0 < r_end; t0 += kBwdTile, buf ^= 1) {
+        const int nt = int(r_end - t0 < kBwdTile ? r_end - t0 : kBwdTile);
+        load_tile(t0 + kBwdTile, buf ^ 1);   // the next tile streams in under this one
+        cp_async_wait_one();
         __syncthreads();
+        uint8_t* base = bufs + buf * tile_bytes;
+        const float* sF = reinterpret_cast<const float*>(base);
+        const op16* sdx = reinterpret_cast<const op16*>(base + size_t(kBwdTile) * C * 4);
+        const float* sB = reinterpret_cast<const float*>(base + size_t(kBwdTile) * C * 4 + size_t(kBwdTile) * k1p * 2);
         for (int i = threadIdx.x; i < kBwdTile * kMaxBasis; i += blockDim.x) {
             const int rr = i / kMaxBasis, o = i - rr * kMaxBasis;
             float g = 0.f;
@@ -996,12 +1025,12 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
                     const float2 f = tc::unpack16(w, fmt);
                     return (col & 1) ? f.y : f.x;
                 };
-                const float b = sB[rr * F + o];
+                const float bo = sB[rr * F + o];
                 g = rd(o);
                 for (int k = 0; k < lf; ++k) {
                     const float fk = float(1 << k);
                     float sn, cs;
-                    sincosf(b * fk, &sn, &cs);
+                    sincosf(bo * fk, &sn, &cs);
                     g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
                 }
                 g *= unscale;
@@ -1025,8 +1054,9 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
                 d_feats[(t0 + rr) * C + c] = dfe;
             }
         }
-        __syncthreads();
+        __syncthreads();   // buffer `buf` and sdB are rewritten next round
     }
+    cp_async_wait_all();
     if (c < C) {
 #pragma unroll
         for (int o = 0; o < kMaxBasis; ++o)
@@ -1111,7 +1141,7 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
     }
     // PE adjoint + basis layer: d_feats = dB . Wb, dWb += dB^T feats
     const int threads = (C + 31) / 32 * 32;
-    int64_t blocks = int64_t(num_sms()) * 4;
+    int64_t blocks = int64_t(num_sms()) * 3;
     int64_t per = (m + blocks - 1) / blocks;
     per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
     blocks = (m + per - 1) / per;
