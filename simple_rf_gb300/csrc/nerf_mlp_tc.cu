@@ -94,7 +94,10 @@ int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
 template <int BN>
 int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
                    tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
-    if (ep.mask || ep.colsum || ep.r1_row) return launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s);
+    if (ep.mask || ep.mask_bits || ep.colsum || ep.r1_row) {
+        if (ep.bits_out) return SRF_ERR_UNSUPPORTED;   // ReLU bits come from forward (4-warp) epilogues only
+        return launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s);
+    }
     return launch_gemm_ew<BN, 4>(a0, a1, b, out, sh, ep, s);
 }
 
@@ -501,6 +504,7 @@ struct TcLayout {
 struct TcWs {
     op16* enc; op16* vext;
     std::vector<op16*> h, hv;
+    std::vector<uint32_t*> hbits;   // ReLU bits of h[j] for the backward-data masks (backward only)
     op16* feat;
     float* sraw; float* rgb;
     std::vector<op16*> W, WT, Wv, WTv;
@@ -546,6 +550,7 @@ size_t carve_tc(const MlpLayout& L, const TcLayout& T, int64_t m, bool bwd, void
     }
     int wmax = L.Wp > L.Wv ? L.Wp : L.Wv;
     if (bwd) {
+        for (int j = 0; j + 1 < L.Dp; ++j) w.hbits.push_back(c.take<uint32_t>(size_t(m) * (L.Wp / 32)));
         w.dz0 = c.take<op16>(size_t(m) * wmax);
         w.dz1 = c.take<op16>(size_t(m) * wmax);
         w.dfeat = L.vdep ? c.take<op16>(size_t(m) * L.Wp) : nullptr;
@@ -625,6 +630,10 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
         const op16* x1 = lm.nsrc > 1 ? w.h[j - 1] : nullptr;
         tc::GemmEpilogue ep = make_epilogue(w.h[j], L.Wp, P[L.idx_trunk_w(j) + 1], 1, fmt, cx.found_inf());
+        if (bwd && j + 1 < L.Dp) {   // the backward-data pass of layer j + 1 masks with these bits
+            ep.bits_out = w.hbits[j];
+            ep.ld_bits = L.Wp / 32;
+        }
         if (j == L.Dp - 1) {
             // sigma head (and, without view dependence, the rgb head) on the last trunk layer's rows
             ep.head_mode = L.vdep ? tc::kHeadSigma : tc::kHeadSigmaRgb;
@@ -744,8 +753,8 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         if (j == 0) break;
         int row0 = lm.nsrc > 1 ? lm.padw[0] : 0;
         tc::GemmEpilogue ep = bwd_epilogue(dz2, L.Wp);
-        ep.mask = w.h[j - 1];
-        ep.ld_mask = L.Wp;
+        ep.mask_bits = w.hbits[j - 1];
+        ep.ld_bits = L.Wp / 32;
         ep.colsum = G[L.idx_trunk_w(j - 1) + 1];
         st = tc_linear(ep, dz, L.Wp, L.Wp, nullptr, 0, 0, w.WT[j], L.Wp, lm.kpad(), row0, m, L.Wp, s);
         if (st) return st;

@@ -38,6 +38,12 @@ struct GemmEpilogue {
     int fmt;                        // operand / output format (kFmtBF16, kFmtF16)
     const uint16_t* mask;           // multiply by (mask[m, n] > 0) when non-NULL
     int64_t ld_mask;
+    // ReLU masks as bits, 32 columns per word: bits_out[m, c] gets bit j set where
+    // stored column 32c + j is > 0 (written when non-NULL); mask_bits multiplies the
+    // result by those bits (the 1-bit form of `mask`, 16x fewer bytes to read)
+    uint32_t* bits_out;
+    const uint32_t* mask_bits;
+    int64_t ld_bits;                // words per row of both
     const float* r1_row;            // result += r1[m] * r1_col[n] (before ReLU/mask) when non-NULL, where
     const float* r1_col;            // r1[m] = r1_row[m], or 0 when r1_gate is given and r1_gate[m] <= 0
     const float* r1_gate;
@@ -99,10 +105,13 @@ struct SmemPlan {
     static constexpr uint32_t kBBlockBytes = BN * kBlockK * 2;
     static constexpr uint32_t kStoreBytes = tma_store_ok(BN, EW) ? uint32_t(EW) * 32 * 128 : 0u;
     // partial head sums handed between the two warps of a lane quadrant: [2 acc][128 rows][4]
-    static constexpr uint32_t kHeadXBytes = 2 * 128 * 4 * 4;
+    static constexpr uint32_t kHeadXBytes = EW == 8 ? 2 * 128 * 4 * 4 : 0u;
+    // ReLU bits of one tile (forward, 4 epilogue warps): [4 warps][32 rows][BN / 32 words]
+    static constexpr uint32_t kBitsBytes = EW == 4 ? 4u * 32 * (BN / 32) * 4 : 0u;
     // 1024 B alignment slack + 256 B of barriers + BN floats each of bias, column
     // sums and r1 mask column sums + 4 x BN head weights + 4 head biases + head exchange
-    static constexpr size_t kReserve = 1024 + 256 + BN * 12 + 4 * BN * 4 + 16 + kHeadXBytes + kStoreBytes;
+    static constexpr size_t kReserve =
+        1024 + 256 + BN * 12 + 4 * BN * 4 + 16 + kHeadXBytes + kStoreBytes + kBitsBytes;
     static __host__ __device__ int stages(int kb_total) {
         size_t b = size_t(kb_total) * kBBlockBytes;
         if (b + kReserve + 2 * kATileBytes > kMaxSmem) return 0;
@@ -144,7 +153,8 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
     float* scol2 = scol + BN;                              // BN floats
     float* shw = scol2 + BN;                               // 4 x BN floats
     float* shb = shw + 4 * BN;                             // 4 floats
-    float* shx = shb + 4;                                  // [2][128][4] partial head sums
+    float* shx = shb + 4;                                  // [2][128][4] partial head sums (8 epilogue warps)
+    uint32_t* sbits = reinterpret_cast<uint32_t*>(shx + Plan::kHeadXBytes / 4);   // ReLU bits (4 epilogue warps)
     const int hunits = head_units(ep.head_mode);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -302,6 +312,18 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                     if (ep.relu) v[j] = v[j] > 0.f ? v[j] : 0.f;
                     if (!live) v[j] = 0.f;
                 }
+                if (ep.mask_bits) {   // kernel-uniform branch
+                    const uint32_t mb = live ? ep.mask_bits[m * ep.ld_bits + c] : 0u;
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        if (!((mb >> j) & 1u)) v[j] = 0.f;
+                }
+                if (EW == 4 && ep.bits_out) {   // staged per warp, stored after the tile's last chunk
+                    uint32_t mb = 0u;
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) mb |= uint32_t(v[j] > 0.f) << j;
+                    sbits[((warp - 2) * 32 + lane) * kHalfChunks + cc] = mb;
+                }
                 if (ep.mask) {   // kernel-uniform branch; rows past M contribute zeros
                     float mw[32];
 #pragma unroll
@@ -381,6 +403,22 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                 }
                 if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
                 tmem_ld_wait();
+            }
+            if (EW == 4 && ep.bits_out) {
+                // this warp's 32 rows x kHalfChunks words (whole rows: one warp covers BN)
+                __syncwarp();
+                const uint32_t* wb = sbits + (warp - 2) * 32 * kHalfChunks;
+                if (ep.ld_bits == kHalfChunks && (kHalfChunks % 4) == 0) {
+                    // the 32 rows are contiguous in bits_out: consecutive lanes store consecutive 16 bytes
+                    const int64_t row0 = tile * kBlockM + q * 32;
+                    uint4* dst = reinterpret_cast<uint4*>(ep.bits_out + row0 * ep.ld_bits);
+                    const uint4* src = reinterpret_cast<const uint4*>(wb);
+                    for (int i = lane; i < 32 * kHalfChunks / 4; i += 32)
+                        if (row0 + (i * 4) / kHalfChunks < shape.M) dst[i] = src[i];
+                } else if (live) {
+                    for (int k = 0; k < kHalfChunks; ++k) ep.bits_out[m * ep.ld_bits + c0 + k] = wb[lane * kHalfChunks + k];
+                }
+                __syncwarp();
             }
             if (EW == 8 && hunits) {   // kernel-uniform: half 1 hands its partial dot products to half 0
                 // The slot of accumulator `acc` is rewritten two tiles later, only after this
