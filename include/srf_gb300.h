@@ -266,6 +266,18 @@ int srf_vm_color_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pt
 int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
                           int64_t n_pts, const float* d_features, void* stream);
 
+/* CP decomposition (CpDecomposedTensor, src/models/SimpleTensoRF09.py:964-1123): only
+ * grid->lines are used (planes ignored), line i along world axis vector_axes[i] =
+ * (2, 1, 0)[i], channels-last (L_i, R) with the same R for all three.  Density
+ * features out[p] = sum_r prod_i line_i[r] (:1070-1080); colour features (P, R):
+ * prod_i line_i[r] (:1091-1098).  The backward adds into grad_grid's lines. */
+int srf_cp_density_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features, void* stream);
+int srf_cp_density_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts, int64_t n_pts,
+                            const float* d_features, void* stream);
+int srf_cp_color_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features, void* stream);
+int srf_cp_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts, int64_t n_pts,
+                          const float* d_features, void* stream);
+
 /* Sample validity for TensoRF: inside the bbox and (when alpha_volume != NULL)
  * alpha-mask trilinear value > 0; writes normalised points and a 0/1 mask.
  * Replaces LowRankTensor.forward:705-710 + AlphaGridMask.sample_alpha

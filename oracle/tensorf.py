@@ -129,6 +129,18 @@ def vm_density(planes, lines, pn):
     return acc
 
 
+def cp_lines(lines, pn):
+    """Line i of a CP decomposition at coordinate pn[:, VECTOR_AXES[i]] -> list of (R, P)
+    (CpDecomposedTensor.get_volume_density / get_color lookups, SimpleTensoRF09.py:1070-1078)."""
+    return [grid_sample_2d(lines[i], np.zeros_like(pn[:, VECTOR_AXES[i]]), pn[:, VECTOR_AXES[i]]) for i in range(3)]
+
+
+def cp_density(lines, pn):
+    """sum_r line_0[r] line_1[r] line_2[r] (SimpleTensoRF09.py:1075-1079) before the predictor."""
+    l0, l1, l2 = cp_lines(lines, pn)
+    return np.sum(l0 * l1 * l2, 0)
+
+
 class RendererSpec:
     """MlpFeaturesColorPredictor (SimpleTensoRF09.py:1370-1394)."""
 
@@ -210,7 +222,11 @@ def tensorf_forward(tp, spec, rays_o, rays_d, z, *, alpha_vol=None, alpha_bbox=N
         valid = vm.reshape(n, s)
     pn = normalize_points(pts, bbox).reshape(-1, 3)
     vflat = np.nonzero(valid.reshape(-1))[0]
-    sig_feat = vm_density(tp['planes_density'], tp['lines_density'], pn[vflat])
+    cp = 'planes_density' not in tp   # CP decomposition: lines only (SimpleTensoRF09.py:964-1123)
+    if cp:
+        sig_feat = cp_density(tp['lines_density'], pn[vflat])
+    else:
+        sig_feat = vm_density(tp['planes_density'], tp['lines_density'], pn[vflat])
     if density == 'relu':
         sig_v = relu(sig_feat)
     else:
@@ -223,8 +239,12 @@ def tensorf_forward(tp, spec, rays_o, rays_d, z, *, alpha_vol=None, alpha_bbox=N
     out, cc = composite_forward(sigma, rgb0, z, rays_d, distance_scale=distance_scale)
     surf = out['weights'] > dt(weight_threshold)
     sflat = np.nonzero(surf.reshape(-1))[0]
-    feats = vm_features(tp['planes_color'], tp['lines_color'], pn[sflat])
-    f144 = np.concatenate([(pc * lc) for pc, lc in feats], 0).T
+    if cp:
+        feats = cp_lines(tp['lines_color'], pn[sflat])
+        f144 = (feats[0] * feats[1] * feats[2]).T
+    else:
+        feats = vm_features(tp['planes_color'], tp['lines_color'], pn[sflat])
+        f144 = np.concatenate([(pc * lc) for pc, lc in feats], 0).T
     vd = np.repeat(rays_d / np.sqrt(np.sum(rays_d * rays_d, -1, keepdims=True)), s, axis=0)[sflat]
     rgb_s, rc = renderer_forward(tp, spec, f144, vd)
     rgb = np.zeros((n * s, 3), dtype=rays_o.dtype)
@@ -240,7 +260,7 @@ def tensorf_forward(tp, spec, rays_o, rays_d, z, *, alpha_vol=None, alpha_bbox=N
     cc['rgb'] = rgb
     cc['white_bkgd'] = white
     cache = dict(cc=cc, pn=pn, vflat=vflat, sflat=sflat, sig_feat=sig_feat, feats=feats, rc=rc,
-                 density=density, density_offset=density_offset, n=n, s=s)
+                 density=density, density_offset=density_offset, n=n, s=s, cp=cp)
     return out, cache
 
 
@@ -255,15 +275,23 @@ def tensorf_backward(tp, spec, cache, g):
     drgb_s = drgb.reshape(-1, 3)[sflat]
     gr, df144 = renderer_backward(tp, spec, cache['rc'], drgb_s)
     grads.update(gr)
+    pp = pn[sflat]
+    if cache['cp']:
+        ls = cache['feats']
+        d = df144.T
+        for i in range(3):
+            v = VECTOR_AXES[i]
+            others = ls[(i + 1) % 3] * ls[(i + 2) % 3]
+            grads[f'lines_color.{i}'] = grid_sample_2d_backward(tp['lines_color'][i].shape, np.zeros_like(pp[:, v]),
+                                                                pp[:, v], d * others, dt)
     off = 0
-    for i in range(3):
+    for i in range(0 if cache['cp'] else 3):
         m0, m1 = MATRIX_AXES[i]
         v = VECTOR_AXES[i]
         pc, lc = cache['feats'][i]
         r = pc.shape[0]
         d = df144[:, off:off + r].T
         off += r
-        pp = pn[sflat]
         grads[f'planes_color.{i}'] = grid_sample_2d_backward(tp['planes_color'][i].shape, pp[:, m0], pp[:, m1], d * lc, dt)
         grads[f'lines_color.{i}'] = grid_sample_2d_backward(tp['lines_color'][i].shape, np.zeros_like(pp[:, v]), pp[:, v], d * pc, dt)
     ds = dsig.reshape(-1)[vflat]
@@ -274,6 +302,15 @@ def tensorf_backward(tp, spec, cache, g):
         xx = sf + dt(cache['density_offset'])
         dfeat = ds * sigmoid(xx)
     pv = pn[vflat]
+    if cache['cp']:
+        ls = cp_lines(tp['lines_density'], pv)
+        for i in range(3):
+            v = VECTOR_AXES[i]
+            others = ls[(i + 1) % 3] * ls[(i + 2) % 3]
+            grads[f'lines_density.{i}'] = grid_sample_2d_backward(tp['lines_density'][i].shape,
+                                                                  np.zeros_like(pv[:, v]), pv[:, v],
+                                                                  dfeat[None, :] * others, dt)
+        return grads
     feats = vm_features(tp['planes_density'], tp['lines_density'], pv)
     for i in range(3):
         m0, m1 = MATRIX_AXES[i]

@@ -89,6 +89,10 @@ _SIGS = {
     'srf_vm_density_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_vm_color_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_vm_color_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_cp_density_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_cp_density_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_cp_color_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_cp_color_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_tensorf_sample_mask': (c_int, [P, P, P, c_int, c_int, FP, P, c_int, c_int, c_int, FP, P, P, P]),
     'srf_alpha_mask_query': (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
     'srf_compact_workspace_size': (c_size_t, [c_int64]),

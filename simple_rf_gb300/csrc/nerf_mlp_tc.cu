@@ -89,15 +89,16 @@ int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
     return launch_status();
 }
 
-// Backward epilogues (ReLU mask, column sums, the sigma-head adjoint) carry enough
-// per-element work to keep 8 epilogue warps busy; forward epilogues run on 4.
+// 8 epilogue warps (two per tensor-memory lane quadrant) keep the TMA-store epilogue
+// ahead of the memory system; they need two more 4 KB staging areas, so layers whose
+// resident weights leave fewer than two activation stages (K = 320 at N = 256) and the
+// 64-wide layers (32 columns per warp: no 64-column TMA boxes) run on 4.
 template <int BN>
 int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
                    tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
-    if (ep.mask || ep.mask_bits || ep.colsum || ep.r1_row) {
-        if (ep.bits_out) return SRF_ERR_UNSUPPORTED;   // ReLU bits come from forward (4-warp) epilogues only
-        return launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s);
-    }
+    const int kb = sh.kb0 + sh.kb1;
+    const bool eight = BN >= 128 && tc::SmemPlan<BN, 8>::stages(kb) >= 2;
+    if (eight) return launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s);
     return launch_gemm_ew<BN, 4>(a0, a1, b, out, sh, ep, s);
 }
 

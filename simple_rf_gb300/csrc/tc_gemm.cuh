@@ -293,8 +293,11 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             tmem_ld_32x32b_x32(tbase + uint32_t(c0 * 32), rbuf[0]);
             tmem_ld_wait();
             // chunks in pairs: the register buffer index stays static while only two copies
-            // of the chunk body are inlined
-#pragma unroll 1
+            // of the chunk body are inlined (8 warps: every chunk unrolled, at most 4, so
+            // the ReLU bits of the row stay in registers)
+            constexpr int kPairUnroll = EW == 8 ? (kHalfChunks + 1) / 2 : 1;
+            uint32_t rbits[EW == 8 ? kHalfChunks : 1];
+#pragma unroll kPairUnroll
             for (int cp = 0; cp < kHalfChunks; cp += 2)
 #pragma unroll
             for (int hf = 0; hf < 2; ++hf) {
@@ -318,11 +321,12 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                     for (int j = 0; j < 32; ++j)
                         if (!((mb >> j) & 1u)) v[j] = 0.f;
                 }
-                if (EW == 4 && ep.bits_out) {   // staged per warp, stored after the tile's last chunk
+                if (ep.bits_out) {   // stored after the tile's last chunk
                     uint32_t mb = 0u;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) mb |= uint32_t(v[j] > 0.f) << j;
-                    sbits[((warp - 2) * 32 + lane) * kHalfChunks + cc] = mb;
+                    if (EW == 8) rbits[cc] = mb;
+                    else sbits[((warp - 2) * 32 + lane) * kHalfChunks + cc] = mb;
                 }
                 if (ep.mask) {   // kernel-uniform branch; rows past M contribute zeros
                     float mw[32];
@@ -419,6 +423,18 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                     for (int k = 0; k < kHalfChunks; ++k) ep.bits_out[m * ep.ld_bits + c0 + k] = wb[lane * kHalfChunks + k];
                 }
                 __syncwarp();
+            }
+            if (EW == 8 && ep.bits_out && live) {
+                // this warp's kHalfChunks words of the row (words c0 .. c0 + kHalfChunks - 1)
+                uint32_t* dst = ep.bits_out + m * ep.ld_bits + c0;
+                if (kHalfChunks == 4 && (ep.ld_bits % 4) == 0) {
+                    *reinterpret_cast<uint4*>(dst) = make_uint4(rbits[0], rbits[kHalfChunks > 1 ? 1 : 0],
+                                                                rbits[kHalfChunks > 2 ? 2 : 0],
+                                                                rbits[kHalfChunks > 3 ? 3 : 0]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kHalfChunks; ++k) dst[k] = rbits[k];
+                }
             }
             if (EW == 8 && hunits) {   // kernel-uniform: half 1 hands its partial dot products to half 0
                 // The slot of accumulator `acc` is rewritten two tiles later, only after this

@@ -333,6 +333,63 @@ int launch_grouped(int G, int64_t n, F&& launch) {
     }
 }
 
+// CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123): three lines,
+// line i along world axis kVectorAxes[i], all with the same R components;
+// density = sum_r prod_i line_i[r], colour features = prod_i line_i[r] per r.
+__device__ __forceinline__ void cp_taps(const srf_vm_grid& g, const float* p, Taps (&t)[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) t[i] = line_taps(p[kVectorAxes[i]], g.res[kVectorAxes[i]]);
+}
+
+__device__ __forceinline__ float line_value(const float* __restrict__ line, int R, int r, const Taps& t) {
+    float v = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        if (t.idx[c] >= 0) v += line[int64_t(t.idx[c]) * R + r] * t.w[c];
+    return v;
+}
+
+__global__ void cp_fwd_kernel(srf_vm_grid g, const float* __restrict__ pts, int64_t n, int per_component,
+                              float* out) {
+    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    Taps t[3];
+    cp_taps(g, pts + 3 * p, t);
+    const int R = g.n_comp[0];
+    float acc = 0.f;
+    for (int r = 0; r < R; ++r) {
+        const float v = line_value(g.lines[0], R, r, t[0]) * line_value(g.lines[1], R, r, t[1]) *
+                        line_value(g.lines[2], R, r, t[2]);
+        if (per_component) out[p * R + r] = v;
+        else acc += v;
+    }
+    if (!per_component) out[p] = acc;
+}
+
+// d line_i[r] at its taps += w * d_r * prod_{j != i} line_j[r]
+__global__ void cp_bwd_kernel(srf_vm_grid gg, srf_vm_grid g, const float* __restrict__ pts, int64_t n,
+                              const float* __restrict__ dfeat, int per_component) {
+    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    Taps t[3];
+    cp_taps(g, pts + 3 * p, t);
+    const int R = g.n_comp[0];
+    for (int r = 0; r < R; ++r) {
+        const float d = per_component ? dfeat[p * R + r] : dfeat[p];
+        if (d == 0.f) continue;
+        const float v[3] = {line_value(g.lines[0], R, r, t[0]), line_value(g.lines[1], R, r, t[1]),
+                            line_value(g.lines[2], R, r, t[2])};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float di = d * v[(i + 1) % 3] * v[(i + 2) % 3];
+            if (di == 0.f) continue;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (t[i].idx[c] >= 0) atomicAdd(gg.lines[i] + int64_t(t[i].idx[c]) * R + r, di * t[i].w[c]);
+        }
+    }
+}
+
 // AlphaGridMask.sample_alpha + "> 0": true iff an occupied in-bound corner has a
 // positive trilinear weight (all terms are >= 0, so the float sum is positive
 // exactly then).  Weights use torch's CPU 3-D formula ((x1 - ix) * (y1 - iy) * ...).
@@ -797,4 +854,62 @@ extern "C" int srf_density_activation_backward(float* d_features, const float* d
     density_act_bwd_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(d_features, d_sigma_dense, features, idx,
                                                                           count_dev, n, mode, offset);
     return launch_status();
+}
+
+// ---------------------------------------------------------------- CP lines --
+
+static int check_cp_grid(const srf_vm_grid* g) {
+    if (!g) return SRF_ERR_NULL;
+    for (int i = 0; i < 3; ++i) {
+        if (!g->lines[i]) return SRF_ERR_NULL;
+        if (g->res[i] < 1 || g->n_comp[i] != g->n_comp[0] || g->n_comp[0] < 1 || g->n_comp[0] > 1024)
+            return SRF_ERR_SHAPE;
+    }
+    return SRF_OK;
+}
+
+static int cp_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features, int per_component,
+                      void* stream) {
+    int st = check_cp_grid(grid);
+    if (st) return st;
+    if (n_pts < 0) return SRF_ERR_SHAPE;
+    if (n_pts == 0) return SRF_OK;
+    if (!pts || !features) return SRF_ERR_NULL;
+    cp_fwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, per_component, features);
+    return launch_status();
+}
+
+static int cp_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts, int64_t n_pts,
+                       const float* d_features, int per_component, void* stream) {
+    int st = check_cp_grid(grid);
+    if (st) return st;
+    if ((st = check_cp_grid(grad_grid))) return st;
+    for (int i = 0; i < 3; ++i)
+        if (grad_grid->n_comp[i] != grid->n_comp[i] || grad_grid->res[i] != grid->res[i]) return SRF_ERR_SHAPE;
+    if (n_pts < 0) return SRF_ERR_SHAPE;
+    if (n_pts == 0) return SRF_OK;
+    if (!pts || !d_features) return SRF_ERR_NULL;
+    cp_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features,
+                                                                   per_component);
+    return launch_status();
+}
+
+extern "C" int srf_cp_density_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features,
+                                      void* stream) {
+    return cp_forward(grid, pts, n_pts, features, 0, stream);
+}
+
+extern "C" int srf_cp_density_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                       int64_t n_pts, const float* d_features, void* stream) {
+    return cp_backward(grad_grid, grid, pts, n_pts, d_features, 0, stream);
+}
+
+extern "C" int srf_cp_color_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pts, float* features,
+                                    void* stream) {
+    return cp_forward(grid, pts, n_pts, features, 1, stream);
+}
+
+extern "C" int srf_cp_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                     int64_t n_pts, const float* d_features, void* stream) {
+    return cp_backward(grad_grid, grid, pts, n_pts, d_features, 1, stream);
 }

@@ -109,6 +109,53 @@ def vm_color(grid, pts):
     return _VmFunction.apply('color', grid.res, pts.contiguous(), *grid.tensors())
 
 
+def _cp_struct(res, lines):
+    g = _lib.VmGrid()
+    for i in range(3):
+        g.res[i] = res[i]
+        g.n_comp[i] = lines[i].shape[1]
+        if not _is_cl(lines[i]) or lines[i].dtype != torch.float32 or not lines[i].is_cuda:
+            raise RuntimeError('CP lines must be channels_last float32 CUDA tensors')
+        g.lines[i] = lines[i].data_ptr()
+    return g
+
+
+class _CpFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, kind, res, pts, *lines):
+        g = _cp_struct(res, lines)
+        p = pts.shape[0]
+        _require(pts, 'pts', (p, 3))
+        if kind == 'density':
+            out = torch.empty(p, device=pts.device)
+            call('srf_cp_density_forward', ctypes.byref(g), _ptr(pts), p, _ptr(out), _stream())
+        else:
+            out = torch.empty(p, lines[0].shape[1], device=pts.device)
+            call('srf_cp_color_forward', ctypes.byref(g), _ptr(pts), p, _ptr(out), _stream())
+        ctx.kind, ctx.res = kind, res
+        ctx.save_for_backward(pts, *lines)
+        return out
+
+    @staticmethod
+    def backward(ctx, dout):
+        pts, *lines = ctx.saved_tensors
+        grads = [torch.zeros_like(x) for x in lines]
+        g, gg = _cp_struct(ctx.res, lines), _cp_struct(ctx.res, grads)
+        name = 'srf_cp_density_backward' if ctx.kind == 'density' else 'srf_cp_color_backward'
+        call(name, ctypes.byref(gg), ctypes.byref(g), _ptr(pts), pts.shape[0], _ptr(dout.contiguous()), _stream())
+        return (None, None, None) + tuple(grads)
+
+
+def cp_density(lines, res, pts):
+    """CP density features sum_r prod_i line_i[r] (SimpleTensoRF09.py:1070-1080)."""
+    return _CpFunction.apply('density', [int(r) for r in res], pts.contiguous(), *lines)
+
+
+def cp_color(lines, res, pts):
+    """CP colour features (P, R) = prod_i line_i[r] (SimpleTensoRF09.py:1091-1098)."""
+    return _CpFunction.apply('color', [int(r) for r in res], pts.contiguous(), *lines)
+
+
 def alpha_mask_query(volume, pts_norm):
     """AlphaGridMask.sample_alpha(...) > 0 on normalised points (SimpleTensoRF09.py:1342-1349)."""
     vol = volume.reshape(volume.shape[-3:]).contiguous()

@@ -14,7 +14,8 @@ Training-time maintenance (alpha-mask rebuild, bbox shrink, grid upsampling,
 optimizer surgery; SimpleTensoRF09.py:821-944) runs every few thousand
 iterations and is written with torch tensor ops on the channels-last views,
 with the dense density evaluation on the VM density kernel.  The CP
-decomposition (``CpDecomposedTensor``) raises NotImplementedError.
+decomposition (``CpDecomposedTensor``, SimpleTensoRF09.py:964-1123) is
+``GbCpTensor``: three lines per density/colour tensor on the CP lookup kernels.
 """
 import numpy
 import torch
@@ -98,10 +99,13 @@ class MlpFeaturesColorPredictor(torch.nn.Module):
 class GbVmTensor(torch.nn.Module):
     """LowRankTensor + VmDecomposedTensor (SimpleTensoRF09.py:582-961, 1126-1320)."""
 
+    DECOMPOSITION = 'VectorMatrix'
+
     def __init__(self, name, configs, tensor_configs, model_configs):
         super().__init__()
-        if tensor_configs['decomposition_type'] != 'VectorMatrix':
-            raise NotImplementedError('only the VectorMatrix decomposition runs on the srf_gb300 kernels')
+        if tensor_configs['decomposition_type'] != self.DECOMPOSITION:
+            raise ValueError(f"{type(self).__name__} is the {self.DECOMPOSITION} decomposition, configs ask for "
+                             f"{tensor_configs['decomposition_type']} (use make_tensor_model)")
         if tensor_configs.get('predict_visibility', False):
             raise NotImplementedError('predict_visibility is not supported')
         self.name = name
@@ -118,10 +122,7 @@ class GbVmTensor(torch.nn.Module):
         self.update_tensor_params(compute_resolution_in_voxels(tensor_configs['num_voxels_initial'], bbox), bbox)
         self.alpha_mask = None
         self.optimizers = None
-        self.matrices_density, self.vectors_density = self.create_decomposed_tensor(
-            tensor_configs['num_components_density'], self.resolution)
-        self.matrices_color, self.vectors_color = self.create_decomposed_tensor(
-            tensor_configs['num_components_color'], self.resolution)
+        self.build_tensor()
         self.basis_matrix_color = torch.nn.Linear(sum(tensor_configs['num_components_color']),
                                                   tensor_configs['features_dimension_color'], bias=False)
         self.density_mode = {'ReLU': 0, 'SoftPlus': 1}[tensor_configs['density_predictor']]
@@ -145,6 +146,25 @@ class GbVmTensor(torch.nn.Module):
         self.step_size = torch.mean(self.voxel_length) * nvps
         n = (torch.linalg.norm(self.resolution.float()) / nvps).round().long()
         self.num_samples = torch.clamp(n, max=int(self.tensor_configs['num_samples_max']))
+
+    def build_tensor(self):
+        """VmDecomposedTensor.build_tensor (:1140-1152): density and colour planes + lines."""
+        tc = self.tensor_configs
+        self.matrices_density, self.vectors_density = self.create_decomposed_tensor(tc['num_components_density'],
+                                                                                    self.resolution)
+        self.matrices_color, self.vectors_color = self.create_decomposed_tensor(tc['num_components_color'],
+                                                                                self.resolution)
+
+    def density_features(self, pts):
+        return T.vm_density(self._grid('density'), pts)
+
+    def color_features(self, pts):
+        return T.vm_color(self._grid('color'), pts)
+
+    def tensor_parameters(self):
+        """The grid parameters in the reference's optimizer order (:1167-1194)."""
+        return list(self.vectors_density) + list(self.matrices_density) + list(self.vectors_color) + \
+            list(self.matrices_color)
 
     def create_decomposed_tensor(self, num_components, resolution, scale=0.1):
         """Planes (1,R,res[m1],res[m0]) and lines (1,R,res[v],1), stored channels-last."""
@@ -170,10 +190,7 @@ class GbVmTensor(torch.nn.Module):
         """SimpleTensoRF09.py:1167-1194."""
         tensor_params = torch.nn.ParameterList()
         network_params = torch.nn.ParameterList()
-        tensor_params.extend(self.vectors_density)
-        tensor_params.extend(self.matrices_density)
-        tensor_params.extend(self.vectors_color)
-        tensor_params.extend(self.matrices_color)
+        tensor_params.extend(self.tensor_parameters())
         network_params.extend(self.basis_matrix_color.parameters())
         network_params.extend(self.color_predictor.parameters())
         return [{'name': f'{self.name}_tensor_params', 'params': tensor_params,
@@ -206,7 +223,7 @@ class GbVmTensor(torch.nn.Module):
         idx_v, cnt_v = T.compact(mask)
         nv = int(cnt_v.item())
         pv = T.gather_rows(pn, idx_v, cnt_v, nv)
-        feat = T.vm_density(self._grid('density'), pv) if nv else torch.zeros(0, device=dev)
+        feat = self.density_features(pv) if nv else torch.zeros(0, device=dev)
         sigma = T.density_activation(feat, idx_v, cnt_v, rows, self.density_mode, self.density_offset).view(n, s)
         flags = _lib.SRF_COMPOSITE_NDC if self.ndc else 0
         zero_rgb = torch.zeros(n, s, 3, device=dev)
@@ -227,7 +244,7 @@ class GbVmTensor(torch.nn.Module):
         self.last_sample_counts = {'marched': rows, 'valid': nv, 'surface': ns}
         if ns:
             ps = T.gather_rows(pn, idx_s, cnt_s, ns)
-            feats = T.vm_color(self._grid('color'), ps)
+            feats = self.color_features(ps)
             view_s = None
             if self.tensor_configs['view_dependent_color']:
                 view_s = T.gather_rows(input_dict['view_dirs'].contiguous().float(), idx_s, cnt_s, ns, s)
@@ -281,9 +298,11 @@ class GbVmTensor(torch.nn.Module):
     def upsample_model_resolution(self, iter_num):
         res = compute_resolution_in_voxels(self.get_new_num_voxels(iter_num), self.bounding_box)
         self.update_tensor_params(res, self.bounding_box)
-        self.matrices_density, self.vectors_density = self.resize(self.matrices_density, self.vectors_density,
-                                                                  self.resolution)
-        self.matrices_color, self.vectors_color = self.resize(self.matrices_color, self.vectors_color, self.resolution)
+        self.resample_tensor(self.resolution)
+
+    def resample_tensor(self, res):
+        self.matrices_density, self.vectors_density = self.resize(self.matrices_density, self.vectors_density, res)
+        self.matrices_color, self.vectors_color = self.resize(self.matrices_color, self.vectors_color, res)
 
     def resize(self, mats, vecs, res):
         """Bilinear (align_corners) resampling of planes and lines to a new resolution (:1284-1301)."""
@@ -306,8 +325,7 @@ class GbVmTensor(torch.nn.Module):
             keep = (self.alpha_mask.sample_alpha(xyz) > 0).to(torch.uint8)
         idx, cnt = T.compact(keep)
         nv = int(cnt.item())
-        feat = T.vm_density(self._grid('density'), T.gather_rows(pn, idx, cnt, nv)) if nv else \
-            torch.zeros(0, device=xyz.device)
+        feat = self.density_features(T.gather_rows(pn, idx, cnt, nv)) if nv else torch.zeros(0, device=xyz.device)
         sigma = T.density_activation(feat, idx, cnt, xyz.shape[0], self.density_mode, self.density_offset)
         return 1 - torch.exp(-sigma * length)
 
@@ -347,6 +365,9 @@ class GbVmTensor(torch.nn.Module):
             fixed[1] = (1 - br_r) * self.bounding_box[0] + br_r * self.bounding_box[1]
             bbox_new = fixed
         self.update_tensor_params(b_r - t_l, bbox_new)
+        self.crop_tensor(t_l, b_r)
+
+    def crop_tensor(self, t_l, b_r):
         for plist, vlist in ((self.matrices_density, self.vectors_density), (self.matrices_color, self.vectors_color)):
             for i in range(3):
                 m0, m1 = MATRIX_AXES[i]
@@ -377,8 +398,67 @@ class GbVmTensor(torch.nn.Module):
             self.alpha_mask = AlphaGridMask(sd[key].float(), sd[f'{prefix}alpha_mask.bounding_box'])
         res = sd.get(f'{prefix}resolution')
         if res is not None:
-            self.matrices_density, self.vectors_density = self.resize(self.matrices_density, self.vectors_density, res)
-            self.matrices_color, self.vectors_color = self.resize(self.matrices_color, self.vectors_color, res)
+            self.resample_tensor(res)
+
+
+class GbCpTensor(GbVmTensor):
+    """LowRankTensor + CpDecomposedTensor (SimpleTensoRF09.py:964-1123): density and colour
+    from three lines each (vector_axes (2, 1, 0)), on the CP lookup kernels."""
+
+    DECOMPOSITION = 'CandecompParafac'
+
+    def build_tensor(self):
+        """CpDecomposedTensor.build_tensor (:979-987)."""
+        tc = self.tensor_configs
+        self.vectors_density = self.create_decomposed_tensor(tc['num_components_density'], self.resolution)
+        self.vectors_color = self.create_decomposed_tensor(tc['num_components_color'], self.resolution)
+
+    def create_decomposed_tensor(self, num_components, resolution, scale=0.1):
+        """Lines (1, R, res[vector_axes[i]], 1), R = num_components[0] (:989-996), channels-last."""
+        return torch.nn.ParameterList([torch.nn.Parameter(T.to_channels_last(
+            scale * torch.randn(1, num_components[0], int(resolution[VECTOR_AXES[i]]), 1))) for i in range(3)])
+
+    def _lines(self, kind):
+        lines = self.vectors_density if kind == 'density' else self.vectors_color
+        for p in lines:
+            if not p.is_contiguous(memory_format=torch.channels_last):
+                p.data = T.to_channels_last(p.data)
+        return list(lines)
+
+    def density_features(self, pts):
+        return T.cp_density(self._lines('density'), self.resolution, pts)
+
+    def color_features(self, pts):
+        return T.cp_color(self._lines('color'), self.resolution, pts)
+
+    def tensor_parameters(self):
+        """(:998-1026): density lines, then colour lines."""
+        return list(self.vectors_density) + list(self.vectors_color)
+
+    def resample_tensor(self, res):
+        """upsample_vectors (:1106-1116)."""
+        def up(vecs):
+            return torch.nn.ParameterList([torch.nn.Parameter(T.to_channels_last(tF.interpolate(
+                vecs[i].data, size=(int(res[VECTOR_AXES[i]]), 1), mode='bilinear', align_corners=True)))
+                for i in range(3)])
+        self.vectors_density = up(self.vectors_density)
+        self.vectors_color = up(self.vectors_color)
+
+    def crop_tensor(self, t_l, b_r):
+        """shrink_tensor (:1118-1123)."""
+        for vlist in (self.vectors_density, self.vectors_color):
+            for i in range(3):
+                v = VECTOR_AXES[i]
+                vlist[i] = torch.nn.Parameter(T.to_channels_last(vlist[i].data[..., t_l[v]:b_r[v], :]))
+
+
+def make_tensor_model(name, configs, tensor_configs, model_configs):
+    """SimpleTensoRF.get_tensor_model (SimpleTensoRF09.py:534-544)."""
+    kinds = {GbVmTensor.DECOMPOSITION: GbVmTensor, GbCpTensor.DECOMPOSITION: GbCpTensor}
+    kind = tensor_configs['decomposition_type']
+    if kind not in kinds:
+        raise RuntimeError(f'Unknown tensor decomposition: {kind}')
+    return kinds[kind](name, configs, tensor_configs, model_configs)
 
 
 class GbSimpleTensoRF(torch.nn.Module):
@@ -407,9 +487,9 @@ class GbSimpleTensoRF(torch.nn.Module):
     def build_nerf(self):
         m = self.configs['model']
         if self.coarse_model_needed:
-            self.coarse_model = GbVmTensor('coarse_model', self.configs, m['coarse_model'], self.model_configs)
+            self.coarse_model = make_tensor_model('coarse_model', self.configs, m['coarse_model'], self.model_configs)
         if self.fine_model_needed:
-            self.fine_model = GbVmTensor('fine_model', self.configs, m['fine_model'], self.model_configs)
+            self.fine_model = make_tensor_model('fine_model', self.configs, m['fine_model'], self.model_configs)
         self.intrinsics_learner = IntrinsicsLearner(numpy.array(self.model_configs['intrinsics']),
                                                     learn_focal=m['learn_camera_focal_length'])
         self.extrinsics_learner = ExtrinsicsLearner(numpy.array(self.model_configs['extrinsics']),
@@ -421,7 +501,8 @@ class GbSimpleTensoRF(torch.nn.Module):
                 entry = {'name': aug['name'], 'coarse_model': None, 'fine_model': None}
                 for key in ('coarse_model', 'fine_model'):
                     if key in aug:
-                        entry[key] = GbVmTensor(f"{aug['name']}_{key}", self.configs, aug[key], self.model_configs)
+                        entry[key] = make_tensor_model(f"{aug['name']}_{key}", self.configs, aug[key],
+                                                       self.model_configs)
                         nn_dict[key] = entry[key]
                 self.augmented_models.append(entry)
                 self.augmented_models_nn.append(nn_dict)

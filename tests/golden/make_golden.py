@@ -381,6 +381,79 @@ def tensorf_case():
     return out
 
 
+def tensorf_cp_case():
+    """CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123): density and
+    colour from three lines each, then the same renderer; LowRankTensor.forward on a
+    small grid with autograd gradients."""
+    g = torch.Generator().manual_seed(37)
+    res = torch.tensor([18, 20, 22])
+    bbox = [[-1.5, -1.5, -1.5], [1.5, 1.5, 1.5]]
+    tcfg = {'decomposition_type': 'CandecompParafac', 'num_samples_max': 1e6, 'num_components_density': [5],
+            'num_components_color': [6], 'bounding_box': bbox, 'num_voxels_initial': int(res.prod()),
+            'num_voxels_final': int(res.prod()), 'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5,
+            'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4,
+            'use_view_dirs': True, 'view_dependent_color': True, 'views_positional_encoding_degree': 2,
+            'features_positional_encoding_degree': 2, 'features_dimension_color': 7, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 16, 'predict_visibility': False}
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': False}, 'database': 'synthetic'}
+    tm = RT.CpDecomposedTensor('coarse_model', configs, tcfg, {'bounding_box': bbox})
+    tm.update_tensor_params(res, torch.tensor(bbox))
+    tm.vectors_density = tm.create_decomposed_tensor([5], res, 0.1)
+    tm.vectors_color = tm.create_decomposed_tensor([6], res, 0.1)
+    with torch.no_grad():
+        for prm in tm.vectors_density:
+            prm.copy_(torch.randn(prm.shape, generator=g) * 0.4 + 0.5)
+        for prm in tm.vectors_color:
+            prm.copy_(torch.randn(prm.shape, generator=g) * 0.5)
+        for prm in list(tm.basis_matrix_color.parameters()) + list(tm.color_predictor.parameters()):
+            prm.copy_(torch.randn(prm.shape, generator=g) * 0.3)
+    tm.train()
+    n = 10
+    o = torch.zeros(n, 3)
+    o[:, 2] = -3.0
+    o[:, :2] = torch.rand(n, 2, generator=g) * 0.6 - 0.3
+    d = torch.randn(n, 3, generator=g) * 0.15
+    d[:, 2] = 1.0
+    d = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    u = torch.rand(n, 1, generator=g)
+    fake = types.SimpleNamespace(ndc=False, training=True,
+                                 configs={'model': {'perturb': True, 'lindisp': False}},
+                                 model_configs={'near': 0.5, 'far': 6.0})
+    with patched_rand([u]):
+        z = RT.SimpleTensoRF.get_z_vals_coarse(fake, {'pixel_id': torch.zeros(n, 3)},
+                                               {'rays_o': o, 'rays_d': d}, tm)
+    pts = o[:, None, :] + d[:, None, :] * z[:, :, None]
+    vdir = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    inp = {'pts': pts, 'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vdir}
+    with patched_rand([torch.tensor([0.25])]):       # white-background coin: rand < 0.5 -> white
+        ret = tm(inp, retraw=True)
+    tg = torch.Generator().manual_seed(33)
+    loss = 0
+    out = {}
+    for k in ('rgb', 'depth', 'acc'):
+        c = torch.randn(ret[k].shape, generator=tg)
+        out[f'cot_{k}'] = c.numpy()
+        loss = loss + torch.sum(ret[k] * c)
+    loss.backward()
+    out.update({'res': res.numpy(), 'bbox': np.array(bbox, np.float32), 'u': u.numpy(), 'rays_o': o.numpy(),
+                'rays_d': d.numpy(), 'z': z.numpy(), 'step_size': tm.step_size.numpy(),
+                'num_samples': tm.num_samples.numpy()})
+    for i in range(3):
+        out[f'lines_density.{i}'] = tm.vectors_density[i].detach().numpy()[0]
+        out[f'lines_color.{i}'] = tm.vectors_color[i].detach().numpy()[0]
+        out[f'grad_lines_density.{i}'] = tm.vectors_density[i].grad.numpy()[0]
+        out[f'grad_lines_color.{i}'] = tm.vectors_color[i].grad.numpy()[0]
+    out['basis_matrix_color.weight'] = tm.basis_matrix_color.weight.detach().numpy()
+    out['grad_basis_matrix_color.weight'] = tm.basis_matrix_color.weight.grad.numpy()
+    for k, prm in tm.color_predictor.named_parameters():
+        out['color_predictor.' + k] = prm.detach().numpy()
+        out['grad_color_predictor.' + k] = prm.grad.numpy()
+    for k, v in ret.items():
+        out['out_' + k] = v.detach().numpy()
+    return out
+
+
 def losses_case():
     """The reference's per-ray losses on random inputs with autograd gradients:
     MassConcentrationLoss06.compute_entropy_loss (64 and 67 samples, 5 bins),
@@ -489,6 +562,7 @@ def main():
             augs=[{'name': 'views_augmentation', 'coarse_model': mlp_cfg(lp=4, views=False, vdr=False)}],
             aug_seeds=[77]),
         'tensorf': tensorf_case,
+        'tensorf_cp': tensorf_cp_case,
         'losses': losses_case,
         'reprojection': reprojection_case,
     }

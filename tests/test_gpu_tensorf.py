@@ -133,3 +133,48 @@ def test_tensorf_tensor_core_renderer_against_fp32(precision, bar):
     print(precision, 'rgb max-abs', err, 'renderer+colour-grid gradient rel-L2', rel)
     assert err < 2e-3, err
     assert rel < bar, rel
+
+
+def test_tensorf_cp_matches_reference_golden(golden):
+    """The CP decomposition (GbCpTensor on the CP lookup kernels) against
+    CpDecomposedTensor's own outputs and autograd gradients (golden tensorf_cp)."""
+    g = golden('tensorf_cp')
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300 import tensorf as T
+    from simple_rf_gb300.tensorf_model import GbCpTensor, make_tensor_model
+    tc = dict(_tcfg())
+    tc.update(decomposition_type='CandecompParafac', num_components_density=[5], num_components_color=[6])
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
+    tm = make_tensor_model('coarse_model', configs, tc, {'bounding_box': tc['bounding_box']})
+    assert isinstance(tm, GbCpTensor)
+    tm.update_tensor_params(torch.tensor(g['res']), torch.tensor(g['bbox']))
+    with torch.no_grad():
+        for kind, plist in (('lines_density', tm.vectors_density), ('lines_color', tm.vectors_color)):
+            for i in range(3):
+                plist[i] = torch.nn.Parameter(T.to_channels_last(torch.from_numpy(g[f'{kind}.{i}'])[None]))
+        tm.basis_matrix_color.weight.copy_(torch.from_numpy(g['basis_matrix_color.weight']))
+        for k, prm in tm.color_predictor.named_parameters():
+            prm.copy_(torch.from_numpy(g['color_predictor.' + k]))
+    tm = tm.to(DEV)
+    tm.eval()
+    o = torch.from_numpy(g['rays_o']).to(DEV)
+    d = torch.from_numpy(g['rays_d']).to(DEV)
+    z = torch.from_numpy(g['z']).to(DEV)
+    vd = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=True)
+    for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'depth_var'):
+        ref = g['out_' + k]
+        got = out[k].detach().cpu().numpy()
+        np.testing.assert_allclose(got, ref, rtol=1e-4, atol=2e-4 * max(1.0, float(np.abs(ref).max())), err_msg=k)
+    loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'acc'))
+    loss.backward()
+    pairs = [(f'lines_density.{i}', tm.vectors_density[i].grad[0]) for i in range(3)]
+    pairs += [(f'lines_color.{i}', tm.vectors_color[i].grad[0]) for i in range(3)]
+    pairs.append(('basis_matrix_color.weight', tm.basis_matrix_color.weight.grad))
+    for k, prm in tm.color_predictor.named_parameters():
+        pairs.append(('color_predictor.' + k, prm.grad))
+    for name, grad in pairs:
+        ref = g['grad_' + name]
+        rel = np.linalg.norm(grad.detach().cpu().numpy() - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert rel < 1e-3, (name, rel)

@@ -220,6 +220,28 @@ def test_tensorf_forward_backward(golden):
         assert err < 1e-4, (k, err)
 
 
+def test_tensorf_cp_forward_backward(golden):
+    """The oracle's CP path against CpDecomposedTensor (golden tensorf_cp)."""
+    g = golden('tensorf_cp')
+    tp = {'bbox': g['bbox']}
+    for kind in ('lines_density', 'lines_color'):
+        tp[kind] = [g[f'{kind}.{i}'] for i in range(3)]
+    for k in g:
+        if k.startswith('color_predictor.') or k == 'basis_matrix_color.weight':
+            tp[k] = g[k]
+    spec = ot.RendererSpec(features_dim=7, features_pe=2, views_pe=2, units=16)
+    out, cache = ot.tensorf_forward(tp, spec, g['rays_o'], g['rays_d'], g['z'], white=True)
+    for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'raw_rgb', 'depth_var'):
+        ref = g['out_' + k]
+        close(out[k], ref, rtol=1e-4, atol=1e-5 * max(1.0, float(np.abs(ref).max())))
+    grads = ot.tensorf_backward(tp, spec, cache, {k: g[f'cot_{k}'] for k in ('rgb', 'depth', 'acc')})
+    assert set(grads) >= {'lines_density.0', 'lines_color.2', 'basis_matrix_color.weight'}
+    for k, v in grads.items():
+        ref = g['grad_' + k]
+        err = np.linalg.norm(v - ref) / max(np.linalg.norm(ref), 1e-12)
+        assert err < 1e-4, (k, err)
+
+
 def test_alpha_mask_query(golden):
     g = golden('tensorf')
     pos = ot.grid_sample_3d_positive(g['alpha_vol'], ot.normalize_points(g['alpha_q'], g['bbox']))
