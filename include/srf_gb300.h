@@ -444,6 +444,26 @@ int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const
                                  const float* intrinsics0, const float* images, int height, int width, int channels,
                                  int patch_w, int patch_h, float rmse_threshold, uint8_t* mask1, uint8_t* mask2,
                                  void* stream);
+/* One grid of the total-variation loss: element (c, h, w) of the (1, channels,
+ * height, width) parameter at data[c*stride_channel + h*stride_height +
+ * w*stride_width] (channels-last: stride_channel 1); grad (may be NULL) has the
+ * same strides. */
+typedef struct srf_tv_component {
+    const float* data;
+    float* grad;
+    int channels, height, width;
+    int64_t stride_channel, stride_height, stride_width;
+} srf_tv_component;
+/* TotalVariationLoss04.compute_tv_loss (src/loss_functions/TotalVariationLoss04.py:97-116)
+ * over up to 8 components (a VM model's three planes, or a CP model's three lines):
+ * loss_dev (may be NULL) += weight * sum_i 2 (sum (P[h+1] - P[h])^2 / numel_h +
+ * sum (P[w+1] - P[w])^2 / numel_w), numel_* the element counts of the difference
+ * tensors floored at 1; each component's grad += s * d loss / d data, s =
+ * *scale_dev, or 1 when scale_dev is NULL (a device scalar, e.g. autograd's
+ * incoming gradient).  weight = iter_weight * the loss's weight_density or
+ * weight_color. */
+int srf_tv_loss(const srf_tv_component* components, int n_components, float weight, const float* scale_dev,
+                float* loss_dev, void* stream);
 /* *counter_dev += value on the stream (advances a graph-replayed step count),
  * unless skip_dev != NULL and *skip_dev != 0. */
 int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, void* stream);

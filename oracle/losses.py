@@ -159,3 +159,32 @@ def reprojection_depth_loss(depth1, depth2, mask1, mask2):
     both = np.asarray(mask1, bool) & np.asarray(mask2, bool)
     l2, g2, _ = depth_mse(depth2, depth1, both)
     return l1 + l2, g1, g2
+
+
+def tv_loss(components, weight=1.0):
+    """TotalVariationLoss04.compute_tv_loss (src/loss_functions/TotalVariationLoss04.py:97-116)
+    times ``weight``: per (1, R, H, W) component, 2 (sum of squared H differences /
+    their count + the same along W), each count floored at 1 (:103-104).  Returns
+    (loss, [d loss / d component])."""
+    loss = 0.0
+    grads = []
+    for c in components:
+        c = np.asarray(c)
+        dt = c.dtype.type
+        dh = c[:, :, 1:, :] - c[:, :, :-1, :]
+        dw = c[:, :, :, 1:] - c[:, :, :, :-1]
+        nh, nw = max(dh.size, 1), max(dw.size, 1)
+        loss += float(weight) * 2.0 * (float(np.sum(dh * dh)) / nh + float(np.sum(dw * dw)) / nw)
+        g = np.zeros_like(c)
+        ch, cw = dt(4.0 * weight / nh), dt(4.0 * weight / nw)
+        g[:, :, 1:, :] += ch * dh
+        g[:, :, :-1, :] -= ch * dh
+        g[:, :, :, 1:] += cw * dw
+        g[:, :, :, :-1] -= cw * dw
+        grads.append(g)
+    return loss, grads
+
+
+def tv_iter_weight(lr_decay_ratio, lr_decay_iters, iter_num):
+    """TotalVariationLoss04.get_iter_weight (:118-120)."""
+    return lr_decay_ratio ** ((iter_num + 1) / lr_decay_iters)

@@ -44,6 +44,11 @@ class VmGrid(ctypes.Structure):
     _fields_ = [('res', c_int * 3), ('n_comp', c_int * 3), ('planes', P * 3), ('lines', P * 3)]
 
 
+class TvComponent(ctypes.Structure):
+    _fields_ = [('data', P), ('grad', P), ('channels', c_int), ('height', c_int), ('width', c_int),
+                ('stride_channel', c_int64), ('stride_height', c_int64), ('stride_width', c_int64)]
+
+
 SRF_COMPOSITE_NDC = 1
 SRF_COMPOSITE_WHITE_BKGD = 2
 SRF_PRECISION_FP32 = 0
@@ -120,6 +125,7 @@ _SIGS = {
     'srf_depth_reprojection_masks': (c_int, [P, P, P, P, P, c_int, P, c_int, P, P, c_int, c_int, c_int, c_int, c_int,
                                              c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
+    'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
     'srf_launch_count': (c_int64, []),
 }
 

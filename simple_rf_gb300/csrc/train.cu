@@ -323,6 +323,48 @@ __global__ void ray_points_kernel(const float* __restrict__ o, const float* __re
     for (int a = 0; a < 3; ++a) pts[3 * idx + a] = __fadd_rn(o[3 * r + a], __fmul_rn(d[3 * r + a], zz));
 }
 
+// One component of the total-variation loss: an (R, H, W) grid with element
+// strides (sr, sh, sw), its gradient (same strides) and the loss weights of the
+// H and W differences, weight * 2 / numel.
+struct TvComp {
+    const float* p;
+    float* g;
+    int r, h, w;
+    int64_t sr, sh, sw;
+    float ch, cw;
+};
+constexpr int kMaxTvComps = 8;
+struct TvBatch {
+    TvComp c[kMaxTvComps];
+};
+
+// TotalVariationLoss04.compute_tv_loss (TotalVariationLoss04.py:97-116):
+// loss += sum ch (P[h+1] - P[h])^2 + cw (P[w+1] - P[w])^2 over the component,
+// grad += scale * d loss / dP, a thread per element (r fastest, so a channels-last
+// grid is read in order).  blockIdx.y picks the component.
+__global__ void __launch_bounds__(256) tv_kernel(const __grid_constant__ TvBatch b, const float* scale_dev,
+                                                 float* loss) {
+    __shared__ float red[32];
+    const TvComp& c = b.c[blockIdx.y];
+    const float gs = scale_dev ? *scale_dev : 1.f;
+    const uint32_t n = uint32_t(c.r) * uint32_t(c.h) * uint32_t(c.w);
+    float l = 0.f;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t r = j % uint32_t(c.r), t = j / uint32_t(c.r);
+        const int w = int(t % uint32_t(c.w)), h = int(t / uint32_t(c.w));
+        const int64_t off = int64_t(r) * c.sr + int64_t(h) * c.sh + int64_t(w) * c.sw;
+        const float x = c.p[off];
+        const float dn = h + 1 < c.h ? c.p[off + c.sh] - x : 0.f;    // P[h+1] - P[h]
+        const float up = h > 0 ? x - c.p[off - c.sh] : 0.f;          // P[h] - P[h-1]
+        const float rt = w + 1 < c.w ? c.p[off + c.sw] - x : 0.f;
+        const float lf = w > 0 ? x - c.p[off - c.sw] : 0.f;
+        l += c.ch * dn * dn + c.cw * rt * rt;
+        if (c.g) c.g[off] += gs * 2.f * (c.ch * (up - dn) + c.cw * (lf - rt));
+    }
+    l = block_sum(l, red);
+    if (loss && threadIdx.x == 0 && l != 0.f) atomicAdd(loss, l);
+}
+
 }  // namespace
 }  // namespace srf
 
@@ -473,5 +515,35 @@ extern "C" int srf_depth_reprojection_masks(const float* rays_o, const float* ra
     reprojection_masks_kernel<<<grid_1d(n_rays, 128), 128, 0, as_stream(stream)>>>(
         rays_o, rays_d, depth1, depth2, pixel_ids, n_rays, poses, n_views, intrinsics0, images, height, width,
         channels, patch_w / 2, patch_h / 2, rmse_threshold, mask1, mask2, device_flag());
+    return launch_status();
+}
+
+extern "C" int srf_tv_loss(const srf_tv_component* components, int n_components, float weight, const float* scale_dev,
+                           float* loss_dev, void* stream) {
+    if (n_components < 0 || n_components > kMaxTvComps) return SRF_ERR_SHAPE;
+    if (n_components == 0) return SRF_OK;
+    if (!components) return SRF_ERR_NULL;
+    TvBatch b = {};
+    uint32_t most = 0;
+    for (int i = 0; i < n_components; ++i) {
+        const srf_tv_component& s = components[i];
+        if (s.channels < 1 || s.height < 1 || s.width < 1) return SRF_ERR_SHAPE;
+        const int64_t n = int64_t(s.channels) * s.height * s.width;
+        if (n > int64_t(0x7fffffff)) return SRF_ERR_SHAPE;
+        if (!s.data) return SRF_ERR_NULL;
+        // numel of the difference tensors, at least 1 (TotalVariationLoss04.py:103-104)
+        const int64_t nh = int64_t(s.channels) * (s.height - 1) * s.width;
+        const int64_t nw = int64_t(s.channels) * s.height * (s.width - 1);
+        b.c[i] = {s.data, s.grad, s.channels, s.height, s.width, s.stride_channel, s.stride_height, s.stride_width,
+                  float(2.0 * weight / double(nh > 1 ? nh : 1)), float(2.0 * weight / double(nw > 1 ? nw : 1))};
+        if (uint32_t(n) > most) most = uint32_t(n);
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned gx = grid_1d(most, 256);
+    const unsigned cap = unsigned(sms > 0 ? sms : 152) * 8u / unsigned(n_components);
+    if (gx > cap) gx = cap > 0 ? cap : 1;
+    tv_kernel<<<dim3(gx, n_components), 256, 0, as_stream(stream)>>>(b, scale_dev, loss_dev);
     return launch_status();
 }

@@ -349,3 +349,72 @@ def pixel_rays(pixel_id, intrinsics, extrinsics, half_pixel=False):
     d = torch.empty(n, 3, device=k.device)
     call('srf_pixel_rays', _ptr(pid), _ptr(k), _ptr(e), n, int(half_pixel), _ptr(o), _ptr(d), _stream())
     return o, d
+
+
+_TV_MAX = 8
+
+
+def _tv_struct(comps, grads=None):
+    arr = (_lib.TvComponent * len(comps))()
+    for i, p in enumerate(comps):
+        if p.dim() != 4 or p.shape[0] != 1:
+            raise ValueError(f'TV component {i}: expected (1, R, H, W), got {tuple(p.shape)}')
+        if not p.is_cuda or p.dtype != torch.float32:
+            raise RuntimeError(f'TV component {i} must be a float32 CUDA tensor (the srf_gb300 kernels have no '
+                               'CPU path)')
+        g = None if grads is None else grads[i]
+        if g is not None and (g.stride() != p.stride() or g.shape != p.shape):
+            raise ValueError(f'TV component {i}: gradient strides {g.stride()} differ from {p.stride()}')
+        arr[i] = _lib.TvComponent(p.data_ptr(), None if g is None else g.data_ptr(), p.shape[1], p.shape[2],
+                                  p.shape[3], p.stride(1), p.stride(2), p.stride(3))
+    return arr
+
+
+class TvLossFunction(torch.autograd.Function):
+    """srf_tv_loss forward (loss only) and backward (gradients scaled by the incoming
+    gradient on the device)."""
+
+    @staticmethod
+    def forward(ctx, weight, *comps):
+        loss = torch.zeros((), device=comps[0].device)
+        for i in range(0, len(comps), _TV_MAX):
+            part = comps[i:i + _TV_MAX]
+            call('srf_tv_loss', _tv_struct(part), len(part), float(weight), None, _ptr(loss), _stream())
+        ctx.save_for_backward(*comps)
+        ctx.weight = float(weight)
+        return loss
+
+    @staticmethod
+    def backward(ctx, g):
+        comps = ctx.saved_tensors
+        grads = [torch.zeros_like(p) for p in comps]
+        g = g.float().contiguous()
+        for i in range(0, len(comps), _TV_MAX):
+            part = comps[i:i + _TV_MAX]
+            call('srf_tv_loss', _tv_struct(part, grads[i:i + _TV_MAX]), len(part), ctx.weight, _ptr(g), None,
+                 _stream())
+        return (None, *grads)
+
+
+def tv_loss(components, weight=1.0):
+    """weight * TotalVariationLoss04.compute_tv_loss's sum over (1, R, H, W) grids
+    (src/loss_functions/TotalVariationLoss04.py:97-116), differentiable."""
+    comps = [p if p.dtype == torch.float32 else p.float() for p in components]
+    if not comps:
+        return torch.zeros(())
+    return TvLossFunction.apply(float(weight), *comps)
+
+
+def tv_loss_accumulate(components, weight, loss=None):
+    """The same loss added into ``loss`` (a device scalar, may be None) with each
+    component's gradient added into its ``.grad`` in the same launch (for fused
+    training steps that own the gradient buffers)."""
+    comps = list(components)
+    for p in comps:
+        if p.grad is None:
+            p.grad = torch.zeros_like(p)
+    for i in range(0, len(comps), _TV_MAX):
+        part = comps[i:i + _TV_MAX]
+        call('srf_tv_loss', _tv_struct([p.detach() for p in part], [p.grad for p in part]), len(part),
+             float(weight), None, _ptr(loss), _stream())
+    return loss

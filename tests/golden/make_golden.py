@@ -547,6 +547,34 @@ def reprojection_case():
                 grad1=d1.grad.numpy(), grad2=d2.grad.numpy())
 
 
+def tv_case():
+    """TotalVariationLoss04 on random grids with autograd gradients:
+    compute_tv_loss on three VM-like planes of unequal shapes (one with a single
+    row), on three CP-like lines (1, R, L, 1), and the iteration weight of a
+    configured instance."""
+    from loss_functions import TotalVariationLoss04 as LTV
+    g = torch.Generator().manual_seed(47)
+    out = {}
+    sets = {'vm': [(1, 6, 17, 23), (1, 4, 9, 31), (1, 5, 1, 12)],
+            'cp': [(1, 7, 29, 1), (1, 3, 40, 1), (1, 5, 11, 1)]}
+    iter_weight = 0.37
+    for tag, shapes in sets.items():
+        comps = [(torch.randn(*sh, generator=g) * 0.1).requires_grad_(True) for sh in shapes]
+        loss = LTV.TotalVariationLoss.compute_tv_loss(comps, iter_weight, False)['loss_value']
+        loss.backward()
+        for i, c in enumerate(comps):
+            out[f'{tag}_comp{i}'] = c.detach().numpy()
+            out[f'{tag}_grad{i}'] = c.grad.numpy()
+        out[f'{tag}_loss'] = loss.detach().numpy()
+    out['iter_weight'] = np.array(iter_weight)
+    cfg = {'model': {}, 'num_iterations': 30000,
+           'optimizers': [{'name': 'optimizer_main', 'lr_decay_ratio': 0.1, 'lr_decay_iters': None}]}
+    tv = LTV.TotalVariationLoss(cfg, {'weight_density': 1.0, 'weight_color': 1.0})
+    out['decay_iter_num'] = np.array(1234)
+    out['decay_weight'] = np.array(tv.get_iter_weight(1234))
+    return out
+
+
 def main():
     cases = {
         'nerf_sampling': sampling_case,
@@ -565,6 +593,7 @@ def main():
         'tensorf_cp': tensorf_cp_case,
         'losses': losses_case,
         'reprojection': reprojection_case,
+        'tv': tv_case,
     }
     only = sys.argv[1:]
     for name, fn in cases.items():

@@ -145,3 +145,105 @@ def test_reprojection_masks_against_oracle_random_scene():
     bad = (m1 != r1) | (m2 != r2)
     assert r1.sum() > 100 and r2.sum() > 100
     assert not (bad & ~(near(p1) | near(p2))).any(), np.flatnonzero(bad)[:10]
+
+
+def _tv_gpu(comps_np, weight, channels_last):
+    from simple_rf_gb300 import functional as F
+    ps = []
+    for c in comps_np:
+        p = _t(c)
+        if channels_last:
+            p = p.contiguous(memory_format=torch.channels_last)
+        ps.append(p.requires_grad_(True))
+    loss = F.tv_loss(ps, weight)
+    loss.backward()
+    torch.cuda.synchronize()
+    return float(loss.item()), [p.grad.cpu().numpy() for p in ps], ps
+
+
+@pytest.mark.parametrize('channels_last', [False, True])
+def test_tv_loss_matches_reference_golden(golden, channels_last):
+    g = golden('tv')
+    w = float(g['iter_weight'])
+    for tag in ('vm', 'cp'):
+        comps = [g[f'{tag}_comp{i}'] for i in range(3)]
+        loss, grads, ps = _tv_gpu(comps, w, channels_last)
+        assert abs(loss - float(g[f'{tag}_loss'])) < 1e-5 * abs(float(g[f'{tag}_loss'])), tag
+        for i in range(3):
+            ref = g[f'{tag}_grad{i}']
+            assert ps[i].grad.stride() == ps[i].stride()
+            np.testing.assert_allclose(grads[i], ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+
+
+def test_tv_loss_full_size_planes_against_oracle():
+    # the three 300^2 x 48 colour planes of the 300^3 model, channels-last as the drop-in stores them
+    gen = torch.Generator().manual_seed(5)
+    comps = [(torch.randn(1, 48, 300, 300, generator=gen) * 0.1).numpy() for _ in range(3)]
+    loss, grads, _ = _tv_gpu(comps, 0.25, True)
+    ref_loss, ref_grads = ol.tv_loss([c.astype(np.float64) for c in comps], 0.25)
+    assert abs(loss - ref_loss) < 1e-5 * abs(ref_loss)
+    for a, b in zip(grads, ref_grads):
+        np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-5 * np.abs(b).max())
+
+
+def test_tv_loss_accumulate_adds_into_grad():
+    from simple_rf_gb300 import functional as F
+    gen = torch.Generator().manual_seed(6)
+    comps = [torch.randn(1, 4, 13, 21, generator=gen) for _ in range(2)]
+    ps = [c.to(DEV).contiguous(memory_format=torch.channels_last).requires_grad_(True) for c in comps]
+    for p in ps:
+        p.grad = torch.full_like(p, 0.5)
+    loss = torch.zeros((), device=DEV)
+    F.tv_loss_accumulate(ps, 3.0, loss)
+    torch.cuda.synchronize()
+    ref_loss, ref_grads = ol.tv_loss([c.numpy().astype(np.float64) for c in comps], 3.0)
+    assert abs(float(loss.item()) - ref_loss) < 1e-5 * ref_loss
+    for p, rg in zip(ps, ref_grads):
+        np.testing.assert_allclose(p.grad.cpu().numpy(), rg + 0.5, rtol=1e-5, atol=1e-5 * np.abs(rg).max())
+
+
+def test_tv_drop_in_loss_module_on_augmented_models():
+    """TotalVariationLoss.compute_loss over a model's augmented VM (coarse) and CP
+    (fine) grids: loss and parameter gradients against the oracle."""
+    import types
+    from simple_rf_gb300.bench_tensorf import tensor_configs, BBOX
+    from simple_rf_gb300.losses import TotalVariationLoss
+    from simple_rf_gb300.tensorf_model import make_tensor_model
+    torch.manual_seed(3)
+    cfg = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
+    vm = make_tensor_model('views_augmentation_coarse_model', cfg, tensor_configs(20 ** 3), {'bounding_box': BBOX})
+    tc = dict(tensor_configs(16 ** 3), decomposition_type='CandecompParafac', num_components_density=[8],
+              num_components_color=[24])
+    cp = make_tensor_model('views_augmentation_fine_model', cfg, tc, {'bounding_box': BBOX})
+    vm, cp = vm.to(DEV), cp.to(DEV)
+    model = types.SimpleNamespace(module=types.SimpleNamespace(
+        augmented_models=[{'name': 'views_augmentation', 'coarse_model': vm, 'fine_model': cp}]))
+    configs = {'model': {'augmentations': [{'name': 'views_augmentation', 'coarse_model': {}, 'fine_model': {}}]},
+               'num_iterations': 1000,
+               'optimizers': [{'name': 'optimizer_main', 'lr_decay_ratio': 0.1, 'lr_decay_iters': None}]}
+    tv = TotalVariationLoss(configs, {'weight_density': 0.5, 'weight_color': 0.25})
+    loss = tv.compute_loss({'target_rgb': torch.zeros(1, 3, device=DEV), 'iter_num': 99}, {}, model)['loss_value']
+    loss.backward()
+    iw = ol.tv_iter_weight(0.1, 1000, 99)
+    ref = 0.0
+    for grids, w in ((vm.matrices_density, 0.5), (vm.matrices_color, 0.25), (cp.vectors_density, 0.5),
+                     (cp.vectors_color, 0.25)):
+        l, grads = ol.tv_loss([p.detach().cpu().numpy().astype(np.float64) for p in grids], iw * w)
+        ref += l
+        for p, rg in zip(grids, grads):
+            np.testing.assert_allclose(p.grad.cpu().numpy(), rg, rtol=1e-5, atol=1e-5 * np.abs(rg).max())
+    assert abs(float(loss.item()) - ref) < 1e-5 * ref
+
+
+def test_tv_loss_rejects_bad_shapes():
+    from simple_rf_gb300 import _lib
+    lib = _lib.load()
+    p = torch.zeros(1, 2, 3, 4, device=DEV)
+    c = _lib.TvComponent(p.data_ptr(), None, 2, 3, 4, 1, 8, 2)
+    arr = (_lib.TvComponent * 9)(*([c] * 9))
+    assert lib.srf_tv_loss(arr, 9, 1.0, None, None, None) != 0                    # more than 8 components
+    bad = (_lib.TvComponent * 1)(_lib.TvComponent(p.data_ptr(), None, 0, 3, 4, 1, 8, 2))
+    assert lib.srf_tv_loss(bad, 1, 1.0, None, None, None) != 0                    # empty channel axis
+    null = (_lib.TvComponent * 1)(_lib.TvComponent(None, None, 2, 3, 4, 1, 8, 2))
+    assert lib.srf_tv_loss(null, 1, 1.0, None, None, None) != 0
+    assert lib.srf_tv_loss(None, 0, 1.0, None, None, None) == 0

@@ -46,3 +46,21 @@ def test_reprojection_masks_and_loss_match_reference(golden):
     assert abs(loss - float(g['loss'])) < 1e-5 * float(g['loss'])
     np.testing.assert_allclose(g1, g['grad1'], rtol=1e-5, atol=1e-9)
     np.testing.assert_allclose(g2, g['grad2'], rtol=1e-5, atol=1e-9)
+
+
+def test_tv_loss_matches_reference(golden):
+    g = golden('tv')
+    w = float(g['iter_weight'])
+    for tag in ('vm', 'cp'):
+        comps = [g[f'{tag}_comp{i}'].astype(np.float64) for i in range(3)]
+        loss, grads = ol.tv_loss(comps, w)
+        assert abs(loss - float(g[f'{tag}_loss'])) < 1e-5 * abs(float(g[f'{tag}_loss'])), tag
+        for i in range(3):
+            np.testing.assert_allclose(grads[i], g[f'{tag}_grad{i}'], rtol=1e-5, atol=1e-9)
+    assert abs(ol.tv_iter_weight(0.1, 30000, int(g['decay_iter_num'])) - float(g['decay_weight'])) < 1e-12
+
+
+def test_tv_loss_single_row_and_column():
+    # a (1, R, 1, 1) grid has no differences: loss 0, gradient 0 (counts floored at 1)
+    loss, grads = ol.tv_loss([np.ones((1, 3, 1, 1))], 2.0)
+    assert loss == 0.0 and not grads[0].any()
