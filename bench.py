@@ -412,7 +412,8 @@ def run_ours(args):
         variants['nerf_fp16'] = time_variant('nerf', 'fp16', args.steps, dev, stream)
         for prec, k in (('bf16', args.steps), ('fp16', args.steps), ('fp32', k32)):
             variants[f'nerf_pair_{prec}'] = time_variant('nerf_pair', prec, k, dev, stream)
-        variants['tensorf_fp16'] = time_tensorf('fp16', 5, dev, stream)
+        # the same warm-up and timed steps for both (surface-sample counts drift as the grids train)
+        variants['tensorf_fp16'] = time_tensorf('fp16', 3, dev, stream)
         variants['tensorf_fp32'] = time_tensorf('fp32', 3, dev, stream)
         variants['render'] = time_render(dev, stream)
     import ctypes

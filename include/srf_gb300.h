@@ -212,7 +212,7 @@ typedef struct {
     int n_rays, n_samples, flags;
     float distance_scale;          /* 1 for NeRF, tensor_configs['distance_scale'] for TensoRF */
     const float* sigma;            /* (N,S)                                       */
-    const float* rgb;              /* (N,S,3)                                     */
+    const float* rgb;              /* (N,S,3); NULL = zero colours (density pass) */
     const float* z;                /* (N,S) depth used for delta (NDC depth if NDC) */
     const float* rays_d;           /* (N,3) world directions                       */
     const float* rays_o;           /* (N,3) world origins (NDC only)               */

@@ -84,8 +84,8 @@ class TensorfTrainStep:
         loss = 0.0
         counts = []
         for i, tm in enumerate(self.models):
-            s = int(tm.num_samples.item())
-            z = F.aabb_z(o, d, s, tm.bounding_box.detach().cpu(), 2.0, 6.0, float(tm.step_size), u[:, i].contiguous())
+            bbox, s, step = tm.host_geometry()
+            z = F.aabb_z(o, d, s, bbox, 2.0, 6.0, step, u[:, i].contiguous())
             out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=False)
             loss = loss + torch.mean(torch.mean((out['rgb'] - t_rgb) ** 2, -1))
             counts.append(dict(tm.last_sample_counts))

@@ -108,13 +108,15 @@ __global__ void composite_fwd_kernel(srf_composite_args a) {
     float* sA = sT + a.n_samples;
     RayCtx c = make_ctx(a, r);
     forward_scan(c, sT, sA);
-    const float* rgb = a.rgb + int64_t(r) * c.s * 3;
+    const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;   // NULL: zero colours
     float cr = 0.f, cg = 0.f, cb = 0.f, acc = 0.f, wz = 0.f, wzn = 0.f;
     for (int i = lane; i < c.s; i += 32) {
         float w = sA[i] * sT[i];
-        cr += w * rgb[3 * i];
-        cg += w * rgb[3 * i + 1];
-        cb += w * rgb[3 * i + 2];
+        if (rgb) {
+            cr += w * rgb[3 * i];
+            cg += w * rgb[3 * i + 1];
+            cb += w * rgb[3 * i + 2];
+        }
         acc += w;
         float zi = c.z[i];
         if (c.ndc) {
@@ -176,7 +178,7 @@ __global__ void composite_bwd_kernel(srf_composite_args a) {
     float* sA = sT + a.n_samples;
     RayCtx c = make_ctx(a, r);
     forward_scan(c, sT, sA);
-    const float* rgb = a.rgb + int64_t(r) * c.s * 3;
+    const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;
     // forward sums: acc, depth (and NDC depth)
     float acc = 0.f, wz = 0.f, wzn = 0.f;
     for (int i = lane; i < c.s; i += 32) {
@@ -223,7 +225,7 @@ __global__ void composite_bwd_kernel(srf_composite_args a) {
     auto G_of = [&](int i) -> float {
         float zi = c.z[i];
         float zm = c.ndc ? depth_from_ndc(zi, c.oz, c.dz) : zi;
-        float g = rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 + gacc;
+        float g = (rgb ? rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 : 0.f) + gacc;
         if (a.g_weights) g += a.g_weights[ro + i];
         float d = zm - depth;
         g += gd * d * inv + gv * (d * d - 2.f * bsum * d * inv);
@@ -325,7 +327,6 @@ int check_args(const srf_composite_args* a, bool bwd) {
     if (!a || !a->sigma || !a->z || !a->rays_d) return SRF_ERR_NULL;
     if ((a->flags & SRF_COMPOSITE_NDC) && (!a->rays_o || !a->rays_d_ndc)) return SRF_ERR_NULL;
     if (a->n_rays < 0 || a->n_samples < 1 || a->n_samples > 16384) return SRF_ERR_SHAPE;
-    if (!a->rgb) return SRF_ERR_NULL;
     if (bwd && !a->d_sigma) return SRF_ERR_NULL;
     return SRF_OK;
 }

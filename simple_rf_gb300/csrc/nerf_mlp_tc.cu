@@ -778,8 +778,6 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
 
 namespace {
 
-constexpr int kBasisRows = 128;     // samples per block of the basis + encoding pass
-constexpr int kBasisThreads = 256;  // threads per block: 32 row groups of 4 x 8 column groups of 4
 constexpr int kMaxBasis = 32;    // largest basis width (features_dimension_color) it holds in registers
 
 struct RenderLayout {
@@ -836,18 +834,66 @@ size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size
     return c.used;
 }
 
-// B = feats . Wb^T (FP32) and x = [PE(B, lf), PE(view, lv), 0...] in format fmt for
-// kBasisRows samples per block.  The block copies its feature rows into shared
-// memory with coalesced loads (row stride C + 1 words) next to Wb transposed and
-// padded to kMaxBasis columns; thread t computes rows 4 (t / 8) .. +3 times
-// columns 4 (t % 8) .. +3 (per input: 4 row reads, spread over 4 banks x 8-way
-// broadcast, and one 128-bit weight read), then writes its PE entries into the
-// same row area re-used as the 16-bit staging, which the block stores with
-// consecutive threads on consecutive 4-byte words.
-__host__ __device__ inline size_t basis_stage_bytes(int C, int k1p) {
-    size_t fb = size_t(kBasisRows) * (C + 1) * sizeof(float);
-    size_t xb = size_t(kBasisRows) * (k1p + 2) * sizeof(op16);
-    return fb > xb ? fb : xb;
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// B = feats . Wb^T (FP32) and x = [PE(B, lf), PE(view, lv), 0...] in format fmt,
+// a persistent pass over tiles of 16 * RPT samples.  Each block keeps Wb transposed
+// (C x kMaxBasis, zero-padded) in shared memory and two feature-tile buffers (row
+// stride C + 4 words) filled by 16-byte asynchronous copies issued two tiles
+// ahead, so the loads of the next tile overlap the arithmetic of this one.
+// Product: thread t (128 per block) owns columns 4 (t % 8) .. +3 of rows t / 8 +
+// 16 i, i < RPT; per 4 inputs it reads one float4 of each of its rows and four
+// float4 weight rows (the four rows a warp touches fall in distinct banks) and
+// accumulates with packed two-lane FMAs (the same rounding as scalar FMAs, in
+// the same order).  Encoding: B goes through shared memory and a warp takes one
+// row at a time, lane f feature f (lanes F .. F + 2 the view direction): one
+// sincosf of the value, the 2^k multiples by the double-angle recurrence
+// sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a) (fp32 error
+// ~ 2^k ulp, far below the 16-bit rounding of the output), written into the
+// consumed tile buffer as the 16-bit staging (row stride k1p + 8), which the
+// block stores as 16-byte vectors.
+constexpr int kEncThreads = 128;
+
+// (d0, d1) += a * (b0, b1) with one packed two-lane FMA (fma.rn per lane)
+__device__ __forceinline__ void ffma2(float& d0, float& d1, float a, float b0, float b1) {
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %2};\n\tmov.b64 pb, {%3, %4};\n\tmov.b64 pd, {%0, %1};\n\t"
+        "fma.rn.f32x2 pd, pa, pb, pd;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "+f"(d0), "+f"(d1)
+        : "f"(a), "f"(b0), "f"(b1));
+}
+
+// (d0, d1) += (a0, a1) * (b0, b1) with one packed two-lane FMA
+__device__ __forceinline__ void fma2v(float& d0, float& d1, float a0, float a1, float b0, float b1) {
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\tmov.b64 pd, {%0, %1};\n\t"
+        "fma.rn.f32x2 pd, pa, pb, pd;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "+f"(d0), "+f"(d1)
+        : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
+__host__ __device__ inline int enc_tile_rows(int rpt) { return 16 * rpt; }
+constexpr int kEncBStride = kMaxBasis + 1;   // row stride (words) of the B tile in shared memory
+// the 16-bit staging rows of a tile (16-byte multiple), followed by its B rows
+__host__ __device__ inline size_t enc_stage_bytes(int k1p, int rpt) {
+    return size_t(enc_tile_rows(rpt)) * (k1p + 8) * sizeof(op16);
+}
+__host__ __device__ inline size_t enc_buf_bytes(int C, int k1p, int rpt) {
+    size_t fb = size_t(enc_tile_rows(rpt)) * (C + 4) * sizeof(float);
+    size_t xb = enc_stage_bytes(k1p, rpt) + size_t(enc_tile_rows(rpt)) * kEncBStride * sizeof(float);
+    const size_t m = fb > xb ? fb : xb;
+    return (m + 15) / 16 * 16;
+}
+__host__ __device__ inline size_t enc_smem_bytes(int C, int k1p, int rpt) {
+    return size_t(C) * kMaxBasis * sizeof(float) + 2 * enc_buf_bytes(C, k1p, rpt);
 }
 
 // WbT[c, o] = Wb[o, c] for o < F, 0 up to kMaxBasis: the layout the basis pass
@@ -859,93 +905,131 @@ __global__ void transpose_basis_kernel(const float* __restrict__ Wb, int F, int 
     WbT[i] = o < F ? Wb[o * C + c] : 0.f;
 }
 
-__global__ void __launch_bounds__(kBasisThreads)
+template <int RPT>
+__global__ void __launch_bounds__(kEncThreads)
     basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ WbT, int F,
-                        const float* __restrict__ view, int64_t M, int lf, int lv, int k1p, float* B, op16* x,
+                        const float* __restrict__ view, int64_t M, int lf, int lv, int k1, int k1p, float* B, op16* x,
                         int fmt) {
-    extern __shared__ float bsm[];
-    float* sWt = bsm;                                          // C x kMaxBasis (Wb^T, zero-padded)
-    float* sF = bsm + C * kMaxBasis;                           // kBasisRows x (C + 1), then the 16-bit rows
-    op16* srow = reinterpret_cast<op16*>(sF);                  // kBasisRows x (k1p + 2)
-    const int stride = k1p + 2;
-    const int64_t row0 = int64_t(blockIdx.x) * kBasisRows;
-    const int64_t rows = M - row0 < kBasisRows ? M - row0 : kBasisRows;
+    extern __shared__ __align__(16) float esm[];
+    constexpr int T = 16 * RPT;
+    float* sWt = esm;                                          // C x kMaxBasis
+    const size_t buf_words = enc_buf_bytes(C, k1p, RPT) / sizeof(float);
+    float* bufs = esm + size_t(C) * kMaxBasis;
+    const int S = C + 4, XS = k1p + 8;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t ntiles = (M + T - 1) / T;
     {
         const float4* src = reinterpret_cast<const float4*>(WbT);
         float4* dst = reinterpret_cast<float4*>(sWt);
-        for (int i = threadIdx.x; i < C * kMaxBasis / 4; i += blockDim.x) dst[i] = src[i];
+        for (int i = tid; i < C * kMaxBasis / 4; i += kEncThreads) dst[i] = src[i];
     }
-    {   // warp w copies rows w, w + nwarps, ... (lanes along the row: coalesced, no division)
-        const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-        const float* gf = feats + row0 * C;
-        for (int rr = threadIdx.x >> 5; rr < rows; rr += nw) {
-            const float* g = gf + int64_t(rr) * C;
-            float* d = sF + rr * (C + 1);
-#pragma unroll 4
-            for (int c = lane; c < C; c += 32) d[c] = g[c];
-        }
-    }
-    __syncthreads();
-    const int rg = threadIdx.x >> 3, cg = threadIdx.x & 7;   // rows rg*4.., columns cg*4..
-    float acc[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-    const float* f0 = sF + (rg * 4) * (C + 1);
-    for (int c = 0; c < C; ++c) {
-        const float4 wv = *reinterpret_cast<const float4*>(sWt + c * kMaxBasis + cg * 4);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const float fv = f0[i * (C + 1) + c];
-            acc[i][0] += fv * wv.x;
-            acc[i][1] += fv * wv.y;
-            acc[i][2] += fv * wv.z;
-            acc[i][3] += fv * wv.w;
-        }
-    }
-    __syncthreads();   // the row area becomes the staging of the encoded rows
-    for (int i = threadIdx.x; i < kBasisRows * stride / 2; i += blockDim.x) reinterpret_cast<uint32_t*>(srow)[i] = 0u;
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int r = rg * 4 + i;
-        if (r >= rows) break;
-        const int64_t m = row0 + r;
-        op16* my = srow + r * stride;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int o = cg * 4 + j;
-            if (o >= F) break;
-            const float v = acc[i][j];
-            B[m * F + o] = v;
-            my[o] = tc::to16(v, fmt);
-            for (int k = 0; k < lf; ++k) {
-                float sn, cs;
-                sincosf(v * float(1 << k), &sn, &cs);
-                my[F + 2 * k * F + o] = tc::to16(sn, fmt);
-                my[F + (2 * k + 1) * F + o] = tc::to16(cs, fmt);
+    // asynchronous copy of tile t's feature rows into buffer b (nothing past the last tile)
+    auto issue = [&](int64_t t, int b) {
+        if (t < ntiles) {
+            const int64_t r0 = t * T;
+            const int rows = M - r0 < T ? int(M - r0) : T;
+            float* dst = bufs + b * buf_words;
+            for (int r = warp; r < rows; r += kEncThreads / 32) {
+                const float* g = feats + (r0 + r) * C;
+                for (int q = lane; q < C / 4; q += 32) cp_async16(dst + r * S + 4 * q, g + 4 * q);
             }
         }
-        if (view && cg == 0) {
-            const int v0 = F * (2 * lf + 1);
-            for (int a = 0; a < 3; ++a) {
-                const float q = view[m * 3 + a];
-                my[v0 + a] = tc::to16(q, fmt);
-                for (int k = 0; k < lv; ++k) {
-                    float sn, cs;
-                    sincosf(q * float(1 << k), &sn, &cs);
-                    my[v0 + 3 + 6 * k + a] = tc::to16(sn, fmt);
-                    my[v0 + 6 + 6 * k + a] = tc::to16(cs, fmt);
+        cp_async_commit();
+    };
+    int64_t tile = blockIdx.x;
+    issue(tile, 0);
+    issue(tile + gridDim.x, 1);
+    const int rg = tid >> 3, cg = tid & 7;
+    const float4* w4 = reinterpret_cast<const float4*>(sWt) + cg;   // + c * (kMaxBasis / 4)
+    for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+        const int b = k & 1;
+        float* buf = bufs + b * buf_words;
+        const int64_t row0 = tile * T;
+        const int rows = M - row0 < T ? int(M - row0) : T;
+        cp_async_wait_one();
+        __syncthreads();
+        float acc[RPT][4];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        const float* f0 = buf + rg * S;
+        for (int c = 0; c < C; c += 4) {
+            const float4 wa = w4[(c + 0) * (kMaxBasis / 4)], wb = w4[(c + 1) * (kMaxBasis / 4)];
+            const float4 wc = w4[(c + 2) * (kMaxBasis / 4)], wd = w4[(c + 3) * (kMaxBasis / 4)];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const float4 f = *reinterpret_cast<const float4*>(f0 + 16 * i * S + c);
+                ffma2(acc[i][0], acc[i][1], f.x, wa.x, wa.y);
+                ffma2(acc[i][2], acc[i][3], f.x, wa.z, wa.w);
+                ffma2(acc[i][0], acc[i][1], f.y, wb.x, wb.y);
+                ffma2(acc[i][2], acc[i][3], f.y, wb.z, wb.w);
+                ffma2(acc[i][0], acc[i][1], f.z, wc.x, wc.y);
+                ffma2(acc[i][2], acc[i][3], f.z, wc.z, wc.w);
+                ffma2(acc[i][0], acc[i][1], f.w, wd.x, wd.y);
+                ffma2(acc[i][2], acc[i][3], f.w, wd.z, wd.w);
+            }
+        }
+        __syncthreads();   // the tile buffer becomes the staging + B tile
+        op16* stage = reinterpret_cast<op16*>(buf);
+        float* sB = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(buf) + enc_stage_bytes(k1p, RPT));
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            const int r = rg + 16 * i;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) sB[r * kEncBStride + cg * 4 + j] = acc[i][j];
+        }
+        __syncthreads();
+        const int v0 = F * (2 * lf + 1);
+        for (int r = warp; r < rows; r += kEncThreads / 32) {
+            const int64_t m = row0 + r;
+            op16* my = stage + r * XS;
+            if (lane < F) {
+                const float v = sB[r * kEncBStride + lane];
+                B[m * F + lane] = v;
+                my[lane] = tc::to16(v, fmt);
+                float sn, cs;
+                sincosf(v, &sn, &cs);
+                for (int q = 0; q < lf; ++q) {
+                    my[F + 2 * q * F + lane] = tc::to16(sn, fmt);
+                    my[F + (2 * q + 1) * F + lane] = tc::to16(cs, fmt);
+                    const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
+                    sn = s2;
+                    cs = c2;
                 }
             }
+            if (view) {
+                const int a = lane - (F <= 29 ? F : 0);   // lanes F .. F + 2, or 0 .. 2 past 29 features
+                if (F > 29) __syncwarp();
+                if (a >= 0 && a < 3) {
+                    const float vq = view[m * 3 + a];
+                    my[v0 + a] = tc::to16(vq, fmt);
+                    float sn, cs;
+                    sincosf(vq, &sn, &cs);
+                    for (int q = 0; q < lv; ++q) {
+                        my[v0 + 3 + 6 * q + a] = tc::to16(sn, fmt);
+                        my[v0 + 6 + 6 * q + a] = tc::to16(cs, fmt);
+                        const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
+                        sn = s2;
+                        cs = c2;
+                    }
+                }
+            }
+            for (int c = k1 + lane; c < k1p; c += 32) my[c] = op16(0);
         }
+        __syncthreads();
+        {
+            const int nq = k1p / 8;
+            for (int r = warp; r < rows; r += kEncThreads / 32) {
+                const uint4* src = reinterpret_cast<const uint4*>(stage + r * XS);
+                uint4* dst = reinterpret_cast<uint4*>(x + (row0 + r) * k1p);
+                for (int q = lane; q < nq; q += 32) dst[q] = src[q];
+            }
+        }
+        __syncthreads();   // staging consumed: the buffer takes tile + 2 grid
+        issue(tile + 2 * int64_t(gridDim.x), b);
     }
-    __syncthreads();
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(srow);
-    const int wx = k1p / 2, ws = stride / 2;
-    uint32_t* gx = reinterpret_cast<uint32_t*>(x + row0 * k1p);
-    for (int w = threadIdx.x; w < rows * wx; w += blockDim.x) gx[w] = src[(w / wx) * ws + w % wx];
+    cp_async_wait_all();
 }
 
 // Basis-layer backward fused with the PE adjoint, over a contiguous range of rows
@@ -959,16 +1043,6 @@ __global__ void __launch_bounds__(kBasisThreads)
 // the arithmetic of tile t.  Thread c owns feature column c, with its Wb column
 // and its dWb accumulators in registers; dB rows are shared-memory broadcasts.
 constexpr int kBwdTile = 32;
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // shared bytes of one tile buffer: feature rows, dx rows, B rows (16-byte multiples)
 __host__ __device__ inline size_t basis_tile_bytes(int C, int F, int k1p) {
@@ -1037,11 +1111,14 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
                 };
                 const float bo = sB[rr * F + o];
                 g = rd(o);
+                float sn, cs;   // sin, cos of 2^k B by the double-angle recurrence
+                sincosf(bo, &sn, &cs);
                 for (int k = 0; k < lf; ++k) {
                     const float fk = float(1 << k);
-                    float sn, cs;
-                    sincosf(bo * fk, &sn, &cs);
                     g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
+                    const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
+                    sn = s2;
+                    cs = c2;
                 }
                 g *= unscale;
             }
@@ -1051,17 +1128,17 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
         if (c < C) {
             for (int rr = 0; rr < nt; ++rr) {
                 const float f = sF[rr * C + c];
-                float dfe = 0.f;
+                float de = 0.f, dd = 0.f;   // even / odd basis columns of dB . Wb
 #pragma unroll
                 for (int o4 = 0; o4 < kMaxBasis; o4 += 4) {
+                    if (o4 >= F) break;
                     const float4 d = *reinterpret_cast<const float4*>(sdB + rr * kMaxBasis + o4);
-                    dfe += d.x * wcol[o4] + d.y * wcol[o4 + 1] + d.z * wcol[o4 + 2] + d.w * wcol[o4 + 3];
-                    acc[o4] += d.x * f;
-                    acc[o4 + 1] += d.y * f;
-                    acc[o4 + 2] += d.z * f;
-                    acc[o4 + 3] += d.w * f;
+                    fma2v(de, dd, d.x, d.y, wcol[o4], wcol[o4 + 1]);
+                    fma2v(de, dd, d.z, d.w, wcol[o4 + 2], wcol[o4 + 3]);
+                    ffma2(acc[o4], acc[o4 + 1], f, d.x, d.y);
+                    ffma2(acc[o4 + 2], acc[o4 + 3], f, d.z, d.w);
                 }
-                d_feats[(t0 + rr) * C + c] = dfe;
+                d_feats[(t0 + rr) * C + c] = de + dd;
             }
         }
         __syncthreads();   // buffer `buf` and sdB are rewritten next round
@@ -1082,6 +1159,41 @@ size_t render_tc_workspace(int C, int F, int U, int lf, int lv, int view, int64_
     return carve_render(R, m, bwd, nullptr, ~size_t(0), nullptr);
 }
 
+template <int RPT>
+int launch_basis_encode_rpt(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
+                            int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
+    const size_t smem = enc_smem_bytes(C, k1p, RPT);
+    cudaError_t e = cudaFuncSetAttribute(basis_encode_kernel<RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem));
+    int per_sm = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_encode_kernel<RPT>, kEncThreads, smem);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    const int64_t tiles = (m + enc_tile_rows(RPT) - 1) / enc_tile_rows(RPT);
+    int64_t grid = int64_t(num_sms()) * (per_sm > 0 ? per_sm : 1);
+    if (grid > tiles) grid = tiles;
+    basis_encode_kernel<RPT><<<unsigned(grid), kEncThreads, smem, s>>>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B,
+                                                                       x, fmt);
+    return launch_status();
+}
+
+// The basis + encoding pass with the deepest tile (4, 2 or 1 rows per thread) whose
+// shared memory fits.
+int launch_basis_encode(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
+                        int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
+    if (m <= 0) return SRF_OK;
+    if (enc_smem_bytes(C, k1p, 4) <= tc::kMaxSmem)
+        return launch_basis_encode_rpt<4>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+    if (enc_smem_bytes(C, k1p, 2) <= tc::kMaxSmem)
+        return launch_basis_encode_rpt<2>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+    if (enc_smem_bytes(C, k1p, 1) <= tc::kMaxSmem)
+        return launch_basis_encode_rpt<1>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+    return SRF_ERR_UNSUPPORTED;
+}
+
 // P = {Wb (F x C), W1 (U x k1), b1, W2 (U x U), b2, W3 (3 x U), b3}
 int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float* const* P, const float* feats,
                       const float* vdirs, int64_t m, float* rgb, bool bwd, void* ws, size_t ws_bytes, int fmt,
@@ -1094,21 +1206,12 @@ int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float
     int st;
     if ((st = pack(R.l1, P[1], w.W1, w.W1T, fmt, s))) return st;
     if ((st = pack(R.l2, P[3], w.W2, w.W2T, fmt, s))) return st;
-    const size_t smem = size_t(C) * kMaxBasis * sizeof(float) + basis_stage_bytes(C, R.k1p);
-    if (smem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(basis_encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(smem));
-        if (e != cudaSuccess) {
-            set_cuda_error(e);
-            return SRF_ERR_CUDA;
-        }
-    }
+    if (!aligned16(feats)) return SRF_ERR_ALIGN;
     transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
     if ((st = launch_status())) return st;
-    basis_encode_kernel<<<unsigned((m + kBasisRows - 1) / kBasisRows), kBasisThreads, smem, s>>>(
-        feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1p, w.B, w.x, fmt);
-    if ((st = launch_status())) return st;
+    if ((st = launch_basis_encode(feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x, fmt,
+                                  s)))
+        return st;
     if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
                         w.W1, R.k1p, U, 0, m, U, s)))
         return st;

@@ -243,7 +243,8 @@ class CompositeFunction(torch.autograd.Function):
     def forward(ctx, sigma, rgb, z, rays_d, rays_o, rays_d_ndc, flags, distance_scale, white_per_ray):
         n, s = sigma.shape
         _require(sigma, 'sigma', (n, s))
-        _require(rgb, 'rgb', (n, s, 3))
+        if rgb is not None:
+            _require(rgb, 'rgb', (n, s, 3))
         _require(z, 'z', (n, s))
         _require(rays_d, 'rays_d', (n, 3))
         ndc = bool(flags & _lib.SRF_COMPOSITE_NDC)
@@ -259,7 +260,7 @@ class CompositeFunction(torch.autograd.Function):
             out['depth_var_ndc'] = torch.empty(n, device=dev)
         a = _lib.CompositeArgs()
         a.n_rays, a.n_samples, a.flags, a.distance_scale = n, s, int(flags), float(distance_scale)
-        a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), rays_d.data_ptr()
+        a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), _ptr(rgb), z.data_ptr(), rays_d.data_ptr()
         if ndc:
             a.rays_o, a.rays_d_ndc = rays_o.data_ptr(), rays_d_ndc.data_ptr()
         if white_per_ray is not None:
@@ -281,7 +282,7 @@ class CompositeFunction(torch.autograd.Function):
         n, s = sigma.shape
         a = _lib.CompositeArgs()
         a.n_rays, a.n_samples, a.flags, a.distance_scale = n, s, ctx.flags, ctx.ds
-        a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), rays_d.data_ptr()
+        a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), _ptr(rgb), z.data_ptr(), rays_d.data_ptr()
         if ctx.flags & _lib.SRF_COMPOSITE_NDC:
             a.rays_o, a.rays_d_ndc = rays_o.data_ptr(), rays_d_ndc.data_ptr()
         if white is not None:
@@ -295,8 +296,8 @@ class CompositeFunction(torch.autograd.Function):
                 keep.append(g)
                 setattr(a, name, g.data_ptr())
         d_sigma = torch.empty_like(sigma)
-        d_rgb = torch.empty_like(rgb)
-        a.d_sigma, a.d_rgb = d_sigma.data_ptr(), d_rgb.data_ptr()
+        d_rgb = torch.empty_like(rgb) if rgb is not None and ctx.needs_input_grad[1] else None
+        a.d_sigma, a.d_rgb = d_sigma.data_ptr(), _ptr(d_rgb)
         call('srf_composite_backward', ctypes.byref(a), _stream())
         return d_sigma, d_rgb, None, None, None, None, None, None, None
 
@@ -327,7 +328,8 @@ def composite(sigma, rgb, z, rays_d, *, ndc=False, rays_o=None, rays_d_ndc=None,
     flags = (_lib.SRF_COMPOSITE_NDC if ndc else 0) | (_lib.SRF_COMPOSITE_WHITE_BKGD if white_bkgd else 0)
     if white_per_ray is not None:
         white_per_ray = white_per_ray.to(torch.uint8).contiguous()
-    outs = CompositeFunction.apply(sigma.contiguous(), rgb.contiguous(), z.contiguous(), rays_d.contiguous(),
+    outs = CompositeFunction.apply(sigma.contiguous(), None if rgb is None else rgb.contiguous(), z.contiguous(),
+                                   rays_d.contiguous(),
                                    None if rays_o is None else rays_o.contiguous(),
                                    None if rays_d_ndc is None else rays_d_ndc.contiguous(), flags, distance_scale,
                                    white_per_ray)

@@ -17,6 +17,8 @@ with the dense density evaluation on the VM density kernel.  The CP
 decomposition (``CpDecomposedTensor``, SimpleTensoRF09.py:964-1123) is
 ``GbCpTensor``: three lines per density/colour tensor on the CP lookup kernels.
 """
+import weakref
+
 import numpy
 import torch
 import torch.nn.functional as tF
@@ -36,6 +38,19 @@ def compute_resolution_in_voxels(num_voxels, bounding_box):
     lo, hi = bounding_box
     size = ((hi - lo).prod() / num_voxels).pow(1 / len(lo))
     return ((hi - lo) / size).long()
+
+
+def cached_host(owner, tag, t):
+    """The values of tensor ``t`` as a host list, re-read (one device sync) only when
+    ``t`` is a different tensor object or was modified in place since the last read:
+    the model's geometry buffers change only when the grid is resized or loaded."""
+    cache = owner.__dict__.setdefault('_host_cache', {})
+    hit = cache.get(tag)
+    if hit is not None and hit[0]() is t and hit[1] == t._version:
+        return hit[2]
+    val = t.detach().cpu().reshape(-1).tolist()
+    cache[tag] = (weakref.ref(t), t._version, val)
+    return val
 
 
 class AlphaGridMask(torch.nn.Module):
@@ -207,7 +222,7 @@ class GbVmTensor(torch.nn.Module):
         n, s = z.shape
         rows = n * s
         dev = z.device
-        bbox = self.bounding_box.detach().float().cpu().reshape(-1).tolist()
+        bbox = cached_host(self, 'bbox', self.bounding_box)
         pn = torch.empty(rows, 3, device=dev)
         mask = torch.empty(rows, dtype=torch.uint8, device=dev)
         vol = None
@@ -216,7 +231,7 @@ class GbVmTensor(torch.nn.Module):
         if self.alpha_mask is not None:
             vol = self.alpha_mask.volume()
             vd, vh, vw = vol.shape
-            abox = _lib.host_floats(self.alpha_mask.bounding_box.detach().float().cpu().reshape(-1).tolist())
+            abox = _lib.host_floats(cached_host(self.alpha_mask, 'bbox', self.alpha_mask.bounding_box))
         _lib.call('srf_tensorf_sample_mask', F._ptr(o.contiguous()), F._ptr(d.contiguous()), F._ptr(z.contiguous()),
                   n, s, _lib.host_floats(bbox), F._ptr(vol), vd, vh, vw, abox, F._ptr(pn), F._ptr(mask), F._stream())
         # density on the valid samples (uneven per ray): compact, gather, VM lookup
@@ -225,12 +240,10 @@ class GbVmTensor(torch.nn.Module):
         pv = T.gather_rows(pn, idx_v, cnt_v, nv)
         feat = self.density_features(pv) if nv else torch.zeros(0, device=dev)
         sigma = T.density_activation(feat, idx_v, cnt_v, rows, self.density_mode, self.density_offset).view(n, s)
-        flags = _lib.SRF_COMPOSITE_NDC if self.ndc else 0
-        zero_rgb = torch.zeros(n, s, 3, device=dev)
-        vr = F.composite(sigma, zero_rgb, z, input_dict['rays_d'], ndc=self.ndc, rays_o=input_dict['rays_o'],
+        # the density pass composites no colour (rgb None reads as zeros)
+        vr = F.composite(sigma, None, z, input_dict['rays_d'], ndc=self.ndc, rays_o=input_dict['rays_o'],
                          rays_d_ndc=input_dict.get('rays_d_ndc'),
                          distance_scale=self.tensor_configs['distance_scale'])
-        del flags
         out = {k: vr[k] for k in ('acc', 'alpha', 'visibility', 'weights', 'depth', 'depth_var')}
         if self.ndc:
             out['depth_ndc'], out['depth_var_ndc'] = vr['depth_ndc'], vr['depth_var_ndc']
@@ -271,6 +284,11 @@ class GbVmTensor(torch.nn.Module):
             out['raw_sigma'] = sigma[..., None]
             out['raw_rgb'] = rgb
         return out
+
+    def host_geometry(self):
+        """(bbox as 6 floats, num_samples, step_size) on the host, cached between resizes."""
+        return (cached_host(self, 'bbox', self.bounding_box), int(cached_host(self, 'num_samples', self.num_samples)[0]),
+                float(cached_host(self, 'step_size', self.step_size)[0]))
 
     def normalize_points(self, pts):
         """SimpleTensoRF09.py:763-765."""
@@ -633,7 +651,7 @@ class GbSimpleTensoRF(torch.nn.Module):
     def get_z_vals_coarse(self, input_dict, output_dict, tensor_model):
         """SimpleTensoRF09.py:353-401."""
         n = input_dict['pixel_id'].shape[0]
-        s = int(tensor_model.num_samples.item())
+        bbox, s, step = tensor_model.host_geometry()
         perturb = self.training and self.configs['model']['perturb']
         dev = input_dict['pixel_id'].device
         if self.ndc:
@@ -642,8 +660,7 @@ class GbSimpleTensoRF(torch.nn.Module):
             return F.stratified_z(n, s, near, far, u, lindisp=self.configs['model']['lindisp'], device=dev)
         near, far = self.model_configs['near'], self.model_configs['far']
         u = torch.rand(n, device=dev) if perturb else None
-        return F.aabb_z(output_dict['rays_o'], output_dict['rays_d'], s, tensor_model.bounding_box.detach().cpu(),
-                        near, far, float(tensor_model.step_size), u)
+        return F.aabb_z(output_dict['rays_o'], output_dict['rays_d'], s, bbox, near, far, step, u)
 
 
 # ModelFactory02 convention (class name = module name minus the two-digit suffix).
