@@ -404,6 +404,22 @@ int srf_rgb_depth_loss(const float* rgb, const float* target_rgb, const float* d
 int srf_adam_step(float* param, const float* grad, float* exp_avg, float* exp_avg_sq, int64_t n, float lr,
                   float beta1, float beta2, float eps, float weight_decay, int step, const int32_t* step_dev,
                   const int32_t* skip_dev, void* stream);
+/* One tensor of a multi-tensor Adam step (its own learning rate, as one param
+ * group of torch.optim.Adam). */
+typedef struct srf_adam_tensor {
+    float* param;
+    const float* grad;
+    float* exp_avg;
+    float* exp_avg_sq;
+    int64_t n;
+    float lr;
+} srf_adam_tensor;
+/* srf_adam_step over several tensors with one launch per 64 tensors (the same
+ * per-element arithmetic); tensors with n == 0 are skipped.  Replaces the
+ * optimizer step over a model's param groups (Trainer10.py:110,
+ * SimpleTensoRF09.py:1167-1194 groups). */
+int srf_adam_multi_step(const srf_adam_tensor* tensors, int n_tensors, float beta1, float beta2, float eps,
+                        float weight_decay, int step, const int32_t* step_dev, const int32_t* skip_dev, void* stream);
 /* Squared depth error with the matching gradients (accumulated into grad_pred and
  * grad_target, either may be NULL): with m_r = mask[r] (all ones when mask == NULL)
  * and count = n, or the number of masked rays when mean_over_mask,

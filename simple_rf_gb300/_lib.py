@@ -49,6 +49,10 @@ class TvComponent(ctypes.Structure):
                 ('stride_channel', c_int64), ('stride_height', c_int64), ('stride_width', c_int64)]
 
 
+class AdamTensor(ctypes.Structure):
+    _fields_ = [('param', P), ('grad', P), ('exp_avg', P), ('exp_avg_sq', P), ('n', c_int64), ('lr', c_float)]
+
+
 SRF_COMPOSITE_NDC = 1
 SRF_COMPOSITE_WHITE_BKGD = 2
 SRF_PRECISION_FP32 = 0
@@ -126,6 +130,8 @@ _SIGS = {
                                              c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
     'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
+    'srf_adam_multi_step': (c_int, [ctypes.POINTER(AdamTensor), c_int, c_float, c_float, c_float, c_float, c_int, P,
+                                    P, P]),
     'srf_launch_count': (c_int64, []),
 }
 

@@ -64,7 +64,7 @@ def synthetic_rays(n, seed, device):
 
 
 class TensorfTrainStep:
-    """forward (both models) -> rgb MSE -> backward -> Adam (srf_adam_step per tensor)."""
+    """forward (both models) -> rgb MSE -> backward -> Adam (one srf_adam_multi_step launch)."""
 
     def __init__(self, models, lr_tensor=0.02, lr_network=1e-3):
         self.models = models
@@ -93,12 +93,9 @@ class TensorfTrainStep:
             p.grad = None
         loss.backward()
         self.t += 1
-        st = F._stream()
-        for (p, lr), (m, v) in zip(self.params, self.state):
-            if p.grad is None:
-                continue
-            _lib.call('srf_adam_step', F._ptr(p.data), F._ptr(p.grad.contiguous(memory_format=_fmt(p))), F._ptr(m),
-                      F._ptr(v), p.numel(), lr, 0.9, 0.99, 1e-8, 0.0, self.t, None, None, st)
+        F.adam_multi_step([(p.data, p.grad.contiguous(memory_format=_fmt(p)), m, v, lr)
+                           for (p, lr), (m, v) in zip(self.params, self.state) if p.grad is not None],
+                          step=self.t, beta1=0.9, beta2=0.99, eps=1e-8)
         self.last = {'loss': loss.detach(), 'samples': counts}
         return loss
 

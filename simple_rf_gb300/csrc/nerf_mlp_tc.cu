@@ -845,17 +845,18 @@ __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wai
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // B = feats . Wb^T (FP32) and x = [PE(B, lf), PE(view, lv), 0...] in format fmt,
-// a persistent pass over tiles of 16 * RPT samples.  Each block keeps Wb transposed
+// a persistent pass over tiles of NT / 8 * RPT samples (NT threads; 128 threads x 2
+// rows, four blocks per SM, measured fastest for 144 components).  Each block keeps Wb transposed
 // (C x kMaxBasis, zero-padded) in shared memory and two feature-tile buffers (row
 // stride C + 4 words) filled by 16-byte asynchronous copies issued two tiles
 // ahead, so the loads of the next tile overlap the arithmetic of this one.
-// Product: thread t (128 per block) owns columns 4 (t % 8) .. +3 of rows t / 8 +
-// 16 i, i < RPT; per 4 inputs it reads one float4 of each of its rows and four
+// Product: thread t owns columns 4 (t % 8) .. +3 of rows t / 8 + (NT / 8) i, i <
+// RPT; per 4 inputs it reads one float4 of each of its rows and four
 // float4 weight rows (the four rows a warp touches fall in distinct banks) and
 // accumulates with packed two-lane FMAs (the same rounding as scalar FMAs, in
-// the same order).  Encoding: B goes through shared memory and a warp takes one
-// row at a time, lane f feature f (lanes F .. F + 2 the view direction): one
-// sincosf of the value, the 2^k multiples by the double-angle recurrence
+// the same order).  Encoding: B goes through shared memory and a warp takes two
+// rows at a time, lane f feature f (lanes F .. F + 2 the view direction): one
+// sincos16 of the value, the 2^k multiples by the double-angle recurrence
 // sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a) (fp32 error
 // ~ 2^k ulp, far below the 16-bit rounding of the output), written into the
 // consumed tile buffer as the 16-bit staging (row stride k1p + 8), which the
@@ -864,36 +865,52 @@ constexpr int kEncThreads = 128;
 
 // (d0, d1) += a * (b0, b1) with one packed two-lane FMA (fma.rn per lane)
 __device__ __forceinline__ void ffma2(float& d0, float& d1, float a, float b0, float b1) {
-    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
-        "mov.b64 pa, {%2, %2};\n\tmov.b64 pb, {%3, %4};\n\tmov.b64 pd, {%0, %1};\n\t"
-        "fma.rn.f32x2 pd, pa, pb, pd;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "+f"(d0), "+f"(d1)
-        : "f"(a), "f"(b0), "f"(b1));
+    const float2 r = __ffma2_rn(make_float2(a, a), make_float2(b0, b1), make_float2(d0, d1));
+    d0 = r.x;
+    d1 = r.y;
+}
+
+// sin and cos of x for the 16-bit encodings: x = k pi/2 + r, k = rint(x 2/pi), r
+// reduced with the two-term Cody-Waite split pi/2 = kPio2Hi + kPio2Lo (the first
+// product exact inside an FMA), |r| <= pi/4, then the hardware approximations on r
+// and the quadrant k mod 4.  Absolute error ~5e-7 (far below 16-bit rounding);
+// sincosf beyond |x| = 1e5, where k no longer fits the reduction's precision.
+constexpr float kPio2Hi = 1.57079637050628662109375f;        // pi/2 rounded to float
+constexpr float kPio2Lo = -4.37113900018624283e-8f;          // pi/2 - kPio2Hi
+__device__ __forceinline__ void sincos16(float x, float* s, float* c) {
+    if (!(fabsf(x) <= 1e5f)) {
+        sincosf(x, s, c);
+        return;
+    }
+    const float k = rintf(x * 0.636619772367581343f);
+    const float r = fmaf(-k, kPio2Lo, fmaf(-k, kPio2Hi, x));
+    const float sr = __sinf(r), cr = __cosf(r);
+    const int q = int(k) & 3;
+    *s = (q & 1) ? ((q & 2) ? -cr : cr) : ((q & 2) ? -sr : sr);
+    *c = (q & 1) ? ((q & 2) ? sr : -sr) : ((q & 2) ? -cr : cr);
 }
 
 // (d0, d1) += (a0, a1) * (b0, b1) with one packed two-lane FMA
 __device__ __forceinline__ void fma2v(float& d0, float& d1, float a0, float a1, float b0, float b1) {
-    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
-        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\tmov.b64 pd, {%0, %1};\n\t"
-        "fma.rn.f32x2 pd, pa, pb, pd;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "+f"(d0), "+f"(d1)
-        : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+    const float2 r = __ffma2_rn(make_float2(a0, a1), make_float2(b0, b1), make_float2(d0, d1));
+    d0 = r.x;
+    d1 = r.y;
 }
 
-__host__ __device__ inline int enc_tile_rows(int rpt) { return 16 * rpt; }
+__host__ __device__ inline int enc_tile_rows(int rpt, int nt) { return nt / 8 * rpt; }
 constexpr int kEncBStride = kMaxBasis + 1;   // row stride (words) of the B tile in shared memory
 // the 16-bit staging rows of a tile (16-byte multiple), followed by its B rows
-__host__ __device__ inline size_t enc_stage_bytes(int k1p, int rpt) {
-    return size_t(enc_tile_rows(rpt)) * (k1p + 8) * sizeof(op16);
+__host__ __device__ inline size_t enc_stage_bytes(int k1p, int rpt, int nt) {
+    return size_t(enc_tile_rows(rpt, nt)) * (k1p + 8) * sizeof(op16);
 }
-__host__ __device__ inline size_t enc_buf_bytes(int C, int k1p, int rpt) {
-    size_t fb = size_t(enc_tile_rows(rpt)) * (C + 4) * sizeof(float);
-    size_t xb = enc_stage_bytes(k1p, rpt) + size_t(enc_tile_rows(rpt)) * kEncBStride * sizeof(float);
+__host__ __device__ inline size_t enc_buf_bytes(int C, int k1p, int rpt, int nt) {
+    size_t fb = size_t(enc_tile_rows(rpt, nt)) * (C + 4) * sizeof(float);
+    size_t xb = enc_stage_bytes(k1p, rpt, nt) + size_t(enc_tile_rows(rpt, nt)) * kEncBStride * sizeof(float);
     const size_t m = fb > xb ? fb : xb;
     return (m + 15) / 16 * 16;
 }
-__host__ __device__ inline size_t enc_smem_bytes(int C, int k1p, int rpt) {
-    return size_t(C) * kMaxBasis * sizeof(float) + 2 * enc_buf_bytes(C, k1p, rpt);
+__host__ __device__ inline size_t enc_smem_bytes(int C, int k1p, int rpt, int nt) {
+    return size_t(C) * kMaxBasis * sizeof(float) + 2 * enc_buf_bytes(C, k1p, rpt, nt);
 }
 
 // WbT[c, o] = Wb[o, c] for o < F, 0 up to kMaxBasis: the layout the basis pass
@@ -905,15 +922,15 @@ __global__ void transpose_basis_kernel(const float* __restrict__ Wb, int F, int 
     WbT[i] = o < F ? Wb[o * C + c] : 0.f;
 }
 
-template <int RPT>
-__global__ void __launch_bounds__(kEncThreads)
+template <int RPT, int NT>
+__global__ void __launch_bounds__(NT)
     basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ WbT, int F,
                         const float* __restrict__ view, int64_t M, int lf, int lv, int k1, int k1p, float* B, op16* x,
                         int fmt) {
     extern __shared__ __align__(16) float esm[];
-    constexpr int T = 16 * RPT;
+    constexpr int RG = NT / 8, T = RG * RPT;                   // row groups, rows per tile
     float* sWt = esm;                                          // C x kMaxBasis
-    const size_t buf_words = enc_buf_bytes(C, k1p, RPT) / sizeof(float);
+    const size_t buf_words = enc_buf_bytes(C, k1p, RPT, NT) / sizeof(float);
     float* bufs = esm + size_t(C) * kMaxBasis;
     const int S = C + 4, XS = k1p + 8;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -921,7 +938,7 @@ __global__ void __launch_bounds__(kEncThreads)
     {
         const float4* src = reinterpret_cast<const float4*>(WbT);
         float4* dst = reinterpret_cast<float4*>(sWt);
-        for (int i = tid; i < C * kMaxBasis / 4; i += kEncThreads) dst[i] = src[i];
+        for (int i = tid; i < C * kMaxBasis / 4; i += NT) dst[i] = src[i];
     }
     // asynchronous copy of tile t's feature rows into buffer b (nothing past the last tile)
     auto issue = [&](int64_t t, int b) {
@@ -929,7 +946,7 @@ __global__ void __launch_bounds__(kEncThreads)
             const int64_t r0 = t * T;
             const int rows = M - r0 < T ? int(M - r0) : T;
             float* dst = bufs + b * buf_words;
-            for (int r = warp; r < rows; r += kEncThreads / 32) {
+            for (int r = warp; r < rows; r += NT / 32) {
                 const float* g = feats + (r0 + r) * C;
                 for (int q = lane; q < C / 4; q += 32) cp_async16(dst + r * S + 4 * q, g + 4 * q);
             }
@@ -948,79 +965,94 @@ __global__ void __launch_bounds__(kEncThreads)
         const int rows = M - row0 < T ? int(M - row0) : T;
         cp_async_wait_one();
         __syncthreads();
-        float acc[RPT][4];
+        float2 acc[RPT][2];
 #pragma unroll
-        for (int i = 0; i < RPT; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        for (int i = 0; i < RPT; ++i) acc[i][0] = acc[i][1] = make_float2(0.f, 0.f);
         const float* f0 = buf + rg * S;
         for (int c = 0; c < C; c += 4) {
             const float4 wa = w4[(c + 0) * (kMaxBasis / 4)], wb = w4[(c + 1) * (kMaxBasis / 4)];
             const float4 wc = w4[(c + 2) * (kMaxBasis / 4)], wd = w4[(c + 3) * (kMaxBasis / 4)];
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
-                const float4 f = *reinterpret_cast<const float4*>(f0 + 16 * i * S + c);
-                ffma2(acc[i][0], acc[i][1], f.x, wa.x, wa.y);
-                ffma2(acc[i][2], acc[i][3], f.x, wa.z, wa.w);
-                ffma2(acc[i][0], acc[i][1], f.y, wb.x, wb.y);
-                ffma2(acc[i][2], acc[i][3], f.y, wb.z, wb.w);
-                ffma2(acc[i][0], acc[i][1], f.z, wc.x, wc.y);
-                ffma2(acc[i][2], acc[i][3], f.z, wc.z, wc.w);
-                ffma2(acc[i][0], acc[i][1], f.w, wd.x, wd.y);
-                ffma2(acc[i][2], acc[i][3], f.w, wd.z, wd.w);
+                const float4 f = *reinterpret_cast<const float4*>(f0 + RG * i * S + c);
+                const float2 fx = make_float2(f.x, f.x), fy = make_float2(f.y, f.y);
+                const float2 fz = make_float2(f.z, f.z), fw = make_float2(f.w, f.w);
+                acc[i][0] = __ffma2_rn(fx, make_float2(wa.x, wa.y), acc[i][0]);
+                acc[i][1] = __ffma2_rn(fx, make_float2(wa.z, wa.w), acc[i][1]);
+                acc[i][0] = __ffma2_rn(fy, make_float2(wb.x, wb.y), acc[i][0]);
+                acc[i][1] = __ffma2_rn(fy, make_float2(wb.z, wb.w), acc[i][1]);
+                acc[i][0] = __ffma2_rn(fz, make_float2(wc.x, wc.y), acc[i][0]);
+                acc[i][1] = __ffma2_rn(fz, make_float2(wc.z, wc.w), acc[i][1]);
+                acc[i][0] = __ffma2_rn(fw, make_float2(wd.x, wd.y), acc[i][0]);
+                acc[i][1] = __ffma2_rn(fw, make_float2(wd.z, wd.w), acc[i][1]);
             }
         }
         __syncthreads();   // the tile buffer becomes the staging + B tile
         op16* stage = reinterpret_cast<op16*>(buf);
-        float* sB = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(buf) + enc_stage_bytes(k1p, RPT));
+        float* sB = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(buf) + enc_stage_bytes(k1p, RPT, NT));
 #pragma unroll
         for (int i = 0; i < RPT; ++i) {
-            const int r = rg + 16 * i;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) sB[r * kEncBStride + cg * 4 + j] = acc[i][j];
+            float* d = sB + (rg + RG * i) * kEncBStride + cg * 4;
+            d[0] = acc[i][0].x;
+            d[1] = acc[i][0].y;
+            d[2] = acc[i][1].x;
+            d[3] = acc[i][1].y;
         }
         __syncthreads();
+        // lane roles: feature f = lane (f < F), view component a (lanes F .. F + 2, or a
+        // second pass on lanes 0 .. 2 when F > 29); each writes its value, then sin and
+        // cos of 2^q value at columns c_sin + q dq and c_sin + q dq + dcos
         const int v0 = F * (2 * lf + 1);
-        for (int r = warp; r < rows; r += kEncThreads / 32) {
-            const int64_t m = row0 + r;
-            op16* my = stage + r * XS;
-            if (lane < F) {
-                const float v = sB[r * kEncBStride + lane];
-                B[m * F + lane] = v;
-                my[lane] = tc::to16(v, fmt);
-                float sn, cs;
-                sincosf(v, &sn, &cs);
-                for (int q = 0; q < lf; ++q) {
-                    my[F + 2 * q * F + lane] = tc::to16(sn, fmt);
-                    my[F + (2 * q + 1) * F + lane] = tc::to16(cs, fmt);
-                    const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
-                    sn = s2;
-                    cs = c2;
-                }
+        const bool view_here = view && F <= 29;
+        for (int pass = 0; pass < ((view && F > 29) ? 2 : 1); ++pass) {
+            int kind = 0, col = 0, csin = 0, dq = 0, dcos = 0, deg = 0;   // kind 1: feature, 2: view
+            if (pass == 0 && lane < F) {
+                kind = 1; col = lane; csin = F + lane; dq = 2 * F; dcos = F; deg = lf;
+            } else if (view && ((pass == 0 && view_here && lane >= F && lane < F + 3) || (pass == 1 && lane < 3))) {
+                const int a = pass == 0 ? lane - F : lane;
+                kind = 2; col = v0 + a; csin = v0 + 3 + a; dq = 6; dcos = 3; deg = lv;
             }
-            if (view) {
-                const int a = lane - (F <= 29 ? F : 0);   // lanes F .. F + 2, or 0 .. 2 past 29 features
-                if (F > 29) __syncwarp();
-                if (a >= 0 && a < 3) {
-                    const float vq = view[m * 3 + a];
-                    my[v0 + a] = tc::to16(vq, fmt);
-                    float sn, cs;
-                    sincosf(vq, &sn, &cs);
-                    for (int q = 0; q < lv; ++q) {
-                        my[v0 + 3 + 6 * q + a] = tc::to16(sn, fmt);
-                        my[v0 + 6 + 6 * q + a] = tc::to16(cs, fmt);
-                        const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
-                        sn = s2;
-                        cs = c2;
+            const int a_view = col - v0;
+            for (int r0 = warp; r0 < rows; r0 += 2 * (NT / 32)) {
+                const int r1 = r0 + NT / 32;
+                const bool two = r1 < rows;
+                float v[2] = {0.f, 0.f};
+                if (kind == 1) {
+                    v[0] = sB[r0 * kEncBStride + lane];
+                    if (two) v[1] = sB[r1 * kEncBStride + lane];
+                } else if (kind == 2) {
+                    v[0] = view[(row0 + r0) * 3 + a_view];
+                    if (two) v[1] = view[(row0 + r1) * 3 + a_view];
+                }
+                float sn[2], cs[2];
+                sincos16(v[0], &sn[0], &cs[0]);
+                sincos16(v[1], &sn[1], &cs[1]);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int r = h ? r1 : r0;
+                    if (kind == 0 || (h && !two)) continue;
+                    op16* my = stage + r * XS;
+                    if (kind == 1) B[(row0 + r) * F + lane] = v[h];
+                    my[col] = tc::to16(v[h], fmt);
+                    float sh = sn[h], ch = cs[h];
+                    for (int q = 0; q < deg; ++q) {
+                        my[csin + q * dq] = tc::to16(sh, fmt);
+                        my[csin + q * dq + dcos] = tc::to16(ch, fmt);
+                        const float s2 = 2.f * sh * ch, c2 = (ch - sh) * (ch + sh);
+                        sh = s2;
+                        ch = c2;
                     }
                 }
             }
+        }
+        for (int r = warp; r < rows; r += NT / 32) {
+            op16* my = stage + r * XS;
             for (int c = k1 + lane; c < k1p; c += 32) my[c] = op16(0);
         }
         __syncthreads();
         {
             const int nq = k1p / 8;
-            for (int r = warp; r < rows; r += kEncThreads / 32) {
+            for (int r = warp; r < rows; r += NT / 32) {
                 const uint4* src = reinterpret_cast<const uint4*>(stage + r * XS);
                 uint4* dst = reinterpret_cast<uint4*>(x + (row0 + r) * k1p);
                 for (int q = lane; q < nq; q += 32) dst[q] = src[q];
@@ -1112,7 +1144,7 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
                 const float bo = sB[rr * F + o];
                 g = rd(o);
                 float sn, cs;   // sin, cos of 2^k B by the double-angle recurrence
-                sincosf(bo, &sn, &cs);
+                sincos16(bo, &sn, &cs);
                 for (int k = 0; k < lf; ++k) {
                     const float fk = float(1 << k);
                     g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
@@ -1159,38 +1191,35 @@ size_t render_tc_workspace(int C, int F, int U, int lf, int lv, int view, int64_
     return carve_render(R, m, bwd, nullptr, ~size_t(0), nullptr);
 }
 
-template <int RPT>
-int launch_basis_encode_rpt(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
+template <int RPT, int NT>
+int launch_basis_encode_cfg(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
                             int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
-    const size_t smem = enc_smem_bytes(C, k1p, RPT);
-    cudaError_t e = cudaFuncSetAttribute(basis_encode_kernel<RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = enc_smem_bytes(C, k1p, RPT, NT);
+    cudaError_t e = cudaFuncSetAttribute(basis_encode_kernel<RPT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(smem));
     int per_sm = 0;
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_encode_kernel<RPT>, kEncThreads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_encode_kernel<RPT, NT>, NT, smem);
     if (e != cudaSuccess) {
         set_cuda_error(e);
         return SRF_ERR_CUDA;
     }
-    const int64_t tiles = (m + enc_tile_rows(RPT) - 1) / enc_tile_rows(RPT);
+    const int64_t tiles = (m + enc_tile_rows(RPT, NT) - 1) / enc_tile_rows(RPT, NT);
     int64_t grid = int64_t(num_sms()) * (per_sm > 0 ? per_sm : 1);
     if (grid > tiles) grid = tiles;
-    basis_encode_kernel<RPT><<<unsigned(grid), kEncThreads, smem, s>>>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B,
-                                                                       x, fmt);
+    basis_encode_kernel<RPT, NT><<<unsigned(grid), NT, smem, s>>>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x,
+                                                                  fmt);
     return launch_status();
 }
 
-// The basis + encoding pass with the deepest tile (4, 2 or 1 rows per thread) whose
-// shared memory fits.
+// The basis + encoding pass with the deepest tile whose shared memory fits.
 int launch_basis_encode(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
                         int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
     if (m <= 0) return SRF_OK;
-    if (enc_smem_bytes(C, k1p, 4) <= tc::kMaxSmem)
-        return launch_basis_encode_rpt<4>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
-    if (enc_smem_bytes(C, k1p, 2) <= tc::kMaxSmem)
-        return launch_basis_encode_rpt<2>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
-    if (enc_smem_bytes(C, k1p, 1) <= tc::kMaxSmem)
-        return launch_basis_encode_rpt<1>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+    if (enc_smem_bytes(C, k1p, 2, kEncThreads) <= tc::kMaxSmem)
+        return launch_basis_encode_cfg<2, kEncThreads>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+    if (enc_smem_bytes(C, k1p, 1, kEncThreads) <= tc::kMaxSmem)
+        return launch_basis_encode_cfg<1, kEncThreads>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
     return SRF_ERR_UNSUPPORTED;
 }
 

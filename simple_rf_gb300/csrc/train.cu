@@ -38,6 +38,20 @@ __global__ void loss_kernel(const float* __restrict__ rgb, const float* __restri
     }
 }
 
+__device__ __forceinline__ void adam_update(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                                            float* __restrict__ v, int64_t i, float lr, float b1, float b2, float eps,
+                                            float wd, float bc1, float bc2_sqrt) {
+    // every rounding spelled out, so each kernel that inlines this computes the same bits
+    float gi = g[i];
+    if (wd != 0.f) gi = __fmaf_rn(wd, p[i], gi);
+    const float mi = __fmaf_rn(b1, m[i], __fmul_rn(1.f - b1, gi));
+    const float vi = __fmaf_rn(b2, v[i], __fmul_rn(__fmul_rn(1.f - b2, gi), gi));
+    m[i] = mi;
+    v[i] = vi;
+    const float denom = __fadd_rn(__fdiv_rn(__fsqrt_rn(vi), bc2_sqrt), eps);
+    p[i] = __fsub_rn(p[i], __fdiv_rn(__fmul_rn(__fdiv_rn(lr, bc1), mi), denom));
+}
+
 // torch.optim.Adam (foreach=False math): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
 // p -= lr / (1 - b1^t) * m / (sqrt(v) / sqrt(1 - b2^t) + eps).  With step_dev the
 // step count t is read on the device (graph replays advance it with srf_counter_add).
@@ -52,15 +66,44 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
         bc1 = 1.f - powf(b1, t);
         bc2_sqrt = sqrtf(1.f - powf(b2, t));
     }
-    for (; i < n; i += stride) {
-        float gi = g[i];
-        if (wd != 0.f) gi += wd * p[i];
-        float mi = b1 * m[i] + (1.f - b1) * gi;
-        float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-        m[i] = mi;
-        v[i] = vi;
-        float denom = sqrtf(vi) / bc2_sqrt + eps;
-        p[i] -= (lr / bc1) * mi / denom;
+    for (; i < n; i += stride) adam_update(p, g, m, v, i, lr, b1, b2, eps, wd, bc1, bc2_sqrt);
+}
+
+// Several tensors in one launch: tensor k covers chunks [chunk0, chunk0 + ceil(n /
+// kAdamChunk)) of a common chunk index space, which the blocks stride over.
+constexpr int kMaxAdamTensors = 64;
+constexpr int64_t kAdamChunk = 8192;
+struct AdamTensor {
+    float* p;
+    const float* g;
+    float* m;
+    float* v;
+    int64_t n;
+    float lr;
+    int64_t chunk0;
+};
+struct AdamBatch {
+    AdamTensor t[kMaxAdamTensors];
+    int count;
+    int64_t chunks;
+};
+
+__global__ void adam_multi_kernel(const __grid_constant__ AdamBatch b, float b1, float b2, float eps, float wd,
+                                  float bc1, float bc2_sqrt, const int* step_dev, const int* skip_dev) {
+    if (skip_dev && *skip_dev) return;
+    if (step_dev) {
+        float t = float(*step_dev);
+        bc1 = 1.f - powf(b1, t);
+        bc2_sqrt = sqrtf(1.f - powf(b2, t));
+    }
+    int k = 0;
+    for (int64_t ch = blockIdx.x; ch < b.chunks; ch += gridDim.x) {
+        while (k + 1 < b.count && b.t[k + 1].chunk0 <= ch) ++k;
+        const AdamTensor& t = b.t[k];
+        const int64_t i0 = (ch - t.chunk0) * kAdamChunk;
+        const int64_t i1 = i0 + kAdamChunk < t.n ? i0 + kAdamChunk : t.n;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+            adam_update(t.p, t.g, t.m, t.v, i, t.lr, b1, b2, eps, wd, bc1, bc2_sqrt);
     }
 }
 
@@ -498,6 +541,41 @@ extern "C" int srf_adam_step(float* param, const float* grad, float* exp_avg, fl
     adam_kernel<<<blocks, 256, 0, as_stream(stream)>>>(param, grad, exp_avg, exp_avg_sq, n, lr, beta1, beta2, eps,
                                                        weight_decay, bc1, bc2, step_dev, skip_dev);
     return launch_status();
+}
+
+extern "C" int srf_adam_multi_step(const srf_adam_tensor* tensors, int n_tensors, float beta1, float beta2, float eps,
+                                   float weight_decay, int step, const int32_t* step_dev, const int32_t* skip_dev,
+                                   void* stream) {
+    if (n_tensors < 0 || (step < 1 && !step_dev)) return SRF_ERR_SHAPE;
+    if (n_tensors == 0) return SRF_OK;
+    if (!tensors) return SRF_ERR_NULL;
+    for (int i = 0; i < n_tensors; ++i) {
+        const srf_adam_tensor& t = tensors[i];
+        if (t.n < 0) return SRF_ERR_SHAPE;
+        if (t.n > 0 && (!t.param || !t.grad || !t.exp_avg || !t.exp_avg_sq)) return SRF_ERR_NULL;
+    }
+    if (step < 1) step = 1;
+    const float bc1 = 1.f - powf(beta1, float(step));
+    const float bc2 = sqrtf(1.f - powf(beta2, float(step)));
+    int i = 0;   // next tensor: each launch takes up to kMaxAdamTensors non-empty ones
+    while (i < n_tensors) {
+        AdamBatch b = {};
+        int64_t chunks = 0;
+        for (; i < n_tensors && b.count < kMaxAdamTensors; ++i) {
+            const srf_adam_tensor& t = tensors[i];
+            if (t.n == 0) continue;
+            b.t[b.count++] = {t.param, t.grad, t.exp_avg, t.exp_avg_sq, t.n, t.lr, chunks};
+            chunks += (t.n + kAdamChunk - 1) / kAdamChunk;
+        }
+        if (!chunks) continue;
+        b.chunks = chunks;
+        unsigned blocks = unsigned(chunks < 152 * 8 ? chunks : 152 * 8);
+        adam_multi_kernel<<<blocks, 256, 0, as_stream(stream)>>>(b, beta1, beta2, eps, weight_decay, bc1, bc2,
+                                                                 step_dev, skip_dev);
+        int st = launch_status();
+        if (st) return st;
+    }
+    return SRF_OK;
 }
 
 extern "C" int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth1,

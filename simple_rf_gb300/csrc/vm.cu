@@ -259,6 +259,7 @@ __global__ void color_fwd_group_kernel(srf_vm_grid g, const float* __restrict__ 
         Taps pt, lt;
         plane_taps(g, i, q, pt, lt);
         const int R = g.n_comp[i];
+#pragma unroll 4
         for (int r = 4 * j; r < R; r += 4 * G) {
             float4 pv, lv;
             interp4(g.planes[i], g.lines[i], R, r, pt, lt, pv, lv);
@@ -284,6 +285,7 @@ __global__ void vm_bwd_group_kernel(srf_vm_grid gg, srf_vm_grid g, const float* 
         const int R = g.n_comp[i];
         float* gpl = gg.planes[i];
         float* gln = gg.lines[i];
+#pragma unroll 4
         for (int r = 4 * j; r < R; r += 4 * G) {
             const float4 d = per_component ? *reinterpret_cast<const float4*>(dfeat + p * ld + off + r)
                                            : make_float4(ds, ds, ds, ds);
@@ -308,16 +310,16 @@ __global__ void vm_bwd_group_kernel(srf_vm_grid gg, srf_vm_grid g, const float* 
     }
 }
 
-// Lanes per point for the group kernels: the smallest power of two >= max_i R_i / 4
-// (0 when some R_i is not a multiple of 4: use the per-thread kernels).
+// Lanes per point for the group kernels: the largest power of two (at most 16) that
+// divides every R_i / 4, so every lane of a group takes the same number of
+// four-component pieces (R = 48: 4 lanes x 3 pieces, each lane's loads independent
+// of one another); 0 when some R_i is not a multiple of 4 (per-thread kernels).
 int group_lanes(const srf_vm_grid& g) {
-    int mx = 0;
+    int G = 16;
     for (int i = 0; i < 3; ++i) {
         if (g.n_comp[i] & 3) return 0;
-        mx = g.n_comp[i] / 4 > mx ? g.n_comp[i] / 4 : mx;
+        while (G > 1 && (g.n_comp[i] / 4) % G) G >>= 1;
     }
-    int G = 1;
-    while (G < mx && G < 32) G <<= 1;
     return G;
 }
 

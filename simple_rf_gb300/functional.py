@@ -310,6 +310,26 @@ def adam_step(param, grad, exp_avg, exp_avg_sq, *, lr, beta1=0.9, beta2=0.999, e
          float(beta1), float(beta2), float(eps), float(weight_decay), int(step), None, None, _stream())
 
 
+def _dense(t):
+    return t.is_contiguous() or (t.dim() == 4 and t.is_contiguous(memory_format=torch.channels_last))
+
+
+def adam_multi_step(tensors, *, step, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
+    """In-place Adam over ``tensors`` = [(param, grad, exp_avg, exp_avg_sq, lr), ...]
+    with one launch per 64 tensors (each tensor's four buffers share one dense layout)."""
+    arr = (_lib.AdamTensor * len(tensors))()
+    for i, (p, g, m, v, lr) in enumerate(tensors):
+        for name, x in (('param', p), ('grad', g), ('exp_avg', m), ('exp_avg_sq', v)):
+            if not x.is_cuda or x.dtype != torch.float32:
+                raise RuntimeError(f'tensor {i} {name} must be a float32 CUDA tensor')
+            if x.shape != p.shape or x.stride() != p.stride() or not _dense(x):
+                raise RuntimeError(f'tensor {i} {name}: layout {tuple(x.shape)} {x.stride()} does not match the '
+                                   f'dense param {tuple(p.shape)} {p.stride()}')
+        arr[i] = _lib.AdamTensor(p.data_ptr(), g.data_ptr(), m.data_ptr(), v.data_ptr(), p.numel(), float(lr))
+    call('srf_adam_multi_step', arr, len(tensors), float(beta1), float(beta2), float(eps), float(weight_decay),
+         int(step), None, None, _stream())
+
+
 def rgb_depth_loss(rgb, target_rgb, depth, target_depth, depth_mask, n_depth_rays, depth_weight, loss=None):
     """Loss of one net's outputs and its gradients w.r.t. rgb (N,3) and depth (N,)."""
     n = rgb.shape[0]

@@ -199,7 +199,7 @@ class GbVmTensor(torch.nn.Module):
         for p in list(mats) + list(vecs):
             if not p.is_contiguous(memory_format=torch.channels_last):
                 p.data = T.to_channels_last(p.data)
-        return T.VmGridTensors(list(mats), list(vecs), [int(r) for r in self.resolution])
+        return T.VmGridTensors(list(mats), list(vecs), [int(r) for r in cached_host(self, 'res', self.resolution)])
 
     def get_trainable_parameters(self, optimizer_configs):
         """SimpleTensoRF09.py:1167-1194."""
@@ -444,10 +444,10 @@ class GbCpTensor(GbVmTensor):
         return list(lines)
 
     def density_features(self, pts):
-        return T.cp_density(self._lines('density'), self.resolution, pts)
+        return T.cp_density(self._lines('density'), cached_host(self, 'res', self.resolution), pts)
 
     def color_features(self, pts):
-        return T.cp_color(self._lines('color'), self.resolution, pts)
+        return T.cp_color(self._lines('color'), cached_host(self, 'res', self.resolution), pts)
 
     def tensor_parameters(self):
         """(:998-1026): density lines, then colour lines."""

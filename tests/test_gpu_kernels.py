@@ -288,6 +288,42 @@ def test_adam_matches_torch():
     np.testing.assert_allclose(n(ours), n(ref.detach()), rtol=1e-6, atol=1e-7)
 
 
+def test_adam_multi_step_matches_single_tensor_steps():
+    """70 tensors (two launches of at most 64), sizes from 0 to several chunks, one
+    channels-last plane, per-tensor learning rates: bitwise equal to srf_adam_step."""
+    from simple_rf_gb300 import functional as F
+    gen = torch.Generator().manual_seed(12)
+    shapes = [(0,), (1,), (8191,), (8192,), (8193,), (3, 50000)] + [(int(s),) for s in torch.randint(1, 3000, (63,),
+                                                                                                     generator=gen)]
+    shapes.append((1, 48, 37, 29))
+    params = []
+    for i, sh in enumerate(shapes):
+        p = torch.randn(*sh, generator=gen).to(DEV)
+        if len(sh) == 4:
+            p = p.contiguous(memory_format=torch.channels_last)
+        params.append(p)
+    multi = [p.clone() for p in params]
+    single = [p.clone() for p in params]
+    sm = [(torch.zeros_like(p), torch.zeros_like(p)) for p in params]
+    ss = [(torch.zeros_like(p), torch.zeros_like(p)) for p in params]
+    lrs = [1e-3 * (1 + i % 7) for i in range(len(params))]
+    for step in range(1, 4):
+        grads = [torch.randn(p.shape, generator=gen).to(DEV).contiguous(memory_format=torch.channels_last)
+                 if p.dim() == 4 else torch.randn(p.shape, generator=gen).to(DEV) for p in params]
+        F.adam_multi_step([(p, g, m, v, lr) for p, g, (m, v), lr in zip(multi, grads, sm, lrs)], step=step,
+                          beta1=0.9, beta2=0.99, eps=1e-8)
+        for p, g, (m, v), lr in zip(single, grads, ss, lrs):
+            if p.numel():
+                F.adam_step(p.view(-1) if p.dim() < 4 else p.permute(0, 2, 3, 1).reshape(-1),
+                            g.view(-1) if g.dim() < 4 else g.permute(0, 2, 3, 1).reshape(-1),
+                            m.view(-1) if m.dim() < 4 else m.permute(0, 2, 3, 1).reshape(-1),
+                            v.view(-1) if v.dim() < 4 else v.permute(0, 2, 3, 1).reshape(-1),
+                            lr=lr, beta1=0.9, beta2=0.99, eps=1e-8, step=step)
+    torch.cuda.synchronize()
+    for a, b in zip(multi, single):
+        assert torch.equal(a, b)
+
+
 def test_loss_kernel():
     from simple_rf_gb300 import functional as F
     rng = np.random.default_rng(10)
