@@ -62,7 +62,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), f'--query-gpu={self.FIELDS}',
-                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                          '--format=csv,noheader,nounits', '-lms', '50'],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -415,6 +415,8 @@ def run_ours(args):
         # the same warm-up and timed steps for both (surface-sample counts drift as the grids train)
         variants['tensorf_fp16'] = time_tensorf('fp16', 3, dev, stream)
         variants['tensorf_fp32'] = time_tensorf('fp32', 3, dev, stream)
+        from simple_rf_gb300.bench_tensorf import ray_batch_sweep
+        variants['tensorf_sweep'] = ray_batch_sweep(dev)
         variants['render'] = time_render(dev, stream)
     import ctypes
     fl = ctypes.c_int(0)
@@ -460,7 +462,8 @@ def run_ours(args):
                                 'alpha mask 128^3 at 15%, renderer PE L=2 -> 128 -> 128 -> 3',
                     'fp16': variants['tensorf_fp16'], 'fp32_plain': variants['tensorf_fp32'],
                     'speedup_fp16_vs_fp32_plain': round(variants['tensorf_fp16']['rays_per_s'] /
-                                                        variants['tensorf_fp32']['rays_per_s'], 2)},
+                                                        variants['tensorf_fp32']['rays_per_s'], 2),
+                    'ray_batch_sweep': variants['tensorf_sweep']},
         'render': dict(variants['render'], workload='8 views x 504x378 NDC rays, NeRF pair (main coarse+fine + '
                                                     'augmented coarse), 64+128 samples, chunks of 65536'),
         'device_flag': fl.value,

@@ -15,6 +15,7 @@ N(0, 0.3^2) per axis, near 2, far 6.  Loss: MSE of each model's rgb against
 targets ~ U[0,1]^3.
 
     python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3 [--precision fp16]
+    python -m simple_rf_gb300.bench_tensorf --sweep        # ray batches 1024 ... 65536
 """
 import argparse
 import json
@@ -105,6 +106,42 @@ def _fmt(p):
         torch.contiguous_format
 
 
+SWEEP_RAYS = (1024, 2048, 4096, 8192, 16384, 32768, 65536)
+
+
+def ray_batch_sweep(device, precisions=('fp16', 'fp32'), sizes=SWEEP_RAYS, warmup=2, steps=3, seed=0):
+    """Train rays/s of the same step over ray batches of 1024 ... 65536 rays: one model
+    pair per precision, trained on from size to size (each size gets its own warm-up),
+    rays drawn afresh per size."""
+    out = {}
+    for prec in precisions:
+        models = make_models(device, seed=seed, precision=prec)
+        st = TensorfTrainStep(models)
+        res = {}
+        for n in sizes:
+            batches = [synthetic_rays(n, 100 + i, device) for i in range(2)]
+            for i in range(warmup):
+                st.step(*batches[i % 2])
+            torch.cuda.synchronize(device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for i in range(steps):
+                st.step(*batches[i % 2])
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            res[str(n)] = {'ms_per_step': round(ms, 3), 'rays_per_s': round(n / ms * 1e3, 1),
+                           'surface_samples': int(st.last['samples'][0]['surface'])}
+            del batches
+        out[prec] = res
+        del st, models
+        torch.cuda.empty_cache()
+    if 'fp16' in out and 'fp32' in out:
+        out['speedup_fp16_vs_fp32_plain'] = {n: round(out['fp16'][n]['rays_per_s'] / out['fp32'][n]['rays_per_s'], 2)
+                                             for n in out['fp16']}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument('--rays', type=int, default=8192)
@@ -112,10 +149,15 @@ def main(argv=None):
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'bf16', 'fp16'],
                     help='renderer MLP: FP32 SIMT or 16-bit tensor cores')
+    ap.add_argument('--sweep', action='store_true', help='ray-batch sweep 1024 ... 65536, FP16 and FP32 plain')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
     dev = torch.device('cuda')
+    if args.sweep:
+        print(json.dumps({'workload': 'tensorf_vm_train_step_ray_batch_sweep_300^3+75^3',
+                          'sweep': ray_batch_sweep(dev)}))
+        return
     models = make_models(dev, precision=args.precision)
     step = TensorfTrainStep(models)
     batches = [synthetic_rays(args.rays, 10 + i, dev) for i in range(4)]
