@@ -126,7 +126,7 @@ def time_steps(step, k, stream):
     return start.elapsed_time(end) / 1000.0
 
 
-def roofline_gemm(dev, hbm_peak, peak_tflops, peak_kind, reps=20):
+def roofline_gemm(dev, hbm_peak, peak_tflops, peak_kind, reps=50):
     """The dominant kernel (tcgen05 layer GEMM, fine-net trunk shape) timed alone."""
     import ctypes
     import torch
@@ -371,8 +371,11 @@ def run_ours(args):
     for i in range(args.warmup):
         bf_step(i)
     barrier()
+    hbm_peak, tf_peak, peak_kind = peaks()
     with ClockSampler(local) as clocks:
         t_bf = time_steps(bf_step, args.steps, stream)
+        # the dominant kernel timed alone right after the step, under the same clock record
+        roof = roofline_gemm(dev, hbm_peak, tf_peak, peak_kind) if rank == 0 else None
     barrier()
     t_bf = max_over_ranks(t_bf)
     # rgb agreement of the BF16 step with the FP32 plain step (same weights, same batch)
@@ -422,8 +425,6 @@ def run_ours(args):
     fl = ctypes.c_int(0)
     _lib.check(_lib.load().srf_read_device_flag(ctypes.byref(fl), ctypes.c_void_p(stream.cuda_stream)), 'flag')
 
-    hbm_peak, tf_peak, peak_kind = peaks()
-    roof = roofline_gemm(dev, hbm_peak, tf_peak, peak_kind) if rank == 0 else None
     if rank != 0:
         if ws > 1:
             import torch.distributed as dist

@@ -67,16 +67,13 @@ int num_sms() {
 
 bool ok16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-template <int BN, int EW>
-int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
-                   tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
-    int kb = sh.kb0 + sh.kb1;
-    if (tc::SmemPlan<BN, EW>::stages(kb) < 2) return SRF_ERR_UNSUPPORTED;
-    size_t smem = tc::SmemPlan<BN, EW>::bytes(kb);
+template <int BN, int EW, int EPI>
+int launch_gemm_epi(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
+                    tc::GemmShape sh, tc::GemmEpilogue ep, size_t smem, cudaStream_t s) {
     static bool attr_done = false;
     if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(tc::tc_gemm_kernel<BN, EW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(tc::kMaxSmem));
+        cudaError_t e = cudaFuncSetAttribute(tc::tc_gemm_kernel<BN, EW, EPI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kMaxSmem));
         if (e != cudaSuccess) {
             set_cuda_error(e);
             return SRF_ERR_CUDA;
@@ -85,8 +82,24 @@ int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
     }
     int64_t tiles = (sh.M + tc::kBlockM - 1) / tc::kBlockM;
     int grid = int(tiles < num_sms() ? tiles : num_sms());
-    tc::tc_gemm_kernel<BN, EW><<<grid, tc::gemm_threads(EW), smem, s>>>(a0, a1, b, out, sh, ep);
+    tc::tc_gemm_kernel<BN, EW, EPI><<<grid, tc::gemm_threads(EW), smem, s>>>(a0, a1, b, out, sh, ep);
     return launch_status();
+}
+
+template <int BN, int EW>
+int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
+                   tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
+    int kb = sh.kb0 + sh.kb1;
+    if (tc::SmemPlan<BN, EW>::stages(kb) < 2) return SRF_ERR_UNSUPPORTED;
+    size_t smem = tc::SmemPlan<BN, EW>::bytes(kb);
+    switch (tc::epi_mode(ep)) {   // the combinations the layers use; anything else runs the full set
+        case tc::kEpiFwd: return launch_gemm_epi<BN, EW, tc::kEpiFwd>(a0, a1, b, out, sh, ep, smem, s);
+        case tc::kEpiDg: return launch_gemm_epi<BN, EW, tc::kEpiDg>(a0, a1, b, out, sh, ep, smem, s);
+        case tc::kEpiDg | tc::kEpiM16:
+            return launch_gemm_epi<BN, EW, tc::kEpiDg | tc::kEpiM16>(a0, a1, b, out, sh, ep, smem, s);
+        case tc::kEpiHead: return launch_gemm_epi<BN, EW, tc::kEpiHead>(a0, a1, b, out, sh, ep, smem, s);
+        default: return launch_gemm_epi<BN, EW, tc::kEpiAll>(a0, a1, b, out, sh, ep, smem, s);
+    }
 }
 
 // 8 epilogue warps (two per tensor-memory lane quadrant) keep the TMA-store epilogue
@@ -155,16 +168,17 @@ int tc_linear(const tc::GemmEpilogue& ep, const op16* x0, int64_t ld0, int k0, c
 }
 
 // splits <= num_sms / (n_dz / 128), so splits * n_dz <= num_sms * 128
+// split partials of dW (np floats per dZ column) and of the dZ column sums (one)
 size_t tc_wgrad_partial_floats(int n_dz, int np) {
     (void)n_dz;
-    return size_t(num_sms()) * 128 * np;
+    return size_t(num_sms()) * 128 * (np + 1);
 }
 
 // partial[split, n, k] = sum_m dz[m, n] x[m, k] (x = [x0 | x1]); returns the split count.
 int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_dz, int n_dz, const op16* x0,
              int64_t ld0, int k0, const op16* x1, int64_t ld1, int k1, int64_t M, int* splits_out, cudaStream_t s,
-             int fmt = tc::kFmtBF16) {
-    if (n_dz % 128 || k0 % 64 || k1 % 64 || k0 <= 0 || k0 + k1 > 512) return SRF_ERR_UNSUPPORTED;
+             int fmt = tc::kFmtBF16, bool ones = false) {
+    if (n_dz % 128 || k0 % 64 || k1 % 64 || k0 <= 0 || k0 + k1 > (ones ? 448 : 512)) return SRF_ERR_UNSUPPORTED;
     if (ld_dz < n_dz || ld0 < k0 || (k1 && (!x1 || ld1 < k1))) return SRF_ERR_SHAPE;
     if (!ok16(dz) || !ok16(x0) || (x1 && !ok16(x1)) || (ld_dz % 8) || (ld0 % 8) || (x1 && (ld1 % 8)))
         return SRF_ERR_ALIGN;
@@ -177,7 +191,7 @@ int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_d
     splits = int((M + chunk - 1) / chunk);
     if (splits < 1) splits = 1;
     int np = k0 + k1;
-    if (size_t(splits) * n_dz * np > partial_floats) return SRF_ERR_WORKSPACE;
+    if (size_t(splits) * n_dz * (np + (ones ? 1 : 0)) > partial_floats) return SRF_ERR_WORKSPACE;
     CUtensorMap mdz, m0, m1;
     if (!make_map(&mdz, dz, uint64_t(n_dz), uint64_t(M), uint64_t(ld_dz) * 2, 64, 64)) return SRF_ERR_CUDA;
     if (!make_map(&m0, x0, uint64_t(k0), uint64_t(M), uint64_t(ld0) * 2, 64, 64)) return SRF_ERR_CUDA;
@@ -187,7 +201,7 @@ int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_d
         m1 = m0;
     }
     int nchunks = np / 64;
-    if (tc::wgrad_stages(nchunks) < 2) return SRF_ERR_UNSUPPORTED;
+    if (tc::wgrad_stages(nchunks, ones) < 2) return SRF_ERR_UNSUPPORTED;
     static bool attr_done = false;
     if (!attr_done) {
         cudaError_t e = cudaFuncSetAttribute(tc::tc_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -198,10 +212,10 @@ int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_d
         }
         attr_done = true;
     }
-    tc::WgradShape sh{M, chunk, n_dz, k0 / 64, k1 / 64, fmt};
+    tc::WgradShape sh{M, chunk, n_dz, k0 / 64, k1 / 64, fmt, ones ? 1 : 0};
     dim3 grid(ntile, splits);
-    tc::tc_wgrad_kernel<<<grid, tc::kThreads, tc::wgrad_smem(nchunks), s>>>(mdz, m0, m1, sh, partial,
-                                                                          device_flag());
+    tc::tc_wgrad_kernel<<<grid, tc::kThreads, tc::wgrad_smem(nchunks, ones), s>>>(
+        mdz, m0, m1, sh, partial, partial + size_t(splits) * n_dz * np, device_flag());
     *splits_out = splits;
     return launch_status();
 }
@@ -242,11 +256,18 @@ __global__ void pack_weight_kernel(LayerMap L, const float* __restrict__ w, op16
     wt[int64_t(kp) * L.n + n] = b;
 }
 
-// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns.
+// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns;
+// bias_grad[n] (when given) += sum_s partial_cs[s, n], the same way.
 __global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits, int n_dz, float* grad,
-                                    const float* gscale) {
+                                    const float* gscale, const float* __restrict__ partial_cs, float* bias_grad) {
     int kp = blockIdx.x * blockDim.x + threadIdx.x;
     int n = blockIdx.y;
+    if (bias_grad && kp == 0) {
+        float acc = 0.f;
+        for (int sp = 0; sp < splits; ++sp) acc += partial_cs[int64_t(sp) * n_dz + n];
+        if (gscale) acc *= gscale[1];
+        bias_grad[n] += acc;
+    }
     int kpad = L.kpad();
     if (kp >= kpad) return;
     int rc = ref_col(L, kp);
@@ -369,46 +390,58 @@ __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict_
     }
 #pragma unroll
     for (int u = 0; u < NO; ++u) dbl[u] = 0.f;
-    for (int64_t r = int64_t(blockIdx.x) * rpb + rloc; r < M; r += int64_t(gridDim.x) * rpb) {
-        float g[NO];
-        int u0 = 0;
-        if (NO == 4) {
-            g[0] = sraw[r] > 0.f ? dsigma[r] : 0.f;
-            u0 = 1;
-        }
+    // two rows per pass: both rows' loads are issued before either row's arithmetic
+    const int64_t stride = int64_t(gridDim.x) * rpb;
+    for (int64_t r0 = int64_t(blockIdx.x) * rpb + rloc; r0 < M; r0 += 2 * stride) {
+        const int64_t rows[2] = {r0, r0 + stride};
+        float g[2][NO], hx[2][8];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float v = rgb[3 * r + c];
-            g[u0 + c] = drgb[3 * r + c] * v * (1.f - v);
-        }
-        uint4 raw = *reinterpret_cast<const uint4*>(h + r * K + chunk * 8);
-        uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
-        float hx[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            float2 f = tc::unpack16(w4[q], fmt);
-            hx[2 * q] = f.x;
-            hx[2 * q + 1] = f.y;
-        }
-        float o[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            float v = 0.f;
-#pragma unroll
-            for (int u = 0; u < NO; ++u) {
-                v += g[u] * w[u][i];
-                dwl[u][i] += g[u] * hx[i];
+        for (int t = 0; t < 2; ++t) {
+            const int64_t r = rows[t];
+            if (r >= M) continue;
+            int u0 = 0;
+            if (NO == 4) {
+                g[t][0] = sraw[r] > 0.f ? dsigma[r] : 0.f;
+                u0 = 1;
             }
-            o[i] = hx[i] > 0.f ? v * gs0 : 0.f;
-            cs[i] += o[i];
-            bad |= !(fabsf(o[i]) <= vmax);
-        }
-        *reinterpret_cast<uint4*>(dz + r * K + chunk * 8) =
-            make_uint4(tc::pack16(o[0], o[1], fmt), tc::pack16(o[2], o[3], fmt), tc::pack16(o[4], o[5], fmt),
-                       tc::pack16(o[6], o[7], fmt));
-        if (chunk == 0) {
 #pragma unroll
-            for (int u = 0; u < NO; ++u) dbl[u] += g[u];
+            for (int c = 0; c < 3; ++c) {
+                float v = rgb[3 * r + c];
+                g[t][u0 + c] = drgb[3 * r + c] * v * (1.f - v);
+            }
+            uint4 raw = *reinterpret_cast<const uint4*>(h + r * K + chunk * 8);
+            uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float2 f = tc::unpack16(w4[q], fmt);
+                hx[t][2 * q] = f.x;
+                hx[t][2 * q + 1] = f.y;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const int64_t r = rows[t];
+            if (r >= M) continue;
+            float o[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                float v = 0.f;
+#pragma unroll
+                for (int u = 0; u < NO; ++u) {
+                    v += g[t][u] * w[u][i];
+                    dwl[u][i] += g[t][u] * hx[t][i];
+                }
+                o[i] = hx[t][i] > 0.f ? v * gs0 : 0.f;
+                cs[i] += o[i];
+                bad |= !(fabsf(o[i]) <= vmax);
+            }
+            *reinterpret_cast<uint4*>(dz + r * K + chunk * 8) =
+                make_uint4(tc::pack16(o[0], o[1], fmt), tc::pack16(o[2], o[3], fmt), tc::pack16(o[4], o[5], fmt),
+                           tc::pack16(o[6], o[7], fmt));
+            if (chunk == 0) {
+#pragma unroll
+                for (int u = 0; u < NO; ++u) dbl[u] += g[t][u];
+            }
         }
     }
     // block reduction over the rloc rows, one quantity (K floats) at a time
@@ -582,14 +615,19 @@ struct TcCtx {
     int* found_inf() const { return scaler ? &scaler->found_inf : nullptr; }
 };
 
+// The layer's weight gradient and, when bias_grad is given, its bias gradient (the
+// sum of dZ over the samples, from the same tensor-core pass).
 int wgrad_layer(const LayerMap& lm, float* partial, size_t partial_floats, const op16* dz, const op16* x0,
-                int64_t ld0, const op16* x1, int64_t ld1, int64_t M, float* grad, const TcCtx& cx, cudaStream_t s) {
+                int64_t ld0, const op16* x1, int64_t ld1, int64_t M, float* grad, const TcCtx& cx, cudaStream_t s,
+                float* bias_grad = nullptr) {
     int splits = 0;
     int st = tc_wgrad(partial, partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
-                      lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt);
+                      lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt, bias_grad != nullptr);
     if (st) return st;
     dim3 grid((lm.kpad() + 127) / 128, lm.n);
-    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale());
+    const int np = lm.kpad();
+    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale(),
+                                             partial + size_t(splits) * lm.n * np, bias_grad);
     return launch_status();
 }
 
@@ -696,33 +734,31 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
     if (L.vdep) {
         // rgb head: dZ of the last view layer, its bias gradient, the head's dW/db
         st = head_bwd_fused<3>(m, L.Wv, nullptr, nullptr, drgb, w.rgb, P[L.idx_rgb_w()], w.hv[L.Dv - 1], dz,
-                               G[L.idx_view_w(L.Dv - 1) + 1], G[L.idx_rgb_w()], G[L.idx_rgb_w() + 1], fmt,
-                               cx.gscale(), cx.found_inf(), s);
+                               nullptr, G[L.idx_rgb_w()], G[L.idx_rgb_w() + 1], fmt, cx.gscale(), cx.found_inf(),
+                               s);
         if (st) return st;
         for (int j = L.Dv - 1; j >= 0; --j) {
             const LayerMap& lm = T.view[j];
             const op16* x0 = j == 0 ? w.feat : w.hv[j - 1];
             int64_t ld0 = j == 0 ? L.Wp : L.Wv;
             st = wgrad_layer(lm, w.partial, w.partial_floats, dz, x0, ld0, lm.nsrc > 1 ? w.vext : nullptr, T.vx_w,
-                             m, G[L.idx_view_w(j)], cx, s);
+                             m, G[L.idx_view_w(j)], cx, s, G[L.idx_view_w(j) + 1]);
             if (st) return st;
             if (j > 0) {
                 tc::GemmEpilogue ep = bwd_epilogue(dz2, L.Wv);
                 ep.mask = w.hv[j - 1];
                 ep.ld_mask = L.Wv;
-                ep.colsum = G[L.idx_view_w(j - 1) + 1];
                 st = tc_linear(ep, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[j], L.Wv, lm.kpad(), 0, m, L.Wv, s);
                 if (st) return st;
                 std::swap(dz, dz2);
             } else {
                 tc::GemmEpilogue ep = bwd_epilogue(w.dfeat, L.Wp);
-                ep.colsum = G[L.idx_feat_w() + 1];
                 st = tc_linear(ep, dz, L.Wv, L.Wv, nullptr, 0, 0, w.WTv[0], L.Wv, lm.kpad(), 0, m, L.Wp, s);
                 if (st) return st;
             }
         }
         st = wgrad_layer(T.feat, w.partial, w.partial_floats, w.dfeat, hl, L.Wp, nullptr, 0, m, G[L.idx_feat_w()],
-                         cx, s);
+                         cx, s, G[L.idx_feat_w() + 1]);
         if (st) return st;
         // feature-layer dgrad with the sigma head's adjoint fused in: dZ_last =
         // (dfeat . Wf + dsig w_sigma) * (h_last > 0), dsig = dsigma * (sraw > 0);
@@ -735,13 +771,11 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         ep.r1_col = P[L.idx_out_w()];
         ep.r1_mask_colsum = G[L.idx_out_w()];
         ep.r1_sum = G[L.idx_out_w() + 1];
-        ep.colsum = G[L.idx_trunk_w(L.Dp - 1) + 1];
         st = tc_linear(ep, w.dfeat, L.Wp, L.Wp, nullptr, 0, 0, w.WTf, L.Wp, L.Wp, 0, m, L.Wp, s);
         if (st) return st;
     } else {
-        st = head_bwd_fused<4>(m, L.Wp, dsigma, w.sraw, drgb, w.rgb, P[L.idx_out_w()], hl, dz,
-                               G[L.idx_trunk_w(L.Dp - 1) + 1], G[L.idx_out_w()], G[L.idx_out_w() + 1], fmt,
-                               cx.gscale(), cx.found_inf(), s);
+        st = head_bwd_fused<4>(m, L.Wp, dsigma, w.sraw, drgb, w.rgb, P[L.idx_out_w()], hl, dz, nullptr,
+                               G[L.idx_out_w()], G[L.idx_out_w() + 1], fmt, cx.gscale(), cx.found_inf(), s);
         if (st) return st;
     }
     for (int j = L.Dp - 1; j >= 0; --j) {
@@ -749,14 +783,13 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         const op16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
         st = wgrad_layer(lm, w.partial, w.partial_floats, dz, x0, ld0, lm.nsrc > 1 ? w.h[j - 1] : nullptr, L.Wp, m,
-                         G[L.idx_trunk_w(j)], cx, s);
+                         G[L.idx_trunk_w(j)], cx, s, G[L.idx_trunk_w(j) + 1]);
         if (st) return st;
         if (j == 0) break;
         int row0 = lm.nsrc > 1 ? lm.padw[0] : 0;
         tc::GemmEpilogue ep = bwd_epilogue(dz2, L.Wp);
         ep.mask_bits = w.hbits[j - 1];
         ep.ld_bits = L.Wp / 32;
-        ep.colsum = G[L.idx_trunk_w(j - 1) + 1];
         st = tc_linear(ep, dz, L.Wp, L.Wp, nullptr, 0, 0, w.WT[j], L.Wp, lm.kpad(), row0, m, L.Wp, s);
         if (st) return st;
         std::swap(dz, dz2);
@@ -1264,17 +1297,18 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
     const TcCtx cx{fmt, scaler};
     int st;
     // rgb head: dZ2 (scaled), db2, dW3, db3
-    if ((st = head_bwd_fused<3>(m, U, nullptr, nullptr, drgb, w.rgb, P[5], w.h2, w.dz0, G[4], G[5], G[6], fmt,
+    if ((st = head_bwd_fused<3>(m, U, nullptr, nullptr, drgb, w.rgb, P[5], w.h2, w.dz0, nullptr, G[5], G[6], fmt,
                                 cx.gscale(), cx.found_inf(), s)))
         return st;
-    if ((st = wgrad_layer(R.l2, w.partial, w.partial_floats, w.dz0, w.h1, U, nullptr, 0, m, G[3], cx, s))) return st;
+    if ((st = wgrad_layer(R.l2, w.partial, w.partial_floats, w.dz0, w.h1, U, nullptr, 0, m, G[3], cx, s, G[4])))
+        return st;
     tc::GemmEpilogue e2 = make_epilogue(w.dz1, U, nullptr, 0, fmt, cx.found_inf());
     e2.gscale = cx.gscale();
     e2.mask = w.h1;
     e2.ld_mask = U;
-    e2.colsum = G[2];
     if ((st = tc_linear(e2, w.dz0, U, U, nullptr, 0, 0, w.W2T, U, U, 0, m, U, s))) return st;
-    if ((st = wgrad_layer(R.l1, w.partial, w.partial_floats, w.dz1, w.x, R.k1p, nullptr, 0, m, G[1], cx, s))) return st;
+    if ((st = wgrad_layer(R.l1, w.partial, w.partial_floats, w.dz1, w.x, R.k1p, nullptr, 0, m, G[1], cx, s, G[2])))
+        return st;
     // dX = dZ1 . W1 (k1p columns, in blocks of at most 128 output columns)
     for (int c0 = 0; c0 < R.k1p; c0 += 128) {
         const int n = R.k1p - c0 >= 128 ? 128 : 64;

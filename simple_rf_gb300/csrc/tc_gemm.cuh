@@ -73,6 +73,24 @@ __host__ __device__ inline int head_units(int mode) {
     return mode == kHeadSigma ? 1 : (mode == kHeadRgb ? 3 : (mode == kHeadSigmaRgb ? 4 : 0));
 }
 
+// Epilogue features compiled into a kernel instance, as bit flags.  A launch takes
+// the narrowest set that covers its GemmEpilogue: the branches of unused features,
+// unrolled over every 32-column chunk, otherwise cost the 256-wide epilogue
+// instruction fetch (measured: the forward layer ran 25% faster with them compiled
+// out).  Always present: bias, ReLU, bits_out, found_inf, the output.
+//   kEpiDg    mask_bits, colsum, the r1 terms (r1_row / r1_col / r1_gate / r1_sum)
+//   kEpiM16   the 16-bit mask and r1_mask_colsum
+//   kEpiHead  the fused heads
+enum : int { kEpiFwd = 0, kEpiDg = 1, kEpiM16 = 2, kEpiHead = 4, kEpiAll = 7 };
+
+inline int epi_mode(const GemmEpilogue& ep) {
+    int e = kEpiFwd;
+    if (ep.mask_bits || ep.colsum || ep.r1_row || ep.r1_sum) e |= kEpiDg;
+    if (ep.mask || ep.r1_mask_colsum) e |= kEpiM16 | kEpiDg;
+    if (head_units(ep.head_mode)) e |= kEpiHead;
+    return e;
+}
+
 // Lane i of the warp ends with sum over the 32 lanes of v[i] (recursive halving).
 __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
     const int lane = threadIdx.x & 31;
@@ -123,7 +141,7 @@ struct SmemPlan {
     }
 };
 
-template <int BN, int EW>
+template <int BN, int EW, int EPI>
 __global__ void __launch_bounds__(gemm_threads(EW), 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
                    const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmOut,
@@ -155,7 +173,8 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
     float* shb = shw + 4 * BN;                             // 4 floats
     float* shx = shb + 4;                                  // [2][128][4] partial head sums (8 epilogue warps)
     uint32_t* sbits = reinterpret_cast<uint32_t*>(shx + Plan::kHeadXBytes / 4);   // ReLU bits (4 epilogue warps)
-    const int hunits = head_units(ep.head_mode);
+    constexpr bool kDg = (EPI & kEpiDg) != 0, kM16 = (EPI & kEpiM16) != 0, kHd = (EPI & kEpiHead) != 0;
+    const int hunits = kHd ? head_units(ep.head_mode) : 0;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t num_tiles = (shape.M + kBlockM - 1) / kBlockM;
@@ -275,8 +294,18 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
         const float gs0 = ep.gscale ? ep.gscale[0] : 1.f;
         const float vmax = fmt_max(ep.fmt);
         bool bad = false;
+        // 8 epilogue warps with mask bits: the row's words for this warp's chunks are
+        // loaded before the accumulator wait, so their latency hides behind it
+        constexpr bool kBitsAhead = kDg && EW == 8 && kHalfChunks <= 4;
         for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
             uint32_t acc = t & 1;
+            uint32_t mbw[kBitsAhead ? kHalfChunks : 1];
+            if (kBitsAhead) {
+                const int64_t mr = tile * kBlockM + q * 32 + lane;
+#pragma unroll
+                for (int k = 0; k < (kBitsAhead ? kHalfChunks : 1); ++k)
+                    mbw[k] = (ep.mask_bits && mr < shape.M) ? ep.mask_bits[mr * ep.ld_bits + c0 + k] : 0u;
+            }
             if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
                 *abort_flag = 1;
                 break;
@@ -284,8 +313,8 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             tc_fence_after();
             const int64_t m = tile * kBlockM + q * 32 + lane;
             const bool live = m < shape.M;
-            float r1 = (ep.r1_row && live) ? ep.r1_row[m] : 0.f;
-            if (ep.r1_gate && live && !(ep.r1_gate[m] > 0.f)) r1 = 0.f;
+            float r1 = (kDg && ep.r1_row && live) ? ep.r1_row[m] : 0.f;
+            if (kDg && ep.r1_gate && live && !(ep.r1_gate[m] > 0.f)) r1 = 0.f;
             if (half == 0) r1_total += r1;
             float hacc[4] = {0.f, 0.f, 0.f, 0.f};
             const uint32_t tbase = tmem + acc * BN + (uint32_t(q * 32) << 16);
@@ -311,12 +340,13 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     v[j] = __uint_as_float(r[j]) + sbias[c * 32 + j];
-                    if (ep.r1_row) v[j] += (r1 * gs0) * ep.r1_col[c * 32 + j];
+                    if (kDg && ep.r1_row) v[j] += (r1 * gs0) * ep.r1_col[c * 32 + j];
                     if (ep.relu) v[j] = v[j] > 0.f ? v[j] : 0.f;
                     if (!live) v[j] = 0.f;
                 }
-                if (ep.mask_bits) {   // kernel-uniform branch
-                    const uint32_t mb = live ? ep.mask_bits[m * ep.ld_bits + c] : 0u;
+                if (kDg && ep.mask_bits) {   // kernel-uniform branch
+                    const uint32_t mb = kBitsAhead ? mbw[kBitsAhead ? cc : 0]
+                                                   : (live ? ep.mask_bits[m * ep.ld_bits + c] : 0u);
 #pragma unroll
                     for (int j = 0; j < 32; ++j)
                         if (!((mb >> j) & 1u)) v[j] = 0.f;
@@ -328,7 +358,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                     if (EW == 8) rbits[cc] = mb;
                     else sbits[((warp - 2) * 32 + lane) * kHalfChunks + cc] = mb;
                 }
-                if (ep.mask) {   // kernel-uniform branch; rows past M contribute zeros
+                if (kM16 && ep.mask) {   // kernel-uniform branch; rows past M contribute zeros
                     float mw[32];
 #pragma unroll
                     for (int j = 0; j < 32; ++j) mw[j] = 0.f;
@@ -405,7 +435,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                         for (int j = 0; j < 32; ++j) bad |= !(fabsf(v[j]) <= vmax);
                     }
                 }
-                if (ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
+                if (kDg && ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
                 tmem_ld_wait();
             }
             if (EW == 4 && ep.bits_out) {
@@ -474,7 +504,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             tc_fence_before();
             mbar_arrive(&acc_empty[acc]);
         }
-        if (ep.r1_sum) {
+        if (kDg && ep.r1_sum) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) r1_total += __shfl_xor_sync(0xffffffffu, r1_total, o);
             if (lane == 0) atomicAdd(ep.r1_sum, r1_total);
@@ -485,11 +515,11 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
     }
     __syncthreads();
     if (threadIdx.x == 0 && *abort_flag) raise_flag(ep.flag, kFlagTimeout);
-    if (ep.colsum) {
+    if (kDg && ep.colsum) {
         const float gs1 = ep.gscale ? ep.gscale[1] : 1.f;
         for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.colsum + i, scol[i] * gs1);
     }
-    if (ep.r1_mask_colsum)
+    if (kM16 && ep.r1_mask_colsum)
         for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.r1_mask_colsum + i, scol2[i]);
     if (warp == 1) {
         tc_fence_after();
@@ -511,17 +541,22 @@ struct WgradShape {
     int n_dz;         // columns of dZ (rows of dW)
     int kc0, kc1;     // 64-wide column chunks of X0 / X1
     int fmt;          // operand format (kFmtBF16, kFmtF16)
+    int ones;         // also sum dZ over the samples (a bias gradient), into partial_cs
 };
 
 constexpr uint32_t kBox64Bytes = 64 * 64 * 2;
 
-__host__ __device__ inline int wgrad_stages(int nchunks) {
+// A stage holds the two dZ boxes and the X boxes of 64 samples; one more box of
+// 16-bit ones (when the bias gradient is wanted) is an MMA operand whose product
+// with dZ^T is the sum of dZ over the samples.
+__host__ __device__ inline int wgrad_stages(int nchunks, int ones) {
     size_t stage = size_t(2 + nchunks) * kBox64Bytes;
-    int s = int((kMaxSmem - 1024 - 256) / stage);
+    int s = int((kMaxSmem - 1024 - 256 - (ones ? kBox64Bytes : 0)) / stage);
     return s > 6 ? 6 : s;
 }
-__host__ __device__ inline size_t wgrad_smem(int nchunks) {
-    return 1024 + 256 + size_t(wgrad_stages(nchunks)) * (2 + nchunks) * kBox64Bytes;
+__host__ __device__ inline size_t wgrad_smem(int nchunks, int ones) {
+    return 1024 + 256 + size_t(wgrad_stages(nchunks, ones)) * (2 + nchunks) * kBox64Bytes +
+           (ones ? kBox64Bytes : 0);
 }
 __host__ __device__ inline uint32_t tmem_cols_for(int n) {
     uint32_t c = 32;
@@ -531,14 +566,16 @@ __host__ __device__ inline uint32_t tmem_cols_for(int n) {
 
 __global__ void __launch_bounds__(kThreads, 1)
     tc_wgrad_kernel(const __grid_constant__ CUtensorMap tmDZ, const __grid_constant__ CUtensorMap tmX0,
-                    const __grid_constant__ CUtensorMap tmX1, WgradShape s, float* partial, int* flag) {
+                    const __grid_constant__ CUtensorMap tmX1, WgradShape s, float* partial, float* partial_cs,
+                    int* flag) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int nchunks = s.kc0 + s.kc1;
     const int np = nchunks * 64;
-    const int stages = wgrad_stages(nchunks);
+    const int stages = wgrad_stages(nchunks, s.ones);
     const uint32_t stage_bytes = uint32_t(2 + nchunks) * kBox64Bytes;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(base + size_t(stages) * stage_bytes);
+    uint8_t* sones = base + size_t(stages) * stage_bytes;   // 1024-aligned (stage_bytes is a multiple of 8 KB)
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sones + (s.ones ? kBox64Bytes : 0));
     uint64_t* full = bars;
     uint64_t* empty = bars + 8;
     uint64_t* acc_full = bars + 16;
@@ -552,7 +589,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     int64_t m_end = m_begin + s.m_chunk;
     if (m_end > s.M) m_end = s.M;
     const int nblk = m_end > m_begin ? int((m_end - m_begin + 63) / 64) : 0;
-    const uint32_t ncols = tmem_cols_for(np);
+    const uint32_t ncols = tmem_cols_for(np + (s.ones ? 64 : 0));
+    if (s.ones) {   // 16-bit ones for the generic proxy, then made visible to the tensor core
+        const uint32_t one2 = s.fmt == kFmtF16 ? 0x3C003C00u : 0x3F803F80u;
+        uint4* o = reinterpret_cast<uint4*>(sones);
+        for (int i = threadIdx.x; i < int(kBox64Bytes / 16); i += blockDim.x) o[i] = make_uint4(one2, one2, one2, one2);
+        fence_proxy_async_smem();
+    }
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < stages; ++i) {
@@ -621,6 +664,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     mma_f16(tmem + uint32_t(p * 256), ad, bd, idesc_f16(128, cnt * 64, 1, 1, s.fmt),
                              (b | ks) != 0);
                 }
+                if (s.ones) {   // columns np .. np + 63: every one is sum_m dz[m, n]
+                    uint64_t od = smem_desc(smem_u32(sones) + ks * 2048, kBox64Bytes, 1024, kSwizzle128B);
+                    mma_f16(tmem + uint32_t(np), ad, od, idesc_f16(128, 64, 1, 1, s.fmt), (b | ks) != 0);
+                }
             }
             mma_commit(&empty[st]);
         }
@@ -652,6 +699,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 o[g] = v;
             }
+        }
+        if (s.ones) {
+            uint32_t r[32];
+            tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(np), r);
+            tmem_ld_wait();
+            if (n < s.n_dz) partial_cs[int64_t(blockIdx.y) * s.n_dz + n] = (nblk > 0 && ok) ? __uint_as_float(r[0]) : 0.f;
         }
     }
     __syncthreads();
