@@ -168,16 +168,16 @@ int tc_linear(const tc::GemmEpilogue& ep, const op16* x0, int64_t ld0, int k0, c
 }
 
 // splits <= num_sms / (n_dz / 128), so splits * n_dz <= num_sms * 128
-// split partials of dW (np floats per dZ column) and of the dZ column sums (one)
 size_t tc_wgrad_partial_floats(int n_dz, int np) {
     (void)n_dz;
-    return size_t(num_sms()) * 128 * (np + 1);
+    return size_t(num_sms()) * 128 * np;
 }
 
 // partial[split, n, k] = sum_m dz[m, n] x[m, k] (x = [x0 | x1]); returns the split count.
 int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_dz, int n_dz, const op16* x0,
              int64_t ld0, int k0, const op16* x1, int64_t ld1, int k1, int64_t M, int* splits_out, cudaStream_t s,
-             int fmt = tc::kFmtBF16, bool ones = false) {
+             int fmt = tc::kFmtBF16, float* bias_grad = nullptr, const float* gscale = nullptr) {
+    const bool ones = bias_grad != nullptr;
     if (n_dz % 128 || k0 % 64 || k1 % 64 || k0 <= 0 || k0 + k1 > (ones ? 448 : 512)) return SRF_ERR_UNSUPPORTED;
     if (ld_dz < n_dz || ld0 < k0 || (k1 && (!x1 || ld1 < k1))) return SRF_ERR_SHAPE;
     if (!ok16(dz) || !ok16(x0) || (x1 && !ok16(x1)) || (ld_dz % 8) || (ld0 % 8) || (x1 && (ld1 % 8)))
@@ -191,7 +191,7 @@ int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_d
     splits = int((M + chunk - 1) / chunk);
     if (splits < 1) splits = 1;
     int np = k0 + k1;
-    if (size_t(splits) * n_dz * (np + (ones ? 1 : 0)) > partial_floats) return SRF_ERR_WORKSPACE;
+    if (size_t(splits) * n_dz * np > partial_floats) return SRF_ERR_WORKSPACE;
     CUtensorMap mdz, m0, m1;
     if (!make_map(&mdz, dz, uint64_t(n_dz), uint64_t(M), uint64_t(ld_dz) * 2, 64, 64)) return SRF_ERR_CUDA;
     if (!make_map(&m0, x0, uint64_t(k0), uint64_t(M), uint64_t(ld0) * 2, 64, 64)) return SRF_ERR_CUDA;
@@ -214,8 +214,8 @@ int tc_wgrad(float* partial, size_t partial_floats, const op16* dz, int64_t ld_d
     }
     tc::WgradShape sh{M, chunk, n_dz, k0 / 64, k1 / 64, fmt, ones ? 1 : 0};
     dim3 grid(ntile, splits);
-    tc::tc_wgrad_kernel<<<grid, tc::kThreads, tc::wgrad_smem(nchunks, ones), s>>>(
-        mdz, m0, m1, sh, partial, partial + size_t(splits) * n_dz * np, device_flag());
+    tc::tc_wgrad_kernel<<<grid, tc::kThreads, tc::wgrad_smem(nchunks, ones), s>>>(mdz, m0, m1, sh, partial,
+                                                                                bias_grad, gscale, device_flag());
     *splits_out = splits;
     return launch_status();
 }
@@ -256,18 +256,11 @@ __global__ void pack_weight_kernel(LayerMap L, const float* __restrict__ w, op16
     wt[int64_t(kp) * L.n + n] = b;
 }
 
-// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns;
-// bias_grad[n] (when given) += sum_s partial_cs[s, n], the same way.
+// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns.
 __global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits, int n_dz, float* grad,
-                                    const float* gscale, const float* __restrict__ partial_cs, float* bias_grad) {
+                                    const float* gscale) {
     int kp = blockIdx.x * blockDim.x + threadIdx.x;
     int n = blockIdx.y;
-    if (bias_grad && kp == 0) {
-        float acc = 0.f;
-        for (int sp = 0; sp < splits; ++sp) acc += partial_cs[int64_t(sp) * n_dz + n];
-        if (gscale) acc *= gscale[1];
-        bias_grad[n] += acc;
-    }
     int kpad = L.kpad();
     if (kp >= kpad) return;
     int rc = ref_col(L, kp);
@@ -484,6 +477,64 @@ int head_bwd_fused(int64_t M, int K, const float* dsigma, const float* sraw, con
     return launch_status();
 }
 
+// Sigma head gradients (SimpleNeRF17.py:735-741 adjoint): with g[m] = dsigma[m] when
+// the raw sigma is positive (the ReLU), else 0, dW[k] += sum_m g[m] h[m, k] and
+// db += sum_m g[m] over the last trunk layer's stored 16-bit rows h (K columns,
+// K = 8 x 32).  A warp per row and 8 columns per lane, two rows in flight per warp;
+// the block's sums go out with one atomic per column.
+__global__ void __launch_bounds__(256) sigma_head_wgrad_kernel(int64_t M, int K, const float* __restrict__ dsigma,
+                                                               const float* __restrict__ sraw,
+                                                               const op16* __restrict__ h, float* dW, float* db,
+                                                               int fmt) {
+    __shared__ float red[8][256 + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gsum = 0.f;
+    const int64_t stride = int64_t(gridDim.x) * 8;
+    for (int64_t r0 = int64_t(blockIdx.x) * 8 + warp; r0 < M; r0 += 2 * stride) {
+        const int64_t rows[2] = {r0, r0 + stride};
+        float g[2] = {0.f, 0.f};
+        uint4 raw[2];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            if (rows[t] >= M) continue;
+            g[t] = sraw[rows[t]] > 0.f ? dsigma[rows[t]] : 0.f;
+            raw[t] = *reinterpret_cast<const uint4*>(h + rows[t] * K + lane * 8);
+        }
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            if (rows[t] >= M || g[t] == 0.f) continue;
+            const uint32_t w4[4] = {raw[t].x, raw[t].y, raw[t].z, raw[t].w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float2 f = tc::unpack16(w4[q], fmt);
+                acc[2 * q] += g[t] * f.x;
+                acc[2 * q + 1] += g[t] * f.y;
+            }
+            gsum += g[t];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) red[warp][lane * 8 + i] = acc[i];
+    __syncthreads();
+    if (threadIdx.x < K) {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += red[w][threadIdx.x];
+        atomicAdd(dW + threadIdx.x, s);
+    }
+    if (lane == 0) atomicAdd(db, gsum);
+}
+
+int sigma_head_wgrad(int64_t M, int K, const float* dsigma, const float* sraw, const op16* h, float* dW, float* db,
+                     int fmt, cudaStream_t s) {
+    if (K != 256) return SRF_ERR_UNSUPPORTED;
+    if (M <= 0) return SRF_OK;
+    int64_t blocks = (M + 15) / 16;
+    if (blocks > int64_t(num_sms()) * 4) blocks = int64_t(num_sms()) * 4;
+    sigma_head_wgrad_kernel<<<unsigned(blocks), 256, 0, s>>>(M, K, dsigma, sraw, h, dW, db, fmt);
+    return launch_status();
+}
+
 int pad64(int x) { return (x + 63) / 64 * 64; }
 
 // ------------------------------------------------------------ layout -------
@@ -584,7 +635,8 @@ size_t carve_tc(const MlpLayout& L, const TcLayout& T, int64_t m, bool bwd, void
     }
     int wmax = L.Wp > L.Wv ? L.Wp : L.Wv;
     if (bwd) {
-        for (int j = 0; j + 1 < L.Dp; ++j) w.hbits.push_back(c.take<uint32_t>(size_t(m) * (L.Wp / 32)));
+        // h[j] feeds trunk layer j + 1's mask, and h[Dp - 1] the feature layer's (view-dependent nets)
+        for (int j = 0; j < L.Dp; ++j) w.hbits.push_back(c.take<uint32_t>(size_t(m) * (L.Wp / 32)));
         w.dz0 = c.take<op16>(size_t(m) * wmax);
         w.dz1 = c.take<op16>(size_t(m) * wmax);
         w.dfeat = L.vdep ? c.take<op16>(size_t(m) * L.Wp) : nullptr;
@@ -622,12 +674,10 @@ int wgrad_layer(const LayerMap& lm, float* partial, size_t partial_floats, const
                 float* bias_grad = nullptr) {
     int splits = 0;
     int st = tc_wgrad(partial, partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
-                      lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt, bias_grad != nullptr);
+                      lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt, bias_grad, cx.gscale());
     if (st) return st;
     dim3 grid((lm.kpad() + 127) / 128, lm.n);
-    const int np = lm.kpad();
-    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale(),
-                                             partial + size_t(splits) * lm.n * np, bias_grad);
+    reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale());
     return launch_status();
 }
 
@@ -669,7 +719,7 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
         int64_t ld0 = j == 0 || j - 1 == L.skip ? T.enc_w : L.Wp;
         const op16* x1 = lm.nsrc > 1 ? w.h[j - 1] : nullptr;
         tc::GemmEpilogue ep = make_epilogue(w.h[j], L.Wp, P[L.idx_trunk_w(j) + 1], 1, fmt, cx.found_inf());
-        if (bwd && j + 1 < L.Dp) {   // the backward-data pass of layer j + 1 masks with these bits
+        if (bwd && (j + 1 < L.Dp || L.vdep)) {   // the backward-data pass after h[j] masks with these bits
             ep.bits_out = w.hbits[j];
             ep.ld_bits = L.Wp / 32;
         }
@@ -764,14 +814,14 @@ int mlp_tc_backward(const MlpLayout& L, const float* const* P, const float* dsig
         // (dfeat . Wf + dsig w_sigma) * (h_last > 0), dsig = dsigma * (sraw > 0);
         // the same pass adds the sigma head's weight (sum dsig h_last) and bias gradients
         tc::GemmEpilogue ep = bwd_epilogue(dz, L.Wp);
-        ep.mask = hl;
-        ep.ld_mask = L.Wp;
+        ep.mask_bits = w.hbits[L.Dp - 1];
+        ep.ld_bits = L.Wp / 32;
         ep.r1_row = dsigma;
         ep.r1_gate = w.sraw;
         ep.r1_col = P[L.idx_out_w()];
-        ep.r1_mask_colsum = G[L.idx_out_w()];
-        ep.r1_sum = G[L.idx_out_w() + 1];
         st = tc_linear(ep, w.dfeat, L.Wp, L.Wp, nullptr, 0, 0, w.WTf, L.Wp, L.Wp, 0, m, L.Wp, s);
+        if (st) return st;
+        st = sigma_head_wgrad(m, L.Wp, dsigma, w.sraw, hl, G[L.idx_out_w()], G[L.idx_out_w() + 1], fmt, s);
         if (st) return st;
     } else {
         st = head_bwd_fused<4>(m, L.Wp, dsigma, w.sraw, drgb, w.rgb, P[L.idx_out_w()], hl, dz, nullptr,

@@ -541,7 +541,7 @@ struct WgradShape {
     int n_dz;         // columns of dZ (rows of dW)
     int kc0, kc1;     // 64-wide column chunks of X0 / X1
     int fmt;          // operand format (kFmtBF16, kFmtF16)
-    int ones;         // also sum dZ over the samples (a bias gradient), into partial_cs
+    int ones;         // also sum dZ over the samples (a bias gradient), added into bias_grad
 };
 
 constexpr uint32_t kBox64Bytes = 64 * 64 * 2;
@@ -566,8 +566,8 @@ __host__ __device__ inline uint32_t tmem_cols_for(int n) {
 
 __global__ void __launch_bounds__(kThreads, 1)
     tc_wgrad_kernel(const __grid_constant__ CUtensorMap tmDZ, const __grid_constant__ CUtensorMap tmX0,
-                    const __grid_constant__ CUtensorMap tmX1, WgradShape s, float* partial, float* partial_cs,
-                    int* flag) {
+                    const __grid_constant__ CUtensorMap tmX1, WgradShape s, float* partial, float* bias_grad,
+                    const float* gscale, int* flag) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int nchunks = s.kc0 + s.kc1;
@@ -704,7 +704,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             uint32_t r[32];
             tmem_ld_32x32b_x32(tmem + (uint32_t(q * 32) << 16) + uint32_t(np), r);
             tmem_ld_wait();
-            if (n < s.n_dz) partial_cs[int64_t(blockIdx.y) * s.n_dz + n] = (nblk > 0 && ok) ? __uint_as_float(r[0]) : 0.f;
+            // this split's part, times 1 / loss scale; one atomic per dZ column and split
+            if (n < s.n_dz && nblk > 0 && ok) atomicAdd(bias_grad + n, __uint_as_float(r[0]) * (gscale ? gscale[1] : 1.f));
         }
     }
     __syncthreads();
