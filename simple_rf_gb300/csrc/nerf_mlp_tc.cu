@@ -94,9 +94,10 @@ int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
     size_t smem = tc::SmemPlan<BN, EW>::bytes(kb);
     switch (tc::epi_mode(ep)) {   // the combinations the layers use; anything else runs the full set
         case tc::kEpiFwd: return launch_gemm_epi<BN, EW, tc::kEpiFwd>(a0, a1, b, out, sh, ep, smem, s);
-        case tc::kEpiDg: return launch_gemm_epi<BN, EW, tc::kEpiDg>(a0, a1, b, out, sh, ep, smem, s);
-        case tc::kEpiDg | tc::kEpiM16:
-            return launch_gemm_epi<BN, EW, tc::kEpiDg | tc::kEpiM16>(a0, a1, b, out, sh, ep, smem, s);
+        case tc::kEpiBits: return launch_gemm_epi<BN, EW, tc::kEpiBits>(a0, a1, b, out, sh, ep, smem, s);
+        case tc::kEpiBits | tc::kEpiR1:
+            return launch_gemm_epi<BN, EW, tc::kEpiBits | tc::kEpiR1>(a0, a1, b, out, sh, ep, smem, s);
+        case tc::kEpiM16: return launch_gemm_epi<BN, EW, tc::kEpiM16>(a0, a1, b, out, sh, ep, smem, s);
         case tc::kEpiHead: return launch_gemm_epi<BN, EW, tc::kEpiHead>(a0, a1, b, out, sh, ep, smem, s);
         default: return launch_gemm_epi<BN, EW, tc::kEpiAll>(a0, a1, b, out, sh, ep, smem, s);
     }

@@ -74,20 +74,25 @@ __host__ __device__ inline int head_units(int mode) {
 }
 
 // Epilogue features compiled into a kernel instance, as bit flags.  A launch takes
-// the narrowest set that covers its GemmEpilogue: the branches of unused features,
-// unrolled over every 32-column chunk, otherwise cost the 256-wide epilogue
-// instruction fetch (measured: the forward layer ran 25% faster with them compiled
-// out).  Always present: bias, ReLU, bits_out, found_inf, the output.
-//   kEpiDg    mask_bits, colsum, the r1 terms (r1_row / r1_col / r1_gate / r1_sum)
-//   kEpiM16   the 16-bit mask and r1_mask_colsum
+// the narrowest instantiated set that covers its GemmEpilogue: the branches of
+// unused features, unrolled over every 32-column chunk, otherwise cost the 256-wide
+// epilogue instruction fetch (measured: the forward layer ran 25% faster with them
+// compiled out).  Always present: bias, ReLU, bits_out, found_inf, the output.
+//   kEpiBits  mask_bits (the backward-data ReLU mask)
+//   kEpiM16   the 16-bit mask
 //   kEpiHead  the fused heads
-enum : int { kEpiFwd = 0, kEpiDg = 1, kEpiM16 = 2, kEpiHead = 4, kEpiAll = 7 };
+//   kEpiR1    the r1 terms (r1_row / r1_col / r1_gate / r1_sum; r1_mask_colsum with kEpiM16)
+//   kEpiCs    colsum
+enum : int { kEpiFwd = 0, kEpiBits = 1, kEpiM16 = 2, kEpiHead = 4, kEpiR1 = 8, kEpiCs = 16, kEpiAll = 31 };
 
 inline int epi_mode(const GemmEpilogue& ep) {
     int e = kEpiFwd;
-    if (ep.mask_bits || ep.colsum || ep.r1_row || ep.r1_sum) e |= kEpiDg;
-    if (ep.mask || ep.r1_mask_colsum) e |= kEpiM16 | kEpiDg;
+    if (ep.mask_bits) e |= kEpiBits;
+    if (ep.mask) e |= kEpiM16;
     if (head_units(ep.head_mode)) e |= kEpiHead;
+    if (ep.r1_row || ep.r1_sum) e |= kEpiR1;
+    if (ep.r1_mask_colsum) e |= kEpiM16 | kEpiR1;
+    if (ep.colsum) e |= kEpiCs;
     return e;
 }
 
@@ -173,7 +178,8 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
     float* shb = shw + 4 * BN;                             // 4 floats
     float* shx = shb + 4;                                  // [2][128][4] partial head sums (8 epilogue warps)
     uint32_t* sbits = reinterpret_cast<uint32_t*>(shx + Plan::kHeadXBytes / 4);   // ReLU bits (4 epilogue warps)
-    constexpr bool kDg = (EPI & kEpiDg) != 0, kM16 = (EPI & kEpiM16) != 0, kHd = (EPI & kEpiHead) != 0;
+    constexpr bool kBits = (EPI & kEpiBits) != 0, kM16 = (EPI & kEpiM16) != 0, kHd = (EPI & kEpiHead) != 0;
+    constexpr bool kR1 = (EPI & kEpiR1) != 0, kCs = (EPI & kEpiCs) != 0;
     const int hunits = kHd ? head_units(ep.head_mode) : 0;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -296,15 +302,25 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
         bool bad = false;
         // 8 epilogue warps with mask bits: the row's words for this warp's chunks are
         // loaded before the accumulator wait, so their latency hides behind it
-        constexpr bool kBitsAhead = kDg && EW == 8 && kHalfChunks <= 4;
+        constexpr bool kBitsAhead = kBits && EW == 8 && kHalfChunks <= 4;
         for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
             uint32_t acc = t & 1;
             uint32_t mbw[kBitsAhead ? kHalfChunks : 1];
             if (kBitsAhead) {
                 const int64_t mr = tile * kBlockM + q * 32 + lane;
+                const uint32_t* src = ep.mask_bits + mr * ep.ld_bits + c0;
+                if (kHalfChunks == 4 && (ep.ld_bits & 3) == 0) {   // one 16-byte load (c0 is 0 or 4)
+                    const uint4 v = (ep.mask_bits && mr < shape.M) ? *reinterpret_cast<const uint4*>(src)
+                                                                   : make_uint4(0u, 0u, 0u, 0u);
+                    mbw[0] = v.x;
+                    mbw[kHalfChunks > 1 ? 1 : 0] = v.y;
+                    mbw[kHalfChunks > 2 ? 2 : 0] = v.z;
+                    mbw[kHalfChunks > 3 ? 3 : 0] = v.w;
+                } else {
 #pragma unroll
-                for (int k = 0; k < (kBitsAhead ? kHalfChunks : 1); ++k)
-                    mbw[k] = (ep.mask_bits && mr < shape.M) ? ep.mask_bits[mr * ep.ld_bits + c0 + k] : 0u;
+                    for (int k = 0; k < (kBitsAhead ? kHalfChunks : 1); ++k)
+                        mbw[k] = (ep.mask_bits && mr < shape.M) ? src[k] : 0u;
+                }
             }
             if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
                 *abort_flag = 1;
@@ -313,8 +329,8 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             tc_fence_after();
             const int64_t m = tile * kBlockM + q * 32 + lane;
             const bool live = m < shape.M;
-            float r1 = (kDg && ep.r1_row && live) ? ep.r1_row[m] : 0.f;
-            if (kDg && ep.r1_gate && live && !(ep.r1_gate[m] > 0.f)) r1 = 0.f;
+            float r1 = (kR1 && ep.r1_row && live) ? ep.r1_row[m] : 0.f;
+            if (kR1 && ep.r1_gate && live && !(ep.r1_gate[m] > 0.f)) r1 = 0.f;
             if (half == 0) r1_total += r1;
             float hacc[4] = {0.f, 0.f, 0.f, 0.f};
             const uint32_t tbase = tmem + acc * BN + (uint32_t(q * 32) << 16);
@@ -340,11 +356,11 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     v[j] = __uint_as_float(r[j]) + sbias[c * 32 + j];
-                    if (kDg && ep.r1_row) v[j] += (r1 * gs0) * ep.r1_col[c * 32 + j];
+                    if (kR1 && ep.r1_row) v[j] += (r1 * gs0) * ep.r1_col[c * 32 + j];
                     if (ep.relu) v[j] = v[j] > 0.f ? v[j] : 0.f;
                     if (!live) v[j] = 0.f;
                 }
-                if (kDg && ep.mask_bits) {   // kernel-uniform branch
+                if (kBits && ep.mask_bits) {   // kernel-uniform branch
                     const uint32_t mb = kBitsAhead ? mbw[kBitsAhead ? cc : 0]
                                                    : (live ? ep.mask_bits[m * ep.ld_bits + c] : 0u);
 #pragma unroll
@@ -378,7 +394,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                             }
                         }
                     }
-                    if (ep.r1_mask_colsum) {   // needs the mask; r1 is 0 on rows past M
+                    if (kR1 && ep.r1_mask_colsum) {   // needs the mask; r1 is 0 on rows past M
 #pragma unroll
                         for (int j = 0; j < 32; ++j) mw[j] *= r1;
                         atomicAdd(&scol2[c * 32 + lane], warp_reduce_scatter32(mw));
@@ -435,7 +451,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
                         for (int j = 0; j < 32; ++j) bad |= !(fabsf(v[j]) <= vmax);
                     }
                 }
-                if (kDg && ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
+                if (kCs && ep.colsum) atomicAdd(&scol[c * 32 + lane], warp_reduce_scatter32(v));
                 tmem_ld_wait();
             }
             if (EW == 4 && ep.bits_out) {
@@ -504,7 +520,7 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
             tc_fence_before();
             mbar_arrive(&acc_empty[acc]);
         }
-        if (kDg && ep.r1_sum) {
+        if (kR1 && ep.r1_sum) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) r1_total += __shfl_xor_sync(0xffffffffu, r1_total, o);
             if (lane == 0) atomicAdd(ep.r1_sum, r1_total);
@@ -515,11 +531,11 @@ __global__ void __launch_bounds__(gemm_threads(EW), 1)
     }
     __syncthreads();
     if (threadIdx.x == 0 && *abort_flag) raise_flag(ep.flag, kFlagTimeout);
-    if (kDg && ep.colsum) {
+    if (kCs && ep.colsum) {
         const float gs1 = ep.gscale ? ep.gscale[1] : 1.f;
         for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.colsum + i, scol[i] * gs1);
     }
-    if (kM16 && ep.r1_mask_colsum)
+    if (kM16 && kR1 && ep.r1_mask_colsum)
         for (int i = threadIdx.x; i < BN; i += blockDim.x) atomicAdd(ep.r1_mask_colsum + i, scol2[i]);
     if (warp == 1) {
         tc_fence_after();
