@@ -258,21 +258,32 @@ __global__ void pack_weight_kernel(LayerMap L, const float* __restrict__ w, op16
 }
 
 // grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns.
-__global__ void reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits, int n_dz, float* grad,
-                                    const float* gscale) {
-    int kp = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = blockIdx.y;
-    int kpad = L.kpad();
-    if (kp >= kpad) return;
-    int rc = ref_col(L, kp);
-    if (rc < 0) return;
+// A block covers 32 columns of one row n: warp w sums splits w, w + 4, ... (lane =
+// column, coalesced), and the four partial sums meet in shared memory.
+__global__ void __launch_bounds__(128) reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits,
+                                                           int n_dz, float* grad, const float* gscale) {
+    __shared__ float part[4][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int kp = blockIdx.x * 32 + lane;
+    const int n = blockIdx.y;
+    const int kpad = L.kpad();
     float acc = 0.f;
-    const float* src = partial + int64_t(n) * kpad + kp;
-    const int64_t step = int64_t(n_dz) * kpad;
+    if (kp < kpad) {
+        const float* src = partial + int64_t(n) * kpad + kp;
+        const int64_t step = int64_t(n_dz) * kpad;
 #pragma unroll 8
-    for (int sp = 0; sp < splits; ++sp) acc += src[sp * step];
-    if (gscale) acc *= gscale[1];
-    grad[int64_t(n) * L.kref() + rc] += acc;
+        for (int sp = warp; sp < splits; sp += 4) acc += src[sp * step];
+    }
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && kp < kpad) {
+        const int rc = ref_col(L, kp);
+        if (rc >= 0) {
+            float sum = part[0][lane] + part[1][lane] + part[2][lane] + part[3][lane];
+            if (gscale) sum *= gscale[1];
+            grad[int64_t(n) * L.kref() + rc] += sum;
+        }
+    }
 }
 
 // enc[m] = PE(pts[m], Lp)[:pin] zero-padded to enc_w; vext[m] = [PE(pts[m])[pin:ppe],
@@ -352,46 +363,43 @@ __global__ void __launch_bounds__(kEncRows)
 //                the ReLU of the raw sigma and the sigmoid of rgb;
 //   dz[m, k]   = S (sum_u g[m, u] W[u, k]) * (h[m, k] > 0)   (fmt, the previous layer's dZ,
 //                times the loss scale S = gscale[0], 1 when gscale is NULL)
-//   colsum[k] += sum_m dz[m, k] / S                          (that layer's bias gradient)
+//   colsum[k] += sum_m dz[m, k] / S                          (that layer's bias gradient, when given)
 //   dW[u, k]  += sum_m g[m, u] h[m, k];  db[u] += sum_m g[m, u]  (the head's own gradients)
-// One thread owns 8 consecutive columns (a 16-byte chunk) of a row; a block
-// covers rows_per_block rows and strides over the rest, keeping its partial
-// sums in registers until one shared-memory reduction at the end.
-template <int NO>
-__global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict__ dsigma,
-                                      const float* __restrict__ sraw, const float* __restrict__ drgb,
-                                      const float* __restrict__ rgb, const float* __restrict__ W,
-                                      const op16* __restrict__ h, op16* dz, float* colsum, float* dW, float* db,
-                                      int fmt, const float* gscale, int* found_inf) {
-    extern __shared__ float red[];
+// A warp takes a row at a time with lane j owning columns CPL j .. CPL j + CPL - 1
+// (K = 32 CPL: one coalesced 256- or 512-byte row per access) and keeps four rows'
+// loads in flight; partial sums stay in registers until one shared-memory
+// reduction over the block's 8 warps at the end.
+template <int NO, int CPL>
+__global__ void __launch_bounds__(256)
+    head_bwd_fused_kernel(int64_t M, int K, const float* __restrict__ dsigma, const float* __restrict__ sraw,
+                          const float* __restrict__ drgb, const float* __restrict__ rgb, const float* __restrict__ W,
+                          const op16* __restrict__ h, op16* dz, float* colsum, float* dW, float* db, int fmt,
+                          const float* gscale, int* found_inf) {
+    constexpr int RPP = 4;   // independent rows in flight per warp
+    __shared__ float red[8][256 + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float gs0 = gscale ? gscale[0] : 1.f, gs1 = gscale ? gscale[1] : 1.f;
     const float vmax = tc::fmt_max(fmt);
     bool bad = false;
-    const int cpr = K / 8;
-    const int rpb = blockDim.x / cpr;
-    const int chunk = threadIdx.x % cpr, rloc = threadIdx.x / cpr;
-    float w[NO][8];
+    float w[NO][CPL], dwl[NO][CPL], cs[CPL], dbl[NO];
 #pragma unroll
-    for (int u = 0; u < NO; ++u)
+    for (int u = 0; u < NO; ++u) {
+        dbl[u] = 0.f;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) w[u][i] = W[u * K + chunk * 8 + i];
-    float cs[8], dwl[NO][8], dbl[NO];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        cs[i] = 0.f;
-#pragma unroll
-        for (int u = 0; u < NO; ++u) dwl[u][i] = 0.f;
+        for (int i = 0; i < CPL; ++i) {
+            w[u][i] = W[u * K + lane * CPL + i];
+            dwl[u][i] = 0.f;
+        }
     }
 #pragma unroll
-    for (int u = 0; u < NO; ++u) dbl[u] = 0.f;
-    // two rows per pass: both rows' loads are issued before either row's arithmetic
-    const int64_t stride = int64_t(gridDim.x) * rpb;
-    for (int64_t r0 = int64_t(blockIdx.x) * rpb + rloc; r0 < M; r0 += 2 * stride) {
-        const int64_t rows[2] = {r0, r0 + stride};
-        float g[2][NO], hx[2][8];
+    for (int i = 0; i < CPL; ++i) cs[i] = 0.f;
+    const int64_t wstride = int64_t(gridDim.x) * 8;
+    for (int64_t r0 = int64_t(blockIdx.x) * 8 + warp; r0 < M; r0 += RPP * wstride) {
+        float g[RPP][NO];
+        uint32_t raw[RPP][CPL / 2];
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            const int64_t r = rows[t];
+        for (int t = 0; t < RPP; ++t) {   // every row's loads before any row's arithmetic
+            const int64_t r = r0 + t * wstride;
             if (r >= M) continue;
             int u0 = 0;
             if (NO == 4) {
@@ -400,65 +408,70 @@ __global__ void head_bwd_fused_kernel(int64_t M, int K, const float* __restrict_
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                float v = rgb[3 * r + c];
+                const float v = rgb[3 * r + c];
                 g[t][u0 + c] = drgb[3 * r + c] * v * (1.f - v);
             }
-            uint4 raw = *reinterpret_cast<const uint4*>(h + r * K + chunk * 8);
-            uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                float2 f = tc::unpack16(w4[q], fmt);
-                hx[t][2 * q] = f.x;
-                hx[t][2 * q + 1] = f.y;
+            const op16* hr = h + r * K + lane * CPL;
+            if (CPL == 8) {
+                const uint4 q = *reinterpret_cast<const uint4*>(hr);
+                raw[t][0] = q.x; raw[t][CPL / 2 > 1 ? 1 : 0] = q.y;
+                raw[t][CPL / 2 > 2 ? 2 : 0] = q.z; raw[t][CPL / 2 > 3 ? 3 : 0] = q.w;
+            } else {
+                const uint2 q = *reinterpret_cast<const uint2*>(hr);
+                raw[t][0] = q.x; raw[t][CPL / 2 > 1 ? 1 : 0] = q.y;
             }
         }
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            const int64_t r = rows[t];
+        for (int t = 0; t < RPP; ++t) {
+            const int64_t r = r0 + t * wstride;
             if (r >= M) continue;
-            float o[8];
+            uint32_t o[CPL / 2];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                float v = 0.f;
+            for (int p = 0; p < CPL / 2; ++p) {
+                const float2 hx = tc::unpack16(raw[t][p], fmt);
+                float v0 = 0.f, v1 = 0.f;
 #pragma unroll
                 for (int u = 0; u < NO; ++u) {
-                    v += g[t][u] * w[u][i];
-                    dwl[u][i] += g[t][u] * hx[t][i];
+                    v0 += g[t][u] * w[u][2 * p];
+                    v1 += g[t][u] * w[u][2 * p + 1];
+                    dwl[u][2 * p] += g[t][u] * hx.x;
+                    dwl[u][2 * p + 1] += g[t][u] * hx.y;
                 }
-                o[i] = hx[t][i] > 0.f ? v * gs0 : 0.f;
-                cs[i] += o[i];
-                bad |= !(fabsf(o[i]) <= vmax);
+                v0 = hx.x > 0.f ? v0 * gs0 : 0.f;
+                v1 = hx.y > 0.f ? v1 * gs0 : 0.f;
+                cs[2 * p] += v0;
+                cs[2 * p + 1] += v1;
+                bad |= !(fabsf(v0) <= vmax) || !(fabsf(v1) <= vmax);
+                o[p] = tc::pack16(v0, v1, fmt);
             }
-            *reinterpret_cast<uint4*>(dz + r * K + chunk * 8) =
-                make_uint4(tc::pack16(o[0], o[1], fmt), tc::pack16(o[2], o[3], fmt), tc::pack16(o[4], o[5], fmt),
-                           tc::pack16(o[6], o[7], fmt));
-            if (chunk == 0) {
+            op16* dr = dz + r * K + lane * CPL;
+            if (CPL == 8) *reinterpret_cast<uint4*>(dr) = make_uint4(o[0], o[CPL / 2 > 1 ? 1 : 0],
+                                                                     o[CPL / 2 > 2 ? 2 : 0], o[CPL / 2 > 3 ? 3 : 0]);
+            else *reinterpret_cast<uint2*>(dr) = make_uint2(o[0], o[CPL / 2 > 1 ? 1 : 0]);
+            if (lane == 0) {
 #pragma unroll
                 for (int u = 0; u < NO; ++u) dbl[u] += g[t][u];
             }
         }
     }
-    // block reduction over the rloc rows, one quantity (K floats) at a time
-    auto reduce = [&](const float (&vals)[8], float* dst) {
+    // block sums over the 8 warps, one K-vector at a time, then one atomic per column
+    auto reduce = [&](const float (&vals)[CPL], float* dst, float scale) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) red[rloc * K + chunk * 8 + i] = vals[i];
+        for (int i = 0; i < CPL; ++i) red[warp][lane * CPL + i] = vals[i];
         __syncthreads();
         for (int k = threadIdx.x; k < K; k += blockDim.x) {
-            float s = 0.f;
-            for (int rr = 0; rr < rpb; ++rr) s += red[rr * K + k];
-            atomicAdd(dst + k, s);
+            float sum = 0.f;
+#pragma unroll
+            for (int ww = 0; ww < 8; ++ww) sum += red[ww][k];
+            atomicAdd(dst + k, sum * scale);
         }
         __syncthreads();
     };
     if (found_inf && bad) atomicExch(found_inf, 1);
-    if (colsum) {
+    if (colsum) reduce(cs, colsum, gs1);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) cs[i] *= gs1;
-        reduce(cs, colsum);
-    }
-#pragma unroll
-    for (int u = 0; u < NO; ++u) reduce(dwl[u], dW + u * K);
-    if (chunk == 0) {
+    for (int u = 0; u < NO; ++u) reduce(dwl[u], dW + u * K, 1.f);
+    if (lane == 0) {
 #pragma unroll
         for (int u = 0; u < NO; ++u) atomicAdd(db + u, dbl[u]);
     }
@@ -468,13 +481,16 @@ template <int NO>
 int head_bwd_fused(int64_t M, int K, const float* dsigma, const float* sraw, const float* drgb, const float* rgb,
                    const float* W, const op16* h, op16* dz, float* colsum, float* dW, float* db, int fmt,
                    const float* gscale, int* found_inf, cudaStream_t s) {
-    const int threads = 256;
-    const int rpb = threads / (K / 8);
-    int64_t blocks = (M + rpb - 1) / rpb;
+    if (K != 128 && K != 256) return SRF_ERR_UNSUPPORTED;
+    if (M <= 0) return SRF_OK;
+    int64_t blocks = (M + 31) / 32;
     if (blocks > int64_t(num_sms()) * 8) blocks = int64_t(num_sms()) * 8;
-    if (blocks < 1) blocks = 1;
-    head_bwd_fused_kernel<NO><<<unsigned(blocks), threads, size_t(rpb) * K * sizeof(float), s>>>(
-        M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum, dW, db, fmt, gscale, found_inf);
+    if (K == 128)
+        head_bwd_fused_kernel<NO, 4><<<unsigned(blocks), 256, 0, s>>>(M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum,
+                                                                     dW, db, fmt, gscale, found_inf);
+    else
+        head_bwd_fused_kernel<NO, 8><<<unsigned(blocks), 256, 0, s>>>(M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum,
+                                                                     dW, db, fmt, gscale, found_inf);
     return launch_status();
 }
 
@@ -677,7 +693,7 @@ int wgrad_layer(const LayerMap& lm, float* partial, size_t partial_floats, const
     int st = tc_wgrad(partial, partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
                       lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt, bias_grad, cx.gscale());
     if (st) return st;
-    dim3 grid((lm.kpad() + 127) / 128, lm.n);
+    dim3 grid((lm.kpad() + 31) / 32, lm.n);
     reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale());
     return launch_status();
 }
