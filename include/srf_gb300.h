@@ -480,6 +480,19 @@ typedef struct srf_tv_component {
  * weight_color. */
 int srf_tv_loss(const srf_tv_component* components, int n_components, float weight, const float* scale_dev,
                 float* loss_dev, void* stream);
+/* Online tuning of equivalent kernel shapes (on by default).  The first call of a
+ * tuned launch site with a new shape times each candidate on that call's own
+ * inputs and caches the fastest: the layer GEMM's epilogue warp count (site 1, key
+ * BN, K blocks, epilogue flags), the TensoRF basis pass's tile (site 2, key C, k1p)
+ * and the VM colour gather's lanes per point (site 3, key R0, R1, R2).  Nothing is
+ * timed during CUDA-graph capture or when disabled (the launches then take the
+ * built-in rules), and only launches whose outputs are plain overwrites are tuned.
+ * The table can be listed (count / entry) and preloaded (set) to reuse choices. */
+int srf_autotune_enable(int on);
+int srf_autotune_count(void);
+int srf_autotune_entry(int index, int* site, int64_t* a, int64_t* b, int64_t* c, int* choice);
+int srf_autotune_set(int site, int64_t a, int64_t b, int64_t c, int choice);
+int srf_autotune_clear(void);
 /* *counter_dev += value on the stream (advances a graph-replayed step count),
  * unless skip_dev != NULL and *skip_dev != 0. */
 int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, void* stream);

@@ -130,6 +130,12 @@ _SIGS = {
                                              c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
     'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
+    'srf_autotune_enable': (c_int, [c_int]),
+    'srf_autotune_count': (c_int, []),
+    'srf_autotune_entry': (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int64), ctypes.POINTER(c_int64),
+                                   ctypes.POINTER(c_int64), ctypes.POINTER(c_int)]),
+    'srf_autotune_set': (c_int, [c_int, c_int64, c_int64, c_int64, c_int]),
+    'srf_autotune_clear': (c_int, []),
     'srf_adam_multi_step': (c_int, [ctypes.POINTER(AdamTensor), c_int, c_float, c_float, c_float, c_float, c_int, P,
                                     P, P]),
     'srf_launch_count': (c_int64, []),

@@ -2,7 +2,11 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
+#include "autotune.cuh"
 #include "srf_common.cuh"
 
 namespace {
@@ -36,7 +40,79 @@ int* device_flag() {
     return cache[dev];
 }
 
+namespace tune {
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int64_t, int64_t, int64_t>, int> g_tune_table;
+std::atomic<int> g_tune_on{1};
+}  // namespace
+
+bool enabled() { return g_tune_on.load() != 0; }
+
+int lookup(const Key& k) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_table.find(std::make_tuple(k.site, k.a, k.b, k.c));
+    return it == g_tune_table.end() ? -1 : it->second;
+}
+
+void store(const Key& k, int choice) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_table[std::make_tuple(k.site, k.a, k.b, k.c)] = choice;
+}
+
+int count() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    return int(g_tune_table.size());
+}
+
+bool entry(int i, Key* k, int* choice) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (i < 0 || i >= int(g_tune_table.size())) return false;
+    auto it = g_tune_table.begin();
+    std::advance(it, i);
+    *k = Key{std::get<0>(it->first), std::get<1>(it->first), std::get<2>(it->first), std::get<3>(it->first)};
+    *choice = it->second;
+    return true;
+}
+
+void clear() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_table.clear();
+}
+
+void set_enabled(int on) { g_tune_on.store(on ? 1 : 0); }
+}  // namespace tune
+
 }  // namespace srf
+
+extern "C" int srf_autotune_enable(int on) {
+    srf::tune::set_enabled(on);
+    return SRF_OK;
+}
+
+extern "C" int srf_autotune_count(void) { return srf::tune::count(); }
+
+extern "C" int srf_autotune_entry(int index, int* site, int64_t* a, int64_t* b, int64_t* c, int* choice) {
+    if (!site || !a || !b || !c || !choice) return SRF_ERR_NULL;
+    srf::tune::Key k{};
+    if (!srf::tune::entry(index, &k, choice)) return SRF_ERR_SHAPE;
+    *site = k.site;
+    *a = k.a;
+    *b = k.b;
+    *c = k.c;
+    return SRF_OK;
+}
+
+extern "C" int srf_autotune_set(int site, int64_t a, int64_t b, int64_t c, int choice) {
+    if (choice < 0) return SRF_ERR_SHAPE;
+    srf::tune::store(srf::tune::Key{site, a, b, c}, choice);
+    return SRF_OK;
+}
+
+extern "C" int srf_autotune_clear(void) {
+    srf::tune::clear();
+    return SRF_OK;
+}
 
 extern "C" const char* srf_status_string(int status) {
     switch (status) {

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "nerf_mlp.h"
+#include "autotune.cuh"
 #include "tc_gemm.cuh"
 
 namespace srf {
@@ -107,13 +108,23 @@ int launch_gemm_ew(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorM
 // ahead of the memory system; they need two more 4 KB staging areas, so layers whose
 // resident weights leave fewer than two activation stages (K = 320 at N = 256) and the
 // 64-wide layers (32 columns per warp: no 64-column TMA boxes) run on 4.
+// Where both fit and the epilogue only overwrites its outputs, the tuner times the two
+// on the first call of each (BN, K blocks, epilogue flags) and keeps the faster.
 template <int BN>
 int launch_gemm_bn(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b, const CUtensorMap& out,
                    tc::GemmShape sh, tc::GemmEpilogue ep, cudaStream_t s) {
     const int kb = sh.kb0 + sh.kb1;
     const bool eight = BN >= 128 && tc::SmemPlan<BN, 8>::stages(kb) >= 2;
-    if (eight) return launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s);
-    return launch_gemm_ew<BN, 4>(a0, a1, b, out, sh, ep, s);
+    const bool four = tc::SmemPlan<BN, 4>::stages(kb) >= 2;
+    const bool pure = !ep.colsum && !ep.r1_sum && !ep.r1_mask_colsum;
+    auto run = [&](int i) {
+        return i == 0 ? launch_gemm_ew<BN, 8>(a0, a1, b, out, sh, ep, s) : launch_gemm_ew<BN, 4>(a0, a1, b, out, sh, ep, s);
+    };
+    if (eight && four && pure) {
+        const tune::Key key{tune::kSiteGemmEpilogueWarps, BN, kb, tc::epi_mode(ep)};
+        return run(tune::pick(key, 2, 0, s, run));
+    }
+    return run(eight ? 0 : 1);
 }
 
 }  // namespace
@@ -1312,15 +1323,29 @@ int launch_basis_encode_cfg(const float* feats, int C, const float* WbT, int F, 
     return launch_status();
 }
 
-// The basis + encoding pass with the deepest tile whose shared memory fits.
+// The basis + encoding pass: tile shapes (rows per thread x threads) the tuner picks
+// from per (C, k1p); without tuning, the first whose shared memory fits (128 x 2
+// measured fastest for C = 144).
 int launch_basis_encode(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
                         int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
     if (m <= 0) return SRF_OK;
-    if (enc_smem_bytes(C, k1p, 2, kEncThreads) <= tc::kMaxSmem)
-        return launch_basis_encode_cfg<2, kEncThreads>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
-    if (enc_smem_bytes(C, k1p, 1, kEncThreads) <= tc::kMaxSmem)
-        return launch_basis_encode_cfg<1, kEncThreads>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
-    return SRF_ERR_UNSUPPORTED;
+    auto run = [&](int i) -> int {
+#define SRF_ENC(R, N)                                                                                             \
+    (enc_smem_bytes(C, k1p, R, N) <= tc::kMaxSmem                                                                 \
+         ? launch_basis_encode_cfg<R, N>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s)                \
+         : SRF_ERR_UNSUPPORTED)
+        switch (i) {
+            case 0: return SRF_ENC(2, 128);
+            case 1: return SRF_ENC(4, 128);
+            case 2: return SRF_ENC(1, 256);
+            case 3: return SRF_ENC(2, 256);
+            default: return SRF_ENC(1, 128);
+        }
+#undef SRF_ENC
+    };
+    const int fallback = enc_smem_bytes(C, k1p, 2, 128) <= tc::kMaxSmem ? 0 : 4;
+    const tune::Key key{tune::kSiteBasisEncode, C, k1p, 0};
+    return run(tune::pick(key, 5, fallback, s, run));
 }
 
 // P = {Wb (F x C), W1 (U x k1), b1, W2 (U x U), b2, W3 (3 x U), b3}

@@ -8,6 +8,7 @@
 #include <mutex>
 #include <type_traits>
 
+#include "autotune.cuh"
 #include "srf_common.cuh"
 
 namespace srf {
@@ -649,16 +650,27 @@ extern "C" int srf_vm_color_forward(const srf_vm_grid* grid, const float* pts, i
     if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
     int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
     const int G = group_lanes(*grid);
-    if (G && (ld & 3) == 0 && aligned16(features)) {
-        return launch_grouped(G, n_pts, [&](auto gc) {
-            constexpr int g = decltype(gc)::value;
-            color_fwd_group_kernel<g><<<grid_1d(n_pts * g, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, ld,
-                                                                                              features);
+    // candidates: every group size that divides the component counts (G, G/2, ..., 1),
+    // then the per-thread kernel; the tuner times them per (R0, R1, R2)
+    int cand[6], nc = 0;
+    if (G && (ld & 3) == 0 && aligned16(features))
+        for (int g = G; g >= 1; g >>= 1) cand[nc++] = g;
+    cand[nc++] = 0;
+    auto run = [&](int i) -> int {
+        const int g = cand[i];
+        if (g == 0) {
+            color_fwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, ld, features);
+            return launch_status();
+        }
+        return launch_grouped(g, n_pts, [&](auto gc) {
+            constexpr int gg = decltype(gc)::value;
+            color_fwd_group_kernel<gg><<<grid_1d(n_pts * gg, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts,
+                                                                                                ld, features);
             return launch_status();
         });
-    }
-    color_fwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grid, pts, n_pts, ld, features);
-    return launch_status();
+    };
+    const tune::Key key{tune::kSiteVmColorGroup, grid->n_comp[0], grid->n_comp[1], grid->n_comp[2]};
+    return run(tune::pick(key, nc, 0, as_stream(stream), run));
 }
 
 extern "C" int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,

@@ -340,3 +340,44 @@ def test_loss_kernel():
     assert abs(float(loss.item()) - ref_loss) < 1e-5 * max(1, ref_loss)
     np.testing.assert_allclose(n(g_rgb), grads['rgb_c'], rtol=1e-5, atol=1e-9)
     np.testing.assert_allclose(n(g_depth), grads['depth_c'], rtol=1e-5, atol=1e-9)
+
+
+def test_autotuned_launches_match_untuned_results():
+    """The tuned sites (layer GEMM epilogue warps, VM colour lanes per point, TensoRF
+    basis tile) give bitwise the same results as the built-in choices, and record
+    their choices."""
+    import ctypes
+    from simple_rf_gb300 import _lib, autotune
+    from simple_rf_gb300 import tensorf as T
+    gen = torch.Generator(device='cuda').manual_seed(21)
+    m, k, n = 40000, 256, 256
+    x = torch.randn(m, k, device=DEV, generator=gen).to(torch.bfloat16)
+    w = (torch.randn(n, k, device=DEV, generator=gen) * 0.05).to(torch.bfloat16)
+    b = torch.randn(n, device=DEV, generator=gen)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda q: ctypes.c_void_p(q.data_ptr())  # noqa: E731
+
+    def gemm():
+        y = torch.empty(m, n, device=DEV, dtype=torch.bfloat16)
+        _lib.call('srf_bf16_linear', p(y), n, p(x), k, k, None, 0, 0, p(w), k, n, 0, p(b), m, n, 1, None, 0, None, st)
+        return y
+
+    planes = [torch.randn(1, 48, 40, 40, device=DEV, generator=gen) * 0.1 for _ in range(3)]
+    lines = [torch.randn(1, 48, 40, 1, device=DEV, generator=gen) * 0.1 for _ in range(3)]
+    grid = T.VmGridTensors([T.to_channels_last(q) for q in planes], [T.to_channels_last(q) for q in lines], [40] * 3)
+    pts = torch.rand(30000, 3, device=DEV, generator=gen) * 2 - 1
+
+    def color():
+        return T.vm_color(grid, pts)
+
+    autotune.clear()
+    autotune.enable(False)
+    ref_y, ref_c = gemm(), color()
+    autotune.enable(True)
+    y1, c1 = gemm(), color()      # tuned now
+    y2, c2 = gemm(), color()      # from the table
+    torch.cuda.synchronize()
+    sites = {e['site'] for e in autotune.table()}
+    assert {1, 3} <= sites
+    assert torch.equal(y1, ref_y) and torch.equal(y2, ref_y)
+    assert torch.equal(c1, ref_c) and torch.equal(c2, ref_c)
