@@ -172,6 +172,35 @@ def roofline_gemm(dev, hbm_peak, peak_tflops, peak_kind, reps=50):
             'tensor_frac_of_bf16_burst': round(flops / t / 1e12 / peak_tflops, 4)}
 
 
+def kernel_rooflines(hbm_peak, peak_kind):
+    """The memory-bound kernels of the path timed alone (CUDA events, 20 launches
+    after 3 warm-up launches) with their algorithmic bytes per launch:
+    compositing forward / adjoint over a 65,536-ray render chunk of 192 samples
+    (302 MB of per-sample inputs, larger than L2), and the TensoRF VM lookups and
+    their scatter-add adjoints at the 300^3 grid over 1.25M ray-ordered points
+    (R = 48 colour, R = 16 density; the 52 MB of planes stay L2-resident, so
+    the fraction of the HBM copy peak may exceed 1)."""
+    import argparse as _ap
+    import torch
+    from simple_rf_gb300 import bench_kernels as bk
+    runs = [('composite', dict(rays=65536, samples=192, backward=False)),
+            ('composite', dict(rays=65536, samples=192, backward=True)),
+            ('vm', dict(rays=1216, samples=1024, comps=48, kind='color', res=300, backward=False)),
+            ('vm', dict(rays=1216, samples=1024, comps=48, kind='color', res=300, backward=True)),
+            ('vm', dict(rays=1216, samples=1024, comps=16, kind='density', res=300, backward=False)),
+            ('vm', dict(rays=1216, samples=1024, comps=16, kind='density', res=300, backward=True))]
+    out = []
+    for which, kw in runs:
+        args = _ap.Namespace(reps=20, warmup=3, **kw)
+        r = getattr(bk, which)(args)
+        out.append({'kernel': r['kernel'], 'workload': {k: v for k, v in kw.items() if k != 'backward'},
+                    'launch_ms': round(r['ms'], 4), 'algorithmic_bytes_per_launch': int(r['bytes']),
+                    'achieved': round(r['gbs'], 1), 'peak': hbm_peak, 'unit': 'GB/s',
+                    'frac': round(r['gbs'] / hbm_peak, 4), 'peak_source': peak_kind + ' copy bandwidth'})
+        torch.cuda.empty_cache()
+    return out
+
+
 def rgb_agreement(step_cls, batch, dev):
     """Coarse-pass rgb of the BF16 step against the FP32 plain step from the same
     weights and batch (the fine pass samples different depths once the coarse
@@ -376,6 +405,7 @@ def run_ours(args):
         t_bf = time_steps(bf_step, args.steps, stream)
         # the dominant kernel timed alone right after the step, under the same clock record
         roof = roofline_gemm(dev, hbm_peak, tf_peak, peak_kind) if rank == 0 else None
+        kroofs = kernel_rooflines(hbm_peak, peak_kind) if rank == 0 else None
     barrier()
     t_bf = max_over_ranks(t_bf)
     # rgb agreement of the BF16 step with the FP32 plain step (same weights, same batch)
@@ -474,6 +504,7 @@ def run_ours(args):
         'gpu_launches_per_step': launches,
         'clocks': clocks.summary(),
         'roofline': roof,
+        'kernel_rooflines': kroofs,
     }
     if ws == 1:
         line['cpu_baseline'] = cpu_baseline()

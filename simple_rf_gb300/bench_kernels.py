@@ -2,7 +2,8 @@
 
     python -m simple_rf_gb300.bench_kernels gemm --m 786432 --k 256 --n 256
     python -m simple_rf_gb300.bench_kernels wgrad --m 786432 --n 256 --k 256
-    python -m simple_rf_gb300.bench_kernels composite --rays 4096 --samples 192
+    python -m simple_rf_gb300.bench_kernels composite --rays 4096 --samples 192 [--backward]
+    python -m simple_rf_gb300.bench_kernels vm --rays 1216 --samples 1024 --comps 48 [--kind density] [--backward]
 
 Each prints one JSON line: the average launch time over --reps launches
 (CUDA events on the launching stream, after --warmup launches) and the achieved
@@ -83,6 +84,8 @@ def wgrad(args):
 
 
 def composite(args):
+    """Compositing forward (or, with --backward, the reverse-scan adjoint, which
+    recomputes the forward scan) over rays x samples."""
     nr, s = args.rays, args.samples
     g = torch.Generator(device='cuda').manual_seed(0)
     sigma = torch.rand(nr, s, device='cuda', generator=g)
@@ -94,20 +97,87 @@ def composite(args):
     a = _lib.CompositeArgs()
     a.n_rays, a.n_samples, a.flags, a.distance_scale = nr, s, _lib.SRF_COMPOSITE_WHITE_BKGD, 1.0
     a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), d.data_ptr()
-    a.rgb_map, a.acc, a.depth, a.depth_var, a.weights = (outs['rgb_map'].data_ptr(), outs['acc'].data_ptr(),
-                                                         outs['depth'].data_ptr(), outs['dv'].data_ptr(), w.data_ptr())
+    if args.backward:
+        g_rgb = torch.randn(nr, 3, device='cuda', generator=g)
+        g_depth = torch.randn(nr, device='cuda', generator=g)
+        d_sigma = torch.empty(nr, s, device='cuda')
+        d_rgb = torch.empty(nr, s, 3, device='cuda')
+        a.g_rgb, a.g_depth, a.d_sigma, a.d_rgb = g_rgb.data_ptr(), g_depth.data_ptr(), d_sigma.data_ptr(), \
+            d_rgb.data_ptr()
+        name = 'srf_composite_backward'
+        # reads sigma, rgb, z; writes d_sigma, d_rgb
+        nbytes = nr * s * (4 + 12 + 4 + 4 + 12) + nr * (12 + 12 + 4)
+    else:
+        a.rgb_map, a.acc, a.depth, a.depth_var, a.weights = (outs['rgb_map'].data_ptr(), outs['acc'].data_ptr(),
+                                                             outs['depth'].data_ptr(), outs['dv'].data_ptr(),
+                                                             w.data_ptr())
+        name = 'srf_composite_forward'
+        # reads sigma, rgb, z; writes weights
+        nbytes = nr * s * (4 + 12 + 4 + 4) + nr * (12 + 12)
 
     def run():
-        _lib.call('srf_composite_forward', ctypes.byref(a), _st())
+        _lib.call(name, ctypes.byref(a), _st())
     t = _time(run, args.reps, args.warmup)
-    nbytes = nr * s * (4 + 12 + 4 + 4) + nr * (12 + 12)
-    return {'kernel': 'composite_fwd_kernel', 'rays': nr, 'samples': s, 'ms': t * 1e3, 'gbs': nbytes / t / 1e9,
-            'bytes': nbytes}
+    return {'kernel': 'composite_bwd_kernel' if args.backward else 'composite_fwd_kernel', 'rays': nr, 'samples': s,
+            'ms': t * 1e3, 'gbs': nbytes / t / 1e9, 'bytes': nbytes}
+
+
+def vm_points(n_rays, samples, seed=0):
+    """Normalised sample points in ray order (what the renderer hands the VM
+    lookups): rays through the box, ``samples`` evenly spaced points on each."""
+    g = torch.Generator(device='cuda').manual_seed(seed)
+    o = torch.rand(n_rays, 3, device='cuda', generator=g) * 2 - 1
+    e = torch.rand(n_rays, 3, device='cuda', generator=g) * 2 - 1
+    t = torch.linspace(0, 1, samples, device='cuda')
+    return (o[:, None, :] + (e - o)[:, None, :] * t[None, :, None]).reshape(-1, 3).contiguous()
+
+
+def vm(args):
+    """VM plane/line gathers (or, with --backward, the 128-bit scatter-add
+    adjoint) at a res^3 grid with R components per plane/line.  Algorithmic
+    bytes per point: 3 planes x 4 corners + 3 lines x 2 ends, R floats each
+    (3456 B at R = 48, 1152 B at R = 16), plus the point and the features; the
+    backward reads d_features and both factors' corners and read-modify-writes
+    the gradient corners (3x the corner bytes).  The
+    grid itself (3 x res^2 x R x 4 B, 51.8 MB at 300^2 x 48) stays in the 129 MB
+    L2, so the fraction of the HBM copy peak can exceed 1."""
+    from .tensorf import VmGridTensors, _grid_struct
+    res, r, p = args.res, args.comps, args.rays * args.samples
+    g = torch.Generator(device='cuda').manual_seed(0)
+    planes = [(torch.randn(1, r, res, res, device='cuda', generator=g) * 0.1).contiguous(
+        memory_format=torch.channels_last) for _ in range(3)]
+    lines = [(torch.randn(1, r, res, 1, device='cuda', generator=g) * 0.1).contiguous(
+        memory_format=torch.channels_last) for _ in range(3)]
+    grid = VmGridTensors(planes, lines, [res] * 3)
+    gs = _grid_struct(grid.res, grid.planes, grid.lines)
+    pts = vm_points(args.rays, args.samples)
+    color = args.kind == 'color'
+    feat = torch.empty(p, 3 * r if color else 1, device='cuda')
+    corner = (3 * 4 + 3 * 2) * r * 4
+    if args.backward:
+        gp = [torch.zeros_like(x) for x in planes]
+        gl = [torch.zeros_like(x) for x in lines]
+        gg = _grid_struct(grid.res, gp, gl)
+        dfeat = torch.randn(p, feat.shape[1], device='cuda', generator=g)
+        name = 'srf_vm_color_backward' if color else 'srf_vm_density_backward'
+
+        def run():
+            _lib.call(name, ctypes.byref(gg), ctypes.byref(gs), _p(pts), p, _p(dfeat), _st())
+        nbytes = p * (3 * corner + 12 + feat.shape[1] * 4)
+    else:
+        name = 'srf_vm_color_forward' if color else 'srf_vm_density_forward'
+
+        def run():
+            _lib.call(name, ctypes.byref(gs), _p(pts), p, _p(feat), _st())
+        nbytes = p * (corner + 12 + feat.shape[1] * 4)
+    t = _time(run, args.reps, args.warmup)
+    return {'kernel': name, 'res': res, 'comps': r, 'points': p, 'ms': t * 1e3, 'gbs': nbytes / t / 1e9,
+            'bytes': nbytes, 'bytes_per_point': nbytes // p}
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('which', choices=['gemm', 'wgrad', 'composite'])
+    ap.add_argument('which', choices=['gemm', 'wgrad', 'composite', 'vm'])
     ap.add_argument('--m', type=int, default=786432)
     ap.add_argument('--k', type=int, default=256)
     ap.add_argument('--n', type=int, default=256)
@@ -116,10 +186,14 @@ def main(argv=None):
     ap.add_argument('--reps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--dgrad', action='store_true', help='gemm: backward-data epilogue (mask + column sums)')
+    ap.add_argument('--backward', action='store_true', help='composite / vm: the adjoint kernel')
+    ap.add_argument('--kind', choices=['color', 'density'], default='color', help='vm: which lookup')
+    ap.add_argument('--res', type=int, default=300, help='vm: grid resolution per axis')
+    ap.add_argument('--comps', type=int, default=48, help='vm: components per plane/line')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
-    res = {'gemm': gemm, 'wgrad': wgrad, 'composite': composite}[args.which](args)
+    res = {'gemm': gemm, 'wgrad': wgrad, 'composite': composite, 'vm': vm}[args.which](args)
     print(json.dumps({k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.items()}))
 
 

@@ -8,6 +8,7 @@ kernels.  Inputs must be contiguous float32 CUDA tensors; nothing here runs on
 the CPU.
 """
 import ctypes
+import math
 
 import torch
 
@@ -179,6 +180,52 @@ def found_inf_ptr(scaler):
     return None if scaler is None else ctypes.c_void_p(scaler.data_ptr() + 8)
 
 
+# Bytes of saved activations one NerfMlpFunction call may hold between its
+# forward and backward; None = half of the device memory free at the call.
+_activation_budget = [None]
+
+
+class activation_budget:
+    """Context manager (or plain call) setting the activation budget of the
+    NeRF MLP autograd op: ``with activation_budget(8 << 30): loss = model(...)``.
+
+    A forward whose backward workspace would exceed the budget keeps only its
+    inputs; its backward recomputes the activations ray chunk by ray chunk (each
+    chunk within the budget) and accumulates the parameter gradients chunk by
+    chunk.  ``None`` restores the default (half of the free device memory)."""
+
+    def __init__(self, nbytes):
+        self.prev = _activation_budget[0]
+        _activation_budget[0] = None if nbytes is None else int(nbytes)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        _activation_budget[0] = self.prev
+
+
+def recompute_rows(m, dir_div, budget, ws_bytes):
+    """Rows per recomputation chunk: the largest multiple of lcm(dir_div, 128)
+    (whole rays, and 512-byte aligned sub-tensor offsets) whose backward
+    workspace ``ws_bytes(rows)`` fits ``budget``; 0 when all m rows fit (no
+    recomputation).  Raises when even one unit exceeds the budget."""
+    if m == 0 or ws_bytes(m) <= budget:
+        return 0
+    unit = dir_div * 128 // math.gcd(dir_div, 128)
+    if ws_bytes(unit) > budget:
+        raise RuntimeError(f'activation budget {budget} B is below one chunk of {unit} samples '
+                           f'({ws_bytes(unit)} B of workspace)')
+    lo, hi = 1, max(1, -(-m // unit))
+    while lo < hi:  # largest k with ws_bytes(k * unit) <= budget
+        mid = (lo + hi + 1) // 2
+        if ws_bytes(mid * unit) <= budget:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo * unit
+
+
 class NerfMlpFunction(torch.autograd.Function):
     """MLP.forward (SimpleNeRF17.py:696-785) with the hand-written backward.
 
@@ -187,7 +234,15 @@ class NerfMlpFunction(torch.autograd.Function):
     through the layers; srf_loss_scaler_fit); a gradient that still leaves the
     FP16 range gives non-finite parameter gradients and sets the scaler's
     found_inf.  The fused training step (train_step.py) instead carries one
-    dynamic scale across steps and skips steps that overflow."""
+    dynamic scale across steps and skips steps that overflow.
+
+    When the activations the backward needs exceed the activation budget
+    (:class:`activation_budget`), the forward runs chunk by chunk without keeping
+    them and the backward recomputes each chunk's activations just before that
+    chunk's adjoint (same kernels, same rows: the recomputed activations equal
+    the first pass's bit for bit); the parameter gradients then sum the chunks'
+    contributions (the order of the sum over samples differs from the unchunked
+    pass by rounding only)."""
 
     @staticmethod
     def forward(ctx, spec, precision, pts, dirs, dir_div, noise, *params):
@@ -199,20 +254,36 @@ class NerfMlpFunction(torch.autograd.Function):
             _require(noise, 'noise', (m,))
         params = [p.detach().contiguous() for p in params]
         need_grad = any(ctx.needs_input_grad[6:])
-        ws = torch.empty(max(spec.workspace_bytes(m, precision, need_grad), 1), dtype=torch.uint8,
-                         device=pts.device)
         sigma = torch.empty(m, device=pts.device)
         rgb = torch.empty(m, 3, device=pts.device)
         scaler = None
         if precision == _lib.SRF_PRECISION_FP16:
             scaler = loss_scaler(pts.device)
+        rows = 0
+        if need_grad:
+            budget = _activation_budget[0]
+            if budget is None:
+                budget = torch.cuda.mem_get_info(pts.device)[0] // 2
+            rows = recompute_rows(m, dir_div, budget, lambda r: spec.workspace_bytes(r, precision, True))
+        ctx.spec, ctx.precision, ctx.dir_div, ctx.m, ctx.scaler = spec, precision, dir_div, m, scaler
+        ctx.params = params
+        ctx.rows = rows
+        ctx.set_materialize_grads(True)
+        if rows:
+            ws = torch.empty(max(spec.workspace_bytes(rows, precision, False), 1), dtype=torch.uint8,
+                             device=pts.device)
+            for r0 in range(0, m, rows):
+                _mlp_chunk_forward(spec, precision, params, pts, dirs, dir_div, noise, r0, min(rows, m - r0),
+                                   sigma, rgb, False, ws, scaler)
+            ctx.inputs = (pts, dirs, noise)
+            ctx.ws = None
+            return sigma, rgb
+        ws = torch.empty(max(spec.workspace_bytes(m, precision, need_grad), 1), dtype=torch.uint8,
+                         device=pts.device)
         call('srf_nerf_mlp_forward', ctypes.byref(spec.desc), _ptr_array(params), _ptr(pts), _ptr(dirs),
              int(dir_div), m, _ptr(noise), _ptr(sigma), _ptr(rgb), precision, int(need_grad), _ptr(ws),
              ws.numel(), _ptr(scaler), _stream())
-        ctx.spec, ctx.precision, ctx.dir_div, ctx.m, ctx.scaler = spec, precision, dir_div, m, scaler
         ctx.ws = ws if need_grad else None
-        ctx.params = params
-        ctx.set_materialize_grads(True)
         return sigma, rgb
 
     @staticmethod
@@ -223,11 +294,43 @@ class NerfMlpFunction(torch.autograd.Function):
         if ctx.scaler is not None:
             call('srf_loss_scaler_fit', _ptr(ctx.scaler), _ptr(dsigma), dsigma.numel(), _ptr(drgb), drgb.numel(),
                  1024.0, _stream())
+        if ctx.rows:
+            spec, precision, m, rows = ctx.spec, ctx.precision, ctx.m, ctx.rows
+            pts, dirs, noise = ctx.inputs
+            dev = pts.device
+            ws = torch.empty(max(spec.workspace_bytes(rows, precision, True), 1), dtype=torch.uint8, device=dev)
+            sig = torch.empty(rows, device=dev)
+            col = torch.empty(rows, 3, device=dev)
+            gp = _ptr_array(grads)
+            for i, r0 in enumerate(range(0, m, rows)):
+                r = min(rows, m - r0)
+                _mlp_chunk_forward(spec, precision, ctx.params, pts, dirs, ctx.dir_div, noise, r0, r, sig, col,
+                                   True, ws, ctx.scaler, out_offset=False)
+                call('srf_nerf_mlp_backward', ctypes.byref(spec.desc), _ptr_array(ctx.params),
+                     _ptr_at(dsigma, r0), _ptr_at(drgb, 3 * r0), int(ctx.dir_div), r, gp, int(i > 0), precision,
+                     _ptr(ws), ws.numel(), _ptr(ctx.scaler), _stream())
+            ctx.inputs = None
+            return (None, None, None, None, None, None) + tuple(grads)
         call('srf_nerf_mlp_backward', ctypes.byref(ctx.spec.desc), _ptr_array(ctx.params), _ptr(dsigma), _ptr(drgb),
              int(ctx.dir_div), ctx.m, _ptr_array(grads), 0, ctx.precision, _ptr(ctx.ws), ctx.ws.numel(),
              _ptr(ctx.scaler), _stream())
         ctx.ws = None
         return (None, None, None, None, None, None) + tuple(grads)
+
+
+def _ptr_at(t, offset):
+    """Device address of element ``offset`` of a contiguous tensor (None passes through)."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr() + offset * t.element_size())
+
+
+def _mlp_chunk_forward(spec, precision, params, pts, dirs, dir_div, noise, r0, r, sigma, rgb, for_backward, ws,
+                       scaler, out_offset=True):
+    """srf_nerf_mlp_forward over rows [r0, r0 + r) (r0 a multiple of dir_div);
+    outputs at the same rows of sigma/rgb, or at their start with out_offset=False."""
+    o = r0 if out_offset else 0
+    call('srf_nerf_mlp_forward', ctypes.byref(spec.desc), _ptr_array(params), _ptr_at(pts, 3 * r0),
+         _ptr_at(dirs, 3 * (r0 // dir_div)), int(dir_div), r, _ptr_at(noise, r0), _ptr_at(sigma, o),
+         _ptr_at(rgb, 3 * o), precision, int(for_backward), _ptr(ws), ws.numel(), _ptr(scaler), _stream())
 
 
 # -------------------------------------------------------------- compositing --

@@ -85,8 +85,13 @@ class GbMLP(torch.nn.Module):
         if self.training and self.raw_noise_std > 0:
             noise = torch.randn(pts.shape[0], device=pts.device) * self.raw_noise_std
         dirs = dirs.contiguous() if (dirs is not None and self.spec.use_view_dirs) else None
-        return F.NerfMlpFunction.apply(self.spec, self.precision, pts.contiguous(), dirs, dir_div, noise,
-                                       *self.parameters())
+        args = (self.spec, self.precision, pts.contiguous(), dirs, dir_div, noise, *self.parameters())
+        budget = self.configs['model'].get('activation_budget_bytes')
+        if budget is None:
+            return F.NerfMlpFunction.apply(*args)
+        # above the budget the backward recomputes activations per ray chunk instead of keeping them
+        with F.activation_budget(budget):
+            return F.NerfMlpFunction.apply(*args)
 
     def forward(self, input_batch: dict):
         """Reference contract (SimpleNeRF17.py:696): {'pts', 'view_dirs'} -> {'sigma', 'rgb'}."""

@@ -149,6 +149,47 @@ def test_fp16_train_step_meets_gradient_bar():
         assert rel < 1e-2, (tag, rel)
 
 
+@pytest.mark.parametrize('precision', ['fp32', 'fp16'])
+def test_step_gradients_against_fp64_finite_differences(precision):
+    """Gradients of the step on a 64-ray subset against float64 central finite
+    differences of the loss (depths held at the ones the GPU sampled, as the
+    reference's detach does, SimpleNeRF17.py:368): along each net's whole
+    gradient direction, seven single-tensor gradient directions and a random unit
+    direction.  FP32 plain: within max(1e-4, 3 e32) of the difference quotient,
+    e32 being the float32 oracle's own error on the same direction; FP16
+    operands: within 1e-2.  Random directions are compared on the scale of the
+    gradient norm (their directional derivative is a cancelling sum)."""
+    from oracle import fd
+    step, params, out, grads, host = _run_step(precision, n_rays=64, sigma_bias=0.5)
+    o, d, t_rgb, t_depth = [np.asarray(x, np.float64) for x in host[:4]]
+    mask = np.zeros(64)
+    mask[:16] = 1
+    _, _, g32 = _oracle(params, host, out['z_fine'], np.float32)
+    spec = on.MlpSpec()
+    keys = ('pts_linears.0.weight', 'pts_linears.5.weight', 'pts_output_linear.weight', 'pts_output_linear.bias',
+            'feature_linear.weight', 'views_linears.0.weight', 'views_output_linear.bias')
+    rng = np.random.default_rng(0)
+    worst = 0.0
+    for tag in ('coarse', 'fine'):
+        z = out[f'z_{tag}'].astype(np.float64)
+
+        def loss(prm):
+            return fd.level_loss(prm, spec, o, d, z, t_rgb, t_depth, mask)
+        gnorm = np.sqrt(sum(float(np.sum(v * v)) for v in grads[tag].values()))
+        for name, v in fd.unit_directions(grads[tag], keys, rng):
+            num = fd.directional_derivative(loss, params[tag], v, 1e-6)
+            scale = gnorm if name == 'random' else abs(num)
+            err = abs(fd.dot(grads[tag], v) - num) / scale
+            if precision == 'fp32':
+                e32 = abs(fd.dot(g32[tag], v) - num) / scale
+                bar = max(1e-4, 3 * e32)
+            else:
+                bar = 1e-2
+            worst = max(worst, err / bar)
+            assert err < bar, (tag, name, err, bar)
+    print(precision, 'worst finite-difference error / bar', worst)
+
+
 def test_fp16_overflow_skips_the_step():
     """A loss scale of 2^100 overflows the FP16 gradients: found_inf is raised,
     Adam leaves every parameter and the step count untouched, and the end of the
