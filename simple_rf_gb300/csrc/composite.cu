@@ -29,11 +29,16 @@ struct RayCtx {
     float oz, dz;   // world origin/direction z (NDC depth conversion)
 };
 
-// SimpleNeRF17.py:541-558 convert_depth_from_ndc (near = 1).
+// SimpleNeRF17.py:541-558 convert_depth_from_ndc (near = 1).  Every product
+// and sum is rounded on its own, as the reference's separate torch ops round
+// them (no fused multiply-adds): near z_ndc = 1 the factor 1 / (1 - z_ndc)
+// multiplies any rounding difference of the preceding terms.
 __device__ __forceinline__ float depth_from_ndc(float zn, float oz, float dz) {
     float tn = -(1.f + oz) / dz;
     float c = zn == 1.f ? 1e-3f : 0.f;
-    return (oz + tn * dz) / dz * (1.f / (1.f - zn + c) - 1.f) + tn;
+    float a = __fadd_rn(oz, __fmul_rn(tn, dz)) / dz;
+    float b = __fsub_rn(1.f / __fadd_rn(__fsub_rn(1.f, zn), c), 1.f);
+    return __fadd_rn(__fmul_rn(a, b), tn);
 }
 
 // Per-sample quantities of sample i.
@@ -291,6 +296,266 @@ __global__ void composite_bwd_kernel(srf_composite_args a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident variants for rays of at most 32 * R samples (R <= 8: every
+// NeRF configuration, 64 / 128 / 192 / 256 samples).  Lane j holds samples
+// j, j + 32, ..., j + 32 (R - 1) in registers: every global load of the ray is
+// issued before the first scan step (the per-round loads of the shared-memory
+// kernels wait for the previous round's scan), and the R rounds' scans only
+// chain through one carry.  Arithmetic, and the order of every product and sum,
+// are those of the shared-memory kernels, so the outputs are identical.
+// ---------------------------------------------------------------------------
+
+template <int R>
+__device__ __forceinline__ void scan_rounds(float (&T)[R], int lane) {
+    float carry = 1.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        float inc = T[k];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            float t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc *= t;
+        }
+        float exc = __shfl_up_sync(0xffffffffu, inc, 1);
+        if (lane == 0) exc = 1.f;
+        T[k] = carry * exc;
+        carry = carry * __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+template <int R>
+__global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_args a) {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (r >= a.n_rays) return;
+    RayCtx c = make_ctx(a, r);
+    const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;   // NULL: zero colours
+    float al[R], T[R], zz[R], c0[R], c1[R], c2[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = 32 * k + lane;
+        al[k] = 0.f;
+        T[k] = 1.f;
+        zz[k] = 0.f;
+        c0[k] = c1[k] = c2[k] = 0.f;
+        if (i < c.s) {
+            float delta, ex, alpha, p;
+            sample_terms(c, i, delta, ex, alpha, p);
+            al[k] = alpha;
+            T[k] = p;
+            zz[k] = c.z[i];
+            if (rgb) {
+                c0[k] = rgb[3 * i];
+                c1[k] = rgb[3 * i + 1];
+                c2[k] = rgb[3 * i + 2];
+            }
+        }
+    }
+    scan_rounds<R>(T, lane);
+    float cr = 0.f, cg = 0.f, cb = 0.f, acc = 0.f, wz = 0.f, wzn = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (32 * k + lane < c.s) {
+            float w = al[k] * T[k];
+            if (rgb) {
+                cr += w * c0[k];
+                cg += w * c1[k];
+                cb += w * c2[k];
+            }
+            acc += w;
+            if (c.ndc) {
+                wzn += w * zz[k];
+                wz += w * depth_from_ndc(zz[k], c.oz, c.dz);
+            } else {
+                wz += w * zz[k];
+            }
+        }
+    }
+    cr = warp_sum(cr); cg = warp_sum(cg); cb = warp_sum(cb);
+    acc = warp_sum(acc); wz = warp_sum(wz); wzn = warp_sum(wzn);
+    float depth = wz / (acc + kEps);
+    float depth_ndc = wzn / (acc + kEps);
+    float var = 0.f, var_ndc = 0.f;
+    int64_t ro = int64_t(r) * c.s;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = 32 * k + lane;
+        if (i < c.s) {
+            float w = al[k] * T[k];
+            float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
+            float d = zm - depth;
+            var += w * (d * d);
+            if (c.ndc) {
+                float dn = zz[k] - depth_ndc;
+                var_ndc += w * (dn * dn);
+            }
+            if (a.alpha) a.alpha[ro + i] = al[k];
+            if (a.visibility) a.visibility[ro + i] = T[k];
+            if (a.weights) a.weights[ro + i] = w;
+        }
+    }
+    var = warp_sum(var);
+    var_ndc = warp_sum(var_ndc);
+    if (lane == 0) {
+        if (white_for(a, r)) {
+            cr = cr + (1.f - acc);
+            cg = cg + (1.f - acc);
+            cb = cb + (1.f - acc);
+        }
+        if (a.rgb_map) {
+            a.rgb_map[3 * r] = cr;
+            a.rgb_map[3 * r + 1] = cg;
+            a.rgb_map[3 * r + 2] = cb;
+        }
+        if (a.acc) a.acc[r] = acc;
+        if (a.depth) a.depth[r] = depth;
+        if (a.depth_var) a.depth_var[r] = var;
+        if (c.ndc) {
+            if (a.depth_ndc) a.depth_ndc[r] = depth_ndc;
+            if (a.depth_var_ndc) a.depth_var_ndc[r] = var_ndc;
+        }
+    }
+}
+
+template <int R>
+__global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_args a) {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (r >= a.n_rays) return;
+    RayCtx c = make_ctx(a, r);
+    const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;
+    const int64_t ro = int64_t(r) * c.s;
+    // G holds dL/dw_i once formed; until then the colour dot product's partial terms
+    float al[R], T[R], ex_[R], dl[R], zz[R], G[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = 32 * k + lane;
+        al[k] = 0.f;
+        T[k] = 1.f;
+        ex_[k] = dl[k] = zz[k] = G[k] = 0.f;
+        if (i < c.s) {
+            float delta, ex, alpha, p;
+            sample_terms(c, i, delta, ex, alpha, p);
+            al[k] = alpha;
+            T[k] = p;
+            ex_[k] = ex;
+            dl[k] = delta;
+            zz[k] = c.z[i];
+            if (a.g_weights) G[k] = a.g_weights[ro + i];
+        }
+    }
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    if (a.g_rgb) {
+        g0 = a.g_rgb[3 * r];
+        g1 = a.g_rgb[3 * r + 1];
+        g2 = a.g_rgb[3 * r + 2];
+    }
+    float gacc = a.g_acc ? a.g_acc[r] : 0.f;
+    if (white_for(a, r)) gacc -= g0 + g1 + g2;
+    // colour terms of G (the loads stay off the scan's dependency chain)
+    float cdot[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = 32 * k + lane;
+        cdot[k] = (rgb && i < c.s) ? rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 : 0.f;
+    }
+    scan_rounds<R>(T, lane);
+    float acc = 0.f, wz = 0.f, wzn = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (32 * k + lane < c.s) {
+            float w = al[k] * T[k];
+            acc += w;
+            if (c.ndc) {
+                wzn += w * zz[k];
+                wz += w * depth_from_ndc(zz[k], c.oz, c.dz);
+            } else {
+                wz += w * zz[k];
+            }
+        }
+    }
+    acc = warp_sum(acc); wz = warp_sum(wz); wzn = warp_sum(wzn);
+    float inv = 1.f / (acc + kEps);
+    float depth = wz / (acc + kEps), depth_ndc = wzn / (acc + kEps);
+    float gd = a.g_depth ? a.g_depth[r] : 0.f;
+    float gv = a.g_depth_var ? a.g_depth_var[r] : 0.f;
+    float gdn = (c.ndc && a.g_depth_ndc) ? a.g_depth_ndc[r] : 0.f;
+    float gvn = (c.ndc && a.g_depth_var_ndc) ? a.g_depth_var_ndc[r] : 0.f;
+    float bsum = 0.f, bsum_n = 0.f;
+    if (gv != 0.f || gvn != 0.f) {
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if (32 * k + lane < c.s) {
+                float w = al[k] * T[k];
+                float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
+                bsum += w * (zm - depth);
+                if (c.ndc) bsum_n += w * (zz[k] - depth_ndc);
+            }
+        }
+        bsum = warp_sum(bsum);
+        bsum_n = warp_sum(bsum_n);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
+        float g = cdot[k] + gacc;
+        if (a.g_weights) g += G[k];
+        float d = zm - depth;
+        g += gd * d * inv + gv * (d * d - 2.f * bsum * d * inv);
+        if (c.ndc) {
+            float dn = zz[k] - depth_ndc;
+            g += gdn * dn * inv + gvn * (dn * dn - 2.f * bsum_n * dn * inv);
+        }
+        G[k] = g;
+    }
+    // reverse affine scan: R_i = G_{i+1} a_{i+1} + p_{i+1} R_{i+1}, R_{S-1} = 0
+    float carry = 0.f, next_ga = 0.f, next_p = 0.f;
+#pragma unroll
+    for (int k = R - 1; k >= 0; --k) {
+        const int i = 32 * k + lane;
+        if (32 * k >= c.s) continue;   // warp-uniform: rounds past the ray's end
+        bool in = i < c.s;
+        float Gi = in ? G[k] : 0.f, alpha = in ? al[k] : 0.f, Tk = in ? T[k] : 0.f;
+        float p = in ? 1.f - alpha + 1e-10f : 1.f;
+        float ga = Gi * alpha;
+        float ga_next = __shfl_down_sync(0xffffffffu, ga, 1);
+        float p_next = __shfl_down_sync(0xffffffffu, p, 1);
+        if (lane == 31) {
+            ga_next = next_ga;
+            p_next = next_p;
+        }
+        float A = in && i + 1 < c.s ? ga_next : 0.f;
+        float B = in && i + 1 < c.s ? p_next : 0.f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            float A2 = __shfl_down_sync(0xffffffffu, A, o);
+            float B2 = __shfl_down_sync(0xffffffffu, B, o);
+            if (lane + o < 32) {
+                A = A + B * A2;
+                B = B * B2;
+            }
+        }
+        float Rr = A + B * carry;
+        if (in) {
+            float dalpha = Tk * (Gi - Rr);
+            float dx = -dalpha * ex_[k];
+            dx = dx * c.ds;
+            a.d_sigma[ro + i] = -dx * dl[k];
+            if (a.d_rgb) {
+                float w = alpha * Tk;
+                float* dr = a.d_rgb + (ro + i) * 3;
+                dr[0] = w * g0;
+                dr[1] = w * g1;
+                dr[2] = w * g2;
+            }
+        }
+        carry = __shfl_sync(0xffffffffu, Rr, 0);
+        next_ga = __shfl_sync(0xffffffffu, ga, 0);
+        next_p = __shfl_sync(0xffffffffu, p, 0);
+    }
+}
+
 // out[r, c] = sum_s w[r, s] x[r, s, c] (one warp per ray); the adjoint gives
 // dw[r, s] = sum_c g[r, c] x[r, s, c] and dx[r, s, c] = w[r, s] g[r, c].
 __global__ void weighted_sum_kernel(const float* __restrict__ w, const float* __restrict__ x, int n, int s, int c,
@@ -349,6 +614,20 @@ int launch(K kernel, const srf_composite_args* a, void* stream) {
     return launch_status();
 }
 
+// Rounds of 32 samples of the register-resident kernels for rays of n samples
+// (rounded up to an even count, <= 8), or 0 for the shared-memory kernels.
+inline int reg_rounds(int n) {
+    int r = (n + 31) / 32;
+    r += r & 1;
+    return r <= 8 ? r : 0;
+}
+
+template <class K>
+int launch_reg(K kernel, const srf_composite_args* a, void* stream) {
+    kernel<<<grid_1d(a->n_rays, 8), 256, 0, as_stream(stream)>>>(*a);
+    return launch_status();
+}
+
 }  // namespace
 }  // namespace srf
 
@@ -357,13 +636,25 @@ using namespace srf;
 extern "C" int srf_composite_forward(const srf_composite_args* args, void* stream) {
     int st = check_args(args, false);
     if (st != SRF_OK || args->n_rays == 0) return st;
-    return launch(composite_fwd_kernel, args, stream);
+    switch (reg_rounds(args->n_samples)) {
+        case 2: return launch_reg(composite_fwd_reg_kernel<2>, args, stream);
+        case 4: return launch_reg(composite_fwd_reg_kernel<4>, args, stream);
+        case 6: return launch_reg(composite_fwd_reg_kernel<6>, args, stream);
+        case 8: return launch_reg(composite_fwd_reg_kernel<8>, args, stream);
+        default: return launch(composite_fwd_kernel, args, stream);
+    }
 }
 
 extern "C" int srf_composite_backward(const srf_composite_args* args, void* stream) {
     int st = check_args(args, true);
     if (st != SRF_OK || args->n_rays == 0) return st;
-    return launch(composite_bwd_kernel, args, stream);
+    switch (reg_rounds(args->n_samples)) {
+        case 2: return launch_reg(composite_bwd_reg_kernel<2>, args, stream);
+        case 4: return launch_reg(composite_bwd_reg_kernel<4>, args, stream);
+        case 6: return launch_reg(composite_bwd_reg_kernel<6>, args, stream);
+        case 8: return launch_reg(composite_bwd_reg_kernel<8>, args, stream);
+        default: return launch(composite_bwd_kernel, args, stream);
+    }
 }
 
 extern "C" int srf_weighted_sum(const float* weights, const float* values, int n_rays, int n_samples, int channels,

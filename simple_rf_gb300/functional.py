@@ -56,7 +56,8 @@ def sample_pdf(bins, weights, n_samples, u=None):
     if u is not None:
         _require(u, 'u', (n, n_samples))
     out = torch.empty(n, n_samples, device=bins.device)
-    call('srf_sample_pdf', _ptr(out), _ptr(bins), _ptr(weights), _ptr(u), n, nb, n_samples, _stream())
+    if n:
+        call('srf_sample_pdf', _ptr(out), _ptr(bins), _ptr(weights), _ptr(u), n, nb, n_samples, _stream())
     return out
 
 
@@ -69,7 +70,8 @@ def fine_z(z_coarse, weights_coarse, n_fine, u=None):
     if u is not None:
         _require(u, 'u', (n, n_fine))
     out = torch.empty(n, nc + n_fine, device=z_coarse.device)
-    call('srf_fine_z', _ptr(out), _ptr(z_coarse), _ptr(weights_coarse), _ptr(u), n, nc, n_fine, _stream())
+    if n:  # an empty batch has NULL data pointers: nothing to launch
+        call('srf_fine_z', _ptr(out), _ptr(z_coarse), _ptr(weights_coarse), _ptr(u), n, nc, n_fine, _stream())
     return out
 
 
@@ -269,6 +271,9 @@ class NerfMlpFunction(torch.autograd.Function):
         ctx.params = params
         ctx.rows = rows
         ctx.set_materialize_grads(True)
+        if m == 0:  # an empty batch has NULL data pointers: nothing to launch
+            ctx.ws = None
+            return sigma, rgb
         if rows:
             ws = torch.empty(max(spec.workspace_bytes(rows, precision, False), 1), dtype=torch.uint8,
                              device=pts.device)
@@ -288,6 +293,8 @@ class NerfMlpFunction(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, dsigma, drgb):
+        if ctx.m == 0:
+            return (None, None, None, None, None, None) + tuple(torch.zeros_like(p) for p in ctx.params)
         grads = [torch.empty_like(p) for p in ctx.params]
         dsigma = dsigma.contiguous()
         drgb = drgb.contiguous()
@@ -371,7 +378,8 @@ class CompositeFunction(torch.autograd.Function):
         for k in _COMPOSITE_OUT:
             if out[k] is not None:
                 setattr(a, 'rgb_map' if k == 'rgb' else k, out[k].data_ptr())
-        call('srf_composite_forward', ctypes.byref(a), _stream())
+        if n:
+            call('srf_composite_forward', ctypes.byref(a), _stream())
         ctx.save_for_backward(sigma, rgb, z, rays_d, rays_o, rays_d_ndc, white_per_ray)
         ctx.flags, ctx.ds = int(flags), float(distance_scale)
         ctx.set_materialize_grads(False)
@@ -401,7 +409,8 @@ class CompositeFunction(torch.autograd.Function):
         d_sigma = torch.empty_like(sigma)
         d_rgb = torch.empty_like(rgb) if rgb is not None and ctx.needs_input_grad[1] else None
         a.d_sigma, a.d_rgb = d_sigma.data_ptr(), _ptr(d_rgb)
-        call('srf_composite_backward', ctypes.byref(a), _stream())
+        if n:
+            call('srf_composite_backward', ctypes.byref(a), _stream())
         return d_sigma, d_rgb, None, None, None, None, None, None, None
 
 

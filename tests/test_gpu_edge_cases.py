@@ -1,0 +1,164 @@
+"""Edge cases of the hot path against the oracle: ray lengths on either side of
+every compositing kernel variant (1 ... 5000 samples: register-resident rounds
+up to 256 samples, shared-memory scans beyond), empty batches, all-zero coarse
+weights (the pdf floor and the denom < 1e-5 rule of SimpleNeRF17.py:400-413),
+and TensoRF rays that miss the bounding box (no valid samples).
+
+Tolerances as in tests/test_gpu_kernels.py: 1e-5 relative (absolute floor 1e-6
+of the value range) on compositing outputs, 1e-5 relative L2 on its adjoints
+(5e-5 for rays of more than 2048 samples, see below); fine samples 1e-5.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import nerf as on
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from simple_rf_gb300 import build as b
+    b.build()
+
+
+def t(x):
+    return torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(DEV)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize('s', [1, 2, 31, 33, 64, 100, 192, 255, 256, 257, 1039, 5000])
+@pytest.mark.parametrize('ndc', [False, True])
+def test_composite_every_ray_length(s, ndc):
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(s)
+    nr = 19
+    sigma = np.maximum(rng.standard_normal((nr, s)) * 3, 0).astype(np.float32)
+    sigma[0] = 0                      # a fully transparent ray
+    sigma[1, s // 2:] = 1e4           # an opaque wall half way
+    rgb = rng.random((nr, s, 3), dtype=np.float32)
+    kw = {}
+    if ndc:
+        o = np.zeros((nr, 3), np.float32)
+        o[:, :2] = rng.uniform(-1, 1, (nr, 2))
+        o[:, 2] = -1
+        d = np.stack([rng.uniform(-.2, .2, nr), rng.uniform(-.2, .2, nr), -rng.uniform(.8, 1.2, nr)],
+                     1).astype(np.float32)
+        f = np.full(nr, 400.0, np.float32)
+        _, dn = on.ndc_rays(o, d, 378, 504, f, f, 1.0)
+        z = np.sort(rng.random((nr, s), dtype=np.float32), 1)
+        z[2, -1] = 1.0                # the last NDC sample exactly at infinity
+        kw = dict(ndc=True, rays_o=o, rays_d_ndc=dn.astype(np.float32))
+    else:
+        d = rng.standard_normal((nr, 3)).astype(np.float32)
+        z = (2 + 4 * np.sort(rng.random((nr, s), dtype=np.float32), 1)).astype(np.float32)
+    ref, cache = on.composite_forward(sigma, rgb, z, d, white_bkgd=True, **kw)
+    sg, rg = t(sigma).requires_grad_(True), t(rgb).requires_grad_(True)
+    got = F.composite(sg, rg, t(z), t(d), white_bkgd=True, ndc=ndc,
+                      rays_o=t(kw['rays_o']) if ndc else None, rays_d_ndc=t(kw['rays_d_ndc']) if ndc else None)
+    # Rays longer than any configuration (5000 samples): the float32 running
+    # product of 5000 transmittance factors drifts up to ~3e-5 from the oracle's
+    # double-accumulated cumprod (torch's own CUDA cumprod accumulates in float
+    # too); every length up to 2048 holds 1e-5.
+    # NDC metric depth: the far samples (z_ndc -> 1, metric depth up to ~1e4)
+    # carry alphas 1 - exp(-x) with x ~ 1e-4, which float32 holds to ~5e-4
+    # relative, yet a weight of 1e-5 there is ~10% of a ray's depth: float32
+    # evaluations of the reference formula (numpy on two hosts, the GPU) spread
+    # by ~1.5e-5 around the float64 value (the depth_var terms are worse).
+    long_ray = s > 2048
+    for k, v in ref.items():
+        if k.startswith('depth_var'):
+            rtol = 2e-4
+        elif long_ray or (ndc and k == 'depth'):
+            rtol = 5e-5
+        else:
+            rtol = 1e-5
+        np.testing.assert_allclose(got[k].detach().cpu().numpy(), v, rtol=rtol,
+                                   atol=1e-6 * max(1.0, float(np.abs(v).max())), err_msg=f'{k} s={s}')
+    cot = {k: rng.standard_normal(ref[k].shape).astype(np.float32) for k in ref if k not in ('alpha', 'visibility')}
+    sum((got[k] * t(c)).sum() for k, c in cot.items()).backward()
+    ds, dr = on.composite_backward(cache, cot)
+    # float32 transmittance products over 1000+ samples drift ~2e-6 from the
+    # oracle's double-accumulated cumprod: 1e-5 holds for every length
+    bar = 5e-5 if long_ray else 1e-5
+    assert rel_l2(sg.grad.cpu().numpy(), ds) < bar, s
+    assert rel_l2(rg.grad.cpu().numpy(), dr) < bar, s
+
+
+def test_composite_without_colour_and_with_per_ray_background():
+    """rgb NULL (the TensoRF density pass) and a per-ray white-background coin."""
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(3)
+    nr, s = 40, 192
+    sigma = np.maximum(rng.standard_normal((nr, s)), 0).astype(np.float32)
+    d = rng.standard_normal((nr, 3)).astype(np.float32)
+    z = (2 + 4 * np.sort(rng.random((nr, s), dtype=np.float32), 1)).astype(np.float32)
+    coin = rng.random(nr) < 0.5
+    got = F.composite(t(sigma), None, t(z), t(d), distance_scale=25.0,
+                      white_per_ray=torch.from_numpy(coin).to(DEV))
+    ref, _ = on.composite_forward(sigma, np.zeros((nr, s, 3), np.float32), z, d, distance_scale=25.0)
+    exp_rgb = ref['rgb'] + np.where(coin[:, None], 1 - ref['acc'][:, None], 0)
+    np.testing.assert_allclose(got['rgb'].cpu().numpy(), exp_rgb, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(got['weights'].cpu().numpy(), ref['weights'], rtol=1e-5, atol=1e-6)
+
+
+def test_empty_batches():
+    """Zero rays / zero samples through compositing, sampling and the MLP."""
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300 import functional as F
+    e = torch.zeros(0, 64, device=DEV)
+    out = F.composite(e, torch.zeros(0, 64, 3, device=DEV), e, torch.zeros(0, 3, device=DEV), white_bkgd=True)
+    assert out['rgb'].shape == (0, 3) and out['weights'].shape == (0, 64)
+    z = F.fine_z(e, e, 128, torch.zeros(0, 128, device=DEV))
+    assert z.shape == (0, 192)
+    spec = F.MlpSpec()
+    params = [torch.zeros(int(nm), device=DEV).requires_grad_(True) for nm in spec.param_numel]
+    sigma, rgb = F.NerfMlpFunction.apply(spec, _lib.SRF_PRECISION_FP32, torch.zeros(0, 3, device=DEV),
+                                         torch.zeros(0, 3, device=DEV), 64, None, *params)
+    assert sigma.shape == (0,) and rgb.shape == (0, 3)
+    (sigma.sum() + rgb.sum()).backward()
+    assert all(p.grad is not None and torch.count_nonzero(p.grad) == 0 for p in params)
+
+
+def test_fine_sampling_with_all_zero_coarse_weights():
+    """Weights that are all zero leave only the 1e-5 pdf floor: the fine samples
+    follow the uniform inverse CDF of the bins, exactly as the oracle's."""
+    from simple_rf_gb300 import functional as F
+    rng = np.random.default_rng(11)
+    nr, sc, sf = 50, 64, 128
+    zc = on.stratified_z(2.0, 6.0, nr, sc, rng.random((nr, sc), dtype=np.float32))
+    w = np.zeros((nr, sc), np.float32)
+    w[::2, 5] = 1e-9                  # below the floor's scale on every other ray
+    u = rng.random((nr, sf), dtype=np.float32)
+    got = F.fine_z(t(zc), t(w), sf, t(u)).cpu().numpy()
+    ref = on.fine_z(zc, w, sf, u)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5)
+    assert np.all(np.diff(got, axis=1) >= 0)
+
+
+def test_tensorf_rays_that_miss_the_box():
+    """Every ray misses the bounding box: no valid samples, zero weights, white
+    background; the compaction sees an empty mask.  As in the reference (whose
+    sigma stays a zero tensor when no sample is valid, SimpleTensoRF09.py:1220),
+    no parameter reaches the outputs."""
+    from simple_rf_gb300.tensorf_model import GbVmTensor
+    from simple_rf_gb300.bench_tensorf import tensor_configs
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
+    bbox = [[-1.5] * 3, [1.5] * 3]
+    tm = GbVmTensor('coarse_model', configs, tensor_configs(32 ** 3), {'bounding_box': bbox}).to(DEV)
+    n, s = 64, 100
+    o = torch.zeros(n, 3, device=DEV)
+    o[:, 0] = 10.0
+    d = torch.zeros(n, 3, device=DEV)
+    d[:, 0] = 1.0                     # pointing away from the box
+    z = torch.linspace(2.0, 6.0, s, device=DEV).repeat(n, 1).contiguous()
+    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': d}, retraw=True)
+    assert tm.last_sample_counts['valid'] == 0 and tm.last_sample_counts['surface'] == 0
+    assert torch.count_nonzero(out['weights']) == 0
+    assert torch.equal(out['rgb'], torch.ones_like(out['rgb']))
+    assert not out['rgb'].requires_grad
