@@ -24,6 +24,7 @@ import torch
 
 from . import _lib
 from . import functional as F
+from .tensorf_model import forward_models
 
 BBOX = [[-1.5] * 3, [1.5] * 3]
 
@@ -83,13 +84,15 @@ class TensorfTrainStep:
         n = o.shape[0]
         vd = F.view_dirs(d)
         loss = 0.0
-        counts = []
+        calls = []
         for i, tm in enumerate(self.models):
             bbox, s, step = tm.host_geometry()
             z = F.aabb_z(o, d, s, bbox, 2.0, 6.0, step, u[:, i].contiguous())
-            out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=False)
+            calls.append((tm, {'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}))
+        # both models' phases side by side: two host reads of sample counts per step
+        for out in forward_models(calls, retraw=False):
             loss = loss + torch.mean(torch.mean((out['rgb'] - t_rgb) ** 2, -1))
-            counts.append(dict(tm.last_sample_counts))
+        counts = [dict(tm.last_sample_counts) for tm in self.models]
         for p, _ in self.params:
             p.grad = None
         loss.backward()

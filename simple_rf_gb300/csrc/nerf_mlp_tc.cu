@@ -1269,9 +1269,32 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
         }
         __syncthreads();
         if (c < C) {
-            for (int rr = 0; rr < nt; ++rr) {
+            // two rows per pass: their dB . Wb chains are independent (the dWb
+            // accumulators still take the rows in order)
+            int rr = 0;
+            for (; rr + 1 < nt; rr += 2) {
+                const float f0 = sF[rr * C + c], f1 = sF[(rr + 1) * C + c];
+                float de0 = 0.f, dd0 = 0.f, de1 = 0.f, dd1 = 0.f;   // even / odd basis columns of dB . Wb
+#pragma unroll
+                for (int o4 = 0; o4 < kMaxBasis; o4 += 4) {
+                    if (o4 >= F) break;
+                    const float4 d0 = *reinterpret_cast<const float4*>(sdB + rr * kMaxBasis + o4);
+                    const float4 d1 = *reinterpret_cast<const float4*>(sdB + (rr + 1) * kMaxBasis + o4);
+                    fma2v(de0, dd0, d0.x, d0.y, wcol[o4], wcol[o4 + 1]);
+                    fma2v(de1, dd1, d1.x, d1.y, wcol[o4], wcol[o4 + 1]);
+                    fma2v(de0, dd0, d0.z, d0.w, wcol[o4 + 2], wcol[o4 + 3]);
+                    fma2v(de1, dd1, d1.z, d1.w, wcol[o4 + 2], wcol[o4 + 3]);
+                    ffma2(acc[o4], acc[o4 + 1], f0, d0.x, d0.y);
+                    ffma2(acc[o4 + 2], acc[o4 + 3], f0, d0.z, d0.w);
+                    ffma2(acc[o4], acc[o4 + 1], f1, d1.x, d1.y);
+                    ffma2(acc[o4 + 2], acc[o4 + 3], f1, d1.z, d1.w);
+                }
+                d_feats[(t0 + rr) * C + c] = de0 + dd0;
+                d_feats[(t0 + rr + 1) * C + c] = de1 + dd1;
+            }
+            for (; rr < nt; ++rr) {
                 const float f = sF[rr * C + c];
-                float de = 0.f, dd = 0.f;   // even / odd basis columns of dB . Wb
+                float de = 0.f, dd = 0.f;
 #pragma unroll
                 for (int o4 = 0; o4 < kMaxBasis; o4 += 4) {
                     if (o4 >= F) break;

@@ -215,7 +215,19 @@ class GbVmTensor(torch.nn.Module):
 
     # ------------------------------------------------------------- forward --
     def forward(self, input_dict, retraw):
-        """LowRankTensor.forward (SimpleTensoRF09.py:701-761) on the CUDA path."""
+        """LowRankTensor.forward (SimpleTensoRF09.py:701-761) on the CUDA path.
+
+        Three phases separated by the two host reads of a sample count (valid
+        samples, then surface samples), which size the compacted launches;
+        :func:`forward_models` runs the phases of several models side by side so
+        that one host read serves them all."""
+        st = self.forward_begin(input_dict)
+        self.forward_density(st, int(st['cnt_v'].item()))
+        return self.forward_color(st, int(st['cnt_s'].item()), retraw)
+
+    def forward_begin(self, input_dict):
+        """Validity (bounding box and alpha mask, SimpleTensoRF09.py:705-710) and
+        the compaction of the valid samples; the count stays on the device."""
         z = input_dict['z_vals_ndc'] if self.ndc else input_dict['z_vals']
         o, d = (input_dict['rays_o_ndc'], input_dict['rays_d_ndc']) if self.ndc else \
             (input_dict['rays_o'], input_dict['rays_d'])
@@ -234,9 +246,18 @@ class GbVmTensor(torch.nn.Module):
             abox = _lib.host_floats(cached_host(self.alpha_mask, 'bbox', self.alpha_mask.bounding_box))
         _lib.call('srf_tensorf_sample_mask', F._ptr(o.contiguous()), F._ptr(d.contiguous()), F._ptr(z.contiguous()),
                   n, s, _lib.host_floats(bbox), F._ptr(vol), vd, vh, vw, abox, F._ptr(pn), F._ptr(mask), F._stream())
-        # density on the valid samples (uneven per ray): compact, gather, VM lookup
         idx_v, cnt_v = T.compact(mask)
-        nv = int(cnt_v.item())
+        return {'input': input_dict, 'z': z, 'n': n, 's': s, 'pn': pn, 'idx_v': idx_v, 'cnt_v': cnt_v}
+
+    def forward_density(self, st, nv):
+        """Density on the nv valid samples (uneven per ray: gather, VM lookup,
+        activation, SimpleTensoRF09.py:1214-1239), the volume-rendering weights
+        (:767-814) and the compaction of the surface samples (weights above the
+        threshold, :726); that count stays on the device."""
+        input_dict, z, n, s, pn = st['input'], st['z'], st['n'], st['s'], st['pn']
+        rows = n * s
+        dev = z.device
+        idx_v, cnt_v = st['idx_v'], st['cnt_v']
         pv = T.gather_rows(pn, idx_v, cnt_v, nv)
         feat = self.density_features(pv) if nv else torch.zeros(0, device=dev)
         sigma = T.density_activation(feat, idx_v, cnt_v, rows, self.density_mode, self.density_offset).view(n, s)
@@ -247,14 +268,23 @@ class GbVmTensor(torch.nn.Module):
         out = {k: vr[k] for k in ('acc', 'alpha', 'visibility', 'weights', 'depth', 'depth_var')}
         if self.ndc:
             out['depth_ndc'], out['depth_var_ndc'] = vr['depth_ndc'], vr['depth_var_ndc']
-        # colour on the surface samples (weights > threshold)
         w = vr['weights']
         smask = torch.empty(rows, dtype=torch.uint8, device=dev)
         _lib.call('srf_threshold_mask', F._ptr(w.detach().contiguous()), rows,
                   float(self.tensor_configs['ray_marching_weight_threshold']), F._ptr(smask), F._stream())
         idx_s, cnt_s = T.compact(smask)
-        ns = int(cnt_s.item())
-        self.last_sample_counts = {'marched': rows, 'valid': nv, 'surface': ns}
+        st.update({'nv': nv, 'sigma': sigma, 'out': out, 'idx_s': idx_s, 'cnt_s': cnt_s})
+
+    def forward_color(self, st, ns, retraw):
+        """Colour on the ns surface samples (SimpleTensoRF09.py:1241-1272 and the
+        renderer MLP), compositing of the colour and the white background
+        (:743-747)."""
+        input_dict, n, s, pn, out = st['input'], st['n'], st['s'], st['pn'], st['out']
+        rows = n * s
+        dev = pn.device
+        idx_s, cnt_s = st['idx_s'], st['cnt_s']
+        w = out['weights']
+        self.last_sample_counts = {'marched': rows, 'valid': st['nv'], 'surface': ns}
         if ns:
             ps = T.gather_rows(pn, idx_s, cnt_s, ns)
             feats = self.color_features(ps)
@@ -281,7 +311,7 @@ class GbVmTensor(torch.nn.Module):
             rgb_map = rgb_map + (1 - out['acc'][..., None])
         out['rgb'] = rgb_map
         if retraw:
-            out['raw_sigma'] = sigma[..., None]
+            out['raw_sigma'] = st['sigma'][..., None]
             out['raw_rgb'] = rgb
         return out
 
@@ -479,6 +509,24 @@ def make_tensor_model(name, configs, tensor_configs, model_configs):
     return kinds[kind](name, configs, tensor_configs, model_configs)
 
 
+def _host_counts(counts):
+    """Device sample counts -> host ints in one device-to-host read."""
+    return [int(v) for v in torch.cat([c.reshape(1) for c in counts]).cpu().tolist()]
+
+
+def forward_models(calls, retraw):
+    """``[model(input_dict, retraw) for model, input_dict in calls]`` with the
+    phases of every model enqueued before each host read of the sample counts:
+    two device-to-host reads for the whole list instead of two per model (the
+    GPU holds every model's pending work while the host waits).  Outputs are
+    those of calling the models one by one."""
+    states = [m.forward_begin(inp) for m, inp in calls]
+    for (m, _), st, nv in zip(calls, states, _host_counts([st['cnt_v'] for st in states])):
+        m.forward_density(st, nv)
+    return [m.forward_color(st, ns, retraw)
+            for (m, _), st, ns in zip(calls, states, _host_counts([st['cnt_s'] for st in states]))]
+
+
 class GbSimpleTensoRF(torch.nn.Module):
     """Drop-in for ``SimpleTensoRF`` (src/models/SimpleTensoRF09.py:16)."""
 
@@ -617,30 +665,31 @@ class GbSimpleTensoRF(torch.nn.Module):
         if self.coarse_model_needed:
             z_c = self.get_z_vals_coarse(input_dict, ret, self.coarse_model)
             mi = model_input(z_c)
-            outs = self.coarse_model(mi, retraw)
+            # the main and augmented models on the same samples (:244-296), their
+            # phases side by side (forward_models)
+            augs = [aug for aug in self.augmented_models if aug['coarse_model'] is not None] if train_augs else []
+            res = forward_models([(self.coarse_model, mi)] + [(aug['coarse_model'], mi) for aug in augs], retraw)
+            outs = res[0]
             weights_c = outs['weights']
             ret['z_vals_coarse'] = z_c
             for k, v in outs.items():
                 ret[f'{k}_coarse'] = v
-            if train_augs:
-                for aug in self.augmented_models:
-                    if aug['coarse_model'] is not None:
-                        for k, v in aug['coarse_model'](mi, retraw).items():
-                            ret[f"{aug['name']}_{k}_coarse"] = v
+            for aug, aug_out in zip(augs, res[1:]):
+                for k, v in aug_out.items():
+                    ret[f"{aug['name']}_{k}_coarse"] = v
         if self.fine_model_needed:
             nf = m['fine_model']['num_samples']
             u = torch.rand(z_c.shape[0], nf, device=z_c.device) if (m['perturb'] and self.training) else None
             z_f = F.fine_z(z_c.contiguous(), weights_c.detach(), nf, u)
             mi = model_input(z_f)
-            outs = self.fine_model(mi, retraw)
+            augs = [aug for aug in self.augmented_models if aug['fine_model'] is not None] if train_augs else []
+            res = forward_models([(self.fine_model, mi)] + [(aug['fine_model'], mi) for aug in augs], retraw)
             ret['z_vals_fine'] = z_f
-            for k, v in outs.items():
+            for k, v in res[0].items():
                 ret[f'{k}_fine'] = v
-            if train_augs:
-                for aug in self.augmented_models:
-                    if aug['fine_model'] is not None:
-                        for k, v in aug['fine_model'](mi, retraw).items():
-                            ret[f"{aug['name']}_{k}_fine"] = v
+            for aug, aug_out in zip(augs, res[1:]):
+                for k, v in aug_out.items():
+                    ret[f"{aug['name']}_{k}_fine"] = v
         if not retraw:
             for tag, needed in (('coarse', self.coarse_model_needed), ('fine', self.fine_model_needed)):
                 if needed:
