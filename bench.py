@@ -260,23 +260,30 @@ def time_variant(config, precision, steps, dev, stream):
     return out
 
 
-def time_tensorf(precision, steps, dev, stream):
+def time_tensorf(precision, steps, dev, stream, graph=True):
     """TensoRF VM training step (300^3 main + 75^3 augmented model, 8192 rays; see
-    simple_rf_gb300/bench_tensorf.py) through the drop-in modules."""
+    simple_rf_gb300/bench_tensorf.py) through the drop-in modules: captured as one
+    CUDA graph (capacity-sized compacted launches), or eager with graph=False."""
     import torch
-    from simple_rf_gb300.bench_tensorf import TensorfTrainStep, make_models, synthetic_rays
+    from simple_rf_gb300.bench_tensorf import TensorfGraphStep, TensorfTrainStep, make_models, synthetic_rays
     models = make_models(dev, precision=precision)
-    st = TensorfTrainStep(models)
+    st = TensorfGraphStep(models, 8192) if graph else TensorfTrainStep(models)
     batches = [synthetic_rays(8192, 10 + i, dev) for i in range(4)]
-    for i in range(2):
+    for i in range(3):
         st.step(*batches[i % 4])
     torch.cuda.synchronize(dev)
     t = time_steps(lambda i: st.step(*batches[i % 4]), steps, stream)
-    counts = {m.name: dict(c) for m, c in zip(models, st.last['samples'])}
+    samples = st.sample_counts() if graph else st.last['samples']
+    counts = {m.name: dict(c) for m, c in zip(models, samples)}
+    out = {'ms_per_step': round(1e3 * t / steps, 3), 'rays_per_s': round(8192 * steps / t, 1), 'steps': steps,
+           'samples_per_step': counts, 'cuda_graph': graph}
+    if graph:
+        out['capacities'] = st.caps
+        out['recaptures'] = st.recaptures
+        out['gpu_launches_per_step'] = st.launches_per_step
     del st, models, batches
     torch.cuda.empty_cache()
-    return {'ms_per_step': round(1e3 * t / steps, 3), 'rays_per_s': round(8192 * steps / t, 1), 'steps': steps,
-            'samples_per_step': counts}
+    return out
 
 
 def time_render(dev, stream):
@@ -446,8 +453,9 @@ def run_ours(args):
         for prec, k in (('bf16', args.steps), ('fp16', args.steps), ('fp32', k32)):
             variants[f'nerf_pair_{prec}'] = time_variant('nerf_pair', prec, k, dev, stream)
         # the same warm-up and timed steps for both (surface-sample counts drift as the grids train)
-        variants['tensorf_fp16'] = time_tensorf('fp16', 3, dev, stream)
-        variants['tensorf_fp32'] = time_tensorf('fp32', 3, dev, stream)
+        variants['tensorf_fp16'] = time_tensorf('fp16', args.steps, dev, stream, graph=False)
+        variants['tensorf_fp16_graph'] = time_tensorf('fp16', args.steps, dev, stream, graph=True)
+        variants['tensorf_fp32'] = time_tensorf('fp32', 5, dev, stream, graph=False)
         from simple_rf_gb300.bench_tensorf import ray_batch_sweep
         variants['tensorf_sweep'] = ray_batch_sweep(dev)
         variants['render'] = time_render(dev, stream)
@@ -491,9 +499,12 @@ def run_ours(args):
                                                           variants['nerf_pair_fp32']['rays_per_s'], 2)},
         'tensorf': {'workload': 'TensoRF VM fwd+bwd+Adam, 300^3 (R 16/48) + 75^3 augmented model, 8192 rays, '
                                 'alpha mask 128^3 at 15%, renderer PE L=2 -> 128 -> 128 -> 3',
-                    'fp16': variants['tensorf_fp16'], 'fp32_plain': variants['tensorf_fp32'],
+                    'fp16': variants['tensorf_fp16'], 'fp16_graph': variants['tensorf_fp16_graph'],
+                    'fp32_plain': variants['tensorf_fp32'],
                     'speedup_fp16_vs_fp32_plain': round(variants['tensorf_fp16']['rays_per_s'] /
                                                         variants['tensorf_fp32']['rays_per_s'], 2),
+                    'speedup_fp16_graph_vs_fp32_plain': round(variants['tensorf_fp16_graph']['rays_per_s'] /
+                                                              variants['tensorf_fp32']['rays_per_s'], 2),
                     'ray_batch_sweep': variants['tensorf_sweep']},
         'render': dict(variants['render'], workload='8 views x 504x378 NDC rays, NeRF pair (main coarse+fine + '
                                                     'augmented coarse), 64+128 samples, chunks of 65536'),

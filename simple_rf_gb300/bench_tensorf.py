@@ -14,10 +14,11 @@ radius 4 about the box centre, directions towards the centre perturbed by
 N(0, 0.3^2) per axis, near 2, far 6.  Loss: MSE of each model's rgb against
 targets ~ U[0,1]^3.
 
-    python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3 [--precision fp16]
+    python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3 [--precision fp16] [--eager]
     python -m simple_rf_gb300.bench_tensorf --sweep        # ray batches 1024 ... 65536
 """
 import argparse
+import ctypes
 import json
 
 import torch
@@ -104,6 +105,154 @@ class TensorfTrainStep:
         return loss
 
 
+class TensorfGraphStep:
+    """The TensorfTrainStep step (both models' forward, rgb MSE, backward, one
+    multi-tensor Adam launch) captured as one CUDA graph for a fixed ray count.
+
+    A replay cannot read the compacted sample counts on the host, so the
+    captured step sizes the valid- and surface-sample launches by capacities:
+    15% above the counts of an uncaptured counting pass, rounded up to 1024
+    rows.  Rows past a device count are zero points whose outputs nothing reads
+    and whose gradients are zero, so a replay computes what TensorfTrainStep
+    computes (up to the grouping of the sums over samples).  A count above its
+    capacity raises a device flag that skips the Adam update and the step
+    counter; the call reads the flag once its replay has ended and, when it is
+    set, re-captures with capacities 25% above the counts and redoes the batch.
+    Padding rows still cost the renderer MLP and basis passes their full work,
+    so the uncaptured step stays faster once per-step host work is hidden
+    behind the GPU (8192 rays and up); the captured step wins on small batches.
+    """
+
+    MARGIN = 1.15
+    REGROW = 1.25
+    ROUND = 1024
+
+    def __init__(self, models, n_rays, lr_tensor=0.02, lr_network=1e-3, state=None, step_dev=None):
+        self.models = models
+        self.n = int(n_rays)
+        dev = models[0].matrices_density[0].device
+        self.dev = dev
+        self.params = []
+        for tm in models:
+            tensor_ps = list(tm.matrices_density) + list(tm.vectors_density) + list(tm.matrices_color) + \
+                list(tm.vectors_color)
+            net_ps = [tm.basis_matrix_color.weight] + list(tm.color_predictor.parameters())
+            self.params += [(p, lr_tensor) for p in tensor_ps] + [(p, lr_network) for p in net_ps]
+        self.state = state if state is not None else [(torch.zeros_like(p), torch.zeros_like(p))
+                                                      for p, _ in self.params]
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.step_dev = step_dev if step_dev is not None else torch.zeros(1, **i32)
+        self.ovf = torch.zeros(1, **i32)
+        k = len(models)
+        self.caps_dev = torch.zeros(2 * k, **i32)
+        self.flags_dev = torch.zeros(1 + 2 * k, **i32)
+        self.flags_host = torch.zeros(1 + 2 * k, dtype=torch.int32, pin_memory=True)
+        self.loss = torch.zeros(1, device=dev)
+        f32 = dict(device=dev, dtype=torch.float32)
+        self.o, self.d = torch.zeros(self.n, 3, **f32), torch.zeros(self.n, 3, **f32)
+        self.t_rgb, self.u = torch.zeros(self.n, 3, **f32), torch.zeros(self.n, k, **f32)
+        self.caps = None
+        self.graph = None
+        self.done = torch.cuda.Event()
+        self.launches_per_step = None
+        self.recaptures = 0
+
+    def _calls(self):
+        vd = F.view_dirs(self.d)
+        calls = []
+        for i, tm in enumerate(self.models):
+            bbox, s, step = tm.host_geometry()
+            z = F.aabb_z(self.o, self.d, s, bbox, 2.0, 6.0, step, self.u[:, i].contiguous())
+            calls.append((tm, {'z_vals': z, 'rays_o': self.o, 'rays_d': self.d, 'view_dirs': vd}))
+        return calls
+
+    def _body(self, dry):
+        self.ovf.zero_()
+        calls = self._calls()
+        states = [tm.forward_begin(inp) for tm, inp in calls]
+        for (tm, _), st, (cv, _) in zip(calls, states, self.caps):
+            tm.forward_density(st, cv, capacity=True)
+        loss = 0.0
+        for (tm, _), st, (_, cs) in zip(calls, states, self.caps):
+            out = tm.forward_color(st, cs, retraw=False, capacity=True)
+            loss = loss + torch.mean(torch.mean((out['rgb'] - self.t_rgb) ** 2, -1))
+        counts = torch.cat([torch.cat([st['cnt_v'].reshape(1), st['cnt_s'].reshape(1)]) for st in states])
+        self.ovf.copy_((counts > self.caps_dev).any().to(torch.int32).reshape(1))
+        if dry:
+            self.ovf.fill_(1)   # the dry run before a capture leaves parameters and step count alone
+        for p, _ in self.params:
+            p.grad = None
+        loss.backward()
+        st = ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+        _lib.call('srf_counter_add', F._ptr(self.step_dev), 1, F._ptr(self.ovf), st)
+        F.adam_multi_step([(p.data, p.grad.contiguous(memory_format=_fmt(p)), m, v, lr)
+                           for (p, lr), (m, v) in zip(self.params, self.state) if p.grad is not None],
+                          step=1, beta1=0.9, beta2=0.99, eps=1e-8, step_dev=self.step_dev, skip_dev=self.ovf)
+        self.loss.copy_(loss.detach().reshape(1))
+        self.flags_dev[:1].copy_(self.ovf)
+        self.flags_dev[1:].copy_(counts)
+        self.flags_host.copy_(self.flags_dev, non_blocking=True)
+
+    def _counts(self):
+        with torch.no_grad():
+            forward_models(self._calls(), retraw=False)
+        return [(tm.last_sample_counts['valid'], tm.last_sample_counts['surface']) for tm in self.models]
+
+    def _capture(self, counts, margin):
+        def cap(x):
+            return (int(x * margin) // self.ROUND + 1) * self.ROUND
+        self.caps = [(cap(v), cap(s)) for v, s in counts]
+        self.caps_dev.copy_(torch.tensor([c for pair in self.caps for c in pair], dtype=torch.int32))
+        self.graph = None
+        torch.cuda.synchronize(self.dev)
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            self._body(dry=True)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        torch.cuda.synchronize(self.dev)
+        lib = _lib.load()
+        l0 = lib.srf_launch_count()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._body(dry=False)
+        self.launches_per_step = int(lib.srf_launch_count() - l0)
+        self.graph = g
+
+    def _replay(self, batch):
+        for dst, src in zip((self.o, self.d, self.t_rgb, self.u), batch):
+            dst.copy_(src)
+        self.graph.replay()
+        self.done.record()
+
+    def step(self, o, d, t_rgb, u):
+        """One training step on this batch (device tensors); returns the loss
+        buffer.  The host waits for the replay to read its overflow flag: a replay
+        that overflowed a capacity (its update skipped) is re-captured with
+        larger capacities and redone before the call returns."""
+        batch = (o, d, t_rgb, u)
+        if self.graph is None:
+            for dst, src in zip((self.o, self.d, self.t_rgb, self.u), batch):
+                dst.copy_(src)
+            self._capture(self._counts(), self.MARGIN)
+        self._replay(batch)
+        self.done.synchronize()
+        while int(self.flags_host[0]):
+            c = self.flags_host[1:].tolist()
+            self.recaptures += 1
+            self._capture([(max(c[2 * i], cv), max(c[2 * i + 1], cs)) for i, (cv, cs) in enumerate(self.caps)],
+                          max(self.MARGIN, self.REGROW))
+            self._replay(batch)
+            self.done.synchronize()
+        return self.loss
+
+    def sample_counts(self):
+        """Valid and surface sample counts of the last finished replay, per model."""
+        self.done.synchronize()
+        c = self.flags_host[1:].tolist()
+        return [{'marched': None, 'valid': c[2 * i], 'surface': c[2 * i + 1]} for i in range(len(self.models))]
+
+
 def _fmt(p):
     return torch.channels_last if p.dim() == 4 and p.is_contiguous(memory_format=torch.channels_last) else \
         torch.contiguous_format
@@ -112,16 +261,26 @@ def _fmt(p):
 SWEEP_RAYS = (1024, 2048, 4096, 8192, 16384, 32768, 65536)
 
 
-def ray_batch_sweep(device, precisions=('fp16', 'fp32'), sizes=SWEEP_RAYS, warmup=2, steps=3, seed=0):
+def ray_batch_sweep(device, modes=(('fp16', False), ('fp16', True), ('fp32', False)), sizes=SWEEP_RAYS, warmup=2,
+                    steps=3, seed=0):
     """Train rays/s of the same step over ray batches of 1024 ... 65536 rays: one model
-    pair per precision, trained on from size to size (each size gets its own warm-up),
-    rays drawn afresh per size."""
+    pair per (precision, captured-or-not) mode, trained on from size to size (each size
+    gets its own warm-up, and its own CUDA graph when captured), rays drawn afresh per
+    size.  Keys: 'fp16' / 'fp32' (uncaptured, one host read of the sample counts per
+    phase), 'fp16_graph' (TensorfGraphStep)."""
     out = {}
-    for prec in precisions:
+    for prec, graph in modes:
         models = make_models(device, seed=seed, precision=prec)
-        st = TensorfTrainStep(models)
+        eager = None if graph else TensorfTrainStep(models)
+        state = step_dev = None
         res = {}
         for n in sizes:
+            if graph:
+                # Adam state and step count carry over from size to size
+                st = TensorfGraphStep(models, n, state=state, step_dev=step_dev)
+                state, step_dev = st.state, st.step_dev
+            else:
+                st = eager
             batches = [synthetic_rays(n, 100 + i, device) for i in range(2)]
             for i in range(warmup):
                 st.step(*batches[i % 2])
@@ -133,15 +292,21 @@ def ray_batch_sweep(device, precisions=('fp16', 'fp32'), sizes=SWEEP_RAYS, warmu
             e1.record()
             e1.synchronize()
             ms = e0.elapsed_time(e1) / steps
+            surf = st.sample_counts()[0]['surface'] if graph else st.last['samples'][0]['surface']
             res[str(n)] = {'ms_per_step': round(ms, 3), 'rays_per_s': round(n / ms * 1e3, 1),
-                           'surface_samples': int(st.last['samples'][0]['surface'])}
+                           'surface_samples': int(surf)}
+            if graph:
+                res[str(n)]['recaptures'] = st.recaptures
+                del st
             del batches
-        out[prec] = res
-        del st, models
+            torch.cuda.empty_cache()
+        out[prec + ('_graph' if graph else '')] = res
+        del models, eager, state, step_dev
         torch.cuda.empty_cache()
-    if 'fp16' in out and 'fp32' in out:
-        out['speedup_fp16_vs_fp32_plain'] = {n: round(out['fp16'][n]['rays_per_s'] / out['fp32'][n]['rays_per_s'], 2)
-                                             for n in out['fp16']}
+    for key in ('fp16', 'fp16_graph'):
+        if key in out and 'fp32' in out:
+            out[f'speedup_{key}_vs_fp32_plain'] = {n: round(out[key][n]['rays_per_s'] / out['fp32'][n]['rays_per_s'], 2)
+                                                   for n in out[key]}
     return out
 
 
@@ -153,6 +318,7 @@ def main(argv=None):
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'bf16', 'fp16'],
                     help='renderer MLP: FP32 SIMT or 16-bit tensor cores')
     ap.add_argument('--sweep', action='store_true', help='ray-batch sweep 1024 ... 65536, FP16 and FP32 plain')
+    ap.add_argument('--eager', action='store_true', help='the uncaptured step (host reads of the sample counts)')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
@@ -162,7 +328,7 @@ def main(argv=None):
                           'sweep': ray_batch_sweep(dev)}))
         return
     models = make_models(dev, precision=args.precision)
-    step = TensorfTrainStep(models)
+    step = TensorfTrainStep(models) if args.eager else TensorfGraphStep(models, args.rays)
     batches = [synthetic_rays(args.rays, 10 + i, dev) for i in range(4)]
     for i in range(args.warmup):
         step.step(*batches[i % 4])
@@ -176,12 +342,16 @@ def main(argv=None):
     e1.record()
     e1.synchronize()
     ms = e0.elapsed_time(e1) / max(args.steps, 1)
-    launches = (lib.srf_launch_count() - l0) / max(args.steps, 1)
+    if args.eager:
+        launches = (lib.srf_launch_count() - l0) / max(args.steps, 1)
+        samples, loss = step.last['samples'], step.last['loss']
+    else:
+        launches, samples, loss = step.launches_per_step, step.sample_counts(), step.loss
     print(json.dumps({'workload': f'tensorf_vm_train_step_{args.rays}rays_300^3+75^3', 'rays': args.rays,
-                      'precision': args.precision,
+                      'precision': args.precision, 'cuda_graph': not args.eager,
                       'ms_per_step': round(ms, 4), 'rays_per_s': round(args.rays / ms * 1e3, 1),
-                      'samples_per_step': {m.name: c for m, c in zip(models, step.last['samples'])},
-                      'gpu_launches_per_step': launches, 'loss': float(step.last['loss'].item())}))
+                      'samples_per_step': {m.name: c for m, c in zip(models, samples)},
+                      'gpu_launches_per_step': launches, 'loss': float(loss.item())}))
 
 
 if __name__ == '__main__':

@@ -426,9 +426,13 @@ def _dense(t):
     return t.is_contiguous() or (t.dim() == 4 and t.is_contiguous(memory_format=torch.channels_last))
 
 
-def adam_multi_step(tensors, *, step, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
+def adam_multi_step(tensors, *, step, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0, step_dev=None,
+                    skip_dev=None):
     """In-place Adam over ``tensors`` = [(param, grad, exp_avg, exp_avg_sq, lr), ...]
-    with one launch per 64 tensors (each tensor's four buffers share one dense layout)."""
+    with one launch per 64 tensors (each tensor's four buffers share one dense layout).
+    ``step_dev`` (device int32, read instead of ``step``) and ``skip_dev`` (device
+    int32: nonzero skips the update) keep the step free of host values, for
+    graph capture."""
     arr = (_lib.AdamTensor * len(tensors))()
     for i, (p, g, m, v, lr) in enumerate(tensors):
         for name, x in (('param', p), ('grad', g), ('exp_avg', m), ('exp_avg_sq', v)):
@@ -439,7 +443,7 @@ def adam_multi_step(tensors, *, step, beta1=0.9, beta2=0.999, eps=1e-8, weight_d
                                    f'dense param {tuple(p.shape)} {p.stride()}')
         arr[i] = _lib.AdamTensor(p.data_ptr(), g.data_ptr(), m.data_ptr(), v.data_ptr(), p.numel(), float(lr))
     call('srf_adam_multi_step', arr, len(tensors), float(beta1), float(beta2), float(eps), float(weight_decay),
-         int(step), None, None, _stream())
+         int(step), _ptr(step_dev), _ptr(skip_dev), _stream())
 
 
 def rgb_depth_loss(rgb, target_rgb, depth, target_depth, depth_mask, n_depth_rays, depth_weight, loss=None):

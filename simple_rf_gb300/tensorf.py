@@ -242,10 +242,12 @@ def weighted_sum(w, x):
     return _WeightedSum.apply(w.contiguous(), x.contiguous())
 
 
-def gather_rows(src, idx, count, n, row_div=1):
-    """dst[i] = src[idx[i] // row_div] for i < count (no gradient)."""
+def gather_rows(src, idx, count, n, row_div=1, zero_tail=False):
+    """dst[i] = src[idx[i] // row_div] for i < count (no gradient).  Rows from
+    count to n are left unwritten, or zero with ``zero_tail`` (n is then a
+    capacity that may exceed the device count)."""
     cols = src.shape[-1]
-    dst = torch.empty(n, cols, device=src.device)
+    dst = (torch.zeros if zero_tail else torch.empty)(n, cols, device=src.device)
     if n:
         call('srf_gather_rows', _ptr(dst), _ptr(src.contiguous()), _ptr(idx), _ptr(count), n, cols, int(row_div),
              _stream())
@@ -269,7 +271,8 @@ class _ScatterRows(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         idx, count = ctx.saved_tensors
-        return gather_rows(g.contiguous(), idx, count, ctx.n), None, None, None
+        # rows past the device count (a capacity-sized source) get zero gradient
+        return gather_rows(g.contiguous(), idx, count, ctx.n, zero_tail=True), None, None, None
 
 
 def scatter_rows(src, idx, count, rows):

@@ -249,16 +249,20 @@ class GbVmTensor(torch.nn.Module):
         idx_v, cnt_v = T.compact(mask)
         return {'input': input_dict, 'z': z, 'n': n, 's': s, 'pn': pn, 'idx_v': idx_v, 'cnt_v': cnt_v}
 
-    def forward_density(self, st, nv):
+    def forward_density(self, st, nv, capacity=False):
         """Density on the nv valid samples (uneven per ray: gather, VM lookup,
         activation, SimpleTensoRF09.py:1214-1239), the volume-rendering weights
         (:767-814) and the compaction of the surface samples (weights above the
-        threshold, :726); that count stays on the device."""
+        threshold, :726); that count stays on the device.
+
+        With ``capacity`` nv is an upper bound chosen without reading the device
+        count (graph capture): rows past the count are zero points whose features
+        nothing reads, and a count above nv is the caller's to detect."""
         input_dict, z, n, s, pn = st['input'], st['z'], st['n'], st['s'], st['pn']
         rows = n * s
         dev = z.device
         idx_v, cnt_v = st['idx_v'], st['cnt_v']
-        pv = T.gather_rows(pn, idx_v, cnt_v, nv)
+        pv = T.gather_rows(pn, idx_v, cnt_v, nv, zero_tail=capacity)
         feat = self.density_features(pv) if nv else torch.zeros(0, device=dev)
         sigma = T.density_activation(feat, idx_v, cnt_v, rows, self.density_mode, self.density_offset).view(n, s)
         # the density pass composites no colour (rgb None reads as zeros)
@@ -275,22 +279,25 @@ class GbVmTensor(torch.nn.Module):
         idx_s, cnt_s = T.compact(smask)
         st.update({'nv': nv, 'sigma': sigma, 'out': out, 'idx_s': idx_s, 'cnt_s': cnt_s})
 
-    def forward_color(self, st, ns, retraw):
+    def forward_color(self, st, ns, retraw, capacity=False):
         """Colour on the ns surface samples (SimpleTensoRF09.py:1241-1272 and the
         renderer MLP), compositing of the colour and the white background
-        (:743-747)."""
+        (:743-747).  ``capacity``: ns is an upper bound, as in forward_density
+        (rows past the count render zero points whose colours nothing reads
+        and whose gradients are zero)."""
         input_dict, n, s, pn, out = st['input'], st['n'], st['s'], st['pn'], st['out']
         rows = n * s
         dev = pn.device
         idx_s, cnt_s = st['idx_s'], st['cnt_s']
         w = out['weights']
-        self.last_sample_counts = {'marched': rows, 'valid': st['nv'], 'surface': ns}
+        self.last_sample_counts = None if capacity else {'marched': rows, 'valid': st['nv'], 'surface': ns}
         if ns:
-            ps = T.gather_rows(pn, idx_s, cnt_s, ns)
+            ps = T.gather_rows(pn, idx_s, cnt_s, ns, zero_tail=capacity)
             feats = self.color_features(ps)
             view_s = None
             if self.tensor_configs['view_dependent_color']:
-                view_s = T.gather_rows(input_dict['view_dirs'].contiguous().float(), idx_s, cnt_s, ns, s)
+                view_s = T.gather_rows(input_dict['view_dirs'].contiguous().float(), idx_s, cnt_s, ns, s,
+                                       zero_tail=capacity)
             if self.precision == _lib.SRF_PRECISION_FP32:
                 cin = {'features': T.linear(feats, self.basis_matrix_color.weight)}
                 if view_s is not None:

@@ -178,3 +178,59 @@ def test_tensorf_cp_matches_reference_golden(golden):
         ref = g['grad_' + name]
         rel = np.linalg.norm(grad.detach().cpu().numpy() - ref) / max(np.linalg.norm(ref), 1e-30)
         assert rel < 1e-3, (name, rel)
+
+
+def _grads(step):
+    return [p.grad.detach().double().clone() for p, _ in step.params]
+
+
+def _rel(a, b):
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b).clamp_min(1e-30))
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'fp16'])
+def test_graph_step_matches_eager_step(precision):
+    """The TensoRF training step captured as a CUDA graph (capacity-sized
+    compacted launches) against the uncaptured step, from the same models on the
+    same batches: losses within 1e-5 relative, parameter gradients within 1e-4
+    relative L2 per tensor (only the grouping of sums over samples differs).  With
+    the 16-bit renderer the bar after the first update is 1e-2: parameters that
+    differ at float32 rounding level flip 16-bit roundings of the renderer's
+    operands (relative resolution 1e-3)."""
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300.bench_tensorf import TensorfGraphStep, TensorfTrainStep, make_models, synthetic_rays
+    ea = TensorfTrainStep(make_models(DEV, seed=3, precision=precision, grids=(64, 32)))
+    gb = TensorfGraphStep(make_models(DEV, seed=3, precision=precision, grids=(64, 32)), 2048)
+    for i in range(3):
+        batch = synthetic_rays(2048, 40 + i, DEV)
+        la = float(ea.step(*batch).item())
+        lb = float(gb.step(*batch).item())
+        assert abs(la - lb) <= 1e-5 * abs(la), (i, la, lb)
+        ga, gg = _grads(ea), _grads(gb)
+        bar = 1e-4 if (precision == 'fp32' or i == 0) else 1e-2
+        for (p, _), x, y in zip(ea.params, ga, gg):
+            assert _rel(y, x) < bar, (i, tuple(p.shape), _rel(y, x))
+    counts = gb.sample_counts()
+    assert [c['surface'] for c in counts] == [c['surface'] for c in ea.last['samples']]
+    assert int(gb.step_dev.item()) == 3
+
+
+def test_graph_step_redoes_a_step_that_overflowed():
+    """Capacities below the sample counts: the replay raises the overflow flag
+    and skips its update; the call re-captures with larger capacities and redoes
+    the batch, so it returns what the uncaptured step computes."""
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300.bench_tensorf import TensorfGraphStep, TensorfTrainStep, make_models, synthetic_rays
+    ea = TensorfTrainStep(make_models(DEV, seed=4, precision='fp32', grids=(64, 32)))
+    gb = TensorfGraphStep(make_models(DEV, seed=4, precision='fp32', grids=(64, 32)), 2048)
+    gb.MARGIN = 0.5   # the first capture is sized at half the counts
+    for i in range(2):
+        batch = synthetic_rays(2048, 50 + i, DEV)
+        la = float(ea.step(*batch).item())
+        lb = float(gb.step(*batch).item())
+        assert abs(la - lb) <= 1e-5 * abs(la), (i, la, lb)
+        for (p, _), x, y in zip(ea.params, _grads(ea), _grads(gb)):
+            assert _rel(y, x) < 1e-4, (i, tuple(p.shape), _rel(y, x))
+    assert gb.recaptures >= 1 and int(gb.flags_host[0]) == 0 and int(gb.step_dev.item()) == 2
