@@ -201,11 +201,15 @@ def renderer_backward(p, spec, c, drgb):
 
 
 def tensorf_forward(tp, spec, rays_o, rays_d, z, *, alpha_vol=None, alpha_bbox=None, distance_scale=25.0,
-                    weight_threshold=1e-4, white=False, density='relu', density_offset=-10.0):
-    """LowRankTensor.forward (SimpleTensoRF09.py:701-761), non-NDC, VM decomposition.
+                    weight_threshold=1e-4, white=False, density='relu', density_offset=-10.0, world_rays=None):
+    """LowRankTensor.forward (SimpleTensoRF09.py:701-761), VM (or CP) decomposition.
 
     tp: dict with 'bbox' (2,3), 'planes_density'/'lines_density'/'planes_color'/'lines_color'
     (lists of (R,H,W) / (R,L,1)), and renderer params.  z (N,S).
+    ``world_rays`` = (rays_o, rays_d) in world space switches to NDC mode: rays_o,
+    rays_d and z are then the NDC rays and depths that the samples march along
+    (SimpleTensoRF09.py:263-277), and compositing takes its deltas from the NDC
+    rays and converts depths with the world rays (:779-797).
     Returns the output dict plus a cache for :func:`tensorf_backward`.
     """
     n, s = z.shape
@@ -236,7 +240,11 @@ def tensorf_forward(tp, spec, rays_o, rays_d, z, *, alpha_vol=None, alpha_bbox=N
     sigma[vflat] = sig_v
     sigma = sigma.reshape(n, s)
     rgb0 = np.zeros((n, s, 3), dtype=rays_o.dtype)
-    out, cc = composite_forward(sigma, rgb0, z, rays_d, distance_scale=distance_scale)
+    if world_rays is None:
+        out, cc = composite_forward(sigma, rgb0, z, rays_d, distance_scale=distance_scale)
+    else:
+        out, cc = composite_forward(sigma, rgb0, z, world_rays[1], ndc=True, rays_o=world_rays[0],
+                                    rays_d_ndc=rays_d, distance_scale=distance_scale)
     surf = out['weights'] > dt(weight_threshold)
     sflat = np.nonzero(surf.reshape(-1))[0]
     if cp:

@@ -381,6 +381,86 @@ def tensorf_case():
     return out
 
 
+def tensorf_ndc_case():
+    """LowRankTensor.forward in NDC mode (the reference's forward-facing TensoRF
+    configuration, NerfLlffTrainerTester10.py:894-1087: NDC bounding box, stratified
+    NDC depths from get_z_vals_coarse :364-381, NDC marching points, metric depth via
+    CommonUtils04.convert_depth_from_ndc) on a small grid, with autograd gradients."""
+    g = torch.Generator().manual_seed(41)
+    res = torch.tensor([20, 22, 24])
+    bbox = [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]]
+    tcfg = {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [4, 3, 2],
+            'num_components_color': [6, 5, 4], 'bounding_box': bbox, 'num_voxels_initial': int(res.prod()),
+            'num_voxels_final': int(res.prod()), 'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5,
+            'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4,
+            'use_view_dirs': True, 'view_dependent_color': True, 'views_positional_encoding_degree': 2,
+            'features_positional_encoding_degree': 2, 'features_dimension_color': 7, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 16, 'predict_visibility': False}
+    configs = {'data_loader': {'ndc': True}, 'model': {'white_bkgd': False}, 'database': 'synthetic'}
+    tm = RT.VmDecomposedTensor('coarse_model', configs, tcfg, {'bounding_box': bbox})
+    tm.update_tensor_params(res, torch.tensor(bbox))
+    tm.matrices_density, tm.vectors_density = tm.create_decomposed_tensor([4, 3, 2], res, 0.1)
+    tm.matrices_color, tm.vectors_color = tm.create_decomposed_tensor([6, 5, 4], res, 0.1)
+    with torch.no_grad():
+        for plist in (tm.matrices_density, tm.vectors_density):
+            for prm in plist:
+                prm.copy_(torch.randn(prm.shape, generator=g) * 0.3 + 0.15)
+        for plist in (tm.matrices_color, tm.vectors_color):
+            for prm in plist:
+                prm.copy_(torch.randn(prm.shape, generator=g) * 0.3)
+        for prm in list(tm.basis_matrix_color.parameters()) + list(tm.color_predictor.parameters()):
+            prm.copy_(torch.randn(prm.shape, generator=g) * 0.3)
+    vol = (torch.rand(12, 10, 8, generator=g) < 0.3).float()
+    tm.alpha_mask = RT.AlphaGridMask(vol, torch.tensor(bbox))
+    tm.train()
+    n = 12
+    o, d = ndc_world_rays(n, 43)
+    intr = torch.tensor([[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]])[None].repeat(n, 1, 1)
+    o_ndc, d_ndc = CU.get_ndc_rays_tr(o, d, (378, 504), intr, near=1.0)
+    s = int(tm.num_samples.item())
+    u = torch.rand(n, s, generator=g)
+    fake = types.SimpleNamespace(ndc=True, training=True,
+                                 configs={'model': {'perturb': True, 'lindisp': False}},
+                                 model_configs={'near': 1.0, 'far': 100.0, 'near_ndc': 0.0, 'far_ndc': 1.0})
+    with patched_rand([u]):
+        z = RT.SimpleTensoRF.get_z_vals_coarse(fake, {'pixel_id': torch.zeros(n, 3)}, {'rays_o': o, 'rays_d': d}, tm)
+    pts = o_ndc[:, None, :] + d_ndc[:, None, :] * z[:, :, None]
+    vdir = CU.get_view_dirs_tr(d_ndc)
+    inp = {'pts': pts, 'z_vals': z, 'z_vals_ndc': z, 'rays_o': o, 'rays_d': d, 'rays_d_ndc': d_ndc,
+           'view_dirs': vdir}
+    with patched_rand([torch.tensor([0.75])]):       # white-background coin: rand >= 0.5 -> no white
+        ret = tm(inp, retraw=True)
+    tg = torch.Generator().manual_seed(47)
+    loss = 0
+    out = {}
+    for k in ('rgb', 'depth', 'depth_ndc', 'acc'):
+        c = torch.randn(ret[k].shape, generator=tg)
+        out[f'cot_{k}'] = c.numpy()
+        loss = loss + torch.sum(ret[k] * c)
+    loss.backward()
+    out.update({'res': res.numpy(), 'bbox': np.array(bbox, np.float32), 'alpha_vol': vol.numpy(), 'u': u.numpy(),
+                'rays_o': o.numpy(), 'rays_d': d.numpy(), 'rays_o_ndc': o_ndc.numpy(), 'rays_d_ndc': d_ndc.numpy(),
+                'view_dirs': vdir.numpy(), 'z': z.numpy(), 'num_samples': tm.num_samples.numpy()})
+    for i in range(3):
+        out[f'planes_density.{i}'] = tm.matrices_density[i].detach().numpy()[0]
+        out[f'lines_density.{i}'] = tm.vectors_density[i].detach().numpy()[0]
+        out[f'planes_color.{i}'] = tm.matrices_color[i].detach().numpy()[0]
+        out[f'lines_color.{i}'] = tm.vectors_color[i].detach().numpy()[0]
+        out[f'grad_planes_density.{i}'] = tm.matrices_density[i].grad.numpy()[0]
+        out[f'grad_lines_density.{i}'] = tm.vectors_density[i].grad.numpy()[0]
+        out[f'grad_planes_color.{i}'] = tm.matrices_color[i].grad.numpy()[0]
+        out[f'grad_lines_color.{i}'] = tm.vectors_color[i].grad.numpy()[0]
+    out['basis_matrix_color.weight'] = tm.basis_matrix_color.weight.detach().numpy()
+    out['grad_basis_matrix_color.weight'] = tm.basis_matrix_color.weight.grad.numpy()
+    for k, prm in tm.color_predictor.named_parameters():
+        out['color_predictor.' + k] = prm.detach().numpy()
+        out['grad_color_predictor.' + k] = prm.grad.numpy()
+    for k, v in ret.items():
+        out['out_' + k] = v.detach().numpy()
+    return out
+
+
 def tensorf_cp_case():
     """CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123): density and
     colour from three lines each, then the same renderer; LowRankTensor.forward on a
@@ -590,6 +670,7 @@ def main():
             augs=[{'name': 'views_augmentation', 'coarse_model': mlp_cfg(lp=4, views=False, vdr=False)}],
             aug_seeds=[77]),
         'tensorf': tensorf_case,
+        'tensorf_ndc': tensorf_ndc_case,
         'tensorf_cp': tensorf_cp_case,
         'losses': losses_case,
         'reprojection': reprojection_case,

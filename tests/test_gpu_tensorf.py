@@ -25,13 +25,14 @@ def _tcfg():
             'color_predictor': 'MLP_Features', 'num_units_color_predictor': 16, 'predict_visibility': False}
 
 
-def _model(g):
+def _model(g, ndc=False):
     from simple_rf_gb300 import build as b
     b.build()
     from simple_rf_gb300 import tensorf as T
     from simple_rf_gb300.tensorf_model import AlphaGridMask, GbVmTensor
-    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}
-    tm = GbVmTensor('coarse_model', configs, _tcfg(), {'bounding_box': _tcfg()['bounding_box']})
+    configs = {'data_loader': {'ndc': ndc}, 'model': {'white_bkgd': not ndc}}
+    tcfg = dict(_tcfg(), bounding_box=g['bbox'].tolist())
+    tm = GbVmTensor('coarse_model', configs, tcfg, {'bounding_box': tcfg['bounding_box']})
     tm.update_tensor_params(torch.tensor(g['res']), torch.tensor(g['bbox']))
     with torch.no_grad():
         for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
@@ -60,6 +61,38 @@ def test_tensorf_forward_backward_matches_reference_golden(golden):
         got = out[k].detach().cpu().numpy()
         np.testing.assert_allclose(got, ref, rtol=1e-4, atol=2e-4 * max(1.0, float(np.abs(ref).max())), err_msg=k)
     loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'acc'))
+    loss.backward()
+    pairs = []
+    for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                        ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+        for i in range(3):
+            pairs.append((f'{kind}.{i}', plist[i].grad[0]))
+    pairs.append(('basis_matrix_color.weight', tm.basis_matrix_color.weight.grad))
+    for k, prm in tm.color_predictor.named_parameters():
+        pairs.append(('color_predictor.' + k, prm.grad))
+    for name, grad in pairs:
+        ref = g['grad_' + name]
+        got = grad.detach().cpu().numpy()
+        rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert rel < 1e-3, (name, rel)
+
+
+def test_tensorf_ndc_forward_backward_matches_reference_golden(golden):
+    """NDC mode (the forward-facing TensoRF configuration): samples march along
+    the NDC rays, compositing takes NDC deltas and converts depths with the world
+    rays; outputs and gradients against the reference's LowRankTensor.forward
+    (golden tensorf_ndc, no white background: the coin came up >= 0.5)."""
+    g = golden('tensorf_ndc')
+    tm = _model(g, ndc=True)
+    tm.eval()
+    t = {k: torch.from_numpy(g[k]).to(DEV) for k in ('rays_o', 'rays_d', 'rays_o_ndc', 'rays_d_ndc', 'view_dirs', 'z')}
+    out = tm({'z_vals_ndc': t['z'], 'rays_o_ndc': t['rays_o_ndc'], 'rays_d_ndc': t['rays_d_ndc'],
+              'rays_o': t['rays_o'], 'rays_d': t['rays_d'], 'view_dirs': t['view_dirs']}, retraw=True)
+    for k in ('rgb', 'depth', 'depth_ndc', 'acc', 'weights', 'raw_sigma', 'depth_var', 'depth_var_ndc'):
+        ref = g['out_' + k]
+        got = out[k].detach().cpu().numpy()
+        np.testing.assert_allclose(got, ref, rtol=1e-4, atol=2e-4 * max(1.0, float(np.abs(ref).max())), err_msg=k)
+    loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'depth_ndc', 'acc'))
     loss.backward()
     pairs = []
     for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),

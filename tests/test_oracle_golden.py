@@ -220,6 +220,26 @@ def test_tensorf_forward_backward(golden):
         assert err < 1e-4, (k, err)
 
 
+def test_tensorf_ndc_forward_backward(golden):
+    """The oracle's NDC path against LowRankTensor.forward in NDC mode (golden
+    tensorf_ndc): stratified NDC depths, NDC marching, metric depth conversion."""
+    g = golden('tensorf_ndc')
+    tp = _tensorf_params(g)
+    spec = ot.RendererSpec(features_dim=7, features_pe=2, views_pe=2, units=16)
+    n, s = g['z'].shape
+    close(on.stratified_z(0.0, 1.0, n, s, g['u']), g['z'], rtol=1e-6, atol=1e-7)
+    out, cache = ot.tensorf_forward(tp, spec, g['rays_o_ndc'], g['rays_d_ndc'], g['z'], alpha_vol=g['alpha_vol'],
+                                    alpha_bbox=g['bbox'], white=False, world_rays=(g['rays_o'], g['rays_d']))
+    for k in ('rgb', 'depth', 'depth_ndc', 'acc', 'weights', 'raw_sigma', 'raw_rgb', 'depth_var', 'depth_var_ndc'):
+        ref = g['out_' + k]
+        close(out[k], ref, rtol=1e-4, atol=1e-5 * max(1.0, float(np.abs(ref).max())))
+    grads = ot.tensorf_backward(tp, spec, cache, {k: g[f'cot_{k}'] for k in ('rgb', 'depth', 'depth_ndc', 'acc')})
+    for k, v in grads.items():
+        ref = g['grad_' + k]
+        err = np.linalg.norm(v - ref) / max(np.linalg.norm(ref), 1e-12)
+        assert err < 1e-4, (k, err)
+
+
 def test_tensorf_cp_forward_backward(golden):
     """The oracle's CP path against CpDecomposedTensor (golden tensorf_cp)."""
     g = golden('tensorf_cp')
