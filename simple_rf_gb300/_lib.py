@@ -164,7 +164,24 @@ def load():
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    _tuner_from_env()
     return lib
+
+
+def _tuner_from_env():
+    """SRF_AUTOTUNE_TABLE=path preloads the tile-shape tuner's choices from a JSON
+    table (autotune.save's format) when the file exists; SRF_AUTOTUNE_SAVE=path
+    writes the table at exit.  A profiler replays and slows every launch, so a
+    profiled process should start from the choices of an unprofiled run."""
+    table, save = os.environ.get('SRF_AUTOTUNE_TABLE'), os.environ.get('SRF_AUTOTUNE_SAVE')
+    if not (table or save):
+        return
+    from . import autotune
+    if table and os.path.exists(table):
+        autotune.load(table)
+    if save:
+        import atexit
+        atexit.register(autotune.save, save)
 
 
 def check(status, what=''):
