@@ -1432,10 +1432,6 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
     }
     // PE adjoint + basis layer: d_feats = dB . Wb, dWb += dB^T feats
     const int threads = (C + 31) / 32 * 32;
-    int64_t blocks = int64_t(num_sms()) * 3;
-    int64_t per = (m + blocks - 1) / blocks;
-    per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
-    blocks = (m + per - 1) / per;
     const size_t bsmem = basis_bwd_smem(C, F, R.k1p);
     if (bsmem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
     if (bsmem > 48 * 1024) {
@@ -1446,6 +1442,16 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
             return SRF_ERR_CUDA;
         }
     }
+    // as many resident blocks as registers and shared memory allow, each over a
+    // contiguous range of rows
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_bwd_kernel, threads, bsmem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    int64_t blocks = int64_t(num_sms()) * per_sm;
+    int64_t per = (m + blocks - 1) / blocks;
+    per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
+    blocks = (m + per - 1) / per;
     basis_bwd_kernel<<<unsigned(blocks), threads, bsmem, s>>>(w.dx, w.B, feats, P[0], m, F, C, lf, R.k1p, fmt,
                                                              cx.gscale(), per, d_feats, G[0]);
     return launch_status();
