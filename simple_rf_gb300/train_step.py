@@ -129,7 +129,7 @@ class NerfTrainStep:
     def __init__(self, n_rays=4096, n_coarse=64, n_fine=128, near=2.0, far=6.0, white_bkgd=True,
                  depth_fraction=0.25, depth_weight=0.1, precision='bf16', spec_kwargs=None, lr=5e-4,
                  betas=(0.9, 0.999), eps=1e-8, seed=0, device='cuda', ndc=None, aug=None, aug_fine=False,
-                 consistency_weight=0.1, train=True, perturb=True, loss_scale_init=65536.0):
+                 consistency_weight=0.1, train=True, perturb=True, loss_scale_init=65536.0, concurrent_aug=True):
         self.dev = torch.device(device)
         self.n, self.sc, self.sf = n_rays, n_coarse, n_fine
         self.s = n_coarse + n_fine
@@ -177,6 +177,11 @@ class NerfTrainStep:
                       for lv, ss in (('coarse', sc), ('fine', s))}
         self.loss = torch.zeros(1, **f32)
         self.step_count = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        # augmented coarse nets run on their own streams, concurrently with the main
+        # nets (they share only the read-only samples; their depth joins the main
+        # stream for the consistency term)
+        self.side = [torch.cuda.Stream(self.dev) for net in self.run[2:] if net.level == 'coarse'] \
+            if concurrent_aug else []
         self.graph = None
         self.launches_per_step = None
 
@@ -233,6 +238,8 @@ class NerfTrainStep:
         u_c, u_f = (self.u_c, self.u_f) if self.perturb else (None, None)
         chk(lib.srf_stratified_z(_vp(zc), _vp(u_c), n, self.sc, self.near, self.far, 0, st), 'stratified_z')
         main_coarse = self.run[0]
+        main_stream = torch.cuda.current_stream(self.dev)
+        side_of, done = {}, {}
         for level in ('coarse', 'fine'):
             lv = self.level[level]
             ss = lv['z'].shape[1]
@@ -240,36 +247,52 @@ class NerfTrainStep:
                 chk(lib.srf_fine_z(_vp(lv['z']), _vp(zc), _vp(main_coarse.b['weights']), _vp(u_f), n, self.sc,
                                    self.sf, st), 'fine_z')
             chk(lib.srf_ray_points(_vp(po), _vp(pd), _vp(lv['z']), n, ss, _vp(lv['pts']), st), 'ray_points')
+            if level == 'coarse' and self.side:
+                fork = torch.cuda.Event()
+                fork.record(main_stream)
+                for net, side in zip((x for x in self.run[2:] if x.level == 'coarse'), self.side):
+                    side.wait_event(fork)
+                    side_of[net.name] = side
             for net in (x for x in self.run if x.level == level):
                 b = net.b
+                sp = _P(side_of[net.name].cuda_stream) if net.name in side_of else st
                 chk(lib.srf_nerf_mlp_forward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(lv['pts']),
                                              _vp(self.vdirs), ss, n * ss, None, _vp(b['sigma']), _vp(b['rgb']),
                                              self.precision, int(self.train), _vp(b['ws']), b['ws'].numel(),
-                                             _vp(self.scaler), st),
+                                             _vp(self.scaler), sp),
                     'mlp_forward')
-                chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(net, False)), st),
+                chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(net, False)), sp),
                     'composite_forward')
-                if not self.train:
-                    continue
-                chk(lib.srf_rgb_depth_loss(_vp(b['rgb_map']), _vp(self.target_rgb), _vp(b['depth']),
-                                           _vp(self.target_depth), _vp(self.depth_mask), n, self.n_depth,
-                                           self.depth_weight, _vp(self.loss), _vp(b['g_rgb']), _vp(b['g_depth']),
-                                           st), 'loss')
+                if self.train:
+                    chk(lib.srf_rgb_depth_loss(_vp(b['rgb_map']), _vp(self.target_rgb), _vp(b['depth']),
+                                               _vp(self.target_depth), _vp(self.depth_mask), n, self.n_depth,
+                                               self.depth_weight, _vp(self.loss), _vp(b['g_rgb']),
+                                               _vp(b['g_depth']), sp), 'loss')
+                if net.name in side_of:
+                    ev = torch.cuda.Event()
+                    ev.record(side_of[net.name])
+                    done[net.name] = ev   # its depth is final here
+                    if self.train:
+                        # an augmented net's gradients do not depend on the main nets:
+                        # its backward follows right away on its own stream
+                        self._backward(lib, net, sp)
         if not self.train:
+            for ev in done.values():
+                main_stream.wait_event(ev)
             return
         # augmented depth as a (detached) target of the main coarse depth
         for net in self.run[2:]:
             if net.level == 'coarse' and self.consistency_weight > 0:
+                if net.name in done:
+                    main_stream.wait_event(done[net.name])
                 chk(lib.srf_depth_mse_loss(_vp(main_coarse.b['depth']), _vp(net.b['depth']), None, n,
                                            self.consistency_weight, 0, _vp(self.loss), _vp(main_coarse.b['g_depth']),
                                            None, st), 'consistency')
         for net in reversed(self.run):
-            b = net.b
-            ss = self.level[net.level]['z'].shape[1]
-            chk(lib.srf_composite_backward(ctypes.byref(self._composite_args(net, True)), st), 'composite_backward')
-            chk(lib.srf_nerf_mlp_backward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(b['d_sigma']),
-                                          _vp(b['d_rgb']), ss, n * ss, net.state.gptr, 0, self.precision, _vp(b['ws']),
-                                          b['ws'].numel(), _vp(self.scaler), st), 'mlp_backward')
+            if net.name not in side_of:
+                self._backward(lib, net, st)
+        for side in side_of.values():
+            main_stream.wait_stream(side)
         chk(lib.srf_counter_add(_vp(self.step_count), 1, self.found_inf, st), 'counter')
         for net in self.nets.values():
             chk(lib.srf_adam_step(_vp(net.flat), _vp(net.grad), _vp(net.m), _vp(net.v), net.flat.numel(), self.lr,
@@ -277,6 +300,16 @@ class NerfTrainStep:
                                   self.found_inf, st), 'adam')
         if self.scaler is not None:
             chk(lib.srf_loss_scaler_update(_vp(self.scaler), 2.0, 0.5, 2000, st), 'loss_scaler_update')
+
+    def _backward(self, lib, net, stream):
+        b = net.b
+        ss = self.level[net.level]['z'].shape[1]
+        _lib.check(lib.srf_composite_backward(ctypes.byref(self._composite_args(net, True)), stream),
+                   'composite_backward')
+        _lib.check(lib.srf_nerf_mlp_backward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(b['d_sigma']),
+                                             _vp(b['d_rgb']), ss, self.n * ss, net.state.gptr, 0, self.precision,
+                                             _vp(b['ws']), b['ws'].numel(), _vp(self.scaler), stream),
+                   'mlp_backward')
 
     # ------------------------------------------------------------- public --
     def set_batch(self, rays_o, rays_d, target_rgb, target_depth, u_coarse, u_fine, non_blocking=True):

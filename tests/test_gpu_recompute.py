@@ -58,3 +58,44 @@ def test_recomputed_backward_matches_stored_activations(precision):
     for name, a, b in zip(spec.param_names, g0, g1):
         rel = float(torch.linalg.norm(a - b) / torch.linalg.norm(a).clamp_min(1e-30))
         assert rel < bar, (name, rel)
+
+
+def test_drop_in_model_activation_budget_config():
+    """configs['model']['activation_budget_bytes'] on the drop-in GbSimpleNeRF:
+    the same rendered outputs and (within 1e-5 relative L2) the same parameter
+    gradients as without a budget, with the backward recomputing ray chunks."""
+    from simple_rf_gb300.nerf import GbSimpleNeRF
+    mc = {'num_samples': 64, 'points_net_depth': 8, 'views_net_depth': 1, 'points_net_width': 256,
+          'views_net_width': 128, 'points_positional_encoding_degree': 10, 'views_positional_encoding_degree': 4,
+          'use_view_dirs': True, 'view_dependent_rgb': True, 'predict_visibility': False}
+    mf = dict(mc, num_samples=128)
+    intr = np.array([[300.0, 0, 32.0], [0, 300.0, 32.0], [0, 0, 1.0]])
+    ext = np.eye(4)
+    model_configs = {'intrinsics': intr[None], 'extrinsics': ext[None], 'resolution': (64, 64), 'near': 2.0,
+                     'far': 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0}
+    rng = np.random.default_rng(3)
+    pix = np.stack([np.zeros(256), rng.integers(0, 64, 256), rng.integers(0, 64, 256)], 1).astype(np.int32)
+    grads, outs = [], []
+    for budget in (None, 8 << 20):
+        model_cfg = {'name': 'GbSimpleNeRF01', 'coarse_model': mc, 'fine_model': mf, 'learn_camera_focal_length': False,
+                     'learn_camera_rotation': False, 'learn_camera_translation': False, 'chunk': 4096,
+                     'lindisp': False, 'netchunk': 16384, 'perturb': False, 'raw_noise_std': 0.0, 'white_bkgd': True}
+        if budget is not None:
+            model_cfg['activation_budget_bytes'] = budget
+        torch.manual_seed(0)
+        model = GbSimpleNeRF({'data_loader': {'ndc': False}, 'model': model_cfg}, model_configs).to(DEV)
+        spec = on.MlpSpec()
+        with torch.no_grad():
+            for mod, seed in ((model.coarse_model, 0), (model.fine_model, 1)):
+                p = on.xavier_params(spec, seed)
+                for name, prm in mod.named_parameters():
+                    prm.copy_(torch.from_numpy(p[name]))
+        batch = {'pixel_id': torch.from_numpy(pix).to(DEV), 'num_frames': 1, 'common_data': {}}
+        ret = model(batch, retraw=True)
+        (ret['rgb_coarse'].sum() + ret['rgb_fine'].sum() + 0.1 * ret['depth_fine'].sum()).backward()
+        outs.append(ret['rgb_fine'].detach())
+        grads.append([p.grad.detach().double().clone() for p in list(model.coarse_model.parameters()) +
+                      list(model.fine_model.parameters())])
+    assert torch.equal(outs[0], outs[1])
+    for a, b in zip(*grads):
+        assert float(torch.linalg.norm(a - b) / torch.linalg.norm(a).clamp_min(1e-30)) < 1e-5
