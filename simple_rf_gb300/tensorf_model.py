@@ -521,17 +521,61 @@ def _host_counts(counts):
     return [int(v) for v in torch.cat([c.reshape(1) for c in counts]).cpu().tolist()]
 
 
-def forward_models(calls, retraw):
+_SIDE_STREAMS = {}
+
+
+def _side_stream(device, i):
+    key = (str(device), i)
+    if key not in _SIDE_STREAMS:
+        _SIDE_STREAMS[key] = torch.cuda.Stream(device)
+    return _SIDE_STREAMS[key]
+
+
+def forward_models(calls, retraw, concurrent=True):
     """``[model(input_dict, retraw) for model, input_dict in calls]`` with the
     phases of every model enqueued before each host read of the sample counts:
     two device-to-host reads for the whole list instead of two per model (the
-    GPU holds every model's pending work while the host waits).  Outputs are
-    those of calling the models one by one."""
-    states = [m.forward_begin(inp) for m, inp in calls]
-    for (m, _), st, nv in zip(calls, states, _host_counts([st['cnt_v'] for st in states])):
-        m.forward_density(st, nv)
-    return [m.forward_color(st, ns, retraw)
-            for (m, _), st, ns in zip(calls, states, _host_counts([st['cnt_s'] for st in states]))]
+    GPU holds every model's pending work while the host waits).  With
+    ``concurrent`` every model after the first runs on a stream of its own, so
+    the models' kernels overlap (their backward passes follow the same streams);
+    the outputs are joined to the caller's stream.  Outputs are those of calling
+    the models one by one."""
+    main = torch.cuda.current_stream()
+    streams = [main] * len(calls)
+    if concurrent and len(calls) > 1:
+        dev = main.device
+        streams = [main] + [_side_stream(dev, i) for i in range(1, len(calls))]
+        for (_, inp), st in zip(calls[1:], streams[1:]):
+            st.wait_stream(main)
+            for t in inp.values():
+                if torch.is_tensor(t) and t.is_cuda:
+                    t.record_stream(st)
+    sides = streams[1:] if streams[0] is not streams[-1] else []
+
+    def join():
+        for st in sides:
+            main.wait_stream(st)
+
+    states = []
+    for (m, inp), st in zip(calls, streams):
+        with torch.cuda.stream(st):
+            states.append(m.forward_begin(inp))
+    join()
+    for (m, _), st, state, nv in zip(calls, streams, states, _host_counts([x['cnt_v'] for x in states])):
+        with torch.cuda.stream(st):
+            m.forward_density(state, nv)
+    join()
+    outs = []
+    for (m, _), st, state, ns in zip(calls, streams, states, _host_counts([x['cnt_s'] for x in states])):
+        with torch.cuda.stream(st):
+            outs.append(m.forward_color(state, ns, retraw))
+    join()
+    for out, st in zip(outs, streams):
+        if st is not main:
+            for t in out.values():
+                if torch.is_tensor(t) and t.is_cuda:
+                    t.record_stream(main)
+    return outs
 
 
 class GbSimpleTensoRF(torch.nn.Module):
