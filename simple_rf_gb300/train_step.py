@@ -129,7 +129,8 @@ class NerfTrainStep:
     def __init__(self, n_rays=4096, n_coarse=64, n_fine=128, near=2.0, far=6.0, white_bkgd=True,
                  depth_fraction=0.25, depth_weight=0.1, precision='bf16', spec_kwargs=None, lr=5e-4,
                  betas=(0.9, 0.999), eps=1e-8, seed=0, device='cuda', ndc=None, aug=None, aug_fine=False,
-                 consistency_weight=0.1, train=True, perturb=True, loss_scale_init=65536.0, concurrent_aug=True):
+                 consistency_weight=0.1, train=True, perturb=True, loss_scale_init=65536.0, concurrent_aug=True,
+                 overlap_coarse=True):
         self.dev = torch.device(device)
         self.n, self.sc, self.sf = n_rays, n_coarse, n_fine
         self.s = n_coarse + n_fine
@@ -182,6 +183,9 @@ class NerfTrainStep:
         # stream for the consistency term)
         self.side = [torch.cuda.Stream(self.dev) for net in self.run[2:] if net.level == 'coarse'] \
             if concurrent_aug else []
+        # the main coarse net's backward needs only its own forward: it runs on a
+        # stream of its own while the fine net evaluates
+        self.cb_stream = torch.cuda.Stream(self.dev) if (overlap_coarse and train) else None
         self.graph = None
         self.launches_per_step = None
 
@@ -276,22 +280,22 @@ class NerfTrainStep:
                         # an augmented net's gradients do not depend on the main nets:
                         # its backward follows right away on its own stream
                         self._backward(lib, net, sp)
+            if level == 'coarse' and self.cb_stream is not None:
+                cb = self.cb_stream
+                ev = torch.cuda.Event()
+                ev.record(main_stream)
+                cb.wait_event(ev)
+                self._coarse_backward(lib, main_coarse, done, cb)
         if not self.train:
             for ev in done.values():
                 main_stream.wait_event(ev)
             return
-        # augmented depth as a (detached) target of the main coarse depth
-        for net in self.run[2:]:
-            if net.level == 'coarse' and self.consistency_weight > 0:
-                if net.name in done:
-                    main_stream.wait_event(done[net.name])
-                chk(lib.srf_depth_mse_loss(_vp(main_coarse.b['depth']), _vp(net.b['depth']), None, n,
-                                           self.consistency_weight, 0, _vp(self.loss), _vp(main_coarse.b['g_depth']),
-                                           None, st), 'consistency')
+        if self.cb_stream is None:
+            self._coarse_backward(lib, main_coarse, done, main_stream)
         for net in reversed(self.run):
-            if net.name not in side_of:
+            if net.name not in side_of and net is not main_coarse:
                 self._backward(lib, net, st)
-        for side in side_of.values():
+        for side in list(side_of.values()) + ([self.cb_stream] if self.cb_stream is not None else []):
             main_stream.wait_stream(side)
         chk(lib.srf_counter_add(_vp(self.step_count), 1, self.found_inf, st), 'counter')
         for net in self.nets.values():
@@ -300,6 +304,19 @@ class NerfTrainStep:
                                   self.found_inf, st), 'adam')
         if self.scaler is not None:
             chk(lib.srf_loss_scaler_update(_vp(self.scaler), 2.0, 0.5, 2000, st), 'loss_scaler_update')
+
+    def _coarse_backward(self, lib, main_coarse, done, stream):
+        """The consistency term (augmented coarse depth as a detached target of the
+        main coarse depth) and the main coarse net's backward, on ``stream``."""
+        sp = _P(stream.cuda_stream)
+        for net in self.run[2:]:
+            if net.level == 'coarse' and self.consistency_weight > 0:
+                if net.name in done:
+                    stream.wait_event(done[net.name])
+                _lib.check(lib.srf_depth_mse_loss(_vp(main_coarse.b['depth']), _vp(net.b['depth']), None, self.n,
+                                                  self.consistency_weight, 0, _vp(self.loss),
+                                                  _vp(main_coarse.b['g_depth']), None, sp), 'consistency')
+        self._backward(lib, main_coarse, sp)
 
     def _backward(self, lib, net, stream):
         b = net.b
