@@ -47,6 +47,14 @@ int64_t srf_launch_count(void);
  * range violations) that kernels set instead of trapping.  Synchronises `stream`.
  * Writes the flag value (0 = clean) to *flag_out. */
 int srf_read_device_flag(int* flag_out, void* stream);
+/* A non-blocking CUDA stream of the current device, and its release (the
+ * release returns at once; pending work finishes first).  Concurrent stages of a
+ * step (an augmented net's pass, the coarse net's backward) need streams that
+ * are distinct CUDA streams; pooled streams of a host framework may alias one
+ * another.  No reference counterpart (the reference
+ * runs on PyTorch's current stream). */
+int srf_stream_create(void** stream_out);
+int srf_stream_destroy(void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Ray generation and sampling                                               */

@@ -67,6 +67,8 @@ _SIGS = {
     'srf_version': (c_char_p, []),
     'srf_last_cuda_error': (c_char_p, []),
     'srf_read_device_flag': (c_int, [ctypes.POINTER(c_int), P]),
+    'srf_stream_create': (c_int, [ctypes.POINTER(P)]),
+    'srf_stream_destroy': (c_int, [P]),
     'srf_pixel_rays': (c_int, [P, P, P, c_int, c_int, P, P, P]),
     'srf_ndc_rays': (c_int, [P, P, P, P, c_int, c_int, c_int, c_float, P, P, P, P]),
     'srf_stratified_z': (c_int, [P, P, c_int, c_int, c_float, c_float, c_int, P]),
@@ -182,6 +184,22 @@ def _tuner_from_env():
     if save:
         import atexit
         atexit.register(autotune.save, save)
+
+
+def new_stream(device):
+    """A CUDA stream of its own on ``device`` (srf_stream_create), as a torch
+    stream; released when the returned object is collected.  Torch's pooled
+    streams can alias one another (and the stream a CUDA graph is captured on),
+    which would serialise stages meant to run concurrently."""
+    import weakref
+    import torch
+    lib = load()
+    ptr = P()
+    with torch.cuda.device(device):
+        check(lib.srf_stream_create(ctypes.byref(ptr)), 'srf_stream_create')
+    st = torch.cuda.ExternalStream(ptr.value, device=device)
+    weakref.finalize(st, lib.srf_stream_destroy, P(ptr.value))
+    return st
 
 
 def check(status, what=''):

@@ -135,6 +135,28 @@ extern "C" const char* srf_last_cuda_error(void) { return g_last_error; }
 
 extern "C" int64_t srf_launch_count(void) { return srf::g_launches.load(); }
 
+extern "C" int srf_stream_create(void** stream_out) {
+    if (!stream_out) return SRF_ERR_NULL;
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        srf::set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    *stream_out = st;
+    return SRF_OK;
+}
+
+extern "C" int srf_stream_destroy(void* stream) {
+    if (!stream) return SRF_ERR_NULL;
+    cudaError_t e = cudaStreamDestroy(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        srf::set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    return SRF_OK;
+}
+
 extern "C" int srf_read_device_flag(int* flag_out, void* stream) {
     if (!flag_out) return SRF_ERR_NULL;
     int* f = srf::device_flag();

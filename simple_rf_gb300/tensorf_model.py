@@ -527,7 +527,7 @@ _SIDE_STREAMS = {}
 def _side_stream(device, i):
     key = (str(device), i)
     if key not in _SIDE_STREAMS:
-        _SIDE_STREAMS[key] = torch.cuda.Stream(device)
+        _SIDE_STREAMS[key] = _lib.new_stream(device)
     return _SIDE_STREAMS[key]
 
 

@@ -181,11 +181,11 @@ class NerfTrainStep:
         # augmented coarse nets run on their own streams, concurrently with the main
         # nets (they share only the read-only samples; their depth joins the main
         # stream for the consistency term)
-        self.side = [torch.cuda.Stream(self.dev) for net in self.run[2:] if net.level == 'coarse'] \
+        self.side = [_lib.new_stream(self.dev) for net in self.run[2:] if net.level == 'coarse'] \
             if concurrent_aug else []
         # the main coarse net's backward needs only its own forward: it runs on a
         # stream of its own while the fine net evaluates
-        self.cb_stream = torch.cuda.Stream(self.dev) if (overlap_coarse and train) else None
+        self.cb_stream = _lib.new_stream(self.dev) if (overlap_coarse and train) else None
         self.graph = None
         self.launches_per_step = None
 
