@@ -17,10 +17,13 @@ from .tensorf_model import forward_models
 
 
 class TensorfTrainStep:
-    """forward (both models) -> rgb MSE -> backward -> Adam (one srf_adam_multi_step launch)."""
+    """forward (every model) -> rgb MSE -> backward -> Adam (one srf_adam_multi_step launch).
+    Samples march from ``near`` to ``far`` along each ray inside each model's box
+    (SimpleTensoRF09.py:388-400)."""
 
-    def __init__(self, models, lr_tensor=0.02, lr_network=1e-3):
+    def __init__(self, models, lr_tensor=0.02, lr_network=1e-3, near=2.0, far=6.0):
         self.models = models
+        self.near, self.far = float(near), float(far)
         self.params = []
         for tm in models:
             tensor_ps = list(tm.matrices_density) + list(tm.vectors_density) + list(tm.matrices_color) + \
@@ -32,13 +35,12 @@ class TensorfTrainStep:
         self.last = {}
 
     def step(self, o, d, t_rgb, u):
-        n = o.shape[0]
         vd = F.view_dirs(d)
         loss = 0.0
         calls = []
         for i, tm in enumerate(self.models):
             bbox, s, step = tm.host_geometry()
-            z = F.aabb_z(o, d, s, bbox, 2.0, 6.0, step, u[:, i].contiguous())
+            z = F.aabb_z(o, d, s, bbox, self.near, self.far, step, u[:, i].contiguous())
             calls.append((tm, {'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}))
         # both models' phases side by side: two host reads of sample counts per step
         for out in forward_models(calls, retraw=False):
@@ -77,8 +79,10 @@ class TensorfGraphStep:
     REGROW = 1.25
     ROUND = 1024
 
-    def __init__(self, models, n_rays, lr_tensor=0.02, lr_network=1e-3, state=None, step_dev=None):
+    def __init__(self, models, n_rays, lr_tensor=0.02, lr_network=1e-3, state=None, step_dev=None, near=2.0,
+                 far=6.0):
         self.models = models
+        self.near, self.far = float(near), float(far)
         self.n = int(n_rays)
         dev = models[0].matrices_density[0].device
         self.dev = dev
@@ -112,7 +116,7 @@ class TensorfGraphStep:
         calls = []
         for i, tm in enumerate(self.models):
             bbox, s, step = tm.host_geometry()
-            z = F.aabb_z(self.o, self.d, s, bbox, 2.0, 6.0, step, self.u[:, i].contiguous())
+            z = F.aabb_z(self.o, self.d, s, bbox, self.near, self.far, step, self.u[:, i].contiguous())
             calls.append((tm, {'z_vals': z, 'rays_o': self.o, 'rays_d': self.d, 'view_dirs': vd}))
         return calls
 
