@@ -114,6 +114,24 @@ def dist_setup(args):
     return ws, rank, local
 
 
+def max_over_ranks(x, device):
+    """The largest x over the ranks of the default process group (a timed
+    region's duration: the slowest replica bounds the job); x itself without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rays_per_s(world_size, rays_per_step, steps, seconds):
+    """Whole-job throughput of replicas that each train rays_per_step rays per
+    step: every rank's rays over the slowest rank's time."""
+    return world_size * rays_per_step * steps / seconds
+
+
 def time_steps(step, k, stream):
     import torch
     start = torch.cuda.Event(enable_timing=True)
@@ -387,14 +405,6 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    def max_over_ranks(x):
-        if ws == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     # ---- BF16 tcgen05 step (headline) ----
     bf = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision='bf16', device=dev)
     bf.set_batch(*pool[0])
@@ -414,7 +424,7 @@ def run_ours(args):
         roof = roofline_gemm(dev, hbm_peak, tf_peak, peak_kind) if rank == 0 else None
         kroofs = kernel_rooflines(hbm_peak, peak_kind) if rank == 0 else None
     barrier()
-    t_bf = max_over_ranks(t_bf)
+    t_bf = max_over_ranks(t_bf, dev)
     # rgb agreement of the BF16 step with the FP32 plain step (same weights, same batch)
     loss_host = torch.zeros(1, pin_memory=True)
 
@@ -426,7 +436,7 @@ def run_ours(args):
     for i in range(args.warmup):
         e2e_step(i)
     barrier()
-    t_e2e = max_over_ranks(time_steps(e2e_step, args.steps, stream))
+    t_e2e = max_over_ranks(time_steps(e2e_step, args.steps, stream), dev)
     barrier()
     launches = bf.launches_per_step
 
@@ -442,7 +452,7 @@ def run_ours(args):
 
     fp_step(0)
     barrier()
-    t_fp = max_over_ranks(time_steps(fp_step, k32, stream))
+    t_fp = max_over_ranks(time_steps(fp_step, k32, stream), dev)
     barrier()
 
     acc = rgb_agreement(NerfTrainStep, pool[1], dev)
@@ -469,7 +479,7 @@ def run_ours(args):
             dist.barrier()
             dist.destroy_process_group()
         return 0
-    value = ws * N_RAYS * args.steps / t_bf
+    value = job_rays_per_s(ws, N_RAYS, args.steps, t_bf)
     line = {
         'metric': METRIC, 'value': round(value, 1), 'unit': 'rays/s', 'n_gpus': ws, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': round(1e3 * t_bf / args.steps, 4), 'higher_is_better': True,
@@ -483,7 +493,7 @@ def run_ours(args):
                    'cuda_graph': True},
         'samples_per_s': round(value * (N_COARSE + N_COARSE + N_FINE), 1),
         'tflops_model': round(value * 6 * MACS_PER_SAMPLE * (N_COARSE + N_COARSE + N_FINE) / 1e12, 1),
-        'fp32_plain': {'value': round(ws * N_RAYS * k32 / t_fp, 1), 'unit': 'rays/s',
+        'fp32_plain': {'value': round(job_rays_per_s(ws, N_RAYS, k32, t_fp), 1), 'unit': 'rays/s',
                        'ms_per_step': round(1e3 * t_fp / k32, 3), 'steps': k32},
         'speedup_bf16_vs_fp32_plain': round((N_RAYS * args.steps / t_bf) / (N_RAYS * k32 / t_fp), 2),
         'accuracy': acc,
@@ -509,7 +519,8 @@ def run_ours(args):
         'render': dict(variants['render'], workload='8 views x 504x378 NDC rays, NeRF pair (main coarse+fine + '
                                                     'augmented coarse), 64+128 samples, chunks of 65536'),
         'device_flag': fl.value,
-        'e2e': {'value': round(ws * N_RAYS * args.steps / t_e2e, 1), 'unit': 'rays/s', 'h2d_bytes_per_step': h2d,
+        'e2e': {'value': round(job_rays_per_s(ws, N_RAYS, args.steps, t_e2e), 1), 'unit': 'rays/s',
+                'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': 4},
         'gpu_launches': launches * args.steps if launches else None,
         'gpu_launches_per_step': launches,
