@@ -213,7 +213,12 @@ int srf_bf16_wgrad(float* partial, size_t partial_bytes, int* splits, const void
 
 enum {
     SRF_COMPOSITE_NDC = 1,        /* z is NDC depth; also emit depth_ndc / depth_var_ndc  */
-    SRF_COMPOSITE_WHITE_BKGD = 2  /* rgb += 1 - acc                                        */
+    SRF_COMPOSITE_WHITE_BKGD = 2, /* rgb += 1 - acc                                        */
+    /* transmittance T_i = exp(-sum_{j<i} sigma_j delta_j) (one exclusive sum scan)
+     * instead of the reference's exclusive cumprod of 1 - alpha_j + 1e-10; the two
+     * differ by the 1e-10 terms and rounding only.  Rays of at most 256 samples
+     * (SRF_ERR_UNSUPPORTED beyond).  The 16-bit training steps use it. */
+    SRF_COMPOSITE_EXP_PREFIX = 4
 };
 
 typedef struct {

@@ -55,6 +55,7 @@ class AdamTensor(ctypes.Structure):
 
 SRF_COMPOSITE_NDC = 1
 SRF_COMPOSITE_WHITE_BKGD = 2
+SRF_COMPOSITE_EXP_PREFIX = 4
 SRF_PRECISION_FP32 = 0
 SRF_PRECISION_BF16 = 1
 SRF_PRECISION_FP16 = 2

@@ -54,6 +54,11 @@ __device__ __forceinline__ void sample_terms(const RayCtx& c, int i, float& delt
     p = 1.f - alpha + 1e-10f;
 }
 
+// y = sigma delta ds of sample i (the exponent of its 1 - alpha).
+__device__ __forceinline__ float sigma_y(const RayCtx& c, int i, float delta) {
+    return c.sigma[i] * delta * c.ds;
+}
+
 // Pass over the ray storing T (exclusive cumprod of p) and alpha in shared memory.
 __device__ void forward_scan(const RayCtx& c, float* sT, float* sA) {
     int lane = threadIdx.x & 31;
@@ -324,12 +329,33 @@ __device__ __forceinline__ void scan_rounds(float (&T)[R], int lane) {
     }
 }
 
+// Exp-of-prefix-sum transmittance: on entry Y[k] holds y = sigma delta ds of
+// each sample; on exit it holds T = exp(-(sum of y over the earlier samples)).
+template <int R>
+__device__ __forceinline__ void exp_scan_rounds(float (&Y)[R], int lane) {
+    float carry = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        float inc = Y[k];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            float t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        float exc = __shfl_up_sync(0xffffffffu, inc, 1);
+        if (lane == 0) exc = 0.f;
+        Y[k] = expf(-(carry + exc));
+        carry = carry + __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
 template <int R>
 __global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_args a) {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int r = blockIdx.x * (blockDim.x >> 5) + warp;
     if (r >= a.n_rays) return;
     RayCtx c = make_ctx(a, r);
+    const bool exp_prefix = (a.flags & SRF_COMPOSITE_EXP_PREFIX) != 0;
     const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;   // NULL: zero colours
     float al[R], T[R], zz[R], c0[R], c1[R], c2[R];
 #pragma unroll
@@ -343,16 +369,21 @@ __global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_ar
             float delta, ex, alpha, p;
             sample_terms(c, i, delta, ex, alpha, p);
             al[k] = alpha;
-            T[k] = p;
+            T[k] = exp_prefix ? sigma_y(c, i, delta) : p;
             zz[k] = c.z[i];
             if (rgb) {
                 c0[k] = rgb[3 * i];
                 c1[k] = rgb[3 * i + 1];
                 c2[k] = rgb[3 * i + 2];
             }
+        } else if (exp_prefix) {
+            T[k] = 0.f;
         }
     }
-    scan_rounds<R>(T, lane);
+    if (exp_prefix)
+        exp_scan_rounds<R>(T, lane);
+    else
+        scan_rounds<R>(T, lane);
     float cr = 0.f, cg = 0.f, cb = 0.f, acc = 0.f, wz = 0.f, wzn = 0.f;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -424,6 +455,7 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
     int r = blockIdx.x * (blockDim.x >> 5) + warp;
     if (r >= a.n_rays) return;
     RayCtx c = make_ctx(a, r);
+    const bool exp_prefix = (a.flags & SRF_COMPOSITE_EXP_PREFIX) != 0;
     const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;
     const int64_t ro = int64_t(r) * c.s;
     // G holds dL/dw_i once formed; until then the colour dot product's partial terms
@@ -438,7 +470,7 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
             float delta, ex, alpha, p;
             sample_terms(c, i, delta, ex, alpha, p);
             al[k] = alpha;
-            T[k] = p;
+            T[k] = exp_prefix ? sigma_y(c, i, delta) : p;
             ex_[k] = ex;
             dl[k] = delta;
             zz[k] = c.z[i];
@@ -459,8 +491,12 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
     for (int k = 0; k < R; ++k) {
         const int i = 32 * k + lane;
         cdot[k] = (rgb && i < c.s) ? rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 : 0.f;
+        if (exp_prefix && i >= c.s) T[k] = 0.f;
     }
-    scan_rounds<R>(T, lane);
+    if (exp_prefix)
+        exp_scan_rounds<R>(T, lane);
+    else
+        scan_rounds<R>(T, lane);
     float acc = 0.f, wz = 0.f, wzn = 0.f;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -508,6 +544,38 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
             g += gdn * dn * inv + gvn * (dn * dn - 2.f * bsum_n * dn * inv);
         }
         G[k] = g;
+    }
+    if (exp_prefix) {
+        // w_i = (1 - e^{-y_i}) T_i with T_i = exp(-sum_{j<i} y_j):
+        // dL/dy_k = G_k e^{-y_k} T_k - sum_{i>k} G_i w_i (a reverse exclusive sum scan)
+        float carry = 0.f;
+#pragma unroll
+        for (int k = R - 1; k >= 0; --k) {
+            const int i = 32 * k + lane;
+            if (32 * k >= c.s) continue;   // warp-uniform
+            const bool in = i < c.s;
+            const float w = in ? al[k] * T[k] : 0.f;
+            const float gw = in ? G[k] * w : 0.f;
+            float inc = gw;   // inclusive suffix sum over lanes lane..31 of this round
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                float t = __shfl_down_sync(0xffffffffu, inc, o);
+                if (lane + o < 32) inc += t;
+            }
+            const float after = carry + (inc - gw);   // sum over the samples after i
+            if (in) {
+                const float dy = G[k] * ex_[k] * T[k] - after;
+                a.d_sigma[ro + i] = dy * c.ds * dl[k];
+                if (a.d_rgb) {
+                    float* dr = a.d_rgb + (ro + i) * 3;
+                    dr[0] = w * g0;
+                    dr[1] = w * g1;
+                    dr[2] = w * g2;
+                }
+            }
+            carry = carry + __shfl_sync(0xffffffffu, inc, 0);
+        }
+        return;
     }
     // reverse affine scan: R_i = G_{i+1} a_{i+1} + p_{i+1} R_{i+1}, R_{S-1} = 0
     float carry = 0.f, next_ga = 0.f, next_p = 0.f;
@@ -636,6 +704,7 @@ using namespace srf;
 extern "C" int srf_composite_forward(const srf_composite_args* args, void* stream) {
     int st = check_args(args, false);
     if (st != SRF_OK || args->n_rays == 0) return st;
+    if ((args->flags & SRF_COMPOSITE_EXP_PREFIX) && !reg_rounds(args->n_samples)) return SRF_ERR_UNSUPPORTED;
     switch (reg_rounds(args->n_samples)) {
         case 2: return launch_reg(composite_fwd_reg_kernel<2>, args, stream);
         case 4: return launch_reg(composite_fwd_reg_kernel<4>, args, stream);
@@ -648,6 +717,7 @@ extern "C" int srf_composite_forward(const srf_composite_args* args, void* strea
 extern "C" int srf_composite_backward(const srf_composite_args* args, void* stream) {
     int st = check_args(args, true);
     if (st != SRF_OK || args->n_rays == 0) return st;
+    if ((args->flags & SRF_COMPOSITE_EXP_PREFIX) && !reg_rounds(args->n_samples)) return SRF_ERR_UNSUPPORTED;
     switch (reg_rounds(args->n_samples)) {
         case 2: return launch_reg(composite_bwd_reg_kernel<2>, args, stream);
         case 4: return launch_reg(composite_bwd_reg_kernel<4>, args, stream);

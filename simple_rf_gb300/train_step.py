@@ -206,6 +206,10 @@ class NerfTrainStep:
         a = _lib.CompositeArgs()
         a.n_rays, a.n_samples = self.n, z.shape[1]
         a.flags = (_lib.SRF_COMPOSITE_WHITE_BKGD if self.white else 0) | (_lib.SRF_COMPOSITE_NDC if self.ndc else 0)
+        if self.precision != _lib.SRF_PRECISION_FP32 and a.n_samples <= 256:
+            # the 16-bit steps take transmittance as exp of an exclusive prefix sum of
+            # sigma delta; the FP32 plain step keeps the reference's cumprod form
+            a.flags |= _lib.SRF_COMPOSITE_EXP_PREFIX
         a.distance_scale = 1.0
         a.sigma, a.rgb, a.z, a.rays_d = b['sigma'].data_ptr(), b['rgb'].data_ptr(), z.data_ptr(), \
             self.rays_d.data_ptr()
