@@ -152,10 +152,17 @@ class TensorfGraphStep:
             forward_models(self._calls(), retraw=False)
         return [(tm.last_sample_counts['valid'], tm.last_sample_counts['surface']) for tm in self.models]
 
-    def _capture(self, counts, margin):
+    @classmethod
+    def capacities(cls, counts, margin):
+        """(valid, surface) launch capacities for per-model (valid, surface)
+        sample counts: margin above each count, rounded up to the next multiple of
+        ROUND rows (always above the count, so a capacity of 0 never occurs)."""
         def cap(x):
-            return (int(x * margin) // self.ROUND + 1) * self.ROUND
-        self.caps = [(cap(v), cap(s)) for v, s in counts]
+            return (int(x * margin) // cls.ROUND + 1) * cls.ROUND
+        return [(cap(v), cap(s)) for v, s in counts]
+
+    def _capture(self, counts, margin):
+        self.caps = self.capacities(counts, margin)
         self.caps_dev.copy_(torch.tensor([c for pair in self.caps for c in pair], dtype=torch.int32))
         self.graph = None
         torch.cuda.synchronize(self.dev)

@@ -30,3 +30,16 @@ def test_chunks_are_whole_rays_within_budget(m, div, budget):
 def test_budget_below_one_unit_raises():
     with pytest.raises(RuntimeError, match='activation budget'):
         recompute_rows(4096 * 192, 192, _ws(384) - 1, _ws)
+
+
+def test_tensorf_graph_step_capacities():
+    """Capacities of the captured TensoRF step: above every count by the margin,
+    multiples of 1024 rows, and growing by the re-capture margin after an overflow."""
+    from simple_rf_gb300.tensorf_step import TensorfGraphStep as G
+    caps = G.capacities([(2349211, 1141923), (581631, 288894), (0, 0)], G.MARGIN)
+    for (v, s), (cv, cs) in zip([(2349211, 1141923), (581631, 288894), (0, 0)], caps):
+        assert cv % G.ROUND == 0 and cs % G.ROUND == 0
+        assert cv > v * G.MARGIN and cs > s * G.MARGIN
+        assert cv - v * G.MARGIN <= G.ROUND and cs - s * G.MARGIN <= G.ROUND
+    grown = G.capacities([(c[0] + 1, c[1] + 1) for c in caps], G.REGROW)
+    assert all(g[0] > c[0] and g[1] > c[1] for g, c in zip(grown, caps))
