@@ -461,6 +461,42 @@ def tensorf_ndc_case():
     return out
 
 
+def tensorf_cfg(vox, dens, col, bbox):
+    return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': dens,
+            'num_components_color': col, 'bounding_box': bbox, 'num_voxels_initial': vox, 'num_voxels_final': vox,
+            'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5, 'alpha_mask_update_iters': [],
+            'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4, 'use_view_dirs': True,
+            'view_dependent_color': True, 'views_positional_encoding_degree': 0,
+            'features_positional_encoding_degree': 0, 'features_dimension_color': 27, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 128, 'predict_visibility': False}
+
+
+def state_dict_case():
+    """state_dict keys and shapes of the reference's SimpleNeRF (main coarse + fine
+    nets, a views and a points augmentation, camera learners) and SimpleTensoRF
+    (main VM model and an augmented one at NDC bounding box), the configurations
+    of the reference's demos at reduced grid sizes; the drop-in models must
+    produce the same so checkpoints load either way."""
+    augs = [{'name': 'views_augmentation', 'coarse_model': mlp_cfg(lp=4, views=False, vdr=False)},
+            {'name': 'points_augmentation', 'coarse_model': mlp_cfg(lps=3)}]
+    configs, model_configs = nerf_configs(mlp_cfg(ns=64), mlp_cfg(ns=128), ndc=True, augs=augs)
+    nerf = RN.SimpleNeRF(configs, model_configs)
+    bbox = [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]]
+    model = {'name': 'SimpleTensoRF09', 'coarse_model': tensorf_cfg(24 ** 3, [16, 4, 4], [48, 12, 12], bbox),
+             'augmentations': [{'name': 'points_augmentation',
+                                'coarse_model': tensorf_cfg(12 ** 3, [16, 4, 4], [48, 12, 12], bbox)}],
+             'learn_camera_focal_length': False, 'learn_camera_rotation': False, 'learn_camera_translation': False,
+             'chunk': 1 << 16, 'lindisp': False, 'perturb': True, 'white_bkgd': False}
+    tconfigs = {'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}
+    tmodel_configs = dict(model_configs, bounding_box=np.array(bbox))
+    tensorf = RT.SimpleTensoRF(tconfigs, tmodel_configs)
+    out = {}
+    for tag, m in (('nerf', nerf), ('tensorf', tensorf)):
+        out[f'{tag}_keys'] = np.array([f"{k}:{'x'.join(str(d) for d in v.shape)}" for k, v in m.state_dict().items()])
+    return out
+
+
 def tensorf_cp_case():
     """CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123): density and
     colour from three lines each, then the same renderer; LowRankTensor.forward on a
@@ -672,6 +708,7 @@ def main():
         'tensorf': tensorf_case,
         'tensorf_ndc': tensorf_ndc_case,
         'tensorf_cp': tensorf_cp_case,
+        'state_dicts': state_dict_case,
         'losses': losses_case,
         'reprojection': reprojection_case,
         'tv': tv_case,

@@ -1,0 +1,63 @@
+"""The drop-in models keep the reference's state_dict: the same keys in the same
+order with the same shapes as the reference's SimpleNeRF and SimpleTensoRF built
+from the same configurations (golden state_dicts.npz from the reference's own
+classes), so checkpoints written by either load into the other
+(Trainer10.py:364-394).  Built on the CPU: construction launches no kernel."""
+import numpy as np
+import pytest
+
+TBOX = [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]]
+
+
+def _mlp(ns=64, lp=10, lv=4, views=True, vdr=True, lps=None):
+    c = {'num_samples': ns, 'points_net_depth': 8, 'views_net_depth': 1, 'points_net_width': 256,
+         'views_net_width': 128, 'points_positional_encoding_degree': lp, 'views_positional_encoding_degree': lv,
+         'use_view_dirs': views, 'view_dependent_rgb': vdr, 'predict_visibility': False}
+    if lps is not None:
+        c['points_sigma_positional_encoding_degree'] = lps
+    return c
+
+
+def _model_configs():
+    return {'intrinsics': np.eye(3)[None], 'extrinsics': np.eye(4)[None], 'resolution': (378, 504), 'near': 1.0,
+            'far': 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0}
+
+
+def _tcfg(vox):
+    return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [16, 4, 4],
+            'num_components_color': [48, 12, 12], 'bounding_box': TBOX, 'num_voxels_initial': vox,
+            'num_voxels_final': vox, 'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5,
+            'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4,
+            'use_view_dirs': True, 'view_dependent_color': True, 'views_positional_encoding_degree': 0,
+            'features_positional_encoding_degree': 0, 'features_dimension_color': 27, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 128, 'predict_visibility': False}
+
+
+def _signature(model):
+    return [f"{k}:{'x'.join(str(d) for d in v.shape)}" for k, v in model.state_dict().items()]
+
+
+def test_nerf_state_dict_matches_reference(golden):
+    pytest.importorskip('torch')
+    from simple_rf_gb300.nerf import GbSimpleNeRF
+    augs = [{'name': 'views_augmentation', 'coarse_model': _mlp(lp=4, views=False, vdr=False)},
+            {'name': 'points_augmentation', 'coarse_model': _mlp(lps=3)}]
+    model = {'name': 'GbSimpleNeRF01', 'coarse_model': _mlp(), 'fine_model': _mlp(ns=128),
+             'learn_camera_focal_length': False, 'learn_camera_rotation': False, 'learn_camera_translation': False,
+             'chunk': 1 << 20, 'lindisp': False, 'netchunk': 1 << 20, 'perturb': True, 'raw_noise_std': 0.0,
+             'white_bkgd': False, 'augmentations': augs}
+    m = GbSimpleNeRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'synthetic'}, _model_configs())
+    assert _signature(m) == list(golden('state_dicts')['nerf_keys'])
+
+
+def test_tensorf_state_dict_matches_reference(golden):
+    pytest.importorskip('torch')
+    from simple_rf_gb300.tensorf_model import GbSimpleTensoRF
+    model = {'name': 'GbSimpleTensoRF01', 'coarse_model': _tcfg(24 ** 3),
+             'augmentations': [{'name': 'points_augmentation', 'coarse_model': _tcfg(12 ** 3)}],
+             'learn_camera_focal_length': False, 'learn_camera_rotation': False, 'learn_camera_translation': False,
+             'chunk': 1 << 16, 'lindisp': False, 'perturb': True, 'white_bkgd': False}
+    mc = dict(_model_configs(), bounding_box=np.array(TBOX))
+    m = GbSimpleTensoRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}, mc)
+    assert _signature(m) == list(golden('state_dicts')['tensorf_keys'])
