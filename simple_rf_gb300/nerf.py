@@ -312,7 +312,10 @@ class GbSimpleNeRF(torch.nn.Module):
             sigma, rgb = mlp.run(pts, view_dirs, s)
             sigma, rgb = sigma.reshape(n, s), rgb.reshape(n, s, 3)
             out = self.volume_rendering_z(sigma, rgb, z, rays_o, rays_d, ret.get('rays_d_ndc'))
-            return out, {'sigma': sigma[..., None], 'rgb': rgb}
+            # the reference MLP's output dict (SimpleNeRF17.py:696-724): sigma, the colour
+            # under its view-(in)dependent name, and the colour again as 'rgb'
+            colour = 'rgb_view_dependent' if mlp.view_dep_rgb else 'rgb_view_independent'
+            return out, {'sigma': sigma[..., None], colour: rgb, 'rgb': rgb}
 
         weights_coarse = z_coarse = None
         if self.coarse_model_needed:

@@ -497,6 +497,41 @@ def state_dict_case():
     return out
 
 
+def output_keys_case():
+    """Keys and shapes of the reference models' forward output dicts, in training
+    mode (augmented models run, raw outputs kept) and in evaluation mode, for
+    the configurations of state_dict_case on 8 pixels of one frame: the contract
+    Trainer10, Tester07 and the loss functions consume."""
+    torch.manual_seed(0)
+    augs = [{'name': 'views_augmentation', 'coarse_model': mlp_cfg(lp=4, views=False, vdr=False)},
+            {'name': 'points_augmentation', 'coarse_model': mlp_cfg(lps=3)}]
+    configs, model_configs = nerf_configs(mlp_cfg(ns=16), mlp_cfg(ns=32), ndc=True, augs=augs)
+    model_configs['intrinsics'] = np.array([[[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]]])
+    nerf = RN.SimpleNeRF(configs, model_configs)
+    bbox = [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]]
+    model = {'name': 'SimpleTensoRF09', 'coarse_model': tensorf_cfg(24 ** 3, [16, 4, 4], [48, 12, 12], bbox),
+             'augmentations': [{'name': 'points_augmentation',
+                                'coarse_model': tensorf_cfg(12 ** 3, [16, 4, 4], [48, 12, 12], bbox)}],
+             'learn_camera_focal_length': False, 'learn_camera_rotation': False, 'learn_camera_translation': False,
+             'chunk': 1 << 16, 'lindisp': False, 'perturb': True, 'white_bkgd': False}
+    tconfigs = {'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}
+    tensorf = RT.SimpleTensoRF(tconfigs, dict(model_configs, bounding_box=np.array(bbox)))
+    g = torch.Generator().manual_seed(3)
+    pix = torch.stack([torch.zeros(8, dtype=torch.long), torch.randint(0, 504, (8,), generator=g),
+                       torch.randint(0, 378, (8,), generator=g)], 1)
+    batch = {'pixel_id': pix, 'num_frames': 1, 'iter_num': 1, 'sub_batch_index': 1, 'common_data': {}}
+    out = {}
+    for tag, m in (('nerf', nerf), ('tensorf', tensorf)):
+        for mode, train in (('train', True), ('eval', False)):
+            m.train(train)
+            with torch.set_grad_enabled(train):
+                ret = m(batch, retraw=False)
+            out[f'{tag}_{mode}'] = np.array(sorted(f"{k}:{'x'.join(str(d) for d in v.shape)}"
+                                                   for k, v in ret.items() if isinstance(v, torch.Tensor)))
+    out['pixel_id'] = pix.numpy()
+    return out
+
+
 def tensorf_cp_case():
     """CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123): density and
     colour from three lines each, then the same renderer; LowRankTensor.forward on a
@@ -709,6 +744,7 @@ def main():
         'tensorf_ndc': tensorf_ndc_case,
         'tensorf_cp': tensorf_cp_case,
         'state_dicts': state_dict_case,
+        'output_keys': output_keys_case,
         'losses': losses_case,
         'reprojection': reprojection_case,
         'tv': tv_case,

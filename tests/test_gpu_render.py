@@ -68,3 +68,56 @@ def test_bf16_graph_render_equals_eager():
     for tag in a:
         for k in a[tag]:
             assert torch.equal(a[tag][k], b[tag][k]), (tag, k)
+
+
+def test_drop_in_output_dicts_match_reference_keys(golden):
+    """The drop-in models' forward output dicts carry the reference's keys with
+    the reference's shapes (golden output_keys from SimpleNeRF / SimpleTensoRF on
+    8 pixels of one frame), in training mode (augmented models, raw outputs) and
+    in evaluation mode: the contract Trainer10, Tester07 and the losses read."""
+    from simple_rf_gb300.nerf import GbSimpleNeRF
+    from simple_rf_gb300.tensorf_model import GbSimpleTensoRF
+    g = golden('output_keys')
+
+    def mlp(ns, lp=10, lv=4, views=True, vdr=True, lps=None):
+        c = {'num_samples': ns, 'points_net_depth': 8, 'views_net_depth': 1, 'points_net_width': 256,
+             'views_net_width': 128, 'points_positional_encoding_degree': lp, 'views_positional_encoding_degree': lv,
+             'use_view_dirs': views, 'view_dependent_rgb': vdr, 'predict_visibility': False}
+        if lps is not None:
+            c['points_sigma_positional_encoding_degree'] = lps
+        return c
+
+    def tcfg(vox):
+        return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [16, 4, 4],
+                'num_components_color': [48, 12, 12], 'bounding_box': [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]],
+                'num_voxels_initial': vox, 'num_voxels_final': vox, 'tensor_upsampling_iters': [],
+                'num_voxels_per_sample': 0.5, 'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4,
+                'ray_marching_weight_threshold': 1e-4, 'use_view_dirs': True, 'view_dependent_color': True,
+                'views_positional_encoding_degree': 0, 'features_positional_encoding_degree': 0,
+                'features_dimension_color': 27, 'density_offset': -10, 'distance_scale': 25,
+                'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features', 'num_units_color_predictor': 128,
+                'predict_visibility': False}
+
+    mc = {'intrinsics': np.array([[[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]]]), 'extrinsics': np.eye(4)[None],
+          'resolution': (378, 504), 'near': 1.0, 'far': 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0}
+    cams = {'learn_camera_focal_length': False, 'learn_camera_rotation': False, 'learn_camera_translation': False}
+    nerf = GbSimpleNeRF({'data_loader': {'ndc': True}, 'database': 'synthetic', 'model': dict(
+        cams, name='GbSimpleNeRF01', coarse_model=mlp(16), fine_model=mlp(32), chunk=1 << 20, lindisp=False,
+        netchunk=1 << 20, perturb=True, raw_noise_std=0.0, white_bkgd=False,
+        augmentations=[{'name': 'views_augmentation', 'coarse_model': mlp(16, lp=4, views=False, vdr=False)},
+                       {'name': 'points_augmentation', 'coarse_model': mlp(16, lps=3)}])}, mc)
+    bbox = np.array([[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]])
+    tensorf = GbSimpleTensoRF({'data_loader': {'ndc': True}, 'database': 'NeRF_LLFF', 'model': dict(
+        cams, name='GbSimpleTensoRF01', coarse_model=tcfg(24 ** 3), chunk=1 << 16, lindisp=False, perturb=True,
+        white_bkgd=False, augmentations=[{'name': 'points_augmentation', 'coarse_model': tcfg(12 ** 3)}])},
+        dict(mc, bounding_box=bbox))
+    batch = {'pixel_id': torch.from_numpy(g['pixel_id']).to(DEV), 'num_frames': 1, 'iter_num': 1,
+             'sub_batch_index': 1, 'common_data': {}}
+    for tag, m in (('nerf', nerf.to(DEV)), ('tensorf', tensorf.to(DEV))):
+        for mode, train in (('train', True), ('eval', False)):
+            m.train(train)
+            with torch.set_grad_enabled(train):
+                ret = m(batch, retraw=False)
+            got = sorted(f"{k}:{'x'.join(str(d) for d in v.shape)}" for k, v in ret.items()
+                         if isinstance(v, torch.Tensor))
+            assert got == list(g[f'{tag}_{mode}']), (tag, mode, sorted(set(got) ^ set(g[f'{tag}_{mode}'])))
