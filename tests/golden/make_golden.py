@@ -492,8 +492,13 @@ def state_dict_case():
     tmodel_configs = dict(model_configs, bounding_box=np.array(bbox))
     tensorf = RT.SimpleTensoRF(tconfigs, tmodel_configs)
     out = {}
+    opt = {'lr_initial': 5e-4, 'lr_initial_tensor': 0.02, 'lr_initial_network': 1e-3}
     for tag, m in (('nerf', nerf), ('tensorf', tensorf)):
         out[f'{tag}_keys'] = np.array([f"{k}:{'x'.join(str(d) for d in v.shape)}" for k, v in m.state_dict().items()])
+        # the optimizer's parameter groups (Trainer10.py:509-520 reads them): name, lr, parameter shapes
+        out[f'{tag}_groups'] = np.array([f"{g['name']}|{g['lr']}|" + ','.join('x'.join(str(d) for d in p.shape)
+                                                                           for p in g['params'])
+                                         for g in m.get_trainable_parameters(opt)])
     return out
 
 

@@ -1,8 +1,10 @@
-"""The drop-in models keep the reference's state_dict: the same keys in the same
-order with the same shapes as the reference's SimpleNeRF and SimpleTensoRF built
-from the same configurations (golden state_dicts.npz from the reference's own
-classes), so checkpoints written by either load into the other
-(Trainer10.py:364-394).  Built on the CPU: construction launches no kernel."""
+"""The drop-in models keep the reference's state_dict and optimizer parameter
+groups: the same keys in the same order with the same shapes, and the same
+groups (names, learning rates, parameter shapes in order), as the reference's
+SimpleNeRF and SimpleTensoRF built from the same configurations (golden
+state_dicts.npz from the reference's own classes), so checkpoints written by
+either load into the other (Trainer10.py:364-394) and the optimizer state lines
+up (Trainer10.py:509-520).  Built on the CPU: construction launches no kernel."""
 import numpy as np
 import pytest
 
@@ -38,6 +40,15 @@ def _signature(model):
     return [f"{k}:{'x'.join(str(d) for d in v.shape)}" for k, v in model.state_dict().items()]
 
 
+OPT = {'lr_initial': 5e-4, 'lr_initial_tensor': 0.02, 'lr_initial_network': 1e-3}
+
+
+def _groups(model):
+    """The optimizer's parameter groups as the trainer builds them (Trainer10.py:509-520)."""
+    return [f"{g['name']}|{g['lr']}|" + ','.join('x'.join(str(d) for d in p.shape) for p in g['params'])
+            for g in model.get_trainable_parameters(OPT)]
+
+
 def test_nerf_state_dict_matches_reference(golden):
     pytest.importorskip('torch')
     from simple_rf_gb300.nerf import GbSimpleNeRF
@@ -49,6 +60,7 @@ def test_nerf_state_dict_matches_reference(golden):
              'white_bkgd': False, 'augmentations': augs}
     m = GbSimpleNeRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'synthetic'}, _model_configs())
     assert _signature(m) == list(golden('state_dicts')['nerf_keys'])
+    assert _groups(m) == list(golden('state_dicts')['nerf_groups'])
 
 
 def test_tensorf_state_dict_matches_reference(golden):
@@ -61,3 +73,4 @@ def test_tensorf_state_dict_matches_reference(golden):
     mc = dict(_model_configs(), bounding_box=np.array(TBOX))
     m = GbSimpleTensoRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}, mc)
     assert _signature(m) == list(golden('state_dicts')['tensorf_keys'])
+    assert _groups(m) == list(golden('state_dicts')['tensorf_groups'])
