@@ -74,3 +74,30 @@ def test_tensorf_state_dict_matches_reference(golden):
     m = GbSimpleTensoRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}, mc)
     assert _signature(m) == list(golden('state_dicts')['tensorf_keys'])
     assert _groups(m) == list(golden('state_dicts')['tensorf_groups'])
+
+
+def test_tensorf_checkpoint_of_another_resolution_loads():
+    """A checkpoint written after the grid was upsampled (and an alpha mask built)
+    loads into a model constructed at the initial resolution: the load hook
+    (SimpleTensoRF09.py:946-961, 1196-1212) rebuilds the alpha mask and resizes
+    the planes and lines first, and every tensor then equals the checkpoint's."""
+    torch = pytest.importorskip('torch')
+    from simple_rf_gb300.tensorf_model import AlphaGridMask, GbSimpleTensoRF
+
+    def build(vox):
+        model = {'name': 'GbSimpleTensoRF01', 'coarse_model': _tcfg(vox), 'learn_camera_focal_length': False,
+                 'learn_camera_rotation': False, 'learn_camera_translation': False, 'chunk': 1 << 16,
+                 'lindisp': False, 'perturb': True, 'white_bkgd': False}
+        mc = dict(_model_configs(), bounding_box=np.array(TBOX))
+        return GbSimpleTensoRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}, mc)
+
+    src, dst = build(24 ** 3), build(12 ** 3)
+    vol = torch.rand(10, 12, 14, generator=torch.Generator().manual_seed(0)) < 0.3
+    src.coarse_model.alpha_mask = AlphaGridMask(vol, torch.tensor(TBOX))
+    sd = src.state_dict()
+    assert sd['coarse_model.alpha_mask.alpha_volume'].dtype == torch.bool
+    dst.load_state_dict(sd)
+    out = dst.state_dict()
+    assert list(out) == list(sd)
+    for k, v in sd.items():
+        assert out[k].shape == v.shape and torch.equal(out[k].to(v.dtype), v), k
