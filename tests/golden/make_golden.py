@@ -537,6 +537,60 @@ def output_keys_case():
     return out
 
 
+def tensorf_maintenance_case():
+    """VmDecomposedTensor's grid maintenance on a small grid: upsample_vectors_and_matrices
+    to a new resolution (SimpleTensoRF09.py:1284-1301) and shrink_tensor to an occupied
+    box (:899-914, 1303-1320, with an alpha mask of another resolution, so the box is
+    snapped to the grid) -- the planes, lines, resolution, box and sample count after each."""
+    g = torch.Generator().manual_seed(53)
+    res = torch.tensor([20, 22, 24])
+    bbox = [[-1.5, -1.5, -1.5], [1.5, 1.5, 1.5]]
+    tcfg = {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': [4, 3, 2],
+            'num_components_color': [6, 5, 4], 'bounding_box': bbox, 'num_voxels_initial': int(res.prod()),
+            'num_voxels_final': int(res.prod()), 'tensor_upsampling_iters': [], 'num_voxels_per_sample': 0.5,
+            'alpha_mask_update_iters': [], 'alpha_mask_threshold': 1e-4, 'ray_marching_weight_threshold': 1e-4,
+            'use_view_dirs': True, 'view_dependent_color': True, 'views_positional_encoding_degree': 2,
+            'features_positional_encoding_degree': 2, 'features_dimension_color': 7, 'density_offset': -10,
+            'distance_scale': 25, 'density_predictor': 'ReLU', 'color_predictor': 'MLP_Features',
+            'num_units_color_predictor': 16, 'predict_visibility': False}
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': False}, 'database': 'synthetic'}
+    tm = RT.VmDecomposedTensor('coarse_model', configs, tcfg, {'bounding_box': bbox})
+    tm.update_tensor_params(res, torch.tensor(bbox))
+    tm.matrices_density, tm.vectors_density = tm.create_decomposed_tensor([4, 3, 2], res, 0.1)
+    tm.matrices_color, tm.vectors_color = tm.create_decomposed_tensor([6, 5, 4], res, 0.1)
+    with torch.no_grad():
+        for plist in (tm.matrices_density, tm.vectors_density, tm.matrices_color, tm.vectors_color):
+            for prm in plist:
+                prm.copy_(torch.randn(prm.shape, generator=g))
+    out = {'res': res.numpy(), 'bbox': np.array(bbox, np.float32)}
+    kinds = (('planes_density', 'matrices_density'), ('lines_density', 'vectors_density'),
+             ('planes_color', 'matrices_color'), ('lines_color', 'vectors_color'))
+    for kind, attr in kinds:
+        for i in range(3):
+            out[f'{kind}.{i}'] = getattr(tm, attr)[i].detach().numpy()[0]
+    res_up = torch.tensor([30, 28, 26])
+    md, vd = tm.upsample_vectors_and_matrices(tm.matrices_density, tm.vectors_density, res_up)
+    mcl, vcl = tm.upsample_vectors_and_matrices(tm.matrices_color, tm.vectors_color, res_up)
+    out['res_up'] = res_up.numpy()
+    for kind, plist in (('planes_density', md), ('lines_density', vd), ('planes_color', mcl), ('lines_color', vcl)):
+        for i in range(3):
+            out[f'up_{kind}.{i}'] = plist[i].detach().numpy()[0]
+    vol = (torch.rand(10, 12, 14, generator=g) < 0.3).float()
+    tm.alpha_mask = RT.AlphaGridMask(vol, torch.tensor(bbox))
+    box_new = torch.tensor([[-1.0, -1.2, -0.8], [1.1, 0.9, 1.3]])
+    tm.shrink_tensor(box_new)
+    out['alpha_vol'] = vol.numpy()
+    out['box_new'] = box_new.numpy()
+    for kind, attr in kinds:
+        for i in range(3):
+            out[f'shrunk_{kind}.{i}'] = getattr(tm, attr)[i].detach().numpy()[0]
+    out['shrunk_res'] = tm.resolution.numpy()
+    out['shrunk_bbox'] = tm.bounding_box.numpy()
+    out['shrunk_num_samples'] = tm.num_samples.numpy()
+    out['shrunk_step_size'] = tm.step_size.numpy()
+    return out
+
+
 def tensorf_cp_case():
     """CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123): density and
     colour from three lines each, then the same renderer; LowRankTensor.forward on a
@@ -750,6 +804,7 @@ def main():
         'tensorf_cp': tensorf_cp_case,
         'state_dicts': state_dict_case,
         'output_keys': output_keys_case,
+        'tensorf_maintenance': tensorf_maintenance_case,
         'losses': losses_case,
         'reprojection': reprojection_case,
         'tv': tv_case,

@@ -101,3 +101,53 @@ def test_tensorf_checkpoint_of_another_resolution_loads():
     assert list(out) == list(sd)
     for k, v in sd.items():
         assert out[k].shape == v.shape and torch.equal(out[k].to(v.dtype), v), k
+
+
+def _vm_from_golden(g):
+    torch = pytest.importorskip('torch')
+    from simple_rf_gb300 import tensorf as T
+    from simple_rf_gb300.tensorf_model import GbVmTensor
+    bbox = g['bbox'].tolist()
+    tcfg = dict(_tcfg(int(np.prod(g['res']))), bounding_box=bbox, num_components_density=[4, 3, 2],
+                num_components_color=[6, 5, 4], views_positional_encoding_degree=2,
+                features_positional_encoding_degree=2, features_dimension_color=7, num_units_color_predictor=16)
+    tm = GbVmTensor('coarse_model', {'data_loader': {'ndc': False}, 'model': {'white_bkgd': False}}, tcfg,
+                    {'bounding_box': bbox})
+    tm.update_tensor_params(torch.tensor(g['res']), torch.tensor(g['bbox']))
+    with torch.no_grad():
+        for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                            ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+            for i in range(3):
+                plist[i] = torch.nn.Parameter(T.to_channels_last(torch.from_numpy(g[f'{kind}.{i}'])[None]))
+    return tm
+
+
+def _grids(tm):
+    return {f'{kind}.{i}': plist[i].detach()[0].numpy()
+            for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                                ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color))
+            for i in range(3)}
+
+
+def test_tensorf_grid_upsample_and_shrink_match_reference(golden):
+    """The drop-in's grid maintenance on the channels-last tensors against the
+    reference's VmDecomposedTensor (golden tensorf_maintenance): bilinear
+    upsampling to a new resolution (SimpleTensoRF09.py:1284-1301) within 1e-6, and
+    shrinking to an occupied box with an alpha mask of another resolution
+    (:899-914, 1303-1320) exactly, with the same resolution, box and sample count."""
+    torch = pytest.importorskip('torch')
+    from simple_rf_gb300.tensorf_model import AlphaGridMask
+    g = golden('tensorf_maintenance')
+    tm = _vm_from_golden(g)
+    tm.resample_tensor(torch.tensor(g['res_up']))
+    for k, v in _grids(tm).items():
+        np.testing.assert_allclose(v, g[f'up_{k}'], rtol=1e-6, atol=1e-6, err_msg=k)
+    tm = _vm_from_golden(g)
+    tm.alpha_mask = AlphaGridMask(torch.from_numpy(g['alpha_vol']), torch.from_numpy(g['bbox']))
+    tm.shrink_tensor(torch.from_numpy(g['box_new']))
+    for k, v in _grids(tm).items():
+        np.testing.assert_array_equal(v, g[f'shrunk_{k}'], err_msg=k)
+    np.testing.assert_array_equal(tm.resolution.numpy(), g['shrunk_res'])
+    np.testing.assert_allclose(tm.bounding_box.numpy(), g['shrunk_bbox'], rtol=1e-6)
+    assert int(tm.num_samples) == int(g['shrunk_num_samples'])
+    np.testing.assert_allclose(float(tm.step_size), float(g['shrunk_step_size']), rtol=1e-6)
