@@ -567,14 +567,43 @@ def tensorf_maintenance_case():
              ('planes_color', 'matrices_color'), ('lines_color', 'vectors_color'))
     for kind, attr in kinds:
         for i in range(3):
-            out[f'{kind}.{i}'] = getattr(tm, attr)[i].detach().numpy()[0]
+            out[f'{kind}.{i}'] = getattr(tm, attr)[i].detach().numpy()[0].copy()
     res_up = torch.tensor([30, 28, 26])
     md, vd = tm.upsample_vectors_and_matrices(tm.matrices_density, tm.vectors_density, res_up)
     mcl, vcl = tm.upsample_vectors_and_matrices(tm.matrices_color, tm.vectors_color, res_up)
     out['res_up'] = res_up.numpy()
     for kind, plist in (('planes_density', md), ('lines_density', vd), ('planes_color', mcl), ('lines_color', vcl)):
         for i in range(3):
-            out[f'up_{kind}.{i}'] = plist[i].detach().numpy()[0]
+            out[f'up_{kind}.{i}'] = plist[i].detach().numpy()[0].copy()
+    # the alpha-mask rebuild (:849-876) on a sparse density: planes shifted negative
+    with torch.no_grad():
+        dens0 = [(p.detach().clone(), l.detach().clone()) for p, l in zip(tm.matrices_density, tm.vectors_density)]
+        for prm in tm.matrices_density:
+            prm.mul_(0.3).sub_(0.25)
+        for prm in tm.vectors_density:
+            prm.mul_(0.3).add_(0.5)
+        # confined to a window of the grid (3 voxels in from each face), so the
+        # occupied box is smaller than the grid's
+        for i in range(3):
+            (a0, a1), v = tm.matrix_axes[i], tm.vector_axes[i]
+            pm, lv = tm.matrices_density[i], tm.vectors_density[i]
+            keep_p = torch.zeros_like(pm)
+            keep_p[..., 3:int(res[a1]) - 4, 3:int(res[a0]) - 4] = 1
+            keep_l = torch.zeros_like(lv)
+            keep_l[..., 3:int(res[v]) - 4, :] = 1
+            pm.mul_(keep_p)
+            lv.mul_(keep_l)
+    for i in range(3):
+        out[f'amask_planes_density.{i}'] = tm.matrices_density[i].detach().numpy()[0].copy()
+        out[f'amask_lines_density.{i}'] = tm.vectors_density[i].detach().numpy()[0].copy()
+    box_alpha = tm.update_alpha_mask(0)
+    out['amask_volume'] = tm.alpha_mask.alpha_volume.detach().numpy().reshape(tm.alpha_mask.alpha_volume.shape[-3:])
+    out['amask_box'] = box_alpha.numpy()
+    out['amask_step_size'] = tm.step_size.numpy()
+    with torch.no_grad():
+        for (p0, l0), pm, lv in zip(dens0, tm.matrices_density, tm.vectors_density):
+            pm.copy_(p0)
+            lv.copy_(l0)
     vol = (torch.rand(10, 12, 14, generator=g) < 0.3).float()
     tm.alpha_mask = RT.AlphaGridMask(vol, torch.tensor(bbox))
     box_new = torch.tensor([[-1.0, -1.2, -0.8], [1.1, 0.9, 1.3]])
@@ -583,7 +612,7 @@ def tensorf_maintenance_case():
     out['box_new'] = box_new.numpy()
     for kind, attr in kinds:
         for i in range(3):
-            out[f'shrunk_{kind}.{i}'] = getattr(tm, attr)[i].detach().numpy()[0]
+            out[f'shrunk_{kind}.{i}'] = getattr(tm, attr)[i].detach().numpy()[0].copy()
     out['shrunk_res'] = tm.resolution.numpy()
     out['shrunk_bbox'] = tm.bounding_box.numpy()
     out['shrunk_num_samples'] = tm.num_samples.numpy()

@@ -267,3 +267,39 @@ def test_graph_step_redoes_a_step_that_overflowed():
         for (p, _), x, y in zip(ea.params, _grads(ea), _grads(gb)):
             assert _rel(y, x) < 1e-4, (i, tuple(p.shape), _rel(y, x))
     assert gb.recaptures >= 1 and int(gb.flags_host[0]) == 0 and int(gb.step_dev.item()) == 2
+
+
+def test_alpha_mask_rebuild_matches_reference(golden):
+    """LowRankTensor.update_alpha_mask (SimpleTensoRF09.py:849-876) on the drop-in:
+    dense alpha of the density over the grid (the VM density kernel), 3^3 max-pool,
+    threshold, and the occupied box, against the reference's (golden
+    tensorf_maintenance: a density confined to a window of a 20 x 22 x 24 grid).
+    A voxel whose pooled alpha sits on the 1e-4 threshold may switch sides between
+    float32 evaluations: at most 0.1% of the volume may differ, and the box by at
+    most one voxel."""
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300 import tensorf as T
+    from simple_rf_gb300.tensorf_model import GbVmTensor
+    g = golden('tensorf_maintenance')
+    bbox = g['bbox'].tolist()
+    tcfg = dict(_tcfg(), bounding_box=bbox, num_voxels_initial=int(np.prod(g['res'])),
+                num_voxels_final=int(np.prod(g['res'])), num_components_density=[4, 3, 2],
+                num_components_color=[6, 5, 4])
+    tm = GbVmTensor('coarse_model', {'data_loader': {'ndc': False}, 'model': {'white_bkgd': False}}, tcfg,
+                    {'bounding_box': bbox})
+    tm.update_tensor_params(torch.tensor(g['res']), torch.tensor(g['bbox']))
+    with torch.no_grad():
+        for kind, plist in (('amask_planes_density', tm.matrices_density), ('amask_lines_density', tm.vectors_density),
+                            ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+            for i in range(3):
+                plist[i] = torch.nn.Parameter(T.to_channels_last(torch.from_numpy(g[f'{kind}.{i}'])[None]))
+    tm = tm.to(DEV)
+    np.testing.assert_allclose(float(tm.step_size), float(g['amask_step_size']), rtol=1e-6)
+    box = tm.update_alpha_mask(0).cpu().numpy()
+    vol = tm.alpha_mask.volume().cpu().numpy()
+    ref = g['amask_volume']
+    assert vol.shape == ref.shape
+    assert np.mean(vol != ref) <= 1e-3, np.mean(vol != ref)
+    voxel = (g['bbox'][1] - g['bbox'][0]) / (g['res'] - 1)
+    assert np.all(np.abs(box - g['amask_box']) <= voxel * 1.0001), (box, g['amask_box'])

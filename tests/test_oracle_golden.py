@@ -266,3 +266,27 @@ def test_alpha_mask_query(golden):
     g = golden('tensorf')
     pos = ot.grid_sample_3d_positive(g['alpha_vol'], ot.normalize_points(g['alpha_q'], g['bbox']))
     assert np.array_equal(pos, g['alpha_q_pos'])
+
+
+def test_alpha_mask_rebuild(golden):
+    """LowRankTensor.update_alpha_mask (SimpleTensoRF09.py:849-876) restated on the
+    oracle's VM density: alpha = 1 - exp(-relu(density) step) on the grid nodes,
+    3^3 max-pool, threshold 1e-4, against the reference's volume (golden
+    tensorf_maintenance)."""
+    import torch
+    g = golden('tensorf_maintenance')
+    res, bbox = g['res'], g['bbox']
+    t = [np.linspace(0, 1, r, dtype=np.float32) for r in res]
+    s = np.stack(np.meshgrid(*t, indexing='ij'), -1)
+    xyz = bbox[0] * (1 - s) + bbox[1] * s
+    pn = ((xyz - bbox[0]) / (bbox[1] - bbox[0]) * 2 - 1).reshape(-1, 3).astype(np.float32)
+    planes = [g[f'amask_planes_density.{i}'] for i in range(3)]
+    lines = [g[f'amask_lines_density.{i}'] for i in range(3)]
+    alpha = 1 - np.exp(-np.maximum(ot.vm_density(planes, lines, pn), 0) * g['amask_step_size'])
+    a = torch.from_numpy(alpha.reshape(tuple(res))).transpose(0, 2).contiguous()[None, None]
+    a = torch.nn.functional.max_pool3d(a, 3, 1, 1).view(tuple(res[::-1]))
+    vol = (a >= 1e-4).float().numpy()
+    assert np.array_equal(vol, g['amask_volume'])
+    occ = np.argwhere(vol > 0.5)[:, ::-1]   # (x, y, z) node indices of the occupied voxels
+    box = bbox[0] + (bbox[1] - bbox[0]) * np.stack([occ.min(0), occ.max(0)]) / (res - 1)
+    np.testing.assert_allclose(box, g['amask_box'], rtol=1e-6, atol=1e-6)
