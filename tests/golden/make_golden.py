@@ -491,9 +491,13 @@ def state_dict_case():
     tconfigs = {'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}
     tmodel_configs = dict(model_configs, bounding_box=np.array(bbox))
     tensorf = RT.SimpleTensoRF(tconfigs, tmodel_configs)
+    cp_cfg = dict(tensorf_cfg(24 ** 3, [16], [48], bbox), decomposition_type='CandecompParafac')
+    cp_model = dict(model, coarse_model=cp_cfg)
+    del cp_model['augmentations']
+    tensorf_cp = RT.SimpleTensoRF(dict(tconfigs, model=cp_model), dict(model_configs, bounding_box=np.array(bbox)))
     out = {}
     opt = {'lr_initial': 5e-4, 'lr_initial_tensor': 0.02, 'lr_initial_network': 1e-3}
-    for tag, m in (('nerf', nerf), ('tensorf', tensorf)):
+    for tag, m in (('nerf', nerf), ('tensorf', tensorf), ('tensorf_cp', tensorf_cp)):
         out[f'{tag}_keys'] = np.array([f"{k}:{'x'.join(str(d) for d in v.shape)}" for k, v in m.state_dict().items()])
         # the optimizer's parameter groups (Trainer10.py:509-520 reads them): name, lr, parameter shapes
         out[f'{tag}_groups'] = np.array([f"{g['name']}|{g['lr']}|" + ','.join('x'.join(str(d) for d in p.shape)

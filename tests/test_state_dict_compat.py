@@ -151,3 +151,20 @@ def test_tensorf_grid_upsample_and_shrink_match_reference(golden):
     np.testing.assert_allclose(tm.bounding_box.numpy(), g['shrunk_bbox'], rtol=1e-6)
     assert int(tm.num_samples) == int(g['shrunk_num_samples'])
     np.testing.assert_allclose(float(tm.step_size), float(g['shrunk_step_size']), rtol=1e-6)
+
+
+def test_tensorf_cp_state_dict_matches_reference(golden):
+    """The CP decomposition (CpDecomposedTensor, SimpleTensoRF09.py:964-1123) as
+    the drop-in builds it through the same factory: state_dict and parameter groups."""
+    pytest.importorskip('torch')
+    from simple_rf_gb300.tensorf_model import GbCpTensor, GbSimpleTensoRF
+    cp = dict(_tcfg(24 ** 3), decomposition_type='CandecompParafac', num_components_density=[16],
+              num_components_color=[48])
+    model = {'name': 'GbSimpleTensoRF01', 'coarse_model': cp, 'learn_camera_focal_length': False,
+             'learn_camera_rotation': False, 'learn_camera_translation': False, 'chunk': 1 << 16,
+             'lindisp': False, 'perturb': True, 'white_bkgd': False}
+    mc = dict(_model_configs(), bounding_box=np.array(TBOX))
+    m = GbSimpleTensoRF({'data_loader': {'ndc': True}, 'model': model, 'database': 'NeRF_LLFF'}, mc)
+    assert isinstance(m.coarse_model, GbCpTensor)
+    assert _signature(m) == list(golden('state_dicts')['tensorf_cp_keys'])
+    assert _groups(m) == list(golden('state_dicts')['tensorf_cp_groups'])
