@@ -818,6 +818,35 @@ def tv_case():
     return out
 
 
+def camera_learners_case():
+    """Learnt camera poses (ExtrinsicsLearner, SimpleNeRF17.py:817-912) and
+    intrinsics (IntrinsicsLearner, SimpleNeRF17.py:788-814): seeded axis-angle
+    and translation deltas on 5 frames, the composed extrinsics for 7 frame ids
+    (repeats included), and the gradients of a fixed weighted sum of them with
+    respect to the deltas."""
+    g = np.random.default_rng(21)
+    n = 5
+    init = np.tile(np.eye(4), (n, 1, 1))
+    init[:, :3, :3] = np.linalg.qr(g.standard_normal((n, 3, 3)))[0]
+    init[:, :3, 3] = g.standard_normal((n, 3))
+    intr = np.tile(np.array([[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]]), (n, 1, 1))
+    r = (g.standard_normal((n, 3)) * 0.3).astype(np.float32)
+    r[2] = 0.0   # the zero rotation (the 1e-15 guard of the angle)
+    t = (g.standard_normal((n, 3)) * 0.2).astype(np.float32)
+    ids = np.array([0, 2, 4, 1, 2, 3, 0])
+    wsum = g.standard_normal((len(ids), 4, 4)).astype(np.float32)
+    el = RN.ExtrinsicsLearner(init, learn_rotation=True, learn_translation=True)
+    with torch.no_grad():
+        el.r.copy_(torch.from_numpy(r))
+        el.t.copy_(torch.from_numpy(t))
+    ext = el(torch.from_numpy(ids))
+    (ext * torch.from_numpy(wsum)).sum().backward()
+    il = RN.IntrinsicsLearner(intr, learn_focal=False)
+    return {'init_extrinsics': init, 'init_intrinsics': intr, 'r': r, 't': t, 'ids': ids, 'wsum': wsum,
+            'extrinsics': ext.detach().numpy(), 'grad_r': el.r.grad.numpy(), 'grad_t': el.t.grad.numpy(),
+            'intrinsics': il(torch.from_numpy(ids)).numpy()}
+
+
 def main():
     cases = {
         'nerf_sampling': sampling_case,
@@ -841,6 +870,7 @@ def main():
         'losses': losses_case,
         'reprojection': reprojection_case,
         'tv': tv_case,
+        'camera_learners': camera_learners_case,
     }
     only = sys.argv[1:]
     for name, fn in cases.items():
