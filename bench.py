@@ -9,14 +9,19 @@ o ~ N(0, 0.1^2), d = normalize(N(0, I)), targets ~ U[0,1]^3, depth ~ U[2,6].
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value`  : train rays/s of the BF16 tcgen05 step, inputs resident in HBM,
-           whole step replayed as one CUDA graph, timed with CUDA events.
+`value`  : train rays/s of the 16-bit tcgen05 step (FP16 operands, FP32
+           accumulation, FP32 master weights, dynamic loss scale: the operand
+           type that meets both accuracy bars of the metric; the BF16-operand
+           step, 1% faster but 2-2.5% gradient error, is reported beside it),
+           inputs resident in HBM, whole step replayed as one CUDA graph,
+           timed with CUDA events.
 `e2e`    : the same through the public train-step API with host (pinned)
            inputs copied H2D and the loss read back D2H every step.
 `fp32_plain`: the FP32 SIMT path on the same workload (the headline ratio's
            denominator), fewer steps.
 `--impl reference`: the reference algorithm's CPU restatement (the numpy
-           oracle port of SimpleNeRF17) timed on the host cores.
+           oracle port of SimpleNeRF17) timed on the host cores, whole
+           4096-ray steps.
 With N > 1 (torchrun) every rank trains its own replica (no collective on the
 data path; rays are independent) and `value` sums the ranks.
 """
@@ -34,6 +39,7 @@ sys.path.insert(0, REPO)
 
 METRIC = 'train rays/s fwd+bwd, BF16 fused vs FP32 plain on 1 GB300 at <=2e-3 RGB error'
 N_RAYS, N_COARSE, N_FINE = 4096, 64, 128
+HEADLINE = 'fp16'
 MACS_PER_SAMPLE = 593408
 
 
@@ -195,6 +201,56 @@ def roofline_gemm(dev, hbm_peak, peak_tflops, peak_kind, reps=50):
             'tensor_frac_of_bf16_burst': round(flops / t / 1e12 / peak_tflops, 4)}
 
 
+def roofline_wgrad(dev, hbm_peak, peak_tflops, peak_kind, reps=50):
+    """The step's dominant kernel (tc_wgrad_kernel: the weight and bias gradient of
+    one 256 x 256 trunk layer over the fine net's 786,432 samples, split over
+    sample ranges into per-split partials) timed alone.  Algorithmic bytes: dZ and
+    X read once (2 B per element) and the FP32 gradient written once."""
+    import ctypes
+    import torch
+    from simple_rf_gb300 import _lib
+    m, k, n = N_RAYS * (N_COARSE + N_FINE), 256, 256
+    lib = _lib.load()
+    dz = (torch.randn(m, n, device=dev) * 0.01).to(torch.bfloat16)
+    x = torch.randn(m, k, device=dev).clamp_min(0).to(torch.bfloat16)
+    ws = int(lib.srf_bf16_wgrad_workspace_size(n, k))
+    part = torch.empty(ws // 4 + 1, device=dev)
+    splits = ctypes.c_int(0)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def launch():
+        _lib.call('srf_bf16_wgrad', p(part), ws, ctypes.byref(splits), p(dz), n, n, p(x), k, k, None, 0, 0, m, st)
+
+    for _ in range(3):
+        launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        launch()
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0 / reps
+    nbytes = (m * n + m * k) * 2 + n * k * 4
+    flops = 2.0 * m * n * k
+    traffic = None
+    tpath = os.path.join(REPO, 'profiles', 'traffic.json')
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get('tc_wgrad_kernel_256_bytes_per_launch')
+        except Exception:
+            traffic = None
+    gbs = nbytes / t / 1e9
+    return {'kernel': f'tc_wgrad_kernel (dW of a 256x256 layer over M={m}, {splits.value} sample splits)',
+            'bound': 'hbm', 'achieved': round(gbs, 1), 'peak': hbm_peak, 'unit': 'GB/s', 'frac': round(gbs / hbm_peak, 4),
+            'peak_source': peak_kind + ' copy bandwidth', 'traffic': traffic, 'launch_ms': round(t * 1e3, 4),
+            'algorithmic_bytes_per_launch': int(nbytes), 'tflops': round(flops / t / 1e12, 1),
+            'tensor_frac_of_bf16_burst': round(flops / t / 1e12 / peak_tflops, 4),
+            'share_of_step': 'largest kernel of the training step (launch list under profiles/)'}
+
+
 def kernel_rooflines(hbm_peak, peak_kind):
     """The memory-bound kernels of the path timed alone (CUDA events, 20 launches
     after 3 warm-up launches) with their algorithmic bytes per launch:
@@ -224,8 +280,24 @@ def kernel_rooflines(hbm_peak, peak_kind):
     return out
 
 
+def fp32_plain_block(ws, k32, t_fp):
+    """The FP32 SIMT step with its arithmetic rate: 6 x 593,408 MAC-FLOP per sample
+    over 64 + 64 + 128 samples per ray, against the FP32 FMA peak of the SMs the
+    GEMM fills (152 SMs x 128 FP32 lanes x 2 FLOP x the maximum SM clock)."""
+    rate = job_rays_per_s(ws, N_RAYS, k32, t_fp)
+    tflops = rate * 6 * MACS_PER_SAMPLE * (N_COARSE + N_COARSE + N_FINE) / 1e12 / ws
+    try:
+        with open(os.path.join(REPO, 'MEASURED_PEAKS.json')) as f:
+            mhz = float(json.load(f)['sm_max_mhz'])
+    except Exception:
+        mhz = 2070.0
+    peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+    return {'value': round(rate, 1), 'unit': 'rays/s', 'ms_per_step': round(1e3 * t_fp / k32, 3), 'steps': k32,
+            'tflops': round(tflops, 1), 'fp32_simt_peak_tflops': round(peak, 1), 'frac_of_fp32_peak': round(tflops / peak, 3)}
+
+
 def rgb_agreement(step_cls, batch, dev):
-    """Coarse-pass rgb of the BF16 step against the FP32 plain step from the same
+    """Coarse-pass rgb of the headline (FP16) and the BF16 step against the FP32 plain step from the same
     weights and batch (the fine pass samples different depths once the coarse
     weights differ, so only the coarse pass compares sample by sample).
 
@@ -238,7 +310,7 @@ def rgb_agreement(step_cls, batch, dev):
     out = {}
     for label, bias in (('', None), ('_sigma_bias_0.5', 0.5)):
         runs = {}
-        for prec in ('bf16', 'fp32'):
+        for prec in ('fp16', 'bf16', 'fp32'):
             s = step_cls(N_RAYS, N_COARSE, N_FINE, precision=prec, device=dev, seed=7)
             if bias is not None:
                 for net in s.nets.values():
@@ -248,12 +320,18 @@ def rgb_agreement(step_cls, batch, dev):
             torch.cuda.synchronize(dev)
             runs[prec] = (s.buf['coarse']['rgb_map'].clone(), s.buf['coarse']['sigma'].view(N_RAYS, N_COARSE)[:, -1] > 0)
             del s
-        (rb, lb), (rf, lf) = runs['bf16'], runs['fp32']
-        err = (rb - rf).abs().max(1).values
-        flip = lb != lf
-        ok = err[~flip]
-        out[f'rgb_max_abs_bf16_vs_fp32{label}'] = round(float(ok.max().item()) if ok.numel() else 0.0, 6)
-        out[f'rays_with_last_sample_flip{label}'] = int(flip.sum().item())
+        rf, lf = runs['fp32']
+        for prec in ('fp16', 'bf16'):
+            rb, lb = runs[prec]
+            err = (rb - rf).abs().max(1).values
+            flip = lb != lf
+            ok = err[~flip]
+            out[f'rgb_max_abs_{prec}_vs_fp32{label}'] = round(float(ok.max().item()) if ok.numel() else 0.0, 6)
+            out[f'rays_with_last_sample_flip_{prec}{label}'] = int(flip.sum().item())
+    out['rays'] = N_RAYS
+    out['against_fp64_oracle'] = ('tests/test_gpu_headline_accuracy.py: the headline step at 4096 rays against the '
+                                  'float64 oracle (rgb max-abs over all rays, flip count, gradient rel-L2)')
+    torch.cuda.empty_cache()
     return out
 
 
@@ -331,62 +409,111 @@ def time_render(dev, stream):
     return out
 
 
+class OracleStep:
+    """One training step of the reference algorithm's CPU restatement (numpy
+    oracle port of SimpleNeRF17's render_rays + the loss + the hand-derived
+    backward + a parameter update) on ``n`` config-2 rays."""
+
+    def __init__(self, n, seed=0):
+        import numpy as np
+        from oracle import nerf as on
+        self.on, self.np = on, np
+        self.spec = on.MlpSpec()
+        self.p = {'coarse': on.xavier_params(self.spec, 0), 'fine': on.xavier_params(self.spec, 1)}
+        self.rng = np.random.default_rng(seed)
+        rng = self.rng
+        self.n = n
+        self.o = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
+        d = rng.standard_normal((n, 3)).astype(np.float32)
+        self.d = d / np.linalg.norm(d, axis=1, keepdims=True)
+        self.t_rgb = rng.random((n, 3), dtype=np.float32)
+        self.t_d = (rng.random(n, dtype=np.float32) * 4 + 2).astype(np.float32)
+        self.mask = np.zeros(n, np.float32)
+        self.mask[:n // 4] = 1
+
+    def __call__(self, chunk=128):
+        """Rays in chunks (as the reference's batchify_rays does): each chunk's
+        forward, its share of the whole-batch loss gradient, its backward; the
+        parameter gradients add up to those of the whole batch."""
+        on, np, n = self.on, self.np, self.n
+        u_c = self.rng.random((n, N_COARSE), dtype=np.float32)
+        u_f = self.rng.random((n, N_FINE), dtype=np.float32)
+        nd = float(self.mask.sum())
+        total = None
+        for i in range(0, n, chunk):
+            sl = slice(i, min(i + chunk, n))
+            m = sl.stop - sl.start
+            ret, caches = on.render_rays(self.p['coarse'], self.p['fine'], self.spec, self.spec, self.o[sl], self.d[sl],
+                                         2.0, 6.0, N_COARSE, N_FINE, u_c[sl], u_f[sl], white_bkgd=True)
+            _, grads = on.train_loss(ret, self.t_rgb[sl], self.t_d[sl], self.mask[sl])
+            nd_chunk = float(self.mask[sl].sum())
+            for k in grads:
+                # train_loss normalised by this chunk's counts; rescale to the whole batch's
+                grads[k] *= np.float32(m / n) if k.startswith('rgb') else np.float32(nd_chunk / nd if nd else 0.0)
+            g = on.backward_render(self.p, {'coarse': self.spec, 'fine': self.spec}, caches, grads, m)
+            if total is None:
+                total = g
+            else:
+                for net in g:
+                    for k in g[net]:
+                        total[net][k] += g[net][k]
+        for net, p in self.p.items():
+            for k in p:
+                p[k] -= np.float32(5e-4) * np.sign(total[net][k])
+
+
 def cpu_baseline(sample_rays=128, min_seconds=10.0):
     """The oracle port of the reference step on the host cores (bounded sample)."""
-    import numpy as np
-    from oracle import nerf as on
-    spec = on.MlpSpec()
-    pc, pf = on.xavier_params(spec, 0), on.xavier_params(spec, 1)
-    rng = np.random.default_rng(0)
-    n = sample_rays
-    o = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
-    d = rng.standard_normal((n, 3)).astype(np.float32)
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    t_rgb = rng.random((n, 3), dtype=np.float32)
-    t_d = (rng.random(n, dtype=np.float32) * 4 + 2).astype(np.float32)
-    mask = np.zeros(n, np.float32)
-    mask[:n // 4] = 1
+    step = OracleStep(sample_rays)
     steps, t0 = 0, time.perf_counter()
     while True:
-        u_c = rng.random((n, N_COARSE), dtype=np.float32)
-        u_f = rng.random((n, N_FINE), dtype=np.float32)
-        ret, caches = on.render_rays(pc, pf, spec, spec, o, d, 2.0, 6.0, N_COARSE, N_FINE, u_c, u_f, white_bkgd=True)
-        _, grads = on.train_loss(ret, t_rgb, t_d, mask)
-        g = on.backward_render({'coarse': pc, 'fine': pf}, {'coarse': spec, 'fine': spec}, caches, grads, n)
-        for net, p in (('coarse', pc), ('fine', pf)):
-            for k in p:
-                p[k] -= np.float32(5e-4) * np.sign(g[net][k])
+        step()
         steps += 1
         el = time.perf_counter() - t0
         if el >= min_seconds or steps >= 50:
             break
-    return {'value': round(n * steps / el, 2), 'unit': 'rays/s', 'cores': os.cpu_count(), 'kind': 'port',
-            'sample': f'{steps} oracle train steps of {n} rays (64+128 samples, 8x256 coarse+fine MLPs, '
+    return {'value': round(sample_rays * steps / el, 2), 'unit': 'rays/s', 'cores': os.cpu_count(), 'kind': 'port',
+            'sample': f'{steps} oracle train steps of {sample_rays} rays (64+128 samples, 8x256 coarse+fine MLPs, '
                       f'numpy float32, BLAS threads = host cores) in {el:.1f} s'}
 
 
 def run_reference(args):
+    """The reference arm: whole config-2 steps (4096 rays) of the oracle port on the
+    host cores; warm-up steps run 64 rays (they only bring up the BLAS threads)."""
     ws = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return 0
-    total_t, total_rays = 0.0, 0
-    for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(sample_rays=64, min_seconds=0.0)
-        if i >= args.warmup:
-            total_rays += 64
-            total_t += 64 / cb['value']
-    v = total_rays / total_t
+    warm = OracleStep(64)
+    for _ in range(args.warmup):
+        warm()
+    step = OracleStep(N_RAYS)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    total_t = time.perf_counter() - t0
+    v = N_RAYS * args.steps / total_t
+    sample = (f'{args.steps} whole steps of {N_RAYS} rays of the training step (numpy oracle port of SimpleNeRF17 '
+              f'render_rays + loss + hand-derived backward + update, float32, BLAS threads = host cores)')
     line = {'impl': 'reference', 'metric': METRIC, 'value': round(v, 2), 'unit': 'rays/s', 'n_gpus': ws,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(1e3 * total_t / args.steps, 2),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': 'nerf_train_step_4096rays_64+128samples_8x256', 'sample_rays_per_step': 64},
+            'config': config_block(ws),
             'cpu_baseline': {'value': round(v, 2), 'unit': 'rays/s', 'cores': os.cpu_count(), 'kind': 'port',
-                             'sample': f'{args.steps} steps of 64 rays of the config-2 step (numpy oracle port of '
-                                       'SimpleNeRF17 forward + hand-derived backward)'},
+                             'sample': sample},
             'e2e': {'value': round(v, 2), 'unit': 'rays/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def config_block(ws):
+    """The workload both arms run (one step = one training step on N_RAYS rays per rank)."""
+    return {'workload': 'nerf_train_step_4096rays_64+128samples_8x256', 'rays_per_step_per_gpu': N_RAYS,
+            'samples': '64 stratified + 128 inverse-CDF (fine net evaluates 192)',
+            'mlp': '8x256 ReLU, skip at layer 5, sigma head, 256->128 view layer, sigmoid rgb; coarse+fine',
+            'loss': 'rgb MSE (coarse+fine) + 0.1 L1 depth on 25% of rays; Adam',
+            'parallelism': f'replicas x{ws}' if ws > 1 else 'single GPU',
+            'l2': 'per-step working set ~5 GB of activations >> 129 MB L2 (no flush needed)'}
 
 
 def run_ours(args):
@@ -410,8 +537,8 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    # ---- BF16 tcgen05 step (headline) ----
-    bf = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision='bf16', device=dev)
+    # ---- 16-bit tcgen05 step (headline) ----
+    bf = NerfTrainStep(N_RAYS, N_COARSE, N_FINE, precision=HEADLINE, device=dev)
     bf.set_batch(*pool[0])
     bf.capture(warmup=2)
 
@@ -426,8 +553,9 @@ def run_ours(args):
     with ClockSampler(local) as clocks:
         t_bf = time_steps(bf_step, args.steps, stream)
         # the dominant kernel timed alone right after the step, under the same clock record
-        roof = roofline_gemm(dev, hbm_peak, tf_peak, peak_kind) if rank == 0 else None
-        kroofs = kernel_rooflines(hbm_peak, peak_kind) if rank == 0 else None
+        roof = roofline_wgrad(dev, hbm_peak, tf_peak, peak_kind) if rank == 0 else None
+        kroofs = [roofline_gemm(dev, hbm_peak, tf_peak, peak_kind)] + kernel_rooflines(hbm_peak, peak_kind) \
+            if rank == 0 else None
     barrier()
     t_bf = max_over_ranks(t_bf, dev)
     # rgb agreement of the BF16 step with the FP32 plain step (same weights, same batch)
@@ -461,10 +589,10 @@ def run_ours(args):
     barrier()
 
     acc = rgb_agreement(NerfTrainStep, pool[1], dev)
-    # FP16-operand mode (meets the 1e-2 gradient bar) and the main + augmented NDC pair
+    # BF16-operand mode (misses the 1e-2 gradient bar) and the main + augmented NDC pair
     variants = {}
     if rank == 0:
-        variants['nerf_fp16'] = time_variant('nerf', 'fp16', args.steps, dev, stream)
+        variants['nerf_bf16'] = time_variant('nerf', 'bf16', args.steps, dev, stream)
         for prec, k in (('bf16', args.steps), ('fp16', args.steps), ('fp32', k32)):
             variants[f'nerf_pair_{prec}'] = time_variant('nerf_pair', prec, k, dev, stream)
         # the same warm-up and timed steps for both (surface-sample counts drift as the grids train)
@@ -488,24 +616,19 @@ def run_ours(args):
     line = {
         'metric': METRIC, 'value': round(value, 1), 'unit': 'rays/s', 'n_gpus': ws, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': round(1e3 * t_bf / args.steps, 4), 'higher_is_better': True,
-        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'bf16', 'data': 'synthetic',
-        'config': {'workload': 'nerf_train_step_4096rays_64+128samples_8x256', 'rays_per_step_per_gpu': N_RAYS,
-                   'samples': '64 stratified + 128 inverse-CDF (fine net evaluates 192)',
-                   'mlp': '8x256 ReLU, skip at layer 5, sigma head, 256->128 view layer, sigmoid rgb; coarse+fine',
-                   'loss': 'rgb MSE (coarse+fine) + 0.1 L1 depth on 25% of rays; Adam',
-                   'parallelism': f'replicas x{ws}' if ws > 1 else 'single GPU',
-                   'l2': 'per-step working set ~5 GB of activations >> 129 MB L2 (no flush needed)',
-                   'cuda_graph': True},
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': HEADLINE, 'data': 'synthetic',
+        'config': dict(config_block(ws), cuda_graph=True,
+                       operands='FP16 operands, FP32 accumulation in tensor memory, FP32 master weights, FP32 PE and '
+                                'compositing, dynamic loss scale (BF16 operands reported under "bf16")'),
         'samples_per_s': round(value * (N_COARSE + N_COARSE + N_FINE), 1),
         'tflops_model': round(value * 6 * MACS_PER_SAMPLE * (N_COARSE + N_COARSE + N_FINE) / 1e12, 1),
-        'fp32_plain': {'value': round(job_rays_per_s(ws, N_RAYS, k32, t_fp), 1), 'unit': 'rays/s',
-                       'ms_per_step': round(1e3 * t_fp / k32, 3), 'steps': k32},
-        'speedup_bf16_vs_fp32_plain': round((N_RAYS * args.steps / t_bf) / (N_RAYS * k32 / t_fp), 2),
+        'fp32_plain': fp32_plain_block(ws, k32, t_fp),
+        'speedup_vs_fp32_plain': round((N_RAYS * args.steps / t_bf) / (N_RAYS * k32 / t_fp), 2),
         'accuracy': acc,
-        'fp16': dict(variants['nerf_fp16'], speedup_vs_fp32_plain=round(
-            variants['nerf_fp16']['rays_per_s'] / (N_RAYS * k32 / t_fp), 2),
-            note='FP16 operands + dynamic loss scale; whole-gradient rel-L2 vs the FP64 oracle < 1e-2 '
-                 '(tests/test_gpu_train_step.py), BF16 operands give 2-2.5%'),
+        'bf16': dict(variants['nerf_bf16'], speedup_vs_fp32_plain=round(
+            variants['nerf_bf16']['rays_per_s'] / (N_RAYS * k32 / t_fp), 2),
+            note='BF16 operands: rgb within 2e-3 of the FP64 oracle, whole-gradient rel-L2 2-2.5% (above the 1e-2 '
+                 'bar; FP16 keeps 3 more mantissa bits at the same bytes and tensor rate)'),
         'nerf_pair': {'workload': 'NDC main coarse+fine + augmented coarse (PE L=4, no view dirs), 4096 rays, '
                                   '64+128 samples, 0.1 depth-consistency term',
                       'bf16': variants['nerf_pair_bf16'], 'fp16': variants['nerf_pair_fp16'],

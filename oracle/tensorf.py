@@ -52,7 +52,8 @@ def grid_sample_2d_backward(shape, gx, gy, grad, dtype):
     for yi, xi, wt in _bilinear_taps(gx, gy, h, w):
         flat = yi * w + xi
         for ch in range(c):
-            np.add.at(gimg[ch], flat, (grad[ch] * wt).astype(np.float64))
+            # a float64 histogram of the tap contributions (np.add.at semantics, faster)
+            gimg[ch] += np.bincount(flat, weights=(grad[ch] * wt).astype(np.float64), minlength=h * w)
     return gimg.reshape(c, h, w).astype(dtype)
 
 
@@ -327,3 +328,30 @@ def tensorf_backward(tp, spec, cache, g):
         grads[f'planes_density.{i}'] = grid_sample_2d_backward(tp['planes_density'][i].shape, pv[:, m0], pv[:, m1], dfeat[None, :] * lc, dt)
         grads[f'lines_density.{i}'] = grid_sample_2d_backward(tp['lines_density'][i].shape, np.zeros_like(pv[:, v]), pv[:, v], dfeat[None, :] * pc, dt)
     return grads
+
+
+def seeded_vm_model(seed, res, n_density, n_color, features, units, views_pe=2, features_pe=2, scale=0.1):
+    """Parameters of a VM model from a numpy PCG64 seed (fixtures regenerate them
+    instead of storing them): planes (R, res[m1], res[m0]) and lines (R, res[v], 1)
+    ~ N(0, scale^2) as VmDecomposedTensor.create_decomposed_tensor draws them
+    (SimpleTensoRF09.py:1154-1165), the basis and renderer layers uniform in
+    +-1/sqrt(fan_in) as torch.nn.Linear's default, the last bias zero (:1393)."""
+    rng = np.random.default_rng(seed)
+    tp = {}
+    for kind, comps in (('density', n_density), ('color', n_color)):
+        tp[f'planes_{kind}'], tp[f'lines_{kind}'] = [], []
+        for i in range(3):
+            m0, m1 = MATRIX_AXES[i]
+            v = VECTOR_AXES[i]
+            tp[f'planes_{kind}'].append(rng.standard_normal((comps[i], res[m1], res[m0]), dtype=np.float32) *
+                                        np.float32(scale))
+            tp[f'lines_{kind}'].append(rng.standard_normal((comps[i], res[v], 1), dtype=np.float32) * np.float32(scale))
+    spec = RendererSpec(features_dim=features, features_pe=features_pe, views_pe=views_pe, units=units)
+    shapes = spec.param_shapes(sum(n_color))
+    for name, shape in shapes.items():
+        # a bias takes the fan-in of its layer's weight
+        fan_in = shapes[name.replace('.bias', '.weight')][1]
+        b = 1.0 / np.sqrt(fan_in)
+        tp[name] = rng.uniform(-b, b, shape).astype(np.float32)
+    tp['color_predictor.mlp.4.bias'][:] = 0
+    return tp, spec

@@ -367,7 +367,7 @@ class NerfTrainStep:
     def outputs(self):
         out = {}
         for net in self.run:
-            for k in ('rgb_map', 'acc', 'depth', 'depth_var', 'weights') + (('depth_ndc',) if self.ndc else ()):
+            for k in ('rgb_map', 'acc', 'depth', 'depth_var', 'weights', 'sigma') + (('depth_ndc',) if self.ndc else ()):
                 out[f'{k}_{net.name}'] = net.b[k]
             out[f'z_{net.name}'] = self.level[net.level]['z']
         return out

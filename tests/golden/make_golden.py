@@ -461,6 +461,84 @@ def tensorf_ndc_case():
     return out
 
 
+REALISTIC = dict(seed=53, res=48, density=[16, 16, 16], color=[48, 48, 48], features=27, units=128, rays=256,
+                 mask_res=32, mask_occupancy=0.15)
+
+
+def tensorf_realistic_case():
+    """LowRankTensor.forward at the benchmark's model shape on a 48^3 grid:
+    16 / 48 components per plane and line, 27 features, 128 renderer units, PE
+    L=2 on features and view directions, ReLU density, distance scale 25, a 32^3
+    alpha mask at 15% occupancy, 256 rays marching from the sphere of radius 4
+    (near 2, far 6) with one uniform per ray.  The parameters come from
+    oracle.tensorf.seeded_vm_model and are not stored; the fixture holds the
+    inputs, the outputs and the autograd gradients of a random-cotangent loss."""
+    from oracle import tensorf as otf
+    c = REALISTIC
+    res = torch.tensor([c['res']] * 3)
+    bbox = [[-1.5] * 3, [1.5] * 3]
+    tcfg = dict(tensorf_cfg(int(res.prod()), c['density'], c['color'], bbox), views_positional_encoding_degree=2,
+                features_positional_encoding_degree=2)
+    configs = {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}, 'database': 'synthetic'}
+    tm = RT.VmDecomposedTensor('coarse_model', configs, tcfg, {'bounding_box': bbox})
+    tm.update_tensor_params(res, torch.tensor(bbox))
+    assert [int(r) for r in tm.resolution] == [c['res']] * 3
+    tp, _ = otf.seeded_vm_model(c['seed'], [c['res']] * 3, c['density'], c['color'], c['features'], c['units'])
+    with torch.no_grad():
+        for kind, mats, vecs in (('density', tm.matrices_density, tm.vectors_density),
+                                 ('color', tm.matrices_color, tm.vectors_color)):
+            for i in range(3):
+                mats[i].copy_(torch.from_numpy(tp[f'planes_{kind}'][i])[None])
+                vecs[i].copy_(torch.from_numpy(tp[f'lines_{kind}'][i])[None])
+        tm.basis_matrix_color.weight.copy_(torch.from_numpy(tp['basis_matrix_color.weight']))
+        for k, prm in tm.color_predictor.named_parameters():
+            prm.copy_(torch.from_numpy(tp['color_predictor.' + k]))
+    rng = np.random.default_rng(c['seed'] + 1)
+    vol = torch.from_numpy((rng.random((c['mask_res'],) * 3) < c['mask_occupancy']).astype(np.float32))
+    tm.alpha_mask = RT.AlphaGridMask(vol, torch.tensor(bbox))
+    tm.eval()
+    n = c['rays']
+    o = rng.standard_normal((n, 3)).astype(np.float32)
+    o = 4.0 * o / np.linalg.norm(o, axis=-1, keepdims=True)
+    d = -o / 4.0 + 0.3 * rng.standard_normal((n, 3)).astype(np.float32)
+    d = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
+    o, d = torch.from_numpy(o), torch.from_numpy(d)
+    u = torch.from_numpy(rng.random((n, 1), dtype=np.float32))
+    fake = types.SimpleNamespace(ndc=False, training=True,
+                                 configs={'model': {'perturb': True, 'lindisp': False}},
+                                 model_configs={'near': 2.0, 'far': 6.0})
+    with patched_rand([u]):
+        z = RT.SimpleTensoRF.get_z_vals_coarse(fake, {'pixel_id': torch.zeros(n, 3)},
+                                               {'rays_o': o, 'rays_d': d}, tm)
+    pts = o[:, None, :] + d[:, None, :] * z[:, :, None]
+    vdir = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    ret = tm({'pts': pts, 'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vdir}, retraw=True)
+    tg = torch.Generator().manual_seed(59)
+    loss = 0
+    out = {}
+    for k in ('rgb', 'depth', 'acc'):
+        cot = torch.randn(ret[k].shape, generator=tg)
+        out[f'cot_{k}'] = cot.numpy()
+        loss = loss + torch.sum(ret[k] * cot)
+    loss.backward()
+    out.update({'bbox': np.array(bbox, np.float32), 'alpha_vol': vol.numpy().astype(np.uint8), 'u': u.numpy(),
+                'rays_o': o.numpy(), 'rays_d': d.numpy(), 'z': z.numpy(), 'step_size': tm.step_size.numpy(),
+                'num_samples': tm.num_samples.numpy()})
+    for k, v in c.items():
+        out[f'cfg_{k}'] = np.array(v)
+    for i in range(3):
+        out[f'grad_planes_density.{i}'] = tm.matrices_density[i].grad.numpy()[0]
+        out[f'grad_lines_density.{i}'] = tm.vectors_density[i].grad.numpy()[0]
+        out[f'grad_planes_color.{i}'] = tm.matrices_color[i].grad.numpy()[0]
+        out[f'grad_lines_color.{i}'] = tm.vectors_color[i].grad.numpy()[0]
+    out['grad_basis_matrix_color.weight'] = tm.basis_matrix_color.weight.grad.numpy()
+    for k, prm in tm.color_predictor.named_parameters():
+        out['grad_color_predictor.' + k] = prm.grad.numpy()
+    for k in ('rgb', 'depth', 'acc', 'weights', 'depth_var', 'raw_sigma'):
+        out['out_' + k] = ret[k].detach().numpy()
+    return out
+
+
 def tensorf_cfg(vox, dens, col, bbox):
     return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': dens,
             'num_components_color': col, 'bounding_box': bbox, 'num_voxels_initial': vox, 'num_voxels_final': vox,
@@ -863,6 +941,7 @@ def main():
             aug_seeds=[77]),
         'tensorf': tensorf_case,
         'tensorf_ndc': tensorf_ndc_case,
+        'tensorf_realistic': tensorf_realistic_case,
         'tensorf_cp': tensorf_cp_case,
         'state_dicts': state_dict_case,
         'output_keys': output_keys_case,

@@ -1,0 +1,339 @@
+"""The FP32 plain path against the oracle at the full sizes of the benchmark
+workloads (the kernel-level tests cover small and ragged shapes):
+
+* NeRF render, 1024 rays, 64 stratified + 128 inverse-CDF samples, separate
+  Xavier-initialised coarse and fine 8x256 nets, explicit uniforms from seed 0,
+  through the functional path and through the drop-in GbSimpleNeRF;
+* NeRF training step, 4096 rays (white background, rgb MSE + 0.1 L1 depth on a
+  quarter of the rays): every output of the fused step and the parameter
+  gradients of both nets;
+* TensoRF VM model, 300^3 grid, 16 / 48 components, 27 features, 128-unit
+  renderer, 128^3 alpha mask at 15% occupancy, 8192 rays: outputs of all rays
+  and the gradients of every grid and renderer parameter.
+
+Tolerances: rgb/depth/weights/acc within 1e-5 relative (absolute floor 1e-6 of
+the value range) of the float32 oracle; gradients as in test_gpu_train_step.py
+(per tensor within max(1e-4, 3x the float32 oracle's own error) of the float64
+oracle) for NeRF, 1e-4 relative L2 against the float32 oracle for TensoRF.
+
+Two places where two correct float32 implementations legitimately disagree are
+excluded explicitly, counted, and the count is asserted to be tiny:
+
+* NeRF, the last sample of a world-space ray (delta = 1e10 |d|,
+  SimpleNeRF17.py:489-492): when its raw sigma pre-activation lies within
+  rounding of 0, one side has sigma = 0 and the other alpha = 1.  Rays whose
+  last sigma is zero on one side only are dropped from the output comparison.
+* TensoRF, the surface threshold (weights > 1e-4, SimpleTensoRF09.py:726): a
+  sample whose weight lies within float32 rounding of 1e-4 may be coloured on
+  one side only.  Rays with a sample whose two weights straddle the threshold,
+  or lie within 1e-5 relative of it, are dropped from the comparison.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import nerf as on
+from oracle import tensorf as ot
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from simple_rf_gb300 import build as b
+    b.build()
+
+
+def _T(x):
+    return torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(DEV)
+
+
+def _close(got, ref, name, rtol=1e-5, rows=None):
+    got, ref = np.asarray(got), np.asarray(ref)
+    if rows is not None:
+        got, ref = got[rows], ref[rows]
+    np.testing.assert_allclose(got, ref, rtol=rtol, atol=1e-6 * max(1.0, float(np.abs(ref).max())), err_msg=name)
+
+
+def _last_sigma_agrees(sig_gpu, sig_ref):
+    """Rays whose last-sample sigma is zero on both sides or positive on both."""
+    return (np.asarray(sig_gpu)[:, -1] > 0) == (np.asarray(sig_ref)[:, -1] > 0)
+
+
+def _config1_inputs(n=1024):
+    rng = np.random.default_rng(0)
+    o = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
+    d = rng.standard_normal((n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    u_c = rng.random((n, 64), dtype=np.float32)
+    u_f = rng.random((n, 128), dtype=np.float32)
+    return o, d, u_c, u_f
+
+
+def test_config1_render_1024_rays_matches_oracle():
+    """Config-1 render through the functional path (stratified z, PE + MLP,
+    compositing, inverse-CDF fine z, fine pass) against the oracle's
+    render_rays (SimpleNeRF17.py:159-328) on the same uniforms."""
+    from simple_rf_gb300 import functional as F
+    n = 1024
+    o, d, u_c, u_f = _config1_inputs(n)
+    ospec = on.MlpSpec()
+    pc, pf = on.xavier_params(ospec, 0), on.xavier_params(ospec, 1)
+    spec = F.MlpSpec()
+    vd = F.view_dirs(_T(d))
+    got = {}
+    with torch.no_grad():
+        def run(p, z):
+            s = z.shape[1]
+            pts = (_T(o)[:, None, :] + _T(d)[:, None, :] * z[:, :, None]).reshape(-1, 3).contiguous()
+            sigma, rgb = F.NerfMlpFunction.apply(spec, 0, pts, vd, s, None, *[_T(p[k]) for k in spec.param_names])
+            out = F.composite(sigma.reshape(n, s), rgb.reshape(n, s, 3), z, _T(d))
+            return out, sigma.reshape(n, s)
+        zc = F.stratified_z(n, 64, 2.0, 6.0, _T(u_c), device=DEV)
+        oc, sc = run(pc, zc)
+        zf = F.fine_z(zc, oc['weights'], 128, _T(u_f))
+        of, sf = run(pf, zf)
+    for tag, out, sig, z in (('coarse', oc, sc, zc), ('fine', of, sf, zf)):
+        for k in ('rgb', 'depth', 'weights', 'acc'):
+            got[f'{k}_{tag}'] = out[k].cpu().numpy()
+        got[f'sigma_{tag}'] = sig.cpu().numpy()
+        got[f'z_{tag}'] = z.cpu().numpy()
+    ref, _ = on.render_rays(pc, pf, ospec, ospec, o, d, 2.0, 6.0, 64, 128, u_c, u_f, z_fine=got['z_fine'],
+                            pts_fp32=True)
+    np.testing.assert_array_equal(got['z_coarse'], ref['z_vals_coarse'])
+    # the oracle's own inverse-CDF depths: equal up to the conditioning of the
+    # sampler (the kernel tests compare it in CDF space)
+    zf_ref = on.fine_z(ref['z_vals_coarse'], ref['weights_coarse'], 128, u_f)
+    frac = float(np.mean(np.abs(got['z_fine'] - zf_ref) <= 1e-5 * np.abs(zf_ref)))
+    assert frac > 0.999, frac
+    keep = _last_sigma_agrees(got['sigma_coarse'], ref['raw_sigma_coarse'][..., 0]) & \
+        _last_sigma_agrees(got['sigma_fine'], ref['raw_sigma_fine'][..., 0])
+    assert keep.mean() > 0.995, int((~keep).sum())
+    for tag in ('coarse', 'fine'):
+        for k in ('rgb', 'depth', 'weights', 'acc'):
+            _close(got[f'{k}_{tag}'], ref[f'{k}_{tag}'], f'{k}_{tag}', rows=keep)
+    print('config 1: rays excluded for a last-sample sigma flip', int((~keep).sum()), 'of', n,
+          '; fine depths equal to the oracle sampler', frac)
+
+
+def test_config1_drop_in_render_1024_rays_matches_oracle():
+    """GbSimpleNeRF.forward in evaluation mode (linspace coarse depths,
+    deterministic inverse CDF) on the config-1 rays, ray generation patched to
+    take the synthetic origins and directions as the reference harness does."""
+    from simple_rf_gb300 import functional as F
+    from simple_rf_gb300.nerf import GbSimpleNeRF
+    mc = {'num_samples': 64, 'points_net_depth': 8, 'views_net_depth': 1, 'points_net_width': 256,
+          'views_net_width': 128, 'points_positional_encoding_degree': 10, 'views_positional_encoding_degree': 4,
+          'use_view_dirs': True, 'view_dependent_rgb': True, 'predict_visibility': False}
+    configs = {'data_loader': {'ndc': False}, 'model': {
+        'name': 'GbSimpleNeRF01', 'coarse_model': mc, 'fine_model': dict(mc, num_samples=128),
+        'learn_camera_focal_length': False, 'learn_camera_rotation': False, 'learn_camera_translation': False,
+        'chunk': 4096, 'lindisp': False, 'netchunk': 16384, 'perturb': False, 'raw_noise_std': 0.0,
+        'white_bkgd': False}}
+    model_configs = {'intrinsics': np.eye(3)[None], 'extrinsics': np.eye(4)[None], 'resolution': (32, 32),
+                     'near': 2.0, 'far': 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0}
+    n = 1024
+    o, d, _, _ = _config1_inputs(n)
+    model = GbSimpleNeRF(configs, model_configs).to(DEV).eval()
+    spec = on.MlpSpec()
+    pc, pf = on.xavier_params(spec, 0), on.xavier_params(spec, 1)
+    with torch.no_grad():
+        for mod, p in ((model.coarse_model, pc), (model.fine_model, pf)):
+            for name, prm in mod.named_parameters():
+                prm.copy_(torch.from_numpy(p[name]))
+    model.generate_rays = lambda input_dict, mode: {'rays_o': _T(o), 'rays_d': _T(d), 'view_dirs': F.view_dirs(_T(d))}
+    batch = {'pixel_id': torch.zeros(n, 3, dtype=torch.int32, device=DEV), 'num_frames': 1, 'common_data': {}}
+    with torch.no_grad():
+        ret = model(batch, retraw=True)
+    got = {k: v.cpu().numpy() for k, v in ret.items() if isinstance(v, torch.Tensor)}
+    ref, _ = on.render_rays(pc, pf, spec, spec, o, d, 2.0, 6.0, 64, 128, None, None, z_fine=got['z_vals_fine'],
+                            pts_fp32=True)
+    keep = _last_sigma_agrees(got['raw_sigma_coarse'][..., 0], ref['raw_sigma_coarse'][..., 0]) & \
+        _last_sigma_agrees(got['raw_sigma_fine'][..., 0], ref['raw_sigma_fine'][..., 0])
+    assert keep.mean() > 0.995, int((~keep).sum())
+    _close(got['z_vals_coarse'], ref['z_vals_coarse'], 'z_vals_coarse', rtol=1e-6)
+    for k in ('rgb_coarse', 'depth_coarse', 'weights_coarse', 'acc_coarse', 'rgb_fine', 'depth_fine',
+              'weights_fine', 'acc_fine', 'depth_var_fine'):
+        _close(got[k], ref[k], k, rows=keep)
+
+
+# --------------------------------------------------------------- config 2 --
+
+def _step(n_rays, precision='fp32', sigma_bias=None, seed=3):
+    from simple_rf_gb300.train_step import NerfTrainStep, synthetic_batch
+    step = NerfTrainStep(n_rays, 64, 128, precision=precision, device=DEV, seed=seed)
+    if sigma_bias is not None:
+        for net in step.nets.values():
+            net.views[net.spec.param_names.index('pts_output_linear.bias')].fill_(sigma_bias)
+    batch = synthetic_batch(n_rays, 64, 128, seed=seed + 1, device=DEV)
+    step.set_batch(*batch)
+    params = {tag: {k: v.double().cpu().numpy() for k, v in net.state_dict().items()} for tag, net in step.nets.items()}
+    step.step()
+    torch.cuda.synchronize()
+    out = {k: v.detach().cpu().numpy() for k, v in step.outputs().items()}
+    grads = {tag: {k: g.double().cpu().numpy() for k, g in zip(net.spec.param_names, net.gviews)}
+             for tag, net in step.nets.items()}
+    host = [x.cpu().numpy() for x in batch]
+    return params, out, grads, host
+
+
+def oracle_step_chunked(params, host, z_fine, dtype, chunk=256, grads=True):
+    """The oracle's config-2 step over ray chunks (rays are independent, so the
+    outputs are those of one whole-batch call; the loss gradients come from the
+    whole batch and the parameter gradients are summed over the chunks)."""
+    o, d, t_rgb, t_depth, u_c, u_f = [np.asarray(x, dtype) for x in host]
+    spec = on.MlpSpec()
+    p = {tag: {k: v.astype(dtype) for k, v in params[tag].items()} for tag in params}
+    n = o.shape[0]
+
+    def fwd(sl):
+        return on.render_rays(p['coarse'], p['fine'], spec, spec, o[sl], d[sl], 2.0, 6.0, 64, 128, u_c[sl], u_f[sl],
+                              white_bkgd=True, z_fine=np.asarray(z_fine[sl], dtype), pts_fp32=True)
+    parts = [fwd(slice(i, i + chunk))[0] for i in range(0, n, chunk)]
+    ret = {k: np.concatenate([r[k] for r in parts], 0) for k in parts[0]}
+    if not grads:
+        return ret, None
+    mask = np.zeros(n, dtype)
+    mask[:n // 4] = 1
+    _, g = on.train_loss(ret, t_rgb, t_depth, mask)
+    total = None
+    for i in range(0, n, chunk):
+        sl = slice(i, i + chunk)
+        _, caches = fwd(sl)
+        gi = on.backward_render(p, {'coarse': spec, 'fine': spec}, caches, {k: v[sl] for k, v in g.items()},
+                                sl.stop - sl.start)
+        if total is None:
+            total = {t: {k: v.astype(np.float64) for k, v in gt.items()} for t, gt in gi.items()}
+        else:
+            for t in gi:
+                for k in gi[t]:
+                    total[t][k] += gi[t][k]
+        del caches
+    return ret, total
+
+
+def test_config2_train_step_4096_rays_outputs_match_oracle():
+    """The fused FP32 plain step at the benchmark's 4096 rays: coarse and fine
+    rgb/depth/weights/acc against the float32 oracle (fine pass on the depths
+    the GPU sampled), the Xavier-initialised nets as trained."""
+    params, out, _, host = _step(4096)
+    ref, _ = oracle_step_chunked(params, host, out['z_fine'], np.float32, chunk=512, grads=False)
+    np.testing.assert_array_equal(out['z_coarse'], ref['z_vals_coarse'])
+    keep = np.ones(4096, bool)
+    for tag in ('coarse', 'fine'):
+        keep &= _last_sigma_agrees(out[f'sigma_{tag}'].reshape(4096, -1), ref[f'raw_sigma_{tag}'][..., 0])
+    assert keep.mean() > 0.995, int((~keep).sum())
+    for tag in ('coarse', 'fine'):
+        for k in ('rgb_map', 'depth', 'weights', 'acc'):
+            key = {'rgb_map': 'rgb'}.get(k, k)
+            _close(out[f'{k}_{tag}'], ref[f'{key}_{tag}'], f'{k}_{tag}', rows=keep)
+    print('config 2: rays excluded for a last-sample sigma flip', int((~keep).sum()), 'of 4096')
+
+
+def test_config2_train_step_4096_rays_gradients_match_fp64_oracle():
+    """Parameter gradients of the 4096-ray FP32 plain step against the float64
+    oracle, on a network whose sigma-head bias keeps every ray off the last-sample
+    step (see test_gpu_train_step.py)."""
+    from test_gpu_train_step import check_fp32_gradients
+    params, out, grads, host = _step(4096, sigma_bias=0.5)
+    _, g64 = oracle_step_chunked(params, host, out['z_fine'], np.float64)
+    _, g32 = oracle_step_chunked(params, host, out['z_fine'], np.float32)
+    check_fp32_gradients(grads, g32, g64)
+
+
+# --------------------------------------------------------------- config 4 --
+
+def _oracle_params(tm):
+    tp = {'bbox': tm.bounding_box.cpu().numpy().astype(np.float32)}
+    for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                        ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+        tp[kind] = [np.ascontiguousarray(p.detach()[0].cpu().numpy()) for p in plist]
+    tp['basis_matrix_color.weight'] = tm.basis_matrix_color.weight.detach().cpu().numpy()
+    for k, prm in tm.color_predictor.named_parameters():
+        tp['color_predictor.' + k] = prm.detach().cpu().numpy()
+    return tp
+
+
+def _config4_run(n_rays, seed=21):
+    from simple_rf_gb300 import functional as F
+    from simple_rf_gb300.bench_tensorf import make_models, synthetic_rays
+    tm = make_models(DEV, precision='fp32')[0]
+    tm.eval()
+    o, d, _, u = synthetic_rays(n_rays, seed, DEV)
+    bbox, s, step = tm.host_geometry()
+    assert (s, tuple(int(r) for r in tm.resolution)) == (1039, (300, 300, 300))
+    z = F.aabb_z(o, d, s, bbox, 2.0, 6.0, step, u[:, 0].contiguous())
+    vd = F.view_dirs(d)
+    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=True)
+    return tm, (o, d, z), out
+
+
+def _oracle_forward(tm, o, d, z):
+    spec = ot.RendererSpec(features_dim=27, features_pe=2, views_pe=2, units=128)
+    am = tm.alpha_mask
+    return ot.tensorf_forward(_oracle_params(tm), spec, o, d, z, alpha_vol=am.volume().float().cpu().numpy(),
+                              alpha_bbox=am.bounding_box.cpu().numpy().astype(np.float32), distance_scale=25.0,
+                              weight_threshold=1e-4, white=True), spec
+
+
+def _threshold_stable(w_gpu, w_ref, thr=1e-4):
+    """Rays none of whose samples straddles the surface threshold between the two
+    weight sets or lies within 1e-5 relative of it."""
+    side = (w_gpu > thr) != (w_ref > thr)
+    near = np.abs(w_ref - thr) <= 1e-5 * thr
+    return ~(side | near).any(1)
+
+
+def test_config4_tensorf_8192_rays_outputs_match_oracle():
+    """The drop-in GbVmTensor at the benchmark's main model (300^3, R 16 / 48,
+    27 features, 128 units, 128^3 alpha mask at 15%, white background, 1039
+    samples per ray) on 8192 rays against the float32 oracle of
+    LowRankTensor.forward (SimpleTensoRF09.py:701-761)."""
+    tm, (o, d, z), out = _config4_run(8192)
+    oh, dh, zh = (x.cpu().numpy() for x in (o, d, z))
+    ref, _ = _oracle_forward(tm, oh, dh, zh)[0]
+    got = {k: v.detach().cpu().numpy() for k, v in out.items()}
+    keep = _threshold_stable(got['weights'], ref['weights'])
+    n_surface = int((ref['weights'] > 1e-4).sum())
+    assert n_surface > 100000, n_surface
+    assert keep.mean() > 0.99, int((~keep).sum())
+    for k in ('rgb', 'depth', 'acc', 'weights', 'depth_var', 'raw_sigma'):
+        _close(got[k], ref[k], k, rows=keep)
+    print('config 4: surface samples', n_surface, '; rays excluded at the surface threshold', int((~keep).sum()),
+          'of 8192')
+
+
+def test_config4_tensorf_gradients_match_oracle():
+    """Gradients of every plane, line, basis and renderer parameter of the config-4
+    main model for a loss on the first 256 of 8192 rays (the other rays carry zero
+    cotangents, so the gradients are those of the 256 rays alone) against the
+    float32 oracle's adjoint, 1e-4 relative L2 per tensor."""
+    tm, (o, d, z), out = _config4_run(8192, seed=22)
+    n_sub = 256
+    rng = np.random.default_rng(5)
+    cot = {k: rng.standard_normal(out[k].shape).astype(np.float32) for k in ('rgb', 'depth', 'acc')}
+    for v in cot.values():
+        v[n_sub:] = 0
+    loss = sum((out[k] * _T(cot[k])).sum() for k in cot)
+    loss.backward()
+    oh, dh, zh = (x[:n_sub].cpu().numpy() for x in (o, d, z))
+    (ref, cache), spec = _oracle_forward(tm, oh, dh, zh)
+    keep = _threshold_stable(out['weights'][:n_sub].detach().cpu().numpy(), ref['weights'])
+    assert keep.all(), int((~keep).sum())
+    g = ot.tensorf_backward(_oracle_params(tm), spec, cache, {k: v[:n_sub] for k, v in cot.items()})
+    pairs = []
+    for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
+                        ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
+        for i in range(3):
+            pairs.append((f'{kind}.{i}', plist[i].grad[0]))
+    pairs.append(('basis_matrix_color.weight', tm.basis_matrix_color.weight.grad))
+    for k, prm in tm.color_predictor.named_parameters():
+        pairs.append(('color_predictor.' + k, prm.grad))
+    worst = 0.0
+    for name, grad in pairs:
+        ref_g = g[name].astype(np.float64)
+        rel = np.linalg.norm(grad.detach().double().cpu().numpy() - ref_g) / max(np.linalg.norm(ref_g), 1e-30)
+        worst = max(worst, rel)
+        assert rel < 1e-4, (name, rel)
+    print('config 4: worst per-tensor gradient rel-L2', worst)

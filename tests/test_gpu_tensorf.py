@@ -2,9 +2,13 @@
 autograd gradients (golden fixture produced by tests/golden/make_golden.py from
 SimpleTensoRF09.LowRankTensor.forward), and against the numpy oracle.
 
-Tolerances: outputs 1e-4 relative (absolute floor 2e-4: a sample whose weight
-sits on the 1e-4 surface threshold may switch sides between implementations and
-moves rgb by at most ~1e-4); parameter gradients 1e-3 relative L2.
+Tolerances: outputs 1e-5 relative (absolute floor 1e-6 of the value range);
+parameter gradients 1e-4 relative L2.  A sample whose weight lies within float32
+rounding of the 1e-4 surface threshold (SimpleTensoRF09.py:726) may be coloured
+by one implementation and not the other: rays holding such a sample are left out
+of the output comparison and counted (at most 1% of the rays), and when any ray
+was left out the gradient bar becomes 1e-3 (the flipped sample's colour term is
+in one gradient only).
 """
 import numpy as np
 import pytest
@@ -48,20 +52,27 @@ def _model(g, ndc=False):
     return tm
 
 
-def test_tensorf_forward_backward_matches_reference_golden(golden):
-    g = golden('tensorf')
-    tm = _model(g)
-    o = torch.from_numpy(g['rays_o']).to(DEV)
-    d = torch.from_numpy(g['rays_d']).to(DEV)
-    z = torch.from_numpy(g['z']).to(DEV)
-    vd = d / torch.linalg.norm(d, dim=-1, keepdim=True)
-    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=True)
-    for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'depth_var'):
-        ref = g['out_' + k]
-        got = out[k].detach().cpu().numpy()
-        np.testing.assert_allclose(got, ref, rtol=1e-4, atol=2e-4 * max(1.0, float(np.abs(ref).max())), err_msg=k)
-    loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'acc'))
-    loss.backward()
+def threshold_stable(w_gpu, w_ref, thr=1e-4):
+    """Rays none of whose samples has weights on both sides of the surface
+    threshold between the two implementations, or within 1e-5 relative of it."""
+    side = (w_gpu > thr) != (w_ref > thr)
+    near = np.abs(w_ref - thr) <= 1e-5 * thr
+    return ~(side | near).any(-1)
+
+
+def compare_outputs(out, g, keys):
+    """Outputs against the golden on the threshold-stable rays; returns the
+    gradient bar (1e-4, or 1e-3 when a ray was left out)."""
+    keep = threshold_stable(out['weights'].detach().cpu().numpy(), g['out_weights'])
+    assert keep.mean() >= 0.99 or keep.sum() >= keep.size - 1, int((~keep).sum())
+    for k in keys:
+        ref = g['out_' + k][keep]
+        got = out[k].detach().cpu().numpy()[keep]
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6 * max(1.0, float(np.abs(ref).max())), err_msg=k)
+    return 1e-4 if keep.all() else 1e-3
+
+
+def compare_gradients(tm, g, bar):
     pairs = []
     for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
                         ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
@@ -70,11 +81,28 @@ def test_tensorf_forward_backward_matches_reference_golden(golden):
     pairs.append(('basis_matrix_color.weight', tm.basis_matrix_color.weight.grad))
     for k, prm in tm.color_predictor.named_parameters():
         pairs.append(('color_predictor.' + k, prm.grad))
+    worst = 0.0
     for name, grad in pairs:
         ref = g['grad_' + name]
-        got = grad.detach().cpu().numpy()
+        got = grad.detach().double().cpu().numpy()
         rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
-        assert rel < 1e-3, (name, rel)
+        worst = max(worst, rel)
+        assert rel < bar, (name, rel)
+    return worst
+
+
+def test_tensorf_forward_backward_matches_reference_golden(golden):
+    g = golden('tensorf')
+    tm = _model(g)
+    o = torch.from_numpy(g['rays_o']).to(DEV)
+    d = torch.from_numpy(g['rays_d']).to(DEV)
+    z = torch.from_numpy(g['z']).to(DEV)
+    vd = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=True)
+    bar = compare_outputs(out, g, ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'depth_var'))
+    loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'acc'))
+    loss.backward()
+    compare_gradients(tm, g, bar)
 
 
 def test_tensorf_ndc_forward_backward_matches_reference_golden(golden):
@@ -88,25 +116,53 @@ def test_tensorf_ndc_forward_backward_matches_reference_golden(golden):
     t = {k: torch.from_numpy(g[k]).to(DEV) for k in ('rays_o', 'rays_d', 'rays_o_ndc', 'rays_d_ndc', 'view_dirs', 'z')}
     out = tm({'z_vals_ndc': t['z'], 'rays_o_ndc': t['rays_o_ndc'], 'rays_d_ndc': t['rays_d_ndc'],
               'rays_o': t['rays_o'], 'rays_d': t['rays_d'], 'view_dirs': t['view_dirs']}, retraw=True)
-    for k in ('rgb', 'depth', 'depth_ndc', 'acc', 'weights', 'raw_sigma', 'depth_var', 'depth_var_ndc'):
-        ref = g['out_' + k]
-        got = out[k].detach().cpu().numpy()
-        np.testing.assert_allclose(got, ref, rtol=1e-4, atol=2e-4 * max(1.0, float(np.abs(ref).max())), err_msg=k)
+    bar = compare_outputs(out, g, ('rgb', 'depth', 'depth_ndc', 'acc', 'weights', 'raw_sigma', 'depth_var',
+                                   'depth_var_ndc'))
     loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'depth_ndc', 'acc'))
     loss.backward()
-    pairs = []
-    for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
-                        ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
-        for i in range(3):
-            pairs.append((f'{kind}.{i}', plist[i].grad[0]))
-    pairs.append(('basis_matrix_color.weight', tm.basis_matrix_color.weight.grad))
-    for k, prm in tm.color_predictor.named_parameters():
-        pairs.append(('color_predictor.' + k, prm.grad))
-    for name, grad in pairs:
-        ref = g['grad_' + name]
-        got = grad.detach().cpu().numpy()
-        rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
-        assert rel < 1e-3, (name, rel)
+    compare_gradients(tm, g, bar)
+
+
+def test_tensorf_realistic_model_matches_reference_golden(golden):
+    """The drop-in GbVmTensor at the benchmark's model shape on a 48^3 grid (16 / 48
+    components, 27 features, 128 renderer units, PE L=2, a 32^3 alpha mask at 15%,
+    white background, 256 rays) against LowRankTensor.forward's outputs and
+    autograd gradients (golden tensorf_realistic)."""
+    from oracle import tensorf as ot
+    from simple_rf_gb300 import tensorf as T
+    from simple_rf_gb300.tensorf_model import AlphaGridMask, GbVmTensor
+    g = golden('tensorf_realistic')
+    c = {k[4:]: g[k] for k in g if k.startswith('cfg_')}
+    tp, _ = ot.seeded_vm_model(int(c['seed']), [int(c['res'])] * 3, list(c['density']), list(c['color']),
+                               int(c['features']), int(c['units']))
+    tcfg = dict(_tcfg(), num_components_density=[int(x) for x in c['density']],
+                num_components_color=[int(x) for x in c['color']], num_voxels_initial=int(c['res']) ** 3,
+                num_voxels_final=int(c['res']) ** 3, features_dimension_color=int(c['features']),
+                num_units_color_predictor=int(c['units']))
+    tm = GbVmTensor('coarse_model', {'data_loader': {'ndc': False}, 'model': {'white_bkgd': True}}, tcfg,
+                    {'bounding_box': tcfg['bounding_box']})
+    assert [int(r) for r in tm.resolution] == [int(c['res'])] * 3
+    with torch.no_grad():
+        for kind, mats, vecs in (('density', tm.matrices_density, tm.vectors_density),
+                                 ('color', tm.matrices_color, tm.vectors_color)):
+            for i in range(3):
+                mats[i] = torch.nn.Parameter(T.to_channels_last(torch.from_numpy(tp[f'planes_{kind}'][i])[None]))
+                vecs[i] = torch.nn.Parameter(T.to_channels_last(torch.from_numpy(tp[f'lines_{kind}'][i])[None]))
+        tm.basis_matrix_color.weight.copy_(torch.from_numpy(tp['basis_matrix_color.weight']))
+        for k, prm in tm.color_predictor.named_parameters():
+            prm.copy_(torch.from_numpy(tp['color_predictor.' + k]))
+    tm = tm.to(DEV)
+    tm.alpha_mask = AlphaGridMask(torch.from_numpy(g['alpha_vol'].astype(np.float32)).to(DEV),
+                                  torch.tensor(g['bbox']).to(DEV))
+    tm.eval()
+    o, d, z = (torch.from_numpy(g[k]).to(DEV) for k in ('rays_o', 'rays_d', 'z'))
+    vd = d / torch.linalg.norm(d, dim=-1, keepdim=True)
+    out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}, retraw=True)
+    assert tm.last_sample_counts['surface'] > 5000
+    bar = compare_outputs(out, g, ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'depth_var'))
+    loss = sum((out[k] * torch.from_numpy(g[f'cot_{k}']).to(DEV)).sum() for k in ('rgb', 'depth', 'acc'))
+    loss.backward()
+    print('realistic golden: worst gradient rel-L2', compare_gradients(tm, g, bar))
 
 
 def test_tensorf_aabb_marching_matches_reference(golden):

@@ -211,13 +211,13 @@ def test_tensorf_forward_backward(golden):
                                     alpha_bbox=g['bbox'], white=True)
     for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'raw_rgb', 'depth_var'):
         ref = g['out_' + k]
-        close(out[k], ref, rtol=1e-4, atol=1e-5 * max(1.0, float(np.abs(ref).max())))
+        close(out[k], ref, rtol=1e-5, atol=1e-6 * max(1.0, float(np.abs(ref).max())))
     assert n == out['rgb'].shape[0]
     grads = ot.tensorf_backward(tp, spec, cache, {k: g[f'cot_{k}'] for k in ('rgb', 'depth', 'acc')})
     for k, v in grads.items():
         ref = g['grad_' + k]
         err = np.linalg.norm(v - ref) / max(np.linalg.norm(ref), 1e-12)
-        assert err < 1e-4, (k, err)
+        assert err < 1e-5, (k, err)
 
 
 def test_tensorf_ndc_forward_backward(golden):
@@ -232,12 +232,12 @@ def test_tensorf_ndc_forward_backward(golden):
                                     alpha_bbox=g['bbox'], white=False, world_rays=(g['rays_o'], g['rays_d']))
     for k in ('rgb', 'depth', 'depth_ndc', 'acc', 'weights', 'raw_sigma', 'raw_rgb', 'depth_var', 'depth_var_ndc'):
         ref = g['out_' + k]
-        close(out[k], ref, rtol=1e-4, atol=1e-5 * max(1.0, float(np.abs(ref).max())))
+        close(out[k], ref, rtol=1e-5, atol=1e-6 * max(1.0, float(np.abs(ref).max())))
     grads = ot.tensorf_backward(tp, spec, cache, {k: g[f'cot_{k}'] for k in ('rgb', 'depth', 'depth_ndc', 'acc')})
     for k, v in grads.items():
         ref = g['grad_' + k]
         err = np.linalg.norm(v - ref) / max(np.linalg.norm(ref), 1e-12)
-        assert err < 1e-4, (k, err)
+        assert err < 1e-5, (k, err)
 
 
 def test_tensorf_cp_forward_backward(golden):
@@ -253,13 +253,39 @@ def test_tensorf_cp_forward_backward(golden):
     out, cache = ot.tensorf_forward(tp, spec, g['rays_o'], g['rays_d'], g['z'], white=True)
     for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'raw_rgb', 'depth_var'):
         ref = g['out_' + k]
-        close(out[k], ref, rtol=1e-4, atol=1e-5 * max(1.0, float(np.abs(ref).max())))
+        close(out[k], ref, rtol=1e-5, atol=1e-6 * max(1.0, float(np.abs(ref).max())))
     grads = ot.tensorf_backward(tp, spec, cache, {k: g[f'cot_{k}'] for k in ('rgb', 'depth', 'acc')})
     assert set(grads) >= {'lines_density.0', 'lines_color.2', 'basis_matrix_color.weight'}
     for k, v in grads.items():
         ref = g['grad_' + k]
         err = np.linalg.norm(v - ref) / max(np.linalg.norm(ref), 1e-12)
-        assert err < 1e-4, (k, err)
+        assert err < 1e-5, (k, err)
+
+
+def test_tensorf_realistic_forward_backward(golden):
+    """The oracle against LowRankTensor.forward at the benchmark's model shape on
+    a 48^3 grid (golden tensorf_realistic: 16 / 48 components, 27 features, 128
+    renderer units, a 32^3 alpha mask at 15%, 256 rays, parameters regenerated
+    from their seed by oracle.tensorf.seeded_vm_model)."""
+    g = golden('tensorf_realistic')
+    c = {k[4:]: g[k] for k in g if k.startswith('cfg_')}
+    tp, spec = ot.seeded_vm_model(int(c['seed']), [int(c['res'])] * 3, list(c['density']), list(c['color']),
+                                  int(c['features']), int(c['units']))
+    tp['bbox'] = g['bbox']
+    z = ot.aabb_z(g['rays_o'], g['rays_d'], g['bbox'], 2.0, 6.0, float(g['step_size']), int(g['num_samples']), g['u'])
+    close(z, g['z'], rtol=1e-6, atol=1e-6)
+    out, cache = ot.tensorf_forward(tp, spec, g['rays_o'], g['rays_d'], g['z'], alpha_vol=g['alpha_vol'].astype(np.float32),
+                                    alpha_bbox=g['bbox'], white=True)
+    assert int((g['out_weights'] > 1e-4).sum()) > 5000
+    for k in ('rgb', 'depth', 'acc', 'weights', 'raw_sigma', 'depth_var'):
+        ref = g['out_' + k]
+        close(out[k], ref, rtol=1e-5, atol=1e-6 * max(1.0, float(np.abs(ref).max())))
+    grads = ot.tensorf_backward(tp, spec, cache, {k: g[f'cot_{k}'] for k in ('rgb', 'depth', 'acc')})
+    assert len(grads) == 19
+    for k, v in grads.items():
+        ref = g['grad_' + k]
+        err = np.linalg.norm(v - ref) / max(np.linalg.norm(ref), 1e-12)
+        assert err < 1e-5, (k, err)
 
 
 def test_alpha_mask_query(golden):
