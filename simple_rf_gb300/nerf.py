@@ -157,6 +157,19 @@ class ExtrinsicsLearner(torch.nn.Module):
         return torch.linalg.inv(c2w)
 
 
+def check_pose_learning(model):
+    """Camera-pose learning (SimpleNeRF17.py:817-912 with learn_camera_rotation or
+    learn_camera_translation; Tester07.optimize_test_camera_params) trains the
+    extrinsics through the rays: the rays of this implementation carry no
+    gradient to the extrinsics, so a training pass with learnable poses is
+    refused instead of silently leaving the poses untouched.  Rendering with
+    learnt poses (evaluation mode) is unaffected."""
+    if model.training and model.extrinsics_learner is not None and \
+            any(p.requires_grad for p in model.extrinsics_learner.parameters()):
+        raise NotImplementedError('camera-pose gradients (learn_camera_rotation / learn_camera_translation) are not '
+                                  'implemented: the rays carry no gradient to the extrinsics')
+
+
 class GbSimpleNeRF(torch.nn.Module):
     """Drop-in for ``SimpleNeRF`` (src/models/SimpleNeRF17.py:14)."""
 
@@ -233,6 +246,7 @@ class GbSimpleNeRF(torch.nn.Module):
 
     def forward(self, input_batch: dict, *, retraw: bool = False, sec_views_vis: bool = False, mode: str = None):
         """SimpleNeRF17.py:104-127."""
+        check_pose_learning(self)
         input_batch = self.deep_dict_copy(input_batch)
         if 'common_data' in input_batch:
             for key, val in input_batch['common_data'].items():

@@ -27,7 +27,7 @@ from torch.nn import ModuleDict, ModuleList
 from . import _lib
 from . import functional as F
 from . import tensorf as T
-from .nerf import ExtrinsicsLearner, IntrinsicsLearner, _precision
+from .nerf import ExtrinsicsLearner, IntrinsicsLearner, _precision, check_pose_learning
 
 MATRIX_AXES = [[0, 1], [0, 2], [1, 2]]   # SimpleTensoRF09.py:1131
 VECTOR_AXES = [2, 1, 0]                  # SimpleTensoRF09.py:1132
@@ -590,8 +590,6 @@ class GbSimpleTensoRF(torch.nn.Module):
         self.fine_model_needed = 'fine_model' in configs['model']
         self.predict_visibility = False
         self.nerf_synthetic = configs.get('database') == 'NeRF_Synthetic'
-        if self.nerf_synthetic:
-            raise NotImplementedError('the NeRF-Synthetic camera convention is not supported')
         self.coarse_model = self.fine_model = None
         self.augmentations_needed = 'augmentations' in configs['model']
         if self.augmentations_needed:
@@ -654,6 +652,7 @@ class GbSimpleTensoRF(torch.nn.Module):
 
     def forward(self, input_batch, *, retraw=False, sec_views_vis=False, mode=None):
         """SimpleTensoRF09.py:133-162."""
+        check_pose_learning(self)
         input_batch = {k: (dict(v) if isinstance(v, dict) else v) for k, v in input_batch.items()}
         if 'common_data' in input_batch:
             for key, val in input_batch['common_data'].items():
@@ -686,22 +685,40 @@ class GbSimpleTensoRF(torch.nn.Module):
     def render_rays(self, input_dict, *, retraw, mode):
         """SimpleTensoRF09.py:194-351."""
         ret = {}
-        # mip_nerf_used=True (+0.5 px) and the x-flip of origins/directions (:205-207)
+        # mip_nerf_used=True (+0.5 px) and the x-flip of origins/directions (:205-207).
+        # The NeRF-Synthetic convention (:205-210) conjugates the pose by
+        # diag(1, -1, -1, 1) and keeps the camera-frame y, z signs: that equals the
+        # default rays with y and z negated (sign flips, exact), the x-flip undone,
+        # and the directions normalised.
         o, d = F.pixel_rays(input_dict['pixel_id'], input_dict['intrinsics'], input_dict['extrinsics'],
                             half_pixel=True)
-        flip = torch.tensor([-1.0, 1.0, 1.0], device=o.device)
+        flip = torch.tensor([1.0, -1.0, -1.0] if self.nerf_synthetic else [-1.0, 1.0, 1.0], device=o.device)
         o, d = (o * flip).contiguous(), (d * flip).contiguous()
+        if self.nerf_synthetic:
+            d = (d / torch.linalg.norm(d, dim=1, keepdim=True)).contiguous()
         ret['rays_o'], ret['rays_d'] = o, d
+        h, w = self.model_configs['resolution']
         if self.ndc:
             k = input_dict['intrinsics'].float()
-            h, w = self.model_configs['resolution']
             ret['rays_o_ndc'], ret['rays_d_ndc'] = F.ndc_rays(o, d, k[:, 0, 0].contiguous(), k[:, 1, 1].contiguous(),
                                                               h, w, self.model_configs['near'])
         m = self.configs['model']
         if any(m[key]['use_view_dirs'] for key in ('coarse_model', 'fine_model') if key in m):
             if mode == 'static_camera':
-                raise NotImplementedError('static_camera view directions are not supported for TensoRF')
-            ret['view_dirs'] = F.view_dirs(ret['rays_d_ndc'] if self.ndc else d)
+                # view directions of the fixed view pose (:222-232): its own rays,
+                # without the half pixel and without the x-flip
+                n = input_dict['pixel_id'].shape[0]
+                cd = input_dict['common_data']
+                vi = cd['view_intrinsic']
+                vk = (vi[None].repeat(n, 1, 1) if vi is not None else input_dict['intrinsics']).float().contiguous()
+                ve = cd['processed_view_pose'][None].repeat(n, 1, 1).float().contiguous()
+                vo, vd = F.pixel_rays(input_dict['pixel_id'], vk, ve)
+                if self.ndc:
+                    _, vd = F.ndc_rays(vo, vd, vk[:, 0, 0].contiguous(), vk[:, 1, 1].contiguous(), h, w,
+                                       self.model_configs['near'])
+                ret['view_dirs'] = F.view_dirs(vd)
+            else:
+                ret['view_dirs'] = F.view_dirs(ret['rays_d_ndc'] if self.ndc else d)
         train_augs = self.augmentations_needed and self.training and mode != 'test_camera_params_optimization'
 
         def model_input(z):

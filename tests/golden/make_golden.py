@@ -539,6 +539,67 @@ def tensorf_realistic_case():
     return out
 
 
+def _pose(angle, t):
+    c, s = np.cos(angle), np.sin(angle)
+    e = np.eye(4)
+    e[:3, :3] = [[c, 0, s], [0, 1, 0], [-s, 0, c]]
+    e[:3, 3] = t
+    return e
+
+
+def tensorf_e2e_case():
+    """SimpleTensoRF.forward from pixel ids in evaluation mode: ray generation with
+    the half pixel and the x-flip (SimpleTensoRF09.py:194-210), NDC rays and view
+    directions (:211-238), NDC / AABB marching (:353-401), the coarse VM model, and
+    the static-camera view directions of a separate view pose (:222-232); in NDC
+    (NeRF-LLFF), world and NeRF-Synthetic conventions.  The state_dicts are stored
+    so the drop-in loads the same weights."""
+    torch.manual_seed(0)
+    intr = np.array([[[400.0, 0, 252.0], [0, 400.0, 189.0], [0, 0, 1.0]]])
+    view_pose = _pose(-0.05, [0.1, 0.0, 0.2])
+    g = torch.Generator().manual_seed(61)
+    n = 64
+    pix = torch.stack([torch.zeros(n, dtype=torch.long), torch.randint(0, 504, (n,), generator=g),
+                       torch.randint(0, 378, (n,), generator=g)], 1)
+    out = {'pixel_id': pix.numpy(), 'intrinsics': intr, 'view_pose': view_pose}
+    # forward-facing camera near the origin for NDC; outside the box, looking at it, otherwise
+    cases = (('ndc', True, 'NeRF_LLFF', [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]], 1.0, 100.0, [0.05, -0.02, 0.3]),
+             ('world', False, 'NeRF_LLFF', [[-1.5] * 3, [1.5] * 3], 2.0, 6.0, [0.05, -0.02, 4.0]),
+             ('synthetic', False, 'NeRF_Synthetic', [[-1.5] * 3, [1.5] * 3], 2.0, 6.0, [0.05, -0.02, 4.0]))
+    for tag, ndc, database, bbox, near, far, t in cases:
+        ext = _pose(0.1, t)[None]
+        out[f'{tag}_extrinsics'] = ext
+        cfg = dict(tensorf_cfg(16 ** 3, [16, 4, 4], [48, 12, 12], bbox), views_positional_encoding_degree=2,
+                   features_positional_encoding_degree=2)
+        model = {'name': 'SimpleTensoRF09', 'coarse_model': cfg, 'learn_camera_focal_length': False,
+                 'learn_camera_rotation': False, 'learn_camera_translation': False, 'chunk': 1 << 16,
+                 'lindisp': False, 'perturb': True, 'white_bkgd': not ndc}
+        model_configs = {'intrinsics': intr, 'extrinsics': ext, 'resolution': (378, 504), 'near': near, 'far': far,
+                         'near_ndc': 0.0, 'far_ndc': 1.0, 'bounding_box': np.array(bbox)}
+        m = RT.SimpleTensoRF({'data_loader': {'ndc': ndc}, 'model': model, 'database': database}, model_configs)
+        with torch.no_grad():
+            for prm in m.coarse_model.matrices_density:
+                prm.add_(0.2)
+            for prm in m.coarse_model.vectors_density:
+                prm.add_(0.2)
+        m.eval()
+        batch = {'pixel_id': pix, 'num_frames': 1, 'iter_num': 1, 'sub_batch_index': 1, 'common_data': {}}
+        with torch.no_grad():
+            ret = m(batch, retraw=True)
+            sbatch = dict(batch, common_data={'view_intrinsic': None,
+                                              'processed_view_pose': torch.from_numpy(view_pose).float()[None]})
+            ret_s = m(sbatch, retraw=True, mode='static_camera')
+        for k, v in m.state_dict().items():
+            out[f'{tag}_sd.{k}'] = v.numpy()
+        for k, v in ret.items():
+            if isinstance(v, torch.Tensor):
+                out[f'{tag}_out.{k}'] = v.numpy()
+        for k in ('view_dirs', 'rgb_coarse', 'depth_coarse'):
+            out[f'{tag}_static.{k}'] = ret_s[k].numpy()
+        assert float(ret['acc_coarse'].max()) > 0.05, (tag, float(ret['acc_coarse'].max()))
+    return out
+
+
 def tensorf_cfg(vox, dens, col, bbox):
     return {'decomposition_type': 'VectorMatrix', 'num_samples_max': 1e6, 'num_components_density': dens,
             'num_components_color': col, 'bounding_box': bbox, 'num_voxels_initial': vox, 'num_voxels_final': vox,
@@ -942,6 +1003,7 @@ def main():
         'tensorf': tensorf_case,
         'tensorf_ndc': tensorf_ndc_case,
         'tensorf_realistic': tensorf_realistic_case,
+        'tensorf_e2e': tensorf_e2e_case,
         'tensorf_cp': tensorf_cp_case,
         'state_dicts': state_dict_case,
         'output_keys': output_keys_case,

@@ -40,3 +40,27 @@ def test_intrinsics_lookup_and_frozen_flags():
     np.testing.assert_allclose(ext.detach().numpy(), g['init_extrinsics'], rtol=0, atol=1e-6)
     groups = el.get_trainable_parameters({'lr_initial': 1e-3})
     assert [gr['name'] for gr in groups] == ['ExtrinsicsLearner_params'] and groups[0]['lr'] == 1e-3
+
+
+def test_pose_learning_is_refused_in_training_and_allowed_in_evaluation():
+    """With learn_camera_rotation / learn_camera_translation on, a training pass of
+    the drop-in raises NotImplementedError (the rays carry no gradient to the
+    extrinsics) before any work; evaluation mode passes the check."""
+    import pytest
+    import torch
+    from simple_rf_gb300.nerf import GbSimpleNeRF, check_pose_learning
+    mc = {'num_samples': 8, 'points_net_depth': 8, 'views_net_depth': 1, 'points_net_width': 256,
+          'views_net_width': 128, 'points_positional_encoding_degree': 10, 'views_positional_encoding_degree': 4,
+          'use_view_dirs': True, 'view_dependent_rgb': True, 'predict_visibility': False}
+    for rot, trans in ((True, False), (False, True)):
+        configs = {'data_loader': {'ndc': False}, 'model': {
+            'name': 'GbSimpleNeRF01', 'coarse_model': mc, 'learn_camera_focal_length': False,
+            'learn_camera_rotation': rot, 'learn_camera_translation': trans, 'chunk': 64, 'lindisp': False,
+            'netchunk': 64, 'perturb': False, 'raw_noise_std': 0.0, 'white_bkgd': False}}
+        model = GbSimpleNeRF(configs, {'intrinsics': np.eye(3)[None], 'extrinsics': np.eye(4)[None],
+                                       'resolution': (8, 8), 'near': 2.0, 'far': 6.0})
+        model.train()
+        with pytest.raises(NotImplementedError):
+            model({'pixel_id': torch.zeros(4, 3, dtype=torch.int32), 'num_frames': 1})
+        model.eval()
+        check_pose_learning(model)

@@ -359,3 +359,53 @@ def test_alpha_mask_rebuild_matches_reference(golden):
     assert np.mean(vol != ref) <= 1e-3, np.mean(vol != ref)
     voxel = (g['bbox'][1] - g['bbox'][0]) / (g['res'] - 1)
     assert np.all(np.abs(box - g['amask_box']) <= voxel * 1.0001), (box, g['amask_box'])
+
+
+@pytest.mark.parametrize('tag', ['ndc', 'world', 'synthetic'])
+def test_drop_in_tensorf_forward_from_pixels_matches_reference(golden, tag):
+    """GbSimpleTensoRF.forward from pixel ids against SimpleTensoRF.forward in
+    evaluation mode (golden tensorf_e2e): rays with the half pixel and the x-flip,
+    NDC rays and view directions, the NeRF-Synthetic convention, NDC / AABB
+    marching, the coarse VM model, and the static-camera view directions of a
+    separate view pose (SimpleTensoRF09.py:194-238, 353-401)."""
+    from simple_rf_gb300.tensorf_model import GbSimpleTensoRF
+    g = golden('tensorf_e2e')
+    ndc = tag == 'ndc'
+    bbox = [[-1.5, -1.67, -1.0], [1.5, 1.67, 1.0]] if ndc else [[-1.5] * 3, [1.5] * 3]
+    cfg = dict(_tcfg(), bounding_box=bbox, num_components_density=[16, 4, 4], num_components_color=[48, 12, 12],
+               num_voxels_initial=16 ** 3, num_voxels_final=16 ** 3, features_dimension_color=27,
+               num_units_color_predictor=128)
+    model = {'name': 'GbSimpleTensoRF01', 'coarse_model': cfg, 'learn_camera_focal_length': False,
+             'learn_camera_rotation': False, 'learn_camera_translation': False, 'chunk': 1 << 16, 'lindisp': False,
+             'perturb': True, 'white_bkgd': not ndc}
+    mc = {'intrinsics': g['intrinsics'], 'extrinsics': g[f'{tag}_extrinsics'], 'resolution': (378, 504),
+          'near': 1.0 if ndc else 2.0, 'far': 100.0 if ndc else 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0,
+          'bounding_box': np.array(bbox)}
+    database = 'NeRF_Synthetic' if tag == 'synthetic' else 'NeRF_LLFF'
+    m = GbSimpleTensoRF({'data_loader': {'ndc': ndc}, 'model': model, 'database': database}, mc)
+    sd = {k[len(tag) + 4:]: torch.from_numpy(g[k]) for k in g.files if k.startswith(f'{tag}_sd.')}
+    m.load_state_dict(sd)
+    m = m.to(DEV).eval()
+    pix = torch.from_numpy(g['pixel_id']).to(DEV)
+    batch = {'pixel_id': pix, 'num_frames': 1, 'iter_num': 1, 'sub_batch_index': 1, 'common_data': {}}
+    with torch.no_grad():
+        ret = m(batch, retraw=True)
+        sbatch = dict(batch, common_data={'view_intrinsic': None, 'processed_view_pose':
+                                          torch.from_numpy(g['view_pose']).float()[None].to(DEV)})
+        ret_s = m(sbatch, retraw=True, mode='static_camera')
+    ref = {k[len(tag) + 5:]: g[k] for k in g.files if k.startswith(f'{tag}_out.')}
+    got = {k: v.cpu().numpy() for k, v in ret.items() if isinstance(v, torch.Tensor)}
+    assert set(ref) <= set(got), set(ref) - set(got)
+    keep = threshold_stable(got['weights_coarse'], ref['weights_coarse'])
+    assert keep.sum() >= keep.size - 1, int((~keep).sum())
+    for k in ('rays_o', 'rays_d', 'view_dirs', 'z_vals_coarse') + (('rays_o_ndc', 'rays_d_ndc') if ndc else ()):
+        np.testing.assert_allclose(got[k], ref[k], rtol=1e-5, atol=1e-6 * max(1.0, float(np.abs(ref[k]).max())),
+                                   err_msg=k)
+    for k in ('rgb_coarse', 'depth_coarse', 'acc_coarse', 'weights_coarse', 'depth_var_coarse') + \
+            (('depth_ndc_coarse',) if ndc else ()):
+        np.testing.assert_allclose(got[k][keep], ref[k][keep], rtol=1e-5,
+                                   atol=1e-6 * max(1.0, float(np.abs(ref[k]).max())), err_msg=k)
+    for k in ('view_dirs', 'rgb_coarse', 'depth_coarse'):
+        r = g[f'{tag}_static.{k}']
+        np.testing.assert_allclose(ret_s[k].cpu().numpy()[keep], r[keep], rtol=1e-5,
+                                   atol=1e-6 * max(1.0, float(np.abs(r).max())), err_msg='static ' + k)
