@@ -251,6 +251,35 @@ def roofline_wgrad(dev, hbm_peak, peak_tflops, peak_kind, reps=50):
             'share_of_step': 'largest kernel of the training step (launch list under profiles/)'}
 
 
+def read_probe(dev, nbytes, passes, reps=5):
+    """Read rate (GB/s) of srf_read_probe over an nbytes device buffer read
+    `passes` times per launch (best of reps launches, CUDA events)."""
+    import ctypes
+    import torch
+    from simple_rf_gb300 import _lib
+    buf = torch.ones(nbytes // 4, device=dev)
+    sink = torch.empty(int(_lib.load().srf_read_probe_blocks()), device=dev)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def launch():
+        _lib.call('srf_read_probe', ctypes.c_void_p(buf.data_ptr()), nbytes, passes,
+                  ctypes.c_void_p(sink.data_ptr()), st)
+    launch()
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch()
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1000.0
+        best = t if best is None else min(best, t)
+    del buf, sink
+    torch.cuda.empty_cache()
+    return nbytes * passes / best / 1e9
+
+
 def kernel_rooflines(hbm_peak, peak_kind):
     """The memory-bound kernels of the path timed alone (CUDA events, 20 launches
     after 3 warm-up launches) with their algorithmic bytes per launch:
@@ -269,31 +298,23 @@ def kernel_rooflines(hbm_peak, peak_kind):
             ('vm', dict(rays=1216, samples=1024, comps=16, kind='density', res=300, backward=False)),
             ('vm', dict(rays=1216, samples=1024, comps=16, kind='density', res=300, backward=True))]
     out = []
+    # the VM planes stay L2-resident: their gathers are bounded by the L2 read rate,
+    # measured here with the same 16-byte loads over a 48 MB buffer (read 40 times)
+    l2 = read_probe(torch.device('cuda', torch.cuda.current_device()), 48 << 20, 40)
     for which, kw in runs:
         args = _ap.Namespace(reps=20, warmup=3, **kw)
         r = getattr(bk, which)(args)
-        out.append({'kernel': r['kernel'], 'workload': {k: v for k, v in kw.items() if k != 'backward'},
-                    'launch_ms': round(r['ms'], 4), 'algorithmic_bytes_per_launch': int(r['bytes']),
-                    'achieved': round(r['gbs'], 1), 'peak': hbm_peak, 'unit': 'GB/s',
-                    'frac': round(r['gbs'] / hbm_peak, 4), 'peak_source': peak_kind + ' copy bandwidth'})
+        row = {'kernel': r['kernel'], 'workload': {k: v for k, v in kw.items() if k != 'backward'},
+               'launch_ms': round(r['ms'], 4), 'algorithmic_bytes_per_launch': int(r['bytes']),
+               'achieved': round(r['gbs'], 1), 'peak': hbm_peak, 'unit': 'GB/s',
+               'frac': round(r['gbs'] / hbm_peak, 4), 'peak_source': peak_kind + ' copy bandwidth'}
+        if which == 'vm':
+            row.update(bound='l2', l2_read_peak=round(l2, 1), frac_of_l2_read=round(r['gbs'] / l2, 4),
+                       note='planes L2-resident: frac against the HBM copy peak is not a roofline; '
+                            'frac_of_l2_read is against the measured L2 streaming-read rate')
+        out.append(row)
         torch.cuda.empty_cache()
     return out
-
-
-def fp32_plain_block(ws, k32, t_fp):
-    """The FP32 SIMT step with its arithmetic rate: 6 x 593,408 MAC-FLOP per sample
-    over 64 + 64 + 128 samples per ray, against the FP32 FMA peak of the SMs the
-    GEMM fills (152 SMs x 128 FP32 lanes x 2 FLOP x the maximum SM clock)."""
-    rate = job_rays_per_s(ws, N_RAYS, k32, t_fp)
-    tflops = rate * 6 * MACS_PER_SAMPLE * (N_COARSE + N_COARSE + N_FINE) / 1e12 / ws
-    try:
-        with open(os.path.join(REPO, 'MEASURED_PEAKS.json')) as f:
-            mhz = float(json.load(f)['sm_max_mhz'])
-    except Exception:
-        mhz = 2070.0
-    peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-    return {'value': round(rate, 1), 'unit': 'rays/s', 'ms_per_step': round(1e3 * t_fp / k32, 3), 'steps': k32,
-            'tflops': round(tflops, 1), 'fp32_simt_peak_tflops': round(peak, 1), 'frac_of_fp32_peak': round(tflops / peak, 3)}
 
 
 def rgb_agreement(step_cls, batch, dev):
@@ -373,11 +394,24 @@ def time_tensorf(precision, steps, dev, stream, graph=True):
     for i in range(3):
         st.step(*batches[i % 4])
     torch.cuda.synchronize(dev)
-    t = time_steps(lambda i: st.step(*batches[i % 4]), steps, stream)
+    seen = {'surface': 0, 'valid': 0}
+
+    def one(i):
+        st.step(*batches[i % 4])
+        if not graph:
+            # the uncaptured step reads its sample counts on the host every step
+            for c in st.last['samples']:
+                seen['surface'] += c['surface']
+                seen['valid'] += c['valid']
+    t = time_steps(one, steps, stream)
     samples = st.sample_counts() if graph else st.last['samples']
+    if graph:
+        # counts of the last step only (a captured step reads none on the host)
+        seen = {k: steps * sum(c[k] for c in samples) for k in seen}
     counts = {m.name: dict(c) for m, c in zip(models, samples)}
     out = {'ms_per_step': round(1e3 * t / steps, 3), 'rays_per_s': round(8192 * steps / t, 1), 'steps': steps,
-           'samples_per_step': counts, 'cuda_graph': graph}
+           'samples_per_step': counts, 'cuda_graph': graph,
+           'surface_samples_per_s': round(seen['surface'] / t, 1), 'valid_samples_per_s': round(seen['valid'] / t, 1)}
     if graph:
         out['capacities'] = st.caps
         out['recaptures'] = st.recaptures
@@ -598,7 +632,7 @@ def run_ours(args):
         # the same warm-up and timed steps for both (surface-sample counts drift as the grids train)
         variants['tensorf_fp16'] = time_tensorf('fp16', args.steps, dev, stream, graph=False)
         variants['tensorf_fp16_graph'] = time_tensorf('fp16', args.steps, dev, stream, graph=True)
-        variants['tensorf_fp32'] = time_tensorf('fp32', 5, dev, stream, graph=False)
+        variants['tensorf_fp32'] = time_tensorf('fp32', args.steps, dev, stream, graph=False)
         from simple_rf_gb300.bench_tensorf import ray_batch_sweep
         variants['tensorf_sweep'] = ray_batch_sweep(dev)
         variants['render'] = time_render(dev, stream)
@@ -641,6 +675,11 @@ def run_ours(args):
                     'fp32_plain': variants['tensorf_fp32'],
                     'speedup_fp16_vs_fp32_plain': round(variants['tensorf_fp16']['rays_per_s'] /
                                                         variants['tensorf_fp32']['rays_per_s'], 2),
+                    'speedup_fp16_vs_fp32_plain_per_surface_sample': round(
+                        variants['tensorf_fp16']['surface_samples_per_s'] /
+                        variants['tensorf_fp32']['surface_samples_per_s'], 2),
+                    'like_for_like': 'both uncaptured arms: same seed, same 3 warm-up and timed steps, sample counts '
+                                     'summed over the timed steps',
                     'speedup_fp16_graph_vs_fp32_plain': round(variants['tensorf_fp16_graph']['rays_per_s'] /
                                                               variants['tensorf_fp32']['rays_per_s'], 2),
                     'ray_batch_sweep': variants['tensorf_sweep']},

@@ -43,6 +43,14 @@ const char* srf_last_cuda_error(void);
 /* Number of kernels this library has launched (or captured into a graph) in
  * this process; used to count launches per training step. */
 int64_t srf_launch_count(void);
+
+/* Read-bandwidth probe (a measurement utility; no counterpart in the reference):
+ * streams `bytes` (multiple of 16, 16-byte aligned) of `buf` `passes` times with
+ * 16-byte loads and writes one float per block to sink (srf_read_probe_blocks()
+ * floats).  A buffer that fits in L2 gives the L2 read rate that bounds the VM
+ * plane gathers (their planes stay L2-resident); a larger one the HBM read rate. */
+int srf_read_probe_blocks(void);
+int srf_read_probe(const void* buf, int64_t bytes, int passes, float* sink, void* stream);
 /* Reads and clears the device-side error flag (bounded-wait timeouts, index
  * range violations) that kernels set instead of trapping.  Synchronises `stream`.
  * Writes the flag value (0 = clean) to *flag_out. */

@@ -69,6 +69,8 @@ _SIGS = {
     'srf_last_cuda_error': (c_char_p, []),
     'srf_read_device_flag': (c_int, [ctypes.POINTER(c_int), P]),
     'srf_stream_create': (c_int, [ctypes.POINTER(P)]),
+    'srf_read_probe_blocks': (c_int, []),
+    'srf_read_probe': (c_int, [P, c_int64, c_int, P, P]),
     'srf_stream_destroy': (c_int, [P]),
     'srf_pixel_rays': (c_int, [P, P, P, c_int, c_int, P, P, P]),
     'srf_ndc_rays': (c_int, [P, P, P, P, c_int, c_int, c_int, c_float, P, P, P, P]),

@@ -173,3 +173,49 @@ extern "C" int srf_read_device_flag(int* flag_out, void* stream) {
     *flag_out = host;
     return SRF_OK;
 }
+
+// ------------------------------------------------------ bandwidth probe ----
+// Streams a buffer `passes` times with 16-byte loads (grid-stride, every block
+// walks the whole buffer's share of its threads), reducing to one float per
+// block so the loads cannot be dropped.  A buffer smaller than L2 measures the
+// L2 read rate the VM gathers are bounded by; a larger one the HBM read rate.
+namespace {
+__global__ void __launch_bounds__(512) read_probe_kernel(const float4* __restrict__ buf, int64_t n4, int passes,
+                                                         float* __restrict__ sink) {
+    float acc = 0.f;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int p = 0; p < passes; ++p) {
+        for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4; i += stride) {
+            float4 v = __ldcg(buf + i);
+            acc += (v.x + v.y) + (v.z + v.w);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ float part[16];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) s += part[w];
+        sink[blockIdx.x] = s;
+    }
+}
+}  // namespace
+
+extern "C" int srf_read_probe_blocks(void) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        return 0;
+    return 4 * sms;
+}
+
+extern "C" int srf_read_probe(const void* buf, int64_t bytes, int passes, float* sink, void* stream) {
+    if (!buf || !sink) return SRF_ERR_NULL;
+    if (bytes < 16 || (bytes & 15) || passes < 1 || (reinterpret_cast<uintptr_t>(buf) & 15)) return SRF_ERR_SHAPE;
+    int blocks = srf_read_probe_blocks();
+    if (blocks <= 0) return SRF_ERR_CUDA;
+    read_probe_kernel<<<blocks, 512, 0, srf::as_stream(stream)>>>(static_cast<const float4*>(buf), bytes / 16, passes,
+                                                                   sink);
+    return srf::launch_status();
+}

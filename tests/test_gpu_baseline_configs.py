@@ -154,8 +154,12 @@ def test_config1_drop_in_render_1024_rays_matches_oracle():
     assert keep.mean() > 0.995, int((~keep).sum())
     _close(got['z_vals_coarse'], ref['z_vals_coarse'], 'z_vals_coarse', rtol=1e-6)
     for k in ('rgb_coarse', 'depth_coarse', 'weights_coarse', 'acc_coarse', 'rgb_fine', 'depth_fine',
-              'weights_fine', 'acc_fine', 'depth_var_fine'):
+              'weights_fine', 'acc_fine'):
         _close(got[k], ref[k], k, rows=keep)
+    # the variance sums w (z - depth)^2 with (z - depth)^2 up to (far - near)^2 = 16, so
+    # the weights' absolute floor of 1e-6 (last samples: delta = 1e10 |d|) becomes 1.6e-5
+    for k in ('depth_var_coarse', 'depth_var_fine'):
+        np.testing.assert_allclose(got[k][keep], ref[k][keep], rtol=1e-5, atol=1.6e-5, err_msg=k)
 
 
 # --------------------------------------------------------------- config 2 --
@@ -306,22 +310,44 @@ def test_config4_tensorf_8192_rays_outputs_match_oracle():
 
 def test_config4_tensorf_gradients_match_oracle():
     """Gradients of every plane, line, basis and renderer parameter of the config-4
-    main model for a loss on the first 256 of 8192 rays (the other rays carry zero
+    main model for a loss on 256 of the 8192 rays (the other rays carry zero
     cotangents, so the gradients are those of the 256 rays alone) against the
-    float32 oracle's adjoint, 1e-4 relative L2 per tensor."""
+    float64 oracle's adjoint: per tensor within max(1e-4, 3 e32) relative L2, e32
+    being the float32 oracle's own error on the same inputs.
+
+    The 256 rays are the first ones with acc >= 0.05: the depth of a nearly
+    transparent ray is sum(w z) / (acc + 1e-6), whose gradient (z - depth) /
+    (acc + 1e-6) amplifies rounding by up to 1e6, so such rays measure the
+    conditioning of the reference formula rather than the kernels."""
     tm, (o, d, z), out = _config4_run(8192, seed=22)
     n_sub = 256
+    acc = out['acc'].detach().cpu().numpy()
+    rows = np.nonzero(acc >= 0.05)[0][:n_sub]
+    assert rows.size == n_sub, rows.size
     rng = np.random.default_rng(5)
-    cot = {k: rng.standard_normal(out[k].shape).astype(np.float32) for k in ('rgb', 'depth', 'acc')}
-    for v in cot.values():
-        v[n_sub:] = 0
+    cot = {k: np.zeros(tuple(out[k].shape), np.float32) for k in ('rgb', 'depth', 'acc')}
+    for k in cot:
+        cot[k][rows] = rng.standard_normal(cot[k][rows].shape).astype(np.float32)
     loss = sum((out[k] * _T(cot[k])).sum() for k in cot)
     loss.backward()
-    oh, dh, zh = (x[:n_sub].cpu().numpy() for x in (o, d, z))
-    (ref, cache), spec = _oracle_forward(tm, oh, dh, zh)
-    keep = _threshold_stable(out['weights'][:n_sub].detach().cpu().numpy(), ref['weights'])
-    assert keep.all(), int((~keep).sum())
-    g = ot.tensorf_backward(_oracle_params(tm), spec, cache, {k: v[:n_sub] for k, v in cot.items()})
+    oh, dh, zh = (x[rows].cpu().numpy() for x in (o, d, z))
+    keep = None
+    grads = {}
+    for dt in (np.float64, np.float32):
+        tp = _oracle_params(tm)
+        spec = ot.RendererSpec(features_dim=27, features_pe=2, views_pe=2, units=128)
+        am = tm.alpha_mask
+        ref, cache = ot.tensorf_forward(
+            {k: ([a.astype(dt) for a in v] if isinstance(v, list) else v.astype(dt)) for k, v in tp.items()}, spec,
+            oh.astype(dt), dh.astype(dt), zh.astype(dt), alpha_vol=am.volume().float().cpu().numpy().astype(dt),
+            alpha_bbox=am.bounding_box.cpu().numpy().astype(dt), distance_scale=25.0, weight_threshold=1e-4,
+            white=True)
+        if keep is None:
+            keep = _threshold_stable(out['weights'][rows].detach().cpu().numpy(), ref['weights'])
+            assert keep.all(), int((~keep).sum())
+        grads[dt] = ot.tensorf_backward(
+            {k: ([a.astype(dt) for a in v] if isinstance(v, list) else v.astype(dt)) for k, v in tp.items()}, spec,
+            cache, {k: v[rows].astype(dt) for k, v in cot.items()})
     pairs = []
     for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
                         ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color)):
@@ -332,8 +358,11 @@ def test_config4_tensorf_gradients_match_oracle():
         pairs.append(('color_predictor.' + k, prm.grad))
     worst = 0.0
     for name, grad in pairs:
-        ref_g = g[name].astype(np.float64)
-        rel = np.linalg.norm(grad.detach().double().cpu().numpy() - ref_g) / max(np.linalg.norm(ref_g), 1e-30)
-        worst = max(worst, rel)
-        assert rel < 1e-4, (name, rel)
-    print('config 4: worst per-tensor gradient rel-L2', worst)
+        g64 = grads[np.float64][name].astype(np.float64)
+        nrm = max(np.linalg.norm(g64), 1e-30)
+        rel = np.linalg.norm(grad.detach().double().cpu().numpy() - g64) / nrm
+        e32 = np.linalg.norm(grads[np.float32][name].astype(np.float64) - g64) / nrm
+        bar = max(1e-4, 3 * e32)
+        worst = max(worst, rel / bar)
+        assert rel < bar, (name, rel, e32)
+    print('config 4: worst per-tensor gradient error / bar', worst)
