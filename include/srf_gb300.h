@@ -254,6 +254,39 @@ int srf_composite_forward(const srf_composite_args* args, void* stream);
 /* Adjoint: reverse-scan transmittance gradient, recomputing the forward per ray. */
 int srf_composite_backward(const srf_composite_args* args, void* stream);
 
+/* A training loss evaluated inside compositing, so that the loss gradient feeds
+ * the compositing adjoint without a round trip of the per-ray outputs or the
+ * (N,S) weights through memory:
+ *   rgb_weight * mean_rays mean_channels (rgb - target_rgb)^2
+ *       (MSE14.compute_mse, src/loss_functions/MSE14.py:81-94; rgb after the white background)
+ * + depth_weight / n_depth_rays * sum over depth_mask rays of |depth - target_depth|
+ *       (the training step's L1 depth term) or (depth - target_depth)^2 with depth_squared
+ *       (SparseDepthMSE14.compute_depth_loss, src/loss_functions/SparseDepthMSE14.py:84-97)
+ * + mc_weight / n_mc_rays * sum over mc_mask rays of the binned entropy of the weights
+ *       (MassConcentrationLoss06.compute_entropy_loss, src/loss_functions/MassConcentrationLoss06.py:63-83;
+ *        num_bins <= 32, 0 = no entropy term).
+ * NULL targets / masks: the term is off / every ray counts. */
+typedef struct {
+    const float* target_rgb;       /* (N,3) or NULL */
+    float rgb_weight;
+    const float* target_depth;     /* (N) or NULL   */
+    const uint8_t* depth_mask;     /* (N) or NULL   */
+    int n_depth_rays;
+    float depth_weight;
+    int depth_squared;
+    int num_bins;
+    const uint8_t* mc_mask;        /* (N) or NULL   */
+    int n_mc_rays;
+    float mc_weight;
+    float* loss;                   /* device float the forward adds the loss value to */
+} srf_composite_loss;
+/* srf_composite_forward that also adds the loss value to *loss->loss. */
+int srf_composite_forward_loss(const srf_composite_args* args, const srf_composite_loss* loss, void* stream);
+/* srf_composite_backward whose output gradients are the loss's (recomputed from the
+ * ray's samples) plus any g_* the args carry (e.g. a depth-consistency term).
+ * Both: rays of at most 256 samples (SRF_ERR_UNSUPPORTED beyond). */
+int srf_composite_backward_loss(const srf_composite_args* args, const srf_composite_loss* loss, void* stream);
+
 /* out (N,C) = sum_s weights (N,S) * values (N,S,C), C <= 4, and its adjoint.
  * Replaces LowRankTensor.volume_render (src/models/SimpleTensoRF09.py:816-819). */
 int srf_weighted_sum(const float* weights, const float* values, int n_rays, int n_samples, int channels, float* out,
@@ -310,6 +343,38 @@ int srf_tensorf_sample_mask(const float* rays_o, const float* rays_d, const floa
 /* Alpha-mask query alone: out[p] = (trilinear(volume, pts_norm[p]) > 0). */
 int srf_alpha_mask_query(const float* alpha_volume, int vol_d, int vol_h, int vol_w, const float* pts_norm,
                          int64_t n_pts, uint8_t* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Grid maintenance (planes (H,W,R) and lines (L,1,R) channels-last)          */
+/* ------------------------------------------------------------------------ */
+
+/* Dense alpha on the nodes of the grid's res[0] x res[1] x res[2] lattice:
+ * node (x,y,z) at bbox_lo (1 - s) + bbox_hi s with s = torch.linspace(0,1,res)
+ * per axis; alpha = clamp(1 - exp(-sigma step), 0, 1), sigma the activated VM
+ * density (density_mode 0 ReLU, 1 softplus(x + offset)), 0 where the optional
+ * current alpha mask (volume + box as in srf_tensorf_sample_mask) is empty.
+ * alpha is written z-major, (res[2], res[1], res[0]).  bbox, alpha_bbox: host (2,3).
+ * Replaces LowRankTensor.update_alpha_mask's dense pass and compute_alpha
+ * (src/models/SimpleTensoRF09.py:849-858, 878-897). */
+int srf_vm_alpha_grid(const srf_vm_grid* grid, const float* bbox, const float* alpha_volume, int vol_d, int vol_h,
+                      int vol_w, const float* alpha_bbox, float step, int density_mode, float density_offset,
+                      float* alpha, void* stream);
+/* 3x3x3 max-pool (padding 1, stride 1) of alpha (gz, gy, gx) and threshold
+ * (>= threshold -> 1, else 0) into volume (gz, gy, gx); bounds (6 device ints)
+ * receive (gx-1-min x, gy-1-min y, gz-1-min z, max x, max y, max z) over the
+ * occupied nodes, all -1 when none is occupied.
+ * Replaces SimpleTensoRF09.py:859-874 (max_pool3d, threshold, occupied box). */
+int srf_alpha_pool_threshold(const float* alpha, int gx, int gy, int gz, float threshold, float* volume,
+                             int32_t* bounds, void* stream);
+/* Bilinear resampling with align_corners=True of a channels-last (h, w, comps)
+ * plane (or a (h, 1, comps) line) to (h_new, w_new, comps).
+ * Replaces F.interpolate in upsample_vectors_and_matrices (SimpleTensoRF09.py:1284-1301). */
+int srf_resample_grid(const float* src, int h, int w, int comps, float* dst, int h_new, int w_new, void* stream);
+/* Crop rows [row0, row0 + h_new) x columns [col0, col0 + w_new) of a channels-last
+ * (h, w, comps) plane or line into dst (h_new, w_new, comps).
+ * Replaces the slicing of shrink_tensor (SimpleTensoRF09.py:1303-1320). */
+int srf_crop_grid(const float* src, int h, int w, int comps, int row0, int col0, float* dst, int h_new, int w_new,
+                  void* stream);
 
 /* Stream compaction: idx[0..count) = positions where mask != 0 (ascending).
  * count is written to *count_dev (device int).  Workspace: srf_compact_workspace_size. */
@@ -481,6 +546,18 @@ int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const
                                  const float* intrinsics0, const float* images, int height, int width, int channels,
                                  int patch_w, int patch_h, float rmse_threshold, uint8_t* mask1, uint8_t* mask2,
                                  void* stream);
+/* The same masks for CoarseFineConsistencyLoss34.compute_loss_nerf
+ * (src/loss_functions/CoarseFineConsistencyLoss34.py:89-168): depth1 the main coarse
+ * depth, depth2 the main fine depth, and no rule for rays whose two reprojections
+ * both leave the image (AugmentationsDepthLoss11's :176-181 is absent there).  The
+ * loss is then compute_depth_mse(depth_coarse, depth_fine, mask2) as above, and on
+ * sparse-depth rays compute_loss_sd (:170-187): srf_depth_mse_loss of the coarse
+ * depth against the detached fine depth over those rays. */
+int srf_coarse_fine_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth_coarse,
+                                       const float* depth_fine, const int32_t* pixel_ids, int n_rays,
+                                       const float* poses, int n_views, const float* intrinsics0, const float* images,
+                                       int height, int width, int channels, int patch_w, int patch_h,
+                                       float rmse_threshold, uint8_t* mask1, uint8_t* mask2, void* stream);
 /* One grid of the total-variation loss: element (c, h, w) of the (1, channels,
  * height, width) parameter at data[c*stride_channel + h*stride_height +
  * w*stride_width] (channels-last: stride_channel 1); grad (may be NULL) has the
@@ -517,6 +594,33 @@ int srf_autotune_clear(void);
 /* *counter_dev += value on the stream (advances a graph-replayed step count),
  * unless skip_dev != NULL and *skip_dev != 0. */
 int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, void* stream);
+
+/* Device-side batch assembly for cached-ray training (replaces
+ * DataPreprocessor10.select_batch_indices and load_nerf_cached_batch,
+ * src/data_preprocessors/DataPreprocessor10.py:496-549, whose host numpy shuffle and
+ * copies keep the training iteration out of a CUDA graph).  Batch b (read from
+ * *batch_counter_dev; 0 when NULL) takes rays ((b mod B) n_rays + i) of epoch
+ * (b div B)'s order, B = pool_size div n_rays; each epoch's order is a fresh keyed
+ * random permutation of [0, pool_size) (seed, epoch), so every epoch visits
+ * B n_rays distinct rays (the pool_size mod n_rays rays an epoch leaves over are
+ * the ones the reference's shorter last slice would take).  Gathers, per batch ray
+ * i: out_index[i] (optional), the pool row's pixel id (image, x, y) (optional),
+ * its `channels` floats of pool_values (e.g. the target colour), and the camera
+ * of its image from intrinsics (n_views,3,3) / extrinsics (n_views,4,4)
+ * (optional: per-ray copies for srf_pixel_rays).  With pool_rows (pool_size
+ * int32, optional) the permuted positions index that list and the gathers read
+ * row pool_rows[...] (the sparse-depth pixels, a subset of the cached rays).
+ * Advance the counter with srf_counter_add after the step.  pool_size <= 2^30. */
+int srf_batch_assemble(const int32_t* pool_rows, const int32_t* pool_pixel_id, const float* pool_values, int channels,
+                       int64_t pool_size, int n_rays, uint64_t seed, const int32_t* batch_counter_dev,
+                       const float* intrinsics,
+                       const float* extrinsics, int n_views, int32_t* out_pixel_id, float* out_values,
+                       int32_t* out_index, float* out_intrinsics, float* out_extrinsics, void* stream);
+/* n uniforms in [0, 1) from a counter-based hash of (seed, *counter_dev, stream_id,
+ * i): the stratified and inverse-CDF uniforms of a captured step
+ * (torch.rand at src/models/SimpleNeRF17.py:355, 397), fresh on every replay as the
+ * counter advances. */
+int srf_uniforms(float* u, int64_t n, uint64_t seed, const int32_t* counter_dev, int stream_id, void* stream);
 /* Sample points pts (N*S,3) = o + d * z (src/models/SimpleNeRF17.py:213-215). */
 int srf_ray_points(const float* rays_o, const float* rays_d, const float* z, int n_rays, int n_samples, float* pts,
                    void* stream);

@@ -108,12 +108,16 @@ def patch(images, img, y, x, hpy, hpx):
 
 
 def reprojection_masks(depth1, depth2, rays_o, rays_d, pixel_ids, poses, k0, images, patch_size=(5, 5),
-                       rmse_threshold=0.1):
+                       rmse_threshold=0.1, both_invalid_rule=True):
     """AugmentationsDepthLoss11.compute_loss_nerf (src/loss_functions/AugmentationsDepthLoss11.py:105-190)
     on rays that are all NeRF rays: returns (mask1, mask2, pos1, pos2), mask1 where
     depth1 reprojects to the more consistent patch in the nearest other view (so
     depth2 is pulled towards depth1 there) and mask2 the reverse; pos* the
-    unrounded reprojected pixel positions (for boundary checks)."""
+    unrounded reprojected pixel positions (for boundary checks).
+    both_invalid_rule=False gives CoarseFineConsistencyLoss34.compute_loss_nerf
+    (src/loss_functions/CoarseFineConsistencyLoss34.py:89-168, depth1 coarse,
+    depth2 fine), which lacks the rule for rays whose reprojections both leave
+    the image (AugmentationsDepthLoss11.py:176-181)."""
     f = np.float32
     v, h, w, _ = images.shape
     hpx, hpy = patch_size[0] // 2, patch_size[1] // 2
@@ -141,9 +145,10 @@ def reprojection_masks(depth1, depth2, rays_o, rays_d, pixel_ids, poses, k0, ima
         rm2[r] = np.sqrt(np.mean(np.square(pa - b2)))
     m1 = ((rm1 < rm2) | ~v2) & (rm1 < rmse_threshold) & v1 & va
     m2 = ((rm2 < rm1) | ~v1) & (rm2 < rmse_threshold) & v2 & va
-    both_invalid = ~(v1 | v2)
-    m1 |= both_invalid & (depth1 > depth2)
-    m2 |= both_invalid & (depth2 > depth1)
+    if both_invalid_rule:
+        both_invalid = ~(v1 | v2)
+        m1 |= both_invalid & (depth1 > depth2)
+        m2 |= both_invalid & (depth2 > depth1)
     return m1, m2, pos1, pos2
 
 
@@ -188,3 +193,26 @@ def tv_loss(components, weight=1.0):
 def tv_iter_weight(lr_decay_ratio, lr_decay_iters, iter_num):
     """TotalVariationLoss04.get_iter_weight (:118-120)."""
     return lr_decay_ratio ** ((iter_num + 1) / lr_decay_iters)
+
+
+def coarse_fine_consistency_loss(depth_coarse, depth_fine, nerf_mask, sd_mask, rays_o, rays_d, pixel_ids, poses, k0,
+                                 images, patch_size=(5, 5), rmse_threshold=0.1):
+    """CoarseFineConsistencyLoss34.compute_loss (src/loss_functions/CoarseFineConsistencyLoss34.py:30-88):
+    on the NeRF rays, the reprojection masks without the both-invalid rule and the
+    depth term of :164-167 (as reprojection_depth_loss: mean over the NeRF rays of
+    mask2 (coarse - fine)^2, gradient into the coarse depth); on the sparse-depth
+    rays (compute_loss_sd, :170-187) the mean squared difference of the coarse
+    depth and the detached fine depth.  Returns (loss, d/d coarse, d/d fine, mask1, mask2)."""
+    nerf = np.asarray(nerf_mask, bool)
+    dc, df = np.asarray(depth_coarse), np.asarray(depth_fine)
+    m1, m2, _, _ = reprojection_masks(dc[nerf], df[nerf], rays_o[nerf], rays_d[nerf], pixel_ids[nerf], poses, k0,
+                                      images, patch_size, rmse_threshold, both_invalid_rule=False)
+    loss, g1, g2 = reprojection_depth_loss(dc[nerf], df[nerf], m1, m2)
+    gc, gf = np.zeros_like(dc), np.zeros_like(df)
+    gc[nerf], gf[nerf] = g1, g2
+    if sd_mask is not None and np.any(sd_mask):
+        sd = np.asarray(sd_mask, bool)
+        l_sd, g_sd, _ = depth_mse(dc[sd], df[sd])
+        loss = loss + l_sd
+        gc[sd] += g_sd
+    return loss, gc, gf, m1, m2

@@ -35,6 +35,12 @@ class CompositeArgs(ctypes.Structure):
                 ('d_sigma', P), ('d_rgb', P)]
 
 
+class CompositeLoss(ctypes.Structure):
+    _fields_ = [('target_rgb', P), ('rgb_weight', c_float), ('target_depth', P), ('depth_mask', P),
+                ('n_depth_rays', c_int), ('depth_weight', c_float), ('depth_squared', c_int), ('num_bins', c_int),
+                ('mc_mask', P), ('n_mc_rays', c_int), ('mc_weight', c_float), ('loss', P)]
+
+
 class RendererDesc(ctypes.Structure):
     _fields_ = [('n_comp', c_int), ('features', c_int), ('units', c_int), ('features_pe_degree', c_int),
                 ('views_pe_degree', c_int), ('view_dependent', c_int)]
@@ -53,6 +59,8 @@ class AdamTensor(ctypes.Structure):
     _fields_ = [('param', P), ('grad', P), ('exp_avg', P), ('exp_avg_sq', P), ('n', c_int64), ('lr', c_float)]
 
 
+SRF_OK, SRF_ERR_NULL, SRF_ERR_SHAPE, SRF_ERR_ALIGN, SRF_ERR_WORKSPACE, SRF_ERR_CUDA = 0, 1, 2, 3, 4, 5
+SRF_ERR_TIMEOUT, SRF_ERR_RANGE, SRF_ERR_UNSUPPORTED = 6, 7, 8
 SRF_COMPOSITE_NDC = 1
 SRF_COMPOSITE_WHITE_BKGD = 2
 SRF_COMPOSITE_EXP_PREFIX = 4
@@ -97,6 +105,8 @@ _SIGS = {
                                c_int, c_int64, P]),
     'srf_composite_forward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
     'srf_composite_backward': (c_int, [ctypes.POINTER(CompositeArgs), P]),
+    'srf_composite_forward_loss': (c_int, [ctypes.POINTER(CompositeArgs), ctypes.POINTER(CompositeLoss), P]),
+    'srf_composite_backward_loss': (c_int, [ctypes.POINTER(CompositeArgs), ctypes.POINTER(CompositeLoss), P]),
     'srf_weighted_sum': (c_int, [P, P, c_int, c_int, c_int, P, P]),
     'srf_weighted_sum_backward': (c_int, [P, P, P, c_int, c_int, c_int, P, P, P]),
     'srf_vm_density_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
@@ -109,6 +119,11 @@ _SIGS = {
     'srf_cp_color_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_tensorf_sample_mask': (c_int, [P, P, P, c_int, c_int, FP, P, c_int, c_int, c_int, FP, P, P, P]),
     'srf_alpha_mask_query': (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
+    'srf_vm_alpha_grid': (c_int, [ctypes.POINTER(VmGrid), FP, P, c_int, c_int, c_int, FP, c_float, c_int, c_float,
+                                  P, P]),
+    'srf_alpha_pool_threshold': (c_int, [P, c_int, c_int, c_int, c_float, P, P, P]),
+    'srf_resample_grid': (c_int, [P, c_int, c_int, c_int, P, c_int, c_int, P]),
+    'srf_crop_grid': (c_int, [P, c_int, c_int, c_int, c_int, c_int, P, c_int, c_int, P]),
     'srf_compact_workspace_size': (c_size_t, [c_int64]),
     'srf_compact': (c_int, [P, c_int64, P, P, P, c_size_t, P]),
     'srf_compact_noalloc': (c_int, [P, c_int64, P, P, P]),
@@ -133,7 +148,11 @@ _SIGS = {
     'srf_mass_concentration_loss': (c_int, [P, c_int, c_int, c_int, P, c_float, P, P, P]),
     'srf_depth_reprojection_masks': (c_int, [P, P, P, P, P, c_int, P, c_int, P, P, c_int, c_int, c_int, c_int, c_int,
                                              c_float, P, P, P]),
+    'srf_coarse_fine_reprojection_masks': (c_int, [P, P, P, P, P, c_int, P, c_int, P, P, c_int, c_int, c_int, c_int, c_int,
+                                             c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
+    'srf_batch_assemble': (c_int, [P, P, P, c_int, c_int64, c_int, ctypes.c_uint64, P, P, P, c_int, P, P, P, P, P, P]),
+    'srf_uniforms': (c_int, [P, c_int64, ctypes.c_uint64, P, c_int, P]),
     'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
     'srf_autotune_enable': (c_int, [c_int]),
     'srf_autotune_count': (c_int, []),

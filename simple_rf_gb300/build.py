@@ -23,7 +23,8 @@ COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relax
           '-I' + os.path.join(REPO, 'include')]
 # Per-file flags: the sampling and compositing formulas (the NDC depth
 # conversion amplifies rounding near z = 1) must round like separate torch ops.
-EXTRA = {'sampling.cu': ['-fmad=false'], 'composite.cu': ['-fmad=false'], 'vm.cu': ['-fmad=false']}
+EXTRA = {'sampling.cu': ['-fmad=false'], 'composite.cu': ['-fmad=false'], 'vm.cu': ['-fmad=false'],
+         'maintenance.cu': ['-fmad=false']}
 
 
 def _nvcc():

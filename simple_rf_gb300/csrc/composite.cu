@@ -109,6 +109,45 @@ __device__ __forceinline__ bool white_for(const srf_composite_args& a, int r) {
     return (a.flags & SRF_COMPOSITE_WHITE_BKGD) || (a.white_per_ray && a.white_per_ray[r]);
 }
 
+// A training loss folded into compositing (srf_composite_loss): the rgb term
+// rgb_scale sum_c (rgb_c - t_c)^2 (MSE14.compute_mse with rgb_scale = 1 / (3 N)),
+// the depth term depth_scale |depth - t| or depth_scale (depth - t)^2 on masked
+// rays, and MassConcentrationLoss06's mc_scale sum_b -x_b ln x_b with x_b the
+// bin sums of the weights + 1e-3.
+struct LossArgs {
+    const float* target_rgb;
+    float rgb_scale;
+    const float* target_depth;
+    const uint8_t* depth_mask;
+    float depth_scale;
+    int depth_squared;
+    BinLayout bins;   // bins.nb == 0: no entropy term
+    const uint8_t* mc_mask;
+    float mc_scale;
+    float* loss;
+};
+
+__device__ __forceinline__ bool depth_term(const LossArgs& L, int r) {
+    return L.target_depth && (!L.depth_mask || L.depth_mask[r]);
+}
+
+__device__ __forceinline__ bool mc_term(const LossArgs& L, int r) {
+    return L.bins.nb > 0 && (!L.mc_mask || L.mc_mask[r]);
+}
+
+// Sum over the ray's samples of bin b of v (lane j holds samples j + 32 k).
+template <int R>
+__device__ __forceinline__ float bin_sum(const float (&v)[R], const BinLayout& bl, int b, int lane) {
+    float part = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = 32 * k + lane;
+        if (i >= bl.start[b] && i < bl.start[b + 1]) part += v[k];
+    }
+    return warp_sum(part);
+}
+
+
 __global__ void composite_fwd_kernel(srf_composite_args a) {
     extern __shared__ float smem[];
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -349,8 +388,8 @@ __device__ __forceinline__ void exp_scan_rounds(float (&Y)[R], int lane) {
     }
 }
 
-template <int R>
-__global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_args a) {
+template <int R, bool LOSS>
+__global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_args a, LossArgs L) {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int r = blockIdx.x * (blockDim.x >> 5) + warp;
     if (r >= a.n_rays) return;
@@ -428,11 +467,34 @@ __global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_ar
     }
     var = warp_sum(var);
     var_ndc = warp_sum(var_ndc);
+    float lray = 0.f;
+    if (LOSS && mc_term(L, r)) {
+        float w[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) w[k] = 32 * k + lane < c.s ? al[k] * T[k] : 0.f;
+        for (int b = 0; b < L.bins.nb; ++b) {
+            const float x = bin_sum<R>(w, L.bins, b, lane) + 1e-3f;
+            lray -= x * logf(x);
+        }
+        lray *= L.mc_scale;
+    }
     if (lane == 0) {
         if (white_for(a, r)) {
             cr = cr + (1.f - acc);
             cg = cg + (1.f - acc);
             cb = cb + (1.f - acc);
+        }
+        if (LOSS) {
+            if (L.target_rgb) {
+                const float e0 = cr - L.target_rgb[3 * r], e1 = cg - L.target_rgb[3 * r + 1],
+                            e2 = cb - L.target_rgb[3 * r + 2];
+                lray += L.rgb_scale * (e0 * e0 + e1 * e1 + e2 * e2);
+            }
+            if (depth_term(L, r)) {
+                const float e = depth - L.target_depth[r];
+                lray += L.depth_scale * (L.depth_squared ? e * e : fabsf(e));
+            }
+            atomicAdd(L.loss, lray);
         }
         if (a.rgb_map) {
             a.rgb_map[3 * r] = cr;
@@ -449,8 +511,8 @@ __global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_ar
     }
 }
 
-template <int R>
-__global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_args a) {
+template <int R, bool LOSS>
+__global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_args a, LossArgs L) {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int r = blockIdx.x * (blockDim.x >> 5) + warp;
     if (r >= a.n_rays) return;
@@ -484,13 +546,20 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
         g2 = a.g_rgb[3 * r + 2];
     }
     float gacc = a.g_acc ? a.g_acc[r] : 0.f;
-    if (white_for(a, r)) gacc -= g0 + g1 + g2;
-    // colour terms of G (the loads stay off the scan's dependency chain)
-    float cdot[R];
+    // colour terms of G (the loads stay off the scan's dependency chain); with a
+    // loss the colours stay in registers until the loss gradient of rgb is known
+    float cdot[R], c0[LOSS ? R : 1], c1[LOSS ? R : 1], c2[LOSS ? R : 1];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int i = 32 * k + lane;
-        cdot[k] = (rgb && i < c.s) ? rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 : 0.f;
+        if (LOSS) {
+            const bool in = rgb && i < c.s;
+            c0[k] = in ? rgb[3 * i] : 0.f;
+            c1[k] = in ? rgb[3 * i + 1] : 0.f;
+            c2[k] = in ? rgb[3 * i + 2] : 0.f;
+        } else {
+            cdot[k] = (rgb && i < c.s) ? rgb[3 * i] * g0 + rgb[3 * i + 1] * g1 + rgb[3 * i + 2] * g2 : 0.f;
+        }
         if (exp_prefix && i >= c.s) T[k] = 0.f;
     }
     if (exp_prefix)
@@ -515,6 +584,53 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
     float inv = 1.f / (acc + kEps);
     float depth = wz / (acc + kEps), depth_ndc = wzn / (acc + kEps);
     float gd = a.g_depth ? a.g_depth[r] : 0.f;
+    if (LOSS) {
+        // the loss gradient of this ray's outputs, from the recomputed forward
+        if (L.target_rgb) {
+            float cr = 0.f, cg = 0.f, cb = 0.f;
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                if (32 * k + lane < c.s) {
+                    const float w = al[k] * T[k];
+                    cr += w * c0[k];
+                    cg += w * c1[k];
+                    cb += w * c2[k];
+                }
+            }
+            cr = warp_sum(cr); cg = warp_sum(cg); cb = warp_sum(cb);
+            if (white_for(a, r)) {
+                cr = cr + (1.f - acc);
+                cg = cg + (1.f - acc);
+                cb = cb + (1.f - acc);
+            }
+            const float s2 = 2.f * L.rgb_scale;
+            g0 += s2 * (cr - L.target_rgb[3 * r]);
+            g1 += s2 * (cg - L.target_rgb[3 * r + 1]);
+            g2 += s2 * (cb - L.target_rgb[3 * r + 2]);
+        }
+        if (depth_term(L, r)) {
+            const float e = depth - L.target_depth[r];
+            gd += L.depth_squared ? 2.f * L.depth_scale * e
+                                  : L.depth_scale * (e > 0.f ? 1.f : (e < 0.f ? -1.f : 0.f));
+        }
+        if (mc_term(L, r)) {
+            float w[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) w[k] = 32 * k + lane < c.s ? al[k] * T[k] : 0.f;
+            for (int b = 0; b < L.bins.nb; ++b) {
+                const float x = bin_sum<R>(w, L.bins, b, lane) + 1e-3f;
+                const float gb = -(logf(x) + 1.f) * L.mc_scale;
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    const int i = 32 * k + lane;
+                    if (i >= L.bins.start[b] && i < L.bins.start[b + 1]) G[k] += gb;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < R; ++k) cdot[k] = c0[k] * g0 + c1[k] * g1 + c2[k] * g2;
+    }
+    if (white_for(a, r)) gacc -= g0 + g1 + g2;
     float gv = a.g_depth_var ? a.g_depth_var[r] : 0.f;
     float gdn = (c.ndc && a.g_depth_ndc) ? a.g_depth_ndc[r] : 0.f;
     float gvn = (c.ndc && a.g_depth_var_ndc) ? a.g_depth_var_ndc[r] : 0.f;
@@ -536,7 +652,7 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
     for (int k = 0; k < R; ++k) {
         float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
         float g = cdot[k] + gacc;
-        if (a.g_weights) g += G[k];
+        if (a.g_weights || (LOSS && mc_term(L, r))) g += G[k];
         float d = zm - depth;
         g += gd * d * inv + gv * (d * d - 2.f * bsum * d * inv);
         if (c.ndc) {
@@ -691,9 +807,54 @@ inline int reg_rounds(int n) {
 }
 
 template <class K>
-int launch_reg(K kernel, const srf_composite_args* a, void* stream) {
-    kernel<<<grid_1d(a->n_rays, 8), 256, 0, as_stream(stream)>>>(*a);
+int launch_reg(K kernel, const srf_composite_args* a, const LossArgs& L, void* stream) {
+    kernel<<<grid_1d(a->n_rays, 8), 256, 0, as_stream(stream)>>>(*a, L);
     return launch_status();
+}
+
+template <bool LOSS>
+int forward_reg(const srf_composite_args* a, const LossArgs& L, void* stream) {
+    switch (reg_rounds(a->n_samples)) {
+        case 2: return launch_reg(composite_fwd_reg_kernel<2, LOSS>, a, L, stream);
+        case 4: return launch_reg(composite_fwd_reg_kernel<4, LOSS>, a, L, stream);
+        case 6: return launch_reg(composite_fwd_reg_kernel<6, LOSS>, a, L, stream);
+        case 8: return launch_reg(composite_fwd_reg_kernel<8, LOSS>, a, L, stream);
+        default: return SRF_ERR_UNSUPPORTED;
+    }
+}
+
+template <bool LOSS>
+int backward_reg(const srf_composite_args* a, const LossArgs& L, void* stream) {
+    switch (reg_rounds(a->n_samples)) {
+        case 2: return launch_reg(composite_bwd_reg_kernel<2, LOSS>, a, L, stream);
+        case 4: return launch_reg(composite_bwd_reg_kernel<4, LOSS>, a, L, stream);
+        case 6: return launch_reg(composite_bwd_reg_kernel<6, LOSS>, a, L, stream);
+        case 8: return launch_reg(composite_bwd_reg_kernel<8, LOSS>, a, L, stream);
+        default: return SRF_ERR_UNSUPPORTED;
+    }
+}
+
+int make_loss(const srf_composite_args* a, const srf_composite_loss* l, LossArgs* L) {
+    if (!l || !l->loss) return SRF_ERR_NULL;
+    if (l->n_depth_rays < 0 || l->n_mc_rays < 0 || l->num_bins < 0 || l->num_bins > 32) return SRF_ERR_SHAPE;
+    *L = LossArgs{};
+    L->loss = l->loss;
+    L->target_rgb = l->target_rgb;
+    L->rgb_scale = a->n_rays > 0 ? l->rgb_weight / float(3 * a->n_rays) : 0.f;
+    if (l->target_depth && l->n_depth_rays > 0) {
+        L->target_depth = l->target_depth;
+        L->depth_mask = l->depth_mask;
+        L->depth_scale = l->depth_weight / float(l->n_depth_rays);
+        L->depth_squared = l->depth_squared != 0;
+    }
+    if (l->num_bins > 0 && l->n_mc_rays > 0) {
+        if (!bin_layout(a->n_samples, l->num_bins, &L->bins)) return SRF_ERR_SHAPE;
+        L->mc_mask = l->mc_mask;
+        L->mc_scale = l->mc_weight / float(l->n_mc_rays);
+    } else {
+        L->bins.nb = 0;
+    }
+    return SRF_OK;
 }
 
 }  // namespace
@@ -705,26 +866,36 @@ extern "C" int srf_composite_forward(const srf_composite_args* args, void* strea
     int st = check_args(args, false);
     if (st != SRF_OK || args->n_rays == 0) return st;
     if ((args->flags & SRF_COMPOSITE_EXP_PREFIX) && !reg_rounds(args->n_samples)) return SRF_ERR_UNSUPPORTED;
-    switch (reg_rounds(args->n_samples)) {
-        case 2: return launch_reg(composite_fwd_reg_kernel<2>, args, stream);
-        case 4: return launch_reg(composite_fwd_reg_kernel<4>, args, stream);
-        case 6: return launch_reg(composite_fwd_reg_kernel<6>, args, stream);
-        case 8: return launch_reg(composite_fwd_reg_kernel<8>, args, stream);
-        default: return launch(composite_fwd_kernel, args, stream);
-    }
+    if (reg_rounds(args->n_samples)) return forward_reg<false>(args, LossArgs{}, stream);
+    return launch(composite_fwd_kernel, args, stream);
 }
 
 extern "C" int srf_composite_backward(const srf_composite_args* args, void* stream) {
     int st = check_args(args, true);
     if (st != SRF_OK || args->n_rays == 0) return st;
     if ((args->flags & SRF_COMPOSITE_EXP_PREFIX) && !reg_rounds(args->n_samples)) return SRF_ERR_UNSUPPORTED;
-    switch (reg_rounds(args->n_samples)) {
-        case 2: return launch_reg(composite_bwd_reg_kernel<2>, args, stream);
-        case 4: return launch_reg(composite_bwd_reg_kernel<4>, args, stream);
-        case 6: return launch_reg(composite_bwd_reg_kernel<6>, args, stream);
-        case 8: return launch_reg(composite_bwd_reg_kernel<8>, args, stream);
-        default: return launch(composite_bwd_kernel, args, stream);
-    }
+    if (reg_rounds(args->n_samples)) return backward_reg<false>(args, LossArgs{}, stream);
+    return launch(composite_bwd_kernel, args, stream);
+}
+
+extern "C" int srf_composite_forward_loss(const srf_composite_args* args, const srf_composite_loss* loss,
+                                          void* stream) {
+    int st = check_args(args, false);
+    if (st != SRF_OK) return st;
+    LossArgs L;
+    if ((st = make_loss(args, loss, &L)) != SRF_OK || args->n_rays == 0) return st;
+    if (!reg_rounds(args->n_samples)) return SRF_ERR_UNSUPPORTED;
+    return forward_reg<true>(args, L, stream);
+}
+
+extern "C" int srf_composite_backward_loss(const srf_composite_args* args, const srf_composite_loss* loss,
+                                           void* stream) {
+    int st = check_args(args, true);
+    if (st != SRF_OK) return st;
+    LossArgs L;
+    if ((st = make_loss(args, loss, &L)) != SRF_OK || args->n_rays == 0) return st;
+    if (!reg_rounds(args->n_samples)) return SRF_ERR_UNSUPPORTED;
+    return backward_reg<true>(args, L, stream);
 }
 
 extern "C" int srf_weighted_sum(const float* weights, const float* values, int n_rays, int n_samples, int channels,

@@ -66,4 +66,36 @@ struct Carver {
 __device__ __forceinline__ float relu_f(float x) { return x > 0.f ? x : 0.f; }
 __device__ __forceinline__ float sigmoid_f(float x) { return 1.f / (1.f + expf(-x)); }
 
+// MassConcentrationLoss06's bins over a ray of s samples: bin b covers samples
+// [start[b], start[b + 1]).
+struct BinLayout {
+    int nb;
+    int start[65];
+};
+
+// torch.linspace(0, B - 1, S % B) (CPU/CUDA formula: start + step i below the
+// halfway point, end - step (steps - 1 - i) above it, in float), truncated: the
+// bins that take one extra sample (MassConcentrationLoss06.py:69-72).
+inline bool bin_layout(int s, int nb, BinLayout* bl) {
+    if (nb < 1 || nb > 64 || s < nb) return false;
+    bool bigger[64] = {};
+    const int per = s / nb, rem = s % nb;
+    if (rem == 1) {
+        bigger[0] = true;
+    } else if (rem > 1) {
+        const float start = 0.f, end = float(nb - 1);
+        const float step = (end - start) / float(rem - 1);
+        for (int i = 0; i < rem; ++i) {
+            float v = i < rem / 2 ? start + step * float(i) : end - step * float(rem - 1 - i);
+            int k = int(v);
+            if (k < 0 || k >= nb) return false;
+            bigger[k] = true;
+        }
+    }
+    bl->nb = nb;
+    bl->start[0] = 0;
+    for (int b = 0; b < nb; ++b) bl->start[b + 1] = bl->start[b] + per + (bigger[b] ? 1 : 0);
+    return bl->start[nb] == s;
+}
+
 }  // namespace srf

@@ -210,12 +210,6 @@ __global__ void depth_mse_kernel(const float* __restrict__ pred, const float* __
     if (threadIdx.x == 0 && loss) atomicAdd(loss, weight * l * inv);
 }
 
-// Bin b of a ray covers samples [start[b], start[b + 1]).
-struct BinLayout {
-    int nb;
-    int start[65];
-};
-
 // Per ray: bin sums b_k of the weights, loss term -sum_k (b_k + 1e-3) ln(b_k + 1e-3);
 // mean over the (masked) rays; d/dw_i = -(ln(b_k + 1e-3) + 1) for i in bin k.  One
 // block of 1024 threads, a warp per ray and a lane per bin.
@@ -283,8 +277,8 @@ __global__ void reprojection_masks_kernel(const float* __restrict__ ro, const fl
                                           const float* __restrict__ d1, const float* __restrict__ d2,
                                           const int32_t* __restrict__ pid, int n, const float* __restrict__ poses,
                                           int V, const float* __restrict__ k0, const float* __restrict__ imgs, int H,
-                                          int W, int C, int hpx, int hpy, float thr, uint8_t* m1, uint8_t* m2,
-                                          int* flag) {
+                                          int W, int C, int hpx, int hpy, float thr, int both_invalid_rule,
+                                          uint8_t* m1, uint8_t* m2, int* flag) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const int ia = pid[3 * r], xa = pid[3 * r + 1], ya = pid[3 * r + 2];
@@ -345,7 +339,7 @@ __global__ void reprojection_masks_kernel(const float* __restrict__ ro, const fl
     const float r2 = patch_rmse(imgs, H, W, C, ia, ys, xs, ib, cy2, cx2, hpy, hpx);
     bool a = ((r1 < r2) || !v2) && (r1 < thr) && v1 && va;
     bool b = ((r2 < r1) || !v1) && (r2 < thr) && v2 && va;
-    if (!(v1 || v2)) {
+    if (both_invalid_rule && !(v1 || v2)) {
         a = a || (d1[r] > d2[r]);
         b = b || (d2[r] > d1[r]);
     }
@@ -422,31 +416,6 @@ extern "C" int srf_depth_mse_loss(const float* pred, const float* target, const 
     depth_mse_kernel<<<1, 1024, 0, as_stream(stream)>>>(pred, target, mask, n, weight, mean_over_mask, loss_dev,
                                                         grad_pred, grad_target);
     return launch_status();
-}
-
-// torch.linspace(0, B - 1, S % B) (CPU/CUDA formula: start + step i below the
-// halfway point, end - step (steps - 1 - i) above it, in float), truncated: the
-// bins that take one extra sample (MassConcentrationLoss06.py:69-72).
-static bool bin_layout(int s, int nb, BinLayout* bl) {
-    if (nb < 1 || nb > 64 || s < nb) return false;
-    bool bigger[64] = {};
-    const int per = s / nb, rem = s % nb;
-    if (rem == 1) {
-        bigger[0] = true;
-    } else if (rem > 1) {
-        const float start = 0.f, end = float(nb - 1);
-        const float step = (end - start) / float(rem - 1);
-        for (int i = 0; i < rem; ++i) {
-            float v = i < rem / 2 ? start + step * float(i) : end - step * float(rem - 1 - i);
-            int k = int(v);
-            if (k < 0 || k >= nb) return false;
-            bigger[k] = true;
-        }
-    }
-    bl->nb = nb;
-    bl->start[0] = 0;
-    for (int b = 0; b < nb; ++b) bl->start[b + 1] = bl->start[b] + per + (bigger[b] ? 1 : 0);
-    return bl->start[nb] == s;
 }
 
 extern "C" int srf_mass_concentration_loss(const float* weights, int n_rays, int n_samples, int num_bins,
@@ -578,12 +547,11 @@ extern "C" int srf_adam_multi_step(const srf_adam_tensor* tensors, int n_tensors
     return SRF_OK;
 }
 
-extern "C" int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth1,
-                                            const float* depth2, const int32_t* pixel_ids, int n_rays,
-                                            const float* poses, int n_views, const float* intrinsics0,
-                                            const float* images, int height, int width, int channels, int patch_w,
-                                            int patch_h, float rmse_threshold, uint8_t* mask1, uint8_t* mask2,
-                                            void* stream) {
+static int reprojection_masks(const float* rays_o, const float* rays_d, const float* depth1, const float* depth2,
+                              const int32_t* pixel_ids, int n_rays, const float* poses, int n_views,
+                              const float* intrinsics0, const float* images, int height, int width, int channels,
+                              int patch_w, int patch_h, float rmse_threshold, int both_invalid_rule, uint8_t* mask1,
+                              uint8_t* mask2, void* stream) {
     if (n_rays < 0 || n_views < 1 || height < 1 || width < 1 || channels < 1 || channels > 64) return SRF_ERR_SHAPE;
     if (patch_w < 1 || patch_h < 1 || patch_w > 31 || patch_h > 31) return SRF_ERR_SHAPE;
     if (n_rays == 0) return SRF_OK;
@@ -592,8 +560,29 @@ extern "C" int srf_depth_reprojection_masks(const float* rays_o, const float* ra
         return SRF_ERR_NULL;
     reprojection_masks_kernel<<<grid_1d(n_rays, 128), 128, 0, as_stream(stream)>>>(
         rays_o, rays_d, depth1, depth2, pixel_ids, n_rays, poses, n_views, intrinsics0, images, height, width,
-        channels, patch_w / 2, patch_h / 2, rmse_threshold, mask1, mask2, device_flag());
+        channels, patch_w / 2, patch_h / 2, rmse_threshold, both_invalid_rule, mask1, mask2, device_flag());
     return launch_status();
+}
+
+extern "C" int srf_depth_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth1,
+                                            const float* depth2, const int32_t* pixel_ids, int n_rays,
+                                            const float* poses, int n_views, const float* intrinsics0,
+                                            const float* images, int height, int width, int channels, int patch_w,
+                                            int patch_h, float rmse_threshold, uint8_t* mask1, uint8_t* mask2,
+                                            void* stream) {
+    return reprojection_masks(rays_o, rays_d, depth1, depth2, pixel_ids, n_rays, poses, n_views, intrinsics0, images,
+                              height, width, channels, patch_w, patch_h, rmse_threshold, 1, mask1, mask2, stream);
+}
+
+extern "C" int srf_coarse_fine_reprojection_masks(const float* rays_o, const float* rays_d, const float* depth_coarse,
+                                                  const float* depth_fine, const int32_t* pixel_ids, int n_rays,
+                                                  const float* poses, int n_views, const float* intrinsics0,
+                                                  const float* images, int height, int width, int channels,
+                                                  int patch_w, int patch_h, float rmse_threshold, uint8_t* mask1,
+                                                  uint8_t* mask2, void* stream) {
+    return reprojection_masks(rays_o, rays_d, depth_coarse, depth_fine, pixel_ids, n_rays, poses, n_views,
+                              intrinsics0, images, height, width, channels, patch_w, patch_h, rmse_threshold, 0, mask1,
+                              mask2, stream);
 }
 
 extern "C" int srf_tv_loss(const srf_tv_component* components, int n_components, float weight, const float* scale_dev,

@@ -594,6 +594,58 @@ __global__ void density_act_bwd_kernel(float* df, const float* __restrict__ ds, 
     }
 }
 
+// torch.linspace(0, 1, n)[i], the CPU formula the reference evaluates
+// (SimpleTensoRF09.py:851-854): the first half counts up from 0, the second
+// half down from 1.
+__device__ __forceinline__ float linspace01(int i, int n) {
+    if (n == 1) return 0.f;
+    const float step = 1.f / float(n - 1);
+    return i < n / 2 ? __fmul_rn(step, float(i)) : __fsub_rn(1.f, __fmul_rn(step, float(n - 1 - i)));
+}
+
+// LowRankTensor.update_alpha_mask's dense pass (SimpleTensoRF09.py:849-858 with
+// compute_alpha :878-897): node (x, y, z) of the res[0] x res[1] x res[2] grid at
+// xyz = lo (1 - s) + hi s, alpha = clamp(1 - exp(-sigma step), 0, 1), sigma the
+// activated VM density, zero where the current alpha mask is empty.  Written
+// z-major (alpha[z][y][x]), the transposed layout the mask volume keeps.
+__global__ void alpha_grid_kernel(srf_vm_grid g, Box box, const float* __restrict__ vol, int vd, int vh, int vw,
+                                  Box abox, float step, int mode, float offset, float* __restrict__ alpha) {
+    const int gx = g.res[0], gy = g.res[1], gz = g.res[2];
+    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= int64_t(gx) * gy * gz) return;
+    const int ix[3] = {int(t % gx), int((t / gx) % gy), int(t / (int64_t(gx) * gy))};
+    float q[3], pn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float s = linspace01(ix[a], g.res[a]);
+        q[a] = __fadd_rn(__fmul_rn(box.lo[a], __fsub_rn(1.f, s)), __fmul_rn(box.hi[a], s));
+    }
+    bool keep = true;
+    if (vol) {
+        float an[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            an[a] = __fsub_rn(__fmul_rn((q[a] - abox.lo[a]) / (abox.hi[a] - abox.lo[a]), 2.f), 1.f);
+        keep = alpha_positive(vol, vd, vh, vw, an[0], an[1], an[2]);
+    }
+    float sigma = 0.f;
+    if (keep) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            pn[a] = __fsub_rn(__fmul_rn((q[a] - box.lo[a]) / (box.hi[a] - box.lo[a]), 2.f), 1.f);
+        float acc = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            Taps pt, lt;
+            plane_taps(g, i, pn, pt, lt);
+            acc = acc + vm_dot(g.planes[i], g.lines[i], g.n_comp[i], pt, lt);
+        }
+        sigma = mode == 0 ? relu_f(acc) : softplus_f(acc + offset);
+    }
+    float a = 1.f - expf(-sigma * step);
+    alpha[t] = fminf(fmaxf(a, 0.f), 1.f);
+}
+
 int check_grid(const srf_vm_grid* g, bool need) {
     if (!g) return SRF_ERR_NULL;
     for (int i = 0; i < 3; ++i) {
@@ -926,4 +978,21 @@ extern "C" int srf_cp_color_forward(const srf_vm_grid* grid, const float* pts, i
 extern "C" int srf_cp_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
                                      int64_t n_pts, const float* d_features, void* stream) {
     return cp_backward(grad_grid, grid, pts, n_pts, d_features, 1, stream);
+}
+
+extern "C" int srf_vm_alpha_grid(const srf_vm_grid* grid, const float* bbox, const float* alpha_volume, int vol_d,
+                                 int vol_h, int vol_w, const float* alpha_bbox, float step, int density_mode,
+                                 float density_offset, float* alpha, void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if (!bbox || !alpha || (alpha_volume && !alpha_bbox)) return SRF_ERR_NULL;
+    if (alpha_volume && (vol_d < 1 || vol_h < 1 || vol_w < 1)) return SRF_ERR_SHAPE;
+    if (density_mode != 0 && density_mode != 1) return SRF_ERR_SHAPE;
+    Box b{{bbox[0], bbox[1], bbox[2]}, {bbox[3], bbox[4], bbox[5]}};
+    Box ab{};
+    if (alpha_bbox) ab = Box{{alpha_bbox[0], alpha_bbox[1], alpha_bbox[2]}, {alpha_bbox[3], alpha_bbox[4], alpha_bbox[5]}};
+    int64_t n = int64_t(grid->res[0]) * grid->res[1] * grid->res[2];
+    alpha_grid_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(*grid, b, alpha_volume, vol_d, vol_h, vol_w, ab,
+                                                                     step, density_mode, density_offset, alpha);
+    return launch_status();
 }

@@ -556,3 +556,31 @@ def tv_loss_accumulate(components, weight, loss=None):
         call('srf_tv_loss', _tv_struct([p.detach() for p in part], [p.grad for p in part]), len(part),
              float(weight), None, _ptr(loss), _stream())
     return loss
+
+
+class _DepthMseFunction(torch.autograd.Function):
+    """mean over the masked rays of (pred - target)^2 with the target detached
+    (srf_depth_mse_loss with mean_over_mask): SparseDepthMSE14.compute_depth_loss
+    (src/loss_functions/SparseDepthMSE14.py:84-97) and CoarseFineConsistencyLoss34.compute_loss_sd
+    (src/loss_functions/CoarseFineConsistencyLoss34.py:170-187)."""
+
+    @staticmethod
+    def forward(ctx, pred, target, mask):
+        p = pred.detach().contiguous().float()
+        t = target.detach().contiguous().float()
+        m = mask.to(torch.uint8).contiguous()
+        loss = torch.zeros(1, device=p.device)
+        g = torch.zeros_like(p)
+        call('srf_depth_mse_loss', _ptr(p), _ptr(t), _ptr(m), p.shape[0], 1.0, 1, _ptr(loss), _ptr(g), None,
+             _stream())
+        ctx.save_for_backward(g)
+        return loss[0]
+
+    @staticmethod
+    def backward(ctx, g_loss):
+        (g,) = ctx.saved_tensors
+        return g * g_loss, None, None
+
+
+def depth_mse(pred, target, mask):
+    return _DepthMseFunction.apply(pred, target, mask)

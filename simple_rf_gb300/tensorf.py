@@ -390,3 +390,65 @@ class _RendererTcFunction(torch.autograd.Function):
 
 def renderer_tc(desc, precision, feats, view, params):
     return _RendererTcFunction.apply(desc, precision, feats, view, *params)
+
+
+# ------------------------------------------------------------ grid maintenance --
+
+def _cl_dims(t):
+    """(h, w, comps) of a channels-last (1, comps, h, w) plane or (1, comps, l, 1) line."""
+    if not _is_cl(t) or t.dtype != torch.float32 or not t.is_cuda:
+        raise RuntimeError('grid tensors must be channels_last float32 CUDA tensors')
+    return int(t.shape[2]), int(t.shape[3]), int(t.shape[1])
+
+
+def resample_grid(t, h_new, w_new):
+    """Bilinear align_corners resampling of a plane (1,R,H,W) or line (1,R,L,1) to
+    (1,R,h_new,w_new), channels-last (upsample_vectors_and_matrices,
+    SimpleTensoRF09.py:1284-1301)."""
+    h, w, r = _cl_dims(t)
+    out = torch.empty(1, r, h_new, w_new, device=t.device).contiguous(memory_format=torch.channels_last)
+    _lib.call('srf_resample_grid', t.data_ptr(), h, w, r, out.data_ptr(), h_new, w_new, _stream(t))
+    return out
+
+
+def crop_grid(t, row0, row1, col0, col1):
+    """Rows [row0, row1) x columns [col0, col1) of a plane or line, channels-last
+    (shrink_tensor, SimpleTensoRF09.py:1303-1320)."""
+    h, w, r = _cl_dims(t)
+    out = torch.empty(1, r, row1 - row0, col1 - col0, device=t.device).contiguous(memory_format=torch.channels_last)
+    _lib.call('srf_crop_grid', t.data_ptr(), h, w, r, row0, col0, out.data_ptr(), row1 - row0, col1 - col0,
+              _stream(t))
+    return out
+
+
+def alpha_grid(grid, bbox, alpha_volume, alpha_bbox, step, density_mode, density_offset):
+    """Dense alpha (res[2], res[1], res[0]) on the grid's nodes (update_alpha_mask's
+    dense pass with compute_alpha, SimpleTensoRF09.py:849-858, 878-897)."""
+    res = grid.res
+    dev = grid.planes[0].device
+    out = torch.empty(res[2], res[1], res[0], device=dev)
+    vd = vh = vw = 0
+    vol = None
+    if alpha_volume is not None:
+        vol = alpha_volume.contiguous().float()
+        vd, vh, vw = vol.shape
+    g = _grid_struct(res, grid.planes, grid.lines)
+    _lib.call('srf_vm_alpha_grid', ctypes.byref(g), _lib.host_floats(bbox), None if vol is None else vol.data_ptr(),
+              vd, vh, vw, None if alpha_bbox is None else _lib.host_floats(alpha_bbox), float(step),
+              int(density_mode), float(density_offset), out.data_ptr(), _stream(out))
+    return out
+
+
+def alpha_pool_threshold(alpha, threshold):
+    """3^3 max-pool and threshold of alpha (gz, gy, gx) -> 0/1 volume, and the
+    occupied node range per axis as ((min x, min y, min z), (max x, max y, max z))
+    or None when no node is occupied (SimpleTensoRF09.py:859-874)."""
+    gz, gy, gx = alpha.shape
+    vol = torch.empty_like(alpha)
+    bounds = torch.empty(6, dtype=torch.int32, device=alpha.device)
+    _lib.call('srf_alpha_pool_threshold', alpha.data_ptr(), gx, gy, gz, float(threshold), vol.data_ptr(),
+              bounds.data_ptr(), _stream(alpha))
+    b = bounds.cpu().tolist()
+    if b[3] < 0:
+        return vol, None
+    return vol, ((gx - 1 - b[0], gy - 1 - b[1], gz - 1 - b[2]), (b[3], b[4], b[5]))

@@ -21,7 +21,6 @@ import weakref
 
 import numpy
 import torch
-import torch.nn.functional as tF
 from torch.nn import ModuleDict, ModuleList
 
 from . import _lib
@@ -360,16 +359,34 @@ class GbVmTensor(torch.nn.Module):
         self.matrices_color, self.vectors_color = self.resize(self.matrices_color, self.vectors_color, res)
 
     def resize(self, mats, vecs, res):
-        """Bilinear (align_corners) resampling of planes and lines to a new resolution (:1284-1301)."""
+        """Bilinear (align_corners) resampling of planes and lines to a new resolution
+        (:1284-1301) on the srf_resample_grid kernel."""
         new_m, new_v = [], []
         for i in range(3):
             m0, m1 = MATRIX_AXES[i]
             v = VECTOR_AXES[i]
-            new_m.append(torch.nn.Parameter(T.to_channels_last(tF.interpolate(
-                mats[i].data, size=(int(res[m1]), int(res[m0])), mode='bilinear', align_corners=True))))
-            new_v.append(torch.nn.Parameter(T.to_channels_last(tF.interpolate(
-                vecs[i].data, size=(int(res[v]), 1), mode='bilinear', align_corners=True))))
+            new_m.append(torch.nn.Parameter(T.resample_grid(T.to_channels_last(mats[i].data), int(res[m1]),
+                                                            int(res[m0]))))
+            new_v.append(torch.nn.Parameter(T.resample_grid(T.to_channels_last(vecs[i].data), int(res[v]), 1)))
         return torch.nn.ParameterList(new_m), torch.nn.ParameterList(new_v)
+
+    def reshape_tensor(self, res):
+        """Planes and lines of the shapes of resolution res (channels-last, on their
+        device), values left for a checkpoint to fill (the load hook)."""
+        for kind in ('density', 'color'):
+            mats = getattr(self, f'matrices_{kind}')
+            vecs = getattr(self, f'vectors_{kind}')
+            new_m, new_v = [], []
+            for i in range(3):
+                m0, m1 = MATRIX_AXES[i]
+                v = VECTOR_AXES[i]
+                r = mats[i].shape[1]
+                new_m.append(torch.nn.Parameter(T.to_channels_last(
+                    torch.zeros(1, r, int(res[m1]), int(res[m0]), device=mats[i].device))))
+                new_v.append(torch.nn.Parameter(T.to_channels_last(
+                    torch.zeros(1, vecs[i].shape[1], int(res[v]), 1, device=vecs[i].device))))
+            setattr(self, f'matrices_{kind}', torch.nn.ParameterList(new_m))
+            setattr(self, f'vectors_{kind}', torch.nn.ParameterList(new_v))
 
     @torch.no_grad()
     def compute_alpha(self, xyz, length):
@@ -385,26 +402,36 @@ class GbVmTensor(torch.nn.Module):
         return 1 - torch.exp(-sigma * length)
 
     @torch.no_grad()
+    def dense_alpha(self):
+        """Alpha of the density on every grid node, z-major (res[2], res[1], res[0])
+        (:849-858, 878-897), on the srf_vm_alpha_grid kernel."""
+        am = self.alpha_mask
+        return T.alpha_grid(self._grid('density'), cached_host(self, 'bbox', self.bounding_box),
+                            None if am is None else am.volume(),
+                            None if am is None else cached_host(am, 'bbox', am.bounding_box),
+                            float(cached_host(self, 'step_size', self.step_size)[0]), self.density_mode,
+                            self.density_offset)
+
+    @torch.no_grad()
     def update_alpha_mask(self, iter_num):
-        """SimpleTensoRF09.py:849-876: dense alpha, 3^3 max-pool, threshold; returns the occupied bbox."""
+        """SimpleTensoRF09.py:849-876: dense alpha of the density on the grid's nodes
+        (srf_vm_alpha_grid), 3^3 max-pool and threshold with the occupied node range
+        (srf_alpha_pool_threshold); returns the occupied box."""
         gs = [int(r) for r in self.resolution]
-        dev = self.bounding_box.device
-        t = [torch.linspace(0, 1, g, device=dev) for g in gs]
-        samples = torch.stack(torch.meshgrid(*t, indexing='ij'), -1)
-        xyz = self.bounding_box[0] * (1 - samples) + self.bounding_box[1] * samples
-        alpha = torch.empty(gs, device=dev).view(-1)
-        flat = xyz.view(-1, 3)
-        chunk = 1 << 22
-        for a in range(0, flat.shape[0], chunk):
-            alpha[a:a + chunk] = self.compute_alpha(flat[a:a + chunk], self.step_size)
-        alpha = alpha.view(gs).clamp(0, 1).transpose(0, 2).contiguous()[None, None]
-        xyz = xyz.transpose(0, 2).contiguous()
-        alpha = tF.max_pool3d(alpha, kernel_size=3, padding=1, stride=1).view(gs[::-1])
-        thr = self.tensor_configs['alpha_mask_threshold']
-        alpha = (alpha >= thr).float()
-        self.alpha_mask = AlphaGridMask(alpha, self.bounding_box)
-        valid = xyz[alpha > 0.5]
-        return torch.stack((valid.amin(0), valid.amax(0)))
+        alpha = self.dense_alpha()
+        vol, rng = T.alpha_pool_threshold(alpha, self.tensor_configs['alpha_mask_threshold'])
+        if rng is None:
+            raise RuntimeError('update_alpha_mask: no grid node is occupied (the reference fails on the empty box)')
+        self.alpha_mask = AlphaGridMask(vol, self.bounding_box)
+        # node coordinates as the reference forms them: CPU linspace, then
+        # bbox_lo (1 - s) + bbox_hi s (:851-856)
+        lo_hi = self.bounding_box.detach().cpu().float()
+        box = torch.empty(2, 3)
+        for a in range(3):
+            s = torch.linspace(0, 1, gs[a])
+            idx = torch.tensor([rng[0][a], rng[1][a]])
+            box[:, a] = lo_hi[0, a] * (1 - s[idx]) + lo_hi[1, a] * s[idx]
+        return box.to(self.bounding_box.device)
 
     @torch.no_grad()
     def shrink_tensor(self, bbox_new):
@@ -423,13 +450,15 @@ class GbVmTensor(torch.nn.Module):
         self.crop_tensor(t_l, b_r)
 
     def crop_tensor(self, t_l, b_r):
+        """The slicing of shrink_tensor (:1303-1320) on the srf_crop_grid kernel."""
+        t_l, b_r = [int(x) for x in t_l], [int(x) for x in b_r]
         for plist, vlist in ((self.matrices_density, self.vectors_density), (self.matrices_color, self.vectors_color)):
             for i in range(3):
                 m0, m1 = MATRIX_AXES[i]
                 v = VECTOR_AXES[i]
-                vlist[i] = torch.nn.Parameter(T.to_channels_last(vlist[i].data[..., t_l[v]:b_r[v], :]))
-                plist[i] = torch.nn.Parameter(T.to_channels_last(
-                    plist[i].data[..., t_l[m1]:b_r[m1], t_l[m0]:b_r[m0]]))
+                vlist[i] = torch.nn.Parameter(T.crop_grid(T.to_channels_last(vlist[i].data), t_l[v], b_r[v], 0, 1))
+                plist[i] = torch.nn.Parameter(T.crop_grid(T.to_channels_last(plist[i].data), t_l[m1], b_r[m1],
+                                                          t_l[m0], b_r[m0]))
 
     def reconfigure_optimizer(self):
         """SimpleTensoRF09.py:916-944: replace this model's param groups in the optimizer."""
@@ -453,7 +482,7 @@ class GbVmTensor(torch.nn.Module):
             self.alpha_mask = AlphaGridMask(sd[key].float(), sd[f'{prefix}alpha_mask.bounding_box'])
         res = sd.get(f'{prefix}resolution')
         if res is not None:
-            self.resample_tensor(res)
+            self.reshape_tensor(res)
 
 
 class GbCpTensor(GbVmTensor):
@@ -491,20 +520,42 @@ class GbCpTensor(GbVmTensor):
         return list(self.vectors_density) + list(self.vectors_color)
 
     def resample_tensor(self, res):
-        """upsample_vectors (:1106-1116)."""
+        """upsample_vectors (:1106-1116) on the srf_resample_grid kernel."""
         def up(vecs):
-            return torch.nn.ParameterList([torch.nn.Parameter(T.to_channels_last(tF.interpolate(
-                vecs[i].data, size=(int(res[VECTOR_AXES[i]]), 1), mode='bilinear', align_corners=True)))
-                for i in range(3)])
+            return torch.nn.ParameterList([torch.nn.Parameter(T.resample_grid(
+                T.to_channels_last(vecs[i].data), int(res[VECTOR_AXES[i]]), 1)) for i in range(3)])
         self.vectors_density = up(self.vectors_density)
         self.vectors_color = up(self.vectors_color)
 
+    def reshape_tensor(self, res):
+        for kind in ('density', 'color'):
+            vecs = getattr(self, f'vectors_{kind}')
+            setattr(self, f'vectors_{kind}', torch.nn.ParameterList([torch.nn.Parameter(T.to_channels_last(
+                torch.zeros(1, vecs[i].shape[1], int(res[VECTOR_AXES[i]]), 1, device=vecs[i].device)))
+                for i in range(3)]))
+
+    @torch.no_grad()
+    def dense_alpha(self):
+        """Alpha on every grid node through the CP density lookups, z-major."""
+        gs = [int(r) for r in self.resolution]
+        dev = self.bounding_box.device
+        t = [torch.linspace(0, 1, g).to(dev) for g in gs]
+        samples = torch.stack(torch.meshgrid(*t, indexing='ij'), -1)
+        xyz = self.bounding_box[0] * (1 - samples) + self.bounding_box[1] * samples
+        alpha = torch.empty(gs, device=dev).view(-1)
+        flat = xyz.view(-1, 3)
+        chunk = 1 << 22
+        for a in range(0, flat.shape[0], chunk):
+            alpha[a:a + chunk] = self.compute_alpha(flat[a:a + chunk], self.step_size)
+        return alpha.view(gs).clamp(0, 1).transpose(0, 2).contiguous()
+
     def crop_tensor(self, t_l, b_r):
-        """shrink_tensor (:1118-1123)."""
+        """shrink_tensor (:1118-1123) on the srf_crop_grid kernel."""
+        t_l, b_r = [int(x) for x in t_l], [int(x) for x in b_r]
         for vlist in (self.vectors_density, self.vectors_color):
             for i in range(3):
                 v = VECTOR_AXES[i]
-                vlist[i] = torch.nn.Parameter(T.to_channels_last(vlist[i].data[..., t_l[v]:b_r[v], :]))
+                vlist[i] = torch.nn.Parameter(T.crop_grid(T.to_channels_last(vlist[i].data), t_l[v], b_r[v], 0, 1))
 
 
 def make_tensor_model(name, configs, tensor_configs, model_configs):

@@ -177,6 +177,7 @@ class NerfTrainStep:
         self.level = {lv: {'z': torch.zeros(n, ss, **f32), 'pts': torch.zeros(n * ss, 3, **f32)}
                       for lv, ss in (('coarse', sc), ('fine', s))}
         self.loss = torch.zeros(1, **f32)
+        self._loss_structs = {}
         self.step_count = torch.zeros(1, dtype=torch.int32, device=self.dev)
         # augmented coarse nets run on their own streams, concurrently with the main
         # nets (they share only the read-only samples; their depth joins the main
@@ -221,9 +222,30 @@ class NerfTrainStep:
             if self.ndc:
                 a.depth_ndc, a.depth_var_ndc = b['depth_ndc'].data_ptr(), b['depth_var_ndc'].data_ptr()
         else:
-            a.g_rgb, a.g_depth = b['g_rgb'].data_ptr(), b['g_depth'].data_ptr()
+            # the rgb / depth loss gradients come from the fused loss; g_depth carries
+            # only the consistency term's share (main coarse net of the pair)
+            if net is self.run[0] and self._consistency():
+                a.g_depth = b['g_depth'].data_ptr()
             a.d_sigma, a.d_rgb = b['d_sigma'].data_ptr(), b['d_rgb'].data_ptr()
         return a
+
+    def _consistency(self):
+        """Whether an augmented coarse net's depth is a consistency target of the main coarse depth."""
+        return self.consistency_weight > 0 and any(x.level == 'coarse' for x in self.run[2:])
+
+    def _loss_args(self, net):
+        """rgb MSE of this net (MSE14.compute_mse) plus, with depth-supervised rays, the
+        L1 depth term, evaluated inside compositing (srf_composite_loss)."""
+        key = net.name
+        if key not in self._loss_structs:
+            L = _lib.CompositeLoss()
+            L.target_rgb, L.rgb_weight = self.target_rgb.data_ptr(), 1.0
+            if self.n_depth > 0:
+                L.target_depth, L.depth_mask = self.target_depth.data_ptr(), self.depth_mask.data_ptr()
+                L.n_depth_rays, L.depth_weight, L.depth_squared = self.n_depth, float(self.depth_weight), 0
+            L.loss = self.loss.data_ptr()
+            self._loss_structs[key] = L
+        return self._loss_structs[key]
 
     def _enqueue(self):
         lib = _lib.load()
@@ -269,13 +291,14 @@ class NerfTrainStep:
                                              self.precision, int(self.train), _vp(b['ws']), b['ws'].numel(),
                                              _vp(self.scaler), sp),
                     'mlp_forward')
-                chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(net, False)), sp),
-                    'composite_forward')
                 if self.train:
-                    chk(lib.srf_rgb_depth_loss(_vp(b['rgb_map']), _vp(self.target_rgb), _vp(b['depth']),
-                                               _vp(self.target_depth), _vp(self.depth_mask), n, self.n_depth,
-                                               self.depth_weight, _vp(self.loss), _vp(b['g_rgb']),
-                                               _vp(b['g_depth']), sp), 'loss')
+                    # the loss of this net's render is evaluated in the compositing
+                    # epilogue; its gradient is recomputed inside the adjoint
+                    chk(lib.srf_composite_forward_loss(ctypes.byref(self._composite_args(net, False)),
+                                                       ctypes.byref(self._loss_args(net)), sp), 'composite_forward')
+                else:
+                    chk(lib.srf_composite_forward(ctypes.byref(self._composite_args(net, False)), sp),
+                        'composite_forward')
                 if net.name in side_of:
                     ev = torch.cuda.Event()
                     ev.record(side_of[net.name])
@@ -313,6 +336,10 @@ class NerfTrainStep:
         """The consistency term (augmented coarse depth as a detached target of the
         main coarse depth) and the main coarse net's backward, on ``stream``."""
         sp = _P(stream.cuda_stream)
+        if self._consistency():
+            # the consistency terms accumulate into the main coarse depth gradient
+            with torch.cuda.stream(stream):
+                main_coarse.b['g_depth'].zero_()
         for net in self.run[2:]:
             if net.level == 'coarse' and self.consistency_weight > 0:
                 if net.name in done:
@@ -325,8 +352,8 @@ class NerfTrainStep:
     def _backward(self, lib, net, stream):
         b = net.b
         ss = self.level[net.level]['z'].shape[1]
-        _lib.check(lib.srf_composite_backward(ctypes.byref(self._composite_args(net, True)), stream),
-                   'composite_backward')
+        _lib.check(lib.srf_composite_backward_loss(ctypes.byref(self._composite_args(net, True)),
+                                                   ctypes.byref(self._loss_args(net)), stream), 'composite_backward')
         _lib.check(lib.srf_nerf_mlp_backward(ctypes.byref(net.spec.desc), net.state.pptr, _vp(b['d_sigma']),
                                              _vp(b['d_rgb']), ss, self.n * ss, net.state.gptr, 0, self.precision,
                                              _vp(b['ws']), b['ws'].numel(), _vp(self.scaler), stream),

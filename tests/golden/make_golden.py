@@ -929,6 +929,63 @@ def reprojection_case():
                 grad1=d1.grad.numpy(), grad2=d2.grad.numpy())
 
 
+def coarse_fine_case():
+    """CoarseFineConsistencyLoss34.compute_loss on the reprojection case's 4 views
+    and 300 rays with coarse / fine depths (some rays reproject outside the image
+    with both depths, where AugmentationsDepthLoss11 would add its both-invalid
+    rule), 40 of them sparse-depth rays: masks (from the spy on compute_depth_mse),
+    loss and autograd gradients into both depths."""
+    from loss_functions import CoarseFineConsistencyLoss34 as LCF
+    g = torch.Generator().manual_seed(43)
+    v, h, w = 4, 30, 40
+    images = torch.rand(v, h, w, 3, generator=g)
+    yy, xx = torch.meshgrid(torch.arange(h).float(), torch.arange(w).float(), indexing='ij')
+    base = torch.stack([torch.sin(xx / 5), torch.cos(yy / 4), torch.sin((xx + yy) / 7)], -1) * 0.5 + 0.5
+    images = 0.9 * base[None].expand(v, h, w, 3) + 0.1 * images
+    poses = torch.eye(4).repeat(v, 1, 1)
+    poses[:, :3, 3] = torch.tensor([[0.0, 0.0, 0.0], [0.06, 0.0, 0.0], [0.0, 0.05, 0.01], [-0.07, 0.02, 0.0]])
+    k = torch.tensor([[30.0, 0.0, w / 2.0], [0.0, 30.0, h / 2.0], [0.0, 0.0, 1.0]])
+    intr = k[None].repeat(v, 1, 1)
+    n = 300
+    img = torch.randint(0, v, (n,), generator=g)
+    px = torch.randint(0, w, (n,), generator=g)
+    py = torch.randint(0, h, (n,), generator=g)
+    pid = torch.stack([img, px, py], -1)
+    rays_o, rays_d = CU.get_rays_tr(pid, intr[img], poses[img], False)
+    dc = 1.5 + torch.rand(n, generator=g) * 2
+    df = 1.5 + torch.rand(n, generator=g) * 2
+    dc[:20] = 0.05          # very near: both reprojections far outside the image
+    df[:20] = 0.04
+    dc, df = dc.requires_grad_(True), df.requires_grad_(True)
+    sd = torch.zeros(n, dtype=torch.bool)
+    sd[-40:] = True
+    nerf = ~sd
+    configs = {'model': {'coarse_model': {}, 'fine_model': {}}, 'data_loader': {'sparse_depth': {}}}
+    loss_fn = LCF.CoarseFineConsistencyLoss(configs, {'patch_size': [5, 5], 'rmse_threshold': 0.2})
+    seen = []
+    orig = LCF.CoarseFineConsistencyLoss.compute_depth_mse.__func__
+
+    def spy(cls, pred_depth, gt_depth, mask=None):
+        seen.append(None if mask is None else mask.clone())
+        return orig(cls, pred_depth, gt_depth, mask)
+
+    LCF.CoarseFineConsistencyLoss.compute_depth_mse = classmethod(spy)
+    try:
+        out = loss_fn.compute_loss(
+            {'target_rgb': torch.zeros(n, 3), 'common_data': {'images': images, 'resolution': (h, w)},
+             'indices_mask_nerf': nerf, 'indices_mask_sparse_depth': sd, 'pixel_id': pid},
+            {'rays_o': rays_o, 'rays_d': rays_d, 'depth_coarse': dc, 'depth_fine': df, 'intrinsics': intr,
+             'extrinsics_all': poses}, None)
+    finally:
+        LCF.CoarseFineConsistencyLoss.compute_depth_mse = classmethod(orig)
+    out['loss_value'].backward()
+    return dict(images=images.numpy(), poses=poses.numpy(), k=k.numpy(), pixel_ids=pid.numpy().astype(np.int32),
+                rays_o=rays_o.numpy(), rays_d=rays_d.numpy(), depth_coarse=dc.detach().numpy(),
+                depth_fine=df.detach().numpy(), nerf_mask=nerf.numpy(), sd_mask=sd.numpy(),
+                loss=out['loss_value'].detach().numpy(), mask1=seen[1].numpy(), mask2=seen[0].numpy(),
+                grad_coarse=dc.grad.numpy(), grad_fine=df.grad.numpy())
+
+
 def tv_case():
     """TotalVariationLoss04 on random grids with autograd gradients:
     compute_tv_loss on three VM-like planes of unequal shapes (one with a single
@@ -1010,6 +1067,7 @@ def main():
         'tensorf_maintenance': tensorf_maintenance_case,
         'losses': losses_case,
         'reprojection': reprojection_case,
+        'coarse_fine': coarse_fine_case,
         'tv': tv_case,
         'camera_learners': camera_learners_case,
     }

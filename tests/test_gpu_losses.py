@@ -247,3 +247,180 @@ def test_tv_loss_rejects_bad_shapes():
     null = (_lib.TvComponent * 1)(_lib.TvComponent(None, None, 2, 3, 4, 1, 8, 2))
     assert lib.srf_tv_loss(null, 1, 1.0, None, None, None) != 0
     assert lib.srf_tv_loss(None, 0, 1.0, None, None, None) == 0
+
+
+def _composite_setup(n, s, seed, white):
+    from simple_rf_gb300 import _lib
+    g = torch.Generator().manual_seed(seed)
+    sigma = (torch.rand(n, s, generator=g) * 3 - 0.5).clamp_min(0).to(DEV)
+    rgb = torch.rand(n, s, 3, generator=g).to(DEV)
+    z = torch.sort(torch.rand(n, s, generator=g) * 4 + 2, 1).values.to(DEV).contiguous()
+    d = torch.nn.functional.normalize(torch.randn(n, 3, generator=g), dim=-1).to(DEV)
+    tr = torch.rand(n, 3, generator=g).to(DEV)
+    td = (torch.rand(n, generator=g) * 4 + 2).to(DEV)
+    dmask = (torch.rand(n, generator=g) < 0.25).to(torch.uint8).to(DEV)
+    mcmask = (torch.rand(n, generator=g) < 0.6).to(torch.uint8).to(DEV)
+    bufs = {k: torch.zeros(n, device=DEV) for k in ('acc', 'depth', 'depth_var')}
+    bufs['rgb_map'] = torch.zeros(n, 3, device=DEV)
+    bufs['weights'] = torch.zeros(n, s, device=DEV)
+    a = _lib.CompositeArgs()
+    a.n_rays, a.n_samples = n, s
+    a.flags = _lib.SRF_COMPOSITE_WHITE_BKGD if white else 0
+    a.distance_scale = 1.0
+    a.sigma, a.rgb, a.z, a.rays_d = sigma.data_ptr(), rgb.data_ptr(), z.data_ptr(), d.data_ptr()
+    a.rgb_map, a.acc, a.depth = bufs['rgb_map'].data_ptr(), bufs['acc'].data_ptr(), bufs['depth'].data_ptr()
+    a.depth_var, a.weights = bufs['depth_var'].data_ptr(), bufs['weights'].data_ptr()
+    keep = (sigma, rgb, z, d)
+    return a, bufs, (tr, td, dmask, mcmask), keep
+
+
+@pytest.mark.parametrize('s,white,bins,squared', [(192, True, 0, 0), (64, False, 5, 0), (256, True, 5, 1),
+                                                  (129, False, 7, 0)])
+def test_composite_fused_loss_matches_separate_kernels(s, white, bins, squared):
+    """srf_composite_forward_loss / srf_composite_backward_loss (the training loss
+    evaluated in the compositing epilogue, its gradient recomputed in the adjoint)
+    against the separate path: srf_composite_forward, the loss kernels
+    (srf_rgb_depth_loss for MSE14 + L1 depth, srf_depth_mse_loss for the squared
+    depth error, srf_mass_concentration_loss for MassConcentrationLoss06), and
+    srf_composite_backward fed with their gradients.  Loss within 1e-6 relative;
+    d_sigma / d_rgb within 1e-6 relative (absolute floor 1e-9 of the range): the
+    fused path sums each bin's weights in another order."""
+    import ctypes
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _stream
+    n = 4096
+    a, bufs, (tr, td, dmask, mcmask), keep = _composite_setup(n, s, 11 + s, white)
+    st = _stream()
+    nd, nmc = int(dmask.sum().item()), int(mcmask.sum().item())
+    # separate kernels
+    _lib.call('srf_composite_forward', ctypes.byref(a), st)
+    loss_ref = torch.zeros(1, device=DEV)
+    g_rgb = torch.zeros(n, 3, device=DEV)
+    g_depth = torch.zeros(n, device=DEV)
+    g_w = torch.zeros(n, s, device=DEV)
+    if squared:
+        _lib.call('srf_rgb_depth_loss', bufs['rgb_map'].data_ptr(), tr.data_ptr(), bufs['depth'].data_ptr(),
+                  td.data_ptr(), None, n, 0, 0.0, loss_ref.data_ptr(), g_rgb.data_ptr(), g_depth.data_ptr(), st)
+        _lib.call('srf_depth_mse_loss', bufs['depth'].data_ptr(), td.data_ptr(), dmask.data_ptr(), n, 0.1, 1,
+                  loss_ref.data_ptr(), g_depth.data_ptr(), None, st)
+    else:
+        _lib.call('srf_rgb_depth_loss', bufs['rgb_map'].data_ptr(), tr.data_ptr(), bufs['depth'].data_ptr(),
+                  td.data_ptr(), dmask.data_ptr(), n, nd, 0.1, loss_ref.data_ptr(), g_rgb.data_ptr(),
+                  g_depth.data_ptr(), st)
+    if bins:
+        _lib.call('srf_mass_concentration_loss', bufs['weights'].data_ptr(), n, s, bins, mcmask.data_ptr(), 0.01,
+                  loss_ref.data_ptr(), g_w.data_ptr(), st)
+    ref_out = {k: v.clone() for k, v in bufs.items()}
+    d_sigma_ref, d_rgb_ref = torch.zeros(n, s, device=DEV), torch.zeros(n, s, 3, device=DEV)
+    a.g_rgb, a.g_depth = g_rgb.data_ptr(), g_depth.data_ptr()
+    a.g_weights = g_w.data_ptr() if bins else None
+    a.d_sigma, a.d_rgb = d_sigma_ref.data_ptr(), d_rgb_ref.data_ptr()
+    _lib.call('srf_composite_backward', ctypes.byref(a), st)
+    # fused
+    for v in bufs.values():
+        v.zero_()
+    L = _lib.CompositeLoss()
+    loss = torch.zeros(1, device=DEV)
+    L.target_rgb, L.rgb_weight = tr.data_ptr(), 1.0
+    L.target_depth, L.depth_mask, L.n_depth_rays, L.depth_weight, L.depth_squared = \
+        td.data_ptr(), dmask.data_ptr(), nd, 0.1, squared
+    if bins:
+        L.num_bins, L.mc_mask, L.n_mc_rays, L.mc_weight = bins, mcmask.data_ptr(), nmc, 0.01
+    L.loss = loss.data_ptr()
+    a.g_rgb = a.g_depth = a.g_weights = None
+    _lib.call('srf_composite_forward_loss', ctypes.byref(a), ctypes.byref(L), st)
+    d_sigma, d_rgb = torch.zeros(n, s, device=DEV), torch.zeros(n, s, 3, device=DEV)
+    a.d_sigma, a.d_rgb = d_sigma.data_ptr(), d_rgb.data_ptr()
+    _lib.call('srf_composite_backward_loss', ctypes.byref(a), ctypes.byref(L), st)
+    torch.cuda.synchronize()
+    for k, v in bufs.items():
+        assert torch.equal(v, ref_out[k]), k
+    assert abs(loss.item() - loss_ref.item()) <= 1e-6 * abs(loss_ref.item()), (loss.item(), loss_ref.item())
+    for got, ref, name in ((d_sigma, d_sigma_ref, 'd_sigma'), (d_rgb, d_rgb_ref, 'd_rgb')):
+        np.testing.assert_allclose(got.cpu().numpy(), ref.cpu().numpy(), rtol=1e-6,
+                                   atol=1e-9 * float(ref.abs().max().item()), err_msg=name)
+    if not bins:
+        assert torch.equal(d_sigma, d_sigma_ref) and torch.equal(d_rgb, d_rgb_ref)
+    del keep
+
+
+def test_composite_fused_loss_rejects_long_rays_and_bad_bins():
+    import ctypes
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _stream
+    a, bufs, (tr, td, dmask, mcmask), keep = _composite_setup(64, 300, 1, False)
+    L = _lib.CompositeLoss()
+    loss = torch.zeros(1, device=DEV)
+    L.target_rgb, L.loss = tr.data_ptr(), loss.data_ptr()
+    lib = _lib.load()
+    assert lib.srf_composite_forward_loss(ctypes.byref(a), ctypes.byref(L), _stream()) == \
+        _lib.SRF_ERR_UNSUPPORTED
+    a, bufs, (tr, td, dmask, mcmask), keep = _composite_setup(64, 64, 2, False)
+    L.num_bins, L.n_mc_rays = 65, 64
+    assert lib.srf_composite_forward_loss(ctypes.byref(a), ctypes.byref(L), _stream()) == _lib.SRF_ERR_SHAPE
+    L.num_bins, L.loss = 5, None
+    assert lib.srf_composite_forward_loss(ctypes.byref(a), ctypes.byref(L), _stream()) == _lib.SRF_ERR_NULL
+
+
+def test_coarse_fine_consistency_drop_in_matches_reference_golden(golden):
+    """The drop-in CoarseFineConsistencyLoss (srf_coarse_fine_reprojection_masks +
+    srf_depth_mse_loss, autograd) against CoarseFineConsistencyLoss34.compute_loss
+    (golden coarse_fine): loss and the gradients into the coarse and fine depths
+    within 1e-5; the kernel's masks equal the reference's on the NeRF rays."""
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _ptr, _stream
+    from simple_rf_gb300.losses import CoarseFineConsistencyLoss
+    g = golden('coarse_fine')
+    nerf = g['nerf_mask']
+    t = {k: _t(g[k]) for k in ('rays_o', 'rays_d', 'images', 'poses', 'k')}
+    pid = _t(g['pixel_ids'], torch.int32)
+    dc = _t(g['depth_coarse']).requires_grad_(True)
+    df = _t(g['depth_fine']).requires_grad_(True)
+    n = dc.shape[0]
+    m1 = torch.empty(n, dtype=torch.uint8, device=DEV)
+    m2 = torch.empty_like(m1)
+    v, h, w, c = g['images'].shape
+    _lib.call('srf_coarse_fine_reprojection_masks', _ptr(t['rays_o']), _ptr(t['rays_d']), _ptr(dc.detach()),
+              _ptr(df.detach()), _ptr(pid), n, _ptr(t['poses']), v, _ptr(t['k']), _ptr(t['images']), h, w, c, 5, 5,
+              0.2, _ptr(m1), _ptr(m2), _stream())
+    np.testing.assert_array_equal(m1.cpu().numpy().astype(bool)[nerf], g['mask1'])
+    np.testing.assert_array_equal(m2.cpu().numpy().astype(bool)[nerf], g['mask2'])
+    configs = {'model': {'coarse_model': {}, 'fine_model': {}}, 'data_loader': {'sparse_depth': {}}}
+    loss_fn = CoarseFineConsistencyLoss(configs, {'patch_size': [5, 5], 'rmse_threshold': 0.2})
+    inp = {'target_rgb': torch.zeros(n, 3, device=DEV), 'pixel_id': pid,
+           'common_data': {'images': t['images'], 'resolution': (h, w)},
+           'indices_mask_nerf': torch.from_numpy(nerf).to(DEV),
+           'indices_mask_sparse_depth': torch.from_numpy(g['sd_mask']).to(DEV)}
+    out = {'rays_o': t['rays_o'], 'rays_d': t['rays_d'], 'depth_coarse': dc, 'depth_fine': df,
+           'intrinsics': t['k'][None].repeat(n, 1, 1), 'extrinsics_all': t['poses']}
+    loss = loss_fn.compute_loss(inp, out, None)['loss_value']
+    loss.backward()
+    assert abs(loss.item() - float(g['loss'])) <= 1e-5 * abs(float(g['loss']))
+    np.testing.assert_allclose(dc.grad.cpu().numpy(), g['grad_coarse'], rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(df.grad.cpu().numpy(), g['grad_fine'], rtol=1e-5, atol=1e-8)
+
+
+def test_augmentations_depth_drop_in_matches_reference_golden(golden):
+    """The drop-in AugmentationsDepthLoss on the reprojection golden: the main depth
+    as depth1, the augmented depth as depth2 (AugmentationsDepthLoss11.compute_loss_nerf),
+    loss and gradients within 1e-5."""
+    from simple_rf_gb300.losses import AugmentationsDepthLoss
+    g = golden('reprojection')
+    t = {k: _t(g[k]) for k in ('rays_o', 'rays_d', 'images', 'poses', 'k')}
+    pid = _t(g['pixel_ids'], torch.int32)
+    d1 = _t(g['depth1']).requires_grad_(True)
+    d2 = _t(g['depth2']).requires_grad_(True)
+    n = d1.shape[0]
+    h, w = g['images'].shape[1:3]
+    configs = {'model': {'coarse_model': {}, 'augmentations': [{'name': 'aug', 'coarse_model': {}}]}}
+    loss_fn = AugmentationsDepthLoss(configs, {'patch_size': [5, 5], 'rmse_threshold': 0.2})
+    inp = {'target_rgb': torch.zeros(n, 3, device=DEV), 'pixel_id': pid,
+           'common_data': {'images': t['images'], 'resolution': (h, w)},
+           'indices_mask_nerf': torch.ones(n, dtype=torch.bool, device=DEV)}
+    out = {'rays_o': t['rays_o'], 'rays_d': t['rays_d'], 'depth_coarse': d1, 'aug_depth_coarse': d2,
+           'intrinsics': t['k'][None].repeat(n, 1, 1), 'extrinsics_all': t['poses']}
+    loss = loss_fn.compute_loss(inp, out, None)['loss_value']
+    loss.backward()
+    assert abs(loss.item() - float(g['loss'])) <= 1e-5 * abs(float(g['loss']))
+    np.testing.assert_allclose(d1.grad.cpu().numpy(), g['grad1'], rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(d2.grad.cpu().numpy(), g['grad2'], rtol=1e-5, atol=1e-8)

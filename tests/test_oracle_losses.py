@@ -64,3 +64,24 @@ def test_tv_loss_single_row_and_column():
     # a (1, R, 1, 1) grid has no differences: loss 0, gradient 0 (counts floored at 1)
     loss, grads = ol.tv_loss([np.ones((1, 3, 1, 1))], 2.0)
     assert loss == 0.0 and not grads[0].any()
+
+
+def test_coarse_fine_consistency_matches_reference(golden):
+    """CoarseFineConsistencyLoss34.compute_loss (golden coarse_fine): masks on the NeRF
+    rays without AugmentationsDepthLoss11's both-invalid rule (20 rays reproject
+    outside the image with both depths), the masked depth term, the sparse-depth
+    term, and the gradients into the coarse and fine depths."""
+    g = golden('coarse_fine')
+    loss, gc, gf, m1, m2 = ol.coarse_fine_consistency_loss(
+        g['depth_coarse'].astype(np.float64), g['depth_fine'].astype(np.float64), g['nerf_mask'], g['sd_mask'],
+        g['rays_o'], g['rays_d'], g['pixel_ids'], g['poses'], g['k'], g['images'], (5, 5), 0.2)
+    np.testing.assert_array_equal(m1, g['mask1'])
+    np.testing.assert_array_equal(m2, g['mask2'])
+    assert abs(loss - float(g['loss'])) <= 1e-5 * abs(float(g['loss']))
+    np.testing.assert_allclose(gc, g['grad_coarse'], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(gf, g['grad_fine'], rtol=1e-5, atol=1e-9)
+    # the rule AugmentationsDepthLoss11 adds would have selected rays here
+    a1, a2, _, _ = ol.reprojection_masks(g['depth_coarse'][g['nerf_mask']], g['depth_fine'][g['nerf_mask']],
+                                         g['rays_o'][g['nerf_mask']], g['rays_d'][g['nerf_mask']],
+                                         g['pixel_ids'][g['nerf_mask']], g['poses'], g['k'], g['images'], (5, 5), 0.2)
+    assert (a1 | a2).sum() > (m1 | m2).sum()

@@ -123,32 +123,36 @@ def _vm_from_golden(g):
 
 
 def _grids(tm):
-    return {f'{kind}.{i}': plist[i].detach()[0].numpy()
+    return {f'{kind}.{i}': plist[i].detach()[0].cpu().numpy()
             for kind, plist in (('planes_density', tm.matrices_density), ('lines_density', tm.vectors_density),
                                 ('planes_color', tm.matrices_color), ('lines_color', tm.vectors_color))
             for i in range(3)}
 
 
+@pytest.mark.gpu
 def test_tensorf_grid_upsample_and_shrink_match_reference(golden):
-    """The drop-in's grid maintenance on the channels-last tensors against the
-    reference's VmDecomposedTensor (golden tensorf_maintenance): bilinear
-    upsampling to a new resolution (SimpleTensoRF09.py:1284-1301) within 1e-6, and
-    shrinking to an occupied box with an alpha mask of another resolution
-    (:899-914, 1303-1320) exactly, with the same resolution, box and sample count."""
+    """The drop-in's grid maintenance kernels (srf_resample_grid, srf_crop_grid) on
+    the channels-last tensors against the reference's VmDecomposedTensor (golden
+    tensorf_maintenance): bilinear upsampling to a new resolution
+    (SimpleTensoRF09.py:1284-1301) within 1e-6, and shrinking to an occupied box
+    with an alpha mask of another resolution (:899-914, 1303-1320) exactly, with
+    the same resolution, box and sample count."""
     torch = pytest.importorskip('torch')
+    from simple_rf_gb300 import build as b
+    b.build()
     from simple_rf_gb300.tensorf_model import AlphaGridMask
     g = golden('tensorf_maintenance')
-    tm = _vm_from_golden(g)
+    tm = _vm_from_golden(g).to('cuda')
     tm.resample_tensor(torch.tensor(g['res_up']))
     for k, v in _grids(tm).items():
         np.testing.assert_allclose(v, g[f'up_{k}'], rtol=1e-6, atol=1e-6, err_msg=k)
-    tm = _vm_from_golden(g)
-    tm.alpha_mask = AlphaGridMask(torch.from_numpy(g['alpha_vol']), torch.from_numpy(g['bbox']))
-    tm.shrink_tensor(torch.from_numpy(g['box_new']))
+    tm = _vm_from_golden(g).to('cuda')
+    tm.alpha_mask = AlphaGridMask(torch.from_numpy(g['alpha_vol']).cuda(), torch.from_numpy(g['bbox']).cuda())
+    tm.shrink_tensor(torch.from_numpy(g['box_new']).cuda())
     for k, v in _grids(tm).items():
         np.testing.assert_array_equal(v, g[f'shrunk_{k}'], err_msg=k)
-    np.testing.assert_array_equal(tm.resolution.numpy(), g['shrunk_res'])
-    np.testing.assert_allclose(tm.bounding_box.numpy(), g['shrunk_bbox'], rtol=1e-6)
+    np.testing.assert_array_equal(tm.resolution.cpu().numpy(), g['shrunk_res'])
+    np.testing.assert_allclose(tm.bounding_box.cpu().numpy(), g['shrunk_bbox'], rtol=1e-6)
     assert int(tm.num_samples) == int(g['shrunk_num_samples'])
     np.testing.assert_allclose(float(tm.step_size), float(g['shrunk_step_size']), rtol=1e-6)
 
