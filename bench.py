@@ -317,6 +317,22 @@ def kernel_rooflines(hbm_peak, peak_kind):
     return out
 
 
+def fp32_plain_block(ws, k32, t_fp):
+    """The FP32 SIMT step with its arithmetic rate: 6 x 593,408 MAC-FLOP per sample
+    over 64 + 64 + 128 samples per ray, against the FP32 FMA peak of the SMs the
+    GEMM fills (152 SMs x 128 FP32 lanes x 2 FLOP x the maximum SM clock)."""
+    rate = job_rays_per_s(ws, N_RAYS, k32, t_fp)
+    tflops = rate * 6 * MACS_PER_SAMPLE * (N_COARSE + N_COARSE + N_FINE) / 1e12 / ws
+    try:
+        with open(os.path.join(REPO, 'MEASURED_PEAKS.json')) as f:
+            mhz = float(json.load(f)['sm_max_mhz'])
+    except Exception:
+        mhz = 2070.0
+    peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+    return {'value': round(rate, 1), 'unit': 'rays/s', 'ms_per_step': round(1e3 * t_fp / k32, 3), 'steps': k32,
+            'tflops': round(tflops, 1), 'fp32_simt_peak_tflops': round(peak, 1), 'frac_of_fp32_peak': round(tflops / peak, 3)}
+
+
 def rgb_agreement(step_cls, batch, dev):
     """Coarse-pass rgb of the headline (FP16) and the BF16 step against the FP32 plain step from the same
     weights and batch (the fine pass samples different depths once the coarse

@@ -117,7 +117,9 @@ class _ReprojectionDepthLoss(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g_loss, _g1, _g2):
         (g1,) = ctx.saved_tensors
-        return g1 * g_loss, None, None, None
+        # depth2 enters only as a detached target: a zero gradient, as in the reference
+        g2 = torch.zeros_like(g1) if ctx.needs_input_grad[1] else None
+        return g1 * g_loss, g2, None, None
 
 
 class _DepthConsistencyLoss:

@@ -189,6 +189,37 @@ class NerfTrainStep:
         self.cb_stream = _lib.new_stream(self.dev) if (overlap_coarse and train) else None
         self.graph = None
         self.launches_per_step = None
+        self.batcher = None
+
+    def attach_batcher(self, batcher, seed=0):
+        """Take every step's batch from ``batcher`` (a GpuRayBatcher over cached rays with
+        cameras) inside the step itself: the batch gathers, the rays of its pixels
+        (srf_pixel_rays, CommonUtils04.get_rays_tr), the stratified and inverse-CDF
+        uniforms (srf_uniforms, keyed by the batch counter) and the counter's advance
+        are enqueued with the render, so a captured step is the whole training
+        iteration of Trainer10.train_one_iter.  No depth supervision in this form."""
+        if batcher.num_rays != self.n or batcher.nsd:
+            raise ValueError('the batcher must serve exactly the step\'s rays (no sparse-depth rows)')
+        if 'intrinsics' not in batcher.out or 'extrinsics' not in batcher.out:
+            raise ValueError('the batcher needs the cameras (intrinsics and extrinsics) to form rays')
+        if self.ndc:
+            raise NotImplementedError('batches from cached rays are supported for world-space rays')
+        self.batcher = batcher
+        self.batch_seed = int(seed) & ((1 << 64) - 1)
+        self.n_depth = 0
+        self.depth_mask.zero_()
+        self._loss_structs = {}
+
+    def _enqueue_batch(self, lib, st):
+        b = self.batcher
+        o = b.assemble()
+        n = self.n
+        _lib.check(lib.srf_pixel_rays(_vp(o['pixel_id']), _vp(o['intrinsics']), _vp(o['extrinsics']), n, 0,
+                                      _vp(self.rays_o), _vp(self.rays_d), st), 'pixel_rays')
+        self.target_rgb.copy_(o['target_rgb'])
+        if self.perturb:
+            for sid, u in enumerate((self.u_c, self.u_f)):
+                _lib.check(lib.srf_uniforms(_vp(u), u.numel(), self.batch_seed, _vp(b.counter), sid, st), 'uniforms')
 
     @property
     def buf(self):
@@ -252,6 +283,8 @@ class NerfTrainStep:
         st = _P(torch.cuda.current_stream(self.dev).cuda_stream)
         chk = _lib.check
         n = self.n
+        if self.batcher is not None:
+            self._enqueue_batch(lib, st)
         if self.ndc:
             h, w = self.ndc['h'], self.ndc['w']
             chk(lib.srf_ndc_rays(_vp(self.rays_o), _vp(self.rays_d), _vp(self.focal), _vp(self.focal), n, h, w,
@@ -331,6 +364,8 @@ class NerfTrainStep:
                                   self.found_inf, st), 'adam')
         if self.scaler is not None:
             chk(lib.srf_loss_scaler_update(_vp(self.scaler), 2.0, 0.5, 2000, st), 'loss_scaler_update')
+        if self.batcher is not None:
+            self.batcher.advance()
 
     def _coarse_backward(self, lib, main_coarse, done, stream):
         """The consistency term (augmented coarse depth as a detached target of the

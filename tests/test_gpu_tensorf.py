@@ -383,7 +383,7 @@ def test_drop_in_tensorf_forward_from_pixels_matches_reference(golden, tag):
           'bounding_box': np.array(bbox)}
     database = 'NeRF_Synthetic' if tag == 'synthetic' else 'NeRF_LLFF'
     m = GbSimpleTensoRF({'data_loader': {'ndc': ndc}, 'model': model, 'database': database}, mc)
-    sd = {k[len(tag) + 4:]: torch.from_numpy(g[k]) for k in g.files if k.startswith(f'{tag}_sd.')}
+    sd = {k[len(tag) + 4:]: torch.from_numpy(g[k]) for k in g if k.startswith(f'{tag}_sd.')}
     m.load_state_dict(sd)
     m = m.to(DEV).eval()
     pix = torch.from_numpy(g['pixel_id']).to(DEV)
@@ -393,7 +393,7 @@ def test_drop_in_tensorf_forward_from_pixels_matches_reference(golden, tag):
         sbatch = dict(batch, common_data={'view_intrinsic': None, 'processed_view_pose':
                                           torch.from_numpy(g['view_pose']).float()[None].to(DEV)})
         ret_s = m(sbatch, retraw=True, mode='static_camera')
-    ref = {k[len(tag) + 5:]: g[k] for k in g.files if k.startswith(f'{tag}_out.')}
+    ref = {k[len(tag) + 5:]: g[k] for k in g if k.startswith(f'{tag}_out.')}
     got = {k: v.cpu().numpy() for k, v in ret.items() if isinstance(v, torch.Tensor)}
     assert set(ref) <= set(got), set(ref) - set(got)
     keep = threshold_stable(got['weights_coarse'], ref['weights_coarse'])
