@@ -6,6 +6,7 @@
 // Formulas follow SimpleNeRF17.py:486-558 (NeRF) and SimpleTensoRF09.py:767-819
 // (TensoRF: the extra distance_scale factor).
 #include "srf_common.cuh"
+#include "tc_primitives.cuh"
 
 namespace srf {
 namespace {
@@ -388,14 +389,13 @@ __device__ __forceinline__ void exp_scan_rounds(float (&Y)[R], int lane) {
     }
 }
 
+// One ray of the forward (lane j holds samples j, j + 32, ...): c's sigma / z and
+// rgb may point at global memory or at a shared-memory copy of the ray.
 template <int R, bool LOSS>
-__global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_args a, LossArgs L) {
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int r = blockIdx.x * (blockDim.x >> 5) + warp;
-    if (r >= a.n_rays) return;
-    RayCtx c = make_ctx(a, r);
+__device__ __forceinline__ void fwd_ray(const srf_composite_args& a, const LossArgs& L, int r, RayCtx c,
+                                        const float* rgb) {
+    const int lane = threadIdx.x & 31;
     const bool exp_prefix = (a.flags & SRF_COMPOSITE_EXP_PREFIX) != 0;
-    const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;   // NULL: zero colours
     float al[R], T[R], zz[R], c0[R], c1[R], c2[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -512,13 +512,20 @@ __global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_ar
 }
 
 template <int R, bool LOSS>
-__global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_args a, LossArgs L) {
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) composite_fwd_reg_kernel(srf_composite_args a, LossArgs L) {
+    int warp = threadIdx.x >> 5;
     int r = blockIdx.x * (blockDim.x >> 5) + warp;
     if (r >= a.n_rays) return;
     RayCtx c = make_ctx(a, r);
+    fwd_ray<R, LOSS>(a, L, r, c, a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr);   // NULL: zero colours
+}
+
+// One ray of the adjoint; sigma / z / rgb as in fwd_ray.
+template <int R, bool LOSS>
+__device__ __forceinline__ void bwd_ray(const srf_composite_args& a, const LossArgs& L, int r, RayCtx c,
+                                        const float* rgb) {
+    const int lane = threadIdx.x & 31;
     const bool exp_prefix = (a.flags & SRF_COMPOSITE_EXP_PREFIX) != 0;
-    const float* rgb = a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr;
     const int64_t ro = int64_t(r) * c.s;
     // G holds dL/dw_i once formed; until then the colour dot product's partial terms
     float al[R], T[R], ex_[R], dl[R], zz[R], G[R];
@@ -740,6 +747,93 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
     }
 }
 
+template <int R, bool LOSS>
+__global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_args a, LossArgs L) {
+    int warp = threadIdx.x >> 5;
+    int r = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (r >= a.n_rays) return;
+    RayCtx c = make_ctx(a, r);
+    bwd_ray<R, LOSS>(a, L, r, c, a.rgb ? a.rgb + int64_t(r) * c.s * 3 : nullptr);
+}
+
+// ---------------------------------------------------------------------------
+// Staged variants: persistent warps, each owning rays r, r + W, r + 2W, ...
+// (W warps in the grid).  Lane 0 of a warp copies the next ray's sigma, z and
+// rgb (contiguous per ray) into the warp's other shared-memory stage with bulk
+// asynchronous copies (cp.async.bulk, completion counted on an mbarrier) while
+// the warp composites the current ray from shared memory, so every warp keeps
+// one ray's bytes in flight independently of its registers.  Needs S % 4 == 0
+// and 16-byte aligned sigma / z / rgb (the bulk copies move 16-byte multiples).
+// A wait that runs out (4 s) raises the device flag and ends the warp.
+// ---------------------------------------------------------------------------
+
+constexpr int kStagedWarps = 8;
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     tc::smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+                 : "memory");
+}
+
+// Stage layout per warp and stage: sigma[S] | z[S] | rgb[3 S] (floats).
+__host__ __device__ __forceinline__ int staged_floats(int s) { return 5 * s; }
+
+__device__ __forceinline__ void stage_ray(const srf_composite_args& a, int r, float* st, uint64_t* bar) {
+    const int s = a.n_samples;
+    const uint32_t b1 = uint32_t(s) * 4u;
+    const uint32_t bytes = a.rgb ? 5u * b1 : 2u * b1;
+    tc::mbar_arrive_expect_tx(bar, bytes);
+    bulk_g2s(st, a.sigma + int64_t(r) * s, b1, bar);
+    bulk_g2s(st + s, a.z + int64_t(r) * s, b1, bar);
+    if (a.rgb) bulk_g2s(st + 2 * s, a.rgb + int64_t(r) * s * 3, 3u * b1, bar);
+}
+
+template <int R, bool LOSS, bool BWD>
+__global__ void __launch_bounds__(kStagedWarps * 32) composite_staged_kernel(srf_composite_args a, LossArgs L,
+                                                                              int* flag) {
+    extern __shared__ __align__(128) float smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int s = a.n_samples;
+    float* mine = smem + size_t(warp) * 2 * staged_floats(s);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + size_t(kStagedWarps) * 2 * staged_floats(s)) + 2 * warp;
+    const int stride = gridDim.x * kStagedWarps;
+    int r = blockIdx.x * kStagedWarps + warp;
+    if (lane == 0) {
+        tc::mbar_init(&bars[0], 1);
+        tc::mbar_init(&bars[1], 1);
+        tc::fence_barrier_init();
+    }
+    __syncwarp();
+    if (r < a.n_rays && lane == 0) stage_ray(a, r, mine, &bars[0]);
+    uint32_t phase0 = 0u, phase1 = 0u;   // mbarrier phases of the two stages
+    for (int k = 0; r < a.n_rays; ++k, r += stride) {
+        const int cur = k & 1;
+        float* st = mine + cur * staged_floats(s);
+        // the other stage was consumed in the previous iteration (the warp synced
+        // after it): prefetch the next ray there
+        if (r + stride < a.n_rays && lane == 0) stage_ray(a, r + stride, mine + (cur ^ 1) * staged_floats(s),
+                                                        &bars[cur ^ 1]);
+        if (!tc::mbar_wait(&bars[cur], cur ? phase1 : phase0, nullptr)) {
+            raise_flag(flag, kFlagTimeout);
+            // drain (bounded) whatever is still in flight into this warp's stages
+            tc::mbar_wait(&bars[cur ^ 1], cur ? phase0 : phase1, nullptr);
+            return;
+        }
+        if (cur) phase1 ^= 1u;
+        else phase0 ^= 1u;
+        RayCtx c = make_ctx(a, r);
+        c.sigma = st;
+        c.z = st + s;
+        const float* rgb = a.rgb ? st + 2 * s : nullptr;
+        if (BWD)
+            bwd_ray<R, LOSS>(a, L, r, c, rgb);
+        else
+            fwd_ray<R, LOSS>(a, L, r, c, rgb);
+        __syncwarp();
+    }
+}
+
 // out[r, c] = sum_s w[r, s] x[r, s, c] (one warp per ray); the adjoint gives
 // dw[r, s] = sum_c g[r, c] x[r, s, c] and dx[r, s, c] = w[r, s] g[r, c].
 __global__ void weighted_sum_kernel(const float* __restrict__ w, const float* __restrict__ x, int n, int s, int c,
@@ -812,24 +906,67 @@ int launch_reg(K kernel, const srf_composite_args* a, const LossArgs& L, void* s
     return launch_status();
 }
 
+bool stageable(const srf_composite_args* a) {
+    auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    return (a->n_samples & 3) == 0 && al16(a->sigma) && al16(a->z) && (!a->rgb || al16(a->rgb));
+}
+
+template <int R, bool LOSS, bool BWD>
+int launch_staged(const srf_composite_args* a, const LossArgs& L, void* stream) {
+    auto kernel = composite_staged_kernel<R, LOSS, BWD>;
+    const size_t smem = size_t(kStagedWarps) * 2 * staged_floats(a->n_samples) * sizeof(float) +
+                        size_t(kStagedWarps) * 2 * sizeof(uint64_t);
+    static int configured = 0;   // per instantiation: the largest shared-memory size set so far
+    if (int(smem) > configured) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+        configured = int(smem);
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kStagedWarps * 32, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return SRF_ERR_CUDA;
+    }
+    const int64_t need = (int64_t(a->n_rays) + kStagedWarps - 1) / kStagedWarps;
+    const int blocks = int(need < int64_t(sms) * per_sm ? need : int64_t(sms) * per_sm);
+    kernel<<<blocks, kStagedWarps * 32, smem, as_stream(stream)>>>(*a, L, device_flag());
+    return launch_status();
+}
+
 template <bool LOSS>
 int forward_reg(const srf_composite_args* a, const LossArgs& L, void* stream) {
+    const bool staged = stageable(a);
     switch (reg_rounds(a->n_samples)) {
-        case 2: return launch_reg(composite_fwd_reg_kernel<2, LOSS>, a, L, stream);
-        case 4: return launch_reg(composite_fwd_reg_kernel<4, LOSS>, a, L, stream);
-        case 6: return launch_reg(composite_fwd_reg_kernel<6, LOSS>, a, L, stream);
-        case 8: return launch_reg(composite_fwd_reg_kernel<8, LOSS>, a, L, stream);
+        case 2: return staged ? launch_staged<2, LOSS, false>(a, L, stream)
+                              : launch_reg(composite_fwd_reg_kernel<2, LOSS>, a, L, stream);
+        case 4: return staged ? launch_staged<4, LOSS, false>(a, L, stream)
+                              : launch_reg(composite_fwd_reg_kernel<4, LOSS>, a, L, stream);
+        case 6: return staged ? launch_staged<6, LOSS, false>(a, L, stream)
+                              : launch_reg(composite_fwd_reg_kernel<6, LOSS>, a, L, stream);
+        case 8: return staged ? launch_staged<8, LOSS, false>(a, L, stream)
+                              : launch_reg(composite_fwd_reg_kernel<8, LOSS>, a, L, stream);
         default: return SRF_ERR_UNSUPPORTED;
     }
 }
 
 template <bool LOSS>
 int backward_reg(const srf_composite_args* a, const LossArgs& L, void* stream) {
+    const bool staged = stageable(a);
     switch (reg_rounds(a->n_samples)) {
-        case 2: return launch_reg(composite_bwd_reg_kernel<2, LOSS>, a, L, stream);
-        case 4: return launch_reg(composite_bwd_reg_kernel<4, LOSS>, a, L, stream);
-        case 6: return launch_reg(composite_bwd_reg_kernel<6, LOSS>, a, L, stream);
-        case 8: return launch_reg(composite_bwd_reg_kernel<8, LOSS>, a, L, stream);
+        case 2: return staged ? launch_staged<2, LOSS, true>(a, L, stream)
+                              : launch_reg(composite_bwd_reg_kernel<2, LOSS>, a, L, stream);
+        case 4: return staged ? launch_staged<4, LOSS, true>(a, L, stream)
+                              : launch_reg(composite_bwd_reg_kernel<4, LOSS>, a, L, stream);
+        case 6: return staged ? launch_staged<6, LOSS, true>(a, L, stream)
+                              : launch_reg(composite_bwd_reg_kernel<6, LOSS>, a, L, stream);
+        case 8: return staged ? launch_staged<8, LOSS, true>(a, L, stream)
+                              : launch_reg(composite_bwd_reg_kernel<8, LOSS>, a, L, stream);
         default: return SRF_ERR_UNSUPPORTED;
     }
 }

@@ -254,3 +254,77 @@ def test_composite_exp_prefix_rejects_long_rays():
     with pytest.raises(RuntimeError, match='UNSUPPORTED'):
         F.CompositeFunction.apply(e, torch.rand(4, s, 3, device=DEV), e.sort(1)[0] + 2, torch.rand(4, 3, device=DEV),
                                   None, None, _lib.SRF_COMPOSITE_EXP_PREFIX, 1.0, None)
+
+
+@pytest.mark.parametrize('s', [64, 192, 256, 100, 4])
+@pytest.mark.parametrize('flags', [0, 1, 2, 4, 6])
+def test_composite_staged_equals_register_kernel(s, flags):
+    """Rays of a multiple of 4 samples with 16-byte aligned inputs run the staged
+    kernels (each warp's next ray copied to shared memory by bulk asynchronous
+    copies while it composites the current one); the same inputs 4 bytes off
+    16-byte alignment run the register kernels that read global memory.  Both
+    compute the same arithmetic in the same order: outputs and adjoints are
+    bitwise equal.  flags: 1 NDC, 2 white background, 4 exp-prefix transmittance."""
+    import ctypes
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300.functional import _stream
+    n = 3000
+    g = torch.Generator().manual_seed(s + flags)
+    sig = (torch.rand(n, s, generator=g) * 3 - 0.5).clamp_min(0)
+    rgb = torch.rand(n, s, 3, generator=g)
+    z = torch.sort(torch.rand(n, s, generator=g) * (0.9 if flags & 1 else 4) + (0.05 if flags & 1 else 2), 1).values
+    d = torch.nn.functional.normalize(torch.randn(n, 3, generator=g), dim=-1)
+    d[:, 2] = -d[:, 2].abs() - 0.5
+    o = torch.randn(n, 3, generator=g) * 0.1
+    o[:, 2] = -1.0
+    gs = {k: torch.randn(sh, generator=g) for k, sh in (('rgb', (n, 3)), ('acc', (n,)), ('depth', (n,)),
+                                                          ('depth_var', (n,)), ('weights', (n, s)))}
+
+    def run(misalign):
+        def put(x):
+            flat = x.reshape(-1)
+            buf = torch.zeros(flat.numel() + 4, device=DEV)
+            off = 1 if misalign else 0
+            buf[off:off + flat.numel()] = flat.to(DEV)
+            return buf, buf[off:off + flat.numel()].view(x.shape)
+        keep = []
+        ins = {}
+        for k, x in (('sigma', sig), ('rgb', rgb), ('z', z)):
+            b, v = put(x)
+            keep.append(b)
+            ins[k] = v
+        d_dev, o_dev = d.to(DEV).contiguous(), o.to(DEV).contiguous()
+        dn = (d_dev / d_dev[:, 2:3].abs()).contiguous()
+        outs = {k: torch.zeros(n, device=DEV) for k in ('acc', 'depth', 'depth_var', 'depth_ndc', 'depth_var_ndc')}
+        outs['rgb_map'] = torch.zeros(n, 3, device=DEV)
+        for k in ('alpha', 'visibility', 'weights', 'd_sigma'):
+            outs[k] = torch.zeros(n, s, device=DEV)
+        outs['d_rgb'] = torch.zeros(n, s, 3, device=DEV)
+        gd = {k: v.to(DEV).contiguous() for k, v in gs.items()}
+        a = _lib.CompositeArgs()
+        a.n_rays, a.n_samples, a.flags, a.distance_scale = n, s, flags, 1.0
+        a.sigma, a.rgb, a.z = ins['sigma'].data_ptr(), ins['rgb'].data_ptr(), ins['z'].data_ptr()
+        a.rays_d, a.rays_o, a.rays_d_ndc = d_dev.data_ptr(), o_dev.data_ptr(), dn.data_ptr()
+        for k in ('rgb_map', 'acc', 'depth', 'depth_var', 'depth_ndc', 'depth_var_ndc', 'alpha', 'visibility',
+                  'weights', 'd_sigma', 'd_rgb'):
+            setattr(a, k, outs[k].data_ptr())
+        a.g_rgb, a.g_acc, a.g_depth = gd['rgb'].data_ptr(), gd['acc'].data_ptr(), gd['depth'].data_ptr()
+        a.g_depth_var, a.g_weights = gd['depth_var'].data_ptr(), gd['weights'].data_ptr()
+        lib = _lib.load()
+        st = _stream()
+        if (flags & 4) and s > 256:
+            return None
+        _lib.check(lib.srf_composite_forward(ctypes.byref(a), st), 'forward')
+        _lib.check(lib.srf_composite_backward(ctypes.byref(a), st), 'backward')
+        torch.cuda.synchronize()
+        del keep
+        return {k: v.cpu() for k, v in outs.items()}
+
+    staged, plain = run(False), run(True)
+    for k in staged:
+        assert torch.equal(staged[k], plain[k]), k
+    import ctypes as _c
+    fl = _c.c_int(0)
+    _lib_mod = __import__('simple_rf_gb300._lib', fromlist=['check'])
+    _lib_mod.check(_lib_mod.load().srf_read_device_flag(_c.byref(fl), None), 'flag')
+    assert fl.value == 0
