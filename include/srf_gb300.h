@@ -391,7 +391,9 @@ int srf_compact(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* count_dev
  *   - n may not exceed SRF_COMPACT_NOALLOC_MAX_ELEMENTS; larger masks return
  *     SRF_ERR_SHAPE without launching anything (use srf_compact for those).
  *   - The first call on a device looks up the array's device address; make that
- *     first call before any CUDA stream capture on that device.
+ *     first call before any CUDA stream capture on that device.  The address is
+ *     cached per device for the context it was looked up in: after
+ *     cudaDeviceReset, reload the library before calling again.
  *   - All calls share the one array: calls whose kernels may overlap on the GPU
  *     (different streams, or different host threads) race and must be ordered by
  *     the caller.  Each call fully rewrites the scratch it reads. */
@@ -403,20 +405,24 @@ int srf_compact_noalloc(const uint8_t* mask, int64_t n, int32_t* idx, int32_t* c
 int srf_threshold_mask(const float* x, int64_t n, float threshold, uint8_t* mask, void* stream);
 
 /* Gather rows src[idx[i]] -> dst[i] (cols floats each), for i < *count_dev (max n). */
-int srf_gather_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
-                    int cols, int src_row_div, void* stream);
+int srf_gather_rows(float* dst, const float* src, int64_t src_rows, const int32_t* idx, const int32_t* count_dev,
+                    int64_t n, int cols, int src_row_div, void* stream);
 /* Scatter rows src[i] -> dst[idx[i]] (dst not cleared; rows not in idx untouched). */
-int srf_scatter_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
-                     int cols, void* stream);
+int srf_scatter_rows(float* dst, int64_t dst_rows, const float* src, const int32_t* idx, const int32_t* count_dev,
+                     int64_t n, int cols, void* stream);
 
 /* Density activation on compacted features: ReLU (mode 0) or softplus(x+offset)
- * (mode 1), written to sigma[idx[i]]; backward multiplies by the derivative.
- * Replaces LowRankTensor.get_density_predictor (src/models/SimpleTensoRF09.py:671-679). */
-int srf_density_activation(float* sigma_dense, const float* features, const int32_t* idx,
+ * (mode 1), written to sigma[idx[i]] of the rows-long dense sigma; backward
+ * multiplies by the derivative.
+ * Replaces LowRankTensor.get_density_predictor (src/models/SimpleTensoRF09.py:671-679).
+ * The row functions above take the row count of the dense side: an index outside
+ * [0, rows) (or past src_rows after the division) is skipped and sets the range
+ * bit of the device flag (srf_read_device_flag) instead of touching memory. */
+int srf_density_activation(float* sigma_dense, int64_t rows, const float* features, const int32_t* idx,
                            const int32_t* count_dev, int64_t n, int mode, float offset, void* stream);
-int srf_density_activation_backward(float* d_features, const float* d_sigma_dense, const float* features,
-                                    const int32_t* idx, const int32_t* count_dev, int64_t n, int mode,
-                                    float offset, void* stream);
+int srf_density_activation_backward(float* d_features, const float* d_sigma_dense, int64_t rows,
+                                    const float* features, const int32_t* idx, const int32_t* count_dev, int64_t n,
+                                    int mode, float offset, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Generic dense layer (TensoRF renderer MLP and basis matrix)               */
@@ -609,10 +615,13 @@ int srf_counter_add(int32_t* counter_dev, int value, const int32_t* skip_dev, vo
  * of its image from intrinsics (n_views,3,3) / extrinsics (n_views,4,4)
  * (optional: per-ray copies for srf_pixel_rays).  With pool_rows (pool_size
  * int32, optional) the permuted positions index that list and the gathers read
- * row pool_rows[...] (the sparse-depth pixels, a subset of the cached rays).
+ * row pool_rows[...] (the sparse-depth pixels, a subset of the cached rays);
+ * table_rows is the row count of pool_pixel_id / pool_values (>= pool_size without
+ * pool_rows): a pool_rows entry outside it gathers row 0 and sets the device flag.
  * Advance the counter with srf_counter_add after the step.  pool_size <= 2^30. */
 int srf_batch_assemble(const int32_t* pool_rows, const int32_t* pool_pixel_id, const float* pool_values, int channels,
-                       int64_t pool_size, int n_rays, uint64_t seed, const int32_t* batch_counter_dev,
+                       int64_t pool_size, int64_t table_rows, int n_rays, uint64_t seed,
+                       const int32_t* batch_counter_dev,
                        const float* intrinsics,
                        const float* extrinsics, int n_views, int32_t* out_pixel_id, float* out_values,
                        int32_t* out_index, float* out_intrinsics, float* out_extrinsics, void* stream);

@@ -128,10 +128,10 @@ _SIGS = {
     'srf_compact': (c_int, [P, c_int64, P, P, P, c_size_t, P]),
     'srf_compact_noalloc': (c_int, [P, c_int64, P, P, P]),
     'srf_threshold_mask': (c_int, [P, c_int64, c_float, P, P]),
-    'srf_gather_rows': (c_int, [P, P, P, P, c_int64, c_int, c_int, P]),
-    'srf_scatter_rows': (c_int, [P, P, P, P, c_int64, c_int, P]),
-    'srf_density_activation': (c_int, [P, P, P, P, c_int64, c_int, c_float, P]),
-    'srf_density_activation_backward': (c_int, [P, P, P, P, P, c_int64, c_int, c_float, P]),
+    'srf_gather_rows': (c_int, [P, P, c_int64, P, P, c_int64, c_int, c_int, P]),
+    'srf_scatter_rows': (c_int, [P, c_int64, P, P, P, c_int64, c_int, P]),
+    'srf_density_activation': (c_int, [P, c_int64, P, P, P, c_int64, c_int, c_float, P]),
+    'srf_density_activation_backward': (c_int, [P, P, c_int64, P, P, P, c_int64, c_int, c_float, P]),
     'srf_tensorf_renderer_workspace_size': (c_size_t, [ctypes.POINTER(RendererDesc), c_int64, c_int, c_int]),
     'srf_tensorf_renderer_forward': (c_int, [ctypes.POINTER(RendererDesc), ctypes.POINTER(P), P, P, c_int64, P, c_int,
                                              c_int, P, c_size_t, P, P]),
@@ -151,7 +151,7 @@ _SIGS = {
     'srf_coarse_fine_reprojection_masks': (c_int, [P, P, P, P, P, c_int, P, c_int, P, P, c_int, c_int, c_int, c_int, c_int,
                                              c_float, P, P, P]),
     'srf_ray_points': (c_int, [P, P, P, c_int, c_int, P, P]),
-    'srf_batch_assemble': (c_int, [P, P, P, c_int, c_int64, c_int, ctypes.c_uint64, P, P, P, c_int, P, P, P, P, P, P]),
+    'srf_batch_assemble': (c_int, [P, P, P, c_int, c_int64, c_int64, c_int, ctypes.c_uint64, P, P, P, c_int, P, P, P, P, P, P]),
     'srf_uniforms': (c_int, [P, c_int64, ctypes.c_uint64, P, c_int, P]),
     'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
     'srf_autotune_enable': (c_int, [c_int]),

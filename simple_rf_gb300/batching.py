@@ -84,7 +84,8 @@ class GpuRayBatcher:
         st = _stream()
         o = self.out
         n = self.num_rays
-        _lib.call('srf_batch_assemble', None, _ptr(self.pool_pid), _ptr(self.pool_rgb), 3, self.pool_pid.shape[0], n,
+        rows = self.pool_pid.shape[0]
+        _lib.call('srf_batch_assemble', None, _ptr(self.pool_pid), _ptr(self.pool_rgb), 3, rows, rows, n,
                   self.seed, _ptr(self.counter), _ptr(self.intr), _ptr(self.extr), self.n_views, _ptr(o['pixel_id']),
                   _ptr(o['target_rgb']), _ptr(o['indices']), _ptr(o.get('intrinsics')), _ptr(o.get('extrinsics')), st)
         if self.nsd:
@@ -94,7 +95,7 @@ class GpuRayBatcher:
             intr_tail = o['intrinsics'][n:] if 'intrinsics' in o else None
             extr_tail = o['extrinsics'][n:] if 'extrinsics' in o else None
             _lib.call('srf_batch_assemble', _ptr(self.sd_rows), _ptr(self.pool_pid), _ptr(self.sd_values), 5,
-                      self.sd_rows.numel(), m, (self.seed ^ 0x5D5D5D5D5D5D5D5D) & ((1 << 64) - 1),
+                      self.sd_rows.numel(), rows, m, (self.seed ^ 0x5D5D5D5D5D5D5D5D) & ((1 << 64) - 1),
                       _ptr(self.counter), _ptr(self.intr), _ptr(self.extr), self.n_views, _ptr(pid_tail),
                       _ptr(self.sd_out), _ptr(o['indices'][n:]), _ptr(intr_tail), _ptr(extr_tail), st)
             o['sparse_depth_values'][n:, 0].copy_(self.sd_out[:, 0])

@@ -70,8 +70,8 @@ __device__ __forceinline__ int64_t permute(int64_t pos, const Perm& p, int* flag
 }
 
 __global__ void batch_assemble_kernel(const int32_t* __restrict__ pool_rows, const int32_t* __restrict__ pool_pid,
-                                      const float* __restrict__ pool_val, int channels, int64_t pool, int n,
-                                      uint64_t seed,
+                                      const float* __restrict__ pool_val, int channels, int64_t pool,
+                                      int64_t table_rows, int n, uint64_t seed,
                                       const int32_t* __restrict__ counter, const float* __restrict__ intr,
                                       const float* __restrict__ extr, int n_views, int32_t* __restrict__ out_pid,
                                       float* __restrict__ out_val, int32_t* __restrict__ out_idx,
@@ -83,7 +83,11 @@ __global__ void batch_assemble_kernel(const int32_t* __restrict__ pool_rows, con
     const int64_t epoch = b / per_epoch;
     const int64_t pos = (b % per_epoch) * n + i;
     const Perm p = make_perm(pool, seed, epoch);
-    const int64_t j = pool_rows ? int64_t(pool_rows[permute(pos, p, flag)]) : permute(pos, p, flag);
+    int64_t j = pool_rows ? int64_t(pool_rows[permute(pos, p, flag)]) : permute(pos, p, flag);
+    if (j < 0 || j >= table_rows) {   // a bad entry of pool_rows: gather row 0 and raise the flag
+        raise_flag(flag, kFlagRange);
+        j = 0;
+    }
     if (out_idx) out_idx[i] = int32_t(j);
     int32_t img = 0;
     if (pool_pid) {
@@ -125,19 +129,20 @@ __global__ void uniforms_kernel(float* __restrict__ u, int64_t n, uint64_t seed,
 using namespace srf;
 
 extern "C" int srf_batch_assemble(const int32_t* pool_rows, const int32_t* pool_pixel_id, const float* pool_values,
-                                  int channels, int64_t pool_size, int n_rays, uint64_t seed,
+                                  int channels, int64_t pool_size, int64_t table_rows, int n_rays, uint64_t seed,
                                   const int32_t* batch_counter_dev,
                                   const float* intrinsics, const float* extrinsics, int n_views,
                                   int32_t* out_pixel_id, float* out_values, int32_t* out_index,
                                   float* out_intrinsics, float* out_extrinsics, void* stream) {
-    if (n_rays < 1 || pool_size < n_rays || pool_size > (int64_t(1) << 30) || channels < 0 || channels > 16)
+    if (n_rays < 1 || pool_size < n_rays || pool_size > (int64_t(1) << 30) || channels < 0 || channels > 16 ||
+        table_rows < 1 || (!pool_rows && table_rows < pool_size))
         return SRF_ERR_SHAPE;
     if (pool_pixel_id && !out_pixel_id) return SRF_ERR_NULL;
     if (channels > 0 && (!pool_values || !out_values)) return SRF_ERR_NULL;
     if ((intrinsics && !out_intrinsics) || (extrinsics && !out_extrinsics)) return SRF_ERR_NULL;
     if ((intrinsics || extrinsics) && (!pool_pixel_id || n_views < 1)) return SRF_ERR_SHAPE;
     batch_assemble_kernel<<<grid_1d(n_rays, 256), 256, 0, as_stream(stream)>>>(
-        pool_rows, pool_pixel_id, pool_values, channels, pool_size, n_rays, seed, batch_counter_dev, intrinsics, extrinsics,
+        pool_rows, pool_pixel_id, pool_values, channels, pool_size, table_rows, n_rays, seed, batch_counter_dev, intrinsics, extrinsics,
         n_views, out_pixel_id, out_values, out_index, out_intrinsics, out_extrinsics, device_flag());
     return launch_status();
 }

@@ -543,8 +543,12 @@ __global__ void write_idx_kernel(const uint8_t* __restrict__ mask, int64_t n, co
     }
 }
 
-__global__ void gather_rows_kernel(float* dst, const float* __restrict__ src, const int32_t* __restrict__ idx,
-                                   const int32_t* count, int64_t n, int cols, int div) {
+// The row gathers and scatters below index with compacted sample indices; an
+// index outside [0, rows) (a caller's bad count or index list) is skipped and
+// raises the device flag's range bit instead of touching memory.
+__global__ void gather_rows_kernel(float* dst, const float* __restrict__ src, int64_t src_rows,
+                                   const int32_t* __restrict__ idx, const int32_t* count, int64_t n, int cols,
+                                   int div, int* flag) {
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t cnt = *count < n ? *count : n;
     if (t >= cnt * cols) return;
@@ -552,17 +556,27 @@ __global__ void gather_rows_kernel(float* dst, const float* __restrict__ src, co
     int c = int(t % cols);
     int64_t row = idx[i];
     if (div > 1) row /= div;
+    if (row < 0 || row >= src_rows) {
+        raise_flag(flag, kFlagRange);
+        return;
+    }
     dst[t] = src[row * cols + c];
 }
 
-__global__ void scatter_rows_kernel(float* dst, const float* __restrict__ src, const int32_t* __restrict__ idx,
-                                    const int32_t* count, int64_t n, int cols) {
+__global__ void scatter_rows_kernel(float* dst, int64_t dst_rows, const float* __restrict__ src,
+                                    const int32_t* __restrict__ idx, const int32_t* count, int64_t n, int cols,
+                                    int* flag) {
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t cnt = *count < n ? *count : n;
     if (t >= cnt * cols) return;
     int64_t i = t / cols;
     int c = int(t % cols);
-    dst[int64_t(idx[i]) * cols + c] = src[t];
+    const int64_t row = idx[i];
+    if (row < 0 || row >= dst_rows) {
+        raise_flag(flag, kFlagRange);
+        return;
+    }
+    dst[row * cols + c] = src[t];
 }
 
 __device__ __forceinline__ float softplus_f(float x) {
@@ -570,23 +584,35 @@ __device__ __forceinline__ float softplus_f(float x) {
     return x > 20.f ? x : log1pf(expf(x));
 }
 
-__global__ void density_act_kernel(float* sigma, const float* __restrict__ f, const int32_t* __restrict__ idx,
-                                   const int32_t* count, int64_t n, int mode, float offset) {
+__global__ void density_act_kernel(float* sigma, int64_t rows, const float* __restrict__ f,
+                                   const int32_t* __restrict__ idx, const int32_t* count, int64_t n, int mode,
+                                   float offset, int* flag) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t cnt = *count < n ? *count : n;
     if (i >= cnt) return;
+    const int64_t row = idx[i];
+    if (row < 0 || row >= rows) {
+        raise_flag(flag, kFlagRange);
+        return;
+    }
     float x = f[i];
-    sigma[idx[i]] = mode == 0 ? relu_f(x) : softplus_f(x + offset);
+    sigma[row] = mode == 0 ? relu_f(x) : softplus_f(x + offset);
 }
 
-__global__ void density_act_bwd_kernel(float* df, const float* __restrict__ ds, const float* __restrict__ f,
-                                       const int32_t* __restrict__ idx, const int32_t* count, int64_t n, int mode,
-                                       float offset) {
+__global__ void density_act_bwd_kernel(float* df, const float* __restrict__ ds, int64_t rows,
+                                       const float* __restrict__ f, const int32_t* __restrict__ idx,
+                                       const int32_t* count, int64_t n, int mode, float offset, int* flag) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t cnt = *count < n ? *count : n;
     if (i >= cnt) return;
+    const int64_t row = idx[i];
+    if (row < 0 || row >= rows) {
+        raise_flag(flag, kFlagRange);
+        df[i] = 0.f;
+        return;
+    }
     float x = f[i];
-    float g = ds[idx[i]];
+    float g = ds[row];
     if (mode == 0) df[i] = x > 0.f ? g : 0.f;
     else {
         float y = x + offset;
@@ -882,43 +908,45 @@ extern "C" int srf_threshold_mask(const float* x, int64_t n, float threshold, ui
     return launch_status();
 }
 
-extern "C" int srf_gather_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
-                               int cols, int src_row_div, void* stream) {
+extern "C" int srf_gather_rows(float* dst, const float* src, int64_t src_rows, const int32_t* idx,
+                               const int32_t* count_dev, int64_t n, int cols, int src_row_div, void* stream) {
     if (!dst || !src || !idx || !count_dev) return SRF_ERR_NULL;
-    if (n < 0 || cols < 1 || src_row_div < 1) return SRF_ERR_SHAPE;
+    if (n < 0 || cols < 1 || src_row_div < 1 || src_rows < 0) return SRF_ERR_SHAPE;
     if (n == 0) return SRF_OK;
-    gather_rows_kernel<<<grid_1d(n * cols, 256), 256, 0, as_stream(stream)>>>(dst, src, idx, count_dev, n, cols,
-                                                                              src_row_div);
+    gather_rows_kernel<<<grid_1d(n * cols, 256), 256, 0, as_stream(stream)>>>(dst, src, src_rows, idx, count_dev, n,
+                                                                              cols, src_row_div, device_flag());
     return launch_status();
 }
 
-extern "C" int srf_scatter_rows(float* dst, const float* src, const int32_t* idx, const int32_t* count_dev, int64_t n,
-                                int cols, void* stream) {
+extern "C" int srf_scatter_rows(float* dst, int64_t dst_rows, const float* src, const int32_t* idx,
+                                const int32_t* count_dev, int64_t n, int cols, void* stream) {
     if (!dst || !src || !idx || !count_dev) return SRF_ERR_NULL;
-    if (n < 0 || cols < 1) return SRF_ERR_SHAPE;
+    if (n < 0 || cols < 1 || dst_rows < 0) return SRF_ERR_SHAPE;
     if (n == 0) return SRF_OK;
-    scatter_rows_kernel<<<grid_1d(n * cols, 256), 256, 0, as_stream(stream)>>>(dst, src, idx, count_dev, n, cols);
+    scatter_rows_kernel<<<grid_1d(n * cols, 256), 256, 0, as_stream(stream)>>>(dst, dst_rows, src, idx, count_dev, n,
+                                                                               cols, device_flag());
     return launch_status();
 }
 
-extern "C" int srf_density_activation(float* sigma_dense, const float* features, const int32_t* idx,
+extern "C" int srf_density_activation(float* sigma_dense, int64_t rows, const float* features, const int32_t* idx,
                                       const int32_t* count_dev, int64_t n, int mode, float offset, void* stream) {
     if (!sigma_dense || !features || !idx || !count_dev) return SRF_ERR_NULL;
-    if (n < 0 || mode < 0 || mode > 1) return SRF_ERR_SHAPE;
+    if (n < 0 || mode < 0 || mode > 1 || rows < 0) return SRF_ERR_SHAPE;
     if (n == 0) return SRF_OK;
-    density_act_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(sigma_dense, features, idx, count_dev, n, mode,
-                                                                      offset);
+    density_act_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(sigma_dense, rows, features, idx, count_dev, n,
+                                                                      mode, offset, device_flag());
     return launch_status();
 }
 
-extern "C" int srf_density_activation_backward(float* d_features, const float* d_sigma_dense, const float* features,
-                                               const int32_t* idx, const int32_t* count_dev, int64_t n, int mode,
-                                               float offset, void* stream) {
+extern "C" int srf_density_activation_backward(float* d_features, const float* d_sigma_dense, int64_t rows,
+                                               const float* features, const int32_t* idx, const int32_t* count_dev,
+                                               int64_t n, int mode, float offset, void* stream) {
     if (!d_features || !d_sigma_dense || !features || !idx || !count_dev) return SRF_ERR_NULL;
-    if (n < 0 || mode < 0 || mode > 1) return SRF_ERR_SHAPE;
+    if (n < 0 || mode < 0 || mode > 1 || rows < 0) return SRF_ERR_SHAPE;
     if (n == 0) return SRF_OK;
-    density_act_bwd_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(d_features, d_sigma_dense, features, idx,
-                                                                          count_dev, n, mode, offset);
+    density_act_bwd_kernel<<<grid_1d(n, 256), 256, 0, as_stream(stream)>>>(d_features, d_sigma_dense, rows, features,
+                                                                          idx, count_dev, n, mode, offset,
+                                                                          device_flag());
     return launch_status();
 }
 

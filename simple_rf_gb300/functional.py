@@ -15,6 +15,21 @@ import torch
 from . import _lib
 from ._lib import call
 
+class nvtx_range:
+    """An NVTX range around one stage of a step (visible in profilers' timelines;
+    under CUDA-graph capture it marks the capture, not the replays)."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        torch.cuda.nvtx.range_push(self.name)
+        return self
+
+    def __exit__(self, *exc):
+        torch.cuda.nvtx.range_pop()
+
+
 def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 

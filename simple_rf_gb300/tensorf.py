@@ -249,8 +249,8 @@ def gather_rows(src, idx, count, n, row_div=1, zero_tail=False):
     cols = src.shape[-1]
     dst = (torch.zeros if zero_tail else torch.empty)(n, cols, device=src.device)
     if n:
-        call('srf_gather_rows', _ptr(dst), _ptr(src.contiguous()), _ptr(idx), _ptr(count), n, cols, int(row_div),
-             _stream())
+        call('srf_gather_rows', _ptr(dst), _ptr(src.contiguous()), src.shape[0], _ptr(idx), _ptr(count), n, cols,
+             int(row_div), _stream())
     return dst
 
 
@@ -263,7 +263,7 @@ class _ScatterRows(torch.autograd.Function):
         n, c = src.shape
         out = torch.zeros(rows, c, device=src.device)
         if n:
-            call('srf_scatter_rows', _ptr(out), _ptr(src.contiguous()), _ptr(idx), _ptr(count), n, c, _stream())
+            call('srf_scatter_rows', _ptr(out), rows, _ptr(src.contiguous()), _ptr(idx), _ptr(count), n, c, _stream())
         ctx.save_for_backward(idx, count)
         ctx.n = n
         return out
@@ -288,8 +288,8 @@ class _DensityActivation(torch.autograd.Function):
         sigma = torch.zeros(rows, device=feat.device)
         n = feat.shape[0]
         if n:
-            call('srf_density_activation', _ptr(sigma), _ptr(feat), _ptr(idx), _ptr(count), n, mode, float(offset),
-                 _stream())
+            call('srf_density_activation', _ptr(sigma), rows, _ptr(feat), _ptr(idx), _ptr(count), n, mode,
+                 float(offset), _stream())
         ctx.save_for_backward(feat, idx, count)
         ctx.mode, ctx.offset = mode, offset
         return sigma
@@ -299,8 +299,8 @@ class _DensityActivation(torch.autograd.Function):
         feat, idx, count = ctx.saved_tensors
         df = torch.zeros_like(feat)
         if feat.shape[0]:
-            call('srf_density_activation_backward', _ptr(df), _ptr(g.contiguous()), _ptr(feat), _ptr(idx), _ptr(count),
-                 feat.shape[0], ctx.mode, float(ctx.offset), _stream())
+            call('srf_density_activation_backward', _ptr(df), _ptr(g.contiguous()), g.shape[0], _ptr(feat), _ptr(idx),
+                 _ptr(count), feat.shape[0], ctx.mode, float(ctx.offset), _stream())
         return df, None, None, None, None, None
 
 

@@ -43,16 +43,19 @@ class TensorfTrainStep:
             z = F.aabb_z(o, d, s, bbox, self.near, self.far, step, u[:, i].contiguous())
             calls.append((tm, {'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': vd}))
         # both models' phases side by side: two host reads of sample counts per step
-        for out in forward_models(calls, retraw=False):
-            loss = loss + torch.mean(torch.mean((out['rgb'] - t_rgb) ** 2, -1))
+        with F.nvtx_range('srf.tensorf.forward'):
+            for out in forward_models(calls, retraw=False):
+                loss = loss + torch.mean(torch.mean((out['rgb'] - t_rgb) ** 2, -1))
         counts = [dict(tm.last_sample_counts) for tm in self.models]
         for p, _ in self.params:
             p.grad = None
-        loss.backward()
+        with F.nvtx_range('srf.tensorf.backward'):
+            loss.backward()
         self.t += 1
-        F.adam_multi_step([(p.data, p.grad.contiguous(memory_format=_fmt(p)), m, v, lr)
-                           for (p, lr), (m, v) in zip(self.params, self.state) if p.grad is not None],
-                          step=self.t, beta1=0.9, beta2=0.99, eps=1e-8)
+        with F.nvtx_range('srf.tensorf.adam'):
+            F.adam_multi_step([(p.data, p.grad.contiguous(memory_format=_fmt(p)), m, v, lr)
+                               for (p, lr), (m, v) in zip(self.params, self.state) if p.grad is not None],
+                              step=self.t, beta1=0.9, beta2=0.99, eps=1e-8)
         self.last = {'loss': loss.detach(), 'samples': counts}
         return loss
 

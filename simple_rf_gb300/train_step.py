@@ -284,7 +284,8 @@ class NerfTrainStep:
         chk = _lib.check
         n = self.n
         if self.batcher is not None:
-            self._enqueue_batch(lib, st)
+            with F.nvtx_range('srf.batch'):
+                self._enqueue_batch(lib, st)
         if self.ndc:
             h, w = self.ndc['h'], self.ndc['w']
             chk(lib.srf_ndc_rays(_vp(self.rays_o), _vp(self.rays_d), _vp(self.focal), _vp(self.focal), n, h, w,
@@ -304,6 +305,7 @@ class NerfTrainStep:
         main_stream = torch.cuda.current_stream(self.dev)
         side_of, done = {}, {}
         for level in ('coarse', 'fine'):
+            torch.cuda.nvtx.range_push(f'srf.{level}')
             lv = self.level[level]
             ss = lv['z'].shape[1]
             if level == 'fine':
@@ -346,10 +348,12 @@ class NerfTrainStep:
                 ev.record(main_stream)
                 cb.wait_event(ev)
                 self._coarse_backward(lib, main_coarse, done, cb)
+            torch.cuda.nvtx.range_pop()
         if not self.train:
             for ev in done.values():
                 main_stream.wait_event(ev)
             return
+        torch.cuda.nvtx.range_push('srf.backward')
         if self.cb_stream is None:
             self._coarse_backward(lib, main_coarse, done, main_stream)
         for net in reversed(self.run):
@@ -357,6 +361,8 @@ class NerfTrainStep:
                 self._backward(lib, net, st)
         for side in list(side_of.values()) + ([self.cb_stream] if self.cb_stream is not None else []):
             main_stream.wait_stream(side)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.nvtx.range_push('srf.adam')
         chk(lib.srf_counter_add(_vp(self.step_count), 1, self.found_inf, st), 'counter')
         for net in self.nets.values():
             chk(lib.srf_adam_step(_vp(net.flat), _vp(net.grad), _vp(net.m), _vp(net.v), net.flat.numel(), self.lr,
@@ -366,6 +372,7 @@ class NerfTrainStep:
             chk(lib.srf_loss_scaler_update(_vp(self.scaler), 2.0, 0.5, 2000, st), 'loss_scaler_update')
         if self.batcher is not None:
             self.batcher.advance()
+        torch.cuda.nvtx.range_pop()
 
     def _coarse_backward(self, lib, main_coarse, done, stream):
         """The consistency term (augmented coarse depth as a detached target of the

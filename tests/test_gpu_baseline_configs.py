@@ -320,7 +320,8 @@ def test_config4_tensorf_gradients_match_oracle():
     (acc + 1e-6) amplifies rounding by up to 1e6, so such rays measure the
     conditioning of the reference formula rather than the kernels) that have no
     sample on the 1e-4 surface threshold between the GPU and the float64 oracle
-    (a sample coloured on one side only adds a renderer term to one gradient)."""
+    (a sample coloured on one side only adds a renderer term to one gradient)
+    and no density at their last sample (whose delta is 1e10 |d|)."""
     tm, (o, d, z), out = _config4_run(8192, seed=22)
     n_sub = 256
     spec = ot.RendererSpec(features_dim=27, features_pe=2, views_pe=2, units=128)
@@ -340,8 +341,14 @@ def test_config4_tensorf_gradients_match_oracle():
     cand = np.nonzero(acc >= 0.05)[0][:2 * n_sub]
     (ref_c, _), _ = oracle(cand, np.float64)
     stable = _threshold_stable(out['weights'][cand].detach().cpu().numpy(), ref_c['weights'])
+    # and no density at the last sample: its delta is 1e10 |d| (SimpleTensoRF09.py:787-791),
+    # so a positive last sigma that sits within rounding of 0 (a density feature summed
+    # to ~0 from terms of ~1e-3) has a gradient of ~1e13 that the two evaluations of
+    # that feature decide, not the kernels
+    last = out['raw_sigma'][cand, -1, 0].detach().cpu().numpy()
+    stable &= (last == 0) & (ref_c['raw_sigma'][:, -1, 0] == 0)
     rows = cand[stable][:n_sub]
-    assert rows.size == n_sub and stable.mean() > 0.95, (rows.size, stable.mean())
+    assert rows.size == n_sub and stable.mean() > 0.9, (rows.size, stable.mean())
     rng = np.random.default_rng(5)
     cot = {k: np.zeros(tuple(out[k].shape), np.float32) for k in ('rgb', 'depth', 'acc')}
     for k in cot:

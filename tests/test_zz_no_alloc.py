@@ -64,6 +64,29 @@ def test_noalloc_compaction_matches_workspace_version_twice():
         assert torch.equal(idx[:c], ref_idx[:c])
 
 
+def test_noalloc_compaction_at_the_size_limit_and_empty():
+    """A mask of exactly the largest accepted size (every scratch slot in use) and
+    an empty mask (the count is reset to 0 without a compaction launch)."""
+    from simple_rf_gb300 import _lib
+    lib = _lib.load()
+    limit = 16384 * 1024
+    rng = np.random.default_rng(7)
+    m = rng.random(limit) < 0.3
+    mask = torch.from_numpy(m.astype(np.uint8)).cuda()
+    ref_idx, ref_cnt = _with_workspace(lib, mask)
+    idx, cnt = _no_alloc(lib, mask)
+    torch.cuda.synchronize()
+    c = int(ref_cnt.item())
+    assert c == int(np.count_nonzero(m)) and int(cnt.item()) == c
+    assert torch.equal(idx[:c], ref_idx[:c])
+    cnt = torch.full((1,), 12345, dtype=torch.int32, device='cuda')
+    one = torch.zeros(1, dtype=torch.uint8, device='cuda')
+    out = torch.zeros(1, dtype=torch.int32, device='cuda')
+    assert lib.srf_compact_noalloc(_p(one), 0, _p(out), _p(cnt), _stream()) == 0
+    torch.cuda.synchronize()
+    assert int(cnt.item()) == 0
+
+
 def test_noalloc_compaction_rejects_oversized_masks():
     from simple_rf_gb300 import _lib
     lib = _lib.load()
