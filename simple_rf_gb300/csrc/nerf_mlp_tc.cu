@@ -1346,6 +1346,285 @@ int launch_basis_encode_cfg(const float* feats, int C, const float* WbT, int F, 
     return launch_status();
 }
 
+// ---------------------------------------------------------------------------
+// The basis pass on the tensor cores: B = feats . Wb^T as a TF32 tcgen05 GEMM
+// (128 sample rows per tile, N = 32 >= F basis outputs, K = C components in
+// 32-float blocks loaded by TMA with the 128-byte swizzle; components past C and
+// basis rows past F read as zeros), the positional encoding of B and of the view
+// direction in the epilogue.  Same outputs and layout as basis_encode_kernel:
+// B (m, F) FP32 for the PE adjoint and x (m, k1p) 16-bit.  The TF32 products
+// round feats and Wb to 10 mantissa bits (relative error ~5e-4), below the
+// 16-bit rounding of x they feed.
+// Warp roles (192 threads, one CTA per SM, persistent over tiles): warp 0 issues
+// the TMA loads (Wb once, then a ring of feature blocks), warp 1 the MMAs into
+// two 32-column tensor-memory accumulators, warps 2..5 read one lane quadrant
+// each (a thread per row), encode the row into shared memory and store the
+// warp's 32 rows with consecutive lanes on consecutive words.  Every mbarrier
+// wait is bounded as in the layer GEMM.
+namespace {
+
+constexpr int kBtStages = 6;
+constexpr uint32_t kBtATile = 128 * 128;   // 128 rows x 32 floats
+constexpr uint32_t kBtBBlock = 32 * 128;   // 32 rows x 32 floats
+
+__host__ __device__ inline int bt_kblocks(int C) { return (C + 31) / 32; }
+__host__ __device__ inline int bt_xwords(int k1p) { return k1p / 2 + 1; }   // odd word stride of a staged x row
+__host__ __device__ inline int bt_bstride(int F) { return F | 1; }            // odd word stride of a staged B row
+__host__ __device__ inline size_t bt_smem(int C, int F, int k1p) {
+    return 1024 + size_t(bt_kblocks(C)) * kBtBBlock + size_t(kBtStages) * kBtATile +
+           size_t(128) * bt_xwords(k1p) * 4 + size_t(128) * bt_bstride(F) * 4 + 16 + 256;
+}
+
+// Instruction descriptor of kind::tf32: F32 accumulator (bits 4-5 = 1), A and B
+// TF32 (format 2 at bits 7-9 and 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t idesc_tf32(int m, int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// 2-D FP32 map: `inner` contiguous floats per row, `outer` rows of `row_bytes`.
+bool make_map_f32(CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                  uint32_t box_in, uint32_t box_out) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {row_bytes};
+    cuuint32_t box[2] = {box_in, box_out};
+    cuuint32_t es[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+__global__ void __launch_bounds__(192, 1)
+    basis_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t M,
+                    int C, int F, const float* __restrict__ view, int lf, int lv, int k1, int k1p,
+                    float* __restrict__ Bout, op16* __restrict__ x, int fmt, int* flag) {
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int KB = bt_kblocks(C);
+    const int XW = bt_xwords(k1p), BS = bt_bstride(F);
+    uint8_t* sB = base;
+    uint8_t* sA = sB + size_t(KB) * kBtBBlock;
+    uint32_t* sX = reinterpret_cast<uint32_t*>(sA + size_t(kBtStages) * kBtATile);
+    float* sBf = reinterpret_cast<float*>(sX + size_t(128) * XW);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(
+        (reinterpret_cast<uintptr_t>(sBf + size_t(128) * BS) + 15) & ~uintptr_t(15));
+    uint64_t* full = bars;                       // [kBtStages]
+    uint64_t* empty = bars + kBtStages;          // [kBtStages]
+    uint64_t* acc_full = bars + 2 * kBtStages;   // [2]
+    uint64_t* acc_empty = acc_full + 2;          // [2]
+    uint64_t* b_full = acc_empty + 2;
+    uint64_t* done = b_full + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t num_tiles = (M + 127) / 128;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kBtStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&acc_full[a], 1);
+            mbar_init(&acc_empty[a], 128);
+        }
+        mbar_init(b_full, 1);
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, 64);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ------------------------------------------------------------ producer
+        prefetch_tmap(&tmA);
+        prefetch_tmap(&tmB);
+        mbar_arrive_expect_tx(b_full, uint32_t(KB) * kBtBBlock);
+        for (int kb = 0; kb < KB; ++kb) tma_load_2d(sB + size_t(kb) * kBtBBlock, &tmB, b_full, kb * 32, 0);
+        uint32_t it = 0;
+        uint32_t last_parity[kBtStages] = {};
+        bool used[kBtStages] = {};
+        for (int64_t tile = blockIdx.x; tile < num_tiles && !*abort_flag; tile += gridDim.x) {
+            for (int kb = 0; kb < KB; ++kb, ++it) {
+                const int s = int(it % kBtStages);
+                const uint32_t ph = (it / kBtStages) & 1;
+                if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[s], kBtATile);
+                tma_load_2d(sA + size_t(s) * kBtATile, &tmA, &full[s], kb * 32, int32_t(tile * 128));
+                used[s] = true;
+                last_parity[s] = ph;
+            }
+        }
+        // every copy this thread started has landed before the CTA may exit
+        for (int s = 0; s < kBtStages; ++s)
+            if (used[s] && !mbar_wait(&full[s], last_parity[s], nullptr)) *abort_flag = 1;
+        if (!mbar_wait(b_full, 0, nullptr)) *abort_flag = 1;
+    } else if (warp == 1 && lane == 0) {
+        // ---------------------------------------------------------------- MMA
+        const uint32_t idesc = idesc_tf32(128, 32);
+        bool ok = mbar_wait(b_full, 0, abort_flag);
+        uint32_t it = 0, t = 0;
+        for (int64_t tile = blockIdx.x; ok && tile < num_tiles; tile += gridDim.x, ++t) {
+            const uint32_t acc = t & 1;
+            if (!mbar_wait(&acc_empty[acc], ((t >> 1) & 1) ^ 1, abort_flag)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t d_tmem = tmem + acc * 32;
+            for (int kb = 0; kb < KB; ++kb, ++it) {
+                const int s = int(it % kBtStages);
+                if (!mbar_wait(&full[s], (it / kBtStages) & 1, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a_addr = smem_u32(sA + size_t(s) * kBtATile);
+                const uint32_t b_addr = smem_u32(sB + size_t(kb) * kBtBBlock);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {   // K = 8 TF32 values (32 bytes) per MMA
+                    const uint64_t ad = smem_desc(a_addr + k * 32, 0, 1024, kSwizzle128B);
+                    const uint64_t bd = smem_desc(b_addr + k * 32, 0, 1024, kSwizzle128B);
+                    mma_tf32(d_tmem, ad, bd, idesc, (kb | k) != 0);
+                }
+                mma_commit(&empty[s]);
+            }
+            if (!ok) break;
+            mma_commit(&acc_full[acc]);
+        }
+        if (!ok) *abort_flag = 1;
+        // all MMAs issued by this thread complete before tensor memory is freed
+        mma_commit(done);
+        if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
+    } else if (warp >= 2) {
+        // ----------------------------------------------------------- epilogue
+        const int q = warp & 3;            // the tensor-memory lane quadrant this warp may read
+        const int slot = (warp - 2) * 32;  // its 32 staging rows
+        op16* myx = reinterpret_cast<op16*>(sX + size_t(slot + lane) * XW);
+        float* myb = sBf + size_t(slot + lane) * BS;
+        const int v0 = F * (2 * lf + 1);
+        const int kw = k1p / 2;
+        uint32_t* xw = reinterpret_cast<uint32_t*>(x);
+        uint32_t t = 0;
+        for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
+            const uint32_t acc = t & 1;
+            if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            uint32_t r[32];
+            tmem_ld_32x32b_x32(tmem + acc * 32 + (uint32_t(q * 32) << 16), r);
+            tmem_ld_wait();
+            tc_fence_before();
+            mbar_arrive(&acc_empty[acc]);
+            const int64_t row0 = tile * 128 + q * 32;
+            const int64_t m = row0 + lane;
+#pragma unroll
+            for (int f = 0; f < 32; ++f) {
+                if (f < F) {
+                    const float v = __uint_as_float(r[f]);
+                    myb[f] = v;
+                    myx[f] = to16(v, fmt);
+                    float sh, ch;
+                    sincos16(v, &sh, &ch);
+                    for (int k = 0; k < lf; ++k) {
+                        myx[F + f + 2 * F * k] = to16(sh, fmt);
+                        myx[2 * F + f + 2 * F * k] = to16(ch, fmt);
+                        const float s2 = 2.f * sh * ch, c2 = (ch - sh) * (ch + sh);
+                        sh = s2;
+                        ch = c2;
+                    }
+                }
+            }
+            if (view) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float v = m < M ? view[m * 3 + a] : 0.f;
+                    myx[v0 + a] = to16(v, fmt);
+                    float sh, ch;
+                    sincos16(v, &sh, &ch);
+                    for (int k = 0; k < lv; ++k) {
+                        myx[v0 + 3 + a + 6 * k] = to16(sh, fmt);
+                        myx[v0 + 6 + a + 6 * k] = to16(ch, fmt);
+                        const float s2 = 2.f * sh * ch, c2 = (ch - sh) * (ch + sh);
+                        sh = s2;
+                        ch = c2;
+                    }
+                }
+            }
+            for (int c = k1; c < k1p; ++c) myx[c] = op16(0);
+            __syncwarp();
+            for (int rr = 0; rr < 32; ++rr) {
+                const int64_t g = row0 + rr;
+                if (g >= M) break;
+                const uint32_t* src = sX + size_t(slot + rr) * XW;
+                for (int w2 = lane; w2 < kw; w2 += 32) xw[g * kw + w2] = src[w2];
+                const float* bs = sBf + size_t(slot + rr) * BS;
+                for (int f = lane; f < F; f += 32) Bout[g * F + f] = bs[f];
+            }
+            __syncwarp();
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 64);
+    }
+    if (threadIdx.x == 0 && *abort_flag) raise_flag(flag, kFlagTimeout);
+}
+
+}  // namespace
+
+// The tensor-core basis pass when its operands fit (C a multiple of 4 up to 256,
+// F <= 32, 16-byte aligned feats and Wb); SRF_ERR_UNSUPPORTED otherwise.
+int launch_basis_tc(const float* feats, int C, const float* Wb, int F, const float* view, int64_t m, int lf, int lv,
+                    int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
+    if (C % 4 || C > 256 || F > 32 || k1p % 2 || !ok16(feats) || !ok16(Wb)) return SRF_ERR_UNSUPPORTED;
+    const size_t smem = bt_smem(C, F, k1p);
+    if (smem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
+    CUtensorMap ma, mb;
+    if (!make_map_f32(&ma, feats, uint64_t(C), uint64_t(m), uint64_t(C) * 4, 32, 128)) return SRF_ERR_CUDA;
+    if (!make_map_f32(&mb, Wb, uint64_t(C), uint64_t(F), uint64_t(C) * 4, 32, 32)) return SRF_ERR_CUDA;
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaError_t e = cudaFuncSetAttribute(basis_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(tc::kMaxSmem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+        attr_done = true;
+    }
+    const int64_t tiles = (m + 127) / 128;
+    const int grid = int(tiles < num_sms() ? tiles : num_sms());
+    basis_tc_kernel<<<grid, 192, smem, s>>>(ma, mb, m, C, F, view, lf, lv, k1, k1p, B, x, fmt, device_flag());
+    return launch_status();
+}
+
 // The basis + encoding pass: tile shapes (rows per thread x threads) the tuner picks
 // from per (C, k1p); without tuning, the first whose shared memory fits (128 x 2
 // measured fastest for C = 144).
@@ -1384,11 +1663,14 @@ int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float
     if ((st = pack(R.l1, P[1], w.W1, w.W1T, fmt, s))) return st;
     if ((st = pack(R.l2, P[3], w.W2, w.W2T, fmt, s))) return st;
     if (!aligned16(feats)) return SRF_ERR_ALIGN;
-    transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
-    if ((st = launch_status())) return st;
-    if ((st = launch_basis_encode(feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x, fmt,
-                                  s)))
-        return st;
+    st = m > 0 ? launch_basis_tc(feats, C, P[0], F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x, fmt, s)
+               : SRF_OK;
+    if (st == SRF_ERR_UNSUPPORTED) {   // operands the tensor-core pass does not take: the SIMT pass
+        transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
+        if ((st = launch_status())) return st;
+        st = launch_basis_encode(feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x, fmt, s);
+    }
+    if (st) return st;
     if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
                         w.W1, R.k1p, U, 0, m, U, s)))
         return st;

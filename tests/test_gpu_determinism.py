@@ -5,8 +5,9 @@ on the same batch.
 Forward outputs are bit-for-bit reproducible (no kernel of the forward
 accumulates with atomics).  Gradients that sum contributions with atomics (the
 bias gradients of the tensor-core weight-gradient kernel, the VM scatter-add)
-may differ in the last bits between replays: they are held to 1e-6 relative,
-and the bitwise-equal share is reported."""
+may differ in the last bits between replays: they are held to 1e-6 relative
+(FP32 step) or 1e-4 of the largest gradient (FP16 step, loss-scaled sums), and
+the bitwise-equal share is reported."""
 import numpy as np
 import pytest
 import torch
@@ -48,7 +49,12 @@ def test_nerf_step_replays_reproduce(precision):
     for tag in g1:
         a, b = g1[tag].cpu().numpy(), g2[tag].cpu().numpy()
         shares[tag] = float(np.mean(a == b))
-        np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-6 * float(np.abs(a).max()), err_msg=tag)
+        worst = float(np.abs(a - b).max() / np.abs(a).max())
+        print(precision, tag, 'largest difference between replays / largest gradient', worst)
+        # FP16: the atomically summed bias gradients add loss-scaled values, whose
+        # summation-order differences survive the unscaling
+        bar = 1e-6 if precision == 'fp32' else 1e-4
+        np.testing.assert_allclose(a, b, rtol=bar, atol=bar * float(np.abs(a).max()), err_msg=tag)
     print(precision, 'share of gradient entries bitwise equal between replays', shares)
 
 
