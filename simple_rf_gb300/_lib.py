@@ -220,7 +220,11 @@ def new_stream(device):
     with torch.cuda.device(device):
         check(lib.srf_stream_create(ctypes.byref(ptr)), 'srf_stream_create')
     st = torch.cuda.ExternalStream(ptr.value, device=device)
-    weakref.finalize(st, lib.srf_stream_destroy, P(ptr.value))
+    fin = weakref.finalize(st, lib.srf_stream_destroy, P(ptr.value))
+    # not at interpreter exit: tensors that recorded this stream can still be freed
+    # after the exit finalizers ran, and the caching allocator then records an event
+    # on the stream; the process's teardown releases it instead
+    fin.atexit = False
     return st
 
 

@@ -1601,11 +1601,15 @@ __global__ void __launch_bounds__(192, 1)
 
 // The tensor-core basis pass when its operands fit (C a multiple of 4 up to 256,
 // F <= 32, 16-byte aligned feats and Wb); SRF_ERR_UNSUPPORTED otherwise.
+bool basis_tc_fits(int C, int F, int k1p, const float* feats, const float* Wb) {
+    return C % 4 == 0 && C <= 256 && F <= 32 && k1p % 2 == 0 && ok16(feats) && ok16(Wb) &&
+           bt_smem(C, F, k1p) <= tc::kMaxSmem;
+}
+
 int launch_basis_tc(const float* feats, int C, const float* Wb, int F, const float* view, int64_t m, int lf, int lv,
                     int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
-    if (C % 4 || C > 256 || F > 32 || k1p % 2 || !ok16(feats) || !ok16(Wb)) return SRF_ERR_UNSUPPORTED;
+    if (!basis_tc_fits(C, F, k1p, feats, Wb)) return SRF_ERR_UNSUPPORTED;
     const size_t smem = bt_smem(C, F, k1p);
-    if (smem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
     CUtensorMap ma, mb;
     if (!make_map_f32(&ma, feats, uint64_t(C), uint64_t(m), uint64_t(C) * 4, 32, 128)) return SRF_ERR_CUDA;
     if (!make_map_f32(&mb, Wb, uint64_t(C), uint64_t(F), uint64_t(C) * 4, 32, 32)) return SRF_ERR_CUDA;
@@ -1625,13 +1629,18 @@ int launch_basis_tc(const float* feats, int C, const float* Wb, int F, const flo
     return launch_status();
 }
 
-// The basis + encoding pass: tile shapes (rows per thread x threads) the tuner picks
-// from per (C, k1p); without tuning, the first whose shared memory fits (128 x 2
-// measured fastest for C = 144).
-int launch_basis_encode(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
-                        int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
+// The basis + encoding pass: the tuner picks per (C, k1p) among the SIMT tile shapes
+// (rows per thread x threads, reading the transposed basis the call writes to WbT)
+// and the tensor-core pass (Wb as stored; candidate 5, where its operands fit).
+// Without tuning: the tensor-core pass where it applies, else the first SIMT shape
+// whose shared memory fits (128 x 2 measured fastest of those for C = 144).
+int launch_basis_encode(const float* feats, int C, const float* Wb, float* WbT, int F, const float* view, int64_t m,
+                        int lf, int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
     if (m <= 0) return SRF_OK;
     auto run = [&](int i) -> int {
+        if (i == 5) return launch_basis_tc(feats, C, Wb, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+        transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(Wb, F, C, WbT);
+        if (const int st = launch_status()) return st;
 #define SRF_ENC(R, N)                                                                                             \
     (enc_smem_bytes(C, k1p, R, N) <= tc::kMaxSmem                                                                 \
          ? launch_basis_encode_cfg<R, N>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s)                \
@@ -1645,9 +1654,10 @@ int launch_basis_encode(const float* feats, int C, const float* WbT, int F, cons
         }
 #undef SRF_ENC
     };
-    const int fallback = enc_smem_bytes(C, k1p, 2, 128) <= tc::kMaxSmem ? 0 : 4;
+    const int fallback =
+        basis_tc_fits(C, F, k1p, feats, Wb) ? 5 : enc_smem_bytes(C, k1p, 2, 128) <= tc::kMaxSmem ? 0 : 4;
     const tune::Key key{tune::kSiteBasisEncode, C, k1p, 0};
-    return run(tune::pick(key, 5, fallback, s, run));
+    return run(tune::pick(key, 6, fallback, s, run));
 }
 
 // P = {Wb (F x C), W1 (U x k1), b1, W2 (U x U), b2, W3 (3 x U), b3}
@@ -1663,14 +1673,9 @@ int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float
     if ((st = pack(R.l1, P[1], w.W1, w.W1T, fmt, s))) return st;
     if ((st = pack(R.l2, P[3], w.W2, w.W2T, fmt, s))) return st;
     if (!aligned16(feats)) return SRF_ERR_ALIGN;
-    st = m > 0 ? launch_basis_tc(feats, C, P[0], F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x, fmt, s)
-               : SRF_OK;
-    if (st == SRF_ERR_UNSUPPORTED) {   // operands the tensor-core pass does not take: the SIMT pass
-        transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
-        if ((st = launch_status())) return st;
-        st = launch_basis_encode(feats, C, w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x, fmt, s);
-    }
-    if (st) return st;
+    if ((st = launch_basis_encode(feats, C, P[0], w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x,
+                                  fmt, s)))
+        return st;
     if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
                         w.W1, R.k1p, U, 0, m, U, s)))
         return st;

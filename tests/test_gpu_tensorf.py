@@ -193,23 +193,33 @@ def test_tensorf_full_size_grid_gather_roundtrip():
     assert c1.shape == (4096, 144) and torch.isfinite(c1).all()
 
 
-@pytest.mark.parametrize('precision,bar', [('fp16', 3e-2), ('bf16', 8e-2)])
-def test_tensorf_tensor_core_renderer_against_fp32(precision, bar):
+@pytest.mark.parametrize('precision,bar,basis', [('fp16', 3e-2, None), ('bf16', 8e-2, None), ('fp16', 3e-2, 0),
+                                                  ('fp16', 3e-2, 5)])
+def test_tensorf_tensor_core_renderer_against_fp32(precision, bar, basis):
     """The 16-bit tensor-core renderer (basis + MlpFeaturesColorPredictor) against
     the FP32 path on the same model and rays (64^3 grid, R = 16/48, 128 units):
     rgb within 2e-3 max-abs; whole gradient of the renderer and the colour grid
-    within `bar` relative L2."""
-    from simple_rf_gb300 import build as b
+    within `bar` relative L2.  `basis` pins the basis pass's tuned choice (0: the
+    SIMT tile 2 x 128, 5: the TF32 tensor-core GEMM; None: what the tuner picks)."""
+    from simple_rf_gb300 import _lib, autotune, build as b
     b.build()
     from simple_rf_gb300.bench_tensorf import make_models, synthetic_rays
+    from simple_rf_gb300 import functional as F
     res = {}
     for prec in ('fp32', precision):
         tm = make_models(DEV, seed=3, precision=prec, grids=(64, 32))[0]
         o, d, t_rgb, u = synthetic_rays(256, 5, DEV)
-        from simple_rf_gb300 import functional as F
         s = int(tm.num_samples.item())
         z = F.aabb_z(o, d, s, tm.bounding_box.detach().cpu(), 2.0, 6.0, float(tm.step_size), u[:, 0].contiguous())
-        out = tm({'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': F.view_dirs(d)}, retraw=False)
+        inp = {'z_vals': z, 'rays_o': o, 'rays_d': d, 'view_dirs': F.view_dirs(d)}
+        if prec != 'fp32' and basis is not None:
+            with torch.no_grad():
+                tm(inp, retraw=False)      # the tuner records the basis site's key
+            keys = [e['key'] for e in autotune.table() if e['site'] == 2]
+            assert keys
+            for k in keys:
+                _lib.check(_lib.load().srf_autotune_set(2, *k, basis), 'srf_autotune_set')
+        out = tm(inp, retraw=False)
         loss = ((out['rgb'] - t_rgb) ** 2).mean()
         loss.backward()
         params = [tm.basis_matrix_color.weight] + list(tm.color_predictor.parameters()) + list(tm.matrices_color) + \
@@ -219,7 +229,9 @@ def test_tensorf_tensor_core_renderer_against_fp32(precision, bar):
     assert c32['surface'] > 1000 and c32 == c16, (c32, c16)
     err = (r16 - r32).abs().max().item()
     rel = ((g16 - g32).norm() / g32.norm()).item()
-    print(precision, 'rgb max-abs', err, 'renderer+colour-grid gradient rel-L2', rel)
+    print(precision, 'basis choice', basis, 'rgb max-abs', err, 'renderer+colour-grid gradient rel-L2', rel)
+    if basis is not None:
+        autotune.clear()
     assert err < 2e-3, err
     assert rel < bar, rel
 
