@@ -471,6 +471,12 @@ int srf_tensorf_renderer_backward(const srf_tensorf_renderer_desc* desc, const f
                                   const float* feats, const float* d_rgb, int64_t m, float* const* grads,
                                   float* d_feats, int precision, void* workspace, size_t workspace_bytes,
                                   srf_loss_scaler* scaler, void* stream);
+/* The basis adjoint of the 16-bit renderer backward (d_feats = dB . Wb, dWb +=
+ * dB^T feats, dB from the PE adjoint): tensor_cores = 1 (default) takes the TF32
+ * tcgen05 pass plus a dWb reduction where the shapes fit (C a multiple of 16 up to
+ * 256), 0 always the fused FP32 SIMT pass.  Both give the same gradients up to the
+ * TF32 rounding of dB and Wb in d_feats.  Process-wide setting. */
+int srf_tensorf_basis_adjoint_path(int tensor_cores);
 /* Positional-encoding backward d x (m,dims) from d out (m, ld) (TensoRF feature PE). */
 int srf_positional_encoding_backward(float* dx, const float* x, const float* dout, int ld_dout, int64_t m,
                                      const int32_t* rows_dev, int dims, int degree, void* stream);

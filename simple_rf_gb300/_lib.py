@@ -155,6 +155,7 @@ _SIGS = {
     'srf_uniforms': (c_int, [P, c_int64, ctypes.c_uint64, P, c_int, P]),
     'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
     'srf_autotune_enable': (c_int, [c_int]),
+    'srf_tensorf_basis_adjoint_path': (c_int, [c_int]),
     'srf_autotune_count': (c_int, []),
     'srf_autotune_entry': (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int64), ctypes.POINTER(c_int64),
                                    ctypes.POINTER(c_int64), ctypes.POINTER(c_int)]),

@@ -11,11 +11,13 @@
 // GEMM over samples (MN-major operands) reduced into the FP32 weight gradient.
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <vector>
 
 #include "nerf_mlp.h"
+
 #include "autotune.cuh"
 #include "tc_gemm.cuh"
 
@@ -243,6 +245,10 @@ struct LayerMap {
     int n;
     int nsrc;
     int pad0[2], padw[2], ref0[2], refw[2];
+    // Blocked first source (nblk > 0): its first nblk blocks of bwr reference columns
+    // each sit at padded stride bwp (bwp - bwr zero columns after each block), the
+    // rest of the source follows from padded column nblk * bwp.
+    int nblk, bwp, bwr;
     __host__ __device__ int kpad() const { return pad0[nsrc - 1] + padw[nsrc - 1]; }
     __host__ __device__ int kref() const { return ref0[nsrc - 1] + refw[nsrc - 1]; }
 };
@@ -250,7 +256,18 @@ struct LayerMap {
 __device__ __forceinline__ int ref_col(const LayerMap& L, int kp) {
     for (int i = 0; i < L.nsrc; ++i) {
         int off = kp - L.pad0[i];
-        if (off >= 0 && off < L.padw[i]) return off < L.refw[i] ? L.ref0[i] + off : -1;
+        if (off >= 0 && off < L.padw[i]) {
+            if (i == 0 && L.nblk > 0) {
+                const int head = L.nblk * L.bwp;
+                if (off < head) {
+                    const int b = off / L.bwp, j = off - b * L.bwp;
+                    return j < L.bwr ? L.ref0[0] + b * L.bwr + j : -1;
+                }
+                const int r = L.nblk * L.bwr + (off - head);
+                return r < L.refw[0] ? L.ref0[0] + r : -1;
+            }
+            return off < L.refw[i] ? L.ref0[i] + off : -1;
+        }
     }
     return -1;
 }
@@ -891,15 +908,25 @@ namespace {
 
 constexpr int kMaxBasis = 32;    // largest basis width (features_dimension_color) it holds in registers
 
+// The renderer's 16-bit input rows x (k1p columns): the 2 lf + 1 feature blocks
+// [B, sin B, cos B, sin 2B, cos 2B, ...] (the reference's PE order) each at a
+// column stride bw = F rounded up to 8 (so every block starts on a 16-byte
+// boundary and can be written as whole vectors), the view block [d, sin d, cos d,
+// ...] from column v0, zeros up to k1p; the packed W1 holds zero columns in the
+// gaps.  B rows (the basis outputs kept for the PE adjoint) have kMaxBasis floats.
 struct RenderLayout {
-    int C, F, U, lf, lv, view, k1, k1p;
+    int C, F, U, lf, lv, view, k1, k1p, bw, bs, v0;
     LayerMap l1, l2;
     bool ok;
     RenderLayout(int c, int f, int u, int lf_, int lv_, int view_) : C(c), F(f), U(u), lf(lf_), lv(lv_), view(view_) {
         k1 = F * (2 * lf + 1) + (view ? 3 * (2 * lv + 1) : 0);
-        k1p = pad64(k1);
+        bw = (F + 7) / 8 * 8;
+        bs = kMaxBasis;
+        v0 = bw * (2 * lf + 1);
+        k1p = pad64(v0 + (view ? 3 * (2 * lv + 1) : 0));
         l1 = LayerMap{};
         l1.n = U; l1.nsrc = 1; l1.padw[0] = k1p; l1.refw[0] = k1;
+        l1.nblk = 2 * lf + 1; l1.bwp = bw; l1.bwr = F;
         l2 = LayerMap{};
         l2.n = U; l2.nsrc = 1; l2.padw[0] = U; l2.refw[0] = U;
         ok = (U == 128 || U == 256) && C >= 4 && C <= 1024 && C % 4 == 0 && F >= 1 && F <= kMaxBasis && k1p <= 256 &&
@@ -909,7 +936,7 @@ struct RenderLayout {
 };
 
 struct RenderWs {
-    float* B;        // (m, F) basis outputs (kept for the PE adjoint)
+    float* B;        // (m, bs) basis outputs (kept for the PE adjoint)
     op16* x;         // (m, k1p)
     op16* h1;        // (m, U)
     op16* h2;        // (m, U)
@@ -917,6 +944,7 @@ struct RenderWs {
     op16 *W1, *W1T, *W2, *W2T;
     float* WbT;      // (C, kMaxBasis)
     op16 *dz0, *dz1, *dx;   // (m, U), (m, U), (m, k1p)
+    float* dB;              // (m, kMaxBasis) basis-output gradients of the tensor-core adjoint
     float* partial;
     size_t partial_floats;
 };
@@ -924,7 +952,7 @@ struct RenderWs {
 size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size_t cap, RenderWs* out) {
     Carver c(base, cap);
     RenderWs w{};
-    w.B = c.take<float>(size_t(m) * R.F);
+    w.B = c.take<float>(size_t(m) * R.bs);
     w.x = c.take<op16>(size_t(m) * R.k1p);
     w.h1 = c.take<op16>(size_t(m) * R.U);
     w.h2 = c.take<op16>(size_t(m) * R.U);
@@ -938,6 +966,7 @@ size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size
         w.dz0 = c.take<op16>(size_t(m) * R.U);
         w.dz1 = c.take<op16>(size_t(m) * R.U);
         w.dx = c.take<op16>(size_t(m) * R.k1p);
+        w.dB = c.take<float>(size_t(m) * kMaxBasis);
         w.partial_floats = tc_wgrad_partial_floats(R.U, 256);
         w.partial = c.take<float>(w.partial_floats);
     }
@@ -947,9 +976,6 @@ size_t carve_render(const RenderLayout& R, int64_t m, bool bwd, void* base, size
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
@@ -972,7 +998,6 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // ~ 2^k ulp, far below the 16-bit rounding of the output), written into the
 // consumed tile buffer as the 16-bit staging (row stride k1p + 8), which the
 // block stores as 16-byte vectors.
-constexpr int kEncThreads = 128;
 
 // (d0, d1) += a * (b0, b1) with one packed two-lane FMA (fma.rn per lane)
 __device__ __forceinline__ void ffma2(float& d0, float& d1, float a, float b0, float b1) {
@@ -1036,8 +1061,8 @@ __global__ void transpose_basis_kernel(const float* __restrict__ Wb, int F, int 
 template <int RPT, int NT>
 __global__ void __launch_bounds__(NT)
     basis_encode_kernel(const float* __restrict__ feats, int C, const float* __restrict__ WbT, int F,
-                        const float* __restrict__ view, int64_t M, int lf, int lv, int k1, int k1p, float* B, op16* x,
-                        int fmt) {
+                        const float* __restrict__ view, int64_t M, int lf, int lv, int bw, int bs, int k1p, float* B,
+                        op16* x, int fmt) {
     extern __shared__ __align__(16) float esm[];
     constexpr int RG = NT / 8, T = RG * RPT;                   // row groups, rows per tile
     float* sWt = esm;                                          // C x kMaxBasis
@@ -1110,15 +1135,21 @@ __global__ void __launch_bounds__(NT)
             d[3] = acc[i][1].y;
         }
         __syncthreads();
+        // every staged row starts as zeros (the gaps after each block and the tail)
+        for (int r = warp; r < rows; r += NT / 32) {
+            uint32_t* my = reinterpret_cast<uint32_t*>(stage + r * XS);
+            for (int c = lane; c < k1p / 2; c += 32) my[c] = 0u;
+        }
+        __syncwarp();
         // lane roles: feature f = lane (f < F), view component a (lanes F .. F + 2, or a
         // second pass on lanes 0 .. 2 when F > 29); each writes its value, then sin and
         // cos of 2^q value at columns c_sin + q dq and c_sin + q dq + dcos
-        const int v0 = F * (2 * lf + 1);
+        const int v0 = bw * (2 * lf + 1);
         const bool view_here = view && F <= 29;
         for (int pass = 0; pass < ((view && F > 29) ? 2 : 1); ++pass) {
             int kind = 0, col = 0, csin = 0, dq = 0, dcos = 0, deg = 0;   // kind 1: feature, 2: view
             if (pass == 0 && lane < F) {
-                kind = 1; col = lane; csin = F + lane; dq = 2 * F; dcos = F; deg = lf;
+                kind = 1; col = lane; csin = bw + lane; dq = 2 * bw; dcos = bw; deg = lf;
             } else if (view && ((pass == 0 && view_here && lane >= F && lane < F + 3) || (pass == 1 && lane < 3))) {
                 const int a = pass == 0 ? lane - F : lane;
                 kind = 2; col = v0 + a; csin = v0 + 3 + a; dq = 6; dcos = 3; deg = lv;
@@ -1143,7 +1174,7 @@ __global__ void __launch_bounds__(NT)
                     const int r = h ? r1 : r0;
                     if (kind == 0 || (h && !two)) continue;
                     op16* my = stage + r * XS;
-                    if (kind == 1) B[(row0 + r) * F + lane] = v[h];
+                    if (kind == 1) B[(row0 + r) * bs + lane] = v[h];
                     my[col] = tc::to16(v[h], fmt);
                     float sh = sn[h], ch = cs[h];
                     for (int q = 0; q < deg; ++q) {
@@ -1155,10 +1186,6 @@ __global__ void __launch_bounds__(NT)
                     }
                 }
             }
-        }
-        for (int r = warp; r < rows; r += NT / 32) {
-            op16* my = stage + r * XS;
-            for (int c = k1 + lane; c < k1p; c += 32) my[c] = op16(0);
         }
         __syncthreads();
         {
@@ -1187,23 +1214,22 @@ __global__ void __launch_bounds__(NT)
 // and its dWb accumulators in registers; dB rows are shared-memory broadcasts.
 constexpr int kBwdTile = 32;
 
-// shared bytes of one tile buffer: feature rows, dx rows, B rows (16-byte multiples)
-__host__ __device__ inline size_t basis_tile_bytes(int C, int F, int k1p) {
-    size_t fb = size_t(kBwdTile) * C * 4, xb = size_t(kBwdTile) * k1p * 2, bb = size_t(kBwdTile) * F * 4;
-    return fb + xb + (bb + 15) / 16 * 16;
+// shared bytes of one tile buffer: feature rows, dx rows, B rows (bs floats each)
+__host__ __device__ inline size_t basis_tile_bytes(int C, int bs, int k1p) {
+    return size_t(kBwdTile) * C * 4 + size_t(kBwdTile) * k1p * 2 + size_t(kBwdTile) * bs * 4;
 }
-__host__ __device__ inline size_t basis_bwd_smem(int C, int F, int k1p) {
-    return size_t(kBwdTile) * kMaxBasis * 4 + 2 * basis_tile_bytes(C, F, k1p);
+__host__ __device__ inline size_t basis_bwd_smem(int C, int bs, int k1p) {
+    return size_t(kBwdTile) * kMaxBasis * 4 + 2 * basis_tile_bytes(C, bs, k1p);
 }
 
 __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __restrict__ B,
                                  const float* __restrict__ feats, const float* __restrict__ Wb, int64_t M, int F,
-                                 int C, int lf, int k1p, int fmt, const float* gscale, int64_t rows_per_block,
-                                 float* d_feats, float* dWb) {
+                                 int C, int lf, int bw, int bs, int k1p, int fmt, const float* gscale,
+                                 int64_t rows_per_block, float* d_feats, float* dWb) {
     extern __shared__ __align__(16) float bb[];
     float* sdB = bb;                                   // kBwdTile x kMaxBasis
     uint8_t* bufs = reinterpret_cast<uint8_t*>(sdB + kBwdTile * kMaxBasis);
-    const size_t tile_bytes = basis_tile_bytes(C, F, k1p);
+    const size_t tile_bytes = basis_tile_bytes(C, bs, k1p);
     const float unscale = gscale ? gscale[1] : 1.f;
     const int c = threadIdx.x;
     float wcol[kMaxBasis], acc[kMaxBasis];
@@ -1226,8 +1252,8 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
             for (int i = threadIdx.x; i < nt * C / 4; i += blockDim.x) cp_async16(sF + 4 * i, gf + 4 * i);
             const op16* gx = dx + t0 * k1p;
             for (int i = threadIdx.x; i < nt * k1p / 8; i += blockDim.x) cp_async16(sdx + 8 * i, gx + 8 * i);
-            const float* gb = B + t0 * F;
-            for (int i = threadIdx.x; i < nt * F; i += blockDim.x) cp_async4(sB + i, gb + i);
+            const float* gb = B + t0 * bs;   // bs is a multiple of 4 floats
+            for (int i = threadIdx.x; i < nt * bs / 4; i += blockDim.x) cp_async16(sB + 4 * i, gb + 4 * i);
         }
         cp_async_commit();
     };
@@ -1252,13 +1278,13 @@ __global__ void basis_bwd_kernel(const op16* __restrict__ dx, const float* __res
                     const float2 f = tc::unpack16(w, fmt);
                     return (col & 1) ? f.y : f.x;
                 };
-                const float bo = sB[rr * F + o];
+                const float bo = sB[rr * bs + o];
                 g = rd(o);
                 float sn, cs;   // sin, cos of 2^k B by the double-angle recurrence
                 sincos16(bo, &sn, &cs);
                 for (int k = 0; k < lf; ++k) {
                     const float fk = float(1 << k);
-                    g += fk * (cs * rd(F + 2 * k * F + o) - sn * rd(F + (2 * k + 1) * F + o));
+                    g += fk * (cs * rd((2 * k + 1) * bw + o) - sn * rd((2 * k + 2) * bw + o));
                     const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
                     sn = s2;
                     cs = c2;
@@ -1327,7 +1353,7 @@ size_t render_tc_workspace(int C, int F, int U, int lf, int lv, int view, int64_
 
 template <int RPT, int NT>
 int launch_basis_encode_cfg(const float* feats, int C, const float* WbT, int F, const float* view, int64_t m, int lf,
-                            int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
+                            int lv, int bw, int bs, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
     const size_t smem = enc_smem_bytes(C, k1p, RPT, NT);
     cudaError_t e = cudaFuncSetAttribute(basis_encode_kernel<RPT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(smem));
@@ -1341,8 +1367,8 @@ int launch_basis_encode_cfg(const float* feats, int C, const float* WbT, int F, 
     const int64_t tiles = (m + enc_tile_rows(RPT, NT) - 1) / enc_tile_rows(RPT, NT);
     int64_t grid = int64_t(num_sms()) * (per_sm > 0 ? per_sm : 1);
     if (grid > tiles) grid = tiles;
-    basis_encode_kernel<RPT, NT><<<unsigned(grid), NT, smem, s>>>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x,
-                                                                  fmt);
+    basis_encode_kernel<RPT, NT><<<unsigned(grid), NT, smem, s>>>(feats, C, WbT, F, view, m, lf, lv, bw, bs, k1p, B,
+                                                                  x, fmt);
     return launch_status();
 }
 
@@ -1351,29 +1377,42 @@ int launch_basis_encode_cfg(const float* feats, int C, const float* WbT, int F, 
 // (128 sample rows per tile, N = 32 >= F basis outputs, K = C components in
 // 32-float blocks loaded by TMA with the 128-byte swizzle; components past C and
 // basis rows past F read as zeros), the positional encoding of B and of the view
-// direction in the epilogue.  Same outputs and layout as basis_encode_kernel:
-// B (m, F) FP32 for the PE adjoint and x (m, k1p) 16-bit.  The TF32 products
-// round feats and Wb to 10 mantissa bits (relative error ~5e-4), below the
-// 16-bit rounding of x they feed.
-// Warp roles (192 threads, one CTA per SM, persistent over tiles): warp 0 issues
+// direction in the epilogue.  Same outputs and layout as basis_encode_kernel (B
+// rows of kMaxBasis floats, x in RenderLayout's blocked columns).  The TF32
+// products round feats and Wb to 10 mantissa bits (relative error ~5e-4), below
+// the 16-bit rounding of x they feed.
+// Warp roles (320 threads, one CTA per SM, persistent over tiles): warp 0 issues
 // the TMA loads (Wb once, then a ring of feature blocks), warp 1 the MMAs into
-// two 32-column tensor-memory accumulators, warps 2..5 read one lane quadrant
-// each (a thread per row), encode the row into shared memory and store the
-// warp's 32 rows with consecutive lanes on consecutive words.  Every mbarrier
-// wait is bounded as in the layer GEMM.
+// four 32-column tensor-memory accumulators, warps 2..9 in two groups of four
+// that take alternate tiles, each warp of a group reading one lane quadrant (a
+// thread per row).  A thread encodes its row eight columns at a time and
+// writes each 16-byte piece into its warp's staging boxes in the 128-byte
+// swizzled layout (the eight rows of a quarter-warp land in eight distinct bank
+// groups); lane 0 then stores the boxes with TMA (x in 64-column boxes, B in one
+// 32-float box) while the warp moves on to its next tile.  Every mbarrier wait
+// is bounded as in the layer GEMM.
 namespace {
 
-constexpr int kBtStages = 6;
+constexpr int kBtMaxStages = 6;
+constexpr int kBtEpiWarps = 8;             // two groups of four
+constexpr int kBtThreads = 64 + 32 * kBtEpiWarps;
 constexpr uint32_t kBtATile = 128 * 128;   // 128 rows x 32 floats
 constexpr uint32_t kBtBBlock = 32 * 128;   // 32 rows x 32 floats
+constexpr uint32_t kBtBox = 32 * 128;      // a staging box: 32 rows x 128 bytes
 
 __host__ __device__ inline int bt_kblocks(int C) { return (C + 31) / 32; }
-__host__ __device__ inline int bt_xwords(int k1p) { return k1p / 2 + 1; }   // odd word stride of a staged x row
-__host__ __device__ inline int bt_bstride(int F) { return F | 1; }            // odd word stride of a staged B row
-__host__ __device__ inline size_t bt_smem(int C, int F, int k1p) {
-    return 1024 + size_t(bt_kblocks(C)) * kBtBBlock + size_t(kBtStages) * kBtATile +
-           size_t(128) * bt_xwords(k1p) * 4 + size_t(128) * bt_bstride(F) * 4 + 16 + 256;
+__host__ __device__ inline size_t bt_stage_bytes(int k1p) { return size_t(k1p / 64 + 1) * kBtBox; }
+__host__ __device__ inline size_t bt_fixed_smem(int C, int k1p) {
+    return 1024 + size_t(bt_kblocks(C)) * kBtBBlock + kBtEpiWarps * bt_stage_bytes(k1p) + 256;
 }
+// feature-block ring stages that fit beside the fixed parts (0 or 1: the pass does not fit)
+inline int bt_stages(int C, int k1p) {
+    const size_t fixed = bt_fixed_smem(C, k1p);
+    if (fixed >= tc::kMaxSmem) return 0;
+    const size_t st = (tc::kMaxSmem - fixed) / kBtATile;
+    return int(st < size_t(kBtMaxStages) ? st : size_t(kBtMaxStages));
+}
+inline size_t bt_smem(int C, int k1p, int stages) { return bt_fixed_smem(C, k1p) + size_t(stages) * kBtATile; }
 
 // Instruction descriptor of kind::tf32: F32 accumulator (bits 4-5 = 1), A and B
 // TF32 (format 2 at bits 7-9 and 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
@@ -1391,62 +1430,73 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint6
         : "memory");
 }
 
-// 2-D FP32 map: `inner` contiguous floats per row, `outer` rows of `row_bytes`.
-bool make_map_f32(CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t outer, uint64_t row_bytes,
-                  uint32_t box_in, uint32_t box_out) {
+// 2-D map of `dtype` elements: `inner` contiguous elements per row, `outer` rows of
+// `row_bytes`, boxes of box_in x box_out with the 128-byte swizzle.
+bool make_map_t(CUtensorMap* m, CUtensorMapDataType dtype, const void* ptr, uint64_t inner, uint64_t outer,
+                uint64_t row_bytes, uint32_t box_in, uint32_t box_out) {
     auto fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {row_bytes};
     cuuint32_t box[2] = {box_in, box_out};
     cuuint32_t es[2] = {1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, es,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+    return fn(m, dtype, 2, const_cast<void*>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-__global__ void __launch_bounds__(192, 1)
-    basis_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t M,
-                    int C, int F, const float* __restrict__ view, int lf, int lv, int k1, int k1p,
-                    float* __restrict__ Bout, op16* __restrict__ x, int fmt, int* flag) {
+// Eight floats -> eight 16-bit words of format FMT; entries at and past `valid` as zeros.
+template <int FMT>
+__device__ __forceinline__ uint4 pack8(const float* a, int valid) {
+    float v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = i < valid ? a[i] : 0.f;
+    return make_uint4(tc::pack16(v[0], v[1], FMT), tc::pack16(v[2], v[3], FMT), tc::pack16(v[4], v[5], FMT),
+                      tc::pack16(v[6], v[7], FMT));
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kBtThreads, 1)
+    basis_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW,
+                    const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmB, int64_t M,
+                    int C, int F, const float* __restrict__ view, int lf, int lv, int bw, int k1p, int stages,
+                    int* flag) {
     using namespace tc;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int KB = bt_kblocks(C);
-    const int XW = bt_xwords(k1p), BS = bt_bstride(F);
-    uint8_t* sB = base;
-    uint8_t* sA = sB + size_t(KB) * kBtBBlock;
-    uint32_t* sX = reinterpret_cast<uint32_t*>(sA + size_t(kBtStages) * kBtATile);
-    float* sBf = reinterpret_cast<float*>(sX + size_t(128) * XW);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(
-        (reinterpret_cast<uintptr_t>(sBf + size_t(128) * BS) + 15) & ~uintptr_t(15));
-    uint64_t* full = bars;                       // [kBtStages]
-    uint64_t* empty = bars + kBtStages;          // [kBtStages]
-    uint64_t* acc_full = bars + 2 * kBtStages;   // [2]
-    uint64_t* acc_empty = acc_full + 2;          // [2]
-    uint64_t* b_full = acc_empty + 2;
-    uint64_t* done = b_full + 1;
+    const int nbx = k1p / 64;   // 64-column x boxes per row group
+    uint8_t* sW = base;
+    uint8_t* sA = sW + size_t(KB) * kBtBBlock;
+    uint8_t* sStage = sA + size_t(stages) * kBtATile;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sStage + kBtEpiWarps * bt_stage_bytes(k1p));
+    uint64_t* full = bars;                          // [kBtMaxStages]
+    uint64_t* empty = bars + kBtMaxStages;          // [kBtMaxStages]
+    uint64_t* acc_full = bars + 2 * kBtMaxStages;   // [4]
+    uint64_t* acc_empty = acc_full + 4;             // [4]
+    uint64_t* w_full = acc_empty + 4;
+    uint64_t* done = w_full + 1;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t num_tiles = (M + 127) / 128;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kBtStages; ++s) {
+        for (int s = 0; s < stages; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < 4; ++a) {
             mbar_init(&acc_full[a], 1);
             mbar_init(&acc_empty[a], 128);
         }
-        mbar_init(b_full, 1);
+        mbar_init(w_full, 1);
         mbar_init(done, 1);
         *abort_flag = 0;
         fence_barrier_init();
     }
     if (warp == 1) {
-        tmem_alloc(tmem_slot, 64);
+        tmem_alloc(tmem_slot, 128);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -1457,16 +1507,16 @@ __global__ void __launch_bounds__(192, 1)
     if (warp == 0 && lane == 0) {
         // ------------------------------------------------------------ producer
         prefetch_tmap(&tmA);
-        prefetch_tmap(&tmB);
-        mbar_arrive_expect_tx(b_full, uint32_t(KB) * kBtBBlock);
-        for (int kb = 0; kb < KB; ++kb) tma_load_2d(sB + size_t(kb) * kBtBBlock, &tmB, b_full, kb * 32, 0);
+        prefetch_tmap(&tmW);
+        mbar_arrive_expect_tx(w_full, uint32_t(KB) * kBtBBlock);
+        for (int kb = 0; kb < KB; ++kb) tma_load_2d(sW + size_t(kb) * kBtBBlock, &tmW, w_full, kb * 32, 0);
         uint32_t it = 0;
-        uint32_t last_parity[kBtStages] = {};
-        bool used[kBtStages] = {};
+        uint32_t last_parity[kBtMaxStages] = {};
+        bool used[kBtMaxStages] = {};
         for (int64_t tile = blockIdx.x; tile < num_tiles && !*abort_flag; tile += gridDim.x) {
             for (int kb = 0; kb < KB; ++kb, ++it) {
-                const int s = int(it % kBtStages);
-                const uint32_t ph = (it / kBtStages) & 1;
+                const int s = int(it % uint32_t(stages));
+                const uint32_t ph = (it / uint32_t(stages)) & 1;
                 if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
                     *abort_flag = 1;
                     break;
@@ -1478,31 +1528,31 @@ __global__ void __launch_bounds__(192, 1)
             }
         }
         // every copy this thread started has landed before the CTA may exit
-        for (int s = 0; s < kBtStages; ++s)
+        for (int s = 0; s < stages; ++s)
             if (used[s] && !mbar_wait(&full[s], last_parity[s], nullptr)) *abort_flag = 1;
-        if (!mbar_wait(b_full, 0, nullptr)) *abort_flag = 1;
+        if (!mbar_wait(w_full, 0, nullptr)) *abort_flag = 1;
     } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMA
         const uint32_t idesc = idesc_tf32(128, 32);
-        bool ok = mbar_wait(b_full, 0, abort_flag);
+        bool ok = mbar_wait(w_full, 0, abort_flag);
         uint32_t it = 0, t = 0;
         for (int64_t tile = blockIdx.x; ok && tile < num_tiles; tile += gridDim.x, ++t) {
-            const uint32_t acc = t & 1;
-            if (!mbar_wait(&acc_empty[acc], ((t >> 1) & 1) ^ 1, abort_flag)) {
+            const uint32_t acc = t & 3;
+            if (!mbar_wait(&acc_empty[acc], ((t >> 2) & 1) ^ 1, abort_flag)) {
                 ok = false;
                 break;
             }
             tc_fence_after();
             const uint32_t d_tmem = tmem + acc * 32;
             for (int kb = 0; kb < KB; ++kb, ++it) {
-                const int s = int(it % kBtStages);
-                if (!mbar_wait(&full[s], (it / kBtStages) & 1, abort_flag)) {
+                const int s = int(it % uint32_t(stages));
+                if (!mbar_wait(&full[s], (it / uint32_t(stages)) & 1, abort_flag)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 const uint32_t a_addr = smem_u32(sA + size_t(s) * kBtATile);
-                const uint32_t b_addr = smem_u32(sB + size_t(kb) * kBtBBlock);
+                const uint32_t b_addr = smem_u32(sW + size_t(kb) * kBtBBlock);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {   // K = 8 TF32 values (32 bytes) per MMA
                     const uint64_t ad = smem_desc(a_addr + k * 32, 0, 1024, kSwizzle128B);
@@ -1520,17 +1570,30 @@ __global__ void __launch_bounds__(192, 1)
         if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
     } else if (warp >= 2) {
         // ----------------------------------------------------------- epilogue
-        const int q = warp & 3;            // the tensor-memory lane quadrant this warp may read
-        const int slot = (warp - 2) * 32;  // its 32 staging rows
-        op16* myx = reinterpret_cast<op16*>(sX + size_t(slot + lane) * XW);
-        float* myb = sBf + size_t(slot + lane) * BS;
-        const int v0 = F * (2 * lf + 1);
-        const int kw = k1p / 2;
-        uint32_t* xw = reinterpret_cast<uint32_t*>(x);
-        uint32_t t = 0;
-        for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++t) {
-            const uint32_t acc = t & 1;
-            if (!mbar_wait(&acc_full[acc], (t >> 1) & 1, abort_flag)) {
+        const int q = warp & 3;           // the tensor-memory lane quadrant this warp may read
+        const int grp = (warp - 2) >> 2;  // group 0 takes the CTA's even tiles, group 1 the odd
+        uint8_t* stX = sStage + size_t(warp - 2) * bt_stage_bytes(k1p);   // nbx boxes, then the B box
+        uint8_t* stB = stX + size_t(nbx) * kBtBox;
+        const uint32_t rowoff = uint32_t(lane) * 128u, sw = uint32_t(lane & 7);
+        // 16-byte piece j (columns 8 j .. 8 j + 7) of this thread's x row
+        auto put_x = [&](int j, uint4 v) {
+            *reinterpret_cast<uint4*>(stX + size_t(j >> 3) * kBtBox + rowoff + ((uint32_t(j & 7) ^ sw) << 4)) = v;
+        };
+        const int fb = bw / 8, vp0 = (2 * lf + 1) * fb, np = k1p / 8;
+        const float zero8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (uint32_t t = uint32_t(grp);; t += 2) {
+            const int64_t tile = blockIdx.x + int64_t(t) * gridDim.x;
+            if (tile >= num_tiles) break;
+            const uint32_t acc = t & 3;
+            const int64_t row0 = tile * 128 + q * 32;
+            const int64_t m = row0 + lane;
+            float dv[3] = {0.f, 0.f, 0.f};
+            if (view && m < M) {
+                dv[0] = view[m * 3];
+                dv[1] = view[m * 3 + 1];
+                dv[2] = view[m * 3 + 2];
+            }
+            if (!mbar_wait(&acc_full[acc], (t >> 2) & 1, abort_flag)) {
                 *abort_flag = 1;
                 break;
             }
@@ -1540,82 +1603,418 @@ __global__ void __launch_bounds__(192, 1)
             tmem_ld_wait();
             tc_fence_before();
             mbar_arrive(&acc_empty[acc]);
-            const int64_t row0 = tile * 128 + q * 32;
-            const int64_t m = row0 + lane;
+            // the previous tile's stores have finished reading the staging boxes
+            if (lane == 0) bulk_wait_read_all();
+            __syncwarp();
+            // B row: columns past F are zeros (Wb rows past F read as zeros)
 #pragma unroll
-            for (int f = 0; f < 32; ++f) {
-                if (f < F) {
-                    const float v = __uint_as_float(r[f]);
-                    myb[f] = v;
-                    myx[f] = to16(v, fmt);
-                    float sh, ch;
-                    sincos16(v, &sh, &ch);
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<uint4*>(stB + rowoff + ((uint32_t(j) ^ sw) << 4)) =
+                    make_uint4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
+            // feature blocks, eight features at a time: B, then sin / cos of 2^k B
+#pragma unroll
+            for (int g = 0; g < kMaxBasis / 8; ++g) {
+                if (g < fb) {
+                    const int valid = F - 8 * g;
+                    float sn[8], cs[8], v[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        v[i] = __uint_as_float(r[8 * g + i]);
+                        sincos16(v[i], &sn[i], &cs[i]);
+                    }
+                    put_x(g, pack8<FMT>(v, valid));
                     for (int k = 0; k < lf; ++k) {
-                        myx[F + f + 2 * F * k] = to16(sh, fmt);
-                        myx[2 * F + f + 2 * F * k] = to16(ch, fmt);
-                        const float s2 = 2.f * sh * ch, c2 = (ch - sh) * (ch + sh);
-                        sh = s2;
-                        ch = c2;
+                        put_x((2 * k + 1) * fb + g, pack8<FMT>(sn, valid));
+                        put_x((2 * k + 2) * fb + g, pack8<FMT>(cs, valid));
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const float s2 = 2.f * sn[i] * cs[i], c2 = (cs[i] - sn[i]) * (cs[i] + sn[i]);
+                            sn[i] = s2;
+                            cs[i] = c2;
+                        }
                     }
                 }
             }
+            // view block [d, sin d, cos d, sin 2d, cos 2d, ...] (lv <= 4: at most 27
+            // values, four pieces), zeros up to k1p
+            float vv[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) vv[i] = 0.f;
             if (view) {
+                float sn[3], cs[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    const float v = m < M ? view[m * 3 + a] : 0.f;
-                    myx[v0 + a] = to16(v, fmt);
-                    float sh, ch;
-                    sincos16(v, &sh, &ch);
-                    for (int k = 0; k < lv; ++k) {
-                        myx[v0 + 3 + a + 6 * k] = to16(sh, fmt);
-                        myx[v0 + 6 + a + 6 * k] = to16(ch, fmt);
-                        const float s2 = 2.f * sh * ch, c2 = (ch - sh) * (ch + sh);
-                        sh = s2;
-                        ch = c2;
+                    vv[a] = dv[a];
+                    sincos16(dv[a], &sn[a], &cs[a]);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (k < lv) {
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            vv[3 + 6 * k + a] = sn[a];
+                            vv[6 + 6 * k + a] = cs[a];
+                            const float s2 = 2.f * sn[a] * cs[a], c2 = (cs[a] - sn[a]) * (cs[a] + sn[a]);
+                            sn[a] = s2;
+                            cs[a] = c2;
+                        }
                     }
                 }
             }
-            for (int c = k1; c < k1p; ++c) myx[c] = op16(0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (vp0 + j < np) put_x(vp0 + j, pack8<FMT>(vv + 8 * j, 8));
+            for (int j = vp0 + 4; j < np; ++j) put_x(j, pack8<FMT>(zero8, 0));
+            fence_proxy_async_smem();
             __syncwarp();
-            for (int rr = 0; rr < 32; ++rr) {
-                const int64_t g = row0 + rr;
-                if (g >= M) break;
-                const uint32_t* src = sX + size_t(slot + rr) * XW;
-                for (int w2 = lane; w2 < kw; w2 += 32) xw[g * kw + w2] = src[w2];
-                const float* bs = sBf + size_t(slot + rr) * BS;
-                for (int f = lane; f < F; f += 32) Bout[g * F + f] = bs[f];
+            if (lane == 0 && row0 < M) {
+                for (int b = 0; b < nbx; ++b) tma_store_2d(&tmX, stX + size_t(b) * kBtBox, b * 64, int32_t(row0));
+                tma_store_2d(&tmB, stB, 0, int32_t(row0));
+                bulk_commit_group();
             }
+        }
+        if (lane == 0) bulk_wait_all();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 128);
+    }
+    if (threadIdx.x == 0 && *abort_flag) raise_flag(flag, kFlagTimeout);
+}
+
+// The basis adjoint on the tensor cores, for the rows of one backward call:
+//   dB[m, o]   = (1 / loss scale) sum over the PE columns of B[m, o] of dx * d(column)/dB
+//   d_feats[m] = dB[m] . Wb              (TF32 tcgen05 GEMM, M = 128 rows, N = C, K = 32)
+// and dB itself written out for basis_wgrad_kernel (dWb += dB^T feats).
+// Warp roles (320 threads, one CTA per SM, persistent over tiles): warp 0 streams
+// each tile's dx (64-column boxes) and B rows through a two-stage TMA ring and
+// loads WbT (C x 32, the B operand, K-major) once; warps 2..9, two groups of four
+// taking alternate tiles (group g the ring stage g and dB tile g), form dB, a
+// thread per row, from the swizzled dx and B rows, write it as the MMA's A tile
+// (128 x 32 floats, 128-byte swizzle) and store their 32 rows of it with TMA; warp
+// 1 issues the four K = 8 MMAs per tile into one of two 256-column accumulators;
+// warps 10..13 read their lane quadrant of the accumulator (a thread per row) and
+// store the d_feats rows with 16-byte stores.  Every mbarrier wait is bounded.
+constexpr int kBbThreads = 448;
+constexpr uint32_t kBbBox = 128 * 128;       // a 128-row x 128-byte box (dx or B rows)
+
+__host__ __device__ inline size_t bb_stage_bytes(int k1p) { return size_t(k1p / 64 + 1) * kBbBox; }
+__host__ __device__ inline size_t bb_smem(int C, int k1p) {
+    return 1024 + size_t((C + 7) / 8 * 8) * 128 + 2 * bb_stage_bytes(k1p) + 2 * size_t(kBbBox) + 256;
+}
+
+__global__ void __launch_bounds__(kBbThreads, 1)
+    basis_bwd_tc_kernel(const __grid_constant__ CUtensorMap tmDX, const __grid_constant__ CUtensorMap tmB,
+                        const __grid_constant__ CUtensorMap tmWT, const __grid_constant__ CUtensorMap tmDB,
+                        int64_t M, int C, int F, int lf, int bw, int k1p, int fmt, const float* gscale,
+                        float* __restrict__ d_feats, int* flag) {
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int nbx = k1p / 64;
+    const uint32_t wt_bytes = uint32_t((C + 7) / 8 * 8) * 128u;
+    uint8_t* sWT = base;
+    uint8_t* sRing = sWT + wt_bytes;                        // 2 stages: nbx dx boxes, then the B box
+    uint8_t* sA = sRing + 2 * bb_stage_bytes(k1p);          // 2 dB tiles
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + 2 * size_t(kBbBox));
+    uint64_t* full = bars;            // [2] ring stage loaded
+    uint64_t* empty = bars + 2;       // [2] ring stage read (128 arrivals)
+    uint64_t* a_full = bars + 4;      // [2] dB tile written (128 arrivals)
+    uint64_t* a_empty = bars + 6;     // [2] dB tile read by the MMAs
+    uint64_t* acc_full = bars + 8;    // [2]
+    uint64_t* acc_empty = bars + 10;  // [2] (128 arrivals)
+    uint64_t* w_full = bars + 12;
+    uint64_t* done = bars + 13;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 14);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t num_tiles = (M + 127) / 128;
+    const int64_t my_tiles = blockIdx.x < num_tiles ? (num_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 128);
+            mbar_init(&a_full[i], 128);
+            mbar_init(&a_empty[i], 1);
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 128);
+        }
+        mbar_init(w_full, 1);
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ------------------------------------------------------------ producer
+        prefetch_tmap(&tmDX);
+        prefetch_tmap(&tmB);
+        prefetch_tmap(&tmWT);
+        mbar_arrive_expect_tx(w_full, uint32_t(C) * 128u);
+        tma_load_2d(sWT, &tmWT, w_full, 0, 0);
+        bool used[2] = {false, false};
+        uint32_t last[2] = {0, 0};
+        for (int64_t t = 0; t < my_tiles && !*abort_flag; ++t) {
+            const int s = int(t & 1);
+            const uint32_t ph = uint32_t(t >> 1) & 1;
+            if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            const int64_t tile = blockIdx.x + t * gridDim.x;
+            uint8_t* st = sRing + size_t(s) * bb_stage_bytes(k1p);
+            mbar_arrive_expect_tx(&full[s], uint32_t(nbx + 1) * kBbBox);
+            for (int j = 0; j < nbx; ++j) tma_load_2d(st + size_t(j) * kBbBox, &tmDX, &full[s], j * 64, int32_t(tile * 128));
+            tma_load_2d(st + size_t(nbx) * kBbBox, &tmB, &full[s], 0, int32_t(tile * 128));
+            used[s] = true;
+            last[s] = ph;
+        }
+        for (int s = 0; s < 2; ++s)
+            if (used[s] && !mbar_wait(&full[s], last[s], nullptr)) *abort_flag = 1;
+        if (!mbar_wait(w_full, 0, nullptr)) *abort_flag = 1;
+    } else if (warp == 1 && lane == 0) {
+        // ---------------------------------------------------------------- MMA
+        const uint32_t idesc = idesc_tf32(128, C);
+        bool ok = mbar_wait(w_full, 0, abort_flag);
+        const uint32_t b_addr = smem_u32(sWT);
+        for (int64_t t = 0; ok && t < my_tiles; ++t) {
+            const int b = int(t & 1);
+            const uint32_t ph = uint32_t(t >> 1) & 1;
+            if (!mbar_wait(&acc_empty[b], ph ^ 1, abort_flag) || !mbar_wait(&a_full[b], ph, abort_flag)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(sA + size_t(b) * kBbBox);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {   // K = 8 TF32 values (32 bytes) per MMA
+                const uint64_t ad = smem_desc(a_addr + k * 32, 0, 1024, kSwizzle128B);
+                const uint64_t bd = smem_desc(b_addr + k * 32, 0, 1024, kSwizzle128B);
+                mma_tf32(tmem + uint32_t(b) * 256u, ad, bd, idesc, k != 0);
+            }
+            mma_commit(&a_empty[b]);
+            mma_commit(&acc_full[b]);
+        }
+        if (!ok) *abort_flag = 1;
+        mma_commit(done);
+        if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
+    } else if (warp >= 2 && warp < 10) {
+        // ------------------------------------------------------------- adjoint
+        const int grp = (warp - 2) >> 2;        // takes the tiles t with t % 2 == grp
+        const int wq = (warp - 2) & 3;          // its 32 rows of the tile
+        const int r = wq * 32 + lane;           // row within the tile
+        const uint32_t rowoff = uint32_t(r) * 128u, sw = uint32_t(r & 7);
+        const float unscale = gscale ? gscale[1] : 1.f;
+        const int fb = bw / 8;
+        for (int64_t t = grp; t < my_tiles; t += 2) {
+            const int s = int(t & 1);
+            const uint32_t ph = uint32_t(t >> 1) & 1;
+            const int64_t row0 = (blockIdx.x + t * gridDim.x) * 128 + wq * 32;
+            if (!mbar_wait(&full[s], ph, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            const uint8_t* st = sRing + size_t(s) * bb_stage_bytes(k1p);
+            const uint8_t* sBrow = st + size_t(nbx) * kBbBox + rowoff;
+            // 16-byte piece p of this row's dx (eight 16-bit columns) as floats
+            auto dx8 = [&](int p, float* o) {
+                const uint4 v = *reinterpret_cast<const uint4*>(st + size_t(p >> 3) * kBbBox + rowoff +
+                                                                ((uint32_t(p & 7) ^ sw) << 4));
+                const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float2 f = unpack16(w[i], fmt);
+                    o[2 * i] = f.x;
+                    o[2 * i + 1] = f.y;
+                }
+            };
+            float dB[32];
+#pragma unroll
+            for (int g = 0; g < kMaxBasis / 8; ++g) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) dB[8 * g + i] = 0.f;
+                if (g < fb) {
+                    float bv[8], sn[8], cs[8], acc[8], ds[8], dc[8];
+                    const float4 b0 = *reinterpret_cast<const float4*>(sBrow + ((uint32_t(2 * g) ^ sw) << 4));
+                    const float4 b1 = *reinterpret_cast<const float4*>(sBrow + ((uint32_t(2 * g + 1) ^ sw) << 4));
+                    bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
+                    bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)   // B columns past F are not written by every forward
+                        if (8 * g + i >= F) bv[i] = 0.f;
+                    dx8(g, acc);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) sincos16(bv[i], &sn[i], &cs[i]);
+                    float fk = 1.f;
+                    for (int k = 0; k < lf; ++k) {
+                        dx8((2 * k + 1) * fb + g, ds);
+                        dx8((2 * k + 2) * fb + g, dc);
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            acc[i] += fk * (cs[i] * ds[i] - sn[i] * dc[i]);
+                            const float s2 = 2.f * sn[i] * cs[i], c2 = (cs[i] - sn[i]) * (cs[i] + sn[i]);
+                            sn[i] = s2;
+                            cs[i] = c2;
+                        }
+                        fk *= 2.f;
+                    }
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) dB[8 * g + i] = 8 * g + i < F ? acc[i] * unscale : 0.f;
+                }
+            }
+            mbar_arrive(&empty[s]);   // this thread is done with the ring stage
+            const int b = int(t & 1);
+            if (!mbar_wait(&a_empty[b], ph ^ 1, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            if (lane == 0) bulk_wait_read_all();   // the dB store from this tile buffer has read it
             __syncwarp();
+            uint8_t* at = sA + size_t(b) * kBbBox;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<float4*>(at + rowoff + ((uint32_t(j) ^ sw) << 4)) =
+                    make_float4(dB[4 * j], dB[4 * j + 1], dB[4 * j + 2], dB[4 * j + 3]);
+            fence_proxy_async_smem();
+            mbar_arrive(&a_full[b]);
+            __syncwarp();
+            if (lane == 0 && row0 < M) {
+                tma_store_2d(&tmDB, at + size_t(wq) * 32 * 128, 0, int32_t(row0));
+                bulk_commit_group();
+            }
+        }
+        if (lane == 0) bulk_wait_all();
+    } else if (warp >= 10) {
+        // ----------------------------------------------------------- epilogue
+        const int q = warp & 3;   // the tensor-memory lane quadrant this warp may read
+        const int nchunk = (C + 31) / 32;
+        for (int64_t t = 0; t < my_tiles; ++t) {
+            const int b = int(t & 1);
+            const uint32_t ph = uint32_t(t >> 1) & 1;
+            const int64_t m = (blockIdx.x + t * gridDim.x) * 128 + q * 32 + lane;
+            if (!mbar_wait(&acc_full[b], ph, abort_flag)) {
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            float* dst = d_feats + m * C;
+            for (int ch = 0; ch < nchunk; ++ch) {
+                uint32_t v[32];
+                tmem_ld_32x32b_x32(tmem + uint32_t(b) * 256u + uint32_t(ch * 32) + (uint32_t(q * 32) << 16), v);
+                tmem_ld_wait();
+                if (m < M) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (ch * 32 + 4 * j < C)
+                            *reinterpret_cast<float4*>(dst + ch * 32 + 4 * j) =
+                                make_float4(__uint_as_float(v[4 * j]), __uint_as_float(v[4 * j + 1]),
+                                            __uint_as_float(v[4 * j + 2]), __uint_as_float(v[4 * j + 3]));
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acc_empty[b]);
         }
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, 64);
+        tmem_dealloc(tmem, 512);
     }
     if (threadIdx.x == 0 && *abort_flag) raise_flag(flag, kFlagTimeout);
 }
 
-}  // namespace
+// dWb[o, c] += sum over rows of dB[m, o] feats[m, c] (dB rows of 32 floats, zeros
+// past F, which the tensor-core adjoint writes), over a contiguous range of rows
+// per block in tiles of 32 rows whose feature and dB rows arrive by asynchronous
+// copies under the previous tile.  A thread holds a 16-feature x 4-column block of
+// dWb in registers (one 128-bit feature load and four 128-bit dB loads feed 64
+// FMAs); kWgRowGroups groups of C / 2 threads take interleaved rows of each tile;
+// at the end the groups meet in shared memory and the block adds its partial sums
+// to dWb atomically.
+constexpr int kWgRowGroups = 4;
 
-// The tensor-core basis pass when its operands fit (C a multiple of 4 up to 256,
-// F <= 32, 16-byte aligned feats and Wb); SRF_ERR_UNSUPPORTED otherwise.
-bool basis_tc_fits(int C, int F, int k1p, const float* feats, const float* Wb) {
-    return C % 4 == 0 && C <= 256 && F <= 32 && k1p % 2 == 0 && ok16(feats) && ok16(Wb) &&
-           bt_smem(C, F, k1p) <= tc::kMaxSmem;
+__global__ void __launch_bounds__(512) basis_wgrad_kernel(const float* __restrict__ dB,
+                                                          const float* __restrict__ feats, int64_t M, int F, int C,
+                                                          int64_t rows_per_block, float* dWb) {
+    extern __shared__ __align__(16) float wsm[];
+    const size_t tile_floats = size_t(kBwdTile) * (C + kMaxBasis);
+    const int ncg = C / 4, per_rg = 2 * ncg;
+    const int rg = threadIdx.x / per_rg, u = threadIdx.x - rg * per_rg;
+    const int h = u / ncg, cg = u - h * ncg;   // features 16 h .. 16 h + 15, columns 4 cg .. 4 cg + 3
+    float acc[16][4];
+#pragma unroll
+    for (int o = 0; o < 16; ++o) acc[o][0] = acc[o][1] = acc[o][2] = acc[o][3] = 0.f;
+    const int64_t r_begin = int64_t(blockIdx.x) * rows_per_block;
+    const int64_t r_end = r_begin + rows_per_block < M ? r_begin + rows_per_block : M;
+    auto load_tile = [&](int64_t t0, int which) {
+        if (t0 < r_end) {
+            const int nt = int(r_end - t0 < kBwdTile ? r_end - t0 : kBwdTile);
+            float* sF = wsm + which * tile_floats;
+            float* sD = sF + size_t(kBwdTile) * C;
+            const float* gf = feats + t0 * C;
+            for (int i = threadIdx.x; i < nt * C / 4; i += blockDim.x) cp_async16(sF + 4 * i, gf + 4 * i);
+            const float* gd = dB + t0 * kMaxBasis;
+            for (int i = threadIdx.x; i < nt * kMaxBasis / 4; i += blockDim.x) cp_async16(sD + 4 * i, gd + 4 * i);
+        }
+        cp_async_commit();
+    };
+    load_tile(r_begin, 0);
+    int buf = 0;
+    for (int64_t t0 = r_begin; t0 < r_end; t0 += kBwdTile, buf ^= 1) {
+        const int nt = int(r_end - t0 < kBwdTile ? r_end - t0 : kBwdTile);
+        load_tile(t0 + kBwdTile, buf ^ 1);
+        cp_async_wait_one();
+        __syncthreads();
+        const float* sF = wsm + buf * tile_floats;
+        const float* sD = sF + size_t(kBwdTile) * C;
+        for (int rr = rg; rr < nt; rr += kWgRowGroups) {
+            const float4 f = *reinterpret_cast<const float4*>(sF + rr * C + 4 * cg);
+            const float4* d = reinterpret_cast<const float4*>(sD + rr * kMaxBasis + 16 * h);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float4 dv = d[j];
+                const float dd[4] = {dv.x, dv.y, dv.z, dv.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    ffma2(acc[4 * j + i][0], acc[4 * j + i][1], dd[i], f.x, f.y);
+                    ffma2(acc[4 * j + i][2], acc[4 * j + i][3], dd[i], f.z, f.w);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // the row groups' partial sums meet in shared memory (32 x C floats)
+    float* red = wsm;
+    for (int i = threadIdx.x; i < kMaxBasis * C; i += blockDim.x) red[i] = 0.f;
+    __syncthreads();
+#pragma unroll
+    for (int o = 0; o < 16; ++o)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) atomicAdd(red + (16 * h + o) * C + 4 * cg + k, acc[o][k]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < F * C; i += blockDim.x) atomicAdd(dWb + i, red[i]);
 }
 
-int launch_basis_tc(const float* feats, int C, const float* Wb, int F, const float* view, int64_t m, int lf, int lv,
-                    int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
-    if (!basis_tc_fits(C, F, k1p, feats, Wb)) return SRF_ERR_UNSUPPORTED;
-    const size_t smem = bt_smem(C, F, k1p);
-    CUtensorMap ma, mb;
-    if (!make_map_f32(&ma, feats, uint64_t(C), uint64_t(m), uint64_t(C) * 4, 32, 128)) return SRF_ERR_CUDA;
-    if (!make_map_f32(&mb, Wb, uint64_t(C), uint64_t(F), uint64_t(C) * 4, 32, 32)) return SRF_ERR_CUDA;
+template <int FMT>
+int launch_basis_tc_fmt(const CUtensorMap& ma, const CUtensorMap& mw, const CUtensorMap& mx, const CUtensorMap& mb,
+                        const RenderLayout& R, const float* view, int64_t m, int stages, cudaStream_t s) {
     static bool attr_done = false;
     if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(basis_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(basis_tc_kernel<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              int(tc::kMaxSmem));
         if (e != cudaSuccess) {
             set_cuda_error(e);
@@ -1625,25 +2024,117 @@ int launch_basis_tc(const float* feats, int C, const float* Wb, int F, const flo
     }
     const int64_t tiles = (m + 127) / 128;
     const int grid = int(tiles < num_sms() ? tiles : num_sms());
-    basis_tc_kernel<<<grid, 192, smem, s>>>(ma, mb, m, C, F, view, lf, lv, k1, k1p, B, x, fmt, device_flag());
+    basis_tc_kernel<FMT><<<grid, kBtThreads, bt_smem(R.C, R.k1p, stages), s>>>(
+        ma, mw, mx, mb, m, R.C, R.F, view, R.lf, R.lv, R.bw, R.k1p, stages, device_flag());
+    return launch_status();
+}
+
+}  // namespace
+
+// Whether the tensor-core basis pass takes these operands: C a multiple of 4 up to
+// 256, F <= 32 (B rows of 32 floats), the view block within four pieces, k1p a
+// multiple of 64 and 16-byte aligned rows.
+bool basis_tc_fits(const RenderLayout& R, const float* feats, const float* Wb, const float* B, const op16* x) {
+    return R.C % 4 == 0 && R.C <= 256 && R.F <= 32 && R.bs == 32 && R.lv <= 4 && R.k1p % 64 == 0 && ok16(feats) &&
+           ok16(Wb) && ok16(B) && ok16(x) && bt_stages(R.C, R.k1p) >= 3;
+}
+
+int launch_basis_tc(const RenderLayout& R, const float* feats, const float* Wb, const float* view, int64_t m,
+                    float* B, op16* x, int fmt, cudaStream_t s) {
+    if (!basis_tc_fits(R, feats, Wb, B, x)) return SRF_ERR_UNSUPPORTED;
+    CUtensorMap ma, mw, mx, mb;
+    if (!make_map_t(&ma, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, feats, uint64_t(R.C), uint64_t(m), uint64_t(R.C) * 4, 32,
+                    128) ||
+        !make_map_t(&mw, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, Wb, uint64_t(R.C), uint64_t(R.F), uint64_t(R.C) * 4, 32,
+                    32) ||
+        !make_map_t(&mx, CU_TENSOR_MAP_DATA_TYPE_UINT16, x, uint64_t(R.k1p), uint64_t(m), uint64_t(R.k1p) * 2, 64,
+                    32) ||
+        !make_map_t(&mb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, B, uint64_t(R.bs), uint64_t(m), uint64_t(R.bs) * 4, 32, 32))
+        return SRF_ERR_CUDA;
+    const int stages = bt_stages(R.C, R.k1p);
+    return fmt == tc::kFmtF16 ? launch_basis_tc_fmt<tc::kFmtF16>(ma, mw, mx, mb, R, view, m, stages, s)
+                              : launch_basis_tc_fmt<tc::kFmtBF16>(ma, mw, mx, mb, R, view, m, stages, s);
+}
+
+// Which basis adjoint the 16-bit renderer backward runs: 1 the tensor-core pass
+// where its shapes fit (default), 0 always the fused SIMT pass.
+std::atomic<int> g_basis_adjoint_tc{1};
+
+// Whether the tensor-core basis adjoint takes these operands: C a multiple of 16 up
+// to 256 (the MMA's N), F <= 32, k1p a multiple of 64, 16-byte aligned rows.
+bool basis_bwd_tc_fits(const RenderLayout& R, const void* dx, const float* B, const float* feats,
+                       const float* d_feats, const float* dB) {
+    return R.C % 16 == 0 && R.C <= 256 && R.F <= 32 && R.bs == 32 && R.k1p % 64 == 0 && ok16(dx) && ok16(B) &&
+           ok16(feats) && ok16(d_feats) && ok16(dB) && bb_smem(R.C, R.k1p) <= tc::kMaxSmem;
+}
+
+int launch_basis_bwd_tc(const RenderLayout& R, const op16* dx, const float* B, const float* WbT, float* dB,
+                        float* d_feats, int fmt, const float* gscale, int64_t m, cudaStream_t s) {
+    CUtensorMap mdx, mb, mwt, mdb;
+    if (!make_map_t(&mdx, CU_TENSOR_MAP_DATA_TYPE_UINT16, dx, uint64_t(R.k1p), uint64_t(m), uint64_t(R.k1p) * 2, 64,
+                    128) ||
+        !make_map_t(&mb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, B, uint64_t(R.bs), uint64_t(m), uint64_t(R.bs) * 4, 32,
+                    128) ||
+        !make_map_t(&mwt, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, WbT, uint64_t(kMaxBasis), uint64_t(R.C),
+                    uint64_t(kMaxBasis) * 4, 32, uint32_t(R.C)) ||
+        !make_map_t(&mdb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, dB, uint64_t(kMaxBasis), uint64_t(m),
+                    uint64_t(kMaxBasis) * 4, 32, 32))
+        return SRF_ERR_CUDA;
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaError_t e = cudaFuncSetAttribute(basis_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(tc::kMaxSmem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+        attr_done = true;
+    }
+    const int64_t tiles = (m + 127) / 128;
+    const int grid = int(tiles < num_sms() ? tiles : num_sms());
+    basis_bwd_tc_kernel<<<grid, kBbThreads, bb_smem(R.C, R.k1p), s>>>(mdx, mb, mwt, mdb, m, R.C, R.F, R.lf, R.bw,
+                                                                       R.k1p, fmt, gscale, d_feats, device_flag());
+    return launch_status();
+}
+
+// dWb += dB^T feats over m rows: as many resident blocks as fit, each over a
+// contiguous range of rows (a multiple of the 32-row tile).
+int launch_basis_wgrad(const RenderLayout& R, const float* dB, const float* feats, int64_t m, float* dWb,
+                       cudaStream_t s) {
+    const int threads = kWgRowGroups * (R.C / 2);   // C a multiple of 16: whole warps, at most 512
+    const size_t smem = 2 * size_t(kBwdTile) * (R.C + kMaxBasis) * sizeof(float);
+    if (smem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
+    cudaError_t e = cudaFuncSetAttribute(basis_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, basis_wgrad_kernel, threads, smem);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    int64_t blocks = int64_t(num_sms()) * (per_sm > 0 ? per_sm : 1);
+    int64_t per = (m + blocks - 1) / blocks;
+    per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
+    blocks = (m + per - 1) / per;
+    basis_wgrad_kernel<<<unsigned(blocks), threads, smem, s>>>(dB, feats, m, R.F, R.C, per, dWb);
     return launch_status();
 }
 
 // The basis + encoding pass: the tuner picks per (C, k1p) among the SIMT tile shapes
 // (rows per thread x threads, reading the transposed basis the call writes to WbT)
 // and the tensor-core pass (Wb as stored; candidate 5, where its operands fit).
-// Without tuning: the tensor-core pass where it applies, else the first SIMT shape
-// whose shared memory fits (128 x 2 measured fastest of those for C = 144).
-int launch_basis_encode(const float* feats, int C, const float* Wb, float* WbT, int F, const float* view, int64_t m,
-                        int lf, int lv, int k1, int k1p, float* B, op16* x, int fmt, cudaStream_t s) {
+// Without tuning: the first SIMT shape whose shared memory fits (128 x 2 measured
+// fastest for C = 144, ahead of the tensor-core pass).
+int launch_basis_encode(const RenderLayout& R, const float* feats, const float* Wb, float* WbT, const float* view,
+                        int64_t m, float* B, op16* x, int fmt, cudaStream_t s) {
     if (m <= 0) return SRF_OK;
+    const int C = R.C, F = R.F, k1p = R.k1p;
     auto run = [&](int i) -> int {
-        if (i == 5) return launch_basis_tc(feats, C, Wb, F, view, m, lf, lv, k1, k1p, B, x, fmt, s);
+        if (i == 5) return launch_basis_tc(R, feats, Wb, view, m, B, x, fmt, s);
         transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(Wb, F, C, WbT);
         if (const int st = launch_status()) return st;
-#define SRF_ENC(R, N)                                                                                             \
-    (enc_smem_bytes(C, k1p, R, N) <= tc::kMaxSmem                                                                 \
-         ? launch_basis_encode_cfg<R, N>(feats, C, WbT, F, view, m, lf, lv, k1, k1p, B, x, fmt, s)                \
+#define SRF_ENC(RR, N)                                                                                            \
+    (enc_smem_bytes(C, k1p, RR, N) <= tc::kMaxSmem                                                                \
+         ? launch_basis_encode_cfg<RR, N>(feats, C, WbT, F, view, m, R.lf, R.lv, R.bw, R.bs, k1p, B, x, fmt, s)  \
          : SRF_ERR_UNSUPPORTED)
         switch (i) {
             case 0: return SRF_ENC(2, 128);
@@ -1654,8 +2145,7 @@ int launch_basis_encode(const float* feats, int C, const float* Wb, float* WbT, 
         }
 #undef SRF_ENC
     };
-    const int fallback =
-        basis_tc_fits(C, F, k1p, feats, Wb) ? 5 : enc_smem_bytes(C, k1p, 2, 128) <= tc::kMaxSmem ? 0 : 4;
+    const int fallback = enc_smem_bytes(C, k1p, 2, 128) <= tc::kMaxSmem ? 0 : 4;
     const tune::Key key{tune::kSiteBasisEncode, C, k1p, 0};
     return run(tune::pick(key, 6, fallback, s, run));
 }
@@ -1673,9 +2163,7 @@ int render_tc_forward(int C, int F, int U, int lf, int lv, int view, const float
     if ((st = pack(R.l1, P[1], w.W1, w.W1T, fmt, s))) return st;
     if ((st = pack(R.l2, P[3], w.W2, w.W2T, fmt, s))) return st;
     if (!aligned16(feats)) return SRF_ERR_ALIGN;
-    if ((st = launch_basis_encode(feats, C, P[0], w.WbT, F, view ? vdirs : nullptr, m, lf, lv, R.k1, R.k1p, w.B, w.x,
-                                  fmt, s)))
-        return st;
+    if ((st = launch_basis_encode(R, feats, P[0], w.WbT, view ? vdirs : nullptr, m, w.B, w.x, fmt, s))) return st;
     if ((st = tc_linear(make_epilogue(w.h1, U, P[2], 1, fmt, cx.found_inf()), w.x, R.k1p, R.k1p, nullptr, 0, 0,
                         w.W1, R.k1p, U, 0, m, U, s)))
         return st;
@@ -1717,9 +2205,17 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
         tc::GemmEpilogue e1 = make_epilogue(w.dx + c0, R.k1p, nullptr, 0, fmt, cx.found_inf());
         if ((st = tc_linear(e1, w.dz1, U, U, nullptr, 0, 0, w.W1T, U, R.k1p, c0, m, n, s))) return st;
     }
-    // PE adjoint + basis layer: d_feats = dB . Wb, dWb += dB^T feats
+    // PE adjoint + basis layer: d_feats = dB . Wb, dWb += dB^T feats; on the tensor
+    // cores (d_feats) and a SIMT reduction (dWb) where the shapes fit, else one
+    // fused SIMT pass
+    if (m > 0 && g_basis_adjoint_tc.load() && basis_bwd_tc_fits(R, w.dx, w.B, feats, d_feats, w.dB)) {
+        transpose_basis_kernel<<<unsigned((C * kMaxBasis + 255) / 256), 256, 0, s>>>(P[0], F, C, w.WbT);
+        if ((st = launch_status())) return st;
+        if ((st = launch_basis_bwd_tc(R, w.dx, w.B, w.WbT, w.dB, d_feats, fmt, cx.gscale(), m, s))) return st;
+        return launch_basis_wgrad(R, w.dB, feats, m, G[0], s);
+    }
     const int threads = (C + 31) / 32 * 32;
-    const size_t bsmem = basis_bwd_smem(C, F, R.k1p);
+    const size_t bsmem = basis_bwd_smem(C, R.bs, R.k1p);
     if (bsmem > tc::kMaxSmem) return SRF_ERR_UNSUPPORTED;
     if (bsmem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(basis_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1739,8 +2235,8 @@ int render_tc_backward(int C, int F, int U, int lf, int lv, int view, const floa
     int64_t per = (m + blocks - 1) / blocks;
     per = (per + kBwdTile - 1) / kBwdTile * kBwdTile;
     blocks = (m + per - 1) / per;
-    basis_bwd_kernel<<<unsigned(blocks), threads, bsmem, s>>>(w.dx, w.B, feats, P[0], m, F, C, lf, R.k1p, fmt,
-                                                             cx.gscale(), per, d_feats, G[0]);
+    basis_bwd_kernel<<<unsigned(blocks), threads, bsmem, s>>>(w.dx, w.B, feats, P[0], m, F, C, lf, R.bw, R.bs,
+                                                             R.k1p, fmt, cx.gscale(), per, d_feats, G[0]);
     return launch_status();
 }
 
@@ -1805,6 +2301,11 @@ extern "C" int srf_tensorf_renderer_forward(const srf_tensorf_renderer_desc* d, 
     return render_tc_forward(d->n_comp, d->features, d->units, d->features_pe_degree, d->views_pe_degree,
                              d->view_dependent, params, feats, view_dirs, m, rgb, for_backward != 0, workspace,
                              workspace_bytes, fmt, scaler, as_stream(stream));
+}
+
+extern "C" int srf_tensorf_basis_adjoint_path(int tensor_cores) {
+    g_basis_adjoint_tc.store(tensor_cores ? 1 : 0);
+    return SRF_OK;
 }
 
 extern "C" int srf_tensorf_renderer_backward(const srf_tensorf_renderer_desc* d, const float* const* params,

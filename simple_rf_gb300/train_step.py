@@ -470,9 +470,13 @@ def main(argv=None):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    for _ in range(args.steps):
-        step.step()
+    # the timed steps are the range a profiler started with profiling off captures
+    torch.cuda.profiler.start()
+    with F.nvtx_range('srf.timed_steps'):
+        for _ in range(args.steps):
+            step.step()
     e1.record()
+    torch.cuda.profiler.stop()
     e1.synchronize()
     ms = e0.elapsed_time(e1) / max(args.steps, 1)
     print(json.dumps({'config': args.config, 'rays': args.rays, 'precision': args.precision, 'graph': not args.eager,

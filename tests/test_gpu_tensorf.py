@@ -224,16 +224,25 @@ def test_tensorf_tensor_core_renderer_against_fp32(precision, bar, basis):
         loss.backward()
         params = [tm.basis_matrix_color.weight] + list(tm.color_predictor.parameters()) + list(tm.matrices_color) + \
             list(tm.vectors_color)
-        res[prec] = (out['rgb'].detach(), torch.cat([p.grad.reshape(-1) for p in params]), tm.last_sample_counts)
-    (r32, g32, c32), (r16, g16, c16) = res['fp32'], res[precision]
+        groups = {'basis': [tm.basis_matrix_color.weight], 'mlp': list(tm.color_predictor.parameters()),
+                  'colour_grid': list(tm.matrices_color) + list(tm.vectors_color)}
+        res[prec] = (out['rgb'].detach(), torch.cat([p.grad.reshape(-1) for p in params]), tm.last_sample_counts,
+                     {k: torch.cat([p.grad.reshape(-1) for p in v]) for k, v in groups.items()})
+    (r32, g32, c32, p32), (r16, g16, c16, p16) = res['fp32'], res[precision]
     assert c32['surface'] > 1000 and c32 == c16, (c32, c16)
     err = (r16 - r32).abs().max().item()
     rel = ((g16 - g32).norm() / g32.norm()).item()
-    print(precision, 'basis choice', basis, 'rgb max-abs', err, 'renderer+colour-grid gradient rel-L2', rel)
+    # each group on its own: the basis weights (dB^T feats) and the colour grid
+    # (through d_feats = dB . Wb) separate the two products of the basis adjoint
+    per = {k: ((p16[k] - p32[k]).norm() / p32[k].norm()).item() for k in p32}
+    print(precision, 'basis choice', basis, 'rgb max-abs', err, 'renderer+colour-grid gradient rel-L2', rel,
+          'per group', per)
     if basis is not None:
         autotune.clear()
     assert err < 2e-3, err
     assert rel < bar, rel
+    for k, v in per.items():
+        assert v < bar, (k, v)
 
 
 def test_tensorf_cp_matches_reference_golden(golden):
@@ -421,3 +430,42 @@ def test_drop_in_tensorf_forward_from_pixels_matches_reference(golden, tag):
         r = g[f'{tag}_static.{k}']
         np.testing.assert_allclose(ret_s[k].cpu().numpy()[keep], r[keep], rtol=1e-5,
                                    atol=1e-6 * max(1.0, float(np.abs(r).max())), err_msg='static ' + k)
+
+
+@pytest.mark.parametrize('precision', ['fp16', 'bf16'])
+def test_basis_adjoint_tensor_cores_match_simt(precision):
+    """The 16-bit renderer backward's two basis adjoints on the same inputs: the TF32
+    tensor-core pass (d_feats = dB . Wb) with its dWb reduction against the fused
+    FP32 SIMT pass.  d_feats and dWb within 3e-3 relative L2 (TF32 keeps 10 mantissa
+    bits of dB and Wb); every other gradient is the same computation (1e-5)."""
+    from simple_rf_gb300 import _lib, build as b, tensorf as T
+    b.build()
+    from simple_rf_gb300.bench_tensorf import make_models
+    tm = make_models(DEV, seed=4, precision=precision, grids=(64, 32))[0]
+    cp = tm.color_predictor
+    gen = torch.Generator(device=DEV).manual_seed(8)
+    m = 20000 + 37
+    feats = torch.randn(m, 144, device=DEV, generator=gen) * 0.3
+    vd = torch.nn.functional.normalize(torch.randn(m, 3, device=DEV, generator=gen), dim=-1)
+    g_rgb = torch.rand(m, 3, device=DEV, generator=gen) * 1e-3
+    desc = _lib.RendererDesc(144, cp.features_dimension, cp.mlp[0].out_features, cp.lf, cp.lv, 1)
+    params = [tm.basis_matrix_color.weight, cp.mlp[0].weight, cp.mlp[0].bias, cp.mlp[2].weight, cp.mlp[2].bias,
+              cp.mlp[4].weight, cp.mlp[4].bias]
+    prec = _lib.PRECISIONS[precision]
+    res = {}
+    lib = _lib.load()
+    try:
+        for path in (1, 0):
+            _lib.check(lib.srf_tensorf_basis_adjoint_path(path), 'srf_tensorf_basis_adjoint_path')
+            f = feats.clone().requires_grad_(True)
+            ps = [p.detach().clone().requires_grad_(True) for p in params]
+            T.renderer_tc(desc, prec, f, vd, ps).backward(g_rgb)
+            torch.cuda.synchronize()
+            res[path] = [f.grad] + [p.grad for p in ps]
+    finally:
+        lib.srf_tensorf_basis_adjoint_path(1)
+    names = ['d_feats', 'basis', 'w1', 'b1', 'w2', 'b2', 'w3', 'b3']
+    for name, tc_g, simt_g in zip(names, res[1], res[0]):
+        rel = ((tc_g - simt_g).norm() / simt_g.norm()).item()
+        print(precision, name, 'tensor-core vs SIMT adjoint rel-L2', rel)
+        assert rel < (3e-3 if name in ('d_feats', 'basis') else 1e-5), (name, rel)
