@@ -16,6 +16,7 @@ targets ~ U[0,1]^3.
 
     python -m simple_rf_gb300.bench_tensorf --rays 8192 --steps 10 --warmup 3 [--precision fp16] [--eager]
     python -m simple_rf_gb300.bench_tensorf --sweep        # ray batches 1024 ... 65536
+    python -m simple_rf_gb300.bench_tensorf --renderer-rows 1200000 --steps 5 [--forward-only] [--adjoint simt]
 """
 import argparse
 import json
@@ -117,6 +118,44 @@ def ray_batch_sweep(device, modes=(('fp16', False), ('fp16', True), ('fp32', Fal
     return out
 
 
+def renderer_case(dev, rows, reps=5, adjoint='tc', backward=True):
+    """The FP16 tensor-core renderer (basis 144 -> 27 + PE + 128 -> 128 -> 3) alone on
+    ``rows`` synthetic surface samples (features ~ N(0, 0.3^2), unit view
+    directions): forward and (``backward``) backward ``reps`` times after three
+    warm-up passes; ``adjoint`` picks the basis adjoint ('tc' or 'simt')."""
+    from . import tensorf as T
+    tm = make_models(dev, precision='fp16', grids=(64, 32))[0]
+    cp = tm.color_predictor
+    g = torch.Generator(device=dev).manual_seed(0)
+    feats = (torch.randn(rows, 144, device=dev, generator=g) * 0.3).requires_grad_(backward)
+    vd = torch.nn.functional.normalize(torch.randn(rows, 3, device=dev, generator=g), dim=-1)
+    d_rgb = torch.rand(rows, 3, device=dev, generator=g)
+    desc = _lib.RendererDesc(144, cp.features_dimension, cp.mlp[0].out_features, cp.lf, cp.lv, 1)
+    params = [tm.basis_matrix_color.weight, cp.mlp[0].weight, cp.mlp[0].bias, cp.mlp[2].weight, cp.mlp[2].bias,
+              cp.mlp[4].weight, cp.mlp[4].bias]
+    _lib.check(_lib.load().srf_tensorf_basis_adjoint_path(int(adjoint == 'tc')), 'srf_tensorf_basis_adjoint_path')
+
+    def once():
+        with torch.set_grad_enabled(backward):
+            rgb = T.renderer_tc(desc, _lib.SRF_PRECISION_FP16, feats, vd, params)
+            if backward:
+                rgb.backward(d_rgb)
+
+    for _ in range(3):
+        once()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.profiler.start()
+    e0.record()
+    for _ in range(reps):
+        once()
+    e1.record()
+    torch.cuda.profiler.stop()
+    e1.synchronize()
+    return {'workload': f'tensorf_renderer_fp16_{rows}rows', 'rows': rows, 'backward': backward, 'adjoint': adjoint,
+            'ms_per_pass': round(e0.elapsed_time(e1) / reps, 4)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument('--rays', type=int, default=8192)
@@ -126,10 +165,18 @@ def main(argv=None):
                     help='renderer MLP: FP32 SIMT or 16-bit tensor cores')
     ap.add_argument('--sweep', action='store_true', help='ray-batch sweep 1024 ... 65536, FP16 and FP32 plain')
     ap.add_argument('--eager', action='store_true', help='the uncaptured step (host reads of the sample counts)')
+    ap.add_argument('--renderer-rows', type=int, default=0,
+                    help='time the FP16 renderer alone (forward + backward) on this many surface samples')
+    ap.add_argument('--forward-only', action='store_true', help='with --renderer-rows: the forward alone')
+    ap.add_argument('--adjoint', default='tc', choices=['tc', 'simt'], help='with --renderer-rows: basis adjoint')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
     dev = torch.device('cuda')
+    if args.renderer_rows:
+        print(json.dumps(renderer_case(dev, args.renderer_rows, reps=args.steps, adjoint=args.adjoint,
+                                       backward=not args.forward_only)))
+        return
     if args.sweep:
         print(json.dumps({'workload': 'tensorf_vm_train_step_ray_batch_sweep_300^3+75^3',
                           'sweep': ray_batch_sweep(dev)}))

@@ -757,22 +757,456 @@ __global__ void __launch_bounds__(256) composite_bwd_reg_kernel(srf_composite_ar
 }
 
 // ---------------------------------------------------------------------------
+// Blocked per-ray bodies for the staged kernels: lane j owns the R contiguous
+// samples R j .. R j + R - 1 of a ray held in shared memory (R even, S % 4 == 0,
+// 16-byte aligned rows), so a scan over the ray is R sequential steps in each lane
+// plus one warp scan of the lanes' totals (instead of a warp scan per 32-sample
+// round), and the loads are 8-byte vectors.  The arithmetic of each sample is that
+// of fwd_ray / bwd_ray; the scans and sums group the products and sums
+// differently.  The per-sample outputs (weights; d_sigma and d_rgb) go into the
+// ray's shared-memory stage, which the caller stores with bulk copies.
+// ---------------------------------------------------------------------------
+
+// On entry T[k] = p of sample R lane + k; on exit the product of p over the ray's
+// earlier samples.
+template <int R>
+__device__ __forceinline__ void scan_blk(float (&T)[R], int lane) {
+    float run = 1.f, ex[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        ex[k] = run;
+        run *= T[k];
+    }
+    float inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc *= t;
+    }
+    float pre = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) pre = 1.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) T[k] = pre * ex[k];
+}
+
+// On entry Y[k] = y = sigma delta ds of sample R lane + k; on exit T = exp(-(sum
+// of y over the earlier samples)).
+template <int R>
+__device__ __forceinline__ void exp_scan_blk(float (&Y)[R], int lane) {
+    float run = 0.f, ex[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        ex[k] = run;
+        run += Y[k];
+    }
+    float inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    float pre = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) pre = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) Y[k] = expf(-(pre + ex[k]));
+}
+
+template <int R>
+__device__ __forceinline__ float bin_sum_blk(const float (&v)[R], const BinLayout& bl, int b, int lane) {
+    float part = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = R * lane + k;
+        if (i >= bl.start[b] && i < bl.start[b + 1]) part += v[k];
+    }
+    return warp_sum(part);
+}
+
+// This lane's sigma, z and rgb from the stage, and the z of the sample after its
+// block (a pair of samples is wholly inside the ray or wholly past its end).
+template <int R>
+__device__ __forceinline__ void load_blk(const RayCtx& c, const float* rgb, int i0, float (&sg)[R], float (&zz)[R],
+                                         float (&c0)[R], float (&c1)[R], float (&c2)[R], float& zlast) {
+#pragma unroll
+    for (int k = 0; k < R; k += 2) {
+        const int i = i0 + k;
+        float2 s2 = make_float2(0.f, 0.f), z2 = s2, r0 = s2, r1 = s2, r2 = s2;
+        if (i < c.s) {
+            s2 = *reinterpret_cast<const float2*>(c.sigma + i);
+            z2 = *reinterpret_cast<const float2*>(c.z + i);
+            if (rgb) {
+                const float2* pr = reinterpret_cast<const float2*>(rgb + 3 * i);
+                r0 = pr[0];
+                r1 = pr[1];
+                r2 = pr[2];
+            }
+        }
+        sg[k] = s2.x; sg[k + 1] = s2.y;
+        zz[k] = z2.x; zz[k + 1] = z2.y;
+        c0[k] = r0.x; c1[k] = r0.y; c2[k] = r1.x;
+        c0[k + 1] = r1.y; c1[k + 1] = r2.x; c2[k + 1] = r2.y;
+    }
+    zlast = i0 + R < c.s ? c.z[i0 + R] : c.inf_depth;
+}
+
+// delta, e^x, alpha and the scan input of sample k of the block (sample_terms).
+template <int R>
+__device__ __forceinline__ void terms_blk(const RayCtx& c, bool exp_prefix, int i0, const float (&sg)[R],
+                                          const float (&zz)[R], float zlast, float (&al)[R], float (&T)[R],
+                                          float (&ex_)[R], float (&dl)[R]) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = i0 + k;
+        al[k] = 0.f;
+        T[k] = exp_prefix ? 0.f : 1.f;
+        ex_[k] = dl[k] = 0.f;
+        if (i < c.s) {
+            const float zn = k + 1 < R ? (i + 1 < c.s ? zz[k + 1] : c.inf_depth) : zlast;
+            const float delta = (zn - zz[k]) * c.dnorm;
+            float x = -sg[k] * delta;
+            x = x * c.ds;
+            const float ex = expf(x);
+            al[k] = 1.f - ex;
+            T[k] = exp_prefix ? sg[k] * delta * c.ds : 1.f - al[k] + 1e-10f;
+            ex_[k] = ex;
+            dl[k] = delta;
+        }
+    }
+}
+
+template <int R, bool LOSS>
+__device__ __forceinline__ void fwd_ray_blk(const srf_composite_args& a, const LossArgs& L, int r, RayCtx c,
+                                            const float* rgb, float* wout) {
+    const int lane = threadIdx.x & 31;
+    const int i0 = R * lane;
+    const bool exp_prefix = (a.flags & SRF_COMPOSITE_EXP_PREFIX) != 0;
+    float sg[R], zz[R], c0[R], c1[R], c2[R], al[R], T[R], ex_[R], dl[R], zlast;
+    load_blk<R>(c, rgb, i0, sg, zz, c0, c1, c2, zlast);
+    terms_blk<R>(c, exp_prefix, i0, sg, zz, zlast, al, T, ex_, dl);
+    if (exp_prefix)
+        exp_scan_blk<R>(T, lane);
+    else
+        scan_blk<R>(T, lane);
+    float cr = 0.f, cg = 0.f, cb = 0.f, acc = 0.f, wz = 0.f, wzn = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (i0 + k < c.s) {
+            const float w = al[k] * T[k];
+            if (rgb) {
+                cr += w * c0[k];
+                cg += w * c1[k];
+                cb += w * c2[k];
+            }
+            acc += w;
+            if (c.ndc) {
+                wzn += w * zz[k];
+                wz += w * depth_from_ndc(zz[k], c.oz, c.dz);
+            } else {
+                wz += w * zz[k];
+            }
+        }
+    }
+    cr = warp_sum(cr); cg = warp_sum(cg); cb = warp_sum(cb);
+    acc = warp_sum(acc); wz = warp_sum(wz); wzn = warp_sum(wzn);
+    const float depth = wz / (acc + kEps);
+    const float depth_ndc = wzn / (acc + kEps);
+    float var = 0.f, var_ndc = 0.f;
+    const int64_t ro = int64_t(r) * c.s;
+    __syncwarp();   // every lane has read its stage rows before the weights overwrite sigma
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = i0 + k;
+        if (i < c.s) {
+            const float w = al[k] * T[k];
+            const float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
+            const float d = zm - depth;
+            var += w * (d * d);
+            if (c.ndc) {
+                const float dn = zz[k] - depth_ndc;
+                var_ndc += w * (dn * dn);
+            }
+            if (a.alpha) a.alpha[ro + i] = al[k];
+            if (a.visibility) a.visibility[ro + i] = T[k];
+            if (a.weights) wout[i] = w;
+        }
+    }
+    var = warp_sum(var);
+    var_ndc = warp_sum(var_ndc);
+    float lray = 0.f;
+    if (LOSS && mc_term(L, r)) {
+        float w[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) w[k] = i0 + k < c.s ? al[k] * T[k] : 0.f;
+        for (int b = 0; b < L.bins.nb; ++b) {
+            const float x = bin_sum_blk<R>(w, L.bins, b, lane) + 1e-3f;
+            lray -= x * logf(x);
+        }
+        lray *= L.mc_scale;
+    }
+    if (lane == 0) {
+        if (white_for(a, r)) {
+            cr = cr + (1.f - acc);
+            cg = cg + (1.f - acc);
+            cb = cb + (1.f - acc);
+        }
+        if (LOSS) {
+            if (L.target_rgb) {
+                const float e0 = cr - L.target_rgb[3 * r], e1 = cg - L.target_rgb[3 * r + 1],
+                            e2 = cb - L.target_rgb[3 * r + 2];
+                lray += L.rgb_scale * (e0 * e0 + e1 * e1 + e2 * e2);
+            }
+            if (depth_term(L, r)) {
+                const float e = depth - L.target_depth[r];
+                lray += L.depth_scale * (L.depth_squared ? e * e : fabsf(e));
+            }
+            atomicAdd(L.loss, lray);
+        }
+        if (a.rgb_map) {
+            a.rgb_map[3 * r] = cr;
+            a.rgb_map[3 * r + 1] = cg;
+            a.rgb_map[3 * r + 2] = cb;
+        }
+        if (a.acc) a.acc[r] = acc;
+        if (a.depth) a.depth[r] = depth;
+        if (a.depth_var) a.depth_var[r] = var;
+        if (c.ndc) {
+            if (a.depth_ndc) a.depth_ndc[r] = depth_ndc;
+            if (a.depth_var_ndc) a.depth_var_ndc[r] = var_ndc;
+        }
+    }
+}
+
+template <int R, bool LOSS>
+__device__ __forceinline__ void bwd_ray_blk(const srf_composite_args& a, const LossArgs& L, int r, RayCtx c,
+                                            const float* rgb, float* dsig_out, float* drgb_out) {
+    const int lane = threadIdx.x & 31;
+    const int i0 = R * lane;
+    const bool exp_prefix = (a.flags & SRF_COMPOSITE_EXP_PREFIX) != 0;
+    const int64_t ro = int64_t(r) * c.s;
+    float sg[R], zz[R], c0[R], c1[R], c2[R], al[R], T[R], ex_[R], dl[R], G[R], zlast;
+    load_blk<R>(c, rgb, i0, sg, zz, c0, c1, c2, zlast);
+    terms_blk<R>(c, exp_prefix, i0, sg, zz, zlast, al, T, ex_, dl);
+#pragma unroll
+    for (int k = 0; k < R; ++k) G[k] = (a.g_weights && i0 + k < c.s) ? a.g_weights[ro + i0 + k] : 0.f;
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    if (a.g_rgb) {
+        g0 = a.g_rgb[3 * r];
+        g1 = a.g_rgb[3 * r + 1];
+        g2 = a.g_rgb[3 * r + 2];
+    }
+    float gacc = a.g_acc ? a.g_acc[r] : 0.f;
+    if (exp_prefix)
+        exp_scan_blk<R>(T, lane);
+    else
+        scan_blk<R>(T, lane);
+    float acc = 0.f, wz = 0.f, wzn = 0.f;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (i0 + k < c.s) {
+            const float w = al[k] * T[k];
+            acc += w;
+            if (c.ndc) {
+                wzn += w * zz[k];
+                wz += w * depth_from_ndc(zz[k], c.oz, c.dz);
+            } else {
+                wz += w * zz[k];
+            }
+        }
+    }
+    acc = warp_sum(acc); wz = warp_sum(wz); wzn = warp_sum(wzn);
+    const float inv = 1.f / (acc + kEps);
+    const float depth = wz / (acc + kEps), depth_ndc = wzn / (acc + kEps);
+    float gd = a.g_depth ? a.g_depth[r] : 0.f;
+    if (LOSS) {
+        if (L.target_rgb) {
+            float cr = 0.f, cg = 0.f, cb = 0.f;
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                if (i0 + k < c.s) {
+                    const float w = al[k] * T[k];
+                    cr += w * c0[k];
+                    cg += w * c1[k];
+                    cb += w * c2[k];
+                }
+            }
+            cr = warp_sum(cr); cg = warp_sum(cg); cb = warp_sum(cb);
+            if (white_for(a, r)) {
+                cr = cr + (1.f - acc);
+                cg = cg + (1.f - acc);
+                cb = cb + (1.f - acc);
+            }
+            const float s2 = 2.f * L.rgb_scale;
+            g0 += s2 * (cr - L.target_rgb[3 * r]);
+            g1 += s2 * (cg - L.target_rgb[3 * r + 1]);
+            g2 += s2 * (cb - L.target_rgb[3 * r + 2]);
+        }
+        if (depth_term(L, r)) {
+            const float e = depth - L.target_depth[r];
+            gd += L.depth_squared ? 2.f * L.depth_scale * e
+                                  : L.depth_scale * (e > 0.f ? 1.f : (e < 0.f ? -1.f : 0.f));
+        }
+        if (mc_term(L, r)) {
+            float w[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) w[k] = i0 + k < c.s ? al[k] * T[k] : 0.f;
+            for (int b = 0; b < L.bins.nb; ++b) {
+                const float x = bin_sum_blk<R>(w, L.bins, b, lane) + 1e-3f;
+                const float gb = -(logf(x) + 1.f) * L.mc_scale;
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    const int i = i0 + k;
+                    if (i >= L.bins.start[b] && i < L.bins.start[b + 1]) G[k] += gb;
+                }
+            }
+        }
+    }
+    if (white_for(a, r)) gacc -= g0 + g1 + g2;
+    const float gv = a.g_depth_var ? a.g_depth_var[r] : 0.f;
+    const float gdn = (c.ndc && a.g_depth_ndc) ? a.g_depth_ndc[r] : 0.f;
+    const float gvn = (c.ndc && a.g_depth_var_ndc) ? a.g_depth_var_ndc[r] : 0.f;
+    float bsum = 0.f, bsum_n = 0.f;
+    if (gv != 0.f || gvn != 0.f) {
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if (i0 + k < c.s) {
+                const float w = al[k] * T[k];
+                const float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
+                bsum += w * (zm - depth);
+                if (c.ndc) bsum_n += w * (zz[k] - depth_ndc);
+            }
+        }
+        bsum = warp_sum(bsum);
+        bsum_n = warp_sum(bsum_n);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const float zm = c.ndc ? depth_from_ndc(zz[k], c.oz, c.dz) : zz[k];
+        float g = c0[k] * g0 + c1[k] * g1 + c2[k] * g2 + gacc + G[k];
+        const float d = zm - depth;
+        g += gd * d * inv + gv * (d * d - 2.f * bsum * d * inv);
+        if (c.ndc) {
+            const float dn = zz[k] - depth_ndc;
+            g += gdn * dn * inv + gvn * (dn * dn - 2.f * bsum_n * dn * inv);
+        }
+        G[k] = g;
+    }
+    __syncwarp();   // every lane has read its stage rows before the gradients overwrite them
+    if (exp_prefix) {
+        // dL/dy_k = G_k e^{-y_k} T_k - sum_{i>k} G_i w_i: suffix sums in the lane, then
+        // over the later lanes
+        float after[R], run = 0.f;
+#pragma unroll
+        for (int k = R - 1; k >= 0; --k) {
+            after[k] = run;
+            if (i0 + k < c.s) run += G[k] * (al[k] * T[k]);
+        }
+        float inc = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float t = __shfl_down_sync(0xffffffffu, inc, o);
+            if (lane + o < 32) inc += t;
+        }
+        float post = __shfl_down_sync(0xffffffffu, inc, 1);
+        if (lane == 31) post = 0.f;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int i = i0 + k;
+            if (i < c.s) {
+                const float w = al[k] * T[k];
+                const float dy = G[k] * ex_[k] * T[k] - (post + after[k]);
+                dsig_out[i] = dy * c.ds * dl[k];
+                if (drgb_out) {
+                    drgb_out[3 * i] = w * g0;
+                    drgb_out[3 * i + 1] = w * g1;
+                    drgb_out[3 * i + 2] = w * g2;
+                }
+            }
+        }
+        return;
+    }
+    // reverse affine scan R_i = G_{i+1} a_{i+1} + p_{i+1} R_{i+1}, R_{S-1} = 0: sample
+    // i's map x -> A_i + B_i x; a lane composes its block's maps, a suffix scan over
+    // the lanes gives each block the R after it, and the lane then walks back.
+    float ga[R], pp[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const bool in = i0 + k < c.s;
+        ga[k] = in ? G[k] * al[k] : 0.f;
+        pp[k] = in ? 1.f - al[k] + 1e-10f : 1.f;
+    }
+    const float ga_n = __shfl_down_sync(0xffffffffu, ga[0], 1);   // the next lane's first sample
+    const float p_n = __shfl_down_sync(0xffffffffu, pp[0], 1);
+    float A[R], B[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int i = i0 + k;
+        const bool has_next = i < c.s && i + 1 < c.s;
+        A[k] = has_next ? (k + 1 < R ? ga[k + 1] : ga_n) : 0.f;
+        B[k] = has_next ? (k + 1 < R ? pp[k + 1] : p_n) : 0.f;
+    }
+    float FA = 0.f, FB = 1.f;   // this block's composed map
+#pragma unroll
+    for (int k = R - 1; k >= 0; --k) {
+        FA = A[k] + B[k] * FA;
+        FB = B[k] * FB;
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float A2 = __shfl_down_sync(0xffffffffu, FA, o);
+        const float B2 = __shfl_down_sync(0xffffffffu, FB, o);
+        if (lane + o < 32) {
+            FA = FA + FB * A2;
+            FB = FB * B2;
+        }
+    }
+    float Rv = __shfl_down_sync(0xffffffffu, FA, 1);   // R of the first sample after this block
+    if (lane == 31) Rv = 0.f;
+#pragma unroll
+    for (int k = R - 1; k >= 0; --k) {
+        Rv = A[k] + B[k] * Rv;
+        const int i = i0 + k;
+        if (i < c.s) {
+            const float dalpha = T[k] * (G[k] - Rv);
+            float dx = -dalpha * ex_[k];
+            dx = dx * c.ds;
+            dsig_out[i] = -dx * dl[k];
+            if (drgb_out) {
+                const float w = al[k] * T[k];
+                drgb_out[3 * i] = w * g0;
+                drgb_out[3 * i + 1] = w * g1;
+                drgb_out[3 * i + 2] = w * g2;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Staged variants: persistent warps, each owning rays r, r + W, r + 2W, ...
 // (W warps in the grid).  Lane 0 of a warp copies the next ray's sigma, z and
 // rgb (contiguous per ray) into the warp's other shared-memory stage with bulk
 // asynchronous copies (cp.async.bulk, completion counted on an mbarrier) while
-// the warp composites the current ray from shared memory, so every warp keeps
-// one ray's bytes in flight independently of its registers.  Needs S % 4 == 0
-// and 16-byte aligned sigma / z / rgb (the bulk copies move 16-byte multiples).
-// A wait that runs out (4 s) raises the device flag and ends the warp.
+// the warp composites the current ray from shared memory (the blocked bodies
+// above), so every warp keeps one ray's bytes in flight independently of its
+// registers; the ray's per-sample outputs leave the stage by bulk copies too.
+// Needs S % 4 == 0 and 16-byte aligned per-sample inputs and outputs (the bulk
+// copies move 16-byte multiples).  A wait that runs out (4 s) raises the device
+// flag and ends the warp.
 // ---------------------------------------------------------------------------
 
 constexpr int kStagedWarps = 8;
+constexpr int kStages = 2;   // rays per warp in shared memory: one composited, the rest in flight
 
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      tc::smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+                 : "memory");
+}
+
+// Shared -> global bulk copy (bulk async group of the issuing thread).
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(tc::smem_u32(src)),
+                 "r"(bytes)
                  : "memory");
 }
 
@@ -790,48 +1224,73 @@ __device__ __forceinline__ void stage_ray(const srf_composite_args& a, int r, fl
 }
 
 template <int R, bool LOSS, bool BWD>
-__global__ void __launch_bounds__(kStagedWarps * 32) composite_staged_kernel(srf_composite_args a, LossArgs L,
-                                                                              int* flag) {
+__global__ void __launch_bounds__(kStagedWarps * 32, 3) composite_staged_kernel(srf_composite_args a, LossArgs L,
+                                                                                 int* flag) {
     extern __shared__ __align__(128) float smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s = a.n_samples;
-    float* mine = smem + size_t(warp) * 2 * staged_floats(s);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + size_t(kStagedWarps) * 2 * staged_floats(s)) + 2 * warp;
+    float* mine = smem + size_t(warp) * kStages * staged_floats(s);
+    uint64_t* bars =
+        reinterpret_cast<uint64_t*>(smem + size_t(kStagedWarps) * kStages * staged_floats(s)) + kStages * warp;
     const int stride = gridDim.x * kStagedWarps;
-    int r = blockIdx.x * kStagedWarps + warp;
+    const int r0 = blockIdx.x * kStagedWarps + warp;
     if (lane == 0) {
-        tc::mbar_init(&bars[0], 1);
-        tc::mbar_init(&bars[1], 1);
+        for (int i = 0; i < kStages; ++i) tc::mbar_init(&bars[i], 1);
         tc::fence_barrier_init();
     }
     __syncwarp();
-    if (r < a.n_rays && lane == 0) stage_ray(a, r, mine, &bars[0]);
-    uint32_t phase0 = 0u, phase1 = 0u;   // mbarrier phases of the two stages
-    for (int k = 0; r < a.n_rays; ++k, r += stride) {
-        const int cur = k & 1;
+    // the first kStages - 1 rays go out before the loop; iteration k prefetches ray
+    // k + kStages - 1 into the stage that ray k - 1 used
+    if (lane == 0)
+        for (int i = 0; i + 1 < kStages; ++i)
+            if (r0 + i * stride < a.n_rays) stage_ray(a, r0 + i * stride, mine + i * staged_floats(s), &bars[i]);
+    uint32_t phases = 0u;   // bit i: the mbarrier phase stage i waits for next
+    int k = 0;
+    for (int r = r0; r < a.n_rays; ++k, r += stride) {
+        const int cur = k % kStages;
         float* st = mine + cur * staged_floats(s);
-        // the other stage was consumed in the previous iteration (the warp synced
-        // after it): prefetch the next ray there
-        if (r + stride < a.n_rays && lane == 0) stage_ray(a, r + stride, mine + (cur ^ 1) * staged_floats(s),
-                                                        &bars[cur ^ 1]);
-        if (!tc::mbar_wait(&bars[cur], cur ? phase1 : phase0, nullptr)) {
+        const int ahead = r + (kStages - 1) * stride;
+        if (ahead < a.n_rays && lane == 0) {
+            const int nxt = (k + kStages - 1) % kStages;
+            tc::bulk_wait_read_all();   // the bulk stores of ray k - 1 have read that stage
+            stage_ray(a, ahead, mine + nxt * staged_floats(s), &bars[nxt]);
+        }
+        if (!tc::mbar_wait(&bars[cur], (phases >> cur) & 1u, nullptr)) {
             raise_flag(flag, kFlagTimeout);
             // drain (bounded) whatever is still in flight into this warp's stages
-            tc::mbar_wait(&bars[cur ^ 1], cur ? phase0 : phase1, nullptr);
+            for (int i = 1; i < kStages; ++i) {
+                const int st2 = (k + i) % kStages;
+                if (r + i * stride < a.n_rays) tc::mbar_wait(&bars[st2], (phases >> st2) & 1u, nullptr);
+            }
+            if (lane == 0) tc::bulk_wait_all();
             return;
         }
-        if (cur) phase1 ^= 1u;
-        else phase0 ^= 1u;
+        phases ^= 1u << cur;
         RayCtx c = make_ctx(a, r);
         c.sigma = st;
         c.z = st + s;
         const float* rgb = a.rgb ? st + 2 * s : nullptr;
+        const int64_t ro = int64_t(r) * s;
+        // the per-sample outputs land in this stage (weights / d_sigma over sigma,
+        // d_rgb over rgb) and leave by bulk copies
         if (BWD)
-            bwd_ray<R, LOSS>(a, L, r, c, rgb);
+            bwd_ray_blk<R, LOSS>(a, L, r, c, rgb, st, a.d_rgb ? st + 2 * s : nullptr);
         else
-            fwd_ray<R, LOSS>(a, L, r, c, rgb);
+            fwd_ray_blk<R, LOSS>(a, L, r, c, rgb, st);
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            if (BWD) {
+                bulk_s2g(a.d_sigma + ro, st, uint32_t(s) * 4u);
+                if (a.d_rgb) bulk_s2g(a.d_rgb + ro * 3, st + 2 * s, uint32_t(s) * 12u);
+            } else if (a.weights) {
+                bulk_s2g(a.weights + ro, st, uint32_t(s) * 4u);
+            }
+            tc::bulk_commit_group();
+        }
         __syncwarp();
     }
+    if (lane == 0) tc::bulk_wait_all();
 }
 
 // out[r, c] = sum_s w[r, s] x[r, s, c] (one warp per ray); the adjoint gives
@@ -908,14 +1367,15 @@ int launch_reg(K kernel, const srf_composite_args* a, const LossArgs& L, void* s
 
 bool stageable(const srf_composite_args* a) {
     auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
-    return (a->n_samples & 3) == 0 && al16(a->sigma) && al16(a->z) && (!a->rgb || al16(a->rgb));
+    return (a->n_samples & 3) == 0 && al16(a->sigma) && al16(a->z) && (!a->rgb || al16(a->rgb)) &&
+           (!a->weights || al16(a->weights)) && (!a->d_sigma || al16(a->d_sigma)) && (!a->d_rgb || al16(a->d_rgb));
 }
 
 template <int R, bool LOSS, bool BWD>
 int launch_staged(const srf_composite_args* a, const LossArgs& L, void* stream) {
     auto kernel = composite_staged_kernel<R, LOSS, BWD>;
-    const size_t smem = size_t(kStagedWarps) * 2 * staged_floats(a->n_samples) * sizeof(float) +
-                        size_t(kStagedWarps) * 2 * sizeof(uint64_t);
+    const size_t smem = size_t(kStagedWarps) * kStages * staged_floats(a->n_samples) * sizeof(float) +
+                        size_t(kStagedWarps) * kStages * sizeof(uint64_t);
     static int configured = 0;   // per instantiation: the largest shared-memory size set so far
     if (int(smem) > configured) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));

@@ -22,6 +22,22 @@ def to_channels_last(t):
     return t.contiguous(memory_format=torch.channels_last)
 
 
+def zeros_like_all(tensors):
+    """Zero tensors shaped, strided (channels-last included) and typed like
+    ``tensors``, carved from one zero-filled buffer: one fill launch instead of one
+    per tensor.  Each view starts on a 16-byte boundary."""
+    if not tensors:
+        return []
+    spans = []
+    total = 0
+    for t in tensors:
+        n = t.numel()
+        spans.append(total)
+        total += (n + 3) // 4 * 4
+    flat = torch.zeros(max(total, 1), dtype=tensors[0].dtype, device=tensors[0].device)
+    return [flat.as_strided(t.shape, t.stride(), off) for t, off in zip(tensors, spans)]
+
+
 def _is_cl(t):
     return t.dim() == 4 and t.is_contiguous(memory_format=torch.channels_last)
 
@@ -90,7 +106,7 @@ class _VmFunction(torch.autograd.Function):
     def backward(ctx, dout):
         pts, *tensors = ctx.saved_tensors
         planes, lines = tensors[:3], tensors[3:]
-        grads = [torch.zeros_like(x) for x in tensors]
+        grads = zeros_like_all(tensors)
         g = _grid_struct(ctx.res, planes, lines)
         gg = _grid_struct(ctx.res, grads[:3], grads[3:])
         dout = dout.contiguous()
@@ -139,7 +155,7 @@ class _CpFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, dout):
         pts, *lines = ctx.saved_tensors
-        grads = [torch.zeros_like(x) for x in lines]
+        grads = zeros_like_all(lines)
         g, gg = _cp_struct(ctx.res, lines), _cp_struct(ctx.res, grads)
         name = 'srf_cp_density_backward' if ctx.kind == 'density' else 'srf_cp_color_backward'
         call(name, ctypes.byref(gg), ctypes.byref(g), _ptr(pts), pts.shape[0], _ptr(dout.contiguous()), _stream())
@@ -376,7 +392,7 @@ class _RendererTcFunction(torch.autograd.Function):
     def backward(ctx, drgb):
         (feats,) = ctx.saved_tensors
         drgb = drgb.contiguous()
-        grads = [torch.zeros_like(p) for p in ctx.params]
+        grads = zeros_like_all(ctx.params)
         d_feats = torch.empty_like(feats)
         if ctx.scaler is not None:
             _lib.call('srf_loss_scaler_fit', F._ptr(ctx.scaler), F._ptr(drgb), drgb.numel(), None, 0, 1024.0,

@@ -258,13 +258,16 @@ def test_composite_exp_prefix_rejects_long_rays():
 
 @pytest.mark.parametrize('s', [64, 192, 256, 100, 4])
 @pytest.mark.parametrize('flags', [0, 1, 2, 4, 6])
-def test_composite_staged_equals_register_kernel(s, flags):
+def test_composite_staged_matches_register_kernel(s, flags):
     """Rays of a multiple of 4 samples with 16-byte aligned inputs run the staged
     kernels (each warp's next ray copied to shared memory by bulk asynchronous
-    copies while it composites the current one); the same inputs 4 bytes off
-    16-byte alignment run the register kernels that read global memory.  Both
-    compute the same arithmetic in the same order: outputs and adjoints are
-    bitwise equal.  flags: 1 NDC, 2 white background, 4 exp-prefix transmittance."""
+    copies while it composites the current one, lane j owning contiguous samples);
+    the same inputs 4 bytes off 16-byte alignment run the register kernels that
+    read global memory (lane j owning samples j, j + 32, ...).  Per sample the
+    arithmetic is the same; the scans and sums group their terms differently, so
+    the outputs and adjoints agree to float32 rounding: 1e-5 relative plus 1e-6 of
+    the output's largest magnitude (the adjoints' differences G - R cancel).
+    flags: 1 NDC, 2 white background, 4 exp-prefix transmittance."""
     import ctypes
     from simple_rf_gb300 import _lib
     from simple_rf_gb300.functional import _stream
@@ -322,7 +325,8 @@ def test_composite_staged_equals_register_kernel(s, flags):
 
     staged, plain = run(False), run(True)
     for k in staged:
-        assert torch.equal(staged[k], plain[k]), k
+        scale = float(plain[k].abs().max()) if plain[k].numel() else 0.0
+        torch.testing.assert_close(staged[k], plain[k], rtol=1e-5, atol=1e-6 * max(scale, 1e-30), msg=k)
     import ctypes as _c
     fl = _c.c_int(0)
     _lib_mod = __import__('simple_rf_gb300._lib', fromlist=['check'])
