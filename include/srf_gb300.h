@@ -319,6 +319,21 @@ int srf_vm_color_forward(const srf_vm_grid* grid, const float* pts, int64_t n_pt
                          void* stream);
 int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
                           int64_t n_pts, const float* d_features, void* stream);
+/* Deterministic forms of the two adjoints: the scatter-add's FP32 atomics sum in
+ * an order that varies from run to run; these round every contribution once to a
+ * 64-bit fixed-point integer (a power-of-two scale S from the largest |d_features|
+ * and |grid value| and the point count, so that no partial sum leaves 63 bits),
+ * add them with integer atomics, whose sums are independent of order, and add
+ * acc / S into grad_grid: bitwise reproducible, each contribution exact to
+ * n max|d| max|grid| 2^-63.  workspace: srf_vm_backward_fixed_workspace_size(grid)
+ * bytes, 16-byte aligned (one int64 per grid element). */
+size_t srf_vm_backward_fixed_workspace_size(const srf_vm_grid* grid);
+int srf_vm_density_backward_fixed(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                  int64_t n_pts, const float* d_features, void* workspace, size_t workspace_bytes,
+                                  void* stream);
+int srf_vm_color_backward_fixed(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                int64_t n_pts, const float* d_features, void* workspace, size_t workspace_bytes,
+                                void* stream);
 
 /* CP decomposition (CpDecomposedTensor, src/models/SimpleTensoRF09.py:964-1123): only
  * grid->lines are used (planes ignored), line i along world axis vector_axes[i] =

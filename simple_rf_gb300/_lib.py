@@ -113,6 +113,11 @@ _SIGS = {
     'srf_vm_density_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_vm_color_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_vm_color_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
+    'srf_vm_backward_fixed_workspace_size': (ctypes.c_size_t, [ctypes.POINTER(VmGrid)]),
+    'srf_vm_density_backward_fixed': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P,
+                                              ctypes.c_size_t, P]),
+    'srf_vm_color_backward_fixed': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P,
+                                            ctypes.c_size_t, P]),
     'srf_cp_density_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_cp_density_backward': (c_int, [ctypes.POINTER(VmGrid), ctypes.POINTER(VmGrid), P, c_int64, P, P]),
     'srf_cp_color_forward': (c_int, [ctypes.POINTER(VmGrid), P, c_int64, P, P]),

@@ -169,6 +169,8 @@ def main(argv=None):
                     help='time the FP16 renderer alone (forward + backward) on this many surface samples')
     ap.add_argument('--forward-only', action='store_true', help='with --renderer-rows: the forward alone')
     ap.add_argument('--adjoint', default='tc', choices=['tc', 'simt'], help='with --renderer-rows: basis adjoint')
+    ap.add_argument('--deterministic', action='store_true',
+                    help='VM grid adjoints through the fixed-point (bitwise reproducible) scatter-add')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
@@ -181,6 +183,9 @@ def main(argv=None):
         print(json.dumps({'workload': 'tensorf_vm_train_step_ray_batch_sweep_300^3+75^3',
                           'sweep': ray_batch_sweep(dev)}))
         return
+    if args.deterministic:
+        from . import tensorf as T
+        T.set_deterministic_scatter(True)
     models = make_models(dev, precision=args.precision)
     step = TensorfTrainStep(models) if args.eager else TensorfGraphStep(models, args.rays)
     batches = [synthetic_rays(args.rays, 10 + i, dev) for i in range(4)]
@@ -207,6 +212,7 @@ def main(argv=None):
         launches, samples, loss = step.launches_per_step, step.sample_counts(), step.loss
     print(json.dumps({'workload': f'tensorf_vm_train_step_{args.rays}rays_300^3+75^3', 'rays': args.rays,
                       'precision': args.precision, 'cuda_graph': not args.eager,
+                      'deterministic_scatter': args.deterministic,
                       'ms_per_step': round(ms, 4), 'rays_per_s': round(args.rays / ms * 1e3, 1),
                       'samples_per_step': {m.name: c for m, c in zip(models, samples)},
                       'gpu_launches_per_step': launches, 'loss': float(loss.item())}))

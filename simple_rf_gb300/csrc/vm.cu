@@ -16,6 +16,8 @@ namespace {
 
 __constant__ int kMatrixAxes[3][2] = {{0, 1}, {0, 2}, {1, 2}};   // SimpleTensoRF09.py:1131
 __constant__ int kVectorAxes[3] = {2, 1, 0};                      // SimpleTensoRF09.py:1132
+constexpr int kMatrixAxesHost[3][2] = {{0, 1}, {0, 2}, {1, 2}};   // the same axes for host code
+constexpr int kVectorAxesHost[3] = {2, 1, 0};
 
 // Bilinear taps of torch's CPU grid sampler (align_corners=True, zeros padding):
 // ix = (x + 1) * ((W - 1) / 2); weights from the fractional parts.
@@ -672,6 +674,154 @@ __global__ void alpha_grid_kernel(srf_vm_grid g, Box box, const float* __restric
     alpha[t] = fminf(fmaxf(a, 0.f), 1.f);
 }
 
+// ---------------------------------------------------------------------------
+// Deterministic scatter-add adjoint: every contribution w_c d line (or plane)
+// value is rounded once to a 64-bit fixed-point integer with a power-of-two
+// scale S and added with integer atomics, whose sums do not depend on the order
+// of the additions; a last pass adds acc / S into the FP32 gradients.  With B the
+// largest |d| times the largest |grid value| (bilinear weights are at most 1 and
+// sum to 1) and at most n contributions per node (a point adds to each of its
+// corners once), S = 2^floor(log2(2^62 / (n B))) keeps every partial sum inside
+// 63 bits; each contribution is exact to 1 / (2 S) = n B 2^-63.
+// Workspace: one int64 per grid element (planes then lines), then the scale
+// (a double) and the two maxima (floats, as ordered integers).
+// ---------------------------------------------------------------------------
+struct FixedLayout {
+    int64_t off[7];    // accumulator offsets of planes 0..2, lines 0..2, and the total
+    size_t bytes;      // accumulators + scale + maxima
+};
+
+__host__ __device__ inline float* fixed_array(const srf_vm_grid& g, int k) {
+    return k < 3 ? g.planes[k] : g.lines[k - 3];
+}
+
+FixedLayout fixed_layout(const srf_vm_grid& g) {
+    FixedLayout L{};
+    int64_t o = 0;
+    for (int k = 0; k < 6; ++k) {
+        L.off[k] = o;
+        const int i = k % 3;
+        o += k < 3 ? int64_t(g.res[kMatrixAxesHost[i][1]]) * g.res[kMatrixAxesHost[i][0]] * g.n_comp[i]
+                   : int64_t(g.res[kVectorAxesHost[i]]) * g.n_comp[i];
+    }
+    L.off[6] = o;
+    L.bytes = size_t(o) * 8 + 16;
+    return L;
+}
+
+// maxima[0] = max |a| over na values, maxima[1] = max |grid value| (as float bits;
+// non-negative floats order like their bit patterns)
+__global__ void fixed_absmax_kernel(const float* __restrict__ a, int64_t na, srf_vm_grid g, FixedLayout L,
+                                    unsigned int* maxima) {
+    float ma = 0.f, mg = 0.f;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < na; i += stride) ma = fmaxf(ma, fabsf(a[i]));
+    for (int k = 0; k < 6; ++k) {
+        const float* src = fixed_array(g, k);
+        const int64_t cnt = L.off[k + 1] - L.off[k];
+        for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < cnt; i += stride)
+            mg = fmaxf(mg, fabsf(src[i]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mg = fmaxf(mg, __shfl_xor_sync(0xffffffffu, mg, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(maxima, __float_as_uint(ma));
+        atomicMax(maxima + 1, __float_as_uint(mg));
+    }
+}
+
+__global__ void fixed_scale_kernel(const unsigned int* maxima, int64_t n, double* scale) {
+    const double b = double(__uint_as_float(maxima[0])) * double(__uint_as_float(maxima[1]));
+    const double bound = b * double(n > 0 ? n : 1);
+    // the largest power of two S with S * bound <= 2^62 (1 for an all-zero bound)
+    int e = 0;
+    if (bound > 0.0 && isfinite(bound)) {
+        frexp(bound, &e);            // bound < 2^e
+        e = 62 - e;
+    }
+    *scale = ldexp(1.0, e);
+}
+
+__device__ __forceinline__ void fixed_add(int64_t* acc, float v, double scale) {
+    if (v != 0.f)
+        atomicAdd(reinterpret_cast<unsigned long long*>(acc), (unsigned long long)llrint(double(v) * scale));
+}
+
+__global__ void vm_bwd_fixed_kernel(srf_vm_grid g, const float* __restrict__ pts, int64_t n,
+                                    const float* __restrict__ dfeat, int ld, int per_component, FixedLayout L,
+                                    int64_t* acc, const double* scale_dev) {
+    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const double scale = *scale_dev;
+    const float* q = pts + 3 * p;
+    const float ds = per_component ? 0.f : dfeat[p];
+    if (!per_component && ds == 0.f) return;
+    int off = 0;
+    for (int i = 0; i < 3; ++i) {
+        Taps pt, lt;
+        plane_taps(g, i, q, pt, lt);
+        const int R = g.n_comp[i];
+        const float* pl = g.planes[i];
+        const float* ln = g.lines[i];
+        int64_t* apl = acc + L.off[i];
+        int64_t* aln = acc + L.off[3 + i];
+        for (int r = 0; r < R; ++r) {
+            float pv = 0.f, lv = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) pv += pl[int64_t(pt.idx[c]) * R + r] * pt.w[c];
+                if (lt.idx[c] >= 0) lv += ln[int64_t(lt.idx[c]) * R + r] * lt.w[c];
+            }
+            const float d = per_component ? dfeat[p * ld + off + r] : ds;
+            const float dp = d * lv, dl = d * pv;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (pt.idx[c] >= 0) fixed_add(apl + int64_t(pt.idx[c]) * R + r, dp * pt.w[c], scale);
+                if (lt.idx[c] >= 0) fixed_add(aln + int64_t(lt.idx[c]) * R + r, dl * lt.w[c], scale);
+            }
+        }
+        off += R;
+    }
+}
+
+// grad += acc / S over every grid element
+__global__ void fixed_to_grad_kernel(srf_vm_grid gg, FixedLayout L, const int64_t* __restrict__ acc,
+                                     const double* scale_dev) {
+    const double inv = 1.0 / *scale_dev;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < L.off[6]; e += stride) {
+        int k = 0;
+        while (k < 5 && e >= L.off[k + 1]) ++k;
+        fixed_array(gg, k)[e - L.off[k]] += float(double(acc[e]) * inv);
+    }
+}
+
+int vm_bwd_fixed(const srf_vm_grid& gg, const srf_vm_grid& g, const float* pts, int64_t n, const float* dfeat,
+                 int ld, int per_component, void* ws, size_t ws_bytes, cudaStream_t s) {
+    const FixedLayout L = fixed_layout(g);
+    if (!ws || ws_bytes < L.bytes) return SRF_ERR_WORKSPACE;
+    if ((reinterpret_cast<uintptr_t>(ws) & 15u) != 0) return SRF_ERR_ALIGN;
+    int64_t* acc = static_cast<int64_t*>(ws);
+    double* scale = reinterpret_cast<double*>(acc + L.off[6]);
+    unsigned int* maxima = reinterpret_cast<unsigned int*>(scale + 1);
+    cudaError_t e = cudaMemsetAsync(ws, 0, L.bytes, s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return SRF_ERR_CUDA;
+    }
+    fixed_absmax_kernel<<<grid_1d(1 << 20, 256), 256, 0, s>>>(dfeat, n * (per_component ? ld : 1), g, L, maxima);
+    if (int st = launch_status()) return st;
+    fixed_scale_kernel<<<1, 1, 0, s>>>(maxima, n, scale);
+    if (int st = launch_status()) return st;
+    vm_bwd_fixed_kernel<<<grid_1d(n, 128), 128, 0, s>>>(g, pts, n, dfeat, ld, per_component, L, acc, scale);
+    if (int st = launch_status()) return st;
+    const int64_t conv = L.off[6] < (int64_t(1) << 22) ? L.off[6] : (int64_t(1) << 22);
+    if (conv > 0) fixed_to_grad_kernel<<<grid_1d(conv, 256), 256, 0, s>>>(gg, L, acc, scale);
+    return launch_status();
+}
+
 int check_grid(const srf_vm_grid* g, bool need) {
     if (!g) return SRF_ERR_NULL;
     for (int i = 0; i < 3; ++i) {
@@ -774,6 +924,41 @@ extern "C" int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_
     }
     vm_bwd_kernel<<<grid_1d(n_pts, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts, n_pts, d_features, ld, 1);
     return launch_status();
+}
+
+extern "C" size_t srf_vm_backward_fixed_workspace_size(const srf_vm_grid* grid) {
+    if (check_grid(grid, false)) return 0;
+    return fixed_layout(*grid).bytes;
+}
+
+// The deterministic adjoints (fixed-point integer accumulation): same arguments as
+// srf_vm_density_backward / srf_vm_color_backward plus the workspace.
+extern "C" int srf_vm_density_backward_fixed(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                             int64_t n_pts, const float* d_features, void* workspace,
+                                             size_t workspace_bytes, void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if ((st = check_grid(grad_grid, true))) return st;
+    if (!pts || !d_features) return SRF_ERR_NULL;
+    if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    for (int i = 0; i < 3; ++i)
+        if (grad_grid->n_comp[i] != grid->n_comp[i] || grad_grid->res[i] != grid->res[i]) return SRF_ERR_SHAPE;
+    return vm_bwd_fixed(*grad_grid, *grid, pts, n_pts, d_features, 1, 0, workspace, workspace_bytes, as_stream(stream));
+}
+
+extern "C" int srf_vm_color_backward_fixed(const srf_vm_grid* grad_grid, const srf_vm_grid* grid, const float* pts,
+                                           int64_t n_pts, const float* d_features, void* workspace,
+                                           size_t workspace_bytes, void* stream) {
+    int st = check_grid(grid, true);
+    if (st) return st;
+    if ((st = check_grid(grad_grid, true))) return st;
+    if (!pts || !d_features) return SRF_ERR_NULL;
+    if (n_pts <= 0) return n_pts < 0 ? SRF_ERR_SHAPE : SRF_OK;
+    for (int i = 0; i < 3; ++i)
+        if (grad_grid->n_comp[i] != grid->n_comp[i] || grad_grid->res[i] != grid->res[i]) return SRF_ERR_SHAPE;
+    const int ld = grid->n_comp[0] + grid->n_comp[1] + grid->n_comp[2];
+    return vm_bwd_fixed(*grad_grid, *grid, pts, n_pts, d_features, ld, 1, workspace, workspace_bytes,
+                        as_stream(stream));
 }
 
 extern "C" int srf_tensorf_sample_mask(const float* rays_o, const float* rays_d, const float* z, int n_rays,

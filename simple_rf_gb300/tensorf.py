@@ -22,6 +22,22 @@ def to_channels_last(t):
     return t.contiguous(memory_format=torch.channels_last)
 
 
+_DETERMINISTIC_SCATTER = False
+
+
+def set_deterministic_scatter(on=True):
+    """Route the VM grid adjoints (vm_density / vm_color backward) through the
+    fixed-point scatter-add (srf_vm_*_backward_fixed), whose gradients are bitwise
+    reproducible, instead of the faster FP32 atomics.  Also on whenever
+    torch.use_deterministic_algorithms(True) is in effect."""
+    global _DETERMINISTIC_SCATTER
+    _DETERMINISTIC_SCATTER = bool(on)
+
+
+def deterministic_scatter():
+    return _DETERMINISTIC_SCATTER or torch.are_deterministic_algorithms_enabled()
+
+
 def zeros_like_all(tensors):
     """Zero tensors shaped, strided (channels-last included) and typed like
     ``tensors``, carved from one zero-filled buffer: one fill launch instead of one
@@ -111,7 +127,13 @@ class _VmFunction(torch.autograd.Function):
         gg = _grid_struct(ctx.res, grads[:3], grads[3:])
         dout = dout.contiguous()
         name = 'srf_vm_density_backward' if ctx.kind == 'density' else 'srf_vm_color_backward'
-        call(name, ctypes.byref(gg), ctypes.byref(g), _ptr(pts), pts.shape[0], _ptr(dout), _stream())
+        if deterministic_scatter():
+            nbytes = int(_lib.load().srf_vm_backward_fixed_workspace_size(ctypes.byref(g)))
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=pts.device)
+            call(name + '_fixed', ctypes.byref(gg), ctypes.byref(g), _ptr(pts), pts.shape[0], _ptr(dout), _ptr(ws),
+                 nbytes, _stream())
+        else:
+            call(name, ctypes.byref(gg), ctypes.byref(g), _ptr(pts), pts.shape[0], _ptr(dout), _stream())
         return (None, None, None) + tuple(grads)
 
 

@@ -89,3 +89,66 @@ def test_tensorf_graph_step_replays_reproduce():
     # the updated parameters differ only through the scatter-add's summation order
     assert worst < 1e-5, worst
     print('tensorf: worst relative difference of updated parameters between replays', worst)
+
+
+@pytest.mark.parametrize('kind', ['density', 'color'])
+def test_vm_fixed_point_scatter_is_bitwise_reproducible(kind):
+    """The deterministic VM adjoint (fixed-point integer accumulation) on points
+    crowded onto a few grid cells (thousands of additions per node): two runs give
+    bitwise equal gradients and match the float64 oracle (grid_sample_2d_backward)
+    within 1e-6 relative L2 (each contribution rounded once); the FP32-atomic
+    gradients, whose long sums round at every addition, within 5e-5.  The share of
+    FP32-atomic entries that differ between two runs is reported."""
+    from oracle import tensorf as ot
+    from simple_rf_gb300 import tensorf as T
+    rng = np.random.default_rng(11)
+    res = (40, 44, 48)
+    comps = (16, 16, 16) if kind == 'density' else (48, 48, 48)
+    planes = [(rng.standard_normal((r, res[ot.MATRIX_AXES[i][1]], res[ot.MATRIX_AXES[i][0]])) * 0.1)
+              .astype(np.float32) for i, r in enumerate(comps)]
+    lines = [(rng.standard_normal((r, res[ot.VECTOR_AXES[i]], 1)) * 0.1).astype(np.float32)
+             for i, r in enumerate(comps)]
+    n_pts = 60000
+    p = rng.uniform(-1, 1, (n_pts, 3)).astype(np.float32)
+    crowd = rng.random(n_pts) < 0.7                      # 70% inside one small box
+    p[crowd] = rng.uniform(-0.05, 0.05, (int(crowd.sum()), 3)).astype(np.float32)
+    pts = torch.from_numpy(p).to(DEV)
+    if kind == 'density':
+        gout = rng.standard_normal(n_pts).astype(np.float32)
+    else:
+        gout = rng.standard_normal((n_pts, sum(comps))).astype(np.float32)
+
+    def grads(deterministic):
+        T.set_deterministic_scatter(deterministic)
+        try:
+            grid = T.VmGridTensors.from_numpy(planes, lines, res, DEV)
+            grid.requires_grad_(True)
+            out = T.vm_density(grid, pts) if kind == 'density' else T.vm_color(grid, pts)
+            (out * torch.from_numpy(gout).to(DEV)).sum().backward()
+            torch.cuda.synchronize()
+            return [grid.plane_grad_numpy(i) for i in range(3)] + [grid.line_grad_numpy(i) for i in range(3)]
+        finally:
+            T.set_deterministic_scatter(False)
+
+    f1, f2 = grads(True), grads(True)
+    a1, a2 = grads(False), grads(False)
+    for x, y in zip(f1, f2):
+        assert np.array_equal(x, y)
+    diff = np.mean(np.concatenate([(x != y).ravel() for x, y in zip(a1, a2)]))
+    feats = ot.vm_features(planes, lines, p)
+    off = 0
+    worst = {'fixed': 0.0, 'atomic': 0.0}
+    for i in range(3):
+        m0, m1 = ot.MATRIX_AXES[i]
+        v = ot.VECTOR_AXES[i]
+        pc, lc = feats[i]
+        r = comps[i]
+        d = gout[None, :].astype(np.float64) if kind == 'density' else gout[:, off:off + r].T.astype(np.float64)
+        off += r
+        ref_p = ot.grid_sample_2d_backward(planes[i].shape, p[:, m0], p[:, m1], d * lc, np.float64)
+        ref_l = ot.grid_sample_2d_backward(lines[i].shape, np.zeros_like(p[:, v]), p[:, v], d * pc, np.float64)
+        for tag, gset in (('fixed', f1), ('atomic', a1)):
+            for got, ref in ((gset[i], ref_p), (gset[3 + i], ref_l)):
+                worst[tag] = max(worst[tag], float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    print(kind, 'rel-L2 vs float64', worst, 'share of FP32-atomic entries differing between runs', diff)
+    assert worst['fixed'] < 1e-6 and worst['atomic'] < 5e-5, worst
