@@ -366,8 +366,6 @@ def rgb_agreement(step_cls, batch, dev):
             out[f'rgb_max_abs_{prec}_vs_fp32{label}'] = round(float(ok.max().item()) if ok.numel() else 0.0, 6)
             out[f'rays_with_last_sample_flip_{prec}{label}'] = int(flip.sum().item())
     out['rays'] = N_RAYS
-    out['against_fp64_oracle'] = ('tests/test_gpu_headline_accuracy.py: the headline step at 4096 rays against the '
-                                  'float64 oracle (rgb max-abs over all rays, flip count, gradient rel-L2)')
     torch.cuda.empty_cache()
     return out
 
@@ -510,6 +508,40 @@ class OracleStep:
         for net, p in self.p.items():
             for k in p:
                 p[k] -= np.float32(5e-4) * np.sign(total[net][k])
+
+
+def oracle_accuracy(step_cls, batch_fn, dev, n_check=256):
+    """Part of the CPU-baseline leg (the oracle runs on the host here): the headline
+    step's rendered rgb on the first n_check rays of a batch against the float64
+    oracle with the same nets, rays and uniforms, the fine pass on the depths the
+    GPU sampled.  A ray whose last-sample raw sigma is zero on one side and
+    positive on the other (the 1e10 last delta) is a flip; the max-abs error is
+    reported over all rays and over the rays without a flip."""
+    import numpy as np
+    import torch
+    from oracle import nerf as on
+    step = step_cls(N_RAYS, N_COARSE, N_FINE, precision=HEADLINE, device=dev, seed=7)
+    batch = batch_fn(N_RAYS, N_COARSE, N_FINE, seed=8, device=dev)
+    step.set_batch(*batch)
+    params = {tag: {k: v.double().cpu().numpy() for k, v in net.state_dict().items()} for tag, net in step.nets.items()}
+    step.step()
+    torch.cuda.synchronize(dev)
+    out = {k: v.detach().cpu().numpy() for k, v in step.outputs().items()}
+    o, d, _, _, u_c, u_f = [x[:n_check].cpu().numpy().astype(np.float64) for x in batch]
+    spec = on.MlpSpec()
+    ref, _ = on.render_rays(params['coarse'], params['fine'], spec, spec, o, d, 2.0, 6.0, N_COARSE, N_FINE, u_c, u_f,
+                            white_bkgd=True, z_fine=out['z_fine'][:n_check].astype(np.float64), pts_fp32=True)
+    flip = np.zeros(n_check, bool)
+    for tag in ('coarse', 'fine'):
+        flip |= (out[f'sigma_{tag}'].reshape(N_RAYS, -1)[:n_check, -1] > 0) != (ref[f'raw_sigma_{tag}'][:, -1, 0] > 0)
+    res = {'rays': n_check, 'precision': HEADLINE, 'rays_with_last_sample_flip': int(flip.sum())}
+    for tag in ('coarse', 'fine'):
+        err = np.abs(out[f'rgb_map_{tag}'][:n_check] - ref[f'rgb_{tag}']).max(1)
+        res[f'rgb_max_abs_{tag}_all_rays'] = round(float(err.max()), 7)
+        res[f'rgb_max_abs_{tag}_no_flip'] = round(float(err[~flip].max()) if (~flip).any() else 0.0, 7)
+    del step
+    torch.cuda.empty_cache()
+    return res
 
 
 def cpu_baseline(sample_rays=128, min_seconds=10.0):
@@ -713,6 +745,7 @@ def run_ours(args):
     }
     if ws == 1:
         line['cpu_baseline'] = cpu_baseline()
+        line['accuracy']['against_fp64_oracle'] = oracle_accuracy(NerfTrainStep, synthetic_batch, dev)
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
