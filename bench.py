@@ -510,6 +510,124 @@ class OracleStep:
                 p[k] -= np.float32(5e-4) * np.sign(total[net][k])
 
 
+def torch_cuda_context(dev, batch, steps=5, warmup=2):
+    """Context only, not a baseline of the ratio: the config-2 step as the
+    reference runs it on a CUDA device, restated with plain torch FP32 ops (no
+    TF32) and autograd: PE (SimpleNeRF17.py:581-613), the 8x256 trunk with the
+    skip after layer 4, sigma and feature heads, the 128-wide view layer and the
+    sigmoid rgb head (:616-785), exclusive-cumprod compositing (:486-539),
+    sample_pdf with searchsorted (:384-417) and the fine pass on the sorted merge
+    (:360-371), the two MSE terms + 0.1 L1 depth on 25% of the rays, Adam.  The
+    whole batch goes through each net at once (the reference's netchunk
+    splitting would only add launches).  Returns rays/s."""
+    import torch
+    import torch.nn.functional as tF
+    prev_tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    g = torch.Generator(device='cpu').manual_seed(0)
+
+    def linear(i, o):
+        w = torch.empty(o, i)
+        torch.nn.init.xavier_uniform_(w, generator=g)
+        return [w.to(dev).requires_grad_(True), torch.zeros(o, device=dev, requires_grad=True)]
+
+    def make_net():
+        trunk = [linear(63, 256)] + [linear(256 + (63 if i == 4 else 0), 256) for i in range(7)]
+        return {'trunk': trunk, 'sigma': linear(256, 1), 'feature': linear(256, 256), 'view': linear(256 + 27, 128),
+                'rgb': linear(128, 3)}
+
+    def params(net):
+        return [t for k in ('trunk',) for wb in net[k] for t in wb] + \
+            [t for k in ('sigma', 'feature', 'view', 'rgb') for t in net[k]]
+
+    def pe(x, degree):
+        parts = [x]
+        for k in range(degree):
+            parts += [torch.sin(x * 2.0 ** k), torch.cos(x * 2.0 ** k)]
+        return torch.cat(parts, -1)
+
+    def run_net(net, pts, dirs):
+        ep, ev = pe(pts, 10), pe(dirs, 4)
+        h = ep
+        for i, (w, b) in enumerate(net['trunk']):
+            h = tF.relu(tF.linear(h, w, b))
+            if i == 4:
+                h = torch.cat([ep, h], -1)
+        sigma = tF.relu(tF.linear(h, *net['sigma']))[..., 0]
+        hv = tF.relu(tF.linear(torch.cat([tF.linear(h, *net['feature']), ev], -1), *net['view']))
+        return sigma, torch.sigmoid(tF.linear(hv, *net['rgb']))
+
+    def composite(sigma, rgb, z, d):
+        n = z.shape[0]
+        dist = torch.cat([z[:, 1:] - z[:, :-1], torch.full((n, 1), 1e10, device=dev)], -1) * d.norm(dim=-1,
+                                                                                                    keepdim=True)
+        alpha = 1.0 - torch.exp(-sigma * dist)
+        trans = torch.cumprod(torch.cat([torch.ones(n, 1, device=dev), 1.0 - alpha + 1e-10], -1), -1)[:, :-1]
+        w = alpha * trans
+        acc = w.sum(-1)
+        return (w[..., None] * rgb).sum(-2) + (1.0 - acc[:, None]), (w * z).sum(-1) / (acc + 1e-6), w
+
+    def fine_depths(z, w, u):
+        mids = 0.5 * (z[:, 1:] + z[:, :-1])
+        wt = w[:, 1:-1].detach() + 1e-5
+        cdf = torch.cumsum(wt / wt.sum(-1, keepdim=True), -1)
+        cdf = torch.cat([torch.zeros_like(cdf[:, :1]), cdf], -1)
+        idx = torch.searchsorted(cdf, u.contiguous(), right=True)
+        lo, hi = (idx - 1).clamp_min(0), idx.clamp_max(cdf.shape[-1] - 1)
+        c0, c1 = cdf.gather(1, lo), cdf.gather(1, hi)
+        b0, b1 = mids.gather(1, lo), mids.gather(1, hi)
+        den = torch.where(c1 - c0 < 1e-5, torch.ones_like(c0), c1 - c0)
+        zs = b0 + (u - c0) / den * (b1 - b0)
+        return torch.sort(torch.cat([z, zs.detach()], -1), -1).values
+
+    nets = {'coarse': make_net(), 'fine': make_net()}
+    opt = torch.optim.Adam([t for net in nets.values() for t in params(net)], lr=5e-4)
+    o, d, t_rgb, t_depth, u_c, u_f = batch
+    n = o.shape[0]
+    mask = torch.zeros(n, device=dev)
+    mask[:n // 4] = 1
+    near, far = 2.0, 6.0
+    t_lin = torch.linspace(0, 1, N_COARSE, device=dev)
+
+    def step():
+        zl = near * (1 - t_lin) + far * t_lin
+        mids = 0.5 * (zl[1:] + zl[:-1])
+        upper = torch.cat([mids, zl[-1:]])
+        lower = torch.cat([zl[:1], mids])
+        z_c = lower + (upper - lower) * u_c
+        dirs = d / d.norm(dim=-1, keepdim=True)
+        loss = 0.0
+        z = z_c
+        for tag in ('coarse', 'fine'):
+            pts = o[:, None, :] + d[:, None, :] * z[..., None]
+            s = z.shape[1]
+            sigma, rgb = run_net(nets[tag], pts.reshape(-1, 3), dirs[:, None, :].expand(n, s, 3).reshape(-1, 3))
+            rgb_map, depth, w = composite(sigma.view(n, s), rgb.view(n, s, 3), z, d)
+            loss = loss + ((rgb_map - t_rgb) ** 2).mean() + 0.1 * ((depth - t_depth).abs() * mask).sum() / mask.sum()
+            if tag == 'coarse':
+                z = fine_depths(z_c, w, u_f)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    torch.backends.cuda.matmul.allow_tf32 = prev_tf32
+    del nets, opt
+    torch.cuda.empty_cache()
+    return {'value': round(n / ms * 1e3, 1), 'unit': 'rays/s', 'ms_per_step': round(ms, 3), 'steps': steps,
+            'what': 'the reference algorithm as plain torch FP32 ops + autograd + torch.optim.Adam on this GPU '
+                    '(context, not the ratio\'s baseline)'}
+
+
 def oracle_accuracy(step_cls, batch_fn, dev, n_check=256):
     """Part of the CPU-baseline leg (the oracle runs on the host here): the headline
     step's rendered rgb on the first n_check rays of a batch against the float64
@@ -744,6 +862,9 @@ def run_ours(args):
         'kernel_rooflines': kroofs,
     }
     if ws == 1:
+        ctx = torch_cuda_context(dev, pool[0])
+        ctx['headline_speedup'] = round(line['value'] / ctx['value'], 2)
+        line['reference_torch_cuda_fp32'] = ctx
         line['cpu_baseline'] = cpu_baseline()
         line['accuracy']['against_fp64_oracle'] = oracle_accuracy(NerfTrainStep, synthetic_batch, dev)
     print(json.dumps(line), flush=True)
