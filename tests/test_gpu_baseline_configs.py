@@ -9,7 +9,10 @@ workloads (the kernel-level tests cover small and ragged shapes):
   gradients of both nets;
 * TensoRF VM model, 300^3 grid, 16 / 48 components, 27 features, 128-unit
   renderer, 128^3 alpha mask at 15% occupancy, 8192 rays: outputs of all rays
-  and the gradients of every grid and renderer parameter.
+  and the gradients of every grid and renderer parameter;
+* the NDC main + augmented pair step, 4096 rays (FP32 plain against float32,
+  the FP16 step's rgb against float64), and one full 504 x 378 view rendered in
+  chunks of 65,536 rays.
 
 Tolerances: rgb/depth/weights/acc within 1e-5 relative (absolute floor 1e-6 of
 the value range) of the float32 oracle; gradients as in test_gpu_train_step.py
@@ -385,3 +388,106 @@ def test_config4_tensorf_gradients_match_oracle():
         worst = max(worst, rel / bar)
         assert rel < bar, (name, rel, e32)
     print('config 4: worst per-tensor gradient error / bar', worst)
+
+
+def _pair_oracle_forward(params, host, z_fine, dtype, chunk=512):
+    """The oracle's forward of the config-3 pair (NDC, main coarse + fine, the
+    augmented coarse net on the same coarse samples) over ray chunks."""
+    o, d, _, _, u_c, u_f = [np.asarray(x, dtype) for x in host]
+    spec = on.MlpSpec()
+    aspec = on.MlpSpec(points_pe_degree=4, use_view_dirs=False, view_dependent_rgb=False)
+    p = {tag: {k: v.astype(dtype) for k, v in params[tag].items()} for tag in params}
+    aug = 'views_augmentation'
+    parts = []
+    for i in range(0, o.shape[0], chunk):
+        sl = slice(i, min(i + chunk, o.shape[0]))
+        focal = np.full(sl.stop - sl.start, 400.0, dtype)
+        ret, _ = on.render_rays(p['coarse'], p['fine'], spec, spec, o[sl], d[sl], 0.0, 1.0, 64, 128, u_c[sl], u_f[sl],
+                                ndc=dict(h=378, w=504, fx=focal, fy=focal, near=1.0),
+                                aug=[(aug, {'coarse': p[f'{aug}_coarse']}, aspec)],
+                                z_fine=np.asarray(z_fine[sl], dtype), pts_fp32=True)
+        parts.append(ret)
+    n0 = min(chunk, o.shape[0])
+    keys = [k for k, v in parts[0].items() if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == n0]
+    return {k: np.concatenate([r[k] for r in parts], 0) for k in keys}
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'fp16'])
+def test_config3_pair_step_4096_rays_matches_oracle(precision):
+    """The config-3 pair step (NDC main coarse + fine + augmented coarse, 4096
+    rays) against the oracle: FP32 plain rgb / weights / acc within 1e-5 of the
+    float32 oracle (acc with one ulp(1) per sample), the NDC depth within 1e-5 of
+    the float64 reduction of the GPU's own weights; the FP16 step's
+    rgb within 2e-3 max-abs of the float64 oracle.  NDC rays end at z = 1 (no
+    1e10 last delta), so no ray is excluded."""
+    from simple_rf_gb300.train_step import make_step
+    aug = 'views_augmentation'
+    step, batch_fn = make_step('nerf_pair', 4096, precision, DEV, seed=5)
+    batch = batch_fn(6, DEV)
+    step.set_batch(*batch)
+    params = {tag: {k: v.double().cpu().numpy() for k, v in net.state_dict().items()} for tag, net in step.nets.items()}
+    step.step()
+    torch.cuda.synchronize()
+    out = {k: v.detach().cpu().numpy() for k, v in step.outputs().items()}
+    host = [x.cpu().numpy() for x in batch]
+    dtype = np.float32 if precision == 'fp32' else np.float64
+    ref = _pair_oracle_forward(params, host, out['z_fine'], dtype)
+
+    def key(k, tag):
+        k = {'rgb_map': 'rgb'}.get(k, k)
+        return f'{aug}_{k}_coarse' if tag.startswith(aug) else f'{k}_{tag}'
+
+    worst = {}
+    for tag in ('coarse', 'fine', f'{aug}_coarse'):
+        if precision == 'fp32':
+            for k in ('rgb_map', 'weights', 'acc'):
+                r = ref[key(k, tag)]
+                atol = out[f'weights_{tag}'].shape[1] * 2.0 ** -23 if k == 'acc' else \
+                    1e-6 * max(1.0, float(np.abs(r).max()))
+                np.testing.assert_allclose(out[f'{k}_{tag}'], r, rtol=1e-5, atol=atol, err_msg=f'{k}_{tag}')
+            # depth_ndc = sum w z / (acc + 1e-6) divides by acc, whose absolute rounding
+            # (one ulp(1) per sample) is large relative to a small acc: the weights are
+            # compared above, the depth as the float64 reduction of the GPU's weights
+            w = out[f'weights_{tag}'].astype(np.float64)
+            zr = np.sum(w * out[f'z_{tag}'].astype(np.float64), -1) / (np.sum(w, -1) + 1e-6)
+            np.testing.assert_allclose(out[f'depth_ndc_{tag}'], zr, rtol=1e-5, atol=1e-6, err_msg=f'depth_ndc_{tag}')
+        else:
+            worst[tag] = float(np.abs(out[f'rgb_map_{tag}'] - ref[key('rgb_map', tag)]).max())
+            assert worst[tag] < 2e-3, (tag, worst[tag])
+    if worst:
+        print('fp16 pair step, 4096 rays: rgb max-abs vs float64', worst)
+
+
+def test_config5_full_view_render_matches_oracle():
+    """One full config-5 view (504 x 378 = 190,512 NDC rays, focal 400) through the
+    FP32 plain pair renderer in chunks of 65,536 (the last chunk partial): rays at
+    the start, across the first chunk boundary and in the partial last chunk
+    against the float32 oracle (rgb and acc of the three nets within 1e-5
+    relative plus one ulp(1) per sample absolute; the fine pass on the depths the
+    GPU sampled)."""
+    from simple_rf_gb300.render import NerfPairRenderer, pixel_rays, synthetic_views
+    aug = 'views_augmentation'
+    pid, intr, ext = synthetic_views(1, 378, 504, focal=400.0, seed=9, device=DEV)
+    o, d = pixel_rays(pid, intr, ext)
+    n = o.shape[0]
+    r = NerfPairRenderer(65536, 'fp32', DEV, seed=4, graph=False)
+    out = r.render(o, d, keep=('rgb', 'acc', 'z'))
+    torch.cuda.synchronize()
+    assert n == 190512 and out['coarse']['rgb'].shape[0] == n
+    sel = np.concatenate([np.arange(0, 256), np.arange(65536 - 256, 65536 + 256), np.arange(n - 512, n)])
+    params = {tag: {k: v.cpu().numpy() for k, v in net.state_dict().items()} for tag, net in r.nets.items()}
+    spec = on.MlpSpec()
+    aspec = on.MlpSpec(points_pe_degree=4, use_view_dirs=False, view_dependent_rgb=False)
+    focal = np.full(sel.size, 400.0, np.float32)
+    ret, _ = on.render_rays(params['coarse'], params['fine'], spec, spec, o.cpu().numpy()[sel], d.cpu().numpy()[sel],
+                            0.0, 1.0, 64, 128, ndc=dict(h=378, w=504, fx=focal, fy=focal, near=1.0),
+                            aug=[(aug, {'coarse': params[f'{aug}_coarse']}, aspec)],
+                            z_fine=out['fine']['z'].cpu().numpy()[sel])
+    for tag, pre in (('coarse', ''), ('fine', ''), (f'{aug}_coarse', f'{aug}_')):
+        lvl = 'fine' if tag == 'fine' else 'coarse'
+        n_s = out[tag]['z'].shape[1]
+        for k in ('rgb', 'acc'):
+            # rgb = sum w c and acc = sum w: each weight carries an absolute rounding of
+            # up to ulp(1) = 2^-23 (1 - alpha, the transmittance products), colours <= 1
+            np.testing.assert_allclose(out[tag][k].cpu().numpy()[sel], ret[f'{pre}{k}_{lvl}'], rtol=1e-5,
+                                       atol=n_s * 2.0 ** -23, err_msg=f'{k}_{tag}')
