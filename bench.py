@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark of the Simple-NeRF training step (fwd + bwd + Adam) on GB300.
 
-Workload (the spec training configuration): 4096 rays per step,
+Workload (the benchmark's training configuration): 4096 rays per step,
 64 stratified coarse + 128 inverse-CDF fine samples, two 8x256 NeRF MLPs with
 the skip at layer 5 and a 128-wide view branch, white background, loss = rgb MSE
 (coarse + fine) + 0.1 * L1 depth on 25% of the rays, Adam.  Synthetic inputs:
@@ -460,7 +460,7 @@ def time_render(dev, stream):
 class OracleStep:
     """One training step of the reference algorithm's CPU restatement (numpy
     oracle port of SimpleNeRF17's render_rays + the loss + the hand-derived
-    backward + a parameter update) on ``n`` config-2 rays."""
+    backward + a parameter update) on ``n`` rays of the 4096-ray training workload."""
 
     def __init__(self, n, seed=0):
         import numpy as np
@@ -511,7 +511,7 @@ class OracleStep:
 
 
 def torch_cuda_context(dev, batch, steps=5, warmup=2):
-    """Context only, not a baseline of the ratio: the config-2 step as the
+    """Context only, not a baseline of the ratio: the 4096-ray training step as the
     reference runs it on a CUDA device, restated with plain torch FP32 ops (no
     TF32) and autograd: PE (SimpleNeRF17.py:581-613), the 8x256 trunk with the
     skip after layer 4, sigma and feature heads, the 128-wide view layer and the
@@ -678,7 +678,7 @@ def cpu_baseline(sample_rays=128, min_seconds=10.0):
 
 
 def run_reference(args):
-    """The reference arm: whole config-2 steps (4096 rays) of the oracle port on the
+    """The reference arm: whole training steps (4096 rays) of the oracle port on the
     host cores; warm-up steps run 64 rays (they only bring up the BLAS threads)."""
     ws = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))

@@ -500,7 +500,7 @@ int srf_positional_encoding_backward(float* dx, const float* x, const float* dou
 /* Training-step helpers                                                     */
 /* ------------------------------------------------------------------------ */
 
-/* Config-2 style loss on one net's outputs: mean over rays of mean over channels
+/* The training step's loss on one net's outputs: mean over rays of mean over channels
  * of (rgb - target)^2 (MSE14.compute_mse, src/loss_functions/MSE14.py:81-94) plus
  * depth_weight * mean |depth - target_depth| over rays with depth_mask != 0.
  * Adds the loss to *loss_dev (device float) and writes g_rgb (N,3), g_depth (N). */

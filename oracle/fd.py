@@ -19,7 +19,7 @@ from . import nerf as on
 
 def level_loss(params, spec, rays_o, rays_d, z, target_rgb, target_depth, depth_mask, *, white_bkgd=True,
                depth_weight=0.1):
-    """One net's share of the config-2 loss at fixed depths ``z`` (N, S):
+    """One net's share of the training step's loss at fixed depths ``z`` (N, S):
     MSE(rgb, target) (MSE14.py:81-94) + depth_weight * mean L1 depth on the
     depth-supervised rays, rendered as SimpleNeRF17.py:486-539 does.
 

@@ -455,7 +455,7 @@ def composite_backward(cache, g):
 
 
 # ----------------------------------------------------------------------------
-# whole-path drivers (config-1 render, config-2 train step)
+# whole-path drivers (the 1024-ray render, the 4096-ray train step)
 # ----------------------------------------------------------------------------
 
 
@@ -463,7 +463,7 @@ def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n
                 u_coarse=None, u_fine=None, white_bkgd=False, ndc=None, aug=None, z_fine=None, pts_fp32=False):
     """SimpleNeRF17.py:159-328 render_rays for synthetic rays (ray generation patched out).
 
-    ``ndc`` = dict(h, w, fx, fy, near) switches to NDC rays (config 3).  ``aug`` =
+    ``ndc`` = dict(h, w, fx, fy, near) switches to NDC rays (the main + augmented pair).  ``aug`` =
     list of (name, params, spec) augmented coarse nets run on the coarse samples
     (:244-261) and, when they also carry fine params, on the fine samples (:296-313).
     ``z_fine`` (N, Sc+Sf) replaces the inverse-CDF depths (tests use it to check
@@ -527,7 +527,7 @@ def render_rays(params_c, params_f, spec_c, spec_f, rays_o, rays_d, near, far, n
 
 
 def train_loss(ret, target_rgb, target_depth, depth_mask, depth_weight=0.1, nets=('coarse', 'fine')):
-    """Training loss of the config-2 step: per net, MSE(rgb, target) (MSE14.py:81-94
+    """Training loss of the 4096-ray training step: per net, MSE(rgb, target) (MSE14.py:81-94
     form: mean over channels then rays) + depth_weight * mean |depth - target| over
     the depth-supervised rays.  Returns (loss, {output_key: grad})."""
     dt = target_rgb.dtype.type

@@ -1,4 +1,4 @@
-// Training-step helpers: the config-2 loss gradient and a fused Adam update.
+// Training-step helpers: the training step's loss gradient and a fused Adam update.
 #include "srf_common.cuh"
 
 namespace srf {

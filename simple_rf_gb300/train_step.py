@@ -115,8 +115,8 @@ class _Net:
 class NerfTrainStep:
     """Preallocated, graph-capturable Simple-NeRF training step.
 
-    Config-2 form (default): world rays, coarse + fine nets, white background.
-    Config-3 form: ``ndc=dict(h=378, w=504, focal=400.0, near=1.0)`` switches to
+    The 4096-ray training form (default): world rays, coarse + fine nets, white background.
+    The NDC pair form: ``ndc=dict(h=378, w=504, focal=400.0, near=1.0)`` switches to
     forward-facing NDC rays (CommonUtils04.py:120-138; z in [near_ndc, far_ndc] =
     [0, 1]) and ``aug=[(name, spec_kwargs), ...]`` adds augmented nets evaluated
     on the same coarse samples (SimpleNeRF17.py:244-261) and, with
@@ -485,7 +485,7 @@ def main(argv=None):
 
 
 def synthetic_batch(n_rays, n_coarse, n_fine, seed, device='cpu', pin=False):
-    """Config-2 synthetic inputs: o ~ N(0, 0.1^2), d = normalize(N(0, I)), rgb
+    """Synthetic inputs of the 4096-ray training step: o ~ N(0, 0.1^2), d = normalize(N(0, I)), rgb
     targets ~ U[0,1]^3, depth targets ~ U[2,6], stratified/pdf uniforms ~ U[0,1)."""
     g = torch.Generator().manual_seed(seed)
     o = torch.randn(n_rays, 3, generator=g) * 0.1

@@ -64,7 +64,7 @@ def _last_sigma_agrees(sig_gpu, sig_ref):
     return (np.asarray(sig_gpu)[:, -1] > 0) == (np.asarray(sig_ref)[:, -1] > 0)
 
 
-def _config1_inputs(n=1024):
+def _render_inputs(n=1024):
     rng = np.random.default_rng(0)
     o = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
     d = rng.standard_normal((n, 3)).astype(np.float32)
@@ -74,13 +74,13 @@ def _config1_inputs(n=1024):
     return o, d, u_c, u_f
 
 
-def test_config1_render_1024_rays_matches_oracle():
-    """Config-1 render through the functional path (stratified z, PE + MLP,
+def test_render_1024_rays_matches_oracle():
+    """The 1024-ray render through the functional path (stratified z, PE + MLP,
     compositing, inverse-CDF fine z, fine pass) against the oracle's
     render_rays (SimpleNeRF17.py:159-328) on the same uniforms."""
     from simple_rf_gb300 import functional as F
     n = 1024
-    o, d, u_c, u_f = _config1_inputs(n)
+    o, d, u_c, u_f = _render_inputs(n)
     ospec = on.MlpSpec()
     pc, pf = on.xavier_params(ospec, 0), on.xavier_params(ospec, 1)
     spec = F.MlpSpec()
@@ -116,13 +116,13 @@ def test_config1_render_1024_rays_matches_oracle():
     for tag in ('coarse', 'fine'):
         for k in ('rgb', 'depth', 'weights', 'acc'):
             _close(got[f'{k}_{tag}'], ref[f'{k}_{tag}'], f'{k}_{tag}', rows=keep)
-    print('config 1: rays excluded for a last-sample sigma flip', int((~keep).sum()), 'of', n,
+    print('1024-ray render: rays excluded for a last-sample sigma flip', int((~keep).sum()), 'of', n,
           '; fine depths equal to the oracle sampler', frac)
 
 
-def test_config1_drop_in_render_1024_rays_matches_oracle():
+def test_drop_in_render_1024_rays_matches_oracle():
     """GbSimpleNeRF.forward in evaluation mode (linspace coarse depths,
-    deterministic inverse CDF) on the config-1 rays, ray generation patched to
+    deterministic inverse CDF) on the same 1024 rays, ray generation patched to
     take the synthetic origins and directions as the reference harness does."""
     from simple_rf_gb300 import functional as F
     from simple_rf_gb300.nerf import GbSimpleNeRF
@@ -137,7 +137,7 @@ def test_config1_drop_in_render_1024_rays_matches_oracle():
     model_configs = {'intrinsics': np.eye(3)[None], 'extrinsics': np.eye(4)[None], 'resolution': (32, 32),
                      'near': 2.0, 'far': 6.0, 'near_ndc': 0.0, 'far_ndc': 1.0}
     n = 1024
-    o, d, _, _ = _config1_inputs(n)
+    o, d, _, _ = _render_inputs(n)
     model = GbSimpleNeRF(configs, model_configs).to(DEV).eval()
     spec = on.MlpSpec()
     pc, pf = on.xavier_params(spec, 0), on.xavier_params(spec, 1)
@@ -165,7 +165,7 @@ def test_config1_drop_in_render_1024_rays_matches_oracle():
         np.testing.assert_allclose(got[k][keep], ref[k][keep], rtol=1e-5, atol=1.6e-5, err_msg=k)
 
 
-# --------------------------------------------------------------- config 2 --
+# ------------------------------------------------------ 4096-ray training step --
 
 def _step(n_rays, precision='fp32', sigma_bias=None, seed=3):
     from simple_rf_gb300.train_step import NerfTrainStep, synthetic_batch
@@ -186,7 +186,7 @@ def _step(n_rays, precision='fp32', sigma_bias=None, seed=3):
 
 
 def oracle_step_chunked(params, host, z_fine, dtype, chunk=256, grads=True):
-    """The oracle's config-2 step over ray chunks (rays are independent, so the
+    """The oracle's 4096-ray training step over ray chunks (rays are independent, so the
     outputs are those of one whole-batch call; the loss gradients come from the
     whole batch and the parameter gradients are summed over the chunks)."""
     o, d, t_rgb, t_depth, u_c, u_f = [np.asarray(x, dtype) for x in host]
@@ -220,7 +220,7 @@ def oracle_step_chunked(params, host, z_fine, dtype, chunk=256, grads=True):
     return ret, total
 
 
-def test_config2_train_step_4096_rays_outputs_match_oracle():
+def test_train_step_4096_rays_outputs_match_oracle():
     """The fused FP32 plain step at the benchmark's 4096 rays: coarse and fine
     rgb/depth/weights/acc against the float32 oracle (fine pass on the depths
     the GPU sampled), the Xavier-initialised nets as trained."""
@@ -235,10 +235,10 @@ def test_config2_train_step_4096_rays_outputs_match_oracle():
         for k in ('rgb_map', 'depth', 'weights', 'acc'):
             key = {'rgb_map': 'rgb'}.get(k, k)
             _close(out[f'{k}_{tag}'], ref[f'{key}_{tag}'], f'{k}_{tag}', rows=keep)
-    print('config 2: rays excluded for a last-sample sigma flip', int((~keep).sum()), 'of 4096')
+    print('4096-ray step: rays excluded for a last-sample sigma flip', int((~keep).sum()), 'of 4096')
 
 
-def test_config2_train_step_4096_rays_gradients_match_fp64_oracle():
+def test_train_step_4096_rays_gradients_match_fp64_oracle():
     """Parameter gradients of the 4096-ray FP32 plain step against the float64
     oracle, on a network whose sigma-head bias keeps every ray off the last-sample
     step (see test_gpu_train_step.py)."""
@@ -249,7 +249,7 @@ def test_config2_train_step_4096_rays_gradients_match_fp64_oracle():
     check_fp32_gradients(grads, g32, g64)
 
 
-# --------------------------------------------------------------- config 4 --
+# --------------------------------------------------------- TensoRF 300^3 --
 
 def _oracle_params(tm):
     tp = {'bbox': tm.bounding_box.cpu().numpy().astype(np.float32)}
@@ -262,7 +262,7 @@ def _oracle_params(tm):
     return tp
 
 
-def _config4_run(n_rays, seed=21):
+def _tensorf_run(n_rays, seed=21):
     from simple_rf_gb300 import functional as F
     from simple_rf_gb300.bench_tensorf import make_models, synthetic_rays
     tm = make_models(DEV, precision='fp32')[0]
@@ -292,12 +292,12 @@ def _threshold_stable(w_gpu, w_ref, thr=1e-4):
     return ~(side | near).any(1)
 
 
-def test_config4_tensorf_8192_rays_outputs_match_oracle():
+def test_tensorf_300cubed_8192_rays_outputs_match_oracle():
     """The drop-in GbVmTensor at the benchmark's main model (300^3, R 16 / 48,
     27 features, 128 units, 128^3 alpha mask at 15%, white background, 1039
     samples per ray) on 8192 rays against the float32 oracle of
     LowRankTensor.forward (SimpleTensoRF09.py:701-761)."""
-    tm, (o, d, z), out = _config4_run(8192)
+    tm, (o, d, z), out = _tensorf_run(8192)
     oh, dh, zh = (x.cpu().numpy() for x in (o, d, z))
     ref, _ = _oracle_forward(tm, oh, dh, zh)[0]
     got = {k: v.detach().cpu().numpy() for k, v in out.items()}
@@ -307,12 +307,12 @@ def test_config4_tensorf_8192_rays_outputs_match_oracle():
     assert keep.mean() > 0.99, int((~keep).sum())
     for k in ('rgb', 'depth', 'acc', 'weights', 'depth_var', 'raw_sigma'):
         _close(got[k], ref[k], k, rows=keep)
-    print('config 4: surface samples', n_surface, '; rays excluded at the surface threshold', int((~keep).sum()),
+    print('TensoRF 300^3: surface samples', n_surface, '; rays excluded at the surface threshold', int((~keep).sum()),
           'of 8192')
 
 
-def test_config4_tensorf_gradients_match_oracle():
-    """Gradients of every plane, line, basis and renderer parameter of the config-4
+def test_tensorf_300cubed_gradients_match_oracle():
+    """Gradients of every plane, line, basis and renderer parameter of the 300^3 TensoRF
     main model for a loss on 256 of the 8192 rays (the other rays carry zero
     cotangents, so the gradients are those of the 256 rays alone) against the
     float64 oracle's adjoint: per tensor within max(1e-4, 3 e32) relative L2, e32
@@ -326,7 +326,7 @@ def test_config4_tensorf_gradients_match_oracle():
     (a sample coloured on one side only adds a renderer term to one gradient),
     no density at their last sample (whose delta is 1e10 |d|) and no density
     feature within 1e-6 of the ReLU's kink."""
-    tm, (o, d, z), out = _config4_run(8192, seed=22)
+    tm, (o, d, z), out = _tensorf_run(8192, seed=22)
     n_sub = 256
     spec = ot.RendererSpec(features_dim=27, features_pe=2, views_pe=2, units=128)
     am = tm.alpha_mask
@@ -387,11 +387,11 @@ def test_config4_tensorf_gradients_match_oracle():
         bar = max(1e-4, 3 * e32)
         worst = max(worst, rel / bar)
         assert rel < bar, (name, rel, e32)
-    print('config 4: worst per-tensor gradient error / bar', worst)
+    print('TensoRF 300^3: worst per-tensor gradient error / bar', worst)
 
 
 def _pair_oracle_forward(params, host, z_fine, dtype, chunk=512):
-    """The oracle's forward of the config-3 pair (NDC, main coarse + fine, the
+    """The oracle's forward of the NDC main + augmented pair (NDC, main coarse + fine, the
     augmented coarse net on the same coarse samples) over ray chunks."""
     o, d, _, _, u_c, u_f = [np.asarray(x, dtype) for x in host]
     spec = on.MlpSpec()
@@ -413,8 +413,8 @@ def _pair_oracle_forward(params, host, z_fine, dtype, chunk=512):
 
 
 @pytest.mark.parametrize('precision', ['fp32', 'fp16'])
-def test_config3_pair_step_4096_rays_matches_oracle(precision):
-    """The config-3 pair step (NDC main coarse + fine + augmented coarse, 4096
+def test_ndc_pair_step_4096_rays_matches_oracle(precision):
+    """The NDC pair step (main coarse + fine + augmented coarse, 4096
     rays) against the oracle: FP32 plain rgb / weights / acc within 1e-5 of the
     float32 oracle (acc with one ulp(1) per sample), the NDC depth within 1e-5 of
     the float64 reduction of the GPU's own weights; the FP16 step's
@@ -458,8 +458,8 @@ def test_config3_pair_step_4096_rays_matches_oracle(precision):
         print('fp16 pair step, 4096 rays: rgb max-abs vs float64', worst)
 
 
-def test_config5_full_view_render_matches_oracle():
-    """One full config-5 view (504 x 378 = 190,512 NDC rays, focal 400) through the
+def test_full_view_render_504x378_matches_oracle():
+    """One full view of the image render (504 x 378 = 190,512 NDC rays, focal 400) through the
     FP32 plain pair renderer in chunks of 65,536 (the last chunk partial): rays at
     the start, across the first chunk boundary and in the partial last chunk
     against the float32 oracle (rgb and acc of the three nets within 1e-5

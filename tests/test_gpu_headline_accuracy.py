@@ -29,7 +29,7 @@ def built():
 
 
 def test_headline_step_rgb_on_4096_rays_against_fp64_oracle():
-    from test_gpu_baseline_configs import _step, oracle_step_chunked
+    from test_gpu_benchmark_workloads import _step, oracle_step_chunked
     params, out, _, host = _step(4096, precision=HEADLINE, seed=7)
     ref, _ = oracle_step_chunked(params, host, out['z_fine'], np.float64, chunk=512, grads=False)
     flip = np.zeros(4096, bool)
@@ -52,7 +52,7 @@ def test_headline_step_gradients_against_fp64_oracle():
     seeded batches whose 1024 rays have no flip against the float64 oracle is
     used (the step is deterministic, so the choice is fixed), and the flips of
     the rejected batches are reported."""
-    from test_gpu_baseline_configs import _step, oracle_step_chunked
+    from test_gpu_benchmark_workloads import _step, oracle_step_chunked
     rejected = {}
     for seed in range(7, 12):
         params, out, grads, host = _step(1024, precision=HEADLINE, sigma_bias=0.5, seed=seed)

@@ -4,7 +4,7 @@ the BF16 NeRF MLP against the float64 oracle.
 Tolerances: the GEMM output is stored in BF16, so 1.5e-2 relative of the
 row scale; weight-gradient partials are FP32 sums of exact BF16 products, so
 1e-4 relative L2.  MLP: rgb within 2e-3 max-abs and parameter gradients within
-1e-2 relative L2 of the float64 oracle (the BF16 bars of the benchmark spec).
+1e-2 relative L2 of the float64 oracle (the accuracy bars of the benchmark metric).
 """
 import ctypes
 

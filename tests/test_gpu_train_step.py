@@ -1,4 +1,4 @@
-"""The fused training step (config-2 shape, reduced ray count) against the oracle,
+"""The fused training step (the 4096-ray workload's shape, fewer rays) against the oracle,
 and the drop-in GbSimpleNeRF against the oracle's render.
 
 FP32 plain path: rgb/depth/weights within 1e-5 relative (absolute floor 1e-6 of
