@@ -313,110 +313,6 @@ __global__ void vm_bwd_group_kernel(srf_vm_grid gg, srf_vm_grid g, const float* 
     }
 }
 
-// a += v w (or a = v w when a starts a new cell), and the reduction of a into row
-// idx's components r .. r + 3 (nothing for an outside corner or an all-zero sum).
-__device__ __forceinline__ void acc4(float4& a, const float4& v, float w, bool add) {
-    const float4 x = make_float4(v.x * w, v.y * w, v.z * w, v.w * w);
-    if (add) {
-        a.x += x.x; a.y += x.y; a.z += x.z; a.w += x.w;
-    } else {
-        a = x;
-    }
-}
-__device__ __forceinline__ void flush4(float* base, int idx, int R, int r, const float4& a) {
-    if (idx >= 0 && (a.x != 0.f || a.y != 0.f || a.z != 0.f || a.w != 0.f))
-        red_add4(base + int64_t(idx) * R + r, a.x, a.y, a.z, a.w);
-}
-
-// Run-aggregated form of the group adjoint: a group of G lanes takes K consecutive
-// points (the compacted samples are in ray order, half a voxel apart, so neighbours
-// often fall in the same plane cell and line segment) and keeps, per plane, the
-// contributions to the current cell's four corners and the current line segment's two
-// taps in registers, adding them to memory only when the cell or segment changes:
-// fewer 128-bit reductions for the same sums (grouped differently).  Lane j takes its
-// pieces r = 4 j, 4 j + 4 G, ... one at a time over the run (re-deriving the taps per
-// piece keeps six float4 sums live instead of six per piece).  A line's taps come
-// from a bilinear lookup on a width-1 image, whose x + 1 corners (slots 1 and 3) are
-// always outside it.
-template <int G, int K>
-__global__ void vm_bwd_run_kernel(srf_vm_grid gg, srf_vm_grid g, const float* __restrict__ pts, int64_t n,
-                                  const float* __restrict__ dfeat, int ld, int per_component) {
-    const int j = threadIdx.x % G;
-    const int64_t p0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / G * K;
-    if (p0 >= n) return;
-    const int64_t p1 = p0 + K < n ? p0 + K : n;
-    int off = 0;
-    for (int i = 0; i < 3; ++i) {
-        const int R = g.n_comp[i];
-        float* gpl = gg.planes[i];
-        float* gln = gg.lines[i];
-        for (int r = 4 * j; r < R; r += 4 * G) {   // one four-component piece at a time
-            float4 ap0 = {}, ap1 = {}, ap2 = {}, ap3 = {}, al0 = {}, al2 = {};
-            int c0 = -1, c1 = -1, c2 = -1, c3 = -1, l0 = -1, l2 = -1;
-            for (int64_t p = p0; p < p1; ++p) {
-                const float* q3 = pts + 3 * p;
-                Taps pt, lt;
-                plane_taps(g, i, q3, pt, lt);
-                const bool same_p = p > p0 && pt.idx[0] == c0 && pt.idx[1] == c1 && pt.idx[2] == c2 &&
-                                    pt.idx[3] == c3;
-                const bool same_l = p > p0 && lt.idx[0] == l0 && lt.idx[2] == l2;
-                if (p > p0 && !same_p) {
-                    flush4(gpl, c0, R, r, ap0);
-                    flush4(gpl, c1, R, r, ap1);
-                    flush4(gpl, c2, R, r, ap2);
-                    flush4(gpl, c3, R, r, ap3);
-                }
-                if (p > p0 && !same_l) {
-                    flush4(gln, l0, R, r, al0);
-                    flush4(gln, l2, R, r, al2);
-                }
-                const float ds = per_component ? 0.f : dfeat[p];
-                const float4 d = per_component ? *reinterpret_cast<const float4*>(dfeat + p * ld + off + r)
-                                               : make_float4(ds, ds, ds, ds);
-                float4 pv, lv;
-                interp4(g.planes[i], g.lines[i], R, r, pt, lt, pv, lv);
-                const float4 dp = make_float4(d.x * lv.x, d.y * lv.y, d.z * lv.z, d.w * lv.w);
-                const float4 dl = make_float4(d.x * pv.x, d.y * pv.y, d.z * pv.z, d.w * pv.w);
-                acc4(ap0, dp, pt.w[0], same_p);
-                acc4(ap1, dp, pt.w[1], same_p);
-                acc4(ap2, dp, pt.w[2], same_p);
-                acc4(ap3, dp, pt.w[3], same_p);
-                acc4(al0, dl, lt.w[0], same_l);
-                acc4(al2, dl, lt.w[2], same_l);
-                c0 = pt.idx[0]; c1 = pt.idx[1]; c2 = pt.idx[2]; c3 = pt.idx[3];
-                l0 = lt.idx[0]; l2 = lt.idx[2];
-            }
-            flush4(gpl, c0, R, r, ap0);
-            flush4(gpl, c1, R, r, ap1);
-            flush4(gpl, c2, R, r, ap2);
-            flush4(gpl, c3, R, r, ap3);
-            flush4(gln, l0, R, r, al0);
-            flush4(gln, l2, R, r, al2);
-        }
-        off += R;
-    }
-}
-
-constexpr bool kRunAdjoint = true;   // the run-aggregated adjoint for grids the group kernels take
-
-// Points per run: 8 when a lane holds one piece per plane (R <= 4 G, the density
-// grids), 4 when it holds several (R = 48: 3 pieces, each re-walking the run), the
-// fastest of 4 / 8 / 16 / 32 measured on 1.25M ray-ordered points at 300^3.
-template <int G>
-int launch_bwd_run(const srf_vm_grid& gg, const srf_vm_grid& g, const float* pts, int64_t n, const float* dfeat,
-                   int ld, int per_component, cudaStream_t s) {
-    int rmax = 0;
-    for (int i = 0; i < 3; ++i) rmax = g.n_comp[i] > rmax ? g.n_comp[i] : rmax;
-    if (rmax <= 4 * G) {
-        const int64_t groups = (n + 7) / 8;
-        vm_bwd_run_kernel<G, 8><<<grid_1d(groups * G, 128), 128, 0, s>>>(gg, g, pts, n, dfeat, ld, per_component);
-    } else {
-        const int64_t groups = (n + 3) / 4;
-        vm_bwd_run_kernel<G, 4><<<grid_1d(groups * G, 128), 128, 0, s>>>(gg, g, pts, n, dfeat, ld, per_component);
-    }
-    return launch_status();
-}
-
 // Lanes per point for the group kernels: the largest power of two (at most 16) that
 // divides every R_i / 4, so every lane of a group takes the same number of
 // four-component pieces (R = 48: 4 lanes x 3 pieces, each lane's loads independent
@@ -965,7 +861,6 @@ extern "C" int srf_vm_density_backward(const srf_vm_grid* grad_grid, const srf_v
     if (G) {
         return launch_grouped(G, n_pts, [&](auto gc) {
             constexpr int g = decltype(gc)::value;
-            if (kRunAdjoint) return launch_bwd_run<g>(*grad_grid, *grid, pts, n_pts, d_features, 1, 0, as_stream(stream));
             vm_bwd_group_kernel<g><<<grid_1d(n_pts * g, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts,
                                                                                            n_pts, d_features, 1, 0);
             return launch_status();
@@ -1022,7 +917,6 @@ extern "C" int srf_vm_color_backward(const srf_vm_grid* grad_grid, const srf_vm_
     if (G) {   // G != 0 implies ld % 4 == 0; d_features alignment is checked above
         return launch_grouped(G, n_pts, [&](auto gc) {
             constexpr int g = decltype(gc)::value;
-            if (kRunAdjoint) return launch_bwd_run<g>(*grad_grid, *grid, pts, n_pts, d_features, ld, 1, as_stream(stream));
             vm_bwd_group_kernel<g><<<grid_1d(n_pts * g, 128), 128, 0, as_stream(stream)>>>(*grad_grid, *grid, pts,
                                                                                            n_pts, d_features, ld, 1);
             return launch_status();
