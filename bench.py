@@ -429,6 +429,7 @@ def time_tensorf(precision, steps, dev, stream, graph=True):
     if graph:
         out['capacities'] = st.caps
         out['recaptures'] = st.recaptures
+        out['capacity_shrinks'] = st.shrinks
         out['gpu_launches_per_step'] = st.launches_per_step
     del st, models, batches
     torch.cuda.empty_cache()

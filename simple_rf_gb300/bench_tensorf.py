@@ -105,6 +105,7 @@ def ray_batch_sweep(device, modes=(('fp16', False), ('fp16', True), ('fp32', Fal
                            'surface_samples': int(surf)}
             if graph:
                 res[str(n)]['recaptures'] = st.recaptures
+                res[str(n)]['capacity_shrinks'] = st.shrinks
                 del st
             del batches
             torch.cuda.empty_cache()

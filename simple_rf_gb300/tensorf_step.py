@@ -7,13 +7,14 @@ multi-tensor Adam launch over every parameter group.
 TensorfTrainStep runs uncaptured (two host reads of sample counts per step);
 TensorfGraphStep captures the whole step as one CUDA graph.
 """
+import collections
 import ctypes
 
 import torch
 
 from . import _lib
 from . import functional as F
-from .tensorf_model import forward_models
+from .tensorf_model import _side_stream, forward_models
 
 
 class TensorfTrainStep:
@@ -74,12 +75,16 @@ class TensorfGraphStep:
     counter; the call reads the flag once its replay has ended and, when it is
     set, re-captures with capacities 25% above the counts and redoes the batch.
     Padding rows still cost the renderer MLP and basis passes their full work,
-    so the uncaptured step stays faster once per-step host work is hidden
-    behind the GPU (8192 rays and up); the captured step wins on small batches.
+    so when the largest counts of the last 8 replays fall below 1 / 1.4 of the
+    capacities (the surface count drops as the density field trains) the next
+    call re-captures with capacities 15% above those counts.
     """
 
-    MARGIN = 1.15
-    REGROW = 1.25
+    MARGIN = 1.15     # capacities above the counts at a capture
+    REGROW = 1.25     # ... at a re-capture after an overflow
+    SHRINK = 1.4      # capacities this far above the counts are re-captured at SHRINK_TO
+    SHRINK_TO = 1.15
+    WINDOW = 8        # replays whose largest counts a shrink keeps room for
     ROUND = 1024
 
     def __init__(self, models, n_rays, lr_tensor=0.02, lr_network=1e-3, state=None, step_dev=None, near=2.0,
@@ -113,6 +118,9 @@ class TensorfGraphStep:
         self.done = torch.cuda.Event()
         self.launches_per_step = None
         self.recaptures = 0
+        self.shrinks = 0
+        self._recent = collections.deque(maxlen=self.WINDOW)   # counts of the last replays
+        self._shrink_to = None
 
     def _calls(self):
         vd = F.view_dirs(self.d)
@@ -126,13 +134,25 @@ class TensorfGraphStep:
     def _body(self, dry):
         self.ovf.zero_()
         calls = self._calls()
-        states = [tm.forward_begin(inp) for tm, inp in calls]
-        for (tm, _), st, (cv, _) in zip(calls, states, self.caps):
-            tm.forward_density(st, cv, capacity=True)
-        loss = 0.0
-        for (tm, _), st, (_, cs) in zip(calls, states, self.caps):
-            out = tm.forward_color(st, cs, retraw=False, capacity=True)
-            loss = loss + torch.mean(torch.mean((out['rgb'] - self.t_rgb) ** 2, -1))
+        # every model after the first on a stream of its own (forked from and joined
+        # back to the capturing stream), as forward_models runs them uncaptured; the
+        # backward of each model's kernels follows its forward's stream
+        main = torch.cuda.current_stream(self.dev)
+        streams = [main] + [_side_stream(self.dev, i) for i in range(1, len(calls))]
+        losses, states = [], []
+        for (tm, inp), sm, (cv, cs) in zip(calls, streams, self.caps):
+            sm.wait_stream(main)
+            with torch.cuda.stream(sm):
+                st = tm.forward_begin(inp)
+                tm.forward_density(st, cv, capacity=True)
+                out = tm.forward_color(st, cs, retraw=False, capacity=True)
+                losses.append(torch.mean(torch.mean((out['rgb'] - self.t_rgb) ** 2, -1)))
+                states.append(st)
+        for sm in streams[1:]:
+            main.wait_stream(sm)
+        loss = losses[0]
+        for x in losses[1:]:
+            loss = loss + x
         counts = torch.cat([torch.cat([st['cnt_v'].reshape(1), st['cnt_s'].reshape(1)]) for st in states])
         self.ovf.copy_((counts > self.caps_dev).any().to(torch.int32).reshape(1))
         if dry:
@@ -199,16 +219,38 @@ class TensorfGraphStep:
             for dst, src in zip((self.o, self.d, self.t_rgb, self.u), batch):
                 dst.copy_(src)
             self._capture(self._counts(), self.MARGIN)
+        elif self._shrink_to is not None:
+            for dst, src in zip((self.o, self.d, self.t_rgb, self.u), batch):
+                dst.copy_(src)
+            self.shrinks += 1
+            self._capture(self._shrink_to, self.SHRINK_TO)
+            self._shrink_to = None
+            self._recent.clear()
         self._replay(batch)
         self.done.synchronize()
         while int(self.flags_host[0]):
-            c = self.flags_host[1:].tolist()
+            # the replay's counts are the full counts even where they overflowed
             self.recaptures += 1
-            self._capture([(max(c[2 * i], cv), max(c[2 * i + 1], cs)) for i, (cv, cs) in enumerate(self.caps)],
-                          max(self.MARGIN, self.REGROW))
+            peak = self._host_counts()
+            for c in self._recent:
+                peak = [(max(a[0], b[0]), max(a[1], b[1])) for a, b in zip(peak, c)]
+            self._capture(peak, max(self.MARGIN, self.REGROW))
             self._replay(batch)
             self.done.synchronize()
+        # capacities far above the counts of every recent batch (the surface count
+        # falls as the density field trains) cost each replay the padded rows' full
+        # work: the next call re-captures them at SHRINK_TO above the recent maxima
+        self._recent.append(self._host_counts())
+        if len(self._recent) == self._recent.maxlen:
+            peak = [tuple(max(c[i][k] for c in self._recent) for k in range(2)) for i in range(len(self.models))]
+            if any(cap > self.SHRINK * max(cnt, self.ROUND) for caps, cnts in zip(self.caps, peak)
+                   for cap, cnt in zip(caps, cnts)):
+                self._shrink_to = peak
         return self.loss
+
+    def _host_counts(self):
+        c = self.flags_host[1:].tolist()
+        return [(c[2 * i], c[2 * i + 1]) for i in range(len(self.models))]
 
     def sample_counts(self):
         """Valid and surface sample counts of the last finished replay, per model."""

@@ -346,6 +346,35 @@ def test_graph_step_redoes_a_step_that_overflowed():
     assert gb.recaptures >= 1 and int(gb.flags_host[0]) == 0 and int(gb.step_dev.item()) == 2
 
 
+def test_graph_step_shrinks_oversized_capacities():
+    """Capacities three times the counts (the window of recent replays set to 2):
+    after two calls the third re-captures at 15% above the largest recent counts;
+    every call returns what the uncaptured step computes.  Learning rates are 0,
+    so both steps see the same parameters at every call (with updates, Adam turns
+    last-bit gradient differences into +-lr steps and the runs drift apart)."""
+    from simple_rf_gb300 import build as b
+    b.build()
+    from simple_rf_gb300.bench_tensorf import TensorfGraphStep, TensorfTrainStep, make_models, synthetic_rays
+    ea = TensorfTrainStep(make_models(DEV, seed=4, precision='fp32', grids=(64, 32)), lr_tensor=0.0, lr_network=0.0)
+    gb = TensorfGraphStep(make_models(DEV, seed=4, precision='fp32', grids=(64, 32)), 2048, lr_tensor=0.0,
+                          lr_network=0.0)
+    gb.MARGIN = 3.0
+    gb._recent = __import__('collections').deque(maxlen=2)
+    for i in range(3):
+        batch = synthetic_rays(2048, 60 + i, DEV)
+        la = float(ea.step(*batch).item())
+        lb = float(gb.step(*batch).item())
+        assert gb.shrinks == (1 if i == 2 else 0), (i, gb.shrinks)
+        assert abs(la - lb) <= 1e-5 * abs(la), (i, la, lb)
+        for (p, _), x, y in zip(ea.params, _grads(ea), _grads(gb)):
+            assert _rel(y, x) < 1e-4, (i, tuple(p.shape), _rel(y, x))
+    counts = gb._host_counts()
+    assert gb.shrinks == 1 and gb.recaptures == 0, (gb.shrinks, gb.recaptures)
+    # re-captured from the recent maxima: at least the last counts, far below the initial 3x
+    for (cv, cs), (nv, ns) in zip(gb.caps, counts):
+        assert nv <= cv <= 2.0 * max(nv, gb.ROUND) and ns <= cs <= 2.0 * max(ns, gb.ROUND), (gb.caps, counts)
+
+
 def test_alpha_mask_rebuild_matches_reference(golden):
     """LowRankTensor.update_alpha_mask (SimpleTensoRF09.py:849-876) on the drop-in:
     dense alpha of the density over the grid (the VM density kernel), 3^3 max-pool,
