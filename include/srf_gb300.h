@@ -185,6 +185,19 @@ int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* const* para
                          const float* dirs, int dir_div, int64_t m, const float* sigma_noise, float* sigma,
                          float* rgb, int precision, int for_backward, void* workspace, size_t workspace_bytes,
                          srf_loss_scaler* scaler, void* stream);
+/* Forward path of the 16-bit NeRF MLP (BF16 / FP16 precision): mode 0 runs one
+ * tcgen05 kernel per layer after the encoder; 1 (default) runs the layers of a
+ * forward-only call (for_backward = 0) as one fused kernel that keeps each
+ * 128-sample tile's activations in shared memory from the encodings to the
+ * heads; 2 also fuses the forward of for_backward calls, which then stores the
+ * activations the backward reads from the fused kernel (measured slower than the
+ * per-layer kernels).  Layouts the fused kernel does not cover (trunk width other
+ * than 256, point PE degree above 10, the points-augmentation variant, a view
+ * branch other than one 128-wide layer) always run per layer.  The paths form
+ * the same products in the same order and round the same activations; the head
+ * dot products sum their partials in another order (last-bit differences).
+ * Returns the previous mode; mode < 0 only queries.  Process-wide setting. */
+int srf_nerf_mlp_fused_path(int mode);
 
 /* Backward: dsigma (m) w.r.t. the ReLU'd sigma, drgb (m,3) w.r.t. the sigmoid
  * rgb; dir_div as in the forward.  grads[i] receives (accumulate ? += : =) the

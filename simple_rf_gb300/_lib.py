@@ -161,6 +161,7 @@ _SIGS = {
     'srf_tv_loss': (c_int, [ctypes.POINTER(TvComponent), c_int, c_float, P, P, P]),
     'srf_autotune_enable': (c_int, [c_int]),
     'srf_tensorf_basis_adjoint_path': (c_int, [c_int]),
+    'srf_nerf_mlp_fused_path': (c_int, [c_int]),
     'srf_autotune_count': (c_int, []),
     'srf_autotune_entry': (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int64), ctypes.POINTER(c_int64),
                                    ctypes.POINTER(c_int64), ctypes.POINTER(c_int)]),

@@ -4,6 +4,7 @@
     python -m simple_rf_gb300.bench_kernels wgrad --m 786432 --n 256 --k 256
     python -m simple_rf_gb300.bench_kernels composite --rays 4096 --samples 192 [--backward]
     python -m simple_rf_gb300.bench_kernels vm --rays 1216 --samples 1024 --comps 48 [--kind density] [--backward]
+    python -m simple_rf_gb300.bench_kernels mlp --m 786432 [--mlp-path fused|layers] [--store] [--precision fp16]
 
 Each prints one JSON line: the average launch time over --reps launches
 (CUDA events on the launching stream, after --warmup launches) and the achieved
@@ -175,9 +176,47 @@ def vm(args):
             'bytes': nbytes, 'bytes_per_point': nbytes // p}
 
 
+def mlp(args):
+    """Forward of the benchmark NeRF MLP (8 x 256 trunk with the skip, 128-wide view
+    layer, PE degrees 10 / 4) over --m samples, 64 samples per view direction; with
+    --store the training forward (the activations the backward reads are stored)."""
+    from . import functional as F
+    lib = _lib.load()
+    prev = lib.srf_nerf_mlp_fused_path(2 if args.mlp_path == 'fused' else 0)
+    spec = F.MlpSpec()
+    g = torch.Generator(device='cuda').manual_seed(0)
+    params = []
+    for name, n in zip(spec.param_names, spec.param_numel):
+        scale = 0.01 if name.endswith('bias') else 0.06
+        params.append(torch.randn(n, device='cuda', generator=g) * scale)
+    m, div = args.m, 64
+    pts = torch.randn(m, 3, device='cuda', generator=g) * 0.7
+    dirs = torch.nn.functional.normalize(torch.randn((m + div - 1) // div, 3, device='cuda', generator=g), dim=1)
+    sigma = torch.empty(m, device='cuda')
+    rgb = torch.empty(m, 3, device='cuda')
+    prec = _lib.PRECISIONS[args.precision]
+    wsb = spec.workspace_bytes(m, prec, args.store)
+    ws = torch.empty(wsb, dtype=torch.uint8, device='cuda')
+    scaler = torch.tensor([65536.0, 1 / 65536.0, 0.0, 0.0], device='cuda')
+    arr = (ctypes.c_void_p * len(params))(*[t.data_ptr() for t in params])
+
+    def run():
+        _lib.call('srf_nerf_mlp_forward', ctypes.byref(spec.desc), arr, _p(pts), _p(dirs), div, m, None, _p(sigma),
+                  _p(rgb), prec, int(args.store), _p(ws), wsb, _p(scaler), _st())
+    try:
+        t = _time(run, args.reps, args.warmup)
+    finally:
+        lib.srf_nerf_mlp_fused_path(prev)
+    macs = sum(n for name, n in zip(spec.param_names, spec.param_numel) if name.endswith('weight'))
+    return {'kernel': 'mlp_fused_kernel' if args.mlp_path == 'fused' else 'per-layer tc_gemm_kernel',
+            'form': 'training forward (stores activations)' if args.store else 'forward only', 'm': m,
+            'precision': args.precision, 'ms': t * 1e3, 'tflops': 2.0 * macs * m / t / 1e12,
+            'ns_per_sample': t / m * 1e9}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('which', choices=['gemm', 'wgrad', 'composite', 'vm'])
+    ap.add_argument('which', choices=['gemm', 'wgrad', 'composite', 'vm', 'mlp'])
     ap.add_argument('--m', type=int, default=786432)
     ap.add_argument('--k', type=int, default=256)
     ap.add_argument('--n', type=int, default=256)
@@ -190,10 +229,13 @@ def main(argv=None):
     ap.add_argument('--kind', choices=['color', 'density'], default='color', help='vm: which lookup')
     ap.add_argument('--res', type=int, default=300, help='vm: grid resolution per axis')
     ap.add_argument('--comps', type=int, default=48, help='vm: components per plane/line')
+    ap.add_argument('--mlp-path', default='fused', choices=['fused', 'layers'], help='mlp: fused kernel or per layer')
+    ap.add_argument('--store', action='store_true', help='mlp: training forward (stores the activations)')
+    ap.add_argument('--precision', default='fp16', choices=['bf16', 'fp16'], help='mlp: operand format')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
-    res = {'gemm': gemm, 'wgrad': wgrad, 'composite': composite, 'vm': vm}[args.which](args)
+    res = {'gemm': gemm, 'wgrad': wgrad, 'composite': composite, 'vm': vm, 'mlp': mlp}[args.which](args)
     print(json.dumps({k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.items()}))
 
 

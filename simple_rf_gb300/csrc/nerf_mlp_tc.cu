@@ -20,6 +20,7 @@
 
 #include "autotune.cuh"
 #include "tc_gemm.cuh"
+#include "tc_mlp_fused.cuh"
 
 namespace srf {
 
@@ -726,6 +727,115 @@ int wgrad_layer(const LayerMap& lm, float* partial, size_t partial_floats, const
     return launch_status();
 }
 
+// Which forwards run as the one fused kernel (tc::mlp_fused_kernel) where the
+// layout fits it: 0 none (one kernel per layer), 1 forward-only calls (default),
+// 2 also the forward of a training step (which stores the activations the
+// backward reads; slower than the per-layer kernels: its row-wise stores from the
+// epilogue registers cost more than the reads they save).
+std::atomic<int> g_mlp_fused{1};
+
+// The fused kernel's layouts: 256-wide trunk of at most 8 layers, a point
+// encoding of at most 64 columns feeding the first layer (and the skip layer)
+// whole, and either no view branch (sigma + rgb on the last trunk layer) or the
+// reference's single 128-wide view layer on [feature, PE(view dirs)] with at most
+// 64 encoding columns.
+bool fused_fits(const MlpLayout& L, const TcLayout& T) {
+    if (L.Wp != 256 || T.enc_w != 64 || L.pin != L.ppe || L.Dp < 1 || L.desc.points_pe_degree > 10) return false;
+    if (L.skip >= 0 && L.skip >= L.Dp - 1) return false;
+    if (L.vdep && (L.Dv != 1 || L.Wv != 128 || T.vx_w != 64 || L.vin != L.vpe || L.vpe <= 0 ||
+                   L.desc.views_pe_degree > 10))
+        return false;
+    return L.Dp + (L.vdep ? 2 : 0) <= tc::kFusedMaxLayers;
+}
+
+// The whole forward in one launch: the layer program of the kernel from the
+// per-layer description, the weight maps, and with store the maps of every
+// activation the backward reads (same buffers and layouts as the per-layer path).
+int launch_fused(const MlpLayout& L, const TcLayout& T, const float* const* P, const TcWs& w, int64_t m,
+                 const float* noise, float* sigma, float* rgb, bool store, const TcCtx& cx, cudaStream_t s) {
+    if (m <= 0) return SRF_OK;
+    tc::FusedProgram pr{};
+    static tc::FusedMaps maps_zero{};
+    tc::FusedMaps maps = maps_zero;
+    int head_off = 0, bias_off = 0;
+    const int last_enc = L.skip >= 0 ? L.skip + 1 : 0;   // the last layer that reads PE(points)
+    auto add = [&](int kind, const op16* wp, int kpad, int n, int ext_kb, int ext_src, int ext_wait, int head,
+                   const float* bias, const float* hw, const float* hb, int enc_last, op16* out, uint32_t* bits) {
+        const int l = pr.nl++;
+        tc::FusedLayer& F = pr.layer[l];
+        F.kind = kind;
+        F.kb = kpad / 64;
+        F.ext_kb = ext_kb;
+        F.ext_src = ext_src;
+        F.ext_wait = ext_wait;
+        F.n = n;
+        F.head = head;
+        F.enc_last = enc_last;
+        F.bias_off = bias_off;
+        F.head_off = head_off;
+        bias_off += n;
+        head_off += tc::head_units(head) * n;
+        pr.bias[l] = bias;
+        pr.head_w[l] = hw;
+        pr.head_b[l] = hb;
+        pr.bits_out[l] = store ? bits : nullptr;
+        pr.out[l] = store ? out : nullptr;
+        return make_map(&maps.w[l], wp, uint64_t(kpad), uint64_t(n), uint64_t(kpad) * 2, 64, uint32_t(n));
+    };
+    bool ok = true;
+    for (int j = 0; j < L.Dp; ++j) {
+        const bool last = j == L.Dp - 1;
+        const int head = last ? (L.vdep ? tc::kHeadSigma : tc::kHeadSigmaRgb) : tc::kHeadNone;
+        const int kind = last ? (L.vdep ? tc::kFusedSigma : tc::kFusedSigmaRgb) : tc::kFusedPlain;
+        const bool enc_in = j == 0 || j - 1 == L.skip;
+        ok = ok && add(kind, w.W[j], T.trunk[j].kpad(), 256, enc_in ? 0 : -1, 0, j == 0, head, P[L.idx_trunk_w(j) + 1],
+                       last ? P[L.idx_out_w()] : nullptr, last ? P[L.idx_out_w() + 1] : nullptr, j == last_enc,
+                       w.h[j], (j + 1 < L.Dp || L.vdep) && store ? w.hbits[j] : nullptr);
+    }
+    if (L.vdep) {
+        ok = ok && add(tc::kFusedLinear, w.Wf, L.Wp, 256, -1, 0, 0, tc::kHeadNone, P[L.idx_feat_w() + 1], nullptr,
+                       nullptr, 0, w.feat, nullptr);
+        ok = ok && add(tc::kFusedView, w.Wv[0], T.view[0].kpad(), 128, 4, 1, 1, tc::kHeadRgb, P[L.idx_view_w(0) + 1],
+                       P[L.idx_rgb_w()], P[L.idx_rgb_w() + 1], 0, w.hv[0], nullptr);
+    }
+    if (!ok) return SRF_ERR_CUDA;
+    if (head_off > tc::kFusedHeadFloats || bias_off > tc::kFusedBiasFloats) return SRF_ERR_UNSUPPORTED;
+    // the encodings the standalone encoder wrote: [m, 64] 16-bit rows, 128-row boxes
+    if (!make_map(&maps.enc, w.enc, uint64_t(T.enc_w), uint64_t(m), uint64_t(T.enc_w) * 2, 64, 128))
+        return SRF_ERR_CUDA;
+    if (L.vdep && !make_map(&maps.vx, w.vext, uint64_t(T.vx_w), uint64_t(m), uint64_t(T.vx_w) * 2, 64, 128))
+        return SRF_ERR_CUDA;
+    pr.fmt = cx.fmt;
+    pr.has_vx = L.vdep ? 1 : 0;
+    // the next tile's ENC once the tile's last ENC reader is two layers back (its MMAs are
+    // then complete), VX two layers into the tile (the previous tile's view layer is done)
+    pr.enc_at = last_enc + 2 < pr.nl ? last_enc + 2 : pr.nl;
+    pr.vx_at = pr.nl - 1 < 2 ? pr.nl - 1 : 2;
+    pr.has_noise = noise != nullptr;
+    pr.M = m;
+    pr.noise = noise;
+    pr.sraw = w.sraw;
+    pr.sigma = sigma;
+    pr.rgb_ws = w.rgb;
+    pr.rgb_out = rgb;
+    pr.found_inf = cx.found_inf();
+    pr.flag = device_flag();
+    static bool attr_done[2] = {false, false};
+    auto kern = store ? tc::mlp_fused_kernel<true> : tc::mlp_fused_kernel<false>;
+    if (!attr_done[store]) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kFusedSmem));
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return SRF_ERR_CUDA;
+        }
+        attr_done[store] = true;
+    }
+    const int64_t tiles = (m + 127) / 128;
+    const int grid = int(tiles < num_sms() ? tiles : num_sms());
+    kern<<<grid, tc::kFusedThreads, tc::kFusedSmem, s>>>(maps, pr);
+    return launch_status();
+}
+
 }  // namespace
 
 size_t mlp_tc_workspace(const MlpLayout& L, int64_t m, bool bwd) {
@@ -758,6 +868,8 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
             vx, w.enc, L.vdep ? w.vext : nullptr, fmt);
     }
     if ((st = launch_status())) return st;
+    const int fused = g_mlp_fused.load();
+    if (fused >= (bwd ? 2 : 1) && fused_fits(L, T)) return launch_fused(L, T, P, w, m, noise, sigma, rgb, bwd, cx, s);
     for (int j = 0; j < L.Dp; ++j) {
         const LayerMap& lm = T.trunk[j];
         const op16* x0 = j == 0 || j - 1 == L.skip ? w.enc : w.h[j - 1];
@@ -2301,6 +2413,13 @@ extern "C" int srf_tensorf_renderer_forward(const srf_tensorf_renderer_desc* d, 
     return render_tc_forward(d->n_comp, d->features, d->units, d->features_pe_degree, d->views_pe_degree,
                              d->view_dependent, params, feats, view_dirs, m, rgb, for_backward != 0, workspace,
                              workspace_bytes, fmt, scaler, as_stream(stream));
+}
+
+extern "C" int srf_nerf_mlp_fused_path(int mode) {
+    if (mode > 2) return SRF_ERR_SHAPE;
+    const int prev = g_mlp_fused.load();
+    if (mode >= 0) g_mlp_fused.store(mode);
+    return prev;
 }
 
 extern "C" int srf_tensorf_basis_adjoint_path(int tensor_cores) {

@@ -111,9 +111,14 @@ def main(argv=None):
     ap.add_argument('--reps', type=int, default=2)
     ap.add_argument('--fp32-rays', type=int, default=4 * 65536,
                     help='rays of the image rendered by the FP32 plain path (a prefix of the full set)')
+    ap.add_argument('--mlp-path', default='default', choices=['default', 'fused', 'layers'],
+                    help='16-bit MLP forward: the library default (fused for forward-only calls), the fused '
+                         'kernel for every forward, or one kernel per layer')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
+    if args.mlp_path != 'default':
+        _lib.load().srf_nerf_mlp_fused_path(2 if args.mlp_path == 'fused' else 0)
     dev = torch.device('cuda')
     pid, intr, ext = synthetic_views(args.views, args.height, args.width, device=dev)
     o, d = pixel_rays(pid, intr, ext)

@@ -446,7 +446,7 @@ def main(argv=None):
     """Run a fused training step on synthetic data and print ms/step:
 
         python -m simple_rf_gb300.train_step --rays 4096 --steps 10 --warmup 3 [--precision fp32] [--eager]
-            [--config nerf|nerf_pair]
+            [--config nerf|nerf_pair] [--mlp-path default|fused|layers]
     """
     import argparse
     import json
@@ -457,9 +457,14 @@ def main(argv=None):
     ap.add_argument('--precision', default='bf16', choices=['bf16', 'fp16', 'fp32'])
     ap.add_argument('--eager', action='store_true', help='launch kernels directly instead of replaying a CUDA graph')
     ap.add_argument('--config', default='nerf', choices=['nerf', 'nerf_pair'])
+    ap.add_argument('--mlp-path', default='default', choices=['default', 'fused', 'layers'],
+                    help='16-bit MLP forward: the library default (fused for forward-only calls), the fused '
+                         'kernel for every forward, or one kernel per layer')
     args = ap.parse_args(argv)
     from . import build as _build
     _build.build()
+    if args.mlp_path != 'default':
+        _lib.load().srf_nerf_mlp_fused_path(2 if args.mlp_path == 'fused' else 0)
     dev = torch.device('cuda')
     step, batch_fn = make_step(args.config, args.rays, args.precision, dev)
     step.set_batch(*batch_fn(1, dev))

@@ -2,10 +2,12 @@
 the backward would keep, the forward stores nothing and the backward recomputes
 each ray chunk's activations before its adjoint.
 
-Bars: sigma/rgb bit-identical to the stored-activation pass (same kernels on the
-same rows); parameter gradients within 1e-5 (FP32) / 1e-4 (16-bit operands)
-relative L2 of the stored-activation pass -- only the grouping of the sum over
-samples differs."""
+Bars: sigma/rgb bit-identical to the stored-activation pass in FP32 (same
+kernels on the same rows) and within 1e-6 relative with 16-bit operands (the
+forward that stores nothing runs the fused MLP kernel, whose head dot products
+sum their partials in another order than the per-layer kernels); parameter
+gradients within 1e-5 (FP32) / 1e-4 (16-bit operands) relative L2 of the
+stored-activation pass -- only the grouping of the sum over samples differs."""
 import numpy as np
 import pytest
 import torch
@@ -53,7 +55,11 @@ def test_recomputed_backward_matches_stored_activations(precision):
     assert rows == 3 * 384 and m % rows != 0  # 11 chunks, the last one partial
     s0, r0, g0 = _run(spec, prec, pts, vd, div, p64, cs, cr, 2 * full)
     s1, r1, g1 = _run(spec, prec, pts, vd, div, p64, cs, cr, budget)
-    assert torch.equal(s0, s1) and torch.equal(r0, r1)
+    if precision == 'fp32':
+        assert torch.equal(s0, s1) and torch.equal(r0, r1)
+    else:
+        torch.testing.assert_close(s1, s0, rtol=1e-6, atol=1e-6 * max(1.0, float(s0.abs().max())))
+        torch.testing.assert_close(r1, r0, rtol=1e-6, atol=1e-6)
     bar = 1e-5 if precision == 'fp32' else 1e-4
     for name, a, b in zip(spec.param_names, g0, g1):
         rel = float(torch.linalg.norm(a - b) / torch.linalg.norm(a).clamp_min(1e-30))
