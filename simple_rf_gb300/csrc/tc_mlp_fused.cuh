@@ -287,14 +287,14 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         // ENC / VX of tile `tile` (the n-th load of that slab) once the MMAs that read the
         // previous contents are done; every copy is waited for before the CTA exits
         auto load_enc = [&](int64_t tile, uint32_t n) {
-            if (n > 0 && !mbar_wait(enc_empty, (n - 1) & 1, abort_flag)) return false;
+            if (n > 0 && !mbar_wait_sleep(enc_empty, (n - 1) & 1, abort_flag)) return false;
             mbar_arrive_expect_tx(enc_full, kActBlockBytes);
             tma_load_2d(enc, &maps.enc, enc_full, 0, int32_t(tile * 128));
             ++enc_loads;
             return true;
         };
         auto load_vx = [&](int64_t tile, uint32_t n) {
-            if (n > 0 && !mbar_wait(vx_empty, (n - 1) & 1, abort_flag)) return false;
+            if (n > 0 && !mbar_wait_sleep(vx_empty, (n - 1) & 1, abort_flag)) return false;
             mbar_arrive_expect_tx(vx_full, kActBlockBytes);
             tma_load_2d(vx, &maps.vx, vx_full, 0, int32_t(tile * 128));
             ++vx_loads;
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                 for (int kb = 0; kb < L.kb; ++kb, ++it) {
                     const int s = int(it % kFusedStages);
                     const uint32_t ph = (it / kFusedStages) & 1;
-                    if (!mbar_wait(&wempty[s], ph ^ 1, abort_flag)) {
+                    if (!mbar_wait_sleep(&wempty[s], ph ^ 1, abort_flag)) {
                         ok = false;
                         break;
                     }
@@ -325,9 +325,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         if (!ok) *abort_flag = 1;
         // every copy this thread started has landed before the CTA may exit
         for (int s = 0; s < kFusedStages; ++s)
-            if (used[s] && !mbar_wait(&wfull[s], last_parity[s], nullptr)) *abort_flag = 1;
-        if (enc_loads && !mbar_wait(enc_full, (enc_loads - 1) & 1, nullptr)) *abort_flag = 1;
-        if (vx_loads && !mbar_wait(vx_full, (vx_loads - 1) & 1, nullptr)) *abort_flag = 1;
+            if (used[s] && !mbar_wait_sleep(&wfull[s], last_parity[s], nullptr)) *abort_flag = 1;
+        if (enc_loads && !mbar_wait_sleep(enc_full, (enc_loads - 1) & 1, nullptr)) *abort_flag = 1;
+        if (vx_loads && !mbar_wait_sleep(vx_full, (vx_loads - 1) & 1, nullptr)) *abort_flag = 1;
     } else if (warp == 1 && lane == 0) {
         // ------------------------------------------------------------------ MMA
         uint32_t it = 0, g = 0, act_seq = 0, enc_seq = 0, vx_seq = 0;   // enc / vx: loads consumed
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
             for (int l = 0; ok && l < P.nl; ++l, ++g) {
                 const FusedLayer& L = P.layer[l];
                 const uint32_t a = g & 1;
-                if (!mbar_wait(&acc_empty[a], ((g >> 1) & 1) ^ 1, abort_flag)) {
+                if (!mbar_wait_sleep(&acc_empty[a], ((g >> 1) & 1) ^ 1, abort_flag)) {
                     ok = false;
                     break;
                 }
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                         if (L.ext_wait) {
                             uint64_t* rdy = L.ext_src ? vx_full : enc_full;
                             uint32_t& seq = L.ext_src ? vx_seq : enc_seq;
-                            if (!mbar_wait(rdy, seq & 1, abort_flag)) {
+                            if (!mbar_wait_sleep(rdy, seq & 1, abort_flag)) {
                                 ok = false;
                                 break;
                             }
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                         }
                         a_addr = smem_u32(L.ext_src ? vx : enc);
                     } else {
-                        if (!mbar_wait(&act_ready[ab], act_seq & 1, abort_flag)) {
+                        if (!mbar_wait_sleep(&act_ready[ab], act_seq & 1, abort_flag)) {
                             ok = false;
                             break;
                         }
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                         ++ab;
                     }
                     const int s = int(it % kFusedStages);
-                    if (!mbar_wait(&wfull[s], (it / kFusedStages) & 1, abort_flag)) {
+                    if (!mbar_wait_sleep(&wfull[s], (it / kFusedStages) & 1, abort_flag)) {
                         ok = false;
                         break;
                     }
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         if (!ok) *abort_flag = 1;
         // all MMAs issued by this thread complete before tensor memory is freed
         mma_commit(done);
-        if (!mbar_wait(done, 0, nullptr)) *abort_flag = 1;
+        if (!mbar_wait_sleep(done, 0, nullptr)) *abort_flag = 1;
     } else if (warp >= 2) {
         // ------------------------------------------------------------- epilogue
         FusedEpi e;
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                 const FusedLayer& L = P.layer[l];
                 const uint32_t a = g & 1;
                 const bool act_out = l + 1 < P.nl;
-                if (!mbar_wait(&acc_full[a], (g >> 1) & 1, abort_flag)) {
+                if (!mbar_wait_sleep(&acc_full[a], (g >> 1) & 1, abort_flag)) {
                     ok = false;
                     break;
                 }
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
 #pragma unroll
                         for (int u = 0; u < 4; ++u) x[u] = hp[u];
                         mbar_arrive(rdy);
-                    } else if (mbar_wait(rdy, (hx_seq >> 1) & 1, abort_flag)) {
+                    } else if (mbar_wait_sleep(rdy, (hx_seq >> 1) & 1, abort_flag)) {
 #pragma unroll
                         for (int u = 0; u < 4; ++u) hp[u] += x[u];
                         if (e.live) {

@@ -47,6 +47,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait with a suspend-time hint: a thread whose phase is not complete sleeps
+// until it completes or the hint (ns) runs out, instead of re-polling the barrier.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ uint64_t globaltimer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -64,6 +78,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
     for (uint32_t i = 0;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((i & 255) == 255) {
+            if (abort_flag && *abort_flag) return false;
+            uint64_t now = globaltimer_ns();
+            if (start == 0) start = now;
+            else if (now - start > kWaitNs) return false;
+        }
+    }
+}
+
+// The bounded wait of mbar_wait with sleeping polls (up to 20 us a poll): fewer
+// shared-memory barrier reads while the waiting role has nothing to do.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    uint64_t start = 0;
+    for (uint32_t i = 0;; ++i) {
+        if (mbar_try_wait_sleep(bar, parity, 20000u)) return true;
+        if ((i & 15) == 15) {
             if (abort_flag && *abort_flag) return false;
             uint64_t now = globaltimer_ns();
             if (start == 0) start = now;
