@@ -286,31 +286,64 @@ __global__ void pack_weight_kernel(LayerMap L, const float* __restrict__ w, op16
     wt[int64_t(kp) * L.n + n] = b;
 }
 
-// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns.
-// A block covers 32 columns of one row n: warp w sums splits w, w + 4, ... (lane =
-// column, coalesced), and the four partial sums meet in shared memory.
-__global__ void __launch_bounds__(128) reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits,
-                                                           int n_dz, float* grad, const float* gscale) {
-    __shared__ float part[4][32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int kp = blockIdx.x * 32 + lane;
+// Up to kPackBatch layers' W -> (Wp, WT) in one launch (blockIdx.z = layer).
+constexpr int kPackBatch = 12;
+struct PackBatch {
+    LayerMap lm[kPackBatch];
+    const float* w[kPackBatch];
+    op16* wp[kPackBatch];
+    op16* wt[kPackBatch];
+};
+
+__global__ void pack_weights_kernel(const __grid_constant__ PackBatch b, int fmt) {
+    const LayerMap& L = b.lm[blockIdx.z];
+    const int kp = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = blockIdx.y;
     const int kpad = L.kpad();
-    float acc = 0.f;
+    if (kp >= kpad || n >= L.n) return;
+    const int rc = ref_col(L, kp);
+    const float v = rc >= 0 ? b.w[blockIdx.z][int64_t(n) * L.kref() + rc] : 0.f;
+    const op16 h = tc::to16(v, fmt);
+    b.wp[blockIdx.z][int64_t(n) * kpad + kp] = h;
+    b.wt[blockIdx.z][int64_t(kp) * L.n + n] = h;
+}
+
+// grad[n, ref] += sum_s partial[s, n, kp] (times 1 / loss scale when gscale) for the mapped columns.
+// A block covers 128 columns of one row n: lane j of warp w adds the 16-byte column
+// quads 4j .. 4j + 3 of splits w, w + 4, ... (512 coalesced bytes a warp load), and the
+// four partial sums meet in shared memory (the same order of additions per column as
+// one column per lane).  kpad is a multiple of 64, so a quad is whole or absent.
+__global__ void __launch_bounds__(128) reduce_wgrad_kernel(LayerMap L, const float* __restrict__ partial, int splits,
+                                                           int n_dz, float* grad, const float* gscale) {
+    __shared__ float4 part[4][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int kp = blockIdx.x * 128 + lane * 4;
+    const int n = blockIdx.y;
+    const int kpad = L.kpad();
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (kp < kpad) {
-        const float* src = partial + int64_t(n) * kpad + kp;
-        const int64_t step = int64_t(n_dz) * kpad;
-#pragma unroll 8
-        for (int sp = warp; sp < splits; sp += 4) acc += src[sp * step];
+        const float4* src = reinterpret_cast<const float4*>(partial + int64_t(n) * kpad + kp);
+        const int64_t step = int64_t(n_dz) * kpad / 4;
+#pragma unroll 4
+        for (int sp = warp; sp < splits; sp += 4) {
+            const float4 v = src[sp * step];
+            acc.x += v.x;
+            acc.y += v.y;
+            acc.z += v.z;
+            acc.w += v.w;
+        }
     }
     part[warp][lane] = acc;
     __syncthreads();
     if (warp == 0 && kp < kpad) {
-        const int rc = ref_col(L, kp);
-        if (rc >= 0) {
-            float sum = part[0][lane] + part[1][lane] + part[2][lane] + part[3][lane];
-            if (gscale) sum *= gscale[1];
-            grad[int64_t(n) * L.kref() + rc] += sum;
+        const float4 a = part[0][lane], b = part[1][lane], c = part[2][lane], d = part[3][lane];
+        const float sums[4] = {a.x + b.x + c.x + d.x, a.y + b.y + c.y + d.y, a.z + b.z + c.z + d.z,
+                               a.w + b.w + c.w + d.w};
+        const float gs = gscale ? gscale[1] : 1.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int rc = ref_col(L, kp + q);
+            if (rc >= 0) grad[int64_t(n) * L.kref() + rc] += gscale ? sums[q] * gs : sums[q];
         }
     }
 }
@@ -705,6 +738,28 @@ int pack(const LayerMap& lm, const float* w, op16* wp, op16* wt, int fmt, cudaSt
     return launch_status();
 }
 
+// Every layer of an MLP packed in ceil(layers / kPackBatch) launches.
+int pack_all(const std::vector<LayerMap>& lms, const std::vector<const float*>& ws, const std::vector<op16*>& wps,
+             const std::vector<op16*>& wts, int fmt, cudaStream_t s) {
+    for (size_t i0 = 0; i0 < lms.size(); i0 += kPackBatch) {
+        PackBatch b{};
+        int kmax = 0, nmax = 0, cnt = 0;
+        for (size_t i = i0; i < lms.size() && cnt < kPackBatch; ++i, ++cnt) {
+            b.lm[cnt] = lms[i];
+            b.w[cnt] = ws[i];
+            b.wp[cnt] = wps[i];
+            b.wt[cnt] = wts[i];
+            kmax = lms[i].kpad() > kmax ? lms[i].kpad() : kmax;
+            nmax = lms[i].n > nmax ? lms[i].n : nmax;
+        }
+        dim3 grid((kmax + 127) / 128, nmax, cnt);
+        pack_weights_kernel<<<grid, 128, 0, s>>>(b, fmt);
+        int st = launch_status();
+        if (st) return st;
+    }
+    return SRF_OK;
+}
+
 // Operand format and loss scaler of one forward/backward call.
 struct TcCtx {
     int fmt;
@@ -722,7 +777,7 @@ int wgrad_layer(const LayerMap& lm, float* partial, size_t partial_floats, const
     int st = tc_wgrad(partial, partial_floats, dz, lm.n, lm.n, x0, ld0, lm.padw[0], x1, ld1,
                       lm.nsrc > 1 ? lm.padw[1] : 0, M, &splits, s, cx.fmt, bias_grad, cx.gscale());
     if (st) return st;
-    dim3 grid((lm.kpad() + 31) / 32, lm.n);
+    dim3 grid((lm.kpad() + 127) / 128, lm.n);
     reduce_wgrad_kernel<<<grid, 128, 0, s>>>(lm, partial, splits, lm.n, grad, cx.gscale());
     return launch_status();
 }
@@ -853,12 +908,29 @@ int mlp_tc_forward(const MlpLayout& L, const float* const* P, const float* pts, 
     TcWs w;
     if (carve_tc(L, T, m, bwd, ws, ws_bytes, &w) > ws_bytes) return SRF_ERR_WORKSPACE;
     int st;
-    for (int j = 0; j < L.Dp; ++j)
-        if ((st = pack(T.trunk[j], P[L.idx_trunk_w(j)], w.W[j], w.WT[j], fmt, s))) return st;
-    if (L.vdep) {
-        if ((st = pack(T.feat, P[L.idx_feat_w()], w.Wf, w.WTf, fmt, s))) return st;
-        for (int j = 0; j < L.Dv; ++j)
-            if ((st = pack(T.view[j], P[L.idx_view_w(j)], w.Wv[j], w.WTv[j], fmt, s))) return st;
+    {
+        std::vector<LayerMap> lms;
+        std::vector<const float*> ws;
+        std::vector<op16*> wps, wts;
+        for (int j = 0; j < L.Dp; ++j) {
+            lms.push_back(T.trunk[j]);
+            ws.push_back(P[L.idx_trunk_w(j)]);
+            wps.push_back(w.W[j]);
+            wts.push_back(w.WT[j]);
+        }
+        if (L.vdep) {
+            lms.push_back(T.feat);
+            ws.push_back(P[L.idx_feat_w()]);
+            wps.push_back(w.Wf);
+            wts.push_back(w.WTf);
+            for (int j = 0; j < L.Dv; ++j) {
+                lms.push_back(T.view[j]);
+                ws.push_back(P[L.idx_view_w(j)]);
+                wps.push_back(w.Wv[j]);
+                wts.push_back(w.WTv[j]);
+            }
+        }
+        if ((st = pack_all(lms, ws, wps, wts, fmt, s))) return st;
     }
     {
         const int vx = L.vdep ? T.vx_w : 0;
