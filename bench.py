@@ -281,9 +281,11 @@ def read_probe(dev, nbytes, passes, reps=5):
 
 
 def kernel_rooflines(hbm_peak, peak_kind):
-    """The memory-bound kernels of the path timed alone (CUDA events, 20 launches
-    after 3 warm-up launches) with their algorithmic bytes per launch:
-    compositing forward / adjoint over a 65,536-ray render chunk of 192 samples
+    """Kernels of the path timed alone (CUDA events, 20 launches after 3 warm-up
+    launches): the fused whole-MLP forward of forward-only calls against the
+    tensor peak (4.2M samples of the benchmark network), and the memory-bound
+    ones with their algorithmic bytes per launch: compositing forward / adjoint
+    over a 65,536-ray render chunk of 192 samples
     (302 MB of per-sample inputs, larger than L2), and the TensoRF VM lookups and
     their scatter-add adjoints at the 300^3 grid over 1.25M ray-ordered points
     (R = 48 colour, R = 16 density; the 52 MB of planes stay L2-resident, so
@@ -298,6 +300,19 @@ def kernel_rooflines(hbm_peak, peak_kind):
             ('vm', dict(rays=1216, samples=1024, comps=16, kind='density', res=300, backward=False)),
             ('vm', dict(rays=1216, samples=1024, comps=16, kind='density', res=300, backward=True))]
     out = []
+    # the fused whole-MLP forward (forward-only calls: render, inference) is tensor-bound:
+    # its dense MAC-FLOPs against the measured 16-bit tensor peak
+    r = bk.mlp(_ap.Namespace(m=4194304, mlp_path='fused', store=False, precision='fp16', reps=20, warmup=3))
+    _, tf_peak, tf_kind = peaks()
+    out.append({'kernel': 'mlp_fused_kernel (whole NeRF MLP forward, 8x256 + skip + view layer)',
+                'workload': {'samples': 4194304, 'precision': 'fp16', 'samples_per_view_dir': 64},
+                'launch_ms': round(r['ms'], 4), 'achieved': round(r['tflops'], 1), 'peak': tf_peak,
+                'unit': 'TFLOP/s', 'frac': round(r['tflops'] / tf_peak, 4), 'bound': 'tensor',
+                'peak_source': tf_kind + ' bf16 burst (FP16 runs at the same rate)',
+                'ns_per_sample': round(r['ns_per_sample'], 4),
+                'note': 'includes the standalone encoder launch; per-layer kernels on the same call: '
+                        'see bench_kernels mlp --mlp-path layers'})
+    torch.cuda.empty_cache()
     # the VM planes stay L2-resident: their gathers are bounded by the L2 read rate,
     # measured here with the same 16-byte loads over a 48 MB buffer (read 40 times)
     l2 = read_probe(torch.device('cuda', torch.cuda.current_device()), 48 << 20, 40)
