@@ -90,15 +90,21 @@ def pixel_rays(pid, intr, ext):
     return F.pixel_rays(pid, intr[view].contiguous(), ext[view].contiguous())
 
 
-def _time_render(r, o, d, reps):
+def _time_render(r, o, d, reps, profile=False):
+    """ms per full render after a capture + warm-up chunk; with profile the timed
+    renders are the range a profiler started with profiling off captures."""
     r.render(o[:r.chunk], d[:r.chunk])            # capture + warm-up
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if profile:
+        torch.cuda.profiler.start()
     e0.record()
     for _ in range(reps):
         out = r.render(o, d)
     e1.record()
     e1.synchronize()
+    if profile:
+        torch.cuda.profiler.stop()
     return e0.elapsed_time(e1) / reps, out
 
 
@@ -128,7 +134,7 @@ def main(argv=None):
            'rays': n, 'chunk': args.chunk}
     r = NerfPairRenderer(args.chunk, 'bf16', dev)
     l0 = lib.srf_launch_count()
-    ms, out = _time_render(r, o, d, args.reps)
+    ms, out = _time_render(r, o, d, args.reps, profile=True)
     spr = r.samples_per_ray()
     res['bf16'] = {'ms': round(ms, 3), 'rays_per_s': round(n / ms * 1e3, 1),
                    'samples_per_s': round(n * spr / ms * 1e3, 1), 'samples_per_ray': spr,
