@@ -155,3 +155,39 @@ def test_fused_path_switch_round_trips():
     assert _mode(-1) == 0
     _mode(prev)
     assert _mode(-1) == prev
+
+
+@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('blowup', [1.0, 30.0])
+def test_fp16_overflow_sets_found_inf(mode, blowup):
+    """FP16 forward-only calls report activations beyond the format's range in the
+    loss scaler's found_inf, the fused kernel (mode 1) as the per-layer kernels
+    (mode 0): weights scaled by 30 push the trunk past 65504 within a few layers;
+    the unscaled net leaves the flag clear."""
+    import ctypes
+    from simple_rf_gb300 import _lib
+    from simple_rf_gb300 import functional as F
+    spec = F.MlpSpec()
+    _, params = _params(spec, {}, 12)
+    params = [p * blowup if name.endswith('weight') else p for name, p in zip(spec.param_names, params)]
+    div, m = 64, 64 * 40 + 7
+    pts, vd, _ = _inputs(m, div, 13)
+    tp, tv = torch.from_numpy(pts).to(DEV), torch.from_numpy(vd).to(DEV)
+    sigma = torch.empty(m, device=DEV)
+    rgb = torch.empty(m, 3, device=DEV)
+    prec = _lib.PRECISIONS['fp16']
+    wsb = spec.workspace_bytes(m, prec, False)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=DEV)
+    scaler = torch.zeros(4, dtype=torch.int32, device=DEV)
+    scaler[:2] = torch.tensor([65536.0, 1 / 65536.0], device=DEV).view(torch.int32)
+    arr = (ctypes.c_void_p * len(params))(*[t.data_ptr() for t in params])
+    prev = _mode(mode)
+    try:
+        _lib.call('srf_nerf_mlp_forward', ctypes.byref(spec.desc), arr, ctypes.c_void_p(tp.data_ptr()),
+                  ctypes.c_void_p(tv.data_ptr()), div, m, None, ctypes.c_void_p(sigma.data_ptr()),
+                  ctypes.c_void_p(rgb.data_ptr()), prec, 0, ctypes.c_void_p(ws.data_ptr()), wsb,
+                  ctypes.c_void_p(scaler.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+    finally:
+        _mode(prev)
+    assert int(scaler[2].item()) == (1 if blowup > 1 else 0), (mode, blowup, int(scaler[2].item()))
