@@ -427,17 +427,19 @@ __global__ void __launch_bounds__(kEncRows)
 //                times the loss scale S = gscale[0], 1 when gscale is NULL)
 //   colsum[k] += sum_m dz[m, k] / S                          (that layer's bias gradient, when given)
 //   dW[u, k]  += sum_m g[m, u] h[m, k];  db[u] += sum_m g[m, u]  (the head's own gradients)
-// A warp takes a row at a time with lane j owning columns CPL j .. CPL j + CPL - 1
-// (K = 32 CPL: one coalesced 256- or 512-byte row per access) and keeps four rows'
-// loads in flight; partial sums stay in registers until one shared-memory
+// A warp takes 32 consecutive rows at a time: lane l computes g of row l from
+// coalesced loads of the per-row head values, then the warp walks the rows, four
+// in flight, lane j owning columns CPL j .. CPL j + CPL - 1 (K = 32 CPL: one
+// coalesced 256- or 512-byte row per access) and taking each row's g from its
+// lane by shuffles.  Partial sums stay in registers until one shared-memory
 // reduction over the block's 8 warps at the end.
 template <int NO, int CPL>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, CPL == 4 ? 3 : 2)
     head_bwd_fused_kernel(int64_t M, int K, const float* __restrict__ dsigma, const float* __restrict__ sraw,
                           const float* __restrict__ drgb, const float* __restrict__ rgb, const float* __restrict__ W,
                           const op16* __restrict__ h, op16* dz, float* colsum, float* dW, float* db, int fmt,
                           const float* gscale, int* found_inf) {
-    constexpr int RPP = 4;   // independent rows in flight per warp
+    constexpr int RPP = 4;   // rows in flight per warp
     __shared__ float red[8][256 + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float gs0 = gscale ? gscale[0] : 1.f, gs1 = gscale ? gscale[1] : 1.f;
@@ -455,64 +457,74 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int i = 0; i < CPL; ++i) cs[i] = 0.f;
-    const int64_t wstride = int64_t(gridDim.x) * 8;
-    for (int64_t r0 = int64_t(blockIdx.x) * 8 + warp; r0 < M; r0 += RPP * wstride) {
-        float g[RPP][NO];
-        uint32_t raw[RPP][CPL / 2];
+    const int64_t gstride = int64_t(gridDim.x) * 8 * 32;
+    for (int64_t base = (int64_t(blockIdx.x) * 8 + warp) * 32; base < M; base += gstride) {
+        // g of row base + lane
+        float gl[NO];
+        {
+            const int64_t r = base + lane;
 #pragma unroll
-        for (int t = 0; t < RPP; ++t) {   // every row's loads before any row's arithmetic
-            const int64_t r = r0 + t * wstride;
-            if (r >= M) continue;
-            int u0 = 0;
-            if (NO == 4) {
-                g[t][0] = sraw[r] > 0.f ? dsigma[r] : 0.f;
-                u0 = 1;
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float v = rgb[3 * r + c];
-                g[t][u0 + c] = drgb[3 * r + c] * v * (1.f - v);
-            }
-            const op16* hr = h + r * K + lane * CPL;
-            if (CPL == 8) {
-                const uint4 q = *reinterpret_cast<const uint4*>(hr);
-                raw[t][0] = q.x; raw[t][CPL / 2 > 1 ? 1 : 0] = q.y;
-                raw[t][CPL / 2 > 2 ? 2 : 0] = q.z; raw[t][CPL / 2 > 3 ? 3 : 0] = q.w;
-            } else {
-                const uint2 q = *reinterpret_cast<const uint2*>(hr);
-                raw[t][0] = q.x; raw[t][CPL / 2 > 1 ? 1 : 0] = q.y;
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < RPP; ++t) {
-            const int64_t r = r0 + t * wstride;
-            if (r >= M) continue;
-            uint32_t o[CPL / 2];
-#pragma unroll
-            for (int p = 0; p < CPL / 2; ++p) {
-                const float2 hx = tc::unpack16(raw[t][p], fmt);
-                float v0 = 0.f, v1 = 0.f;
-#pragma unroll
-                for (int u = 0; u < NO; ++u) {
-                    v0 += g[t][u] * w[u][2 * p];
-                    v1 += g[t][u] * w[u][2 * p + 1];
-                    dwl[u][2 * p] += g[t][u] * hx.x;
-                    dwl[u][2 * p + 1] += g[t][u] * hx.y;
+            for (int u = 0; u < NO; ++u) gl[u] = 0.f;
+            if (r < M) {
+                int u0 = 0;
+                if (NO == 4) {
+                    gl[0] = sraw[r] > 0.f ? dsigma[r] : 0.f;
+                    u0 = 1;
                 }
-                v0 = hx.x > 0.f ? v0 * gs0 : 0.f;
-                v1 = hx.y > 0.f ? v1 * gs0 : 0.f;
-                cs[2 * p] += v0;
-                cs[2 * p + 1] += v1;
-                bad |= !(fabsf(v0) <= vmax) || !(fabsf(v1) <= vmax);
-                o[p] = tc::pack16(v0, v1, fmt);
-            }
-            op16* dr = dz + r * K + lane * CPL;
-            if (CPL == 8) *reinterpret_cast<uint4*>(dr) = make_uint4(o[0], o[CPL / 2 > 1 ? 1 : 0],
-                                                                     o[CPL / 2 > 2 ? 2 : 0], o[CPL / 2 > 3 ? 3 : 0]);
-            else *reinterpret_cast<uint2*>(dr) = make_uint2(o[0], o[CPL / 2 > 1 ? 1 : 0]);
-            if (lane == 0) {
 #pragma unroll
-                for (int u = 0; u < NO; ++u) dbl[u] += g[t][u];
+                for (int c = 0; c < 3; ++c) {
+                    const float v = rgb[3 * r + c];
+                    gl[u0 + c] = drgb[3 * r + c] * v * (1.f - v);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < NO; ++u) dbl[u] += gl[u];
+        }
+        const int nrows = M - base < 32 ? int(M - base) : 32;
+        for (int t0 = 0; t0 < nrows; t0 += RPP) {
+            uint32_t raw[RPP][CPL / 2];
+#pragma unroll
+            for (int t = 0; t < RPP; ++t) {   // every row's loads before any row's arithmetic
+                if (t0 + t >= nrows) continue;
+                const op16* hr = h + (base + t0 + t) * K + lane * CPL;
+                if (CPL == 8) {
+                    const uint4 q = *reinterpret_cast<const uint4*>(hr);
+                    raw[t][0] = q.x; raw[t][CPL / 2 > 1 ? 1 : 0] = q.y;
+                    raw[t][CPL / 2 > 2 ? 2 : 0] = q.z; raw[t][CPL / 2 > 3 ? 3 : 0] = q.w;
+                } else {
+                    const uint2 q = *reinterpret_cast<const uint2*>(hr);
+                    raw[t][0] = q.x; raw[t][CPL / 2 > 1 ? 1 : 0] = q.y;
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < RPP; ++t) {
+                float g[NO];   // row t0 + t's head gradients, from its lane
+#pragma unroll
+                for (int u = 0; u < NO; ++u) g[u] = __shfl_sync(0xffffffffu, gl[u], (t0 + t) & 31);
+                if (t0 + t >= nrows) continue;
+                uint32_t o[CPL / 2];
+#pragma unroll
+                for (int p = 0; p < CPL / 2; ++p) {
+                    const float2 hx = tc::unpack16(raw[t][p], fmt);
+                    float v0 = 0.f, v1 = 0.f;
+#pragma unroll
+                    for (int u = 0; u < NO; ++u) {
+                        v0 += g[u] * w[u][2 * p];
+                        v1 += g[u] * w[u][2 * p + 1];
+                        dwl[u][2 * p] += g[u] * hx.x;
+                        dwl[u][2 * p + 1] += g[u] * hx.y;
+                    }
+                    v0 = hx.x > 0.f ? v0 * gs0 : 0.f;
+                    v1 = hx.y > 0.f ? v1 * gs0 : 0.f;
+                    cs[2 * p] += v0;
+                    cs[2 * p + 1] += v1;
+                    bad |= !(fabsf(v0) <= vmax) || !(fabsf(v1) <= vmax);
+                    o[p] = tc::pack16(v0, v1, fmt);
+                }
+                op16* dr = dz + (base + t0 + t) * K + lane * CPL;
+                if (CPL == 8) *reinterpret_cast<uint4*>(dr) = make_uint4(o[0], o[CPL / 2 > 1 ? 1 : 0],
+                                                                         o[CPL / 2 > 2 ? 2 : 0], o[CPL / 2 > 3 ? 3 : 0]);
+                else *reinterpret_cast<uint2*>(dr) = make_uint2(o[0], o[CPL / 2 > 1 ? 1 : 0]);
             }
         }
     }
@@ -533,9 +545,12 @@ __global__ void __launch_bounds__(256)
     if (colsum) reduce(cs, colsum, gs1);
 #pragma unroll
     for (int u = 0; u < NO; ++u) reduce(dwl[u], dW + u * K, 1.f);
-    if (lane == 0) {
 #pragma unroll
-        for (int u = 0; u < NO; ++u) atomicAdd(db + u, dbl[u]);
+    for (int u = 0; u < NO; ++u) {
+        float v = dbl[u];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) atomicAdd(db + u, v);
     }
 }
 
@@ -545,7 +560,7 @@ int head_bwd_fused(int64_t M, int K, const float* dsigma, const float* sraw, con
                    const float* gscale, int* found_inf, cudaStream_t s) {
     if (K != 128 && K != 256) return SRF_ERR_UNSUPPORTED;
     if (M <= 0) return SRF_OK;
-    int64_t blocks = (M + 31) / 32;
+    int64_t blocks = (M + 255) / 256;   // 8 warps of 32 rows
     if (blocks > int64_t(num_sms()) * 8) blocks = int64_t(num_sms()) * 8;
     if (K == 128)
         head_bwd_fused_kernel<NO, 4><<<unsigned(blocks), 256, 0, s>>>(M, K, dsigma, sraw, drgb, rgb, W, h, dz, colsum,
