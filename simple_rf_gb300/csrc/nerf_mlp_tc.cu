@@ -574,37 +574,40 @@ int head_bwd_fused(int64_t M, int K, const float* dsigma, const float* sraw, con
 // Sigma head gradients (SimpleNeRF17.py:735-741 adjoint): with g[m] = dsigma[m] when
 // the raw sigma is positive (the ReLU), else 0, dW[k] += sum_m g[m] h[m, k] and
 // db += sum_m g[m] over the last trunk layer's stored 16-bit rows h (K columns,
-// K = 8 x 32).  A warp per row and 8 columns per lane, two rows in flight per warp;
-// the block's sums go out with one atomic per column.
+// K = 8 x 32).  A warp takes 32 consecutive rows: lane l computes g of row l from
+// coalesced loads, then the warp walks the rows, four in flight, 8 columns a lane,
+// taking each row's g by a shuffle; the block's sums go out with one atomic per column.
 __global__ void __launch_bounds__(256) sigma_head_wgrad_kernel(int64_t M, int K, const float* __restrict__ dsigma,
                                                                const float* __restrict__ sraw,
                                                                const op16* __restrict__ h, float* dW, float* db,
                                                                int fmt) {
+    constexpr int RPP = 4;
     __shared__ float red[8][256 + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gsum = 0.f;
-    const int64_t stride = int64_t(gridDim.x) * 8;
-    for (int64_t r0 = int64_t(blockIdx.x) * 8 + warp; r0 < M; r0 += 2 * stride) {
-        const int64_t rows[2] = {r0, r0 + stride};
-        float g[2] = {0.f, 0.f};
-        uint4 raw[2];
+    const int64_t gstride = int64_t(gridDim.x) * 8 * 32;
+    for (int64_t base = (int64_t(blockIdx.x) * 8 + warp) * 32; base < M; base += gstride) {
+        const int64_t rl = base + lane;
+        const float gl = rl < M && sraw[rl] > 0.f ? dsigma[rl] : 0.f;
+        gsum += gl;
+        const int nrows = M - base < 32 ? int(M - base) : 32;
+        for (int t0 = 0; t0 < nrows; t0 += RPP) {
+            uint4 raw[RPP];
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            if (rows[t] >= M) continue;
-            g[t] = sraw[rows[t]] > 0.f ? dsigma[rows[t]] : 0.f;
-            raw[t] = *reinterpret_cast<const uint4*>(h + rows[t] * K + lane * 8);
-        }
+            for (int t = 0; t < RPP; ++t)
+                if (t0 + t < nrows) raw[t] = *reinterpret_cast<const uint4*>(h + (base + t0 + t) * K + lane * 8);
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            if (rows[t] >= M || g[t] == 0.f) continue;
-            const uint32_t w4[4] = {raw[t].x, raw[t].y, raw[t].z, raw[t].w};
+            for (int t = 0; t < RPP; ++t) {
+                const float g = __shfl_sync(0xffffffffu, gl, (t0 + t) & 31);
+                if (t0 + t >= nrows || g == 0.f) continue;
+                const uint32_t w4[4] = {raw[t].x, raw[t].y, raw[t].z, raw[t].w};
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float2 f = tc::unpack16(w4[q], fmt);
-                acc[2 * q] += g[t] * f.x;
-                acc[2 * q + 1] += g[t] * f.y;
+                for (int q = 0; q < 4; ++q) {
+                    const float2 f = tc::unpack16(w4[q], fmt);
+                    acc[2 * q] += g * f.x;
+                    acc[2 * q + 1] += g * f.y;
+                }
             }
-            gsum += g[t];
         }
     }
 #pragma unroll
@@ -616,6 +619,8 @@ __global__ void __launch_bounds__(256) sigma_head_wgrad_kernel(int64_t M, int K,
         for (int w = 0; w < 8; ++w) s += red[w][threadIdx.x];
         atomicAdd(dW + threadIdx.x, s);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xffffffffu, gsum, o);
     if (lane == 0) atomicAdd(db, gsum);
 }
 
@@ -623,8 +628,8 @@ int sigma_head_wgrad(int64_t M, int K, const float* dsigma, const float* sraw, c
                      int fmt, cudaStream_t s) {
     if (K != 256) return SRF_ERR_UNSUPPORTED;
     if (M <= 0) return SRF_OK;
-    int64_t blocks = (M + 15) / 16;
-    if (blocks > int64_t(num_sms()) * 4) blocks = int64_t(num_sms()) * 4;
+    int64_t blocks = (M + 255) / 256;   // 8 warps of 32 rows
+    if (blocks > int64_t(num_sms()) * 6) blocks = int64_t(num_sms()) * 6;
     sigma_head_wgrad_kernel<<<unsigned(blocks), 256, 0, s>>>(M, K, dsigma, sraw, h, dW, db, fmt);
     return launch_status();
 }
