@@ -196,7 +196,8 @@ int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* const* para
  * branch other than one 128-wide layer) always run per layer.  The paths form
  * the same products in the same order and round the same activations; the head
  * dot products sum their partials in another order (last-bit differences).
- * Returns the previous mode; mode < 0 only queries.  Process-wide setting. */
+ * Returns the previous mode (0..2); mode < 0 only queries; a mode above 2 changes
+ * nothing and returns -SRF_ERR_SHAPE.  Process-wide setting. */
 int srf_nerf_mlp_fused_path(int mode);
 
 /* Backward: dsigma (m) w.r.t. the ReLU'd sigma, drgb (m,3) w.r.t. the sigmoid

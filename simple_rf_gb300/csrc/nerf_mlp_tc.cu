@@ -2508,7 +2508,7 @@ extern "C" int srf_tensorf_renderer_forward(const srf_tensorf_renderer_desc* d, 
 }
 
 extern "C" int srf_nerf_mlp_fused_path(int mode) {
-    if (mode > 2) return SRF_ERR_SHAPE;
+    if (mode > 2) return -SRF_ERR_SHAPE;   // negative: apart from the modes 0..2
     const int prev = g_mlp_fused.load();
     if (mode >= 0) g_mlp_fused.store(mode);
     return prev;

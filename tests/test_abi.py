@@ -63,6 +63,23 @@ def test_host_side_validation_without_gpu(lib):
     assert lib.srf_compact(None, 10, None, None, None, 0, None) == 1
 
 
+def test_mlp_fused_path_switch(lib):
+    """The MLP forward-path switch is host state only: it round-trips, queries with a
+    negative mode, and rejects modes above 2 with a negative status (apart from the
+    modes it returns)."""
+    prev = lib.srf_nerf_mlp_fused_path(-1)
+    assert prev in (0, 1, 2)
+    try:
+        assert lib.srf_nerf_mlp_fused_path(0) == prev
+        assert lib.srf_nerf_mlp_fused_path(2) == 0
+        assert lib.srf_nerf_mlp_fused_path(-1) == 2
+        assert lib.srf_nerf_mlp_fused_path(3) == -2
+        assert lib.srf_nerf_mlp_fused_path(-1) == 2
+    finally:
+        lib.srf_nerf_mlp_fused_path(prev)
+    assert lib.srf_nerf_mlp_fused_path(-1) == prev
+
+
 def test_mlp_descriptor_and_workspace(lib):
     from simple_rf_gb300 import _lib
     d = _lib.NerfMlpDesc(8, 256, 1, 128, 10, 4, -1, 1, 1, 4)
