@@ -153,21 +153,24 @@ __device__ __forceinline__ void fused_step(const FusedProgram& P, int l, bool ac
     }
 #pragma unroll
     for (int u = 0; u < UNITS; ++u) {
+        // four independent partial sums (short dependency chains), then their sum
         const float4* w4 = reinterpret_cast<const float4*>(hw + u * N + c * 32);
-        float sacc = 0.f;
+        float s4[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const float4 w = w4[g];
-            sacc += v[4 * g] * w.x;
-            sacc += v[4 * g + 1] * w.y;
-            sacc += v[4 * g + 2] * w.z;
-            sacc += v[4 * g + 3] * w.w;
+            s4[0] += v[4 * g] * w.x;
+            s4[1] += v[4 * g + 1] * w.y;
+            s4[2] += v[4 * g + 2] * w.z;
+            s4[3] += v[4 * g + 3] * w.w;
         }
-        hp[u] += sacc;
+        hp[u] += (s4[0] + s4[1]) + (s4[2] + s4[3]);
     }
     if (check) {
+        float m4[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int j = 0; j < 32; ++j) e.mx = max_nan(e.mx, fabsf(v[j]));
+        for (int j = 0; j < 32; ++j) m4[j & 3] = max_nan(m4[j & 3], fabsf(v[j]));
+        e.mx = max_nan(e.mx, max_nan(max_nan(m4[0], m4[1]), max_nan(m4[2], m4[3])));
     }
     if (act_out || (STORE && e.live)) {
         uint8_t* row = act + size_t(i) * kActBlockBytes + e.r * 128;
