@@ -34,14 +34,17 @@ typedef enum {
     SRF_ERR_UNSUPPORTED = 8    /* configuration valid in the reference, not here   */
 } srf_status;
 
-/* Human-readable name of a status code (static string). */
+/* Library utilities, no reference counterpart.  Human-readable name of a status
+ * code (static string). */
 const char* srf_status_string(int status);
-/* Library version, e.g. "srf_gb300 1.0 sm_103a". */
+/* Library version, e.g. "srf_gb300 1.0 sm_103a" (no reference counterpart). */
 const char* srf_version(void);
-/* Text of the last CUDA error seen by this thread (static thread-local buffer). */
+/* Text of the last CUDA error seen by this thread (static thread-local buffer;
+ * no reference counterpart). */
 const char* srf_last_cuda_error(void);
 /* Number of kernels this library has launched (or captured into a graph) in
- * this process; used to count launches per training step. */
+ * this process; used to count launches per training step (no reference
+ * counterpart). */
 int64_t srf_launch_count(void);
 
 /* Read-bandwidth probe (a measurement utility; no counterpart in the reference):
@@ -150,12 +153,14 @@ typedef struct {
     int32_t growth_tracker;
 } srf_loss_scaler;
 
-/* scaler_dev = {init_scale, 1 / init_scale, 0, 0}. */
+/* scaler_dev = {init_scale, 1 / init_scale, 0, 0} (torch.cuda.amp.GradScaler's
+ * constructor, torch/amp/grad_scaler.py). */
 int srf_loss_scaler_init(srf_loss_scaler* scaler_dev, float init_scale, void* stream);
-/* Per-call scale for a backward whose gradients have no running scale: the
- * largest |value| over a (na) and b (nb) maps to within a factor 2 below
- * target, scale = 2^floor(log2(target / max)) in [2^-24, 2^40] (1 when max is 0);
- * found_inf and growth_tracker are cleared. */
+/* Per-call scale for a backward whose gradients have no running scale (no
+ * reference counterpart: the reference trains in FP32): the largest |value| over
+ * a (na) and b (nb) maps to within a factor 2 below target, scale =
+ * 2^floor(log2(target / max)) in [2^-24, 2^40] (1 when max is 0); found_inf and
+ * growth_tracker are cleared. */
 int srf_loss_scaler_fit(srf_loss_scaler* scaler_dev, const float* a, int64_t na, const float* b, int64_t nb,
                         float target, void* stream);
 /* End of a step: if found_inf, scale *= backoff and growth_tracker = 0, else
@@ -185,8 +190,9 @@ int srf_nerf_mlp_forward(const srf_nerf_mlp_desc* desc, const float* const* para
                          const float* dirs, int dir_div, int64_t m, const float* sigma_noise, float* sigma,
                          float* rgb, int precision, int for_backward, void* workspace, size_t workspace_bytes,
                          srf_loss_scaler* scaler, void* stream);
-/* Forward path of the 16-bit NeRF MLP (BF16 / FP16 precision): mode 0 runs one
- * tcgen05 kernel per layer after the encoder; 1 (default) runs the layers of a
+/* Forward path of the 16-bit NeRF MLP (MLP.forward, SimpleNeRF17.py:696-785, at
+ * BF16 / FP16 precision; the switch itself has no reference counterpart): mode 0
+ * runs one tcgen05 kernel per layer after the encoder; 1 (default) runs the layers of a
  * forward-only call (for_backward = 0) as one fused kernel that keeps each
  * 128-sample tile's activations in shared memory from the encodings to the
  * heads; 2 also fuses the forward of for_backward calls, which then stores the
@@ -294,11 +300,14 @@ typedef struct {
     float mc_weight;
     float* loss;                   /* device float the forward adds the loss value to */
 } srf_composite_loss;
-/* srf_composite_forward that also adds the loss value to *loss->loss. */
+/* srf_composite_forward that also adds the loss value to *loss->loss (the losses
+ * of MSE14.py:81-94, MassConcentrationLoss06.py:63-83 and the depth term above,
+ * evaluated in the compositing epilogue). */
 int srf_composite_forward_loss(const srf_composite_args* args, const srf_composite_loss* loss, void* stream);
 /* srf_composite_backward whose output gradients are the loss's (recomputed from the
- * ray's samples) plus any g_* the args carry (e.g. a depth-consistency term).
- * Both: rays of at most 256 samples (SRF_ERR_UNSUPPORTED beyond). */
+ * ray's samples; the autograd of the same loss modules) plus any g_* the args carry
+ * (e.g. a depth-consistency term, CoarseFineConsistencyLoss33.py:35-44).  Both:
+ * rays of at most 256 samples (SRF_ERR_UNSUPPORTED beyond). */
 int srf_composite_backward_loss(const srf_composite_args* args, const srf_composite_loss* loss, void* stream);
 
 /* out (N,C) = sum_s weights (N,S) * values (N,S,C), C <= 4, and its adjoint.
@@ -369,7 +378,8 @@ int srf_tensorf_sample_mask(const float* rays_o, const float* rays_d, const floa
                             const float* bbox /* host (2,3) */, const float* alpha_volume, int vol_d, int vol_h,
                             int vol_w, const float* alpha_bbox /* host (2,3) */, float* pts_norm,
                             uint8_t* mask, void* stream);
-/* Alpha-mask query alone: out[p] = (trilinear(volume, pts_norm[p]) > 0). */
+/* Alpha-mask query alone: out[p] = (trilinear(volume, pts_norm[p]) > 0)
+ * (AlphaGridMask.sample_alpha, src/models/SimpleTensoRF09.py:1342-1349). */
 int srf_alpha_mask_query(const float* alpha_volume, int vol_d, int vol_h, int vol_w, const float* pts_norm,
                          int64_t n_pts, uint8_t* out, void* stream);
 
@@ -491,8 +501,11 @@ typedef struct {
     int view_dependent;       /* view_dependent_color (view PE appended)       */
 } srf_tensorf_renderer_desc;
 
+/* Workspace bytes of the renderer forward (+ backward); no reference counterpart. */
 size_t srf_tensorf_renderer_workspace_size(const srf_tensorf_renderer_desc* desc, int64_t m, int precision,
                                            int for_backward);
+/* Forward / backward of the renderer above (SimpleTensoRF09.py:1151, :1370-1421 and
+ * their autograd). */
 int srf_tensorf_renderer_forward(const srf_tensorf_renderer_desc* desc, const float* const* params, const float* feats,
                                  const float* view_dirs, int64_t m, float* rgb, int precision, int for_backward,
                                  void* workspace, size_t workspace_bytes, srf_loss_scaler* scaler, void* stream);
@@ -500,13 +513,16 @@ int srf_tensorf_renderer_backward(const srf_tensorf_renderer_desc* desc, const f
                                   const float* feats, const float* d_rgb, int64_t m, float* const* grads,
                                   float* d_feats, int precision, void* workspace, size_t workspace_bytes,
                                   srf_loss_scaler* scaler, void* stream);
-/* The basis adjoint of the 16-bit renderer backward (d_feats = dB . Wb, dWb +=
- * dB^T feats, dB from the PE adjoint): tensor_cores = 1 (default) takes the TF32
- * tcgen05 pass plus a dWb reduction where the shapes fit (C a multiple of 16 up to
- * 256), 0 always the fused FP32 SIMT pass.  Both give the same gradients up to the
- * TF32 rounding of dB and Wb in d_feats.  Process-wide setting. */
+/* No reference counterpart.  The basis adjoint of the 16-bit renderer backward
+ * (d_feats = dB . Wb, dWb += dB^T feats, dB from the PE adjoint): tensor_cores = 1
+ * (default) takes the TF32 tcgen05 pass plus a dWb reduction where the shapes fit
+ * (C a multiple of 16 up to 256), 0 always the fused FP32 SIMT pass.  Both give the
+ * same gradients up to the TF32 rounding of dB and Wb in d_feats.  Process-wide
+ * setting. */
 int srf_tensorf_basis_adjoint_path(int tensor_cores);
-/* Positional-encoding backward d x (m,dims) from d out (m, ld) (TensoRF feature PE). */
+/* Positional-encoding backward d x (m,dims) from d out (m, ld): the autograd of
+ * the TensoRF colour predictor's feature PE (MlpFeaturesColorPredictor,
+ * SimpleTensoRF09.py:1370-1421, the encoding of SimpleNeRF17.py:581-613). */
 int srf_positional_encoding_backward(float* dx, const float* x, const float* dout, int ld_dout, int64_t m,
                                      const int32_t* rows_dev, int dims, int degree, void* stream);
 
