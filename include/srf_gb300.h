@@ -4,10 +4,13 @@
  * Every entry point takes caller-owned device pointers, explicit sizes, an
  * explicit CUDA stream (as `void*`, a cudaStream_t) and, where it needs
  * temporaries, a caller-provided workspace.  The library never allocates device
- * memory and never frees caller memory.  All functions are stateless and
- * re-entrant; work is enqueued on the given stream only (so calls are legal
- * inside CUDA stream capture).  Return value: SRF_OK (0) or an srf_status code;
- * no exceptions cross this boundary and no device code traps.
+ * memory and never frees caller memory.  The compute entry points are stateless
+ * and re-entrant; the process-wide state is the device error flag, the path
+ * switches (srf_nerf_mlp_fused_path, srf_tensorf_basis_adjoint_path), the tile
+ * tuner's table (srf_autotune_*) and srf_compact_noalloc's fixed scratch array.
+ * Work is enqueued on the given stream only (so calls are legal inside CUDA
+ * stream capture).  Return value: SRF_OK (0) or an srf_status code; no
+ * exceptions cross this boundary and no device code traps.
  *
  * Reference citations are `file:line` inside the Simple-RF project
  * (NagabhushanSN95/Simple-RF, src/...).
